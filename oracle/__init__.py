@@ -1,0 +1,201 @@
+"""CPU checkers for the xavs2 hot path -- TEST INFRASTRUCTURE ONLY.
+
+``liboracle.so`` is this project's C restatement of the reference algorithms
+(``xavs2_oracle.c``); ``_ref/libxavs2ref.so`` is the reference's own C
+primitives compiled from its source files (only where the reference tree is
+present).  Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
+CPU-baseline leg may import this package; the GPU product never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libxavs2ref.so")
+REF_SRC = os.environ.get("XAVS2_REF_SRC", "/root/reference/source")
+
+# LumaPU order (pixel.h:50-65)
+PU_W = [4, 8, 16, 32, 64, 8, 4, 16, 8, 32, 16, 64, 32, 16, 12, 16, 4, 32, 24, 32, 8, 64, 48, 64, 16]
+PU_H = [4, 8, 16, 32, 64, 4, 8, 8, 16, 16, 32, 32, 64, 12, 16, 4, 16, 24, 32, 8, 32, 48, 64, 16, 64]
+TU_PARTS = [0, 1, 2, 3, 4, 15, 16, 19, 20, 23, 24]
+
+
+class MeParams(ctypes.Structure):
+    _fields_ = [("search_range", ctypes.c_int32), ("lambda_factor", ctypes.c_int32),
+                ("use_hadamard", ctypes.c_int32), ("fractional_me", ctypes.c_int32),
+                ("fast_sub_me", ctypes.c_int32), ("enable_pmvr", ctypes.c_int32)]
+
+
+class Pu(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_int16), ("y", ctypes.c_int16), ("part", ctypes.c_uint8),
+                ("ref", ctypes.c_uint8), ("mvp_x", ctypes.c_int16), ("mvp_y", ctypes.c_int16),
+                ("min_x", ctypes.c_int16), ("min_y", ctypes.c_int16),
+                ("max_x", ctypes.c_int16), ("max_y", ctypes.c_int16)]
+
+
+class MeResult(ctypes.Structure):
+    _fields_ = [("bmv_x", ctypes.c_int16), ("bmv_y", ctypes.c_int16), ("bcost", ctypes.c_int32),
+                ("mvcost", ctypes.c_int32), ("imv_x", ctypes.c_int16), ("imv_y", ctypes.c_int16),
+                ("icost", ctypes.c_int32)]
+
+
+PU_DTYPE = np.dtype([("x", "<i2"), ("y", "<i2"), ("part", "u1"), ("ref", "u1"),
+                     ("mvp_x", "<i2"), ("mvp_y", "<i2"), ("min_x", "<i2"), ("min_y", "<i2"),
+                     ("max_x", "<i2"), ("max_y", "<i2")])
+RESULT_DTYPE = np.dtype([("bmv_x", "<i2"), ("bmv_y", "<i2"), ("bcost", "<i4"), ("mvcost", "<i4"),
+                         ("imv_x", "<i2"), ("imv_y", "<i2"), ("icost", "<i4")])
+assert PU_DTYPE.itemsize == ctypes.sizeof(Pu) == 18
+assert RESULT_DTYPE.itemsize == ctypes.sizeof(MeResult) == 20
+
+
+def build(with_ref=None):
+    """Compile liboracle.so (and the reference build when its sources exist)."""
+    targets = ["all"]
+    if with_ref is None:
+        with_ref = os.path.isdir(REF_SRC)
+    if with_ref:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE, "REF_SRC=" + REF_SRC] + targets, check=True)
+
+
+_oracle = None
+_ref = None
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_S = ctypes.c_ssize_t
+
+# argument types of the C entry points (pointers are passed as c_void_p)
+_ORACLE_SIGS = {
+    "xo_sad": (_I, [_I, _P, _S, _P, _S]), "xo_satd": (_I, [_I, _P, _S, _P, _S]),
+    "xo_sa8d": (_I, [_I, _P, _S, _P, _S]), "xo_ssd": (_I, [_I, _P, _S, _P, _S]),
+    "xo_sad_x3": (None, [_I, _P, _P, _P, _P, _S, _P]),
+    "xo_sad_x4": (None, [_I, _P, _P, _P, _P, _P, _S, _P]),
+    "xo_avg": (None, [_I, _P, _S, _P, _S, _P, _S]),
+    "xo_sub_ps": (None, [_I, _P, _S, _P, _P, _S, _S]),
+    "xo_add_ps": (None, [_I, _P, _S, _P, _P, _S, _S]),
+    "xo_copy_pp": (None, [_I, _P, _S, _P, _S]), "xo_copy_ps": (None, [_I, _P, _S, _P, _S]),
+    "xo_copy_sp": (None, [_I, _P, _S, _P, _S]), "xo_copy_ss": (None, [_I, _P, _S, _P, _S]),
+    "xo_ssd_block": (_I, [_P, _S, _P, _S, _I, _I]),
+    "xo_average": (None, [_P, _I, _P, _I, _P, _I, _I, _I]),
+    "xo_mad": (_I, [_P, _I, _I]),
+    "xo_intpl_luma_hor": (None, [_P, _I, _P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_luma_ver": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_luma_ext": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_luma_block_hor": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_luma_block_ver": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_luma_block_ext": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
+    "xo_intpl_chroma_block_hor": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_chroma_block_ver": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xo_intpl_chroma_block_ext": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
+    "xo_interpolate_frame": (None, [_P, _P, _I, _I, _I, _I, _I]),
+    "xo_expand_border": (None, [_P, _I, _I, _I, _I]),
+    "xo_dct": (None, [_I, _P, _P, _I]), "xo_idct": (None, [_I, _P, _P, _I]),
+    "xo_dct_half": (None, [_I, _P, _P, _I]),
+    "xo_transform_4x4_2nd": (None, [_P, _I]), "xo_inv_transform_4x4_2nd": (None, [_P, _I]),
+    "xo_transform_2nd": (None, [_P, _I, _I, _I, _I]),
+    "xo_inv_transform_2nd": (None, [_P, _I, _I, _I, _I]),
+    "xo_quant": (_I, [_P, _I, _I, _I, _I]), "xo_wquant": (_I, [_P, _I, _I, _I, _I, _P]),
+    "xo_dequant": (None, [_P, _I, _I, _I]), "xo_abs_coeff": (None, [_P, _P, _I]),
+    "xo_add_sign": (_I, [_P, _P, _I]),
+    "xo_tq_chain": (_I, [_I, _P, _P, _I, _I, _I]),
+    "xo_me_search": (_I, [_P, _P, _P, _S, _P, _S, _P]),
+    "xo_me_search_list": (None, [_P, _P, _I, _P, _S, _P, _S, _P, _I]),
+    "xo_pu_set_limits": (None, [_P, _I, _I, _I, _I]),
+}
+_REF_SIGS = {
+    "xr_cmp": (_I, [_I, _I, _P, _S, _P, _S]),
+    "xr_sad_x3": (None, [_I, _P, _P, _P, _P, _S, _P]),
+    "xr_sad_x4": (None, [_I, _P, _P, _P, _P, _P, _S, _P]),
+    "xr_avg": (None, [_I, _P, _S, _P, _S, _P, _S]),
+    "xr_sub_ps": (None, [_I, _P, _S, _P, _P, _S, _S]),
+    "xr_add_ps": (None, [_I, _P, _S, _P, _P, _S, _S]),
+    "xr_copy": (None, [_I, _I, _P, _S, _P, _S]),
+    "xr_ssd_block": (_I, [_P, _S, _P, _S, _I, _I]),
+    "xr_average": (None, [_P, _I, _P, _I, _P, _I, _I, _I]),
+    "xr_mad": (_I, [_P, _I, _I]),
+    "xr_intpl_luma_hor": (None, [_P, _I, _P, _I, _P, _I, _I, _I, _P]),
+    "xr_intpl_luma_ver": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xr_intpl_luma_ext": (None, [_P, _I, _P, _I, _I, _I, _P]),
+    "xr_intpl_block": (None, [_I, _P, _I, _P, _I, _I, _I, _P, _P]),
+    "xr_interpolate_frame": (None, [_P, _I, _I, _I, _I, _I]),
+    "xr_dct": (None, [_I, _I, _P, _P, _I]), "xr_2nd": (None, [_I, _P, _I, _I, _I, _I]),
+    "xr_quant": (_I, [_P, _I, _I, _I, _I]), "xr_wquant": (_I, [_P, _I, _I, _I, _I, _P]),
+    "xr_dequant": (None, [_P, _I, _I, _I]), "xr_abs_coeff": (None, [_P, _P, _I]),
+    "xr_add_sign": (_I, [_P, _P, _I]),
+    "xr_me_search": (_I, [_P, _P, _P, _S, _P, _I, _P]),
+}
+
+
+def _apply_sigs(l, sigs):
+    for name, (res, args) in sigs.items():
+        f = getattr(l, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_SO):
+            build(with_ref=False)
+        _oracle = ctypes.CDLL(ORACLE_SO)
+        _apply_sigs(_oracle, _ORACLE_SIGS)
+        _oracle.xo_luma_filter.restype = ctypes.POINTER(ctypes.c_int8)
+        _oracle.xo_chroma_filter.restype = ctypes.POINTER(ctypes.c_int8)
+    return _oracle
+
+
+def ref_lib():
+    """The reference build, or None where it cannot be built."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            if not os.path.isdir(REF_SRC):
+                return None
+            build(with_ref=True)
+        _ref = ctypes.CDLL(REF_SO)
+        _apply_sigs(_ref, _REF_SIGS)
+        _ref.xr_init()
+    return _ref
+
+
+def ptr(a, off=0):
+    """Pointer to element `off` (flat index) of a contiguous numpy array."""
+    return ctypes.c_void_p(a.ctypes.data + off * a.itemsize)
+
+
+def lambda_factor(qp, factor=0.68):
+    """i_lambda_factor for a P frame without GOP factors (encoder.c:232-341):
+    lambda = 2^((qp-11)/4) * 0.85 * 0.8, factor = round(65536 * sqrt(lambda))."""
+    lam = 2.0 ** ((qp - 11) / 4.0) * factor
+    return int(65536.0 * np.sqrt(lam) + 0.5)
+
+
+def padded_plane(img, pad):
+    """Copy an HxW uint8 image into a buffer with `pad` replicated pixels on
+    each side; returns (buffer, offset of pixel (0,0), stride)."""
+    h, w = img.shape
+    buf = np.pad(img, pad, mode="edge").astype(np.uint8)
+    stride = w + 2 * pad
+    return np.ascontiguousarray(buf).reshape(-1), pad * stride + pad, stride
+
+
+def interpolate_frame(lib_, img, pad=80, mode=2, ref=False, lcu_level=6):
+    """Frame sub-pel planes via the oracle (ref=False) or the reference's own
+    row-wise interpolation (ref=True).  Returns a (16, H+2p, W+2p) array."""
+    h, w = img.shape
+    src, off, stride = padded_plane(img, pad)
+    planes = np.zeros((16, src.size), np.uint8)
+    planes[0] = src
+    arr = (ctypes.c_void_p * 16)()
+    for k in range(16):
+        arr[k] = ptr(planes[k], off).value
+    if ref:
+        lib_.xr_interpolate_frame(arr, stride, w, h, lcu_level, mode)
+    else:
+        lib_.xo_interpolate_frame(arr, ptr(planes[0], off), stride, w, h, pad, mode)
+    return planes.reshape(16, h + 2 * pad, w + 2 * pad)

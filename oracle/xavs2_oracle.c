@@ -1,0 +1,1067 @@
+/*
+ * xavs2_oracle.c -- CPU restatement of the xavs2 encoder hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see xavs2_oracle.h).  Every function restates the
+ * arithmetic of one reference routine; the citation in front of each one is
+ * the reference file:line it follows (paths relative to the xavs2 source
+ * tree).  The formulation is deliberately plain: SATD is computed as a sum
+ * of absolute Hadamard coefficients over the reference's rounding units
+ * instead of its SWAR packing, and the DCTs are direct matrix products built
+ * from one cosine-magnitude table instead of partial butterflies; both are
+ * exact integer identities for 8-bit input (checked against the reference
+ * build in tests/test_oracle_vs_reference.py).
+ */
+#include "xavs2_oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------
+ * PU shapes, in LumaPU order (pixel.h:50-65)
+ * ---------------------------------------------------------------------- */
+static const uint8_t k_pu_w[25] = {4, 8, 16, 32, 64, 8, 4, 16, 8, 32, 16, 64, 32,
+                                   16, 12, 16, 4, 32, 24, 32, 8, 64, 48, 64, 16};
+static const uint8_t k_pu_h[25] = {4, 8, 16, 32, 64, 4, 8, 8, 16, 16, 32, 32, 64,
+                                   12, 16, 4, 16, 24, 32, 8, 32, 48, 64, 16, 64};
+
+int xo_num_parts(void) { return 25; }
+int xo_part_width(int part) { return (part >= 0 && part < 25) ? k_pu_w[part] : 0; }
+int xo_part_height(int part) { return (part >= 0 && part < 25) ? k_pu_h[part] : 0; }
+
+/* PART_INDEX (pixel.h:178, table pixel.c:60-78) */
+int xo_part_index(int w, int h)
+{
+    int i;
+    for (i = 0; i < 25; i++) {
+        if (k_pu_w[i] == w && k_pu_h[i] == h) return i;
+    }
+    return -1;
+}
+
+static inline int iabs(int v) { return v < 0 ? -v : v; }
+static inline int clip3(int lo, int hi, int v) { return v < lo ? lo : (v > hi ? hi : v); }
+static inline uint8_t clip_pel(int v) { return (uint8_t)clip3(0, 255, v); }
+
+/* ------------------------------------------------------------------------
+ * SAD / SSD (pixel.c:93-135, 537-592)
+ * ---------------------------------------------------------------------- */
+static int32_t sad_wh(const uint8_t *a, intptr_t sa, const uint8_t *b, intptr_t sb, int w, int h)
+{
+    int32_t s = 0;
+    int x, y;
+    for (y = 0; y < h; y++, a += sa, b += sb)
+        for (x = 0; x < w; x++) s += iabs(a[x] - b[x]);
+    return s;
+}
+
+int32_t xo_sad(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2)
+{
+    return sad_wh(p1, s1, p2, s2, k_pu_w[part], k_pu_h[part]);
+}
+
+/* sad_x3 / sad_x4: the encode block always has stride FENC_STRIDE = 64
+ * (pixel.c:143-243, common.h:1350). */
+void xo_sad_x3(int part, const uint8_t *fenc, const uint8_t *r0, const uint8_t *r1,
+               const uint8_t *r2, intptr_t i_ref, int32_t res[3])
+{
+    int w = k_pu_w[part], h = k_pu_h[part];
+    res[0] = sad_wh(fenc, 64, r0, i_ref, w, h);
+    res[1] = sad_wh(fenc, 64, r1, i_ref, w, h);
+    res[2] = sad_wh(fenc, 64, r2, i_ref, w, h);
+}
+
+void xo_sad_x4(int part, const uint8_t *fenc, const uint8_t *r0, const uint8_t *r1,
+               const uint8_t *r2, const uint8_t *r3, intptr_t i_ref, int32_t res[4])
+{
+    int w = k_pu_w[part], h = k_pu_h[part];
+    res[0] = sad_wh(fenc, 64, r0, i_ref, w, h);
+    res[1] = sad_wh(fenc, 64, r1, i_ref, w, h);
+    res[2] = sad_wh(fenc, 64, r2, i_ref, w, h);
+    res[3] = sad_wh(fenc, 64, r3, i_ref, w, h);
+}
+
+int32_t xo_ssd_block(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2, int w, int h)
+{
+    int32_t s = 0;
+    int x, y;
+    for (y = 0; y < h; y++, p1 += s1, p2 += s2)
+        for (x = 0; x < w; x++) {
+            int d = p1[x] - p2[x];
+            s += d * d;
+        }
+    return s;
+}
+
+int32_t xo_ssd(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2)
+{
+    return xo_ssd_block(p1, s1, p2, s2, k_pu_w[part], k_pu_h[part]);
+}
+
+/* ------------------------------------------------------------------------
+ * Hadamard costs (pixel.c:297-530)
+ *
+ * hsum4/hsum8 return the unnormalised sum of |H D H^T| over one 4x4 or 8x8
+ * difference block, H the +-1 Hadamard matrix.  The reference packs two
+ * 16-bit lanes per word; for 8-bit samples no lane can overflow (the largest
+ * lane sum is bounded by Parseval), so the plain sum is identical.
+ * ---------------------------------------------------------------------- */
+static void fwht4(int *v)
+{
+    int a = v[0] + v[1], b = v[0] - v[1], c = v[2] + v[3], d = v[2] - v[3];
+    v[0] = a + c; v[1] = b + d; v[2] = a - c; v[3] = b - d;
+}
+
+static void fwht8(int *v)
+{
+    int t[8], i;
+    for (i = 0; i < 4; i++) { t[i] = v[i] + v[i + 4]; t[i + 4] = v[i] - v[i + 4]; }
+    fwht4(t); fwht4(t + 4);
+    for (i = 0; i < 8; i++) v[i] = t[i];
+}
+
+static int hsum4(const uint8_t *a, intptr_t sa, const uint8_t *b, intptr_t sb)
+{
+    int d[4][4], col[4], s = 0, x, y;
+    for (y = 0; y < 4; y++) {
+        for (x = 0; x < 4; x++) d[y][x] = a[y * sa + x] - b[y * sb + x];
+        fwht4(d[y]);
+    }
+    for (x = 0; x < 4; x++) {
+        for (y = 0; y < 4; y++) col[y] = d[y][x];
+        fwht4(col);
+        for (y = 0; y < 4; y++) s += iabs(col[y]);
+    }
+    return s;
+}
+
+static int hsum8(const uint8_t *a, intptr_t sa, const uint8_t *b, intptr_t sb)
+{
+    int d[8][8], col[8], s = 0, x, y;
+    for (y = 0; y < 8; y++) {
+        for (x = 0; x < 8; x++) d[y][x] = a[y * sa + x] - b[y * sb + x];
+        fwht8(d[y]);
+    }
+    for (x = 0; x < 8; x++) {
+        for (y = 0; y < 8; y++) col[y] = d[y][x];
+        fwht8(col);
+        for (y = 0; y < 8; y++) s += iabs(col[y]);
+    }
+    return s;
+}
+
+/* SATD rounding units: shapes 4x4, 4x8, 4x16 and 12x16 tile in 4x4 units
+ * rounded once each (pixel.c:297-322, 354-366, 404-407); every other shape
+ * tiles in 8x4 units whose two 4x4 halves are summed before one rounding
+ * (pixel.c:327-348, 371-403). */
+static int satd_unit4(int w, int h) { return w == 4 || (w == 12 && h == 16); }
+
+int32_t xo_satd(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    int32_t s = 0;
+    if (satd_unit4(w, h)) {
+        for (y = 0; y < h; y += 4)
+            for (x = 0; x < w; x += 4)
+                s += hsum4(p1 + y * s1 + x, s1, p2 + y * s2 + x, s2) >> 1;
+    } else {
+        for (y = 0; y < h; y += 4)
+            for (x = 0; x < w; x += 8)
+                s += (hsum4(p1 + y * s1 + x, s1, p2 + y * s2 + x, s2) +
+                      hsum4(p1 + y * s1 + x + 4, s1, p2 + y * s2 + x + 4, s2)) >> 1;
+    }
+    return s;
+}
+
+/* SA8D: shapes with a 4-sample side alias SATD (pixel.c:508-514); 8x8-unit
+ * shapes round each 8x8 with (s+2)>>2 (pixel.c:454-457, 477-489); the rest
+ * round once per 16x16 (pixel.c:461-472, 494-506). */
+int32_t xo_sa8d(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    int32_t s = 0;
+    int unit16;
+    if (w == 4 || h == 4 || w == 12 || h == 12) return xo_satd(part, p1, s1, p2, s2);
+    /* 8x16, 8x32, 16x8, 32x8, 32x24, 24x32 and 8x8 use 8x8 units */
+    unit16 = !(w == 8 || h == 8 || (w == 32 && h == 24) || (w == 24 && h == 32));
+    if (!unit16) {
+        for (y = 0; y < h; y += 8)
+            for (x = 0; x < w; x += 8)
+                s += (hsum8(p1 + y * s1 + x, s1, p2 + y * s2 + x, s2) + 2) >> 2;
+    } else {
+        for (y = 0; y < h; y += 16)
+            for (x = 0; x < w; x += 16) {
+                int t = hsum8(p1 + y * s1 + x, s1, p2 + y * s2 + x, s2) +
+                        hsum8(p1 + y * s1 + x + 8, s1, p2 + y * s2 + x + 8, s2) +
+                        hsum8(p1 + (y + 8) * s1 + x, s1, p2 + (y + 8) * s2 + x, s2) +
+                        hsum8(p1 + (y + 8) * s1 + x + 8, s1, p2 + (y + 8) * s2 + x + 8, s2);
+                s += (t + 2) >> 2;
+            }
+    }
+    return s;
+}
+
+/* ------------------------------------------------------------------------
+ * block ops (pixel.c:680-856)
+ * ---------------------------------------------------------------------- */
+void xo_avg(int part, uint8_t *dst, intptr_t i_dst, const uint8_t *a, intptr_t i_a,
+            const uint8_t *b, intptr_t i_b)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    for (y = 0; y < h; y++, dst += i_dst, a += i_a, b += i_b)
+        for (x = 0; x < w; x++) dst[x] = (uint8_t)((a[x] + b[x] + 1) >> 1);
+}
+
+void xo_average(uint8_t *dst, int i_dst, const uint8_t *a, int i_a, const uint8_t *b, int i_b,
+                int w, int h)
+{
+    int x, y;
+    for (y = 0; y < h; y++, dst += i_dst, a += i_a, b += i_b)
+        for (x = 0; x < w; x++) dst[x] = (uint8_t)((a[x] + b[x] + 1) >> 1);
+}
+
+void xo_sub_ps(int part, int16_t *dst, intptr_t i_dst, const uint8_t *a, const uint8_t *b,
+               intptr_t i_a, intptr_t i_b)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    for (y = 0; y < h; y++, dst += i_dst, a += i_a, b += i_b)
+        for (x = 0; x < w; x++) dst[x] = (int16_t)(a[x] - b[x]);
+}
+
+void xo_add_ps(int part, uint8_t *dst, intptr_t i_dst, const uint8_t *a, const int16_t *b,
+               intptr_t i_a, intptr_t i_b)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    for (y = 0; y < h; y++, dst += i_dst, a += i_a, b += i_b)
+        for (x = 0; x < w; x++) dst[x] = clip_pel(a[x] + b[x]);
+}
+
+void xo_copy_pp(int part, uint8_t *dst, intptr_t i_dst, const uint8_t *src, intptr_t i_src)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], y;
+    for (y = 0; y < h; y++) memcpy(dst + y * i_dst, src + y * i_src, (size_t)w);
+}
+
+void xo_copy_ps(int part, int16_t *dst, intptr_t i_dst, const uint8_t *src, intptr_t i_src)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++) dst[y * i_dst + x] = (int16_t)src[y * i_src + x];
+}
+
+void xo_copy_sp(int part, uint8_t *dst, intptr_t i_dst, const int16_t *src, intptr_t i_src)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++) dst[y * i_dst + x] = (uint8_t)src[y * i_src + x];
+}
+
+void xo_copy_ss(int part, int16_t *dst, intptr_t i_dst, const int16_t *src, intptr_t i_src)
+{
+    int w = k_pu_w[part], h = k_pu_h[part], y;
+    for (y = 0; y < h; y++) memcpy(dst + y * i_dst, src + y * i_src, (size_t)w * 2);
+}
+
+/* mad_NxN_c (pixel.c:1620-1649): rounded mean, then sum of |p - mean| */
+int xo_mad(const uint8_t *src, int i_src, int cu_size)
+{
+    int n = cu_size * cu_size, sum = 0, mean, mad = 0, x, y;
+    for (y = 0; y < cu_size; y++)
+        for (x = 0; x < cu_size; x++) sum += src[y * i_src + x];
+    mean = (sum + (n >> 1)) / n;
+    for (y = 0; y < cu_size; y++)
+        for (x = 0; x < cu_size; x++) mad += iabs(src[y * i_src + x] - mean);
+    return mad;
+}
+
+/* ------------------------------------------------------------------------
+ * interpolation (mc.c:73-91 taps, 275-547 filters, 593-744 frame planes)
+ * ---------------------------------------------------------------------- */
+/* AVS2 luma 8-tap (quarter-pel) and chroma 4-tap (eighth-pel) filters, as
+ * fixed by the standard. */
+static const int8_t k_luma_taps[4][8] = {
+    {0, 0, 0, 64, 0, 0, 0, 0},
+    {-1, 4, -10, 57, 19, -7, 3, -1},
+    {-1, 4, -11, 40, 40, -11, 4, -1},
+    {-1, 3, -7, 19, 57, -10, 4, -1},
+};
+static const int8_t k_chroma_taps[8][4] = {
+    {0, 64, 0, 0},   {-4, 62, 6, 0},   {-6, 56, 15, -1}, {-5, 47, 25, -3},
+    {-4, 36, 36, -4}, {-3, 25, 47, -5}, {-1, 15, 56, -6}, {0, 6, 62, -4},
+};
+
+const int8_t *xo_luma_filter(int frac) { return k_luma_taps[frac & 3]; }
+const int8_t *xo_chroma_filter(int frac) { return k_chroma_taps[frac & 7]; }
+
+/* 8 taps over p[-3*step .. +4*step] */
+static inline int tap8(const uint8_t *p, intptr_t step, const int8_t *c)
+{
+    int k, s = 0;
+    for (k = 0; k < 8; k++) s += c[k] * p[(k - 3) * step];
+    return s;
+}
+static inline int tap8s(const int16_t *p, intptr_t step, const int8_t *c)
+{
+    int k, s = 0;
+    for (k = 0; k < 8; k++) s += c[k] * p[(k - 3) * step];
+    return s;
+}
+static inline int tap4(const uint8_t *p, intptr_t step, const int8_t *c)
+{
+    int k, s = 0;
+    for (k = 0; k < 4; k++) s += c[k] * p[(k - 1) * step];
+    return s;
+}
+
+/* intpl_luma_hor_c (mc.c:403-417): raw sum to tmp, rounded sample to dst */
+void xo_intpl_luma_hor(uint8_t *dst, int i_dst, int16_t *tmp, int i_tmp, const uint8_t *src,
+                       int i_src, int w, int h, const int8_t *coef)
+{
+    int x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++) {
+            int v = tap8(src + y * i_src + x, 1, coef);
+            tmp[y * i_tmp + x] = (int16_t)v;
+            dst[y * i_dst + x] = clip_pel((v + 32) >> 6);
+        }
+}
+
+/* intpl_luma_ver_c (mc.c:422-435); also the block vertical filter (358) */
+void xo_intpl_luma_ver(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w, int h,
+                       const int8_t *coef)
+{
+    int x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++)
+            dst[y * i_dst + x] = clip_pel((tap8(src + y * i_src + x, i_src, coef) + 32) >> 6);
+}
+
+/* intpl_luma_ext_c (mc.c:501-516): vertical pass over the int16 raw sums */
+void xo_intpl_luma_ext(uint8_t *dst, int i_dst, const int16_t *tmp, int i_tmp, int w, int h,
+                       const int8_t *coef)
+{
+    int x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++)
+            dst[y * i_dst + x] = clip_pel((tap8s(tmp + y * i_tmp + x, i_tmp, coef) + 2048) >> 12);
+}
+
+/* intpl_luma_block_hor_c (mc.c:342-354) */
+void xo_intpl_luma_block_hor(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                             int h, const int8_t *coef)
+{
+    int x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++)
+            dst[y * i_dst + x] = clip_pel((tap8(src + y * i_src + x, 1, coef) + 32) >> 6);
+}
+
+void xo_intpl_luma_block_ver(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                             int h, const int8_t *coef)
+{
+    xo_intpl_luma_ver(dst, i_dst, src, i_src, w, h, coef);
+}
+
+/* intpl_luma_block_ext_c (mc.c:362-398): int16 raw horizontal sums over
+ * rows -3..h+3, then a vertical pass with +2048 >> 12 */
+void xo_intpl_luma_block_ext(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                             int h, const int8_t *coef_x, const int8_t *coef_y)
+{
+    int16_t tmp[(64 + 7) * 64];
+    int x, y;
+    for (y = -3; y < h + 4; y++)
+        for (x = 0; x < w; x++) tmp[(y + 3) * 64 + x] = (int16_t)tap8(src + y * i_src + x, 1, coef_x);
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++)
+            dst[y * i_dst + x] = clip_pel((tap8s(tmp + (y + 3) * 64 + x, 64, coef_y) + 2048) >> 12);
+}
+
+/* intpl_chroma_block_{hor,ver,ext}_c (mc.c:274-337) */
+void xo_intpl_chroma_block_hor(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                               int h, const int8_t *coef)
+{
+    int x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++)
+            dst[y * i_dst + x] = clip_pel((tap4(src + y * i_src + x, 1, coef) + 32) >> 6);
+}
+
+void xo_intpl_chroma_block_ver(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                               int h, const int8_t *coef)
+{
+    int x, y;
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++)
+            dst[y * i_dst + x] = clip_pel((tap4(src + y * i_src + x, i_src, coef) + 32) >> 6);
+}
+
+void xo_intpl_chroma_block_ext(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                               int h, const int8_t *coef_x, const int8_t *coef_y)
+{
+    int32_t tmp[(32 + 3) * 32];
+    int x, y, k;
+    for (y = -1; y < h + 2; y++)
+        for (x = 0; x < w; x++) tmp[(y + 1) * 32 + x] = tap4(src + y * i_src + x, 1, coef_x);
+    for (y = 0; y < h; y++)
+        for (x = 0; x < w; x++) {
+            int s = 0;
+            for (k = 0; k < 4; k++) s += coef_y[k] * tmp[(y + k) * 32 + x];
+            dst[y * i_dst + x] = clip_pel((s + 2048) >> 12);
+        }
+}
+
+/* Frame sub-pel planes (mc.c:593-744, frame.c:471-507).  The reference
+ * filters rows [-4, H+4) x cols [-4, W+4) of each plane and then replicates
+ * that region's edge outwards; every filtered sample is therefore the filter
+ * evaluated at the position clamped into that region, with full-pel reads
+ * clamped into the picture (the padding of the source plane).  This routine
+ * states exactly that: value(x, y) = F(clamp(x,-4,W+3), clamp(y,-4,H+3)). */
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+static int hraw(const uint8_t *src, int stride, int w, int h, int x, int y, int fx)
+{
+    const int8_t *c = k_luma_taps[fx];
+    int k, s = 0, yy = clampi(y, 0, h - 1);
+    for (k = 0; k < 8; k++) s += c[k] * src[yy * stride + clampi(x + k - 3, 0, w - 1)];
+    return (int16_t)s;
+}
+
+static uint8_t subpel_sample(const uint8_t *src, int stride, int w, int h, int x, int y, int fx, int fy)
+{
+    int k, s = 0;
+    if (fy == 0) return clip_pel((hraw(src, stride, w, h, x, y, fx) + 32) >> 6);
+    if (fx == 0) {
+        const int8_t *c = k_luma_taps[fy];
+        int xx = clampi(x, 0, w - 1);
+        for (k = 0; k < 8; k++) s += c[k] * src[clampi(y + k - 3, 0, h - 1) * stride + xx];
+        return clip_pel((s + 32) >> 6);
+    }
+    for (k = 0; k < 8; k++) s += k_luma_taps[fy][k] * hraw(src, stride, w, h, x, y + k - 3, fx);
+    return clip_pel((s + 2048) >> 12);
+}
+
+void xo_interpolate_frame(uint8_t *const planes[16], const uint8_t *src, int stride,
+                          int width, int height, int pad, int mode)
+{
+    int k, x, y;
+    for (k = 1; k < 16; k++) {
+        int fx = k & 3, fy = k >> 2;
+        uint8_t *dst = planes[k];
+        if (mode < 2 && !(k == 2 || k == 8 || k == 10)) continue;
+        if (dst == NULL) continue;
+        /* interior of the filtered region, then replicate outwards */
+        for (y = -4; y < height + 4; y++)
+            for (x = -4; x < width + 4; x++)
+                dst[y * stride + x] = subpel_sample(src, stride, width, height, x, y, fx, fy);
+        for (y = -pad; y < height + pad; y++) {
+            int yy = clampi(y, -4, height + 3);
+            for (x = -pad; x < width + pad; x++) {
+                int xx = clampi(x, -4, width + 3);
+                if (xx != x || yy != y) dst[y * stride + x] = dst[yy * stride + xx];
+            }
+        }
+    }
+}
+
+void xo_expand_border(uint8_t *pix, int stride, int width, int height, int pad)
+{
+    int x, y;
+    for (y = -pad; y < height + pad; y++) {
+        int yy = clampi(y, 0, height - 1);
+        for (x = -pad; x < width + pad; x++) {
+            int xx = clampi(x, 0, width - 1);
+            if (xx != x || yy != y) pix[y * stride + x] = pix[yy * stride + xx];
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * integer DCT (transform.c:59-135 basis, 167-582 passes, 1123-1587 sizes)
+ *
+ * Every AVS2 DCT basis entry is +-c[a] for the reduced angle
+ * a = k(2n+1) mod 128 (units of pi/64); the N-point matrices are the rows
+ * k*32/N of the 32-point one.  A pass is the exact integer product
+ * sum_n T[k][n] x[n] followed by the pass's rounding shift, which is what the
+ * partial butterflies compute.
+ * ---------------------------------------------------------------------- */
+static const int8_t k_avs2_cos[32] = {32, 45, 45, 45, 44, 44, 43, 43, 42, 41, 40,
+                                      39, 38, 36, 35, 34, 32, 30, 29, 27, 25, 23,
+                                      21, 19, 17, 15, 13, 11, 9,  7,  4,  2};
+
+static int basis32(int k, int n)
+{
+    int a = (k * (2 * n + 1)) % 128, s = 1;
+    if (k == 0) return 32;
+    if (a > 64) a = 128 - a;
+    if (a > 32) { a = 64 - a; s = -1; }
+    return s * k_avs2_cos[a];
+}
+
+/* T_N[k][n] */
+static inline int basis(int N, int k, int n) { return basis32(k * (32 / N), n); }
+
+/* forward pass over `lines` vectors of length N (stride `in_stride` between
+ * vectors, unit stride inside), writing coefficient k of vector j to
+ * out[k * lines + j] with int16 wrap */
+static void fwd_pass(const int16_t *in, int in_stride, int16_t *out, int N, int lines, int shift)
+{
+    int j, k, n;
+    int add = (1 << shift) >> 1;
+    for (j = 0; j < lines; j++)
+        for (k = 0; k < N; k++) {
+            int s = 0;
+            for (n = 0; n < N; n++) s += basis(N, k, n) * in[j * in_stride + n];
+            out[k * lines + j] = (int16_t)((s + add) >> shift);
+        }
+}
+
+/* inverse pass: vector j's coefficients are in[k * lines + j]; sample n goes
+ * to out[j * N + n], clipped to a signed `bits`-bit range */
+static void inv_pass(const int16_t *in, int16_t *out, int N, int lines, int shift, int bits)
+{
+    int j, k, n;
+    int add = (1 << shift) >> 1;
+    int hi = (1 << (bits - 1)) - 1, lo = -hi - 1;
+    for (j = 0; j < lines; j++)
+        for (n = 0; n < N; n++) {
+            int s = 0;
+            for (k = 0; k < N; k++) s += basis(N, k, n) * in[k * lines + j];
+            out[j * N + n] = (int16_t)clip3(lo, hi, (s + add) >> shift);
+        }
+}
+
+/* 2-D forward DCT of a w x h block: rows first (length w), then columns. */
+static void dct2d(const int16_t *src, int i_src, int16_t *dst, int w, int h, int s1, int s2)
+{
+    int16_t blk[64 * 64], mid[64 * 64];
+    int y;
+    for (y = 0; y < h; y++) memcpy(blk + y * w, src + y * i_src, (size_t)w * 2);
+    fwd_pass(blk, w, mid, w, h, s1);  /* mid[k][j]: row j, horizontal freq k */
+    fwd_pass(mid, h, dst, h, w, s2);  /* dst[m][k] */
+}
+
+/* 2-D inverse DCT: columns first (length h), then rows (length w). */
+static void idct2d(const int16_t *src, int16_t *dst, int i_dst, int w, int h, int s2, int bits2)
+{
+    int16_t mid[64 * 64], blk[64 * 64];
+    int y;
+    inv_pass(src, mid, h, w, 5, 16);    /* mid[j][n]: column j, row n */
+    inv_pass(mid, blk, w, h, s2, bits2);
+    for (y = 0; y < h; y++) memcpy(dst + y * i_dst, blk + y * w, (size_t)w * 2);
+}
+
+/* 5/3 lifting wavelet that halves a w x h block to its low band
+ * (transform.c:586-783).  The reference stores every lifted sample as
+ * coeff_t, hence the int16 casts. */
+static void lift_fwd(int16_t *v, int n, int vertical)
+{
+    int16_t e[64 + 4], *p = e + 2;
+    int i;
+    memcpy(p, v, (size_t)n * 2);
+    p[-1] = p[1]; p[-2] = p[2]; p[n] = p[n - 2]; p[n + 1] = p[n - 3];
+    for (i = -1; i < n; i += 2) p[i] = (int16_t)(p[i] - ((p[i - 1] + p[i + 1]) >> 1));
+    for (i = 0; i < n; i += 2) {
+        if (vertical)
+            p[i] = (int16_t)((p[i] << 1) + ((p[i - 1] + p[i + 1] + 1) >> 1));
+        else
+            p[i] = (int16_t)(p[i] + ((p[i - 1] + p[i + 1] + 2) >> 2));
+    }
+    for (i = 0; i < n / 2; i++) v[i] = p[2 * i];
+}
+
+static void wavelet_fwd(const int16_t *src, int16_t *ll, int w, int h)
+{
+    int16_t rows[64 * 64], col[64];
+    int x, y;
+    for (y = 0; y < h; y++) {
+        int16_t r[64];
+        memcpy(r, src + y * w, (size_t)w * 2);
+        lift_fwd(r, w, 0);
+        memcpy(rows + y * (w / 2), r, (size_t)(w / 2) * 2);
+    }
+    for (x = 0; x < w / 2; x++) {
+        for (y = 0; y < h; y++) col[y] = rows[y * (w / 2) + x];
+        lift_fwd(col, h, 1);
+        for (y = 0; y < h / 2; y++) ll[y * (w / 2) + x] = col[y];
+    }
+}
+
+/* inverse wavelet (transform.c:787-951): vertical upsampling halves the
+ * low-band samples and averages between them; horizontal upsampling only
+ * averages.  The last odd sample mirrors the last even one. */
+static void lift_inv(const int16_t *in, int16_t *out, int n, int halve)
+{
+    int16_t p[64 + 2];
+    int i;
+    for (i = 0; i < n / 2; i++) p[2 * i] = in[i];
+    p[n] = p[n - 2];
+    if (halve)
+        for (i = 0; i <= n; i += 2) p[i] = (int16_t)(p[i] >> 1);
+    for (i = 1; i < n; i += 2) p[i] = (int16_t)((p[i - 1] + p[i + 1]) >> 1);
+    memcpy(out, p, (size_t)n * 2);
+}
+
+static void wavelet_inv(const int16_t *ll, int16_t *dst, int w, int h)
+{
+    int16_t cols[64 * 64], in[64], out[64];
+    int x, y;
+    for (x = 0; x < w / 2; x++) {
+        for (y = 0; y < h / 2; y++) in[y] = ll[y * (w / 2) + x];
+        lift_inv(in, out, h, 1);
+        for (y = 0; y < h; y++) cols[y * (w / 2) + x] = out[y];
+    }
+    for (y = 0; y < h; y++) lift_inv(cols + y * (w / 2), dst + y * w, w, 0);
+}
+
+int xo_is_tu_shape(int part)
+{
+    switch (part) {
+    case 0: case 1: case 2: case 3: case 4:   /* squares */
+    case 15: case 16: case 19: case 20:       /* 16x4 4x16 32x8 8x32 */
+    case 23: case 24:                         /* 64x16 16x64 */
+        return 1;
+    default:
+        return 0;
+    }
+}
+
+/* Forward shifts per size for 8-bit input: shift1 = log2(N_row)+5+9-16 with
+ * the asymmetric -2 adjustments and the wavelet flag (low bit of the stride)
+ * of dct_32x32/32x8/8x32 (transform.c:1123-1587). */
+void xo_dct(int part, const int16_t *src, int16_t *dst, int i_src)
+{
+    int flag = i_src & 1;
+    int16_t ll[32 * 32];
+    switch (part) {
+    case 0: dct2d(src, i_src, dst, 4, 4, 0, 7); break;
+    case 1: dct2d(src, i_src, dst, 8, 8, 1, 8); break;
+    case 2: dct2d(src, i_src, dst, 16, 16, 2, 9); break;
+    case 3: dct2d(src, i_src & 0xFE, dst, 32, 32, 3 + flag, 10); break;
+    case 15: dct2d(src, i_src, dst, 16, 4, 2, 7); break;      /* 16x4 */
+    case 16: dct2d(src, i_src, dst, 4, 16, 0, 9); break;      /* 4x16 */
+    case 19: dct2d(src, i_src & 0xFE, dst, 32, 8, 3, 8 - flag); break;   /* 32x8 */
+    case 20: dct2d(src, i_src & 0xFE, dst, 8, 32, 1 + flag, 10); break;  /* 8x32 */
+    case 4:  /* 64x64: wavelet to 32x32 (input contiguous, stride 64) */
+        wavelet_fwd(src, ll, 64, 64);
+        dct2d(ll, 32, dst, 32, 32, 4, 10);
+        break;
+    case 23: /* 64x16 -> 32x8 */
+        wavelet_fwd(src, ll, 64, 16);
+        dct2d(ll, 32, dst, 32, 8, 3, 7);
+        break;
+    case 24: /* 16x64 -> 8x32 */
+        wavelet_fwd(src, ll, 16, 64);
+        dct2d(ll, 8, dst, 8, 32, 2, 10);
+        break;
+    default: break;
+    }
+}
+
+/* dct_32x32_half_c (transform.c:1276-1286): keep the top-left 16x16 */
+void xo_dct_half(int part, const int16_t *src, int16_t *dst, int i_src)
+{
+    int y;
+    if (part != 3 && part != 4) return;   /* only 32x32 and 64x64 have one */
+    xo_dct(part, src, dst, part == 4 ? 64 : i_src);
+    for (y = 0; y < 32; y++) {
+        if (y < 16) memset(dst + y * 32 + 16, 0, 16 * 2);
+        else memset(dst + y * 32, 0, 32 * 2);
+    }
+}
+
+/* Inverse: shift 5 with a 16-bit clip, then shift 12 with a 9-bit clip, one
+ * less shift and one more clip bit under the wavelet flag. */
+void xo_idct(int part, const int16_t *src, int16_t *dst, int i_dst)
+{
+    int flag = i_dst & 1;
+    int16_t ll[32 * 32];
+    switch (part) {
+    case 0: idct2d(src, dst, i_dst, 4, 4, 12, 9); break;
+    case 1: idct2d(src, dst, i_dst, 8, 8, 12, 9); break;
+    case 2: idct2d(src, dst, i_dst, 16, 16, 12, 9); break;
+    case 3: idct2d(src, dst, i_dst & 0xFE, 32, 32, 12 - flag, 9 + flag); break;
+    case 15: idct2d(src, dst, i_dst, 16, 4, 12, 9); break;
+    case 16: idct2d(src, dst, i_dst, 4, 16, 12, 9); break;
+    case 19: idct2d(src, dst, i_dst & 0xFE, 32, 8, 12 - flag, 9 + flag); break;
+    case 20: idct2d(src, dst, i_dst & 0xFE, 8, 32, 12 - flag, 9 + flag); break;
+    case 4:
+        idct2d(src, ll, 32, 32, 32, 11, 10);
+        wavelet_inv(ll, dst, 64, 64);
+        break;
+    case 23:
+        idct2d(src, ll, 32, 32, 8, 11, 10);
+        wavelet_inv(ll, dst, 64, 16);
+        break;
+    case 24:
+        idct2d(src, ll, 8, 8, 32, 11, 10);
+        wavelet_inv(ll, dst, 16, 64);
+        break;
+    default: break;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * secondary transforms (transform.c:140-155 matrices, 962-1119)
+ * ---------------------------------------------------------------------- */
+static const int16_t k_sec_mode[16] = {123, -35, -8, -3, -32, -120, 30, 10,
+                                       14, 25, 123, -22, 8, 13, 19, 126};
+static const int16_t k_sec_4x4[16] = {34, 58, 72, 81, 77, 69, -7, -75,
+                                      79, -33, -75, 58, 55, -84, 73, -28};
+
+/* Y = M X (M^T when transposed), on the 4x4 corner of a strided block;
+ * `rows` selects whether the transform runs along rows (X M^T) or columns. */
+static void sec_apply(int16_t *c, int stride, const int16_t *m, int transposed, int along_rows,
+                      int shift, int bits)
+{
+    int x[4][4], i, j, k;
+    int add = (1 << shift) >> 1;
+    int hi = (1 << (bits - 1)) - 1, lo = -hi - 1;
+    for (i = 0; i < 4; i++)
+        for (j = 0; j < 4; j++) x[i][j] = c[i * stride + j];
+    for (i = 0; i < 4; i++)
+        for (j = 0; j < 4; j++) {
+            int s = add;
+            for (k = 0; k < 4; k++) {
+                int mk = transposed ? m[k * 4 + i] : m[i * 4 + k];
+                s += mk * (along_rows ? x[j][k] : x[k][j]);
+            }
+            if (along_rows) c[j * stride + i] = (int16_t)clip3(lo, hi, s >> shift);
+            else c[i * stride + j] = (int16_t)clip3(lo, hi, s >> shift);
+        }
+}
+
+void xo_transform_4x4_2nd(int16_t *coef, int i_coef)
+{
+    sec_apply(coef, i_coef, k_sec_4x4, 0, 1, 1, 16);
+    sec_apply(coef, i_coef, k_sec_4x4, 0, 0, 8, 16);
+}
+
+void xo_inv_transform_4x4_2nd(int16_t *coef, int i_coef)
+{
+    sec_apply(coef, i_coef, k_sec_4x4, 1, 0, 5, 16);
+    sec_apply(coef, i_coef, k_sec_4x4, 1, 1, 14, 9);
+}
+
+static void sec_dirs(int i_mode, int *vt, int *ht)
+{
+    *vt = (i_mode >= 0 && i_mode <= 23);
+    *ht = (i_mode >= 13 && i_mode <= 32) || (i_mode >= 0 && i_mode <= 2);
+}
+
+void xo_transform_2nd(int16_t *coef, int i_coef, int i_mode, int b_top, int b_left)
+{
+    int vt, ht;
+    sec_dirs(i_mode, &vt, &ht);
+    if (vt && b_top) sec_apply(coef, i_coef, k_sec_mode, 0, 0, 7, 16);
+    if (ht && b_left) sec_apply(coef, i_coef, k_sec_mode, 0, 1, 7, 16);
+}
+
+void xo_inv_transform_2nd(int16_t *coef, int i_coef, int i_mode, int b_top, int b_left)
+{
+    int vt, ht;
+    sec_dirs(i_mode, &vt, &ht);
+    if (ht && b_left) sec_apply(coef, i_coef, k_sec_mode, 1, 1, 7, 16);
+    if (vt && b_top) sec_apply(coef, i_coef, k_sec_mode, 1, 0, 7, 16);
+}
+
+/* ------------------------------------------------------------------------
+ * quantisation (quant.c:55-184; rdo.c:659-759 for the parameters)
+ * ---------------------------------------------------------------------- */
+static const uint16_t k_q_scale[80] = {
+    32768, 29775, 27554, 25268, 23170, 21247, 19369, 17770, 16302, 15024, 13777, 12634,
+    11626, 10624, 9742,  8958,  8192,  7512,  6889,  6305,  5793,  5303,  4878,  4467,
+    4091,  3756,  3444,  3161,  2894,  2654,  2435,  2235,  2048,  1878,  1722,  1579,
+    1449,  1329,  1218,  1117,  1024,  939,   861,   790,   724,   664,   609,   558,
+    512,   470,   430,   395,   362,   332,   304,   279,   256,   235,   215,   197,
+    181,   166,   152,   140,   128,   116,   108,   99,    91,    83,    76,    69,
+    64,    59,    54,    49,    45,    41,    38,    35};
+static const uint16_t k_iq_scale[80] = {
+    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495,
+    46177, 50535, 55109, 59933, 65535, 35734, 38968, 42577, 46341, 50617, 55027, 60097,
+    32809, 35734, 38968, 42454, 46382, 50576, 55109, 60056, 65535, 35734, 38968, 42495,
+    46320, 50515, 55109, 60076, 65535, 35744, 38968, 42495, 46341, 50535, 55099, 60087,
+    65535, 35734, 38973, 42500, 46341, 50535, 55109, 60097, 32771, 35734, 38965, 42497,
+    46341, 50535, 55109, 60099, 32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424,
+    32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933};
+/* IQ shift: 15 for qp 0-7, then one less every 8 qp, except that qp 16, 32,
+ * 40 and 48 keep the previous group's shift (quant.c:85-96) */
+static int iq_shift_of(int qp)
+{
+    int s = 15 - (qp >> 3);
+    if (qp == 16 || qp == 32 || qp == 40 || qp == 48) s += 1;
+    return s;
+}
+
+int xo_q_scale(int qp) { return k_q_scale[qp]; }
+int xo_iq_scale(int qp) { return k_iq_scale[qp]; }
+int xo_iq_shift(int qp) { return iq_shift_of(qp); }
+
+/* tab_quant_fwd_add (rdo.c:661-666): floor(2^x * 5 / 31) */
+int xo_quant_fwd_add(int shift, int b_intra)
+{
+    int x = shift + b_intra;
+    return (int)(((int64_t)1 << x) * 5 / 31);
+}
+
+/* quant_c (quant.c:108-120); the sign of zero counts as positive */
+int xo_quant(int16_t *coef, int n, int scale, int shift, int add)
+{
+    int i, nz = 0;
+    for (i = 0; i < n; i++) {
+        int c = coef[i];
+        int q = (iabs(c) * scale + add) >> shift;
+        coef[i] = (int16_t)(c < 0 ? -q : q);
+        nz += coef[i] != 0;
+    }
+    return nz;
+}
+
+/* quant_weighted_c (quant.c:158-169) */
+int xo_wquant(int16_t *coef, int n, int scale, int shift, int add, const int *levelscale)
+{
+    int i, nz = 0;
+    for (i = 0; i < n; i++) {
+        int c = coef[i];
+        int a = (iabs(c) * levelscale[i] + (1 << 18)) >> 19;
+        int q = (a * scale + add) >> shift;
+        coef[i] = (int16_t)(c < 0 ? -q : q);
+        nz += coef[i] != 0;
+    }
+    return nz;
+}
+
+/* dequant_c (quant.c:173-184): zeros stay zero */
+void xo_dequant(int16_t *coef, int n, int scale, int shift)
+{
+    int i;
+    int add = 1 << (shift - 1);
+    for (i = 0; i < n; i++)
+        if (coef[i]) coef[i] = (int16_t)clip3(-32768, 32767, (coef[i] * scale + add) >> shift);
+}
+
+void xo_abs_coeff(int16_t *dst, const int16_t *src, int n)
+{
+    int i;
+    for (i = 0; i < n; i++) dst[i] = (int16_t)iabs(src[i]);
+}
+
+int xo_add_sign(int16_t *dst, const int16_t *abs_val, int n)
+{
+    int i, nz = 0;
+    for (i = 0; i < n; i++) {
+        dst[i] = (int16_t)(dst[i] > 0 ? abs_val[i] : -abs_val[i]);
+        nz += abs_val[i] != 0;
+    }
+    return nz;
+}
+
+static int ilog2i(int v) { int l = 0; while ((1 << (l + 1)) <= v) l++; return l; }
+
+int xo_tq_chain(int part, int16_t *blk, int16_t *coef_out, int qp, int b_intra, int use_2nd)
+{
+    int w = k_pu_w[part], h = k_pu_h[part];
+    int wavelet = (w == 64 || h == 64);
+    int w_tr = wavelet ? w / 2 : w, h_tr = wavelet ? h / 2 : h;
+    /* i_level of the TU: log2 of the side for squares (64 -> 6), one less
+     * than the parent CU level for the split shapes (rdo.c:1440-1463) */
+    int level = (ilog2i(w) + ilog2i(h)) >> 1;
+    int n = w_tr * h_tr, nz, qshift, dqshift;
+    int16_t buf[64 * 64];
+    memcpy(buf, blk, (size_t)w * h * 2);
+    if (part == 0 && use_2nd) xo_transform_4x4_2nd(buf, 4);
+    else xo_dct(part, buf, buf, wavelet ? 64 : w_tr);
+    qshift = 15 + 16 - 9 - level;
+    nz = xo_quant(buf, n, k_q_scale[qp], qshift, xo_quant_fwd_add(qshift, b_intra));
+    memcpy(coef_out, buf, (size_t)n * 2);
+    if (nz == 0) {
+        memset(blk, 0, (size_t)w * h * 2);
+        return 0;
+    }
+    dqshift = iq_shift_of(qp) + 9 + level - 16;
+    xo_dequant(buf, n, k_iq_scale[qp], dqshift);
+    if (part == 0 && use_2nd) {
+        xo_inv_transform_4x4_2nd(buf, 4);
+        memcpy(blk, buf, 32);
+    } else {
+        int16_t out[64 * 64];
+        xo_idct(part, buf, out, wavelet ? 64 : w_tr);
+        memcpy(blk, out, (size_t)w * h * 2);
+    }
+    return nz;
+}
+
+/* ------------------------------------------------------------------------
+ * motion search (me.c:479-579, 614-641, 879-1183; md_inter.c:840-926)
+ * ---------------------------------------------------------------------- */
+/* mvbits (me.c:614-641): 1 bit for 0, else the exp-Golomb length
+ * 2*bitlen(|d|) + 1 */
+int xo_mvbits(int d)
+{
+    int a = iabs(d), bl = 0;
+    if (a == 0) return 1;
+    while (a) { bl++; a >>= 1; }
+    return 2 * bl + 1;
+}
+
+static inline int32_t mv_cost(int lambda, int mvx, int mvy, int pmx, int pmy)
+{
+    return (int32_t)(((int64_t)lambda * (xo_mvbits(mvx - pmx) + xo_mvbits(mvy - pmy))) >> 16);
+}
+
+void xo_pu_set_limits(xo_pu_t *pu, int width, int height, int vmin_qpel, int vmax_qpel)
+{
+    int w = k_pu_w[pu->part], h = k_pu_h[pu->part];
+    int mn, mx;
+    mn = clip3(-8192, 8191, (-64 - pu->x) * 4);
+    mx = clip3(-8192, 8191, (width + 64 - pu->x - w) * 4);
+    pu->min_x = (int16_t)((mn >> 2) + 6);
+    pu->max_x = (int16_t)((mx >> 2) - 6);
+    mn = clip3(vmin_qpel, vmax_qpel, (-64 - pu->y) * 4);
+    mx = clip3(vmin_qpel, vmax_qpel, (height + 64 - pu->y - h) * 4);
+    pu->min_y = (int16_t)((mn >> 2) + 6);
+    pu->max_y = (int16_t)((mx >> 2) - 6);
+}
+
+/* the two spiral orders of me.c:129-139 */
+static const int8_t k_spiral[9][2] = {{0, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, -1},
+                                      {-1, 0}, {1, 0}, {-1, 1}, {1, 1}};
+static const int8_t k_spiral2[9][2] = {{0, 0}, {0, -1}, {-1, -1}, {-1, 0}, {-1, 1},
+                                       {0, 1}, {1, 1}, {1, 0}, {1, -1}};
+
+static inline int in_box(const xo_pu_t *pu, int mx, int my)
+{
+    return mx >= pu->min_x && mx <= pu->max_x && my >= pu->min_y && my <= pu->max_y;
+}
+
+static inline int floor4(int v) { return v >> 2; }   /* arithmetic shift */
+
+int32_t xo_me_search(const xo_me_params_t *prm, const xo_pu_t *pu, const uint8_t *fenc,
+                     intptr_t i_fenc, const uint8_t *const fref[16], intptr_t i_fref,
+                     xo_me_result_t *out)
+{
+    const int part = pu->part, lam = prm->lambda_factor;
+    const int pmx = pu->mvp_x, pmy = pu->mvp_y;
+    const uint8_t *ref0 = fref[0] + pu->y * i_fref + pu->x;
+    int cand[2][2], ncand = 0, i, j, c;
+    int32_t bcost = 1 << 30;
+    int bmx = 0, bmy = 0, omx, omy;
+
+    /* candidates: rounded and clipped MVP, then (0,0) (md_inter.c:840-865,
+     * 957-959); duplicates dropped */
+    {
+        int xs[2] = {(pmx + 2) >> 2, 0}, ys[2] = {(pmy + 2) >> 2, 0};
+        for (c = 0; c < 2; c++) {
+            int x = clip3(pu->min_x, pu->max_x, xs[c]);
+            int y = clip3(pu->min_y, pu->max_y, ys[c]);
+            if (ncand == 1 && cand[0][0] == x && cand[0][1] == y) continue;
+            cand[ncand][0] = x; cand[ncand][1] = y; ncand++;
+        }
+    }
+    for (c = 0; c < ncand; c++) {
+        int mx = cand[c][0], my = cand[c][1];
+        if (in_box(pu, mx, my)) {
+            int32_t cost = xo_sad(part, fenc, i_fenc, ref0 + my * i_fref + mx, i_fref) +
+                           mv_cost(lam, mx * 4, my * 4, pmx, pmy);
+            if (cost < bcost) { bcost = cost; bmx = mx; bmy = my; }
+        }
+    }
+    if (bcost == (1 << 30)) {
+        out->bmv_x = out->bmv_y = out->imv_x = out->imv_y = 0;
+        out->bcost = out->icost = bcost;
+        out->mvcost = 0;
+        return bcost;
+    }
+    /* full search, j outer, i inner, first strictly smaller cost wins
+     * (me.c:1156-1164) */
+    omx = bmx; omy = bmy;
+    for (j = -prm->search_range; j < prm->search_range; j++)
+        for (i = -prm->search_range; i < prm->search_range; i++) {
+            int mx = omx + i, my = omy + j;
+            if (in_box(pu, mx, my)) {
+                int32_t cost = xo_sad(part, fenc, i_fenc, ref0 + my * i_fref + mx, i_fref) +
+                               mv_cost(lam, mx * 4, my * 4, pmx, pmy);
+                if (cost < bcost) { bcost = cost; bmx = mx; bmy = my; }
+            }
+        }
+    out->imv_x = (int16_t)bmx; out->imv_y = (int16_t)bmy;
+    out->icost = bcost;
+    out->bmv_x = (int16_t)(bmx * 4); out->bmv_y = (int16_t)(bmy * 4);
+    out->bcost = bcost;
+    out->mvcost = mv_cost(lam, bmx * 4, bmy * 4, pmx, pmy);
+
+    /* sub-pel refinement (me.c:479-579) */
+    if (prm->fractional_me) {
+        const int8_t (*pat)[2] = prm->fast_sub_me ? k_spiral2 : k_spiral;
+        const int step = prm->fast_sub_me ? 2 : 1;
+        int cx = bmx * 4, cy = bmy * 4, bx = cx, by = cy, pos;
+        int ctr_x = (pmx >> 1) << 1, ctr_y = (pmy >> 1) << 1;
+        int32_t best;
+#define QCOST(mx_, my_)                                                                        \
+    ((prm->use_hadamard ? xo_satd : xo_sad)(                                                  \
+         part, fenc, i_fenc,                                                                   \
+         fref[((my_) & 3) * 4 + ((mx_) & 3)] + (pu->y + floor4(my_)) * i_fref + pu->x +       \
+             floor4(mx_),                                                                      \
+         i_fref) +                                                                             \
+     mv_cost(lam, (mx_), (my_), pmx, pmy))
+        best = prm->use_hadamard ? QCOST(cx, cy) : bcost;
+        for (pos = 1; pos < 9; pos += step) {
+            int mx = cx + 2 * pat[pos][0], my = cy + 2 * pat[pos][1];
+            int32_t cost = QCOST(mx, my);
+            if (cost < best) { best = cost; bx = mx; by = my; }
+        }
+        if (prm->fractional_me > 1) {
+            cx = bx; cy = by;
+            for (pos = 1; pos < 9; pos += step) {
+                int mx, my;
+                if (prm->enable_pmvr) {
+                    /* pmvr_adapt_mv (me.c:412-424), TH_PMVR = 2 */
+                    if (iabs(cx - ctr_x) > 2 || iabs(cy - ctr_y) > 2) {
+                        mx = cx + 2 * pat[pos][0]; my = cy + 2 * pat[pos][1];
+                        if (iabs(mx - ctr_x) <= 2 && iabs(my - ctr_y) <= 2) continue;
+                    } else {
+                        mx = cx + pat[pos][0]; my = cy + pat[pos][1];
+                        if (iabs(mx - ctr_x) > 2 || iabs(my - ctr_y) > 2) continue;
+                    }
+                } else {
+                    mx = cx + pat[pos][0]; my = cy + pat[pos][1];
+                }
+                {
+                    int32_t cost = QCOST(mx, my);
+                    if (cost < best) { best = cost; bx = mx; by = my; }
+                }
+            }
+        }
+#undef QCOST
+        out->bmv_x = (int16_t)bx; out->bmv_y = (int16_t)by;
+        out->bcost = best;
+        out->mvcost = mv_cost(lam, bx, by, pmx, pmy);
+    }
+    return out->bcost;
+}
+
+void xo_me_search_list(const xo_me_params_t *prm, const xo_pu_t *pus, int n_pus,
+                       const uint8_t *fenc, intptr_t i_fenc,
+                       const uint8_t *const *frefs, intptr_t i_fref,
+                       xo_me_result_t *out, int threads)
+{
+    int i;
+#ifdef _OPENMP
+    if (threads > 1) {
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads)
+        for (i = 0; i < n_pus; i++) {
+            const xo_pu_t *pu = &pus[i];
+            xo_me_search(prm, pu, fenc + pu->y * i_fenc + pu->x, i_fenc, frefs + 16 * pu->ref,
+                         i_fref, &out[i]);
+        }
+        return;
+    }
+#endif
+    (void)threads;
+    for (i = 0; i < n_pus; i++) {
+        const xo_pu_t *pu = &pus[i];
+        xo_me_search(prm, pu, fenc + pu->y * i_fenc + pu->x, i_fenc, frefs + 16 * pu->ref, i_fref,
+                     &out[i]);
+    }
+}

@@ -1,0 +1,161 @@
+/*
+ * xavs2_oracle.h -- CPU restatement of the xavs2 encoder hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle that the GPU library is
+ * checked against: a plain-C restatement of the reference algorithms (SAD,
+ * SATD, SA8D, SSD, block ops, AVS2 luma/chroma interpolation, integer DCT
+ * with the 64-point wavelet, secondary transforms, quant/dequant, and the
+ * full-search + sub-pel motion search), written from the reference's
+ * behaviour with one citation per function.  Only tests/, the smoke check
+ * and bench.py's CPU-baseline leg may call it; the product path never does.
+ *
+ * Parity pin: oracle/_ref (the reference's own C primitives compiled from
+ * their source files by oracle/Makefile) is compared with this restatement on
+ * seeded and adversarial inputs, and the golden fixtures under tests/golden/
+ * were produced by that reference build.
+ *
+ * All pixel types follow the reference (8-bit build): pel = uint8_t,
+ * coeff = int16_t, dist = int32_t.
+ */
+#ifndef XAVS2_ORACLE_H
+#define XAVS2_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* LumaPU shape index order (pixel.h:50-65). */
+int  xo_num_parts(void);
+int  xo_part_width(int part);
+int  xo_part_height(int part);
+int  xo_part_index(int w, int h);          /* -1 if (w,h) is not a PU shape */
+
+/* ---- block cost / block ops (pixel.c) --------------------------------- */
+int32_t xo_sad (int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2);
+int32_t xo_satd(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2);
+int32_t xo_sa8d(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2);
+int32_t xo_ssd (int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2);
+void xo_sad_x3(int part, const uint8_t *fenc, const uint8_t *r0, const uint8_t *r1,
+               const uint8_t *r2, intptr_t i_ref, int32_t res[3]);
+void xo_sad_x4(int part, const uint8_t *fenc, const uint8_t *r0, const uint8_t *r1,
+               const uint8_t *r2, const uint8_t *r3, intptr_t i_ref, int32_t res[4]);
+void xo_avg(int part, uint8_t *dst, intptr_t i_dst, const uint8_t *a, intptr_t i_a,
+            const uint8_t *b, intptr_t i_b);
+void xo_sub_ps(int part, int16_t *dst, intptr_t i_dst, const uint8_t *a, const uint8_t *b,
+               intptr_t i_a, intptr_t i_b);
+void xo_add_ps(int part, uint8_t *dst, intptr_t i_dst, const uint8_t *a, const int16_t *b,
+               intptr_t i_a, intptr_t i_b);
+void xo_copy_pp(int part, uint8_t *dst, intptr_t i_dst, const uint8_t *src, intptr_t i_src);
+void xo_copy_ps(int part, int16_t *dst, intptr_t i_dst, const uint8_t *src, intptr_t i_src);
+void xo_copy_sp(int part, uint8_t *dst, intptr_t i_dst, const int16_t *src, intptr_t i_src);
+void xo_copy_ss(int part, int16_t *dst, intptr_t i_dst, const int16_t *src, intptr_t i_src);
+int32_t xo_ssd_block(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2, int w, int h);
+void xo_average(uint8_t *dst, int i_dst, const uint8_t *a, int i_a, const uint8_t *b, int i_b,
+                int w, int h);
+int  xo_mad(const uint8_t *src, int i_src, int cu_size);
+
+/* ---- interpolation (mc.c) --------------------------------------------- */
+const int8_t *xo_luma_filter(int frac);    /* frac 0..3 */
+const int8_t *xo_chroma_filter(int frac);  /* frac 0..7 */
+void xo_intpl_luma_hor(uint8_t *dst, int i_dst, int16_t *tmp, int i_tmp, const uint8_t *src,
+                       int i_src, int w, int h, const int8_t *coef);
+void xo_intpl_luma_ver(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w, int h,
+                       const int8_t *coef);
+void xo_intpl_luma_ext(uint8_t *dst, int i_dst, const int16_t *tmp, int i_tmp, int w, int h,
+                       const int8_t *coef);
+void xo_intpl_luma_block_hor(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                             int h, const int8_t *coef);
+void xo_intpl_luma_block_ver(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                             int h, const int8_t *coef);
+void xo_intpl_luma_block_ext(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                             int h, const int8_t *coef_x, const int8_t *coef_y);
+void xo_intpl_chroma_block_hor(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                               int h, const int8_t *coef);
+void xo_intpl_chroma_block_ver(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                               int h, const int8_t *coef);
+void xo_intpl_chroma_block_ext(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w,
+                               int h, const int8_t *coef_x, const int8_t *coef_y);
+/* Frame-level sub-pel planes.  `planes[k]` (k = 4*dy + dx, 1..15) point at
+ * pixel (0,0) of padded planes with stride `stride` and `pad` valid pixels
+ * on every side; `src` likewise (its padding must already hold the clamped
+ * border).  mode 1 fills planes 2, 8, 10 only (half-pel ME), mode 2 all 15.
+ * Planes not filled may be NULL. */
+void xo_interpolate_frame(uint8_t *const planes[16], const uint8_t *src, int stride,
+                          int width, int height, int pad, int mode);
+/* Replicate-border padding of a plane in place (frame.c plane_expand_border
+ * with both bands on). */
+void xo_expand_border(uint8_t *pix, int stride, int width, int height, int pad);
+
+/* ---- transform / quant (transform.c, quant.c) ------------------------- */
+/* `tu` is a LumaPU index of one of the 11 TU shapes. */
+int  xo_is_tu_shape(int part);
+void xo_dct (int part, const int16_t *src, int16_t *dst, int i_src);
+void xo_idct(int part, const int16_t *src, int16_t *dst, int i_dst);
+void xo_dct_half(int part, const int16_t *src, int16_t *dst, int i_src);
+void xo_transform_4x4_2nd(int16_t *coef, int i_coef);
+void xo_inv_transform_4x4_2nd(int16_t *coef, int i_coef);
+void xo_transform_2nd(int16_t *coef, int i_coef, int i_mode, int b_top, int b_left);
+void xo_inv_transform_2nd(int16_t *coef, int i_coef, int i_mode, int b_top, int b_left);
+int  xo_quant(int16_t *coef, int n, int scale, int shift, int add);
+int  xo_wquant(int16_t *coef, int n, int scale, int shift, int add, const int *levelscale);
+void xo_dequant(int16_t *coef, int n, int scale, int shift);
+void xo_abs_coeff(int16_t *dst, const int16_t *src, int n);
+int  xo_add_sign(int16_t *dst, const int16_t *abs_val, int n);
+int  xo_q_scale(int qp);                   /* tab_Q_TAB[qp] */
+int  xo_iq_scale(int qp);                  /* tab_IQ_TAB[qp] */
+int  xo_iq_shift(int qp);                  /* tab_IQ_SHIFT[qp] */
+int  xo_quant_fwd_add(int shift, int b_intra);
+/* One TU through dct -> quant -> (dequant -> idct when nnz > 0), the way
+ * rdo.c:1333-1370 chains them.  `blk` holds the residual (w x h, stride w)
+ * on entry; `coef_out` gets the quantised levels (w_tr x h_tr) and `blk` the
+ * reconstructed residual.  Returns nnz. */
+int  xo_tq_chain(int part, int16_t *blk, int16_t *coef_out, int qp, int b_intra, int use_2nd);
+
+/* ---- motion search (me.c) --------------------------------------------- */
+typedef struct xo_me_params {
+    int32_t search_range;     /* full search over [-R, R) in both axes   */
+    int32_t lambda_factor;    /* i_lambda_factor (16.16 sqrt(lambda))    */
+    int32_t use_hadamard;     /* fpel_cmp: 1 = SATD, 0 = SAD             */
+    int32_t fractional_me;    /* 0 none, 1 half-pel, 2 half + quarter    */
+    int32_t fast_sub_me;      /* Spiral2 pattern with step 2             */
+    int32_t enable_pmvr;
+} xo_me_params_t;
+
+typedef struct xo_pu {
+    int16_t x, y;             /* luma position of the PU                 */
+    uint8_t part, ref;        /* LumaPU index, reference index           */
+    int16_t mvp_x, mvp_y;     /* predictor, quarter-pel                  */
+    int16_t min_x, min_y;     /* integer-pel search limits (inclusive)   */
+    int16_t max_x, max_y;
+} xo_pu_t;
+
+typedef struct xo_me_result {
+    int16_t bmv_x, bmv_y;     /* final MV, quarter-pel                   */
+    int32_t bcost;            /* final cost                              */
+    int32_t mvcost;           /* MV cost of bmv                          */
+    int16_t imv_x, imv_y;     /* integer-pel best MV                     */
+    int32_t icost;            /* integer-pel best cost                   */
+} xo_me_result_t;
+
+int  xo_mvbits(int d);
+/* Search one PU against one reference.  `fenc` points at the PU's top-left
+ * pixel; `fref[k]` are the 16 sub-pel planes of the reference (k = 0 the
+ * full-pel plane) all pointing at pixel (0,0) with stride `i_fref`. */
+int32_t xo_me_search(const xo_me_params_t *prm, const xo_pu_t *pu, const uint8_t *fenc,
+                     intptr_t i_fenc, const uint8_t *const fref[16], intptr_t i_fref,
+                     xo_me_result_t *out);
+/* Searches every PU of a list (threads > 1 uses OpenMP when available). */
+void xo_me_search_list(const xo_me_params_t *prm, const xo_pu_t *pus, int n_pus,
+                       const uint8_t *fenc, intptr_t i_fenc,
+                       const uint8_t *const *frefs /* [n_refs][16] */, intptr_t i_fref,
+                       xo_me_result_t *out, int threads);
+/* MV search limits from md_inter.c:910-926 (m = 6 margin, 64-pixel pad). */
+void xo_pu_set_limits(xo_pu_t *pu, int width, int height, int vmin_qpel, int vmax_qpel);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
