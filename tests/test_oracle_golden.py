@@ -1,0 +1,95 @@
+"""The oracle against the golden fixtures recorded from the reference's own C
+primitives (tests/golden/make_golden.py).  Runs on CPU everywhere, including
+machines without the reference tree."""
+import ctypes
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import PU_W, PU_H, TU_PARTS, ptr
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return dict(np.load(GOLDEN))
+
+
+def test_costs(olib, g):
+    a, b = g["cost_a"], g["cost_b"]
+    fns = [olib.xo_sad, olib.xo_satd, olib.xo_sa8d, olib.xo_ssd]
+    for i in range(4):
+        for kind in range(4):
+            got = [fns[kind](p, ptr(a[i]), 72, ptr(b[i]), 80) for p in range(25)]
+            assert got == list(g["costs"][i, kind]), (i, kind)
+    for part in range(25):
+        res = (ctypes.c_int32 * 4)()
+        olib.xo_sad_x4(part, ptr(a[0]), ptr(b[0], 0), ptr(b[0], 1), ptr(b[0], 81), ptr(b[0], 163), 80, res)
+        assert list(res) == list(g["sad_x4"][part])
+
+
+def test_block_ops(olib, g):
+    a, b, s = g["cost_a"][0], g["cost_b"][0], g["ops_s"]
+    for part in range(25):
+        avg = np.zeros((64, 64), np.uint8); sub = np.zeros((64, 64), np.int16); add = avg.copy()
+        olib.xo_avg(part, ptr(avg), 64, ptr(a), 72, ptr(b), 80)
+        olib.xo_sub_ps(part, ptr(sub), 64, ptr(a), ptr(b), 72, 80)
+        olib.xo_add_ps(part, ptr(add), 64, ptr(a), ptr(s), 72, 64)
+        assert np.array_equal(avg, g["avg"][part])
+        assert np.array_equal(sub, g["sub_ps"][part])
+        assert np.array_equal(add, g["add_ps"][part])
+
+
+def test_interpolation(olib, g):
+    planes = oracle.interpolate_frame(olib, g["intp_img"], mode=2, ref=False)
+    for k in range(1, 16):
+        assert hashlib.sha256(planes[k].tobytes()).hexdigest() == str(g["intp_sha"][k]), k
+    assert np.array_equal(planes[:, 80:152, 80:216], g["intp_center"])
+
+
+def test_transforms(olib, g):
+    for part in TU_PARTS:
+        w, h = PU_W[part], PU_H[part]
+        wav = w == 64 or h == 64
+        n = (w // 2) * (h // 2) if wav else w * h
+        res = np.ascontiguousarray(g["dct_in_%d" % part])
+        out = np.zeros(64 * 64, np.int16)
+        olib.xo_dct(part, ptr(res), ptr(out), w)
+        assert np.array_equal(out[:n], g["dct_out_%d" % part]), part
+        cbuf = np.zeros(64 * 64, np.int16); cbuf[:n] = g["idct_in_%d" % part]
+        rec = np.zeros(64 * 64, np.int16)
+        olib.xo_idct(part, ptr(cbuf), ptr(rec), w)
+        assert np.array_equal(rec[:w * h], g["idct_out_%d" % part]), part
+    t = g["sec_in"].copy(); olib.xo_transform_4x4_2nd(ptr(t), 4)
+    assert np.array_equal(t, g["sec_fwd"])
+    t = g["sec_in"].copy(); olib.xo_inv_transform_4x4_2nd(ptr(t), 4)
+    assert np.array_equal(t, g["sec_inv"])
+
+
+def test_quant(olib, g):
+    for i, qp in enumerate(g["q_qps"]):
+        c = g["q_in"][i].copy()
+        shift = 17
+        nz = olib.xo_quant(ptr(c), 1024, olib.xo_q_scale(int(qp)), shift, olib.xo_quant_fwd_add(shift, 0))
+        assert nz == g["q_nz"][i] and np.array_equal(c, g["q_out"][i])
+        olib.xo_dequant(ptr(c), 1024, olib.xo_iq_scale(int(qp)), olib.xo_iq_shift(int(qp)) + 9 + 5 - 16)
+        assert np.array_equal(c, g["dq_out"][i])
+
+
+def test_motion_search(olib, g):
+    cur, refimg = g["me_cur"], g["me_ref"]
+    h, w = cur.shape
+    planes = oracle.interpolate_frame(olib, refimg, mode=2, ref=False)
+    flat = np.ascontiguousarray(planes.reshape(16, -1))
+    stride = w + 160
+    off = 80 * stride + 80
+    frefs = (ctypes.c_void_p * 16)(*[ptr(flat[k], off).value for k in range(16)])
+    prm = oracle.MeParams(*[int(v) for v in g["me_params"]])
+    pus = np.ascontiguousarray(g["me_pus"])
+    out = np.zeros(len(pus), oracle.RESULT_DTYPE)
+    olib.xo_me_search_list(ctypes.byref(prm), ptr(pus), len(pus), ptr(cur), w, frefs, stride, ptr(out), 1)
+    assert np.array_equal(out, g["me_out"])
