@@ -1,0 +1,358 @@
+/*
+ * xavs2_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the xavs2
+ * encoder hot path: block costs, interpolation, integer DCT + quantisation and
+ * full-search/sub-pel motion search.
+ *
+ * Two kinds of entry points:
+ *
+ *  1. Drop-ins.  One function per entry of the reference's primitive tables
+ *     (`pixel_funcs_t`, `dct_funcs_t` and the interpolation members of
+ *     `intrinsic_func_t`, source/common/primitives.h:101-221 and
+ *     source/common/pixel.h:124-166), with the same signature, argument
+ *     meaning and in-place behaviour.  Buffers are caller-owned host memory,
+ *     exactly as for the reference's C functions; each call stages its
+ *     operands to the GPU, runs one kernel and copies the result back on a
+ *     per-thread CUDA stream, so the functions may be called from the
+ *     encoder's frame and row threads concurrently.  xavs2gpu_pixel_init /
+ *     xavs2gpu_dct_init / xavs2gpu_quant_init fill tables laid out like the
+ *     reference's so that an encoder can install them wholesale.
+ *
+ *  2. Batched forms (no counterpart in the reference): whole-frame sub-pel
+ *     interpolation, batched block costs, batched transform+quant chains and
+ *     a batched full-search + sub-pel motion search over every PU of a frame.
+ *
+ * Errors: the reference's signatures have no error channel, so failures are
+ * recorded in a process-wide status (xavs2gpu_get_status/get_error).  By
+ * default a failure also prints the message and aborts the process; there is
+ * no CPU fallback and no silently wrong result.
+ *
+ * Types follow the reference's 8-bit build (source/common/basic_types.h:
+ * 50-62): pel = uint8_t, coeff = int16_t, dist = cmp_dist = int32_t,
+ * mct = int16_t.
+ */
+#ifndef XAVS2_GB300_H
+#define XAVS2_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XAVS2GPU_API __attribute__((visibility("default")))
+
+typedef uint8_t xavs2gpu_pel_t;
+typedef int16_t xavs2gpu_coeff_t;
+typedef int32_t xavs2gpu_dist_t;
+
+/* ===========================================================================
+ * status and device selection
+ * ======================================================================== */
+enum {
+    XAVS2GPU_OK = 0,
+    XAVS2GPU_ERR_CUDA = 1,      /* a CUDA call failed                        */
+    XAVS2GPU_ERR_ARG = 2,       /* invalid argument (shape, size, pointer)   */
+    XAVS2GPU_ERR_NO_DEVICE = 3, /* no usable GPU                             */
+    XAVS2GPU_ERR_TIMEOUT = 4,   /* a bounded device wait gave up             */
+    XAVS2GPU_ERR_CAPACITY = 5   /* request larger than the session capacity  */
+};
+
+/* Select the CUDA device used by this thread's calls (default 0). */
+XAVS2GPU_API int xavs2gpu_init(int device);
+XAVS2GPU_API int xavs2gpu_get_status(void);
+XAVS2GPU_API const char *xavs2gpu_get_error(void);
+XAVS2GPU_API void xavs2gpu_clear_error(void);
+/* 1 (default): print and abort on any failure.  0: record and return. */
+XAVS2GPU_API void xavs2gpu_set_abort_on_error(int enable);
+/* Number of kernels this library has launched in the process. */
+XAVS2GPU_API uint64_t xavs2gpu_kernel_launches(void);
+XAVS2GPU_API const char *xavs2gpu_version(void);
+
+/* ===========================================================================
+ * 1. drop-in primitives
+ * ======================================================================== */
+
+/* LumaPU indices, same order as enum LumaPU (source/common/pixel.h:50-65). */
+enum {
+    XAVS2GPU_LUMA_4x4, XAVS2GPU_LUMA_8x8, XAVS2GPU_LUMA_16x16, XAVS2GPU_LUMA_32x32,
+    XAVS2GPU_LUMA_64x64, XAVS2GPU_LUMA_8x4, XAVS2GPU_LUMA_4x8, XAVS2GPU_LUMA_16x8,
+    XAVS2GPU_LUMA_8x16, XAVS2GPU_LUMA_32x16, XAVS2GPU_LUMA_16x32, XAVS2GPU_LUMA_64x32,
+    XAVS2GPU_LUMA_32x64, XAVS2GPU_LUMA_16x12, XAVS2GPU_LUMA_12x16, XAVS2GPU_LUMA_16x4,
+    XAVS2GPU_LUMA_4x16, XAVS2GPU_LUMA_32x24, XAVS2GPU_LUMA_24x32, XAVS2GPU_LUMA_32x8,
+    XAVS2GPU_LUMA_8x32, XAVS2GPU_LUMA_64x48, XAVS2GPU_LUMA_48x64, XAVS2GPU_LUMA_64x16,
+    XAVS2GPU_LUMA_16x64, XAVS2GPU_NUM_PU_SIZES
+};
+
+/* Function pointer types of the reference tables (pixel.h:124-139,
+ * primitives.h:62-118). */
+typedef int32_t (*xavs2gpu_pixel_cmp_t)(const uint8_t *pix1, intptr_t i_pix1, const uint8_t *pix2, intptr_t i_pix2);
+typedef int32_t (*xavs2gpu_pixel_ssd_t)(const uint8_t *pix1, intptr_t i_pix1, const uint8_t *pix2, intptr_t i_pix2);
+typedef int32_t (*xavs2gpu_pixel_ssd2_t)(const uint8_t *pix1, intptr_t i_pix1, const uint8_t *pix2, intptr_t i_pix2, int width, int height);
+typedef void (*xavs2gpu_pixel_cmp_x3_t)(const uint8_t *fenc, const uint8_t *pix0, const uint8_t *pix1, const uint8_t *pix2, intptr_t i_stride, int scores[3]);
+typedef void (*xavs2gpu_pixel_cmp_x4_t)(const uint8_t *fenc, const uint8_t *pix0, const uint8_t *pix1, const uint8_t *pix2, const uint8_t *pix3, intptr_t i_stride, int scores[4]);
+typedef void (*xavs2gpu_copy_pp_t)(uint8_t *dst, intptr_t dstStride, const uint8_t *src, intptr_t srcStride);
+typedef void (*xavs2gpu_copy_sp_t)(uint8_t *dst, intptr_t dstStride, const int16_t *src, intptr_t srcStride);
+typedef void (*xavs2gpu_copy_ps_t)(int16_t *dst, intptr_t dstStride, const uint8_t *src, intptr_t srcStride);
+typedef void (*xavs2gpu_copy_ss_t)(int16_t *dst, intptr_t dstStride, const int16_t *src, intptr_t srcStride);
+typedef void (*xavs2gpu_pixel_sub_ps_t)(int16_t *dst, intptr_t dstride, const uint8_t *src0, const uint8_t *src1, intptr_t sstride0, intptr_t sstride1);
+typedef void (*xavs2gpu_pixel_add_ps_t)(uint8_t *a, intptr_t dstride, const uint8_t *b0, const int16_t *b1, intptr_t sstride0, intptr_t sstride1);
+typedef void (*xavs2gpu_pixel_avg_pp_t)(uint8_t *dst, intptr_t dstride, const uint8_t *src0, intptr_t sstride0, const uint8_t *src1, intptr_t sstride1, int weight);
+typedef int (*xavs2gpu_mad_funcs_t)(uint8_t *p_src, int i_src, int cu_size);
+typedef void (*xavs2gpu_average_t)(uint8_t *dst, int i_dst, uint8_t *src1, int i_src1, uint8_t *src2, int i_src2, int width, int height);
+
+/* Same member order and types as pixel_funcs_t (pixel.h:141-166). */
+typedef struct xavs2gpu_pixel_funcs_t {
+    xavs2gpu_pixel_cmp_t    sad    [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_cmp_t    satd   [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_cmp_t    sa8d   [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_ssd_t    ssd    [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_cmp_x3_t sad_x3 [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_cmp_x4_t sad_x4 [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_sub_ps_t sub_ps [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_add_ps_t add_ps [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_copy_sp_t      copy_sp[XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_copy_ps_t      copy_ps[XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_copy_ss_t      copy_ss[XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_copy_pp_t      copy_pp[XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_avg_pp_t avg    [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_pixel_cmp_t   *intra_cmp;
+    xavs2gpu_pixel_cmp_t   *fpel_cmp;
+    xavs2gpu_mad_funcs_t    madf[4];
+    xavs2gpu_pixel_ssd2_t   ssd_block;
+    xavs2gpu_average_t      average;
+} xavs2gpu_pixel_funcs_t;
+
+/* Replaces xavs2_pixel_init (pixel.c:1050): fills every member with the GPU
+ * functions below.  intra_cmp/fpel_cmp are left as they are; the encoder
+ * points them at the satd or sad array afterwards (encoder.c:1837-1847). */
+XAVS2GPU_API void xavs2gpu_pixel_init(uint32_t cpuid, xavs2gpu_pixel_funcs_t *pixf);
+/* Replaces xavs2_mad_init (pixel.c:1654). */
+XAVS2GPU_API void xavs2gpu_mad_init(uint32_t cpuid, xavs2gpu_mad_funcs_t *madf);
+
+/* Per-shape drop-ins.  Names follow the reference's per-shape C functions
+ * (pixel.c:93-840): xavs2gpu_pixel_sad_WxH replaces xavs2_pixel_sad_WxH, etc. */
+#define XAVS2GPU_DECLARE_PIXEL(w, h)                                                                                  \
+    XAVS2GPU_API int32_t xavs2gpu_pixel_sad_##w##x##h(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2);  \
+    XAVS2GPU_API int32_t xavs2gpu_pixel_satd_##w##x##h(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2); \
+    XAVS2GPU_API int32_t xavs2gpu_pixel_sa8d_##w##x##h(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2); \
+    XAVS2GPU_API int32_t xavs2gpu_pixel_ssd_##w##x##h(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2);  \
+    XAVS2GPU_API void xavs2gpu_pixel_sad_x3_##w##x##h(const uint8_t *fenc, const uint8_t *r0, const uint8_t *r1,       \
+                                                      const uint8_t *r2, intptr_t i_ref, int scores[3]);               \
+    XAVS2GPU_API void xavs2gpu_pixel_sad_x4_##w##x##h(const uint8_t *fenc, const uint8_t *r0, const uint8_t *r1,       \
+                                                      const uint8_t *r2, const uint8_t *r3, intptr_t i_ref,            \
+                                                      int scores[4]);                                                  \
+    XAVS2GPU_API void xavs2gpu_pixel_avg_##w##x##h(uint8_t *dst, intptr_t ds, const uint8_t *a, intptr_t sa,           \
+                                                   const uint8_t *b, intptr_t sb, int weight);                        \
+    XAVS2GPU_API void xavs2gpu_pixel_sub_ps_##w##x##h(int16_t *dst, intptr_t ds, const uint8_t *a, const uint8_t *b,   \
+                                                      intptr_t sa, intptr_t sb);                                       \
+    XAVS2GPU_API void xavs2gpu_pixel_add_ps_##w##x##h(uint8_t *dst, intptr_t ds, const uint8_t *a, const int16_t *b,   \
+                                                      intptr_t sa, intptr_t sb);                                       \
+    XAVS2GPU_API void xavs2gpu_blockcopy_pp_##w##x##h(uint8_t *dst, intptr_t ds, const uint8_t *src, intptr_t ss);     \
+    XAVS2GPU_API void xavs2gpu_blockcopy_ps_##w##x##h(int16_t *dst, intptr_t ds, const uint8_t *src, intptr_t ss);     \
+    XAVS2GPU_API void xavs2gpu_blockcopy_sp_##w##x##h(uint8_t *dst, intptr_t ds, const int16_t *src, intptr_t ss);     \
+    XAVS2GPU_API void xavs2gpu_blockcopy_ss_##w##x##h(int16_t *dst, intptr_t ds, const int16_t *src, intptr_t ss);
+
+#define XAVS2GPU_FOR_EACH_PU(X)                                                                 \
+    X(4, 4) X(8, 8) X(16, 16) X(32, 32) X(64, 64) X(8, 4) X(4, 8) X(16, 8) X(8, 16) X(32, 16)  \
+    X(16, 32) X(64, 32) X(32, 64) X(16, 12) X(12, 16) X(16, 4) X(4, 16) X(32, 24) X(24, 32)    \
+    X(32, 8) X(8, 32) X(64, 48) X(48, 64) X(64, 16) X(16, 64)
+
+XAVS2GPU_FOR_EACH_PU(XAVS2GPU_DECLARE_PIXEL)
+
+/* xavs2_get_block_ssd_c (pixel.c:537), xavs2_pixel_average (pixel.c:844),
+ * mad_NxN_c (pixel.c:1620) */
+XAVS2GPU_API int32_t xavs2gpu_get_block_ssd(const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2, int w, int h);
+XAVS2GPU_API void xavs2gpu_pixel_average(uint8_t *dst, int i_dst, uint8_t *a, int i_a, uint8_t *b, int i_b, int w, int h);
+XAVS2GPU_API int xavs2gpu_mad_NxN(uint8_t *src, int i_src, int cu_size);
+
+/* ---- interpolation: members of intrinsic_func_t (primitives.h:157-171),
+ * C versions in mc.c:274-547.  `coeff` points at the filter taps (8 for
+ * luma, 4 for chroma) exactly as in the reference. */
+XAVS2GPU_API void xavs2gpu_intpl_luma_hor(uint8_t *dst, int i_dst, int16_t *tmp, int i_tmp, uint8_t *src, int i_src, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_ver(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_ext(uint8_t *dst, int i_dst, int16_t *tmp, int i_tmp, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_ver_x3(uint8_t *const dst[3], int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t **coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_hor_x3(uint8_t *const dst[3], int i_dst, int16_t *const tmp[3], int i_tmp, uint8_t *src, int i_src, int width, int height, const int8_t **coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_ext_x3(uint8_t *const dst[3], int i_dst, int16_t *tmp, int i_tmp, int width, int height, const int8_t **coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_block_hor(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_block_ver(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_luma_block_ext(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff_x, const int8_t *coeff_y);
+XAVS2GPU_API void xavs2gpu_intpl_chroma_block_hor(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_chroma_block_ver(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff);
+XAVS2GPU_API void xavs2gpu_intpl_chroma_block_ext(uint8_t *dst, int i_dst, uint8_t *src, int i_src, int width, int height, const int8_t *coeff_x, const int8_t *coeff_y);
+
+/* ---- transform and quantisation (dct_funcs_t, primitives.h:101-119) ---- */
+typedef void (*xavs2gpu_dct_t)(const int16_t *src, int16_t *dst, int i_src);
+
+/* Same member order and types as dct_funcs_t. */
+typedef struct xavs2gpu_dct_funcs_t {
+    xavs2gpu_dct_t dct     [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_dct_t idct    [XAVS2GPU_NUM_PU_SIZES];
+    xavs2gpu_dct_t dct_half[XAVS2GPU_NUM_PU_SIZES];
+    void (*transform_4x4_2nd)    (int16_t *coeff, int i_coeff);
+    void (*inv_transform_4x4_2nd)(int16_t *coeff, int i_coeff);
+    void (*transform_2nd)        (int16_t *coeff, int i_coeff, int i_mode, int b_top, int b_left);
+    void (*inv_transform_2nd)    (int16_t *coeff, int i_coeff, int i_mode, int b_top, int b_left);
+    void (*abs_coeff)(int16_t *coef, const int16_t *src, const int i_coef);
+    int  (*add_sign) (int16_t *coef, const int16_t *abs_val, const int i_coef);
+    int  (*quant)    (int16_t *coef, const int i_coef, const int scale, const int shift, const int add);
+    void (*dequant)  (int16_t *coef, const int i_coef, const int scale, const int shift);
+    int  (*wquant)   (int16_t *coef, const int i_coef, const int scale, const int shift, const int add, int *levelscale);
+} xavs2gpu_dct_funcs_t;
+
+/* Replace xavs2_dct_init (transform.c:1599) and xavs2_quant_init (quant.c:212). */
+XAVS2GPU_API void xavs2gpu_dct_init(uint32_t cpuid, xavs2gpu_dct_funcs_t *dctf);
+XAVS2GPU_API void xavs2gpu_quant_init(uint32_t cpuid, xavs2gpu_dct_funcs_t *dctf);
+
+/* Per-shape transforms (transform.c:1123-1587).  For the 32-point shapes the
+ * lowest bit of the stride is the reference's wavelet flag; the 64-point
+ * shapes read a contiguous block (stride 64 or 16) and write the
+ * (w/2)x(h/2) coefficients contiguously. */
+#define XAVS2GPU_DECLARE_DCT(w, h)                                                               \
+    XAVS2GPU_API void xavs2gpu_dct_##w##x##h(const int16_t *src, int16_t *dst, int i_src);        \
+    XAVS2GPU_API void xavs2gpu_idct_##w##x##h(const int16_t *src, int16_t *dst, int i_dst);
+#define XAVS2GPU_FOR_EACH_TU(X) \
+    X(4, 4) X(8, 8) X(16, 16) X(32, 32) X(64, 64) X(16, 4) X(4, 16) X(32, 8) X(8, 32) X(64, 16) X(16, 64)
+XAVS2GPU_FOR_EACH_TU(XAVS2GPU_DECLARE_DCT)
+XAVS2GPU_API void xavs2gpu_dct_32x32_half(const int16_t *src, int16_t *dst, int i_src);
+XAVS2GPU_API void xavs2gpu_dct_64x64_half(const int16_t *src, int16_t *dst, int i_src);
+XAVS2GPU_API void xavs2gpu_transform_4x4_2nd(int16_t *coeff, int i_coeff);
+XAVS2GPU_API void xavs2gpu_inv_transform_4x4_2nd(int16_t *coeff, int i_coeff);
+XAVS2GPU_API void xavs2gpu_transform_2nd(int16_t *coeff, int i_coeff, int i_mode, int b_top, int b_left);
+XAVS2GPU_API void xavs2gpu_inv_transform_2nd(int16_t *coeff, int i_coeff, int i_mode, int b_top, int b_left);
+/* quant_c, dequant_c, quant_weighted_c, abs_coeff_c, add_sign_c (quant.c:108-184) */
+XAVS2GPU_API int  xavs2gpu_quant(int16_t *coef, const int i_coef, const int scale, const int shift, const int add);
+XAVS2GPU_API void xavs2gpu_dequant(int16_t *coef, const int i_coef, const int scale, const int shift);
+XAVS2GPU_API int  xavs2gpu_quant_weighted(int16_t *coef, const int i_coef, const int scale, const int shift, const int add, int *levelscale);
+XAVS2GPU_API void xavs2gpu_abs_coeff(int16_t *dst, const int16_t *src, const int i_coef);
+XAVS2GPU_API int  xavs2gpu_add_sign(int16_t *dst, const int16_t *abs_val, const int i_coef);
+
+/* ===========================================================================
+ * 2. batched forms (device pointers unless a name ends in _host)
+ * ======================================================================== */
+
+/* ---- block costs over a job list --------------------------------------
+ * out[i] = cost `kind` (0 SAD, 1 SATD, 2 SA8D, 3 SSD) of shape jobs[i].part
+ * between base1 + off1 (stride s1) and base2 + off2 (stride s2); the
+ * per-block results equal the drop-ins'.  Kernels run on `stream`
+ * (a cudaStream_t, 0 = default). */
+typedef struct xavs2gpu_cost_job {
+    int64_t off1, off2;
+    int32_t s1, s2;
+    int32_t part;
+    int32_t pad_;
+} xavs2gpu_cost_job_t;
+XAVS2GPU_API int xavs2gpu_cost_batch(int kind, const xavs2gpu_cost_job_t *jobs, int n, const uint8_t *base1,
+                                     const uint8_t *base2, int32_t *out, void *stream);
+
+/* ---- whole-frame sub-pel planes ----------------------------------------
+ * The reference's interpolate_lcu_row (mc.c:748-785) over every LCU row of a
+ * frame: planes[k] (k = 4*dy + dx) of the 15 quarter-pel positions, each with
+ * the same stride and `pad` pixels of replicated border as `src`, which must
+ * already hold its own replicated border of at least 8 pixels.  mode 1
+ * computes planes 2, 8, 10 (half-pel ME), mode 2 all 15.  Device pointers. */
+XAVS2GPU_API int xavs2gpu_interpolate_frame(const uint8_t *src, int stride, int width, int height, int pad,
+                                            uint8_t *const planes[16], int mode, void *stream);
+/* Replicates the border of a device plane outwards by `pad` pixels
+ * (plane_expand_border, frame.c:471-507, both bands). */
+XAVS2GPU_API int xavs2gpu_expand_border(uint8_t *pix, int stride, int width, int height, int pad, void *stream);
+
+/* ---- batched transform + quant chain -----------------------------------
+ * For every block: dct (or, for a 4x4 block with flag bit 1, the 4x4
+ * secondary transform) -> quant -> when any level is non-zero, dequant ->
+ * inverse transform; the order of the reference's TU reconstruction
+ * (rdo.c:1333-1370, 876-947).  The residual of a block is w x h contiguous
+ * int16 at residual + offset and the reconstructed residual goes to the
+ * same offset of `recon` (all zero when nnz = 0); the quantised levels
+ * ((w/2)x(h/2) for the 64-point shapes) go to coef + coef_offset.
+ * Quant parameters follow tu_quant_forward/inverse (rdo.c:659-759) with
+ * i_level = log2 of the TU side (64 -> 6; the mean of the two side logs for
+ * the split shapes).  nnz[i] = number of non-zero levels, -1 for an invalid
+ * descriptor.  Device pointers. */
+typedef struct xavs2gpu_tq_block {
+    int64_t offset;        /* residual / recon offset (elements)            */
+    int64_t coef_offset;   /* quantised levels offset (elements)            */
+    int32_t part;          /* TU shape as a LumaPU index                    */
+    int32_t qp;            /* 0..79                                         */
+    int32_t flags;         /* bit 0: b_intra, bit 1: 4x4 secondary transform */
+    int32_t pad_;
+} xavs2gpu_tq_block_t;
+XAVS2GPU_API int xavs2gpu_tq_batch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
+                                   int16_t *recon, int32_t *nnz, void *stream);
+
+/* ---- batched motion search -----------------------------------------------
+ * Full search + sub-pel refinement of many PUs against device-resident
+ * reference planes.  Per PU and reference the result equals the
+ * reference's xavs2_me_search (me.c:879-1183) with me_method = full search,
+ * candidates {rounded MVP, (0,0)} built as pred_inter_search_single does
+ * (md_inter.c:840-865, 957-959), and me_subpel_refine (me.c:479-579). */
+typedef struct xavs2gpu_me_params {
+    int32_t search_range;     /* full search over [-R, R) on both axes, R <= 128 */
+    int32_t lambda_factor;    /* h->i_lambda_factor = round(65536*sqrt(lambda))  */
+    int32_t use_hadamard;     /* fpel_cmp: 1 = SATD, 0 = SAD                     */
+    int32_t fractional_me;    /* 0 none, 1 half-pel, 2 half + quarter-pel         */
+    int32_t fast_sub_me;      /* spiral-2 pattern with step 2                     */
+    int32_t enable_pmvr;      /* PMVR restriction of the quarter-pel step         */
+} xavs2gpu_me_params_t;
+
+typedef struct xavs2gpu_pu {
+    int16_t x, y;             /* luma position of the PU                          */
+    uint8_t part, ref;        /* LumaPU index, reference slot                     */
+    int16_t mvp_x, mvp_y;     /* predictor, quarter-pel                           */
+    int16_t min_x, min_y;     /* integer-pel search limits, inclusive             */
+    int16_t max_x, max_y;     /*   (xavs2_me_t mv_min_fpel / mv_max_fpel)         */
+} xavs2gpu_pu_t;
+
+typedef struct xavs2gpu_me_result {
+    int16_t bmv_x, bmv_y;     /* best MV after refinement, quarter-pel (bmv)      */
+    int32_t bcost;            /* its cost (bcost; 1<<30 when no candidate fits)   */
+    int32_t mvcost;           /* MV cost of bmv (mvcost[PDIR_FWD])                */
+    int16_t imv_x, imv_y;     /* integer-pel best MV (bmv2)                       */
+    int32_t icost;            /* integer-pel best cost (bcost2)                   */
+} xavs2gpu_me_result_t;
+
+/* Search limits of a PU the way pred_inter_search_single derives them
+ * (md_inter.c:910-926): a 64-pixel margin minus 6, the vertical range
+ * clipped to [vmin_qpel, vmax_qpel] (encoder.c:852-870). */
+XAVS2GPU_API void xavs2gpu_pu_set_limits(xavs2gpu_pu_t *pu, int width, int height, int vmin_qpel, int vmax_qpel);
+
+typedef struct xavs2gpu_me_session xavs2gpu_me_session_t;
+
+/* A session owns device-resident planes for one current picture and
+ * `num_refs` reference pictures of width x height (each reference with its
+ * 15 quarter-pel planes), a PU list of up to `max_pus` entries, the results
+ * and one CUDA stream.  Returns NULL on failure. */
+XAVS2GPU_API xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int num_refs, int max_pus);
+XAVS2GPU_API void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s);
+/* Load a picture: slot -1 = the current picture, 0..num_refs-1 = references
+ * (their borders are replicated and their sub-pel planes computed on the
+ * device).  _host copies from host memory, _device from device memory. */
+XAVS2GPU_API int xavs2gpu_me_set_picture_host(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride);
+XAVS2GPU_API int xavs2gpu_me_set_picture_device(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride);
+/* Set the PU list (host memory).  The list is uploaded and planned once;
+ * runs reuse it until the next call. */
+XAVS2GPU_API int xavs2gpu_me_set_pus(xavs2gpu_me_session_t *s, const xavs2gpu_pu_t *pus, int n);
+/* Run the search for every PU on the session's stream (asynchronous). */
+XAVS2GPU_API int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm);
+/* Copy the results (one per PU, in list order) to host memory; waits. */
+XAVS2GPU_API int xavs2gpu_me_get_results(xavs2gpu_me_session_t *s, xavs2gpu_me_result_t *out);
+XAVS2GPU_API int xavs2gpu_me_sync(xavs2gpu_me_session_t *s);
+/* Device views for tests and chaining. */
+XAVS2GPU_API const xavs2gpu_me_result_t *xavs2gpu_me_results_device(xavs2gpu_me_session_t *s);
+XAVS2GPU_API uint8_t *xavs2gpu_me_plane_device(xavs2gpu_me_session_t *s, int slot, int k);
+XAVS2GPU_API int xavs2gpu_me_plane_stride(xavs2gpu_me_session_t *s);
+/* Copies plane k of a slot, margin included ((W+160) x (H+160) bytes), to
+ * host memory with row stride `stride`; waits. */
+XAVS2GPU_API int xavs2gpu_me_get_plane(xavs2gpu_me_session_t *s, int slot, int k, uint8_t *out, intptr_t stride);
+XAVS2GPU_API int xavs2gpu_me_plane_pad(xavs2gpu_me_session_t *s);
+XAVS2GPU_API void *xavs2gpu_me_stream(xavs2gpu_me_session_t *s);
+/* How the last xavs2gpu_me_set_pus split the list: PUs searched by the
+ * shared-window CTU kernel and by the per-PU kernel. */
+XAVS2GPU_API void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus, int *n_generic_pus, int *n_ctu_jobs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XAVS2_GB300_H */

@@ -1,0 +1,114 @@
+"""Batched motion search on the GPU against the oracle's restatement of
+xavs2_me_search (full search + sub-pel refinement), bit-exact."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _frames(rng, w, h, shift=(2, -3), noise=5):
+    cur = rng.integers(0, 256, (h, w), dtype=np.uint8)
+    # smooth it a little so that the search has real minima
+    cur = ((cur.astype(np.int32) + np.roll(cur, 1, 0) + np.roll(cur, 1, 1) + np.roll(cur, (1, 1), (0, 1))) // 4).astype(np.uint8)
+    ref = np.clip(np.roll(cur, shift, axis=(0, 1)).astype(np.int16) + rng.integers(-noise, noise + 1, (h, w)),
+                  0, 255).astype(np.uint8)
+    return cur, ref
+
+
+def _oracle(olib, cur, refs, pus, prm, threads=8):
+    h, w = cur.shape
+    stride = w + 160
+    flats = [np.ascontiguousarray(oracle.interpolate_frame(olib, r, mode=2).reshape(16, -1)) for r in refs]
+    frefs = (ctypes.c_void_p * (16 * len(refs)))(
+        *[oracle.ptr(f[k], 80 * stride + 80).value for f in flats for k in range(16)])
+    out = np.zeros(len(pus), oracle.RESULT_DTYPE)
+    oprm = oracle.MeParams(prm.search_range, prm.lambda_factor, prm.use_hadamard, prm.fractional_me,
+                           prm.fast_sub_me, prm.enable_pmvr)
+    olib.xo_me_search_list(ctypes.byref(oprm), oracle.ptr(pus), len(pus), oracle.ptr(cur), w, frefs, stride,
+                           oracle.ptr(out), threads)
+    return out
+
+
+def _run(cur, refs, pus, prm):
+    import xavs2_gb300 as xg
+    h, w = cur.shape
+    s = xg.MeSession(w, h, len(refs), len(pus))
+    s.set_picture(-1, cur)
+    for i, r in enumerate(refs):
+        s.set_picture(i, r)
+    s.set_pus(pus)
+    s.run(prm)
+    out = s.results()
+    stats = s.plan_stats()
+    s.close()
+    return out, stats
+
+
+def _assert_same(got, exp, pus):
+    bad = np.nonzero(got.view(np.uint8).reshape(len(got), -1).any(axis=1) != exp.view(np.uint8).reshape(len(exp), -1).any(axis=1))
+    diff = [i for i in range(len(got)) if got[i].tobytes() != exp[i].tobytes()]
+    assert not diff, "first mismatches: %s" % [(int(pus[i]["x"]), int(pus[i]["y"]), int(pus[i]["part"]),
+                                                 int(pus[i]["ref"]), got[i], exp[i]) for i in diff[:5]]
+
+
+@pytest.mark.parametrize("R,w,h", [(16, 256, 192), (8, 136, 72), (64, 320, 256)])
+def test_ctu_layout_all_pus(gpu, olib, R, w, h):
+    """Every PU of the CTU quadtree layout (all 25 shapes), two references,
+    MVP (0,0): the shared-window CTU kernel, edge CTUs included."""
+    import xavs2_gb300 as xg
+    rng = np.random.default_rng(R + w)
+    cur, ref0 = _frames(rng, w, h)
+    _, ref1 = _frames(rng, w, h, shift=(-3, 4))
+    pus = xg.frame_pus(w, h, 2)
+    if R == 64:
+        pus = pus[rng.random(len(pus)) < 0.25]     # keep the CPU oracle quick
+    prm = xg.MeParams(R, oracle.lambda_factor(32), 1, 2, 0, 0)
+    got, stats = _run(cur, [ref0, ref1], pus, prm)
+    assert stats[0] == len(pus) and stats[1] == 0, stats
+    exp = _oracle(olib, cur, [ref0, ref1], pus, prm)
+    _assert_same(got, exp, pus)
+
+
+def test_generic_pus(gpu, olib):
+    """PUs at arbitrary positions with arbitrary predictors take the per-PU
+    kernel; both paths in one run."""
+    import xavs2_gb300 as xg
+    rng = np.random.default_rng(77)
+    w, h = 160, 96
+    cur, ref0 = _frames(rng, w, h)
+    n = 300
+    pus = np.zeros(n, xg.PU_DTYPE)
+    pus["part"] = rng.integers(0, 25, n)
+    pw = np.array(xg.PU_W)[pus["part"]]
+    ph = np.array(xg.PU_H)[pus["part"]]
+    pus["x"] = (rng.random(n) * (w - pw + 1)).astype(int) // 2 * 2
+    pus["y"] = (rng.random(n) * (h - ph + 1)).astype(int)
+    pus["mvp_x"] = rng.integers(-40, 41, n)
+    pus["mvp_y"] = rng.integers(-40, 41, n)
+    pus = xg.set_limits(pus, w, h)
+    layout = xg.frame_pus(w, h, 1)[::3]
+    allp = np.concatenate([pus, layout])
+    for prm in (xg.MeParams(12, oracle.lambda_factor(32), 1, 2, 0, 0),
+                xg.MeParams(6, oracle.lambda_factor(40), 0, 1, 0, 0),
+                xg.MeParams(10, oracle.lambda_factor(27), 1, 2, 1, 1)):
+        got, stats = _run(cur, [ref0], allp, prm)
+        assert stats[1] >= n
+        exp = _oracle(olib, cur, [ref0], allp, prm)
+        _assert_same(got, exp, allp)
+
+
+def test_golden_me(gpu):
+    """The GPU reproduces the reference's own xavs2_me_search results stored
+    in the golden fixtures."""
+    import os
+    import xavs2_gb300 as xg
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.npz"))
+    p = [int(v) for v in g["me_params"]]
+    prm = xg.MeParams(*p)
+    pus = np.ascontiguousarray(g["me_pus"]).view(xg.PU_DTYPE)
+    got, _ = _run(g["me_cur"], [g["me_ref"]], pus, prm)
+    assert got.tobytes() == g["me_out"].tobytes()

@@ -1,0 +1,540 @@
+// fs_ctu.cuh -- shared-window full search over every PU of a 64x64 CTU.
+//
+// The PU set of a CTU is the one an AVS2 encoder's mode decision searches:
+// for CU sizes 64, 32 and 16 at every quadtree position the 13 PUs of the
+// partitions 2Nx2N, 2NxN, Nx2N, 2NxnU, 2NxnD, nLx2N and nRx2N, and for every
+// 8x8 CU its 8x8, 8x4 and 4x8 PUs plus the four 4x4 blocks -- 849 "slots",
+// covering all 25 LumaPU shapes.  For PUs that share the search centre (0,0)
+// and the MV predictor, the SAD of every PU at a displacement is a sum of the
+// SADs of its 4x4 blocks at that displacement, so one warp computes the 256
+// block SADs of the CTU once per displacement and derives all 849 PU costs
+// from them (sums in registers, warp shuffles across regions).
+//
+// Warp layout: lane = ry*8 + rx*2 + half.  (rx, ry) is one of the 16 16x16
+// regions of the CTU, half selects its top or bottom 8 rows.  A lane owns the
+// 8 4x4 SADs of its half-region, the 18 PUs of its two 8x8 CUs and 6-7 PUs of
+// its 16x16 CU; the 52 PUs of the 32x32 CUs and the 13 of the 64x64 CU are
+// spread over the lanes (2 + 1 per lane at most).
+//
+// A CTA of 4 warps handles one (CTU, reference) and a chunk of 32 search rows
+// (8 per warp) over the whole horizontal range; its reference window lives in
+// shared memory.  Each warp keeps, per PU, the minimum of a 32-bit key
+// (cost << 11 | row-in-warp << 8 | dx+R) for PUs up to 16x16 and per-row keys
+// (cost << 8 | dx+R) for the larger ones, and merges them into the global
+// 64-bit (cost, visit order) keys with atomicMin.
+//
+// Search limits: a PU is valid at a displacement iff the referenced block
+// lies within [-58, W+58) x [-58, H+58) -- the limits pred_inter_search_single
+// derives (md_inter.c:910-926) whenever they bind inside the search window.
+// CTUs near the picture edge run a variant that replaces the SAD of every
+// 4x4 block whose reference falls outside that region by a large value; the
+// PUs containing such a block then never win and are not merged.
+#pragma once
+
+namespace xg {
+
+constexpr int kSlots = 849;
+constexpr int kDyChunk = 32;            // search rows per CTA
+constexpr int kDyWarp = 8;              // search rows per warp
+constexpr int kCtuThreads = 128;
+constexpr uint32_t kPoisonSmall = 126976u;     // > any valid cost of a PU up to 16x16
+constexpr uint32_t kPoisonLarge = 1u << 22;    // replaces a 4x4 SAD outside the limits
+constexpr uint32_t kCapLarge = 2000000u;       // > any valid cost of a 64x64 PU
+constexpr int kLimitMargin = 58;               // 64-pixel margin minus 6 (md_inter.c:913-926)
+
+struct CtuJob {
+    int16_t x0, y0;       // CTU origin
+    int16_t ref;
+    int16_t mvp_x, mvp_y;
+    int16_t border;       // 1: limits may bind inside the window
+    int32_t slot_base;    // index of this job's row in the slot map
+};
+
+struct CtuPlan {
+    int n_jobs = 0, cap_jobs = 0;
+    CtuJob *d_jobs = nullptr;
+    int32_t *d_slots = nullptr;   // [n_jobs][kSlots]: PU index or -1
+};
+
+// ---- slot geometry (host) --------------------------------------------------------
+struct SlotGeom { int ox, oy, part; };
+
+static inline int part_of(int w, int h)
+{
+    for (int i = 0; i < kNumParts; i++)
+        if (h_pu_w[i] == w && h_pu_h[i] == h) return i;
+    return -1;
+}
+
+// mode m of an N x N CU at (cx, cy): 0 2Nx2N, 1-2 2NxN, 3-4 Nx2N, 5-6 2NxnU,
+// 7-8 2NxnD, 9-10 nLx2N, 11-12 nRx2N
+static inline SlotGeom cu_mode_geom(int N, int cx, int cy, int m)
+{
+    const int h2 = N / 2, q = N / 4, q3 = 3 * N / 4;
+    switch (m) {
+    case 0: return {cx, cy, part_of(N, N)};
+    case 1: return {cx, cy, part_of(N, h2)};
+    case 2: return {cx, cy + h2, part_of(N, h2)};
+    case 3: return {cx, cy, part_of(h2, N)};
+    case 4: return {cx + h2, cy, part_of(h2, N)};
+    case 5: return {cx, cy, part_of(N, q)};
+    case 6: return {cx, cy + q, part_of(N, q3)};
+    case 7: return {cx, cy, part_of(N, q3)};
+    case 8: return {cx, cy + q3, part_of(N, q)};
+    case 9: return {cx, cy, part_of(q, N)};
+    case 10: return {cx + q, cy, part_of(q3, N)};
+    case 11: return {cx, cy, part_of(q3, N)};
+    default: return {cx + q3, cy, part_of(q, N)};
+    }
+}
+
+static SlotGeom slot_geom(int s)
+{
+    if (s < 576) {
+        int cu = s / 9, m = s % 9, cx = (cu % 8) * 8, cy = (cu / 8) * 8;
+        switch (m) {
+        case 0: return {cx, cy, part_of(8, 8)};
+        case 1: return {cx, cy, part_of(8, 4)};
+        case 2: return {cx, cy + 4, part_of(8, 4)};
+        case 3: return {cx, cy, part_of(4, 8)};
+        case 4: return {cx + 4, cy, part_of(4, 8)};
+        case 5: return {cx, cy, 0};
+        case 6: return {cx + 4, cy, 0};
+        case 7: return {cx, cy + 4, 0};
+        default: return {cx + 4, cy + 4, 0};
+        }
+    }
+    if (s < 784) {
+        int cu = (s - 576) / 13, m = (s - 576) % 13;
+        return cu_mode_geom(16, (cu % 4) * 16, (cu / 4) * 16, m);
+    }
+    if (s < 836) {
+        int cu = (s - 784) / 13, m = (s - 784) % 13;
+        return cu_mode_geom(32, (cu % 2) * 32, (cu / 2) * 32, m);
+    }
+    return cu_mode_geom(64, 0, 0, s - 836);
+}
+
+// (part, ox/4, oy/4) -> slot, -1 if none
+struct SlotTable {
+    int16_t t[kNumParts][16][16];
+    SlotTable()
+    {
+        memset(t, 0xff, sizeof(t));
+        for (int s = 0; s < kSlots; s++) {
+            SlotGeom g = slot_geom(s);
+            t[g.part][g.oy >> 2][g.ox >> 2] = (int16_t)s;
+        }
+    }
+};
+
+// ---- device helpers ------------------------------------------------------------------
+__device__ __forceinline__ uint32_t sad4_acc(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t d;
+    asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t addmin(uint32_t a, uint32_t b, uint32_t c)
+{
+    return __viaddmin_u32(a, b, c);   // min(a + b, c)
+}
+
+// slot of small key k (0..24) of a lane
+__device__ __forceinline__ int small_slot(int rx, int ry, int half, int k)
+{
+    if (k < 18) {
+        const int side = k / 9, m = k % 9;
+        const int gx = 2 * rx + side, gy = 2 * ry + half;
+        return (gy * 8 + gx) * 9 + m;
+    }
+    // 16-CU keys 18..24 -> modes (half 0 / half 1)
+    const int i = k - 18;
+    const int m0[7] = {0, 1, 3, 5, 6, 9, 10};
+    const int m1[7] = {4, 2, 2, 8, 7, 12, 11};
+    return 576 + (ry * 4 + rx) * 13 + (half ? m1[i] : m0[i]);
+}
+
+// 32-CU key modes per (half, qx, qy) (-1: none); keys A and B
+__constant__ int8_t c_m32[2][2][2][2] = {
+    // half 0: [qx][qy] -> {A, B}
+    {{{1, 0}, {2, 8}}, {{5, 6}, {7, -1}}},
+    // half 1
+    {{{3, 9}, {10, 11}}, {{4, 12}, {-1, -1}}}};
+// coefficients over (X1, X2, X3, X4) for the modes above
+__constant__ int8_t c_c32[2][2][2][2][4] = {
+    {{{{1, 0, 0, 0}, {1, 0, 1, 0}}, {{1, 0, 0, 0}, {1, -1, 0, 0}}},
+     {{{0, 1, 0, 0}, {1, -1, 1, 0}}, {{0, 1, 1, 0}, {0, 0, 0, 0}}}},
+    {{{{1, 0, 0, 0}, {0, 1, 0, 0}}, {{1, -1, 1, 0}, {1, 0, 0, 1}}},
+     {{{1, 0, 0, 0}, {1, -1, 0, 0}}, {{0, 0, 0, 0}, {0, 0, 0, 0}}}}};
+// 64-CU key per lane (lane = ry*8 + rx*2 + half): mode (-1 none) and
+// coefficients over (TOT, P, RS) -- half-0 lanes hold row quantities (RS =
+// sum of a row of regions, P = pair of rows), half-1 lanes the column ones.
+__constant__ int8_t c_m64[32] = {0, 3, 1, -1, 5, 4, 6, 11, -1, 9, -1, -1, -1, -1, -1, 12,
+                                 2, 10, -1, -1, -1, -1, -1, -1, 7, -1, 8, -1, -1, -1, -1, -1};
+__constant__ int8_t c_c64[32][3] = {
+    {1, 0, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}, {0, 1, 0}, {1, 0, -1}, {1, 0, -1},
+    {0, 0, 0}, {0, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 1},
+    {0, 1, 0}, {1, 0, -1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0},
+    {1, 0, -1}, {0, 0, 0}, {0, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+
+template <bool BORDER>
+__global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
+                                                            const int32_t *__restrict__ slots,
+                                                            const uint8_t *__restrict__ cur,
+                                                            const uint8_t *const *refs, Geometry g, int R, int lambda,
+                                                            int ww, unsigned long long *__restrict__ keys)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int job_idx = blockIdx.x / nchunks, chunk = blockIdx.x % nchunks;
+    const CtuJob job = jobs[job_idx];
+    if (BORDER != (job.border != 0)) return;
+    const int dy0 = -R + chunk * kDyChunk;
+    const int wrows = 64 + kDyChunk - 1;
+    const int nd = 2 * R;
+    uint32_t *mvk = reinterpret_cast<uint32_t *>(smem);                 // [kDyChunk][nd]
+    uint8_t *win = smem + sizeof(uint32_t) * kDyChunk * nd;              // [wrows][ww]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // MV cost keys of this chunk's displacements (uniform over the CTU)
+    for (int e = tid; e < kDyChunk * nd; e += kCtuThreads) {
+        const int row = e / nd, dxr = e - row * nd;
+        const int dy = dy0 + row, dx = dxr - R;
+        const uint32_t mvc = (uint32_t)mv_cost_hd(lambda, dx * 4, dy * 4, job.mvp_x, job.mvp_y);
+        mvk[e] = (mvc << 11) | ((uint32_t)(row & (kDyWarp - 1)) << 8) | (uint32_t)dxr;
+    }
+    // reference window: rows y0+dy0 .., columns x0-R .., clamped into the plane
+    const uint8_t *ref = refs[job.ref];
+    const int wx0 = job.x0 - R, wy0 = job.y0 + dy0;
+    for (int e = tid; e < wrows * ww; e += kCtuThreads) {
+        const int r = e / ww, c = e - r * ww;
+        const int y = min(max(wy0 + r, -kPad), g.H + kPad - 1);
+        const int x = min(max(wx0 + c, -kPad), g.W + kPad - 1);
+        win[e] = ref[(ptrdiff_t)y * g.stride + x];
+    }
+    __syncthreads();
+
+    const int half = lane & 1, rx = (lane >> 1) & 3, ry = lane >> 3;
+    const int qx = rx & 1, qy = ry & 1;
+    // current block: 8 rows x 16 pixels of this half-region
+    uint32_t cw[8][4];
+    {
+        const uint8_t *o = cur + (ptrdiff_t)(job.y0 + 16 * ry + 8 * half) * g.stride + job.x0 + 16 * rx;
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(o + (ptrdiff_t)r * g.stride);
+            cw[r][0] = v.x; cw[r][1] = v.y; cw[r][2] = v.z; cw[r][3] = v.w;
+        }
+    }
+    // per-lane coefficient sets for the 32-CU and 64-CU keys
+    int c32a[4], c32b[4], c64[3];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        c32a[k] = c_c32[half][qx][qy][0][k];
+        c32b[k] = c_c32[half][qx][qy][1][k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) c64[k] = c_c64[lane][k];
+    const int m32a = c_m32[half][qx][qy][0], m32b = c_m32[half][qx][qy][1], m64 = c_m64[lane];
+    // shuffle partners: region pairs along the axis this half works on
+    const int pr1 = half ? 8 : 2;     // 32-CU pair (vertical for half 1, horizontal for half 0)
+    const int pr2 = half ? 2 : 8;     // the other 32-CU row/column
+    const int pr3 = half ? 16 : 4;    // 64-CU row / column sums
+    const int pr4 = half ? 2 : 8;     // 64-CU pairs
+    const int pr5 = half ? 4 : 16;    // 64-CU total
+
+    uint32_t ks[25];
+    unsigned long long kl[3] = {~0ull, ~0ull, ~0ull};
+#pragma unroll
+    for (int k = 0; k < 25; k++) ks[k] = 0xffffffffu;
+
+    // block geometry for the border variant
+    const int bx0 = job.x0 + 16 * rx, by0 = job.y0 + 16 * ry + 8 * half;
+
+    for (int rr = 0; rr < kDyWarp; rr++) {
+        const int row = warp * kDyWarp + rr;
+        const int dy = dy0 + row;
+        if (dy >= R) break;
+        const uint8_t *wbase = win + (size_t)(16 * ry + 8 * half + row) * ww + 16 * rx;
+        const uint32_t *mrow = mvk + row * nd;
+        uint32_t rowl[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+        bool brow[2] = {true, true};
+        if (BORDER) {
+#pragma unroll
+            for (int br = 0; br < 2; br++) {
+                const int yb = by0 + 4 * br + dy;
+                brow[br] = yb >= -kLimitMargin && yb + 4 <= g.H + kLimitMargin;
+            }
+        }
+        for (int j0 = 0; j0 < nd; j0 += 4) {
+            uint32_t s[4][2][4];
+#pragma unroll
+            for (int o = 0; o < 4; o++)
+#pragma unroll
+                for (int br = 0; br < 2; br++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) s[o][br][c] = 0;
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const uint32_t *wp = reinterpret_cast<const uint32_t *>(wbase + (size_t)r * ww + j0);
+                uint32_t w5[5];
+#pragma unroll
+                for (int k = 0; k < 5; k++) w5[k] = wp[k];
+#pragma unroll
+                for (int o = 0; o < 4; o++) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const uint32_t a = o ? __funnelshift_r(w5[c], w5[c + 1], 8 * o) : w5[c];
+                        s[o][r >> 2][c] = sad4_acc(cw[r][c], a, s[o][r >> 2][c]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 4; o++) {
+                const int dxr = j0 + o;
+                const uint32_t mks = mrow[dxr];
+                const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
+                uint32_t raw[2][4];
+#pragma unroll
+                for (int br = 0; br < 2; br++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) raw[br][c] = s[o][br][c];
+                if (BORDER) {
+                    const int dx = dxr - R;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const int xb = bx0 + 4 * c + dx;
+                        const bool colok = xb >= -kLimitMargin && xb + 4 <= g.W + kLimitMargin;
+#pragma unroll
+                        for (int br = 0; br < 2; br++)
+                            if (!(colok && brow[br])) raw[br][c] = kPoisonLarge;
+                    }
+                }
+                // small-key domain: SAD << 11 (poison clamped for the small PUs)
+                uint32_t t[2][4];
+#pragma unroll
+                for (int br = 0; br < 2; br++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        t[br][c] = (BORDER ? min(raw[br][c], kPoisonSmall) : raw[br][c]) << 11;
+                // 8x8 CUs of this half: left (cols 0,1) and right (cols 2,3)
+                uint32_t qv[2], at[2], ab[2], vl[2], vr[2];
+#pragma unroll
+                for (int sd = 0; sd < 2; sd++) {
+                    const int c0 = 2 * sd;
+                    at[sd] = t[0][c0] + t[0][c0 + 1];
+                    ab[sd] = t[1][c0] + t[1][c0 + 1];
+                    vl[sd] = t[0][c0] + t[1][c0];
+                    vr[sd] = t[0][c0 + 1] + t[1][c0 + 1];
+                    qv[sd] = at[sd] + ab[sd];
+                    const int kb = 9 * sd;
+                    ks[kb + 0] = addmin(qv[sd], mks, ks[kb + 0]);
+                    ks[kb + 1] = addmin(at[sd], mks, ks[kb + 1]);
+                    ks[kb + 2] = addmin(ab[sd], mks, ks[kb + 2]);
+                    ks[kb + 3] = addmin(vl[sd], mks, ks[kb + 3]);
+                    ks[kb + 4] = addmin(vr[sd], mks, ks[kb + 4]);
+                    ks[kb + 5] = addmin(t[0][c0], mks, ks[kb + 5]);
+                    ks[kb + 6] = addmin(t[0][c0 + 1], mks, ks[kb + 6]);
+                    ks[kb + 7] = addmin(t[1][c0], mks, ks[kb + 7]);
+                    ks[kb + 8] = addmin(t[1][c0 + 1], mks, ks[kb + 8]);
+                }
+                // 16x16 CU: own half (Fh, Lh, strips) + partner half
+                const uint32_t Fh = qv[0] + qv[1];
+                const uint32_t Lh = qv[0];
+                const uint32_t rr_ = half ? ab[0] + ab[1] : at[0] + at[1];   // own outer 16x4 strip
+                const uint32_t c0h = vl[0], c3h = vr[1];
+                const uint32_t Fh_o = __shfl_xor_sync(0xffffffffu, Fh, 1);
+                const uint32_t Lh_o = __shfl_xor_sync(0xffffffffu, Lh, 1);
+                const uint32_t xs = half ? c0h : c3h;
+                const uint32_t xs_o = __shfl_xor_sync(0xffffffffu, xs, 1);
+                const uint32_t F = Fh + Fh_o, L = Lh + Lh_o;
+                const uint32_t cc = (half ? c3h : c0h) + xs_o;          // col 3 (half 1) / col 0 (half 0)
+                ks[18] = addmin(F - (half ? L : 0u), mks, ks[18]);     // 16x16 | 8x16 right
+                ks[19] = addmin(Fh, mks, ks[19]);                      // 16x8 top | bottom
+                ks[20] = addmin(half ? Fh : L, mks, ks[20]);           // 8x16 left | (dup)
+                ks[21] = addmin(rr_, mks, ks[21]);                     // 16x4 y0 | y12
+                ks[22] = addmin(F - rr_, mks, ks[22]);                 // 16x12 y4 | y0
+                ks[23] = addmin(cc, mks, ks[23]);                      // 4x16 x0 | x12
+                ks[24] = addmin(F - cc, mks, ks[24]);                  // 12x16 x4 | x0
+                // large PUs in the raw domain
+                uint32_t Fr, Tr, Lr;
+                if (BORDER) {
+                    uint32_t fh = 0, lh = 0;
+#pragma unroll
+                    for (int br = 0; br < 2; br++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            fh += raw[br][c];
+                            if (c < 2) lh += raw[br][c];
+                        }
+                    const uint32_t fh_o = __shfl_xor_sync(0xffffffffu, fh, 1);
+                    const uint32_t lh_o = __shfl_xor_sync(0xffffffffu, lh, 1);
+                    Fr = fh + fh_o;
+                    Tr = half ? fh_o : fh;
+                    Lr = lh + lh_o;
+                } else {
+                    Fr = F >> 11;
+                    Tr = (half ? Fh_o : Fh) >> 11;
+                    Lr = L >> 11;
+                }
+                // 32x32 CUs
+                const uint32_t a1 = half ? Lr : Tr;
+                const uint32_t F_p = __shfl_xor_sync(0xffffffffu, Fr, pr1);
+                const uint32_t a_p = __shfl_xor_sync(0xffffffffu, a1, pr1);
+                const uint32_t X1 = Fr + F_p, X2 = a1 + a_p;           // FH, TH  |  FV, LV
+                const uint32_t X3 = __shfl_xor_sync(0xffffffffu, X1, pr2);
+                const uint32_t X4 = __shfl_xor_sync(0xffffffffu, X2, pr2);
+                const int va = c32a[0] * (int)X1 + c32a[1] * (int)X2 + c32a[2] * (int)X3 + c32a[3] * (int)X4;
+                const int vb = c32b[0] * (int)X1 + c32b[1] * (int)X2 + c32b[2] * (int)X3 + c32b[3] * (int)X4;
+                // 64x64 CU
+                const uint32_t RS = X1 + __shfl_xor_sync(0xffffffffu, X1, pr3);     // row | column sums
+                const uint32_t P = RS + __shfl_xor_sync(0xffffffffu, RS, pr4);      // row | column pairs
+                const uint32_t TOT = P + __shfl_xor_sync(0xffffffffu, P, pr5);
+                const int v64 = c64[0] * (int)TOT + c64[1] * (int)P + c64[2] * (int)RS;
+                rowl[0] = min(rowl[0], (min((uint32_t)va, kCapLarge) << 8) + mkl);
+                rowl[1] = min(rowl[1], (min((uint32_t)vb, kCapLarge) << 8) + mkl);
+                rowl[2] = min(rowl[2], (min((uint32_t)v64, kCapLarge) << 8) + mkl);
+            }
+        }
+        // fold this row's large-PU minima into 64-bit (cost, order) keys
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint32_t cost = rowl[k] >> 8, dxr = rowl[k] & 0xffu;
+            if (cost >= kCapLarge) continue;
+            const unsigned long long key =
+                ((unsigned long long)cost << 32) | (unsigned)(2 + (dy + R) * nd + (int)dxr);
+            kl[k] = key < kl[k] ? key : kl[k];
+        }
+    }
+    // merge into the global keys
+    const int32_t *smap = slots + (size_t)job.slot_base;
+    const int dyw = dy0 + warp * kDyWarp;
+#pragma unroll
+    for (int k = 0; k < 25; k++) {
+        const uint32_t key = ks[k];
+        const uint32_t cost = key >> 11;
+        if (cost >= kPoisonSmall) continue;
+        const int pu = smap[small_slot(rx, ry, half, k)];
+        if (pu < 0) continue;
+        const int dy = dyw + (int)((key >> 8) & 7), dxr = (int)(key & 0xffu);
+        atomicMin(&keys[pu], ((unsigned long long)cost << 32) | (unsigned)(2 + (dy + R) * nd + dxr));
+    }
+    const int lm[3] = {m32a, m32b, m64};
+    const int cu32 = (ry >> 1) * 2 + (rx >> 1);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (lm[k] < 0 || kl[k] == ~0ull) continue;
+        const int slot = k < 2 ? 784 + cu32 * 13 + lm[k] : 836 + lm[k];
+        const int pu = smap[slot];
+        if (pu >= 0) atomicMin(&keys[pu], kl[k]);
+    }
+}
+
+// ---- host planning -----------------------------------------------------------------
+static inline void ctu_plan_free(CtuPlan &p)
+{
+    if (p.d_jobs) cudaFree(p.d_jobs);
+    if (p.d_slots) cudaFree(p.d_slots);
+    p = CtuPlan();
+}
+
+// Splits a PU list into CTU jobs and the rest (`generic`).  A PU joins its
+// CTU's job when it sits on one of the CTU's slots, its MVP rounds to (0,0)
+// (so the search centre is (0,0)), all PUs of the job share that MVP, and
+// inside the (2R)^2 window its limits allow exactly the displacements the
+// edge rule allows.
+static inline bool same_range_in_window(int lo, int hi, int rule_lo, int rule_hi, int R)
+{
+    return max(lo, -R) == max(rule_lo, -R) && min(hi, R - 1) == min(rule_hi, R - 1);
+}
+
+static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, int W, int H, int nrefs, int R,
+                           std::vector<int> &generic, cudaStream_t st)
+{
+    static const SlotTable table;
+    const int cw = (W + 63) / 64, ch = (H + 63) / 64;
+    const int ngroups = cw * ch * nrefs;
+    std::vector<int> group_job(ngroups, -1);
+    std::vector<CtuJob> jobs;
+    std::vector<int32_t> slots;
+    generic.clear();
+    for (int i = 0; i < (int)pus.size(); i++) {
+        const xavs2gpu_pu_t &u = pus[i];
+        const int w = h_pu_w[u.part], h = h_pu_h[u.part];
+        bool ok = ((u.mvp_x + 2) >> 2) == 0 && ((u.mvp_y + 2) >> 2) == 0 && !(u.x & 3) && !(u.y & 3);
+        // (0,0) must be inside the limits for it to be the centre
+        ok = ok && u.min_x <= 0 && u.max_x >= 0 && u.min_y <= 0 && u.max_y >= 0;
+        ok = ok && same_range_in_window(u.min_x, u.max_x, -kLimitMargin - u.x, W + kLimitMargin - u.x - w, R) &&
+             same_range_in_window(u.min_y, u.max_y, -kLimitMargin - u.y, H + kLimitMargin - u.y - h, R);
+        const int s = ok ? table.t[u.part][(u.y & 63) >> 2][(u.x & 63) >> 2] : -1;
+        if (s < 0) { generic.push_back(i); continue; }
+        const int gidx = ((u.y >> 6) * cw + (u.x >> 6)) * nrefs + u.ref;
+        int j = group_job[gidx];
+        if (j < 0) {
+            j = (int)jobs.size();
+            group_job[gidx] = j;
+            CtuJob cj;
+            cj.x0 = (int16_t)(u.x & ~63); cj.y0 = (int16_t)(u.y & ~63); cj.ref = u.ref;
+            cj.mvp_x = u.mvp_x; cj.mvp_y = u.mvp_y;
+            // can the edge rule bind for any block of this CTU inside the window?
+            cj.border = (cj.x0 - R < -kLimitMargin || cj.x0 + 64 + R > W + kLimitMargin ||
+                         cj.y0 - R < -kLimitMargin || cj.y0 + 64 + R > H + kLimitMargin) ? 1 : 0;
+            cj.slot_base = j * kSlots;
+            jobs.push_back(cj);
+            slots.resize(slots.size() + kSlots, -1);
+        }
+        CtuJob &cj = jobs[j];
+        int32_t &slot = slots[(size_t)cj.slot_base + s];
+        if (cj.mvp_x != u.mvp_x || cj.mvp_y != u.mvp_y || slot >= 0) { generic.push_back(i); continue; }
+        slot = i;
+    }
+    if ((int)jobs.size() > p.cap_jobs) {
+        if (p.d_jobs) cudaFree(p.d_jobs);
+        if (p.d_slots) cudaFree(p.d_slots);
+        p.cap_jobs = (int)jobs.size() + 16;
+        XG_CUDA(cudaMalloc((void **)&p.d_jobs, sizeof(CtuJob) * p.cap_jobs));
+        XG_CUDA(cudaMalloc((void **)&p.d_slots, sizeof(int32_t) * kSlots * p.cap_jobs));
+    }
+    p.n_jobs = (int)jobs.size();
+    if (p.n_jobs) {
+        XG_CUDA(cudaMemcpyAsync(p.d_jobs, jobs.data(), sizeof(CtuJob) * p.n_jobs, cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaMemcpyAsync(p.d_slots, slots.data(), sizeof(int32_t) * slots.size(), cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+    }
+}
+
+static inline size_t ctu_smem_bytes(int R, int &ww)
+{
+    ww = (int)align_up((size_t)64 + 2 * R + 8, 16);
+    return sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
+}
+
+static void ctu_plan_run(const CtuPlan &p, const xavs2gpu_me_params_t &prm, const uint8_t *cur,
+                         const uint8_t *const *refs, const Geometry &g, const PuState *state,
+                         unsigned long long *keys, cudaStream_t st)
+{
+    (void)state;
+    if (p.n_jobs == 0) return;
+    const int R = prm.search_range;
+    int ww;
+    const size_t smem = ctu_smem_bytes(R, ww);
+    static bool attr_done[8] = {false};
+    const int dev = current_device();
+    if (!attr_done[dev]) {
+        const int maxb = (int)ctu_smem_bytes(128, ww);
+        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+        attr_done[dev] = true;
+        ctu_smem_bytes(R, ww);
+    }
+    const int nchunks = (2 * R + kDyChunk - 1) / kDyChunk;
+    const int grid = p.n_jobs * nchunks;
+    fs_ctu_kernel<false><<<grid, kCtuThreads, smem, st>>>(p.d_jobs, nchunks, p.d_slots, cur, refs, g, R,
+                                                          prm.lambda_factor, ww, keys);
+    fs_ctu_kernel<true><<<grid, kCtuThreads, smem, st>>>(p.d_jobs, nchunks, p.d_slots, cur, refs, g, R,
+                                                         prm.lambda_factor, ww, keys);
+    count_launch(2);
+}
+
+}  // namespace xg

@@ -1,0 +1,549 @@
+// me.cu -- batched full-search + sub-pel motion estimation for sm_103a.
+//
+// Per PU and reference the result equals the reference's xavs2_me_search
+// (source/encoder/me.c:879-1183) in full-search mode with me_subpel_refine
+// (me.c:479-579):
+//   1. candidates {clip(IPEL(mvp)), clip(0,0)} (md_inter.c:840-865), first
+//      strictly smaller cost wins; the best one is the search centre;
+//   2. SAD + lambda*mvbits over the (2R)^2 window around the centre, raster
+//      order j (rows) outer, i inner, first strictly smaller cost wins;
+//   3. half-pel then quarter-pel refinement on the frame sub-pel planes with
+//      SATD (or SAD) + lambda*mvbits.
+// "First strictly smaller in visit order" is evaluated as the minimum of the
+// 64-bit key (cost << 32 | visit order), which lets any number of threads
+// search parts of a window in any order and merge with atomicMin.
+//
+// Kernels: me_init_kernel (candidates), fs_ctu_kernel (shared-window search
+// of all PUs of a 64x64 CTU; fs_ctu.cuh), fs_generic_kernel (one PU per CTA)
+// and refine_kernel.
+#include "xavs2gpu_common.cuh"
+
+#include <cstring>
+#include <vector>
+
+namespace xg {
+
+constexpr int kPad = 80;                 // plane margin, as XAVS2_PAD (defines.h:298)
+constexpr unsigned long long kNoKey = ~0ull;
+
+struct PuState {
+    int16_t cand[2][2];
+    int16_t ncand;
+    int16_t valid;     // 1 when a candidate was inside the limits
+    int16_t cx, cy;    // search centre (best candidate)
+};
+
+struct Geometry {
+    int W, H, stride;
+};
+
+__device__ __forceinline__ int sad_block_lane(const uint8_t *a, int sa, const uint8_t *b, int sb, int w, int h, int lane)
+{
+    int s = 0;
+    for (int i = lane; i < w * h; i += 32) {
+        int y = i / w, x = i - y * w;
+        s += iabs_d((int)a[y * sa + x] - (int)b[y * sb + x]);
+    }
+    return s;
+}
+
+__device__ __forceinline__ int warp_sum_i(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ bool in_box(const xavs2gpu_pu_t &p, int mx, int my)
+{
+    return mx >= p.min_x && mx <= p.max_x && my >= p.min_y && my <= p.max_y;
+}
+
+// ---- 1. candidates ----------------------------------------------------------------
+// One warp per PU.  keys[i] starts as the best candidate's (cost, order 0/1).
+__global__ void __launch_bounds__(128) me_init_kernel(const xavs2gpu_pu_t *__restrict__ pus, int n,
+                                                      const uint8_t *__restrict__ cur, const uint8_t *const *refs,
+                                                      Geometry g, int lambda, PuState *__restrict__ state,
+                                                      unsigned long long *__restrict__ keys)
+{
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const xavs2gpu_pu_t p = pus[i];
+    const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+    const uint8_t *ref = refs[p.ref];
+    PuState st;
+    st.ncand = 0;
+    const int xs[2] = {(p.mvp_x + 2) >> 2, 0}, ys[2] = {(p.mvp_y + 2) >> 2, 0};
+    for (int c = 0; c < 2; c++) {
+        int x = min(max(xs[c], (int)p.min_x), (int)p.max_x);
+        int y = min(max(ys[c], (int)p.min_y), (int)p.max_y);
+        if (st.ncand == 1 && st.cand[0][0] == x && st.cand[0][1] == y) continue;
+        st.cand[st.ncand][0] = (int16_t)x;
+        st.cand[st.ncand][1] = (int16_t)y;
+        st.ncand++;
+    }
+    unsigned long long best = kNoKey;
+    const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
+    for (int c = 0; c < st.ncand; c++) {
+        int mx = st.cand[c][0], my = st.cand[c][1];
+        if (!in_box(p, mx, my)) continue;
+        const uint8_t *r = ref + (ptrdiff_t)(p.y + my) * g.stride + p.x + mx;
+        int cost = warp_sum_i(sad_block_lane(o, g.stride, r, g.stride, w, h, lane)) +
+                   mv_cost_hd(lambda, mx * 4, my * 4, p.mvp_x, p.mvp_y);
+        unsigned long long k = ((unsigned long long)(unsigned)cost << 32) | (unsigned)c;
+        if (k < best) best = k;
+    }
+    st.valid = best != kNoKey;
+    int bc = st.valid ? (int)(best & 0xffffffffu) : 0;
+    st.cx = st.valid ? st.cand[bc][0] : 0;
+    st.cy = st.valid ? st.cand[bc][1] : 0;
+    if (lane == 0) {
+        state[i] = st;
+        keys[i] = best;
+    }
+}
+
+// ---- 2b. per-PU full search (one CTA per PU) --------------------------------------
+// Visit order of window position (i, j) is 2 + (j+R)*2R + (i+R).
+__global__ void __launch_bounds__(256) fs_generic_kernel(const int *__restrict__ list, int n,
+                                                         const xavs2gpu_pu_t *__restrict__ pus,
+                                                         const PuState *__restrict__ state,
+                                                         const uint8_t *__restrict__ cur, const uint8_t *const *refs,
+                                                         Geometry g, int R, int lambda,
+                                                         unsigned long long *__restrict__ keys)
+{
+    __shared__ uint8_t s_cur[64 * 64];
+    __shared__ unsigned long long s_red[8];
+    for (int li = blockIdx.x; li < n; li += gridDim.x) {
+        const int i = list[li];
+        const xavs2gpu_pu_t p = pus[i];
+        const PuState st = state[i];
+        if (!st.valid) continue;
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
+        __syncthreads();
+        for (int k = threadIdx.x; k < w * h; k += blockDim.x) s_cur[k] = o[(k / w) * g.stride + k % w];
+        __syncthreads();
+        const uint8_t *ref = refs[p.ref] + (ptrdiff_t)p.y * g.stride + p.x;
+        unsigned long long best = kNoKey;
+        const int npos = 4 * R * R;
+        for (int q = threadIdx.x; q < npos; q += blockDim.x) {
+            const int j = q / (2 * R) - R, ii = q % (2 * R) - R;
+            const int mx = st.cx + ii, my = st.cy + j;
+            if (!in_box(p, mx, my)) continue;
+            const uint8_t *r = ref + (ptrdiff_t)my * g.stride + mx;
+            int s = 0;
+            for (int y = 0; y < h; y++) {
+                const uint8_t *rr = r + (ptrdiff_t)y * g.stride;
+                const uint8_t *cc = s_cur + y * w;
+                for (int x = 0; x < w; x++) s += iabs_d((int)cc[x] - (int)rr[x]);
+            }
+            int cost = s + mv_cost_hd(lambda, mx * 4, my * 4, p.mvp_x, p.mvp_y);
+            unsigned long long k = ((unsigned long long)(unsigned)cost << 32) | (unsigned)(2 + q);
+            if (k < best) best = k;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            unsigned long long other = __shfl_xor_sync(0xffffffffu, best, off);
+            best = other < best ? other : best;
+        }
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < (int)(blockDim.x >> 5); k++) best = s_red[k] < best ? s_red[k] : best;
+            atomicMin(&keys[i], best);
+        }
+    }
+}
+
+// ---- 3. sub-pel refinement ------------------------------------------------------------
+// One warp per PU: the candidate costs of one refinement step are evaluated in
+// parallel, then the first strictly smaller one (spiral order, centre first)
+// is taken, as the reference's sequential loop does.
+__constant__ int8_t c_spiral[2][9][2] = {
+    {{0, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, -1}, {-1, 0}, {1, 0}, {-1, 1}, {1, 1}},
+    {{0, 0}, {0, -1}, {-1, -1}, {-1, 0}, {-1, 1}, {0, 1}, {1, 1}, {1, 0}, {1, -1}}};
+
+// cost (SATD or SAD) of the PU against plane[(my&3)*4 + (mx&3)] at quarter-pel (mx, my)
+__device__ int qpel_cost_warp(const xavs2gpu_pu_t &p, int w, int h, bool hadamard, const uint8_t *o,
+                              const uint8_t *const *planes, const Geometry &g, int mx, int my, int lane)
+{
+    const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(p.y + (my >> 2)) * g.stride + p.x + (mx >> 2);
+    int s = 0;
+    if (!hadamard) {
+        s = sad_block_lane(o, g.stride, r, g.stride, w, h, lane);
+    } else {
+        const bool u4 = satd_unit4(w, h);
+        const int uw = u4 ? 4 : 8, nux = w / uw, nu = nux * (h >> 2);
+        for (int u = lane; u < nu; u += 32) {
+            int uy = u / nux, ux = u - uy * nux;
+            s += satd_unit_d(u4, o + (ptrdiff_t)uy * 4 * g.stride + ux * uw, g.stride,
+                             r + (ptrdiff_t)uy * 4 * g.stride + ux * uw, g.stride);
+        }
+    }
+    return warp_sum_i(s);
+}
+
+__global__ void __launch_bounds__(128) refine_kernel(const xavs2gpu_pu_t *__restrict__ pus, int n,
+                                                     const PuState *__restrict__ state,
+                                                     const unsigned long long *__restrict__ keys,
+                                                     const uint8_t *__restrict__ cur,
+                                                     const uint8_t *const *ref_planes,   // [ref*16 + k]
+                                                     Geometry g, int R, xavs2gpu_me_params_t prm,
+                                                     xavs2gpu_me_result_t *__restrict__ out)
+{
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const xavs2gpu_pu_t p = pus[i];
+    const PuState st = state[i];
+    const unsigned long long key = keys[i];
+    xavs2gpu_me_result_t res;
+    if (!st.valid || key == kNoKey) {
+        res.bmv_x = res.bmv_y = res.imv_x = res.imv_y = 0;
+        res.bcost = res.icost = 1 << 30;
+        res.mvcost = 0;
+        if (lane == 0) out[i] = res;
+        return;
+    }
+    const int icost = (int)(key >> 32);
+    const unsigned order = (unsigned)(key & 0xffffffffu);
+    int bmx, bmy;
+    if (order < 2) {
+        bmx = st.cand[order][0];
+        bmy = st.cand[order][1];
+    } else {
+        const int q = (int)order - 2;
+        bmx = st.cx + q % (2 * R) - R;
+        bmy = st.cy + q / (2 * R) - R;
+    }
+    const int lam = prm.lambda_factor, pmx = p.mvp_x, pmy = p.mvp_y;
+    res.imv_x = (int16_t)bmx;
+    res.imv_y = (int16_t)bmy;
+    res.icost = icost;
+    int bx = bmx * 4, by = bmy * 4, best = icost;
+    if (prm.fractional_me) {
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        const bool had = prm.use_hadamard != 0;
+        const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
+        const uint8_t *const *planes = ref_planes + 16 * p.ref;
+        const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
+        int cx = bx, cy = by;
+        if (had) best = qpel_cost_warp(p, w, h, true, o, planes, g, cx, cy, lane) + mv_cost_hd(lam, cx, cy, pmx, pmy);
+        for (int pos = 1; pos < 9; pos += step) {
+            int mx = cx + 2 * c_spiral[pat][pos][0], my = cy + 2 * c_spiral[pat][pos][1];
+            int c = qpel_cost_warp(p, w, h, had, o, planes, g, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
+            if (c < best) { best = c; bx = mx; by = my; }
+        }
+        if (prm.fractional_me > 1) {
+            cx = bx; cy = by;
+            const int ctr_x = (pmx >> 1) << 1, ctr_y = (pmy >> 1) << 1;
+            for (int pos = 1; pos < 9; pos += step) {
+                int sx = c_spiral[pat][pos][0], sy = c_spiral[pat][pos][1], mx, my;
+                if (prm.enable_pmvr) {
+                    // pmvr_adapt_mv (me.c:412-424), TH_PMVR = 2
+                    if (abs(cx - ctr_x) > 2 || abs(cy - ctr_y) > 2) {
+                        mx = cx + 2 * sx; my = cy + 2 * sy;
+                        if (abs(mx - ctr_x) <= 2 && abs(my - ctr_y) <= 2) continue;
+                    } else {
+                        mx = cx + sx; my = cy + sy;
+                        if (abs(mx - ctr_x) > 2 || abs(my - ctr_y) > 2) continue;
+                    }
+                } else {
+                    mx = cx + sx; my = cy + sy;
+                }
+                int c = qpel_cost_warp(p, w, h, had, o, planes, g, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
+                if (c < best) { best = c; bx = mx; by = my; }
+            }
+        }
+    }
+    res.bmv_x = (int16_t)bx;
+    res.bmv_y = (int16_t)by;
+    res.bcost = best;
+    res.mvcost = mv_cost_hd(lam, bx, by, pmx, pmy);
+    if (lane == 0) out[i] = res;
+}
+
+}  // namespace xg
+
+#include "fs_ctu.cuh"
+
+namespace xg {
+
+// ---- session ---------------------------------------------------------------------
+struct MeSessionImpl {
+    int W = 0, H = 0, nrefs = 0, max_pus = 0;
+    int stride = 0, rows = 0;
+    size_t plane_bytes = 0;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    uint8_t *d_planes = nullptr;          // plane 0: current picture; 1 + r*16 + k: reference r, sub-pel k
+    uint8_t **d_plane_ptrs = nullptr;     // [1 + nrefs*16] pointers at pixel (0,0)
+    const uint8_t **d_ref0 = nullptr;     // [nrefs] full-pel plane of each reference
+    uint8_t *h_stage = nullptr;           // pinned staging for pictures
+    size_t h_stage_cap = 0;
+    uint8_t *d_upload = nullptr;          // device copy of an uploaded picture
+    // PU list and plan
+    int n = 0;
+    xavs2gpu_pu_t *d_pus = nullptr;
+    xavs2gpu_me_result_t *d_res = nullptr;
+    xavs2gpu_me_result_t *h_res = nullptr;   // pinned
+    unsigned long long *d_keys = nullptr;
+    PuState *d_state = nullptr;
+    int *d_generic = nullptr;
+    int n_generic = 0;
+    CtuPlan plan;
+    int plan_R = -1;               // search range the plan was built for (-1: stale)
+    int n_ctu_pus = 0;
+    std::vector<xavs2gpu_pu_t> h_pus;
+
+    uint8_t *plane(int idx) { return d_planes + (size_t)idx * plane_bytes + (size_t)kPad * stride + kPad; }
+};
+
+}  // namespace xg
+
+using namespace xg;
+
+struct xavs2gpu_me_session {
+    MeSessionImpl impl;
+};
+
+extern "C" void xavs2gpu_pu_set_limits(xavs2gpu_pu_t *pu, int width, int height, int vmin_qpel, int vmax_qpel)
+{
+    const int w = h_pu_w[pu->part], h = h_pu_h[pu->part];
+    auto clip = [](int lo, int hi, int v) { return v < lo ? lo : (v > hi ? hi : v); };
+    int mn = clip(-8192, 8191, (-64 - pu->x) * 4), mx = clip(-8192, 8191, (width + 64 - pu->x - w) * 4);
+    pu->min_x = (int16_t)((mn >> 2) + 6);
+    pu->max_x = (int16_t)((mx >> 2) - 6);
+    mn = clip(vmin_qpel, vmax_qpel, (-64 - pu->y) * 4);
+    mx = clip(vmin_qpel, vmax_qpel, (height + 64 - pu->y - h) * 4);
+    pu->min_y = (int16_t)((mn >> 2) + 6);
+    pu->max_y = (int16_t)((mx >> 2) - 6);
+}
+
+extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int num_refs, int max_pus)
+{
+    if (width < 8 || height < 8 || width > 8192 || height > 8192 || num_refs < 1 || num_refs > 16 || max_pus < 1) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_create", "bad size, reference count or PU capacity");
+        return nullptr;
+    }
+    auto *s = new xavs2gpu_me_session();
+    MeSessionImpl &m = s->impl;
+    m.device = current_device();
+    XG_CUDA(cudaSetDevice(m.device));
+    m.W = width; m.H = height; m.nrefs = num_refs; m.max_pus = max_pus;
+    m.stride = (int)align_up((size_t)width + 2 * kPad, 64);
+    m.rows = height + 2 * kPad;
+    m.plane_bytes = align_up((size_t)m.stride * m.rows, 256);
+    const int nplanes = 1 + 16 * num_refs;
+    XG_CUDA(cudaStreamCreateWithFlags(&m.st, cudaStreamNonBlocking));
+    XG_CUDA(cudaMalloc((void **)&m.d_planes, m.plane_bytes * nplanes));
+    XG_CUDA(cudaMemsetAsync(m.d_planes, 0, m.plane_bytes * nplanes, m.st));
+    std::vector<uint8_t *> ptrs(nplanes);
+    for (int k = 0; k < nplanes; k++) ptrs[k] = m.plane(k);
+    XG_CUDA(cudaMalloc((void **)&m.d_plane_ptrs, sizeof(uint8_t *) * nplanes));
+    XG_CUDA(cudaMemcpy(m.d_plane_ptrs, ptrs.data(), sizeof(uint8_t *) * nplanes, cudaMemcpyHostToDevice));
+    std::vector<const uint8_t *> r0(num_refs);
+    for (int r = 0; r < num_refs; r++) r0[r] = m.plane(1 + 16 * r);
+    XG_CUDA(cudaMalloc((void **)&m.d_ref0, sizeof(uint8_t *) * num_refs));
+    XG_CUDA(cudaMemcpy(m.d_ref0, r0.data(), sizeof(uint8_t *) * num_refs, cudaMemcpyHostToDevice));
+    m.h_stage_cap = (size_t)width * height;
+    XG_CUDA(cudaMallocHost((void **)&m.h_stage, m.h_stage_cap));
+    XG_CUDA(cudaMalloc((void **)&m.d_upload, m.h_stage_cap));
+    XG_CUDA(cudaMalloc((void **)&m.d_pus, sizeof(xavs2gpu_pu_t) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_res, sizeof(xavs2gpu_me_result_t) * max_pus));
+    XG_CUDA(cudaMallocHost((void **)&m.h_res, sizeof(xavs2gpu_me_result_t) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_keys, sizeof(unsigned long long) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_state, sizeof(PuState) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_generic, sizeof(int) * max_pus));
+    XG_CUDA(cudaStreamSynchronize(m.st));
+    return s;
+}
+
+extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
+{
+    if (!s) return;
+    MeSessionImpl &m = s->impl;
+    cudaSetDevice(m.device);
+    if (m.st) cudaStreamSynchronize(m.st);
+    ctu_plan_free(m.plan);
+    cudaFree(m.d_planes); cudaFree(m.d_plane_ptrs); cudaFree(m.d_ref0);
+    cudaFreeHost(m.h_stage); cudaFree(m.d_upload);
+    cudaFree(m.d_pus); cudaFree(m.d_res); cudaFreeHost(m.h_res); cudaFree(m.d_keys);
+    cudaFree(m.d_state); cudaFree(m.d_generic);
+    if (m.st) cudaStreamDestroy(m.st);
+    delete s;
+}
+
+// copies a W x H picture (device memory, `stride`) into plane `idx`, then
+// replicates its border; for references also computes the 15 sub-pel planes
+static int load_picture(MeSessionImpl &m, int slot, const uint8_t *dsrc, intptr_t stride)
+{
+    const int idx = slot < 0 ? 0 : 1 + 16 * slot;
+    XG_CUDA(cudaMemcpy2DAsync(m.plane(idx), m.stride, dsrc, stride, m.W, m.H, cudaMemcpyDeviceToDevice, m.st));
+    if (xavs2gpu_expand_border(m.plane(idx), m.stride, m.W, m.H, kPad, m.st) != XAVS2GPU_OK) return XAVS2GPU_ERR_CUDA;
+    if (slot >= 0) {
+        uint8_t *planes[16];
+        for (int k = 0; k < 16; k++) planes[k] = m.plane(idx + k);
+        return xavs2gpu_interpolate_frame(m.plane(idx), m.stride, m.W, m.H, kPad, planes, 2, m.st);
+    }
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_me_set_picture_device(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride)
+{
+    if (!s || slot < -1 || slot >= s->impl.nrefs || stride < s->impl.W) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_picture_device", "bad slot or stride");
+        return XAVS2GPU_ERR_ARG;
+    }
+    XG_CUDA(cudaSetDevice(s->impl.device));
+    return load_picture(s->impl, slot, luma, stride);
+}
+
+extern "C" int xavs2gpu_me_set_picture_host(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride)
+{
+    if (!s || slot < -1 || slot >= s->impl.nrefs || stride < s->impl.W) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_picture_host", "bad slot or stride");
+        return XAVS2GPU_ERR_ARG;
+    }
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaSetDevice(m.device));
+    // the staging buffer may still feed an earlier upload on the stream
+    XG_CUDA(cudaStreamSynchronize(m.st));
+    pack_rows(m.h_stage, luma, stride, m.W, m.H);
+    XG_CUDA(cudaMemcpyAsync(m.d_upload, m.h_stage, (size_t)m.W * m.H, cudaMemcpyHostToDevice, m.st));
+    return load_picture(m, slot, m.d_upload, m.W);
+}
+
+extern "C" int xavs2gpu_me_set_pus(xavs2gpu_me_session_t *s, const xavs2gpu_pu_t *pus, int n)
+{
+    if (!s || n < 0 || n > s->impl.max_pus) {
+        fail(XAVS2GPU_ERR_CAPACITY, "xavs2gpu_me_set_pus", "PU count exceeds the session capacity");
+        return XAVS2GPU_ERR_CAPACITY;
+    }
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaSetDevice(m.device));
+    for (int i = 0; i < n; i++) {
+        const xavs2gpu_pu_t &p = pus[i];
+        const int w = p.part < kNumParts ? h_pu_w[p.part] : 0, h = p.part < kNumParts ? h_pu_h[p.part] : 0;
+        if (p.part >= kNumParts || p.ref >= m.nrefs || p.x < 0 || p.y < 0 || p.x + w > m.W || p.y + h > m.H) {
+            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_pus", "PU outside the picture or bad shape/reference");
+            return XAVS2GPU_ERR_ARG;
+        }
+        // every reference read (window, sub-pel taps) must stay inside the margin
+        if (p.min_x < -kPad + 8 - p.x || p.max_x > m.W + kPad - 8 - p.x - w || p.min_y < -kPad + 8 - p.y ||
+            p.max_y > m.H + kPad - 8 - p.y - h) {
+            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_pus", "search limits reach beyond the 80-pixel margin");
+            return XAVS2GPU_ERR_ARG;
+        }
+    }
+    m.n = n;
+    m.h_pus.assign(pus, pus + n);
+    XG_CUDA(cudaStreamSynchronize(m.st));
+    if (n) XG_CUDA(cudaMemcpyAsync(m.d_pus, pus, sizeof(xavs2gpu_pu_t) * n, cudaMemcpyHostToDevice, m.st));
+    XG_CUDA(cudaStreamSynchronize(m.st));
+    m.plan_R = -1;
+    return XAVS2GPU_OK;
+}
+
+// (Re)builds the split into CTU jobs and per-PU searches for window size R.
+static void ensure_plan(MeSessionImpl &m, int R)
+{
+    if (m.plan_R == R) return;
+    std::vector<int> generic;
+    ctu_plan_build(m.plan, m.h_pus, m.W, m.H, m.nrefs, R, generic, m.st);
+    m.n_generic = (int)generic.size();
+    m.n_ctu_pus = m.n - m.n_generic;
+    if (m.n_generic)
+        XG_CUDA(cudaMemcpyAsync(m.d_generic, generic.data(), sizeof(int) * m.n_generic, cudaMemcpyHostToDevice, m.st));
+    XG_CUDA(cudaStreamSynchronize(m.st));
+    m.plan_R = R;
+}
+
+extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm)
+{
+    if (!s || !prm || prm->search_range < 1 || prm->search_range > 128 || prm->fractional_me < 0 ||
+        prm->fractional_me > 2 || prm->lambda_factor < 0) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_run", "bad parameters");
+        return XAVS2GPU_ERR_ARG;
+    }
+    MeSessionImpl &m = s->impl;
+    if (m.n == 0) return XAVS2GPU_OK;
+    XG_CUDA(cudaSetDevice(m.device));
+    Geometry g{m.W, m.H, m.stride};
+    const int R = prm->search_range, lam = prm->lambda_factor;
+    ensure_plan(m, R);
+    me_init_kernel<<<(m.n * 32 + 127) / 128, 128, 0, m.st>>>(m.d_pus, m.n, m.plane(0), m.d_ref0, g, lam, m.d_state,
+                                                             m.d_keys);
+    count_launch();
+    ctu_plan_run(m.plan, *prm, m.plane(0), m.d_ref0, g, m.d_state, m.d_keys, m.st);
+    if (m.n_generic) {
+        int grid = m.n_generic < 152 * 8 ? m.n_generic : 152 * 8;
+        fs_generic_kernel<<<grid, 256, 0, m.st>>>(m.d_generic, m.n_generic, m.d_pus, m.d_state, m.plane(0), m.d_ref0,
+                                                  g, R, lam, m.d_keys);
+        count_launch();
+    }
+    refine_kernel<<<(m.n * 32 + 127) / 128, 128, 0, m.st>>>(m.d_pus, m.n, m.d_state, m.d_keys, m.plane(0),
+                                                            (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm,
+                                                            m.d_res);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_me_get_results(xavs2gpu_me_session_t *s, xavs2gpu_me_result_t *out)
+{
+    if (!s || !out) return XAVS2GPU_ERR_ARG;
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaSetDevice(m.device));
+    if (m.n) {
+        XG_CUDA(cudaMemcpyAsync(m.h_res, m.d_res, sizeof(xavs2gpu_me_result_t) * m.n, cudaMemcpyDeviceToHost, m.st));
+        XG_CUDA(cudaStreamSynchronize(m.st));
+        memcpy(out, m.h_res, sizeof(xavs2gpu_me_result_t) * m.n);
+    }
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_me_sync(xavs2gpu_me_session_t *s)
+{
+    if (!s) return XAVS2GPU_ERR_ARG;
+    XG_CUDA(cudaStreamSynchronize(s->impl.st));
+    return XAVS2GPU_OK;
+}
+
+extern "C" const xavs2gpu_me_result_t *xavs2gpu_me_results_device(xavs2gpu_me_session_t *s)
+{
+    return s ? s->impl.d_res : nullptr;
+}
+
+extern "C" uint8_t *xavs2gpu_me_plane_device(xavs2gpu_me_session_t *s, int slot, int k)
+{
+    if (!s || slot < -1 || slot >= s->impl.nrefs || k < 0 || k > 15 || (slot < 0 && k != 0)) return nullptr;
+    return s->impl.plane(slot < 0 ? 0 : 1 + 16 * slot + k);
+}
+
+extern "C" int xavs2gpu_me_plane_stride(xavs2gpu_me_session_t *s) { return s ? s->impl.stride : 0; }
+
+extern "C" int xavs2gpu_me_get_plane(xavs2gpu_me_session_t *s, int slot, int k, uint8_t *out, intptr_t stride)
+{
+    uint8_t *p = xavs2gpu_me_plane_device(s, slot, k);
+    if (!p || !out || stride < s->impl.W + 2 * kPad) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_get_plane", "bad slot, plane or stride");
+        return XAVS2GPU_ERR_ARG;
+    }
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaSetDevice(m.device));
+    XG_CUDA(cudaMemcpy2DAsync(out, stride, p - (size_t)kPad * m.stride - kPad, m.stride, m.W + 2 * kPad,
+                              m.H + 2 * kPad, cudaMemcpyDeviceToHost, m.st));
+    XG_CUDA(cudaStreamSynchronize(m.st));
+    return XAVS2GPU_OK;
+}
+extern "C" int xavs2gpu_me_plane_pad(xavs2gpu_me_session_t *) { return kPad; }
+extern "C" void *xavs2gpu_me_stream(xavs2gpu_me_session_t *s) { return s ? (void *)s->impl.st : nullptr; }
+
+extern "C" void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus, int *n_generic_pus, int *n_ctu_jobs)
+{
+    if (!s) return;
+    if (n_ctu_pus) *n_ctu_pus = s->impl.n_ctu_pus;
+    if (n_generic_pus) *n_generic_pus = s->impl.n_generic;
+    if (n_ctu_jobs) *n_ctu_jobs = s->impl.plan.n_jobs;
+}
