@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark: bit-exact batched motion-search block-cost evaluation.
+
+Workload (one step = one picture): 1920x1080 8-bit luma, two reference
+pictures (k-1, k-2), synthetic content with 16 block-local motions
+U[-32, 32] px in quarter-pel steps.  Every PU of the CU-quadtree layout of
+every CTU (all 25 AVS2 PU shapes, 849 per CTU, those fully inside the
+picture) is searched against both references: integer full search over
+[-64, 64)^2 around the best of {MVP, (0,0)} with SAD + lambda*MV bits, then
+half- and quarter-pel refinement with SATD + lambda*MV bits at QP 32 (P
+picture lambda), exactly as xavs2_me_search + me_subpel_refine.  A step also
+loads the three pictures and computes the 15 sub-pel planes of both
+references.
+
+Metric: block-cost evaluations per second (one evaluation = one (PU,
+reference, candidate) cost: MVP/zero candidates, every full-search position
+inside the PU's search limits, and the 17 sub-pel costs).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NREFS, RANGE, QP = 2, 64, 32
+METRIC = "bit-exact block-cost evals/s (1080p batched ME, 2 refs, FS +-64 + quarter-pel SATD)"
+UNIT = "evals/s"
+
+
+def lambda_factor(qp, factor=0.68):
+    lam = 2.0 ** ((qp - 11) / 4.0) * factor
+    return int(65536.0 * np.sqrt(lam) + 0.5)
+
+
+def count_evals(pus, R, frac=2, hadamard=1):
+    """Evaluations per search: 1 candidate (MVP rounds to (0,0)), every
+    full-search position inside the limits, 1 + 8 + 8 sub-pel costs."""
+    nx = np.minimum(pus["max_x"].astype(np.int64), R - 1) - np.maximum(pus["min_x"].astype(np.int64), -R) + 1
+    ny = np.minimum(pus["max_y"].astype(np.int64), R - 1) - np.maximum(pus["min_y"].astype(np.int64), -R) + 1
+    sub = (1 if hadamard else 0) + 8 + (8 if frac > 1 else 0)
+    return int((1 + np.clip(nx, 0, None) * np.clip(ny, 0, None) + sub).sum())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            text, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            text, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in text.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_sample_search(pus, cur, refs, prm_tuple, fraction, seed, threads):
+    """The oracle's restatement of xavs2_me_search over a random sample of
+    the PU list, on `threads` host threads; returns (evals, seconds)."""
+    import oracle
+    olib = oracle.lib()
+    rng = np.random.default_rng(seed)
+    sel = np.ascontiguousarray(pus[rng.random(len(pus)) < fraction])
+    h, w = cur.shape
+    stride = w + 160
+    flats = [np.ascontiguousarray(oracle.interpolate_frame(olib, r, mode=2).reshape(16, -1)) for r in refs]
+    frefs = (ctypes.c_void_p * (16 * len(refs)))(*[oracle.ptr(f[k], 80 * stride + 80).value
+                                                   for f in flats for k in range(16)])
+    out = np.zeros(len(sel), oracle.RESULT_DTYPE)
+    prm = oracle.MeParams(*prm_tuple)
+    t0 = time.perf_counter()
+    olib.xo_me_search_list(ctypes.byref(prm), oracle.ptr(sel), len(sel), oracle.ptr(cur), w, frefs, stride,
+                           oracle.ptr(out), threads)
+    dt = time.perf_counter() - t0
+    return count_evals(sel, prm_tuple[0]), dt, len(sel)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    WIDTH, HEIGHT = args.width, args.height
+    """CPU arm: the oracle port of the reference's search (the reference tree
+    itself is not on this machine), all host threads, a bounded random sample
+    of the picture's PU searches per step."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import xavs2_gb300.synth as synth
+    import xavs2_gb300 as xg
+    cur, refs = synth.me_workload(seed=1, width=WIDTH, height=HEIGHT)
+    pus = xg.frame_pus(WIDTH, HEIGHT, NREFS)
+    prm = (RANGE, lambda_factor(QP), 1, 2, 0, 0)
+    threads = os.cpu_count() or 1
+    frac = args.cpu_fraction
+    for i in range(args.warmup):
+        cpu_sample_search(pus, cur, refs, prm, frac / 4, 100 + i, threads)
+    ev = 0
+    tt = 0.0
+    n = 0
+    for i in range(args.steps):
+        e, dt, k = cpu_sample_search(pus, cur, refs, prm, frac, 200 + i, threads)
+        ev += e
+        tt += dt
+        n += k
+    value = ev / tt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic", "config": {"workload": "me_1080p_2ref_fs64_qpel_satd", "width": WIDTH,
+                                            "height": HEIGHT, "refs": NREFS, "search_range": RANGE, "qp": QP},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "per step a random %.2f%% of the picture's %d PU searches" % (100 * frac, len(pus))},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+
+    WIDTH, HEIGHT = args.width, args.height
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+
+    cur, refs = synth.me_workload(seed=1 + rank, width=WIDTH, height=HEIGHT)
+    pus = xg.frame_pus(WIDTH, HEIGHT, NREFS)
+    prm = xg.MeParams(RANGE, lambda_factor(QP), 1, 2, 0, 0)
+    evals = count_evals(pus, RANGE)
+    sess = xg.MeSession(WIDTH, HEIGHT, NREFS, len(pus))
+    sess.set_pus(pus)
+    stream = torch.cuda.ExternalStream(sess.stream())
+    d_cur = torch.from_numpy(cur).cuda()
+    d_refs = [torch.from_numpy(r).cuda() for r in refs]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")   # > L2 (129 MB)
+    torch.cuda.synchronize()
+
+    def step_device():
+        sess.set_picture_device(-1, d_cur.data_ptr(), WIDTH)
+        for i, r in enumerate(d_refs):
+            sess.set_picture_device(i, r.data_ptr(), WIDTH)
+        sess.run(prm)
+
+    for _ in range(args.warmup):
+        step_device()
+    sess.sync()
+    # correctness spot check against the last warm-up (cheap: a few PUs)
+    res = sess.results()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing: per-step events, L2 flushed between steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    barrier()
+    clk.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step_device()
+            ends[i].record(stream)
+    sess.sync()
+    barrier()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = evals * world * args.steps / (total_ms / 1e3)
+
+    # ---- per-kernel timing on the session stream (separate pass)
+    sess.set_profiling(True)
+    phases = np.zeros(4)
+    interp_ms = 0.0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            ev0.record(stream)
+            for j, r in enumerate(d_refs):
+                sess.set_picture_device(j, r.data_ptr(), WIDTH)
+            ev1.record(stream)
+            sess.set_picture_device(-1, d_cur.data_ptr(), WIDTH)
+            sess.run(prm)
+            phases += np.array(sess.phase_ms())
+            interp_ms += ev0.elapsed_time(ev1)
+    sess.set_profiling(False)
+    phases /= args.steps
+    interp_ms /= args.steps
+    n_ctu, n_gen, n_jobs = sess.plan_stats()
+
+    peaks, peak_src = measured_peaks()
+    n_pos = (2 * RANGE) ** 2
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": total_ms / args.steps,
+                              "kernels_ms": list(phases), "interp_ms": interp_ms,
+                              "config": {"width": WIDTH, "height": HEIGHT}, "plan": [n_ctu, n_gen, n_jobs]}))
+        sess.close()
+        return
+    # ---- end to end through the C ABI with host buffers
+    h2d = WIDTH * HEIGHT * (1 + NREFS)
+    d2h = len(pus) * xg.RESULT_DTYPE.itemsize
+    out = np.zeros(len(pus), xg.RESULT_DTYPE)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        sess.set_picture(-1, cur)
+        for j, r in enumerate(refs):
+            sess.set_picture(j, r)
+        sess.run(prm)
+        out = sess.results()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = evals * world * args.steps / e2e_s
+    same = bool(np.array_equal(out, res))
+
+    # ---- per-call drop-in (one SAD per call, host buffers)
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 256, (64, 64), dtype=np.uint8)
+    b = rng.integers(0, 256, (64, 64), dtype=np.uint8)
+    f = xg.pixel_fn("sad", 2)
+    for _ in range(50):
+        f(xg.ptr(a), 64, xg.ptr(b), 64)
+    n_calls = 2000
+    t0 = time.perf_counter()
+    for _ in range(n_calls):
+        f(xg.ptr(a), 64, xg.ptr(b), 64)
+    per_call = n_calls / (time.perf_counter() - t0)
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel (shared-window CTU search): the
+    # algorithmic work is 4096 absolute differences (one 64x64 CTU) per
+    # (CTU, reference, displacement); the SM peak is 152 SMs x 64 lanes/clk
+    # of VABSDIFF4 (4 pixels each, half the INT32 issue rate) x max SM clock.
+    ctu_px = n_jobs * n_pos * 4096
+    ctu_ms = phases[1]
+    achieved = ctu_px / (ctu_ms / 1e3) / 1e12
+    peak = 152 * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    # interpolation (HBM-bound): 15 planes written with their margin + the source read, per reference
+    plane_bytes = (WIDTH + 160) * (HEIGHT + 160)
+    interp_bytes = NREFS * (15 * plane_bytes + WIDTH * HEIGHT)
+    interp_gbs = interp_bytes / (interp_ms / 1e3) / 1e9
+
+    cpu_e, cpu_s, cpu_n = cpu_sample_search(pus, cur, refs, (RANGE, prm.lambda_factor, 1, 2, 0, 0),
+                                            args.cpu_fraction, 7, os.cpu_count() or 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "me_1080p_2ref_fs64_qpel_satd", "width": WIDTH, "height": HEIGHT, "refs": NREFS,
+                   "search_range": RANGE, "qp": QP, "pus_per_picture": int(len(pus)),
+                   "evals_per_step": evals, "l2": "flushed between steps (512 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "results_equal_device_run": same},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "int", "kernel": "fs_ctu_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "Tpx-absdiff/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "152 SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % peak_src,
+                     "work_per_launch": "%d CTU-ref jobs x %d displacements x 4096 px" % (n_jobs, n_pos),
+                     "kernel_ms": ctu_ms},
+        "kernels_ms": {"candidates": phases[0], "ctu_search": phases[1], "per_pu_search": phases[2],
+                       "subpel_refine": phases[3], "interpolation_2refs": interp_ms},
+        "interpolation_roofline": {"bound": "hbm", "achieved": interp_gbs, "peak": peaks.get("hbm_gbs"),
+                                   "unit": "GB/s", "frac": interp_gbs / peaks.get("hbm_gbs", 6800.0)},
+        "plan": {"ctu_pus": n_ctu, "per_pu_pus": n_gen, "ctu_jobs": n_jobs},
+        "per_call": {"value": per_call, "unit": UNIT, "what": "xavs2gpu_pixel_sad_16x16 with host buffers"},
+        "cpu_baseline": {"value": cpu_e / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": "random %.2f%% (%d) of the picture's PU searches, oracle C port, OpenMP"
+                                   % (100 * args.cpu_fraction, cpu_n)},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    sess.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-fraction", type=float, default=1.0 / 64)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

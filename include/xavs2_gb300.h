@@ -350,6 +350,12 @@ XAVS2GPU_API void *xavs2gpu_me_stream(xavs2gpu_me_session_t *s);
 /* How the last xavs2gpu_me_set_pus split the list: PUs searched by the
  * shared-window CTU kernel and by the per-PU kernel. */
 XAVS2GPU_API void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus, int *n_generic_pus, int *n_ctu_jobs);
+/* Phase timing: when enabled, xavs2gpu_me_run records CUDA events on the
+ * session stream around its phases; xavs2gpu_me_phase_ms waits and returns
+ * the last run's durations in ms: [0] candidates, [1] shared-window CTU
+ * search, [2] per-PU search, [3] sub-pel refinement. */
+XAVS2GPU_API void xavs2gpu_me_set_profiling(xavs2gpu_me_session_t *s, int enable);
+XAVS2GPU_API int xavs2gpu_me_phase_ms(xavs2gpu_me_session_t *s, float ms[4]);
 
 #ifdef __cplusplus
 }

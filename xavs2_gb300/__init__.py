@@ -105,6 +105,8 @@ _SIGS = {
     "xavs2gpu_me_stream": (_P, [_P]),
     "xavs2gpu_me_plan_stats": (None, [_P, _P, _P, _P]),
     "xavs2gpu_me_get_plane": (_I, [_P, _I, _I, _P, _S]),
+    "xavs2gpu_me_set_profiling": (None, [_P, _I]),
+    "xavs2gpu_me_phase_ms": (_I, [_P, _P]),
 }
 
 _PIXEL_CMP = ["sad", "satd", "sa8d", "ssd"]
@@ -236,6 +238,14 @@ class MeSession:
 
     def stream(self):
         return self.lib.xavs2gpu_me_stream(self.h)
+
+    def set_profiling(self, on=True):
+        self.lib.xavs2gpu_me_set_profiling(self.h, 1 if on else 0)
+
+    def phase_ms(self):
+        out = (ctypes.c_float * 4)()
+        self._check(self.lib.xavs2gpu_me_phase_ms(self.h, out), "phase_ms")
+        return list(out)
 
     def plan_stats(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -295,6 +295,8 @@ struct MeSessionImpl {
     int plan_R = -1;               // search range the plan was built for (-1: stale)
     int n_ctu_pus = 0;
     std::vector<xavs2gpu_pu_t> h_pus;
+    bool profiling = false;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
     uint8_t *plane(int idx) { return d_planes + (size_t)idx * plane_bytes + (size_t)kPad * stride + kPad; }
 };
@@ -370,6 +372,8 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     cudaFreeHost(m.h_stage); cudaFree(m.d_upload);
     cudaFree(m.d_pus); cudaFree(m.d_res); cudaFreeHost(m.h_res); cudaFree(m.d_keys);
     cudaFree(m.d_state); cudaFree(m.d_generic);
+    for (auto &e : m.ev)
+        if (e) cudaEventDestroy(e);
     if (m.st) cudaStreamDestroy(m.st);
     delete s;
 }
@@ -472,21 +476,45 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     Geometry g{m.W, m.H, m.stride};
     const int R = prm->search_range, lam = prm->lambda_factor;
     ensure_plan(m, R);
+    if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[0], m.st));
     me_init_kernel<<<(m.n * 32 + 127) / 128, 128, 0, m.st>>>(m.d_pus, m.n, m.plane(0), m.d_ref0, g, lam, m.d_state,
                                                              m.d_keys);
     count_launch();
+    if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[1], m.st));
     ctu_plan_run(m.plan, *prm, m.plane(0), m.d_ref0, g, m.d_state, m.d_keys, m.st);
+    if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
     if (m.n_generic) {
         int grid = m.n_generic < 152 * 8 ? m.n_generic : 152 * 8;
         fs_generic_kernel<<<grid, 256, 0, m.st>>>(m.d_generic, m.n_generic, m.d_pus, m.d_state, m.plane(0), m.d_ref0,
                                                   g, R, lam, m.d_keys);
         count_launch();
     }
+    if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
     refine_kernel<<<(m.n * 32 + 127) / 128, 128, 0, m.st>>>(m.d_pus, m.n, m.d_state, m.d_keys, m.plane(0),
                                                             (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm,
                                                             m.d_res);
     count_launch();
+    if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[4], m.st));
     XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+extern "C" void xavs2gpu_me_set_profiling(xavs2gpu_me_session_t *s, int enable)
+{
+    if (!s) return;
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaSetDevice(m.device));
+    if (enable && !m.ev[0])
+        for (auto &e : m.ev) XG_CUDA(cudaEventCreate(&e));
+    m.profiling = enable != 0;
+}
+
+extern "C" int xavs2gpu_me_phase_ms(xavs2gpu_me_session_t *s, float ms[4])
+{
+    if (!s || !s->impl.profiling) return XAVS2GPU_ERR_ARG;
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaEventSynchronize(m.ev[4]));
+    for (int i = 0; i < 4; i++) XG_CUDA(cudaEventElapsedTime(&ms[i], m.ev[i], m.ev[i + 1]));
     return XAVS2GPU_OK;
 }
 
