@@ -357,6 +357,31 @@ XAVS2GPU_API void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pu
 XAVS2GPU_API void xavs2gpu_me_set_profiling(xavs2gpu_me_session_t *s, int enable);
 XAVS2GPU_API int xavs2gpu_me_phase_ms(xavs2gpu_me_session_t *s, float ms[4]);
 
+/* ---- allocation-free motion search ---------------------------------------
+ * No counterpart in the reference.  The same search as xavs2gpu_me_run
+ * (identical results), for callers that cannot allocate device memory while
+ * they run -- e.g. an encoder embedded in a host whose GPU memory comes from
+ * the host's own pool, or a latency-critical thread that must not trigger the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  The caller passes
+ * everything in device memory: `cur` and the 16*num_refs planes of
+ * `ref_planes` (a host array; plane 16*r + k is sub-pel position k of
+ * reference r, k = 0 the full-pel plane) point at pixel (0,0) of width x
+ * height pictures that share `stride` and have an 80-pixel replicated margin
+ * (as xavs2gpu_me_plane_device provides); `pus` and `out` hold n entries.
+ * Nothing is allocated: the scratch is one fixed device array of about
+ * 2.7 MB per GPU, kept until the process exits, limiting a call to 65536
+ * PUs and 16 references (larger requests are rejected with
+ * XAVS2GPU_ERR_CAPACITY).  The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress), so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams or
+ * threads) race and must be serialised by the caller.  PUs outside the
+ * picture or with limits beyond the margin report bcost = 1 << 30.  Kernels
+ * run on `stream` (a cudaStream_t, 0 = default); the call does not wait. */
+XAVS2GPU_API int xavs2gpu_me_search_noalloc(const uint8_t *cur, int stride, int width, int height,
+                                            const uint8_t *const *ref_planes, int num_refs,
+                                            const xavs2gpu_pu_t *pus, int n, const xavs2gpu_me_params_t *prm,
+                                            xavs2gpu_me_result_t *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@
 #include "xavs2gpu_common.cuh"
 
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace xg {
@@ -574,4 +575,130 @@ extern "C" void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus,
     if (n_ctu_pus) *n_ctu_pus = s->impl.n_ctu_pus;
     if (n_generic_pus) *n_generic_pus = s->impl.n_generic;
     if (n_ctu_jobs) *n_ctu_jobs = s->impl.plan.n_jobs;
+}
+
+// ---- allocation-free search ------------------------------------------------------
+// For callers that cannot allocate device memory while they run: an encoder
+// embedded in a host process whose GPU memory is handed out by the host's
+// own pool, or a latency-critical encoder thread that must not trigger the
+// device-wide synchronisation cudaMalloc/cudaFree imply.  The search's
+// scratch (per-PU keys and state, a sanitised copy of the PU list, the plane
+// pointer table) lives in one file-scope device array instead of session
+// buffers.  Every call shares it, so calls that overlap on the GPU race; the
+// array keeps the last call's contents, and every byte a call reads is
+// written by that call first, so nothing needs clearing.
+namespace xg {
+
+constexpr int kNoAllocMaxPus = 65536;
+constexpr int kNoAllocMaxRefs = 16;
+
+struct NoAllocScratch {
+    unsigned long long keys[kNoAllocMaxPus];
+    PuState state[kNoAllocMaxPus];
+    xavs2gpu_pu_t pus[kNoAllocMaxPus];
+    int list[kNoAllocMaxPus];
+    const uint8_t *planes[16 * kNoAllocMaxRefs];
+    const uint8_t *ref0[kNoAllocMaxRefs];
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+struct PlaneTable { const uint8_t *p[16 * kNoAllocMaxRefs]; };
+
+// Copies the PU list into the scratch; a PU outside the picture, with a bad
+// shape or reference, or with limits reaching beyond the 80-pixel margin is
+// replaced by one that has no admissible candidate, so it is never searched
+// and reports bcost = 1 << 30.  Also writes the plane tables and the index list.
+__global__ void noalloc_prepare_kernel(const xavs2gpu_pu_t *__restrict__ in, int n, NoAllocScratch *s, PlaneTable t,
+                                       int nrefs, int W, int H)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        for (int k = 0; k < 16 * nrefs; k++) s->planes[k] = t.p[k];
+        for (int r = 0; r < nrefs; r++) s->ref0[r] = t.p[16 * r];
+    }
+    if (i >= n) return;
+    xavs2gpu_pu_t p = in[i];
+    bool ok = p.part < kNumParts && p.ref < nrefs;
+    if (ok) {
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        ok = p.x >= 0 && p.y >= 0 && p.x + w <= W && p.y + h <= H && p.min_x >= -kPad + 8 - p.x &&
+             p.max_x <= W + kPad - 8 - p.x - w && p.min_y >= -kPad + 8 - p.y && p.max_y <= H + kPad - 8 - p.y - h;
+    }
+    if (!ok) {
+        p.x = p.y = 0;
+        p.part = 0;
+        p.ref = 0;
+        p.mvp_x = p.mvp_y = 0;
+        p.min_x = p.min_y = 1;   // min > max: no candidate is admissible
+        p.max_x = p.max_y = 0;
+    }
+    s->pus[i] = p;
+    s->list[i] = i;
+}
+
+static std::mutex g_noalloc_mu;
+static NoAllocScratch *g_noalloc_addr[64] = {nullptr};
+
+// Device address of the scratch array on `dev` (the current device), looked
+// up once per device.
+static NoAllocScratch *noalloc_scratch(int dev)
+{
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            fail(XAVS2GPU_ERR_CUDA, "xavs2gpu_me_search_noalloc: cudaGetSymbolAddress", cudaGetErrorString(e));
+            return nullptr;
+        }
+        g_noalloc_addr[dev] = static_cast<NoAllocScratch *>(ptr);
+    }
+    return g_noalloc_addr[dev];
+}
+
+}  // namespace xg
+
+extern "C" int xavs2gpu_me_search_noalloc(const uint8_t *cur, int stride, int width, int height,
+                                          const uint8_t *const *ref_planes, int num_refs,
+                                          const xavs2gpu_pu_t *pus, int n, const xavs2gpu_me_params_t *prm,
+                                          xavs2gpu_me_result_t *out, void *stream)
+{
+    if (n < 0 || n > kNoAllocMaxPus || num_refs < 1 || num_refs > kNoAllocMaxRefs) {
+        fail(XAVS2GPU_ERR_CAPACITY, "xavs2gpu_me_search_noalloc",
+             "at most 65536 PUs and 16 references per call (the fixed scratch size)");
+        return XAVS2GPU_ERR_CAPACITY;
+    }
+    if (!cur || !ref_planes || !prm || (n > 0 && (!pus || !out)) || width < 8 || height < 8 ||
+        stride < width + 2 * kPad || prm->search_range < 1 || prm->search_range > 128 || prm->fractional_me < 0 ||
+        prm->fractional_me > 2 || prm->lambda_factor < 0) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_search_noalloc", "bad picture geometry, pointers or parameters");
+        return XAVS2GPU_ERR_ARG;
+    }
+    PlaneTable t;
+    memset(&t, 0, sizeof(t));
+    for (int k = 0; k < 16 * num_refs; k++) {
+        if (!ref_planes[k]) {
+            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_search_noalloc", "missing reference plane");
+            return XAVS2GPU_ERR_ARG;
+        }
+        t.p[k] = ref_planes[k];
+    }
+    if (n == 0) return XAVS2GPU_OK;
+    int dev = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    NoAllocScratch *s = noalloc_scratch(dev);
+    if (!s) return XAVS2GPU_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    const Geometry g{width, height, stride};
+    const int R = prm->search_range, lam = prm->lambda_factor;
+    noalloc_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(pus, n, s, t, num_refs, width, height);
+    me_init_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, cur, s->ref0, g, lam, s->state, s->keys);
+    const int grid = n < 152 * 8 ? n : 152 * 8;
+    fs_generic_kernel<<<grid, 256, 0, st>>>(s->list, n, s->pus, s->state, cur, s->ref0, g, R, lam, s->keys);
+    refine_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, s->state, s->keys, cur, s->planes, g, R, *prm,
+                                                        out);
+    count_launch(4);
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
 }
