@@ -141,6 +141,14 @@ __device__ __forceinline__ uint32_t addmin(uint32_t a, uint32_t b, uint32_t c)
     return __viaddmin_u32(a, b, c);   // min(a + b, c)
 }
 
+// Window row layout: rows are ww bytes apart (ww a multiple of 128, i.e. each
+// row starts on bank 0) and row i is shifted right by swz(i) words.  In one
+// shared load the 32 lanes read rows 8q + t (q = 2*ry + half, t common) at
+// word 4*rx + k + t'; swz maps the eight q to {0,1,2,3,16,17,18,19}, so with
+// the 4*rx offsets the lanes hit 32 distinct banks.
+__host__ __device__ __forceinline__ int swz(int row) { return ((row >> 3) & 3) + 16 * ((row >> 5) & 1); }
+constexpr int kSwzMax = 19;   // words
+
 // slot of small key k (0..24) of a lane
 __device__ __forceinline__ int small_slot(int rx, int ry, int half, int k)
 {
@@ -207,11 +215,12 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
     // reference window: rows y0+dy0 .., columns x0-R .., clamped into the plane
     const uint8_t *ref = refs[job.ref];
     const int wx0 = job.x0 - R, wy0 = job.y0 + dy0;
-    for (int e = tid; e < wrows * ww; e += kCtuThreads) {
-        const int r = e / ww, c = e - r * ww;
+    const int rowlen = ww - 4 * kSwzMax - 4;   // bytes of a row that are filled
+    for (int e = tid; e < wrows * rowlen; e += kCtuThreads) {
+        const int r = e / rowlen, c = e - r * rowlen;
         const int y = min(max(wy0 + r, -kPad), g.H + kPad - 1);
         const int x = min(max(wx0 + c, -kPad), g.W + kPad - 1);
-        win[e] = ref[(ptrdiff_t)y * g.stride + x];
+        win[r * ww + 4 * swz(r) + c] = ref[(ptrdiff_t)y * g.stride + x];
     }
     __syncthreads();
 
@@ -256,7 +265,7 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
         const int row = warp * kDyWarp + rr;
         const int dy = dy0 + row;
         if (dy >= R) break;
-        const uint8_t *wbase = win + (size_t)(16 * ry + 8 * half + row) * ww + 16 * rx;
+        const int wrow0 = 16 * ry + 8 * half + row;
         const uint32_t *mrow = mvk + row * nd;
         uint32_t rowl[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
         bool brow[2] = {true, true};
@@ -277,7 +286,8 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
                     for (int c = 0; c < 4; c++) s[o][br][c] = 0;
 #pragma unroll
             for (int r = 0; r < 8; r++) {
-                const uint32_t *wp = reinterpret_cast<const uint32_t *>(wbase + (size_t)r * ww + j0);
+                const int wr = wrow0 + r;
+                const uint32_t *wp = reinterpret_cast<const uint32_t *>(win + wr * ww + 4 * swz(wr) + 16 * rx + j0);
                 uint32_t w5[5];
 #pragma unroll
                 for (int k = 0; k < 5; k++) w5[k] = wp[k];
@@ -504,9 +514,11 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
     }
 }
 
+// ww: row pitch of the window (bytes), a multiple of 128 that holds the
+// 64 + 2R + 8 bytes a row needs after its swizzle shift.
 static inline size_t ctu_smem_bytes(int R, int &ww)
 {
-    ww = (int)align_up((size_t)64 + 2 * R + 8, 16);
+    ww = (int)align_up((size_t)64 + 2 * R + 8 + 4 * kSwzMax + 4, 128);
     return sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
 }
 

@@ -412,6 +412,274 @@ __global__ void __launch_bounds__(32 * kRefineWarps) refine_grouped_kernel(
     }
 }
 
+// ---- refinement v3: one thread per search (PUs up to 256 pixels) ---------------
+// The thread runs the reference's sequential loop itself: the positions of a
+// step are fixed by the centre, so their costs are accumulated unit by unit
+// (the current block's unit is loaded once and compared with every
+// position), then the first strictly smaller cost wins in spiral order.
+// Bytes p[0..n) (n = 4 or 8) of an arbitrarily aligned row as ints, from
+// aligned 32-bit loads (the word after the row is read too; every plane has
+// an 80-pixel margin, so it is in bounds).
+template <int N>
+__device__ __forceinline__ void load_row(const uint8_t *p, int (&v)[8])
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    const uint32_t sh = (uint32_t)(a & 3) * 8;
+    const uint32_t w0 = w[0], w1 = w[1];
+    const uint32_t lo = __funnelshift_r(w0, w1, sh);
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = (int)__byte_perm(lo, 0, 0x4440 + k);
+    if (N == 8) {
+        const uint32_t hi = __funnelshift_r(w1, w[2], sh);
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[4 + k] = (int)__byte_perm(hi, 0, 0x4440 + k);
+    }
+}
+
+// SATD (one rounding per unit, pixel.c:321, 347) or SAD of one 4x4 (U4) or
+// 8x4 unit; `c` holds the current block's unit.
+template <bool U4>
+__device__ __forceinline__ int unit_cost_pre(bool had, const int (&c)[4][8], const uint8_t *r, int stride)
+{
+    constexpr int UW = U4 ? 4 : 8;
+    int d[4][8];
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        int v[8];
+        load_row<UW>(r + y * stride, v);
+#pragma unroll
+        for (int x = 0; x < UW; x++) d[y][x] = c[y][x] - v[x];
+    }
+    int s = 0;
+    if (!had) {
+#pragma unroll
+        for (int y = 0; y < 4; y++)
+#pragma unroll
+            for (int x = 0; x < UW; x++) s += iabs_d(d[y][x]);
+        return s;
+    }
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        fwht4_d(d[y][0], d[y][1], d[y][2], d[y][3]);
+        if (!U4) fwht4_d(d[y][4], d[y][5], d[y][6], d[y][7]);
+    }
+#pragma unroll
+    for (int x = 0; x < UW; x++) {
+        int a = d[0][x], b = d[1][x], e = d[2][x], f = d[3][x];
+        fwht4_d(a, b, e, f);
+        s += iabs_d(a) + iabs_d(b) + iabs_d(e) + iabs_d(f);
+    }
+    return s >> 1;
+}
+
+template <bool U4>
+__device__ __forceinline__ void load_unit(const uint8_t *o, int stride, int (&c)[4][8])
+{
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        int v[8];
+        load_row<U4 ? 4 : 8>(o + y * stride, v);
+#pragma unroll
+        for (int x = 0; x < 8; x++) c[y][x] = v[x];
+    }
+}
+
+// Accumulates the costs of up to 9 positions over all units of the PU.
+template <bool U4>
+__device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, const uint8_t *o,
+                                                    const uint8_t *const *planes, int stride, int px, int py,
+                                                    const int (&mxs)[9], const int (&mys)[9], int npos,
+                                                    int (&acc)[9])
+{
+    constexpr int UW = U4 ? 4 : 8;
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[k] = 0;
+    for (int u = 0; u < nu; u++) {
+        const int uy = u / nux, ux = u - uy * nux;
+        int c[4][8];
+        load_unit<U4>(o + (ptrdiff_t)uy * 4 * stride + ux * UW, stride, c);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            if (k < npos) {
+                const int mx = mxs[k], my = mys[k];
+                const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] +
+                                   (ptrdiff_t)(py + uy * 4 + (my >> 2)) * stride + px + ux * UW + (mx >> 2);
+                acc[k] += unit_cost_pre<U4>(had, c, r, stride);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) refine_thread_kernel(const int *__restrict__ list, int n,
+                                                            const xavs2gpu_pu_t *__restrict__ pus,
+                                                            const PuState *__restrict__ state,
+                                                            const unsigned long long *__restrict__ keys,
+                                                            const uint8_t *__restrict__ cur,
+                                                            const uint8_t *const *ref_planes, Geometry g, int R,
+                                                            xavs2gpu_me_params_t prm,
+                                                            xavs2gpu_me_result_t *__restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = list[t];
+    const xavs2gpu_pu_t p = pus[i];
+    const PuState st = state[i];
+    const unsigned long long key = keys[i];
+    xavs2gpu_me_result_t res;
+    if (!st.valid || key == kNoKey) {
+        res.bmv_x = res.bmv_y = res.imv_x = res.imv_y = 0;
+        res.bcost = res.icost = 1 << 30;
+        res.mvcost = 0;
+        out[i] = res;
+        return;
+    }
+    const int icost = (int)(key >> 32);
+    const unsigned order_ = (unsigned)(key & 0xffffffffu);
+    int bmx, bmy;
+    if (order_ < 2) { bmx = st.cand[order_][0]; bmy = st.cand[order_][1]; }
+    else {
+        const int q = (int)order_ - 2;
+        bmx = st.cx + q % (2 * R) - R;
+        bmy = st.cy + q / (2 * R) - R;
+    }
+    res.imv_x = (int16_t)bmx; res.imv_y = (int16_t)bmy; res.icost = icost;
+    const int lam = prm.lambda_factor, pmx = p.mvp_x, pmy = p.mvp_y;
+    int bx = bmx * 4, by = bmy * 4, best = icost;
+    if (prm.fractional_me) {
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        const bool had = prm.use_hadamard != 0;
+        const bool u4 = had ? satd_unit4(w, h) : (w == 4 || w == 12);
+        const int nux = w / (u4 ? 4 : 8), nu = nux * (h >> 2);
+        const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
+        const uint8_t *const *planes = ref_planes + 16 * p.ref;
+        const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
+        const int ctr_x = (pmx >> 1) << 1, ctr_y = (pmy >> 1) << 1;
+        for (int stage = 0; stage < (prm.fractional_me > 1 ? 2 : 1); stage++) {
+            const int cx = bx, cy = by;
+            int mxs[9], mys[9], npos = 0;
+#pragma unroll
+            for (int k = 0; k < 9; k++) { mxs[k] = cx; mys[k] = cy; }
+            if (stage == 0 && had) npos = 1;
+#pragma unroll
+            for (int pos = 1; pos < 9; pos++) {
+                if ((pos - 1) % step) continue;
+                const int sx = c_spiral[pat][pos][0], sy = c_spiral[pat][pos][1];
+                int mx, my;
+                if (stage == 0) {
+                    mx = cx + 2 * sx; my = cy + 2 * sy;
+                } else if (prm.enable_pmvr) {
+                    // pmvr_adapt_mv (me.c:412-424), TH_PMVR = 2
+                    if (abs(cx - ctr_x) > 2 || abs(cy - ctr_y) > 2) {
+                        mx = cx + 2 * sx; my = cy + 2 * sy;
+                        if (abs(mx - ctr_x) <= 2 && abs(my - ctr_y) <= 2) continue;
+                    } else {
+                        mx = cx + sx; my = cy + sy;
+                        if (abs(mx - ctr_x) > 2 || abs(my - ctr_y) > 2) continue;
+                    }
+                } else {
+                    mx = cx + sx; my = cy + sy;
+                }
+#pragma unroll
+                for (int k = 0; k < 9; k++)
+                    if (k == npos) { mxs[k] = mx; mys[k] = my; }
+                npos++;
+            }
+            int acc[9];
+            if (u4) refine_stage_thread<true>(had, nux, nu, o, planes, g.stride, p.x, p.y, mxs, mys, npos, acc);
+            else refine_stage_thread<false>(had, nux, nu, o, planes, g.stride, p.x, p.y, mxs, mys, npos, acc);
+            const int k0 = (stage == 0 && had) ? 1 : 0;
+            if (k0) best = acc[0] + mv_cost_hd(lam, cx, cy, pmx, pmy);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                if (k < k0 || k >= npos) continue;
+                const int c = acc[k] + mv_cost_hd(lam, mxs[k], mys[k], pmx, pmy);
+                if (c < best) { best = c; bx = mxs[k]; by = mys[k]; }
+            }
+        }
+    }
+    res.bmv_x = (int16_t)bx; res.bmv_y = (int16_t)by;
+    res.bcost = best;
+    res.mvcost = mv_cost_hd(lam, bx, by, pmx, pmy);
+    out[i] = res;
+}
+
+// One warp per search for the larger PUs, over a list.
+__global__ void __launch_bounds__(128) refine_warp_list_kernel(const int *__restrict__ list, int n,
+                                                               const xavs2gpu_pu_t *__restrict__ pus,
+                                                               const PuState *__restrict__ state,
+                                                               const unsigned long long *__restrict__ keys,
+                                                               const uint8_t *__restrict__ cur,
+                                                               const uint8_t *const *ref_planes, Geometry g, int R,
+                                                               xavs2gpu_me_params_t prm,
+                                                               xavs2gpu_me_result_t *__restrict__ out)
+{
+    const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wt >= n) return;
+    const int i = list[wt];
+    const xavs2gpu_pu_t p = pus[i];
+    const PuState st = state[i];
+    const unsigned long long key = keys[i];
+    xavs2gpu_me_result_t res;
+    if (!st.valid || key == kNoKey) {
+        res.bmv_x = res.bmv_y = res.imv_x = res.imv_y = 0;
+        res.bcost = res.icost = 1 << 30;
+        res.mvcost = 0;
+        if (lane == 0) out[i] = res;
+        return;
+    }
+    const int icost = (int)(key >> 32);
+    const unsigned order_ = (unsigned)(key & 0xffffffffu);
+    int bmx, bmy;
+    if (order_ < 2) { bmx = st.cand[order_][0]; bmy = st.cand[order_][1]; }
+    else {
+        const int q = (int)order_ - 2;
+        bmx = st.cx + q % (2 * R) - R;
+        bmy = st.cy + q / (2 * R) - R;
+    }
+    const int lam = prm.lambda_factor, pmx = p.mvp_x, pmy = p.mvp_y;
+    res.imv_x = (int16_t)bmx; res.imv_y = (int16_t)bmy; res.icost = icost;
+    int bx = bmx * 4, by = bmy * 4, best = icost;
+    if (prm.fractional_me) {
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        const bool had = prm.use_hadamard != 0;
+        const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
+        const uint8_t *const *planes = ref_planes + 16 * p.ref;
+        const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
+        int cx = bx, cy = by;
+        if (had) best = qpel_cost_warp(p, w, h, true, o, planes, g, cx, cy, lane) + mv_cost_hd(lam, cx, cy, pmx, pmy);
+        for (int pos = 1; pos < 9; pos += step) {
+            int mx = cx + 2 * c_spiral[pat][pos][0], my = cy + 2 * c_spiral[pat][pos][1];
+            int c = qpel_cost_warp(p, w, h, had, o, planes, g, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
+            if (c < best) { best = c; bx = mx; by = my; }
+        }
+        if (prm.fractional_me > 1) {
+            cx = bx; cy = by;
+            const int ctr_x = (pmx >> 1) << 1, ctr_y = (pmy >> 1) << 1;
+            for (int pos = 1; pos < 9; pos += step) {
+                int sx = c_spiral[pat][pos][0], sy = c_spiral[pat][pos][1], mx, my;
+                if (prm.enable_pmvr) {
+                    if (abs(cx - ctr_x) > 2 || abs(cy - ctr_y) > 2) {
+                        mx = cx + 2 * sx; my = cy + 2 * sy;
+                        if (abs(mx - ctr_x) <= 2 && abs(my - ctr_y) <= 2) continue;
+                    } else {
+                        mx = cx + sx; my = cy + sy;
+                        if (abs(mx - ctr_x) > 2 || abs(my - ctr_y) > 2) continue;
+                    }
+                } else {
+                    mx = cx + sx; my = cy + sy;
+                }
+                int c = qpel_cost_warp(p, w, h, had, o, planes, g, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
+                if (c < best) { best = c; bx = mx; by = my; }
+            }
+        }
+    }
+    res.bmv_x = (int16_t)bx; res.bmv_y = (int16_t)by;
+    res.bcost = best;
+    res.mvcost = mv_cost_hd(lam, bx, by, pmx, pmy);
+    if (lane == 0) out[i] = res;
+}
+
 }  // namespace xg
 
 #include "fs_ctu.cuh"
@@ -447,6 +715,8 @@ struct MeSessionImpl {
     int *d_order = nullptr;                 // PU indices sorted by shape
     RefineTask *d_tasks = nullptr;          // refinement warp tasks
     int n_tasks = 0;
+    int *d_small = nullptr, *d_large = nullptr;   // refinement lists: thread / warp per search
+    int n_small = 0, n_large = 0;
     bool profiling = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
@@ -511,6 +781,8 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     XG_CUDA(cudaMalloc((void **)&m.d_generic, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_order, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_tasks, sizeof(RefineTask) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_small, sizeof(int) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_large, sizeof(int) * max_pus));
     XG_CUDA(cudaStreamSynchronize(m.st));
     return s;
 }
@@ -526,6 +798,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     cudaFreeHost(m.h_stage); cudaFree(m.d_upload);
     cudaFree(m.d_pus); cudaFree(m.d_res); cudaFreeHost(m.h_res); cudaFree(m.d_keys);
     cudaFree(m.d_state); cudaFree(m.d_generic); cudaFree(m.d_order); cudaFree(m.d_tasks);
+    cudaFree(m.d_small); cudaFree(m.d_large);
     for (auto &e : m.ev)
         if (e) cudaEventDestroy(e);
     if (m.st) cudaStreamDestroy(m.st);
@@ -634,6 +907,15 @@ static void ensure_plan(MeSessionImpl &m, int R)
         }
     }
     m.n_tasks = (int)tasks.size();
+    std::vector<int> small, large;
+    for (int k = 0; k < m.n; k++) {
+        const int i = order[k];
+        (h_pu_w[m.h_pus[i].part] * h_pu_h[m.h_pus[i].part] <= 256 ? small : large).push_back(i);
+    }
+    m.n_small = (int)small.size();
+    m.n_large = (int)large.size();
+    if (m.n_small) XG_CUDA(cudaMemcpyAsync(m.d_small, small.data(), sizeof(int) * m.n_small, cudaMemcpyHostToDevice, m.st));
+    if (m.n_large) XG_CUDA(cudaMemcpyAsync(m.d_large, large.data(), sizeof(int) * m.n_large, cudaMemcpyHostToDevice, m.st));
     if (m.n) XG_CUDA(cudaMemcpyAsync(m.d_order, order.data(), sizeof(int) * m.n, cudaMemcpyHostToDevice, m.st));
     if (m.n_tasks)
         XG_CUDA(cudaMemcpyAsync(m.d_tasks, tasks.data(), sizeof(RefineTask) * m.n_tasks, cudaMemcpyHostToDevice, m.st));
@@ -668,10 +950,18 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
-    refine_grouped_kernel<<<(m.n_tasks + kRefineWarps - 1) / kRefineWarps, 32 * kRefineWarps, 0, m.st>>>(
-        m.d_tasks, m.n_tasks, m.d_order, m.d_pus, m.d_state, m.d_keys, m.plane(0),
-        (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm, m.d_res);
-    count_launch();
+    if (m.n_small) {
+        refine_thread_kernel<<<(m.n_small + 127) / 128, 128, 0, m.st>>>(
+            m.d_small, m.n_small, m.d_pus, m.d_state, m.d_keys, m.plane(0),
+            (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm, m.d_res);
+        count_launch();
+    }
+    if (m.n_large) {
+        refine_warp_list_kernel<<<(m.n_large * 32 + 127) / 128, 128, 0, m.st>>>(
+            m.d_large, m.n_large, m.d_pus, m.d_state, m.d_keys, m.plane(0),
+            (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm, m.d_res);
+        count_launch();
+    }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[4], m.st));
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
