@@ -187,8 +187,138 @@ __constant__ int8_t c_c64[32][3] = {
     {0, 1, 0}, {1, 0, -1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0},
     {1, 0, -1}, {0, 0, 0}, {0, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 
+// Per-lane constants of the warp layout.
+struct LaneRole {
+    int half, rx, ry;
+    int pr1, pr2, pr3, pr4, pr5;    // shuffle partners (see below)
+    int c32a[4], c32b[4], c64[3];   // coefficient sets of the 32-CU / 64-CU keys
+    int bx0, by0;                   // picture position of the half-region
+};
+
+// Folds the costs of one displacement into the lane's keys.  `raw` are the
+// lane's eight 4x4 SADs; `mks` = (mvc << 11) | (row << 8) | dx+R for the
+// small keys, `mkl` = (mvc << 8) | dx+R for the large ones.
 template <bool BORDER>
-__global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
+__device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (&raw)[2][4], uint32_t mks,
+                                                  uint32_t mkl, int dx, bool brow0, bool brow1, const Geometry &g,
+                                                  uint32_t (&ks)[25], uint32_t (&rowl)[3])
+{
+    const int half = LR.half;
+    if (BORDER) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int xb = LR.bx0 + 4 * c + dx;
+            const bool colok = xb >= -kLimitMargin && xb + 4 <= g.W + kLimitMargin;
+            if (!(colok && brow0)) raw[0][c] = kPoisonLarge;
+            if (!(colok && brow1)) raw[1][c] = kPoisonLarge;
+        }
+    }
+    // small-key domain: SAD << 11 (poison clamped for the small PUs)
+    uint32_t t[2][4];
+#pragma unroll
+    for (int br = 0; br < 2; br++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) t[br][c] = (BORDER ? min(raw[br][c], kPoisonSmall) : raw[br][c]) << 11;
+    // 8x8 CUs of this half: left (cols 0,1) and right (cols 2,3)
+    uint32_t qv[2], at[2], ab[2], vl[2], vr[2];
+#pragma unroll
+    for (int sd = 0; sd < 2; sd++) {
+        const int c0 = 2 * sd;
+        at[sd] = t[0][c0] + t[0][c0 + 1];
+        ab[sd] = t[1][c0] + t[1][c0 + 1];
+        vl[sd] = t[0][c0] + t[1][c0];
+        vr[sd] = t[0][c0 + 1] + t[1][c0 + 1];
+        qv[sd] = at[sd] + ab[sd];
+        const int kb = 9 * sd;
+        ks[kb + 0] = addmin(qv[sd], mks, ks[kb + 0]);
+        ks[kb + 1] = addmin(at[sd], mks, ks[kb + 1]);
+        ks[kb + 2] = addmin(ab[sd], mks, ks[kb + 2]);
+        ks[kb + 3] = addmin(vl[sd], mks, ks[kb + 3]);
+        ks[kb + 4] = addmin(vr[sd], mks, ks[kb + 4]);
+        ks[kb + 5] = addmin(t[0][c0], mks, ks[kb + 5]);
+        ks[kb + 6] = addmin(t[0][c0 + 1], mks, ks[kb + 6]);
+        ks[kb + 7] = addmin(t[1][c0], mks, ks[kb + 7]);
+        ks[kb + 8] = addmin(t[1][c0 + 1], mks, ks[kb + 8]);
+    }
+    // 16x16 CU: own half (Fh, Lh, strips) + partner half
+    const uint32_t Fh = qv[0] + qv[1];
+    const uint32_t Lh = qv[0];
+    const uint32_t rr_ = half ? ab[0] + ab[1] : at[0] + at[1];   // own outer 16x4 strip
+    const uint32_t c0h = vl[0], c3h = vr[1];
+    const uint32_t Fh_o = __shfl_xor_sync(0xffffffffu, Fh, 1);
+    const uint32_t Lh_o = __shfl_xor_sync(0xffffffffu, Lh, 1);
+    const uint32_t xs = half ? c0h : c3h;
+    const uint32_t xs_o = __shfl_xor_sync(0xffffffffu, xs, 1);
+    const uint32_t F = Fh + Fh_o, L = Lh + Lh_o;
+    const uint32_t cc = (half ? c3h : c0h) + xs_o;          // col 3 (half 1) / col 0 (half 0)
+    ks[18] = addmin(F - (half ? L : 0u), mks, ks[18]);     // 16x16 | 8x16 right
+    ks[19] = addmin(Fh, mks, ks[19]);                      // 16x8 top | bottom
+    ks[20] = addmin(half ? Fh : L, mks, ks[20]);           // 8x16 left | (dup)
+    ks[21] = addmin(rr_, mks, ks[21]);                     // 16x4 y0 | y12
+    ks[22] = addmin(F - rr_, mks, ks[22]);                 // 16x12 y4 | y0
+    ks[23] = addmin(cc, mks, ks[23]);                      // 4x16 x0 | x12
+    ks[24] = addmin(F - cc, mks, ks[24]);                  // 12x16 x4 | x0
+    // large PUs in the raw domain
+    uint32_t Fr, Tr, Lr;
+    if (BORDER) {
+        uint32_t fh = 0, lh = 0;
+#pragma unroll
+        for (int br = 0; br < 2; br++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                fh += raw[br][c];
+                if (c < 2) lh += raw[br][c];
+            }
+        const uint32_t fh_o = __shfl_xor_sync(0xffffffffu, fh, 1);
+        const uint32_t lh_o = __shfl_xor_sync(0xffffffffu, lh, 1);
+        Fr = fh + fh_o;
+        Tr = half ? fh_o : fh;
+        Lr = lh + lh_o;
+    } else {
+        Fr = F >> 11;
+        Tr = (half ? Fh_o : Fh) >> 11;
+        Lr = L >> 11;
+    }
+    // 32x32 CUs
+    const uint32_t a1 = half ? Lr : Tr;
+    const uint32_t F_p = __shfl_xor_sync(0xffffffffu, Fr, LR.pr1);
+    const uint32_t a_p = __shfl_xor_sync(0xffffffffu, a1, LR.pr1);
+    const uint32_t X1 = Fr + F_p, X2 = a1 + a_p;           // FH, TH  |  FV, LV
+    const uint32_t X3 = __shfl_xor_sync(0xffffffffu, X1, LR.pr2);
+    const uint32_t X4 = __shfl_xor_sync(0xffffffffu, X2, LR.pr2);
+    const int va = LR.c32a[0] * (int)X1 + LR.c32a[1] * (int)X2 + LR.c32a[2] * (int)X3 + LR.c32a[3] * (int)X4;
+    const int vb = LR.c32b[0] * (int)X1 + LR.c32b[1] * (int)X2 + LR.c32b[2] * (int)X3 + LR.c32b[3] * (int)X4;
+    // 64x64 CU
+    const uint32_t RS = X1 + __shfl_xor_sync(0xffffffffu, X1, LR.pr3);     // row | column sums
+    const uint32_t P = RS + __shfl_xor_sync(0xffffffffu, RS, LR.pr4);      // row | column pairs
+    const uint32_t TOT = P + __shfl_xor_sync(0xffffffffu, P, LR.pr5);
+    const int v64 = LR.c64[0] * (int)TOT + LR.c64[1] * (int)P + LR.c64[2] * (int)RS;
+    rowl[0] = min(rowl[0], (min((uint32_t)va, kCapLarge) << 8) + mkl);
+    rowl[1] = min(rowl[1], (min((uint32_t)vb, kCapLarge) << 8) + mkl);
+    rowl[2] = min(rowl[2], (min((uint32_t)v64, kCapLarge) << 8) + mkl);
+}
+
+// 4x4 SADs of the lane's half-region against window rows wrow0.. at byte
+// offset j (any alignment).
+__device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, int rx, int j, const uint32_t (&cw)[8][4],
+                                       uint32_t (&raw)[2][4])
+{
+    const int j0 = j & ~3, o = j & 3;
+#pragma unroll
+    for (int br = 0; br < 2; br++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) raw[br][c] = 0;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int wr = wrow0 + r;
+        const uint32_t *wp = reinterpret_cast<const uint32_t *>(win + wr * ww + 4 * swz(wr) + 16 * rx + j0);
+#pragma unroll
+        for (int c = 0; c < 4; c++) raw[r >> 2][c] = sad4_acc(cw[r][c], __funnelshift_r(wp[c], wp[c + 1], 8 * o), raw[r >> 2][c]);
+    }
+}
+
+template <bool BORDER>
+__global__ void __launch_bounds__(kCtuThreads, 4) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
                                                             const int32_t *__restrict__ slots,
                                                             const uint8_t *__restrict__ cur,
                                                             const uint8_t *const *refs, Geometry g, int R, int lambda,
@@ -224,7 +354,11 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
     }
     __syncthreads();
 
-    const int half = lane & 1, rx = (lane >> 1) & 3, ry = lane >> 3;
+    LaneRole L;
+    L.half = lane & 1;
+    L.rx = (lane >> 1) & 3;
+    L.ry = lane >> 3;
+    const int half = L.half, rx = L.rx, ry = L.ry;
     const int qx = rx & 1, qy = ry & 1;
     // current block: 8 rows x 16 pixels of this half-region
     uint32_t cw[8][4];
@@ -236,30 +370,62 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
             cw[r][0] = v.x; cw[r][1] = v.y; cw[r][2] = v.z; cw[r][3] = v.w;
         }
     }
-    // per-lane coefficient sets for the 32-CU and 64-CU keys
-    int c32a[4], c32b[4], c64[3];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        c32a[k] = c_c32[half][qx][qy][0][k];
-        c32b[k] = c_c32[half][qx][qy][1][k];
+        L.c32a[k] = c_c32[half][qx][qy][0][k];
+        L.c32b[k] = c_c32[half][qx][qy][1][k];
     }
 #pragma unroll
-    for (int k = 0; k < 3; k++) c64[k] = c_c64[lane][k];
+    for (int k = 0; k < 3; k++) L.c64[k] = c_c64[lane][k];
     const int m32a = c_m32[half][qx][qy][0], m32b = c_m32[half][qx][qy][1], m64 = c_m64[lane];
     // shuffle partners: region pairs along the axis this half works on
-    const int pr1 = half ? 8 : 2;     // 32-CU pair (vertical for half 1, horizontal for half 0)
-    const int pr2 = half ? 2 : 8;     // the other 32-CU row/column
-    const int pr3 = half ? 16 : 4;    // 64-CU row / column sums
-    const int pr4 = half ? 2 : 8;     // 64-CU pairs
-    const int pr5 = half ? 4 : 16;    // 64-CU total
+    L.pr1 = half ? 8 : 2;     // 32-CU pair (vertical for half 1, horizontal for half 0)
+    L.pr2 = half ? 2 : 8;     // the other 32-CU row/column
+    L.pr3 = half ? 16 : 4;    // 64-CU row / column sums
+    L.pr4 = half ? 2 : 8;     // 64-CU pairs
+    L.pr5 = half ? 4 : 16;    // 64-CU total
+    L.bx0 = job.x0 + 16 * rx;
+    L.by0 = job.y0 + 16 * ry + 8 * half;
+    const int32_t *smap = slots + (size_t)job.slot_base;
+    const int cu32 = (ry >> 1) * 2 + (rx >> 1);
+    const int lm[3] = {m32a, m32b, m64};
+
+    // The search candidate (0,0) is visited before the window (me.c:913-917):
+    // its cost enters with visit order 0, so it wins every tie.  The CTA whose
+    // rows contain dy = 0 evaluates it (warp 0).
+    if (warp == 0 && dy0 <= 0 && 0 < dy0 + kDyChunk) {
+        uint32_t ks0[25], rowl0[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+#pragma unroll
+        for (int k = 0; k < 25; k++) ks0[k] = 0xffffffffu;
+        uint32_t raw[2][4];
+        sad_at(win, ww, 16 * ry + 8 * half - dy0, rx, R, cw, raw);
+        const uint32_t mvc0 = (uint32_t)mv_cost_hd(lambda, 0, 0, job.mvp_x, job.mvp_y);
+        bool b0 = true, b1 = true;
+        if (BORDER) {
+            b0 = L.by0 >= -kLimitMargin && L.by0 + 4 <= g.H + kLimitMargin;
+            b1 = L.by0 + 4 >= -kLimitMargin && L.by0 + 8 <= g.H + kLimitMargin;
+        }
+        fold_displacement<BORDER>(L, raw, mvc0 << 11, mvc0 << 8, 0, b0, b1, g, ks0, rowl0);
+#pragma unroll
+        for (int k = 0; k < 25; k++) {
+            const uint32_t cost = ks0[k] >> 11;
+            if (cost >= kPoisonSmall) continue;
+            const int pu = smap[small_slot(rx, ry, half, k)];
+            if (pu >= 0) atomicMin(&keys[pu], (unsigned long long)cost << 32);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint32_t cost = rowl0[k] >> 8;
+            if (lm[k] < 0 || cost >= kCapLarge) continue;
+            const int pu = smap[k < 2 ? 784 + cu32 * 13 + lm[k] : 836 + lm[k]];
+            if (pu >= 0) atomicMin(&keys[pu], (unsigned long long)cost << 32);
+        }
+    }
 
     uint32_t ks[25];
     unsigned long long kl[3] = {~0ull, ~0ull, ~0ull};
 #pragma unroll
     for (int k = 0; k < 25; k++) ks[k] = 0xffffffffu;
-
-    // block geometry for the border variant
-    const int bx0 = job.x0 + 16 * rx, by0 = job.y0 + 16 * ry + 8 * half;
 
     for (int rr = 0; rr < kDyWarp; rr++) {
         const int row = warp * kDyWarp + rr;
@@ -268,13 +434,11 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
         const int wrow0 = 16 * ry + 8 * half + row;
         const uint32_t *mrow = mvk + row * nd;
         uint32_t rowl[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
-        bool brow[2] = {true, true};
+        bool brow0 = true, brow1 = true;
         if (BORDER) {
-#pragma unroll
-            for (int br = 0; br < 2; br++) {
-                const int yb = by0 + 4 * br + dy;
-                brow[br] = yb >= -kLimitMargin && yb + 4 <= g.H + kLimitMargin;
-            }
+            const int yb = L.by0 + dy;
+            brow0 = yb >= -kLimitMargin && yb + 4 <= g.H + kLimitMargin;
+            brow1 = yb + 4 >= -kLimitMargin && yb + 8 <= g.H + kLimitMargin;
         }
         for (int j0 = 0; j0 < nd; j0 += 4) {
             uint32_t s[4][2][4];
@@ -305,106 +469,7 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
                 const int dxr = j0 + o;
                 const uint32_t mks = mrow[dxr];
                 const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
-                uint32_t raw[2][4];
-#pragma unroll
-                for (int br = 0; br < 2; br++)
-#pragma unroll
-                    for (int c = 0; c < 4; c++) raw[br][c] = s[o][br][c];
-                if (BORDER) {
-                    const int dx = dxr - R;
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const int xb = bx0 + 4 * c + dx;
-                        const bool colok = xb >= -kLimitMargin && xb + 4 <= g.W + kLimitMargin;
-#pragma unroll
-                        for (int br = 0; br < 2; br++)
-                            if (!(colok && brow[br])) raw[br][c] = kPoisonLarge;
-                    }
-                }
-                // small-key domain: SAD << 11 (poison clamped for the small PUs)
-                uint32_t t[2][4];
-#pragma unroll
-                for (int br = 0; br < 2; br++)
-#pragma unroll
-                    for (int c = 0; c < 4; c++)
-                        t[br][c] = (BORDER ? min(raw[br][c], kPoisonSmall) : raw[br][c]) << 11;
-                // 8x8 CUs of this half: left (cols 0,1) and right (cols 2,3)
-                uint32_t qv[2], at[2], ab[2], vl[2], vr[2];
-#pragma unroll
-                for (int sd = 0; sd < 2; sd++) {
-                    const int c0 = 2 * sd;
-                    at[sd] = t[0][c0] + t[0][c0 + 1];
-                    ab[sd] = t[1][c0] + t[1][c0 + 1];
-                    vl[sd] = t[0][c0] + t[1][c0];
-                    vr[sd] = t[0][c0 + 1] + t[1][c0 + 1];
-                    qv[sd] = at[sd] + ab[sd];
-                    const int kb = 9 * sd;
-                    ks[kb + 0] = addmin(qv[sd], mks, ks[kb + 0]);
-                    ks[kb + 1] = addmin(at[sd], mks, ks[kb + 1]);
-                    ks[kb + 2] = addmin(ab[sd], mks, ks[kb + 2]);
-                    ks[kb + 3] = addmin(vl[sd], mks, ks[kb + 3]);
-                    ks[kb + 4] = addmin(vr[sd], mks, ks[kb + 4]);
-                    ks[kb + 5] = addmin(t[0][c0], mks, ks[kb + 5]);
-                    ks[kb + 6] = addmin(t[0][c0 + 1], mks, ks[kb + 6]);
-                    ks[kb + 7] = addmin(t[1][c0], mks, ks[kb + 7]);
-                    ks[kb + 8] = addmin(t[1][c0 + 1], mks, ks[kb + 8]);
-                }
-                // 16x16 CU: own half (Fh, Lh, strips) + partner half
-                const uint32_t Fh = qv[0] + qv[1];
-                const uint32_t Lh = qv[0];
-                const uint32_t rr_ = half ? ab[0] + ab[1] : at[0] + at[1];   // own outer 16x4 strip
-                const uint32_t c0h = vl[0], c3h = vr[1];
-                const uint32_t Fh_o = __shfl_xor_sync(0xffffffffu, Fh, 1);
-                const uint32_t Lh_o = __shfl_xor_sync(0xffffffffu, Lh, 1);
-                const uint32_t xs = half ? c0h : c3h;
-                const uint32_t xs_o = __shfl_xor_sync(0xffffffffu, xs, 1);
-                const uint32_t F = Fh + Fh_o, L = Lh + Lh_o;
-                const uint32_t cc = (half ? c3h : c0h) + xs_o;          // col 3 (half 1) / col 0 (half 0)
-                ks[18] = addmin(F - (half ? L : 0u), mks, ks[18]);     // 16x16 | 8x16 right
-                ks[19] = addmin(Fh, mks, ks[19]);                      // 16x8 top | bottom
-                ks[20] = addmin(half ? Fh : L, mks, ks[20]);           // 8x16 left | (dup)
-                ks[21] = addmin(rr_, mks, ks[21]);                     // 16x4 y0 | y12
-                ks[22] = addmin(F - rr_, mks, ks[22]);                 // 16x12 y4 | y0
-                ks[23] = addmin(cc, mks, ks[23]);                      // 4x16 x0 | x12
-                ks[24] = addmin(F - cc, mks, ks[24]);                  // 12x16 x4 | x0
-                // large PUs in the raw domain
-                uint32_t Fr, Tr, Lr;
-                if (BORDER) {
-                    uint32_t fh = 0, lh = 0;
-#pragma unroll
-                    for (int br = 0; br < 2; br++)
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            fh += raw[br][c];
-                            if (c < 2) lh += raw[br][c];
-                        }
-                    const uint32_t fh_o = __shfl_xor_sync(0xffffffffu, fh, 1);
-                    const uint32_t lh_o = __shfl_xor_sync(0xffffffffu, lh, 1);
-                    Fr = fh + fh_o;
-                    Tr = half ? fh_o : fh;
-                    Lr = lh + lh_o;
-                } else {
-                    Fr = F >> 11;
-                    Tr = (half ? Fh_o : Fh) >> 11;
-                    Lr = L >> 11;
-                }
-                // 32x32 CUs
-                const uint32_t a1 = half ? Lr : Tr;
-                const uint32_t F_p = __shfl_xor_sync(0xffffffffu, Fr, pr1);
-                const uint32_t a_p = __shfl_xor_sync(0xffffffffu, a1, pr1);
-                const uint32_t X1 = Fr + F_p, X2 = a1 + a_p;           // FH, TH  |  FV, LV
-                const uint32_t X3 = __shfl_xor_sync(0xffffffffu, X1, pr2);
-                const uint32_t X4 = __shfl_xor_sync(0xffffffffu, X2, pr2);
-                const int va = c32a[0] * (int)X1 + c32a[1] * (int)X2 + c32a[2] * (int)X3 + c32a[3] * (int)X4;
-                const int vb = c32b[0] * (int)X1 + c32b[1] * (int)X2 + c32b[2] * (int)X3 + c32b[3] * (int)X4;
-                // 64x64 CU
-                const uint32_t RS = X1 + __shfl_xor_sync(0xffffffffu, X1, pr3);     // row | column sums
-                const uint32_t P = RS + __shfl_xor_sync(0xffffffffu, RS, pr4);      // row | column pairs
-                const uint32_t TOT = P + __shfl_xor_sync(0xffffffffu, P, pr5);
-                const int v64 = c64[0] * (int)TOT + c64[1] * (int)P + c64[2] * (int)RS;
-                rowl[0] = min(rowl[0], (min((uint32_t)va, kCapLarge) << 8) + mkl);
-                rowl[1] = min(rowl[1], (min((uint32_t)vb, kCapLarge) << 8) + mkl);
-                rowl[2] = min(rowl[2], (min((uint32_t)v64, kCapLarge) << 8) + mkl);
+                fold_displacement<BORDER>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
             }
         }
         // fold this row's large-PU minima into 64-bit (cost, order) keys
@@ -418,7 +483,6 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
         }
     }
     // merge into the global keys
-    const int32_t *smap = slots + (size_t)job.slot_base;
     const int dyw = dy0 + warp * kDyWarp;
 #pragma unroll
     for (int k = 0; k < 25; k++) {
@@ -430,8 +494,6 @@ __global__ void __launch_bounds__(kCtuThreads) fs_ctu_kernel(const CtuJob *__res
         const int dy = dyw + (int)((key >> 8) & 7), dxr = (int)(key & 0xffu);
         atomicMin(&keys[pu], ((unsigned long long)cost << 32) | (unsigned)(2 + (dy + R) * nd + dxr));
     }
-    const int lm[3] = {m32a, m32b, m64};
-    const int cu32 = (ry >> 1) * 2 + (rx >> 1);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         if (lm[k] < 0 || kl[k] == ~0ull) continue;

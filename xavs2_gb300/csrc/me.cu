@@ -62,13 +62,11 @@ __device__ __forceinline__ bool in_box(const xavs2gpu_pu_t &p, int mx, int my)
 
 // ---- 1. candidates ----------------------------------------------------------------
 // One warp per PU.  keys[i] starts as the best candidate's (cost, order 0/1).
-__global__ void __launch_bounds__(128) me_init_kernel(const xavs2gpu_pu_t *__restrict__ pus, int n,
-                                                      const uint8_t *__restrict__ cur, const uint8_t *const *refs,
-                                                      Geometry g, int lambda, PuState *__restrict__ state,
-                                                      unsigned long long *__restrict__ keys)
+__device__ __forceinline__ void init_one(int i, int lane, const xavs2gpu_pu_t *__restrict__ pus,
+                                         const uint8_t *__restrict__ cur, const uint8_t *const *refs,
+                                         const Geometry &g, int lambda, PuState *__restrict__ state,
+                                         unsigned long long *__restrict__ keys)
 {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (i >= n) return;
     const xavs2gpu_pu_t p = pus[i];
     const int w = c_pu_w[p.part], h = c_pu_h[p.part];
     const uint8_t *ref = refs[p.ref];
@@ -102,6 +100,28 @@ __global__ void __launch_bounds__(128) me_init_kernel(const xavs2gpu_pu_t *__res
         state[i] = st;
         keys[i] = best;
     }
+}
+
+__global__ void __launch_bounds__(128) me_init_kernel(const xavs2gpu_pu_t *__restrict__ pus, int n,
+                                                      const uint8_t *__restrict__ cur, const uint8_t *const *refs,
+                                                      Geometry g, int lambda, PuState *__restrict__ state,
+                                                      unsigned long long *__restrict__ keys)
+{
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (i >= n) return;
+    init_one(i, lane, pus, cur, refs, g, lambda, state, keys);
+}
+
+// Same over an index list (the PUs outside the CTU plan).
+__global__ void __launch_bounds__(128) me_init_list_kernel(const int *__restrict__ list, int n,
+                                                           const xavs2gpu_pu_t *__restrict__ pus,
+                                                           const uint8_t *__restrict__ cur, const uint8_t *const *refs,
+                                                           Geometry g, int lambda, PuState *__restrict__ state,
+                                                           unsigned long long *__restrict__ keys)
+{
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (t >= n) return;
+    init_one(list[t], lane, pus, cur, refs, g, lambda, state, keys);
 }
 
 // ---- 2b. per-PU full search (one CTA per PU) --------------------------------------
@@ -886,6 +906,22 @@ static void ensure_plan(MeSessionImpl &m, int R)
     m.n_ctu_pus = m.n - m.n_generic;
     if (m.n_generic)
         XG_CUDA(cudaMemcpyAsync(m.d_generic, generic.data(), sizeof(int) * m.n_generic, cudaMemcpyHostToDevice, m.st));
+    // PUs of the CTU plan have the single candidate (0,0), which is also the
+    // search centre; their state is fixed by the plan (the CTU kernel
+    // evaluates the candidate itself)
+    {
+        std::vector<PuState> st(m.n);
+        std::vector<char> is_generic(m.n, 0);
+        for (int i : generic) is_generic[i] = 1;
+        for (int i = 0; i < m.n; i++) {
+            PuState &x = st[i];
+            memset(&x, 0, sizeof(x));
+            x.ncand = 1;
+            x.valid = is_generic[i] ? 0 : 1;
+        }
+        if (m.n) XG_CUDA(cudaMemcpyAsync(m.d_state, st.data(), sizeof(PuState) * m.n, cudaMemcpyHostToDevice, m.st));
+        XG_CUDA(cudaStreamSynchronize(m.st));
+    }
     // refinement order: PU searches grouped by shape, G per warp task
     std::vector<int> order(m.n), start(kNumParts + 1, 0);
     for (const auto &p : m.h_pus) start[p.part + 1]++;
@@ -937,9 +973,12 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     const int R = prm->search_range, lam = prm->lambda_factor;
     ensure_plan(m, R);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[0], m.st));
-    me_init_kernel<<<(m.n * 32 + 127) / 128, 128, 0, m.st>>>(m.d_pus, m.n, m.plane(0), m.d_ref0, g, lam, m.d_state,
-                                                             m.d_keys);
-    count_launch();
+    XG_CUDA(cudaMemsetAsync(m.d_keys, 0xff, sizeof(unsigned long long) * m.n, m.st));
+    if (m.n_generic) {
+        me_init_list_kernel<<<(m.n_generic * 32 + 127) / 128, 128, 0, m.st>>>(
+            m.d_generic, m.n_generic, m.d_pus, m.plane(0), m.d_ref0, g, lam, m.d_state, m.d_keys);
+        count_launch();
+    }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[1], m.st));
     ctu_plan_run(m.plan, *prm, m.plane(0), m.d_ref0, g, m.d_state, m.d_keys, m.st);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
