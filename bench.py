@@ -351,6 +351,204 @@ def run_ours(args):
     sess.close()
 
 
+# ---- batched transform + quant ---------------------------------------------
+TQ_METRIC = "bit-exact TU blocks/s (batched dct->quant->dequant->idct, 10^6 blocks, TU 4..64)"
+
+
+def tq_bytes(blocks):
+    """Algorithmic bytes of a batch: residual in, levels out, recon out
+    (int16 each), the 32-byte descriptor and the 4-byte nnz per block."""
+    import xavs2_gb300 as xg
+    w = np.asarray(xg.PU_W)[blocks["part"]].astype(np.int64)
+    h = np.asarray(xg.PU_H)[blocks["part"]].astype(np.int64)
+    size = w * h
+    ncoef = np.where((w == 64) | (h == 64), size // 4, size)
+    return int((2 * size + 2 * ncoef + 2 * size).sum() + 36 * len(blocks))
+
+
+def cpu_sample_tq(blocks, residual, fraction, seed, threads):
+    """The oracle's chain over a random sample of the blocks; returns
+    (blocks done, seconds, sample descriptors, levels, recon, nnz)."""
+    import oracle
+    import xavs2_gb300 as xg
+    olib = oracle.lib()
+    rng = np.random.default_rng(seed)
+    sel = np.ascontiguousarray(blocks[rng.random(len(blocks)) < fraction])
+    # repack the sample so its buffers are small
+    w = np.asarray(xg.PU_W)[sel["part"]].astype(np.int64)
+    h = np.asarray(xg.PU_H)[sel["part"]].astype(np.int64)
+    size = w * h
+    ncoef = np.where((w == 64) | (h == 64), size // 4, size)
+    src_off = sel["offset"].copy()
+    sel["offset"] = np.cumsum(size) - size
+    sel["coef_offset"] = np.cumsum(ncoef) - ncoef
+    idx = np.concatenate([np.arange(o, o + n) for o, n in zip(src_off, size)]) if len(sel) else np.zeros(0, np.int64)
+    res = np.ascontiguousarray(residual[idx])
+    coef = np.zeros(int(ncoef.sum()), np.int16)
+    rec = np.zeros(int(size.sum()), np.int16)
+    nnz = np.zeros(len(sel), np.int32)
+    t0 = time.perf_counter()
+    olib.xo_tq_batch(oracle.ptr(sel), len(sel), oracle.ptr(res), oracle.ptr(coef), oracle.ptr(rec),
+                     oracle.ptr(nnz), threads)
+    dt = time.perf_counter() - t0
+    return len(sel), dt, sel, src_off, coef, rec, nnz
+
+
+def run_tq(args):
+    import torch
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+
+    rank, world, local = dist_env()
+    n = args.tq_blocks
+    blocks, nres, ncoef, zero = synth.tq_blocks(n, seed=3 + rank)
+    algo_bytes = tq_bytes(blocks)
+    cfg = {"workload": "tq_batch_1e6_tu4to64", "blocks": n, "tu_sizes": "4,8,16,32,64 uniform",
+           "qp": "uniform 22..51", "secondary_4x4": "50% of 4x4 blocks", "zero_blocks": "10%",
+           "l2": "inputs larger than L2 (%.1f GB per step)" % (algo_bytes / 1e9)}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        res = synth.tq_residual(blocks, zero, nres, seed=4 + rank).numpy()
+        threads = os.cpu_count() or 1
+        for i in range(args.warmup):
+            cpu_sample_tq(blocks, res, args.cpu_fraction / 4, 100 + i, threads)
+        done = 0
+        tt = 0.0
+        for i in range(args.steps):
+            k, dt, *_ = cpu_sample_tq(blocks, res, args.cpu_fraction, 200 + i, threads)
+            done += k
+            tt += dt
+        value = done / tt
+        print(json.dumps({"impl": "reference", "metric": TQ_METRIC, "value": value, "unit": "blocks/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "int16", "data": "synthetic", "config": cfg,
+                          "cpu_baseline": {"value": value, "unit": "blocks/s", "cores": threads, "kind": "port",
+                                           "sample": "per step a random %.2f%% of the %d blocks" %
+                                                     (100 * args.cpu_fraction, n)},
+                          "e2e": {"value": value, "unit": "blocks/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    dev = torch.device("cuda", local)
+    d_res = synth.tq_residual(blocks, zero, nres, seed=4 + rank, device=dev)
+    d_blocks = torch.from_numpy(blocks.view(np.uint8).copy()).to(dev)
+    d_coef = torch.empty(ncoef, dtype=torch.int16, device=dev)
+    d_rec = torch.empty(nres, dtype=torch.int16, device=dev)
+    d_nnz = torch.empty(n, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    tq = xg.fn("xavs2gpu_tq_batch")
+
+    def step(s):
+        rc = tq(d_blocks.data_ptr(), n, d_res.data_ptr(), d_coef.data_ptr(), d_rec.data_ptr(), d_nnz.data_ptr(),
+                s.cuda_stream)
+        assert rc == 0
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step(stream)
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    clk.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            starts[i].record(stream)
+            step(stream)
+            ends[i].record(stream)
+    barrier()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    step_ms = [s_.elapsed_time(e) for s_, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = n * world * args.steps / (total_ms / 1e3)
+    kernel_ms = min(step_ms)
+
+    # end to end with host buffers: pinned residual in, levels + recon + nnz out
+    h_res = d_res.cpu().pin_memory()
+    h_blocks = torch.from_numpy(blocks.view(np.uint8).copy()).pin_memory()
+    h_coef = torch.empty(ncoef, dtype=torch.int16).pin_memory()
+    h_rec = torch.empty(nres, dtype=torch.int16).pin_memory()
+    h_nnz = torch.empty(n, dtype=torch.int32).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            d_blocks.copy_(h_blocks, non_blocking=True)
+            d_res.copy_(h_res, non_blocking=True)
+            step(stream)
+            h_coef.copy_(d_coef, non_blocking=True)
+            h_rec.copy_(d_rec, non_blocking=True)
+            h_nnz.copy_(d_nnz, non_blocking=True)
+        stream.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = n * world * args.steps / e2e_s
+    if rank != 0:
+        return
+    # bit-exactness of a random sample against the oracle (the sample timed
+    # as the CPU baseline)
+    res_np = h_res.numpy()
+    k, cpu_s, sel, src_off, coef, rec, nnz = cpu_sample_tq(blocks, res_np, args.cpu_fraction, 7,
+                                                          os.cpu_count() or 1)
+    g_coef, g_rec, g_nnz = h_coef.numpy(), h_rec.numpy(), h_nnz.numpy()
+    idx = np.searchsorted(blocks["offset"], src_off)
+    exact = bool(np.array_equal(g_nnz[idx], nnz))
+    for j in range(len(sel)):
+        b = blocks[idx[j]]
+        o, co = int(b["offset"]), int(b["coef_offset"])
+        n_in = xg.PU_W[int(b["part"])] * xg.PU_H[int(b["part"])]
+        n_c = n_in // 4 if n_in == 4096 else n_in
+        so, sco = int(sel["offset"][j]), int(sel["coef_offset"][j])
+        if not (np.array_equal(g_rec[o:o + n_in], rec[so:so + n_in]) and
+                np.array_equal(g_coef[co:co + n_c], coef[sco:sco + n_c])):
+            exact = False
+            break
+    peaks, peak_src = measured_peaks()
+    achieved = algo_bytes / (kernel_ms / 1e3) / 1e9
+    line = {
+        "metric": TQ_METRIC, "value": value, "unit": "blocks/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int16", "data": "synthetic", "config": cfg,
+        "e2e": {"value": e2e, "unit": "blocks/s", "h2d_bytes_per_step": int(2 * nres + 32 * n),
+                "d2h_bytes_per_step": int(2 * ncoef + 2 * nres + 4 * n)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "tq_batch", "achieved": achieved,
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
+                     "peak_source": peak_src, "algorithmic_bytes_per_launch": algo_bytes,
+                     "kernel_ms": kernel_ms},
+        "sample_bit_exact": exact,
+        "cpu_baseline": {"value": k / cpu_s, "unit": "blocks/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": "random %.2f%% (%d) of the blocks, oracle C chain, OpenMP"
+                                   % (100 * args.cpu_fraction, k)},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,8 +559,13 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
+    ap.add_argument("--workload", choices=["me", "tq"], default="me",
+                    help="me: batched motion search (default); tq: batched transform+quant")
+    ap.add_argument("--tq-blocks", type=int, default=1000000)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "tq":
+        run_tq(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -68,6 +68,10 @@ XAVS2GPU_API void xavs2gpu_set_abort_on_error(int enable);
 /* Number of kernels this library has launched in the process. */
 XAVS2GPU_API uint64_t xavs2gpu_kernel_launches(void);
 XAVS2GPU_API const char *xavs2gpu_version(void);
+/* Synchronous copies between host and device memory (helpers for bindings
+ * that hold raw device pointers); return the status. */
+XAVS2GPU_API int xavs2gpu_copy_d2h(void *dst, const void *src, size_t bytes);
+XAVS2GPU_API int xavs2gpu_copy_h2d(void *dst, const void *src, size_t bytes);
 
 /* ===========================================================================
  * 1. drop-in primitives
@@ -347,6 +351,10 @@ XAVS2GPU_API int xavs2gpu_me_plane_stride(xavs2gpu_me_session_t *s);
 XAVS2GPU_API int xavs2gpu_me_get_plane(xavs2gpu_me_session_t *s, int slot, int k, uint8_t *out, intptr_t stride);
 XAVS2GPU_API int xavs2gpu_me_plane_pad(xavs2gpu_me_session_t *s);
 XAVS2GPU_API void *xavs2gpu_me_stream(xavs2gpu_me_session_t *s);
+/* Geometry and PU list of a session (host copies). */
+XAVS2GPU_API void xavs2gpu_me_session_info(const xavs2gpu_me_session_t *s, int *width, int *height, int *num_refs,
+                                           int *n_pus);
+XAVS2GPU_API int xavs2gpu_me_session_pus(const xavs2gpu_me_session_t *s, xavs2gpu_pu_t *out);
 /* How the last xavs2gpu_me_set_pus split the list: PUs searched by the
  * shared-window CTU kernel and by the per-PU kernel. */
 XAVS2GPU_API void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus, int *n_generic_pus, int *n_ctu_jobs);
@@ -356,6 +364,167 @@ XAVS2GPU_API void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pu
  * search, [2] per-PU search, [3] sub-pel refinement. */
 XAVS2GPU_API void xavs2gpu_me_set_profiling(xavs2gpu_me_session_t *s, int enable);
 XAVS2GPU_API int xavs2gpu_me_phase_ms(xavs2gpu_me_session_t *s, float ms[4]);
+/* Launch shapes of the sub-pel refinement (no counterpart in the reference;
+ * results never depend on them): searches of at most refine_split_px
+ * pixels refine one per thread, larger ones one per warp; refine_block
+ * threads per CTA (32, 64 or 128). */
+typedef struct xavs2gpu_me_tuning {
+    int32_t refine_split_px;
+    int32_t refine_block;
+} xavs2gpu_me_tuning_t;
+XAVS2GPU_API int xavs2gpu_me_set_tuning(xavs2gpu_me_session_t *s, const xavs2gpu_me_tuning_t *t);
+XAVS2GPU_API int xavs2gpu_me_get_tuning(const xavs2gpu_me_session_t *s, xavs2gpu_me_tuning_t *t);
+/* Builds the search plan for prm->search_range now (host work and one
+ * stream synchronisation) so that the next xavs2gpu_me_run only enqueues
+ * device work -- required before capturing a run into a CUDA graph. */
+XAVS2GPU_API int xavs2gpu_me_prepare(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm);
+
+/* ---- several pictures per launch -------------------------------------------
+ * No counterpart in the reference (its search runs one PU at a time).  The
+ * session's work (CTU jobs, per-PU searches, refinements) of up to 256
+ * sessions -- pictures of any sizes, each with its own resident references
+ * -- is concatenated and searched by one launch of each kernel on `stream`.
+ * Results land in each session's own result array, identical to
+ * xavs2gpu_me_run on that session alone.  The sessions' pictures must be
+ * loaded on `stream` (xavs2gpu_me_set_stream) or before the call. */
+typedef struct xavs2gpu_me_batch xavs2gpu_me_batch_t;
+XAVS2GPU_API xavs2gpu_me_batch_t *xavs2gpu_me_batch_create(void);
+XAVS2GPU_API void xavs2gpu_me_batch_destroy(xavs2gpu_me_batch_t *b);
+XAVS2GPU_API int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session_t *const *sessions, int n,
+                                       const xavs2gpu_me_params_t *prm, void *stream);
+/* Make the session enqueue on `stream` (NULL: back to its own stream).  No
+ * synchronisation: work already enqueued on the previous stream must be
+ * ordered before the next by the caller. */
+XAVS2GPU_API int xavs2gpu_me_set_stream(xavs2gpu_me_session_t *s, void *stream);
+/* Device table of the reference planes in the current slot order: entry
+ * 16 r + k = plane k of reference r (updated in place, stream-ordered, by
+ * xavs2gpu_me_rotate_refs). */
+XAVS2GPU_API const uint8_t *const *xavs2gpu_me_plane_table_device(xavs2gpu_me_session_t *s);
+/* Reference r+1 takes over reference r's planes and reference 0 gets the
+ * oldest buffer (to be overwritten by the next xavs2gpu_me_set_picture_*
+ * of slot 0) -- the reference list update of a P-picture sequence without
+ * moving pixels. */
+XAVS2GPU_API int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s);
+
+/* ---- full-picture chain ---------------------------------------------------
+ * No single counterpart in the reference: the device-side sequence of one
+ * P picture over its leaf CUs -- sub-pel planes of every reference
+ * (interpolate_lcu_row), the current picture, the batched motion search
+ * (xavs2_me_search per PU and reference), the motion-compensated residual of
+ * each CU's 2Nx2N prediction from its best reference (mc_luma on the
+ * frame's sub-pel planes, mc.c:559-589, then pixel_sub_ps), the TU chain of
+ * one CU-sized TU per CU (xavs2gpu_tq_batch), and the reconstruction
+ * clip(pred + residual) (pixel_add_ps) -- enqueued on the session stream,
+ * eagerly or as one captured CUDA graph.  The RDO choices between partition
+ * modes, TU splits and intra stay on the host. */
+typedef struct xavs2gpu_cu {
+    int16_t x, y;              /* luma position of the CU                          */
+    int16_t size;              /* 8, 16, 32 or 64                                  */
+    int16_t pad_;
+    int32_t pu[4];             /* index of the CU's 2Nx2N PU in the session's PU
+                                  list for reference 0..3 (-1: not searched)       */
+    int64_t offset;            /* residual / recon offset (elements), size*size    */
+    int64_t coef_offset;       /* level offset, size*size (64: 32*32)              */
+} xavs2gpu_cu_t;
+
+typedef struct xavs2gpu_chain xavs2gpu_chain_t;
+/* `s` must already hold the PU list the CUs index.  flags bit 0 (feedback):
+ * after each picture the reference sources shift by one (ref r+1 <- ref r)
+ * and the reconstructed picture becomes reference 0, as in an encoder's
+ * P-picture loop.  Returns NULL on failure. */
+XAVS2GPU_API xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, const xavs2gpu_cu_t *cus, int n_cus,
+                                                     int qp, int flags);
+XAVS2GPU_API void xavs2gpu_chain_destroy(xavs2gpu_chain_t *c);
+/* Device source picture (width x height, stride = width): idx 0 = the
+ * current picture, 1 + r = reference r. */
+XAVS2GPU_API uint8_t *xavs2gpu_chain_source(xavs2gpu_chain_t *c, int idx);
+/* Enqueue one picture eagerly / capture it into a CUDA graph (after one
+ * eager run with the same parameters) / launch the captured graph. */
+XAVS2GPU_API int xavs2gpu_chain_run(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm);
+XAVS2GPU_API int xavs2gpu_chain_capture(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm);
+XAVS2GPU_API int xavs2gpu_chain_launch(xavs2gpu_chain_t *c);
+/* Device outputs of the last picture: levels, reconstructed residual, nnz
+ * and TU descriptors per CU (CU order), the reconstructed picture (width x
+ * height, stride = width) and per CU the chosen reference and its MV. */
+typedef struct xavs2gpu_cu_choice {
+    int32_t ref;               /* reference with the smallest 2Nx2N cost (lowest index on ties) */
+    int16_t mv_x, mv_y;        /* its MV, quarter-pel                               */
+} xavs2gpu_cu_choice_t;
+typedef struct xavs2gpu_chain_outputs {
+    int16_t *coef;
+    int16_t *recon_residual;
+    int32_t *nnz;
+    xavs2gpu_tq_block_t *blocks;
+    uint8_t *recon;
+    xavs2gpu_cu_choice_t *choice;
+    int64_t n_residual, n_coef;
+} xavs2gpu_chain_outputs_t;
+XAVS2GPU_API int xavs2gpu_chain_get_outputs(xavs2gpu_chain_t *c, xavs2gpu_chain_outputs_t *o);
+/* Autotuner: times the chain eagerly for every candidate launch shape
+ * (refinement split and CTA size, TU-chain warps per CTA), keeps the fastest
+ * and returns its mean time per picture in ms (*best_ms).  Results do not
+ * depend on the choice.  Invalidates a captured graph. */
+typedef struct xavs2gpu_chain_tuning {
+    xavs2gpu_me_tuning_t me;
+    int32_t tq_warps;          /* warps per CTA of the TU chain: 4 or 8 */
+    int32_t pad_;
+} xavs2gpu_chain_tuning_t;
+XAVS2GPU_API int xavs2gpu_chain_autotune(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm, int reps,
+                                         float *best_ms);
+XAVS2GPU_API int xavs2gpu_chain_get_tuning(const xavs2gpu_chain_t *c, xavs2gpu_chain_tuning_t *t);
+XAVS2GPU_API int xavs2gpu_chain_set_tuning(xavs2gpu_chain_t *c, const xavs2gpu_chain_tuning_t *t);
+/* Kernel nodes of the captured graph (what one xavs2gpu_chain_launch runs). */
+XAVS2GPU_API int xavs2gpu_chain_graph_kernels(const xavs2gpu_chain_t *c);
+
+/* ---- serving ------------------------------------------------------------------
+ * No counterpart in the reference.  Many concurrent streams of different
+ * resolutions submit pictures; a scheduler thread batches the arrived
+ * pictures (at most one per stream, up to max_batch_frames and
+ * max_batch_pixels per batch) and runs every batch with one launch per
+ * kernel: reference update and sub-pel planes per picture, the motion search
+ * of all pictures (xavs2gpu_me_batch_run), each CU's motion-compensated
+ * residual from its best reference, one TU chain over all CUs, the
+ * reconstruction and a per-picture checksum.  Each stream keeps its two
+ * references and their planes resident; streams are admitted against
+ * hbm_budget_bytes.  The first two pictures of a stream only fill its
+ * references (ref_only results); every later picture is searched against
+ * the two before it. */
+typedef struct xavs2gpu_server_config {
+    int64_t hbm_budget_bytes;    /* device memory the server may hold (0: unlimited) */
+    int64_t max_batch_pixels;    /* luma pixels per batch (sizes two batch buffer sets) */
+    int32_t max_batch_frames;    /* pictures per batch, 1..256 */
+    int32_t qp;                  /* quantiser of every TU */
+    xavs2gpu_me_params_t me;     /* search parameters */
+} xavs2gpu_server_config_t;
+
+typedef struct xavs2gpu_server_result {
+    int32_t stream, frame;       /* stream id, picture number within the stream */
+    int64_t tag;                 /* the submitter's tag */
+    int64_t t_submit_ns;         /* steady clock at submission */
+    int64_t t_done_ns;           /* steady clock when the batch completed */
+    uint64_t hash;               /* sum over the 32-bit words w_i of [reconstruction | levels |
+                                    search results] of (w_i + 1) * (2 i + 1) mod 2^64; 0 when ref_only */
+    int32_t batch_frames;        /* pictures in the batch that carried it */
+    int32_t ref_only;
+} xavs2gpu_server_result_t;
+
+typedef struct xavs2gpu_server xavs2gpu_server_t;
+XAVS2GPU_API xavs2gpu_server_t *xavs2gpu_server_create(const xavs2gpu_server_config_t *cfg);
+XAVS2GPU_API void xavs2gpu_server_destroy(xavs2gpu_server_t *s);
+/* A stream of width x height pictures with its leaf-CU PU list (2
+ * references) and CU list (as for xavs2gpu_chain_create) and `ring` pinned
+ * picture slots.  Returns the stream id, or minus an error code
+ * (-XAVS2GPU_ERR_CAPACITY when the device-memory budget is exhausted). */
+XAVS2GPU_API int xavs2gpu_server_open_stream(xavs2gpu_server_t *s, int width, int height, const xavs2gpu_pu_t *pus,
+                                             int n_pus, const xavs2gpu_cu_t *cus, int n_cus, int ring);
+/* Copies the picture into a free slot of the stream and queues it;
+ * XAVS2GPU_ERR_CAPACITY when all of the stream's slots are in use. */
+XAVS2GPU_API int xavs2gpu_server_submit(xavs2gpu_server_t *s, int stream, const uint8_t *luma, intptr_t stride,
+                                        int64_t tag);
+/* Completed pictures (waits up to timeout_ms for the first). */
+XAVS2GPU_API int xavs2gpu_server_poll(xavs2gpu_server_t *s, xavs2gpu_server_result_t *out, int max, int timeout_ms);
+XAVS2GPU_API void xavs2gpu_server_stats(xavs2gpu_server_t *s, int64_t *hbm_used, int64_t *batches, int64_t *frames,
+                                        int64_t *pending);
 
 /* ---- allocation-free motion search ---------------------------------------
  * No counterpart in the reference.  The same search as xavs2gpu_me_run

@@ -102,6 +102,7 @@ _ORACLE_SIGS = {
     "xo_dequant": (None, [_P, _I, _I, _I]), "xo_abs_coeff": (None, [_P, _P, _I]),
     "xo_add_sign": (_I, [_P, _P, _I]),
     "xo_tq_chain": (_I, [_I, _P, _P, _I, _I, _I]),
+    "xo_tq_batch": (None, [_P, _I, _P, _P, _P, _P, _I]),
     "xo_me_search": (_I, [_P, _P, _P, _S, _P, _S, _P]),
     "xo_me_search_list": (None, [_P, _P, _I, _P, _S, _P, _S, _P, _I]),
     "xo_pu_set_limits": (None, [_P, _I, _I, _I, _I]),

@@ -892,6 +892,43 @@ int xo_tq_chain(int part, int16_t *blk, int16_t *coef_out, int qp, int b_intra, 
     return nz;
 }
 
+/* Batch form of xo_tq_chain over the GPU batch descriptor layout
+ * (xavs2gpu_tq_block_t: offset, coef_offset, part, qp, flags): residual and
+ * recon at offset, levels at coef_offset, nnz per block (-1 for an invalid
+ * descriptor).  OpenMP over blocks when threads > 1. */
+static int tq_one(const xo_tq_block_t *b, const int16_t *residual, int16_t *coef, int16_t *recon)
+{
+    int16_t blk[64 * 64], cf[64 * 64];
+    int w, h, n, nz;
+    if (b->part < 0 || b->part >= 25 || b->qp < 0 || b->qp > 79) return -1;
+    w = k_pu_w[b->part];
+    h = k_pu_h[b->part];
+    if (!(w * h == 16 || (w == h && w >= 8) || (w == 16 && h == 4) || (w == 4 && h == 16) ||
+          (w == 32 && h == 8) || (w == 8 && h == 32) || (w == 64 && h == 16) || (w == 16 && h == 64)))
+        return -1;
+    n = (w == 64 || h == 64) ? (w / 2) * (h / 2) : w * h;
+    memcpy(blk, residual + b->offset, (size_t)w * h * 2);
+    nz = xo_tq_chain(b->part, blk, cf, b->qp, b->flags & 1, (b->flags >> 1) & 1);
+    memcpy(coef + b->coef_offset, cf, (size_t)n * 2);
+    memcpy(recon + b->offset, blk, (size_t)w * h * 2);
+    return nz;
+}
+
+void xo_tq_batch(const xo_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef, int16_t *recon,
+                 int32_t *nnz, int threads)
+{
+    int i;
+#ifdef _OPENMP
+    if (threads > 1) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+        for (i = 0; i < n; i++) nnz[i] = tq_one(&blocks[i], residual, coef, recon);
+        return;
+    }
+#endif
+    (void)threads;
+    for (i = 0; i < n; i++) nnz[i] = tq_one(&blocks[i], residual, coef, recon);
+}
+
 /* ------------------------------------------------------------------------
  * motion search (me.c:479-579, 614-641, 879-1183; md_inter.c:840-926)
  * ---------------------------------------------------------------------- */

@@ -113,6 +113,14 @@ int  xo_quant_fwd_add(int shift, int b_intra);
  * reconstructed residual.  Returns nnz. */
 int  xo_tq_chain(int part, int16_t *blk, int16_t *coef_out, int qp, int b_intra, int use_2nd);
 
+/* Batch descriptor (same layout as the GPU library's xavs2gpu_tq_block_t). */
+typedef struct xo_tq_block {
+    int64_t offset, coef_offset;
+    int32_t part, qp, flags, pad_;
+} xo_tq_block_t;
+void xo_tq_batch(const xo_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef, int16_t *recon,
+                 int32_t *nnz, int threads);
+
 /* ---- motion search (me.c) --------------------------------------------- */
 typedef struct xo_me_params {
     int32_t search_range;     /* full search over [-R, R) in both axes   */

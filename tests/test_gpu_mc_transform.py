@@ -213,3 +213,68 @@ def test_tq_batch(gpu, olib):
         assert nnz[i] == nz, i
         assert np.array_equal(coef[co:co + n], cf[:n]), i
         assert np.array_equal(rec[o:o + w * h], blk), i
+
+
+def _run_tq_batch(blocks, res, nres, ncoef):
+    import torch
+    import xavs2_gb300 as xg
+    d_blocks = torch.from_numpy(blocks.view(np.uint8).copy()).cuda()
+    d_res = torch.from_numpy(res).cuda()
+    d_coef = torch.full((ncoef,), 0x5A5A, dtype=torch.int16, device="cuda")
+    d_rec = torch.full((nres,), 0x5A5A, dtype=torch.int16, device="cuda")
+    d_nnz = torch.zeros(len(blocks), dtype=torch.int32, device="cuda")
+    rc = xg.fn("xavs2gpu_tq_batch")(d_blocks.data_ptr(), len(blocks), d_res.data_ptr(), d_coef.data_ptr(),
+                                     d_rec.data_ptr(), d_nnz.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    return d_coef.cpu().numpy(), d_rec.cpu().numpy(), d_nnz.cpu().numpy()
+
+
+def test_tq_batch_edges(gpu, olib):
+    """Extreme residuals (the int16 wrap of the forward passes and the 16-bit
+    clips), blocks at unaligned offsets (element-granular packing), invalid
+    descriptors (a non-TU shape, QP out of range): levels, recon and nnz
+    equal the oracle's chain; invalid blocks report nnz = -1."""
+    rng = np.random.default_rng(77)
+    parts = list(TU_PARTS) * 6
+    n = len(parts) + 2
+    blocks = np.zeros(n, np.dtype([("offset", "<i8"), ("coef_offset", "<i8"), ("part", "<i4"), ("qp", "<i4"),
+                                   ("flags", "<i4"), ("pad_", "<i4")]))
+    off = coff = 0
+    chunks = []
+    for i in range(n):
+        p = parts[i] if i < len(parts) else 0
+        w, h = PU_W[p], PU_H[p]
+        gap = int(rng.integers(0, 3))          # 0..2 elements: breaks 16-byte alignment
+        off += gap
+        chunks.append(np.zeros(gap, np.int16))
+        kind = i % 4
+        if kind == 0:
+            blk = rng.integers(-32768, 32768, w * h)
+        elif kind == 1:
+            blk = np.where(rng.random(w * h) < 0.5, -32768, 32767)
+        elif kind == 2:
+            blk = rng.integers(-2048, 2048, w * h)
+        else:
+            blk = np.clip(np.round(rng.laplace(0, 40, w * h)), -255, 255)
+        chunks.append(blk.astype(np.int16))
+        blocks[i] = (off, coff, p, int(rng.integers(0, 80)), int(rng.integers(0, 4)) if p == 0 else int(rng.integers(0, 2)), 0)
+        off += w * h
+        coff += (w // 2) * (h // 2) if (w == 64 or h == 64) else w * h
+    blocks["part"][-2] = 5            # 8x4 is not a TU shape
+    blocks["qp"][-1] = 80             # out of range
+    res = np.concatenate(chunks)
+    coef, rec, nnz = _run_tq_batch(blocks, res, off, coff)
+    for i, b in enumerate(blocks[:-2]):
+        p = int(b["part"])
+        w, h = PU_W[p], PU_H[p]
+        o, co = int(b["offset"]), int(b["coef_offset"])
+        blk = res[o:o + w * h].copy()
+        cf = np.zeros(w * h, np.int16)
+        nz = olib.xo_tq_chain(p, oracle.ptr(blk), oracle.ptr(cf), int(b["qp"]), int(b["flags"]) & 1,
+                              (int(b["flags"]) >> 1) & 1)
+        nc = (w // 2) * (h // 2) if (w == 64 or h == 64) else w * h
+        assert nnz[i] == nz, (i, p)
+        assert np.array_equal(coef[co:co + nc], cf[:nc]), (i, p)
+        assert np.array_equal(rec[o:o + w * h], blk), (i, p)
+    assert nnz[-2] == -1 and nnz[-1] == -1

@@ -55,6 +55,8 @@ _SIGS = {
     "xavs2gpu_set_abort_on_error": (None, [_I]),
     "xavs2gpu_kernel_launches": (ctypes.c_uint64, []),
     "xavs2gpu_version": (ctypes.c_char_p, []),
+    "xavs2gpu_copy_d2h": (_I, [_P, _P, ctypes.c_size_t]),
+    "xavs2gpu_copy_h2d": (_I, [_P, _P, ctypes.c_size_t]),
     "xavs2gpu_pixel_init": (None, [ctypes.c_uint32, _P]),
     "xavs2gpu_mad_init": (None, [ctypes.c_uint32, _P]),
     "xavs2gpu_dct_init": (None, [ctypes.c_uint32, _P]),
@@ -107,6 +109,27 @@ _SIGS = {
     "xavs2gpu_me_get_plane": (_I, [_P, _I, _I, _P, _S]),
     "xavs2gpu_me_set_profiling": (None, [_P, _I]),
     "xavs2gpu_me_phase_ms": (_I, [_P, _P]),
+    "xavs2gpu_me_set_tuning": (_I, [_P, _P]),
+    "xavs2gpu_me_get_tuning": (_I, [_P, _P]),
+    "xavs2gpu_me_prepare": (_I, [_P, _P]),
+    "xavs2gpu_me_session_info": (None, [_P, _P, _P, _P, _P]),
+    "xavs2gpu_me_session_pus": (_I, [_P, _P]),
+    "xavs2gpu_chain_create": (_P, [_P, _P, _I, _I, _I]),
+    "xavs2gpu_chain_destroy": (None, [_P]),
+    "xavs2gpu_chain_source": (_P, [_P, _I]),
+    "xavs2gpu_chain_run": (_I, [_P, _P]),
+    "xavs2gpu_chain_capture": (_I, [_P, _P]),
+    "xavs2gpu_chain_launch": (_I, [_P]),
+    "xavs2gpu_chain_get_outputs": (_I, [_P, _P]),
+    "xavs2gpu_chain_autotune": (_I, [_P, _P, _I, _P]),
+    "xavs2gpu_chain_get_tuning": (_I, [_P, _P]),
+    "xavs2gpu_chain_set_tuning": (_I, [_P, _P]),
+    "xavs2gpu_chain_graph_kernels": (_I, [_P]),
+    "xavs2gpu_me_batch_create": (_P, []),
+    "xavs2gpu_me_batch_destroy": (None, [_P]),
+    "xavs2gpu_me_batch_run": (_I, [_P, _P, _I, _P, _P]),
+    "xavs2gpu_me_set_stream": (_I, [_P, _P]),
+    "xavs2gpu_me_rotate_refs": (_I, [_P]),
 }
 
 _PIXEL_CMP = ["sad", "satd", "sa8d", "ssd"]
@@ -247,10 +270,122 @@ class MeSession:
         self._check(self.lib.xavs2gpu_me_phase_ms(self.h, out), "phase_ms")
         return list(out)
 
+    def set_stream(self, stream):
+        self._check(self.lib.xavs2gpu_me_set_stream(self.h, ctypes.c_void_p(stream) if stream else None),
+                    "set_stream")
+
+    def rotate_refs(self):
+        self._check(self.lib.xavs2gpu_me_rotate_refs(self.h), "rotate_refs")
+
     def plan_stats(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self.lib.xavs2gpu_me_plan_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
         return a.value, b.value, c.value
+
+
+class MeBatch:
+    """Several sessions searched by one launch of each kernel."""
+
+    def __init__(self):
+        self.lib = load()
+        self.h = self.lib.xavs2gpu_me_batch_create()
+
+    def run(self, sessions, params, stream=None):
+        arr = (ctypes.c_void_p * len(sessions))(*[s.h for s in sessions])
+        rc = self.lib.xavs2gpu_me_batch_run(self.h, arr, len(sessions), ctypes.byref(params),
+                                            ctypes.c_void_p(stream) if stream else None)
+        if rc != 0:
+            raise RuntimeError("me_batch_run failed (%d): %s" % (rc, self.lib.xavs2gpu_get_error()))
+
+    def close(self):
+        if self.h:
+            self.lib.xavs2gpu_me_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MeTuning(ctypes.Structure):
+    _fields_ = [("refine_split_px", ctypes.c_int32), ("refine_block", ctypes.c_int32)]
+
+
+class ChainTuning(ctypes.Structure):
+    _fields_ = [("me", MeTuning), ("tq_warps", ctypes.c_int32), ("pad_", ctypes.c_int32)]
+
+
+class ChainOutputs(ctypes.Structure):
+    _fields_ = [("coef", _P), ("recon_residual", _P), ("nnz", _P), ("blocks", _P), ("recon", _P),
+                ("choice", _P), ("n_residual", ctypes.c_int64), ("n_coef", ctypes.c_int64)]
+
+
+CHOICE_DTYPE = np.dtype([("ref", "<i4"), ("mv_x", "<i2"), ("mv_y", "<i2")])
+
+
+class Chain:
+    """One P picture of the hot path over leaf CUs (xavs2gpu_chain_*): the
+    session `sess` must hold the PU list `cus` refers to."""
+
+    def __init__(self, sess, cus, qp, feedback=False):
+        self.lib = load()
+        self.sess = sess
+        self.cus = np.ascontiguousarray(cus, dtype=CU_DTYPE)
+        self.h = self.lib.xavs2gpu_chain_create(sess.h, ptr(self.cus), len(self.cus), qp, 1 if feedback else 0)
+        if not self.h:
+            raise RuntimeError("xavs2gpu_chain_create failed: %s" % self.lib.xavs2gpu_get_error())
+
+    def close(self):
+        if self.h:
+            self.lib.xavs2gpu_chain_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError("%s failed (%d): %s" % (what, rc, self.lib.xavs2gpu_get_error()))
+
+    def source(self, idx):
+        """Device pointer of source picture idx (0: current, 1 + r: reference r)."""
+        return self.lib.xavs2gpu_chain_source(self.h, idx)
+
+    def run(self, params):
+        self._check(self.lib.xavs2gpu_chain_run(self.h, ctypes.byref(params)), "chain_run")
+
+    def capture(self, params):
+        self._check(self.lib.xavs2gpu_chain_capture(self.h, ctypes.byref(params)), "chain_capture")
+
+    def launch(self):
+        self._check(self.lib.xavs2gpu_chain_launch(self.h), "chain_launch")
+
+    def graph_kernels(self):
+        return self.lib.xavs2gpu_chain_graph_kernels(self.h)
+
+    def autotune(self, params, reps=2):
+        ms = ctypes.c_float()
+        self._check(self.lib.xavs2gpu_chain_autotune(self.h, ctypes.byref(params), reps, ctypes.byref(ms)),
+                    "chain_autotune")
+        return ms.value
+
+    def tuning(self):
+        t = ChainTuning()
+        self._check(self.lib.xavs2gpu_chain_get_tuning(self.h, ctypes.byref(t)), "chain_get_tuning")
+        return t
+
+    def set_tuning(self, t):
+        self._check(self.lib.xavs2gpu_chain_set_tuning(self.h, ctypes.byref(t)), "chain_set_tuning")
+
+    def outputs(self):
+        o = ChainOutputs()
+        self._check(self.lib.xavs2gpu_chain_get_outputs(self.h, ctypes.byref(o)), "chain_get_outputs")
+        return o
 
 
 def set_limits(pus, width, height, vmin=-2048, vmax=2047):
@@ -319,3 +454,79 @@ def frame_pus(width, height, num_refs, mvp=(0, 0), vmin=-2048, vmax=2047):
                 rows.append(a)
     pus = np.concatenate(rows)
     return set_limits(pus, width, height, vmin, vmax)
+
+
+# ---- CU quadtree from a split map (full-frame chain) ------------------------
+CU_DTYPE = np.dtype([("x", "<i2"), ("y", "<i2"), ("size", "<i2"), ("pad_", "<i2"), ("pu", "<i4", (4,)),
+                     ("offset", "<i8"), ("coef_offset", "<i8")])
+_SQUARE_PART = {4: 0, 8: 1, 16: 2, 32: 3, 64: 4}
+
+
+def split_map_cus(width, height, seed, p_split=(0.5, 0.5, 0.5)):
+    """Leaf CUs (x, y, size) of every CTU from a seeded split map: a CU of
+    size 64/32/16 splits into four with probability p_split[depth]; a CU
+    that is not fully inside the picture always splits (8x8 CUs outside are
+    dropped), as the encoder's quadtree does at picture borders."""
+    rng = np.random.default_rng(seed)
+    out = []
+
+    def visit(x, y, n, depth):
+        inside = x + n <= width and y + n <= height
+        if x >= width or y >= height:
+            return
+        if n == 8:
+            if inside:
+                out.append((x, y, 8))
+            return
+        if not inside or rng.random() < p_split[depth]:
+            h = n // 2
+            for dy in (0, h):
+                for dx in (0, h):
+                    visit(x + dx, y + dy, h, depth + 1)
+        else:
+            out.append((x, y, n))
+
+    for y0 in range(0, height, 64):
+        for x0 in range(0, width, 64):
+            visit(x0, y0, 64, 0)
+    return out
+
+
+def cu_pus(cus, width, height, num_refs, mvp=(0, 0), with_4x4=False):
+    """The PUs an encoder searches for the leaf CUs `cus` (every partition
+    mode of the CU: 2Nx2N, 2NxN, Nx2N and the four AMP modes for 16..64;
+    8x8, 8x4, 4x8 for 8x8 CUs, plus 4x4 when `with_4x4`), for each
+    reference, and the CU records (CU_DTYPE) with the index of each CU's
+    2Nx2N PU per reference and packed residual / level offsets."""
+    rows = []
+    for (x, y, n) in cus:
+        if n == 8:
+            modes = [(x, y, 8, 8), (x, y, 8, 4), (x, y + 4, 8, 4), (x, y, 4, 8), (x + 4, y, 4, 8)]
+            if with_4x4:
+                modes += [(x, y, 4, 4), (x + 4, y, 4, 4), (x, y + 4, 4, 4), (x + 4, y + 4, 4, 4)]
+        else:
+            modes = _cu_modes(n, x, y)
+        rows.append(modes)
+    per_ref = sum(len(m) for m in rows)
+    pus = np.zeros(per_ref * num_refs, PU_DTYPE)
+    cu = np.zeros(len(cus), CU_DTYPE)
+    cu["pu"] = -1
+    flat = [t for m in rows for t in m]
+    xs = np.array([t[0] for t in flat], np.int16)
+    ys = np.array([t[1] for t in flat], np.int16)
+    parts = np.array([_part(t[2], t[3]) for t in flat], np.uint8)
+    first = np.cumsum([0] + [len(m) for m in rows])[:-1]
+    for r in range(num_refs):
+        sl = slice(r * per_ref, (r + 1) * per_ref)
+        pus["x"][sl], pus["y"][sl], pus["part"][sl], pus["ref"][sl] = xs, ys, parts, r
+        cu["pu"][:, r] = r * per_ref + first
+    pus["mvp_x"], pus["mvp_y"] = mvp
+    size = np.array([n for (_, _, n) in cus], np.int64)
+    cu["x"] = [c[0] for c in cus]
+    cu["y"] = [c[1] for c in cus]
+    cu["size"] = size
+    area = size * size
+    ncoef = np.where(size == 64, area // 4, area)
+    cu["offset"] = np.cumsum(area) - area
+    cu["coef_offset"] = np.cumsum(ncoef) - ncoef
+    return set_limits(pus, width, height), cu

@@ -46,14 +46,16 @@ struct CtuJob {
     int16_t x0, y0;       // CTU origin
     int16_t ref;
     int16_t mvp_x, mvp_y;
-    int16_t border;       // 1: limits may bind inside the window
-    int32_t slot_base;    // index of this job's row in the slot map
+    uint8_t border;       // 1: limits may bind inside the window
+    uint8_t sess;         // index into the session views of the launch
+    int32_t slot_base;    // index of this job's row in its session's slot map
 };
 
 struct CtuPlan {
     int n_jobs = 0, cap_jobs = 0;
     CtuJob *d_jobs = nullptr;
     int32_t *d_slots = nullptr;   // [n_jobs][kSlots]: PU index or -1
+    std::vector<CtuJob> h_jobs;   // host copy (sess = 0), for multi-session launches
 };
 
 // ---- slot geometry (host) --------------------------------------------------------
@@ -319,15 +321,19 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
 
 template <bool BORDER>
 __global__ void __launch_bounds__(kCtuThreads, 4) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
-                                                            const int32_t *__restrict__ slots,
-                                                            const uint8_t *__restrict__ cur,
-                                                            const uint8_t *const *refs, Geometry g, int R, int lambda,
-                                                            int ww, unsigned long long *__restrict__ keys)
+                                                            const SessView *__restrict__ views, int R, int lambda,
+                                                            int ww)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int job_idx = blockIdx.x / nchunks, chunk = blockIdx.x % nchunks;
     const CtuJob job = jobs[job_idx];
     if (BORDER != (job.border != 0)) return;
+    const SessView &view = views[job.sess];
+    const int32_t *__restrict__ slots = view.slots;
+    const uint8_t *__restrict__ cur = view.cur;
+    const uint8_t *const *refs = view.ref0;
+    const Geometry g = view.g;
+    unsigned long long *__restrict__ keys = view.keys;
     const int dy0 = -R + chunk * kDyChunk;
     const int wrows = 64 + kDyChunk - 1;
     const int nd = 2 * R;
@@ -552,6 +558,7 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
             // can the edge rule bind for any block of this CTU inside the window?
             cj.border = (cj.x0 - R < -kLimitMargin || cj.x0 + 64 + R > W + kLimitMargin ||
                          cj.y0 - R < -kLimitMargin || cj.y0 + 64 + R > H + kLimitMargin) ? 1 : 0;
+            cj.sess = 0;
             cj.slot_base = j * kSlots;
             jobs.push_back(cj);
             slots.resize(slots.size() + kSlots, -1);
@@ -569,6 +576,7 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
         XG_CUDA(cudaMalloc((void **)&p.d_slots, sizeof(int32_t) * kSlots * p.cap_jobs));
     }
     p.n_jobs = (int)jobs.size();
+    p.h_jobs = jobs;
     if (p.n_jobs) {
         XG_CUDA(cudaMemcpyAsync(p.d_jobs, jobs.data(), sizeof(CtuJob) * p.n_jobs, cudaMemcpyHostToDevice, st));
         XG_CUDA(cudaMemcpyAsync(p.d_slots, slots.data(), sizeof(int32_t) * slots.size(), cudaMemcpyHostToDevice, st));
@@ -584,30 +592,27 @@ static inline size_t ctu_smem_bytes(int R, int &ww)
     return sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
 }
 
-static void ctu_plan_run(const CtuPlan &p, const xavs2gpu_me_params_t &prm, const uint8_t *cur,
-                         const uint8_t *const *refs, const Geometry &g, const PuState *state,
-                         unsigned long long *keys, cudaStream_t st)
+// One launch of each variant over `n_jobs` jobs (sessions per job.sess).
+static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, const SessView *d_views, const xavs2gpu_me_params_t &prm,
+                         cudaStream_t st)
 {
-    (void)state;
-    if (p.n_jobs == 0) return;
+    if (n_jobs == 0) return;
     const int R = prm.search_range;
     int ww;
     const size_t smem = ctu_smem_bytes(R, ww);
-    static bool attr_done[8] = {false};
+    static bool attr_done[64] = {false};
     const int dev = current_device();
-    if (!attr_done[dev]) {
-        const int maxb = (int)ctu_smem_bytes(128, ww);
+    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
+        int ww_max;
+        const int maxb = (int)ctu_smem_bytes(128, ww_max);
         XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
         XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
         attr_done[dev] = true;
-        ctu_smem_bytes(R, ww);
     }
     const int nchunks = (2 * R + kDyChunk - 1) / kDyChunk;
-    const int grid = p.n_jobs * nchunks;
-    fs_ctu_kernel<false><<<grid, kCtuThreads, smem, st>>>(p.d_jobs, nchunks, p.d_slots, cur, refs, g, R,
-                                                          prm.lambda_factor, ww, keys);
-    fs_ctu_kernel<true><<<grid, kCtuThreads, smem, st>>>(p.d_jobs, nchunks, p.d_slots, cur, refs, g, R,
-                                                         prm.lambda_factor, ww, keys);
+    const int grid = n_jobs * nchunks;
+    fs_ctu_kernel<false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+    fs_ctu_kernel<true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
     count_launch(2);
 }
 

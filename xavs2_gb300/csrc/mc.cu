@@ -118,8 +118,8 @@ static inline int nblocks(int n, int t = 256) { int b = (n + t - 1) / t; return 
 // Every sample of plane k = 4*fy + fx at (x, y) equals the AVS2 filter
 // evaluated at (clamp(x, -4, W+3), clamp(y, -4, H+3)) with full-pel reads
 // clamped into the picture: the reference filters rows [-4, H+4) x columns
-// [-4, W+4) and replicates that region outwards.  Pass 1 computes that
-// region tile by tile; pass 2 replicates it into the padding.
+// [-4, W+4) and replicates that region outwards.  One kernel writes the
+// whole padded plane directly, so the replication costs no extra pass.
 __constant__ int8_t c_luma_taps[4][8] = {
     {0, 0, 0, 64, 0, 0, 0, 0},
     {-1, 4, -10, 57, 19, -7, 3, -1},
@@ -127,82 +127,198 @@ __constant__ int8_t c_luma_taps[4][8] = {
     {-1, 3, -7, 19, 57, -10, 4, -1},
 };
 
-constexpr int TW = 32, TH = 16;   // output tile
+constexpr int PT_W = 128, PT_H = 16;            // output tile of a padded plane
+constexpr int PS_R = PT_H + 7, PS_C = PT_W + 16; // source window (rows, pitch)
 
 struct PlaneSet { uint8_t *p[16]; };
 
-// 256 threads: each computes 2 vertically adjacent outputs of the tile for
-// every requested plane.
-__global__ void __launch_bounds__(256) frame_subpel_kernel(const uint8_t *__restrict__ src, int stride, int W, int H,
-                                                           PlaneSet planes, int mode)
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+// Stores the 4 bytes of `v` at p[0..3], only those with column < `end_col`
+// when the group straddles the right edge of the padded plane.
+template <bool VEC>
+__device__ __forceinline__ void store_group(uint8_t *p, uint32_t v, int x, int end_col)
 {
-    __shared__ uint8_t s_src[TH + 7][TW + 8];       // rows y0-3 .. y0+TH+3, cols x0-3 .. x0+TW+4
-    __shared__ int16_t s_hor[3][TH + 7][TW];        // raw horizontal sums for fx = 1..3
-    const int x0 = -4 + blockIdx.x * TW, y0 = -4 + blockIdx.y * TH;
-    const int tid = threadIdx.x;
-    for (int i = tid; i < (TH + 7) * (TW + 8); i += 256) {
-        int r = i / (TW + 8), c = i - r * (TW + 8);
-        int sy = min(max(y0 - 3 + r, 0), H - 1);
-        int sx = min(max(x0 - 3 + c, 0), W - 1);
-        s_src[r][c] = src[(size_t)sy * stride + sx];
+    if (VEC && x + 3 < end_col) {
+        *reinterpret_cast<uint32_t *>(p) = v;
+        return;
     }
-    __syncthreads();
-    for (int i = tid; i < 3 * (TH + 7) * TW; i += 256) {
-        int f = i / ((TH + 7) * TW), rem = i - f * (TH + 7) * TW;
-        int r = rem / TW, c = rem - r * TW;
-        int v = 0;
 #pragma unroll
-        for (int k = 0; k < 8; k++) v += c_luma_taps[f + 1][k] * s_src[r][c + k];
-        s_hor[f][r][c] = (int16_t)v;
+    for (int i = 0; i < 4; i++)
+        if (x + i < end_col) p[i] = (uint8_t)(v >> (8 * i));
+}
+
+// Phase 3 of frame_planes_kernel for one horizontal phase FX: the 4-column
+// group g of output rows [y0 + 8*half, y0 + 8*half + 8).
+template <int FX, bool VEC>
+__device__ __forceinline__ void planes_rows(const uint8_t (*s_src)[PS_C], const int16_t (*s_hor)[PS_R][PT_W],
+                                            const PlaneSet &planes, int stride, int W, int H, int pad, int x0,
+                                            int y0, int cx0, int cy0, int g, int half, int mode)
+{
+    const int xg = x0 + 4 * g;
+    const int end_col = W + pad;
+    if (xg >= end_col) return;
+    int lc[4];
+    bool contiguous = true;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        lc[c] = clampi(xg + c, -4, W + 3) - cx0;
+        contiguous &= lc[c] == 4 * g + c;
     }
-    __syncthreads();
-    const int tx = tid & (TW - 1), ty = (tid >> 5) * 2;
-    const int X = x0 + tx;
-    if (X >= W + 4) return;
+    // window element (row j, column c): the source byte at column lc+3 for
+    // FX == 0, else the raw horizontal sum of phase FX
+    auto fetch = [&](int row, int (&dst)[4]) {
+        if (FX == 0) {
 #pragma unroll
-    for (int dy = 0; dy < 2; dy++) {
-        const int r = ty + dy, Y = y0 + r;
-        if (Y >= H + 4) break;
-        const size_t o = (ptrdiff_t)Y * stride + X;
+            for (int c = 0; c < 4; c++) dst[c] = s_src[row][lc[c] + 3];
+        } else if (contiguous) {
+            const uint2 pk = *reinterpret_cast<const uint2 *>(&s_hor[FX - 1][row][4 * g]);
+            dst[0] = (int16_t)(pk.x & 0xFFFF); dst[1] = (int16_t)(pk.x >> 16);
+            dst[2] = (int16_t)(pk.y & 0xFFFF); dst[3] = (int16_t)(pk.y >> 16);
+        } else {
 #pragma unroll
-        for (int k = 1; k < 16; k++) {
-            if (mode < 2 && !(k == 2 || k == 8 || k == 10)) continue;
-            const int fx = k & 3, fy = k >> 2;
-            int v = 0;
-            uint8_t out;
-            if (fy == 0) {
-                out = clip_pel_d((s_hor[fx - 1][r + 3][tx] + 32) >> 6);
-            } else if (fx == 0) {
+            for (int c = 0; c < 4; c++) dst[c] = s_hor[FX - 1][row][lc[c]];
+        }
+    };
+    const int ys = y0 + 8 * half;
+    int cur = clampi(ys, -4, H + 3) - cy0;
+    int win[8][4];
 #pragma unroll
-                for (int j = 0; j < 8; j++) v += c_luma_taps[fy][j] * s_src[r + j][tx + 3];
-                out = clip_pel_d((v + 32) >> 6);
-            } else {
+    for (int j = 0; j < 8; j++) fetch(cur + j, win[j]);
+    uint32_t out[4] = {0, 0, 0, 0};
+    bool have = false;
 #pragma unroll
-                for (int j = 0; j < 8; j++) v += c_luma_taps[fy][j] * s_hor[fx - 1][r + j][tx];
-                out = clip_pel_d((v + 2048) >> 12);
+    for (int t = 0; t < 8; t++) {
+        const int y = ys + t;
+        if (y >= H + pad) break;
+        const int l = clampi(y, -4, H + 3) - cy0;
+        if (l != cur) {
+#pragma unroll
+            for (int j = 0; j < 7; j++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) win[j][c] = win[j + 1][c];
+            fetch(l + 7, win[7]);
+            cur = l;
+            have = false;
+        }
+        if (!have) {
+#pragma unroll
+            for (int fy = 0; fy < 4; fy++) {
+                if (FX == 0 && fy == 0) continue;
+                if (mode < 2 && fy != 0 && fy != 2) continue;
+                uint32_t pk = 0;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    int v;
+                    if (fy == 0) {
+                        v = (win[3][c] + 32) >> 6;
+                    } else {
+                        int s = 0;
+#pragma unroll
+                        for (int j = 0; j < 8; j++) s += c_luma_taps[fy][j] * win[j][c];
+                        v = FX == 0 ? (s + 32) >> 6 : (s + 2048) >> 12;
+                    }
+                    pk |= (uint32_t)clip_pel_d(v) << (8 * c);
+                }
+                out[fy] = pk;
             }
-            planes.p[k][o] = out;
+            have = true;
+        }
+        const ptrdiff_t ro = (ptrdiff_t)y * stride + xg;
+#pragma unroll
+        for (int fy = 0; fy < 4; fy++) {
+            if (FX == 0 && fy == 0) continue;
+            if (mode < 2 && fy != 0 && fy != 2) continue;
+            store_group<VEC>(planes.p[4 * fy + FX] + ro, out[fy], xg, end_col);
         }
     }
 }
 
-// Pass 2: replicate the computed region [-4, W+4) x [-4, H+4) of each
-// requested plane into [-pad, W+pad) x [-pad, H+pad).  `lo`/`hi` give the
-// region that is already valid (lo = -4, hi = W+4 / H+4 for sub-pel planes,
-// 0 / W / H for a full-pel plane).
-__global__ void expand_kernel(PlaneSet planes, int nplanes_mask, int stride, int W, int H, int pad, int lox, int hix,
-                              int loy, int hiy)
+// One CTA writes a 128 x 16 tile of every requested sub-pel plane over the
+// whole padded area [-pad, W+pad) x [-pad, H+pad).  The sample at (x, y) is
+// the filter output at (cx, cy) = (clamp(x, -4, W+3), clamp(y, -4, H+3)), so
+// the tile only needs the clamped columns [cx(x0), cx(x0+127)] and rows
+// [cy(y0), cy(y0+15)] (at most 128 x 16 distinct values).
+//   phase 1: source window (clamped reads) -> shared memory;
+//   phase 2: raw horizontal 8-tap sums for fx = 1..3, 4 columns per item;
+//   phase 3: thread = (row half, fx, 4-column group): slides an 8-row window
+//            down its 8 output rows and emits planes 4*fy + fx for fy = 0..3
+//            as 32-bit stores (a warp writes 128 contiguous bytes of a row).
+template <bool VEC>
+__global__ void __launch_bounds__(256) frame_planes_kernel(const uint8_t *__restrict__ src, int stride, int W, int H,
+                                                           int pad, PlaneSet planes, int mode)
 {
-    const int PW = W + 2 * pad, PH = H + 2 * pad;
-    const int64_t total = (int64_t)PW * PH;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        int y = (int)(i / PW) - pad, x = (int)(i % PW) - pad;
-        int cx = min(max(x, lox), hix - 1), cy = min(max(y, loy), hiy - 1);
-        if (cx == x && cy == y) continue;
-        for (int k = 0; k < 16; k++) {
-            if (!((nplanes_mask >> k) & 1)) continue;
-            uint8_t *p = planes.p[k];
-            p[(ptrdiff_t)y * stride + x] = p[(ptrdiff_t)cy * stride + cx];
+    __shared__ __align__(16) uint8_t s_src[PS_R][PS_C];
+    __shared__ __align__(16) int16_t s_hor[3][PS_R][PT_W];
+    const int x0 = -pad + blockIdx.x * PT_W, y0 = -pad + blockIdx.y * PT_H;
+    const int cx0 = clampi(x0, -4, W + 3), cy0 = clampi(y0, -4, H + 3);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < PS_R * (PT_W + 8); i += 256) {
+        const int r = i / (PT_W + 8), m = i - r * (PT_W + 8);
+        const int sy = clampi(cy0 - 3 + r, 0, H - 1), sx = clampi(cx0 - 3 + m, 0, W - 1);
+        s_src[r][m] = src[(ptrdiff_t)sy * stride + sx];
+    }
+    __syncthreads();
+    for (int i = tid; i < PS_R * (PT_W / 4); i += 256) {
+        const int r = i / (PT_W / 4), g = i - r * (PT_W / 4);
+        const uint32_t *w = reinterpret_cast<const uint32_t *>(&s_src[r][4 * g]);
+        int b[12];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const uint32_t v = w[q];
+#pragma unroll
+            for (int e = 0; e < 4; e++) b[4 * q + e] = (v >> (8 * e)) & 0xFF;
+        }
+#pragma unroll
+        for (int f = 0; f < 3; f++) {
+            if (mode < 2 && f != 1) continue;
+            int o[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                int v = 0;
+#pragma unroll
+                for (int k = 0; k < 8; k++) v += c_luma_taps[f + 1][k] * b[c + k];
+                o[c] = v;
+            }
+            uint2 pk;
+            pk.x = (uint32_t)(o[0] & 0xFFFF) | ((uint32_t)o[1] << 16);
+            pk.y = (uint32_t)(o[2] & 0xFFFF) | ((uint32_t)o[3] << 16);
+            *reinterpret_cast<uint2 *>(&s_hor[f][r][4 * g]) = pk;
+        }
+    }
+    __syncthreads();
+    const int g = tid & 31, fx = (tid >> 5) & 3, half = tid >> 7;
+    switch (fx) {
+    case 0: planes_rows<0, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
+    case 1: if (mode == 2) planes_rows<1, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
+    case 2: planes_rows<2, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
+    default: if (mode == 2) planes_rows<3, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
+    }
+}
+
+// Writes the padding of a full-pel plane: (x, y) outside [0, W) x [0, H)
+// takes the sample at (clamp(x, 0, W-1), clamp(y, 0, H-1)) (plane_expand_border,
+// frame.c:471-507).  One grid row per picture row; 4 columns per thread.
+template <bool VEC>
+__global__ void expand_plane_kernel(uint8_t *pix, int stride, int W, int H, int pad)
+{
+    const int groups = (W + 2 * pad + 3) / 4, end_col = W + pad;
+    const int y = -pad + (int)blockIdx.y;
+    const bool inner_row = y >= 0 && y < H;
+    const uint8_t *srow = pix + (ptrdiff_t)clampi(y, 0, H - 1) * stride;
+    uint8_t *drow = pix + (ptrdiff_t)y * stride;
+    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < groups; gi += gridDim.x * blockDim.x) {
+        const int x = -pad + 4 * gi;
+        if (inner_row && x >= 0 && x + 3 < W) continue;
+        uint32_t v = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) v |= (uint32_t)srow[clampi(x + c, 0, W - 1)] << (8 * c);
+        if (!inner_row) {
+            store_group<VEC>(drow + x, v, x, end_col);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                if ((x + c < 0 || x + c >= W) && x + c < end_col) drow[x + c] = (uint8_t)(v >> (8 * c));
         }
     }
 }
@@ -400,13 +516,14 @@ extern "C" int xavs2gpu_interpolate_frame(const uint8_t *src, int stride, int wi
         }
     }
     cudaStream_t st = (cudaStream_t)stream;
-    dim3 grid((width + 8 + TW - 1) / TW, (height + 8 + TH - 1) / TH);
-    frame_subpel_kernel<<<grid, 256, 0, st>>>(src, stride, width, height, ps, mode);
-    count_launch();
-    int64_t total = (int64_t)(width + 2 * pad) * (height + 2 * pad);
-    int blocks = (int)((total + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    expand_kernel<<<blocks, 256, 0, st>>>(ps, mask, stride, width, height, pad, -4, width + 4, -4, height + 4);
+    bool vec = stride % 4 == 0;
+    for (int k = 1; k < 16; k++)
+        if ((mask >> k) & 1) vec &= ((uintptr_t)planes[k] - (uintptr_t)pad) % 4 == 0;
+    dim3 grid((width + 2 * pad + PT_W - 1) / PT_W, (height + 2 * pad + PT_H - 1) / PT_H);
+    if (vec)
+        frame_planes_kernel<true><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode);
+    else
+        frame_planes_kernel<false><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode);
     count_launch();
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
@@ -418,13 +535,13 @@ extern "C" int xavs2gpu_expand_border(uint8_t *pix, int stride, int width, int h
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_expand_border", "bad geometry");
         return XAVS2GPU_ERR_ARG;
     }
-    PlaneSet ps;
-    memset(&ps, 0, sizeof(ps));
-    ps.p[0] = pix;
-    int64_t total = (int64_t)(width + 2 * pad) * (height + 2 * pad);
-    int blocks = (int)((total + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    expand_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(ps, 1, stride, width, height, pad, 0, width, 0, height);
+    const bool vec = stride % 4 == 0 && ((uintptr_t)pix - (uintptr_t)pad) % 4 == 0;
+    const int groups = (width + 2 * pad + 3) / 4;
+    dim3 grid((groups + 255) / 256, height + 2 * pad);
+    if (vec)
+        expand_plane_kernel<true><<<grid, 256, 0, (cudaStream_t)stream>>>(pix, stride, width, height, pad);
+    else
+        expand_plane_kernel<false><<<grid, 256, 0, (cudaStream_t)stream>>>(pix, stride, width, height, pad);
     count_launch();
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;

@@ -38,6 +38,24 @@ struct Geometry {
     int W, H, stride;
 };
 
+// What the kernels read of one motion-search session.  A launch may cover
+// several sessions (pictures of different sizes): work-list entries carry
+// the session's index in their top 8 bits and the PU index below.
+struct SessView {
+    const uint8_t *cur;             // current picture, pixel (0,0)
+    const uint8_t *const *ref0;     // [nrefs] full-pel reference planes
+    const uint8_t *const *planes;   // [nrefs * 16] sub-pel planes (16 r + k)
+    const xavs2gpu_pu_t *pus;
+    PuState *state;
+    unsigned long long *keys;
+    xavs2gpu_me_result_t *res;
+    const int32_t *slots;           // CTU slot map
+    Geometry g;
+    int n;                          // PUs
+};
+constexpr int kSessShift = 24;
+constexpr uint32_t kIdxMask = (1u << kSessShift) - 1;
+
 __device__ __forceinline__ int sad_block_lane(const uint8_t *a, int sa, const uint8_t *b, int sb, int w, int h, int lane)
 {
     int s = 0;
@@ -112,31 +130,43 @@ __global__ void __launch_bounds__(128) me_init_kernel(const xavs2gpu_pu_t *__res
     init_one(i, lane, pus, cur, refs, g, lambda, state, keys);
 }
 
-// Same over an index list (the PUs outside the CTU plan).
-__global__ void __launch_bounds__(128) me_init_list_kernel(const int *__restrict__ list, int n,
-                                                           const xavs2gpu_pu_t *__restrict__ pus,
-                                                           const uint8_t *__restrict__ cur, const uint8_t *const *refs,
-                                                           Geometry g, int lambda, PuState *__restrict__ state,
-                                                           unsigned long long *__restrict__ keys)
+// Same over a session-tagged list (the PUs outside the CTU plan).
+__global__ void __launch_bounds__(128) me_init_list_kernel(const uint32_t *__restrict__ list, int n,
+                                                           const SessView *__restrict__ views, int lambda)
 {
     const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (t >= n) return;
-    init_one(list[t], lane, pus, cur, refs, g, lambda, state, keys);
+    const uint32_t e = list[t];
+    const SessView &v = views[e >> kSessShift];
+    init_one((int)(e & kIdxMask), lane, v.pus, v.cur, v.ref0, v.g, lambda, v.state, v.keys);
+}
+
+// keys := no key, for every PU of every session of the launch
+__global__ void reset_keys_kernel(const SessView *__restrict__ views, int nviews)
+{
+    for (int s = 0; s < nviews; s++) {
+        const SessView &v = views[s];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x) v.keys[i] = kNoKey;
+    }
 }
 
 // ---- 2b. per-PU full search (one CTA per PU) --------------------------------------
 // Visit order of window position (i, j) is 2 + (j+R)*2R + (i+R).
-__global__ void __launch_bounds__(256) fs_generic_kernel(const int *__restrict__ list, int n,
-                                                         const xavs2gpu_pu_t *__restrict__ pus,
-                                                         const PuState *__restrict__ state,
-                                                         const uint8_t *__restrict__ cur, const uint8_t *const *refs,
-                                                         Geometry g, int R, int lambda,
-                                                         unsigned long long *__restrict__ keys)
+__global__ void __launch_bounds__(256) fs_generic_kernel(const uint32_t *__restrict__ list, int n,
+                                                         const SessView *__restrict__ views, int R, int lambda)
 {
     __shared__ uint8_t s_cur[64 * 64];
     __shared__ unsigned long long s_red[8];
     for (int li = blockIdx.x; li < n; li += gridDim.x) {
-        const int i = list[li];
+        const uint32_t e = list[li];
+        const SessView &v = views[e >> kSessShift];
+        const int i = (int)(e & kIdxMask);
+        const xavs2gpu_pu_t *__restrict__ pus = v.pus;
+        const PuState *__restrict__ state = v.state;
+        const uint8_t *__restrict__ cur = v.cur;
+        const uint8_t *const *refs = v.ref0;
+        const Geometry g = v.g;
+        unsigned long long *__restrict__ keys = v.keys;
         const xavs2gpu_pu_t p = pus[i];
         const PuState st = state[i];
         if (!st.valid) continue;
@@ -531,18 +561,22 @@ __device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, c
     }
 }
 
-__global__ void __launch_bounds__(128) refine_thread_kernel(const int *__restrict__ list, int n,
-                                                            const xavs2gpu_pu_t *__restrict__ pus,
-                                                            const PuState *__restrict__ state,
-                                                            const unsigned long long *__restrict__ keys,
-                                                            const uint8_t *__restrict__ cur,
-                                                            const uint8_t *const *ref_planes, Geometry g, int R,
-                                                            xavs2gpu_me_params_t prm,
-                                                            xavs2gpu_me_result_t *__restrict__ out)
+__global__ void __launch_bounds__(128) refine_thread_kernel(const uint32_t *__restrict__ list, int n,
+                                                            const SessView *__restrict__ views, int R,
+                                                            xavs2gpu_me_params_t prm)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    const int i = list[t];
+    const uint32_t e = list[t];
+    const SessView &v = views[e >> kSessShift];
+    const int i = (int)(e & kIdxMask);
+    const xavs2gpu_pu_t *__restrict__ pus = v.pus;
+    const PuState *__restrict__ state = v.state;
+    const unsigned long long *__restrict__ keys = v.keys;
+    const uint8_t *__restrict__ cur = v.cur;
+    const uint8_t *const *ref_planes = v.planes;
+    const Geometry g = v.g;
+    xavs2gpu_me_result_t *__restrict__ out = v.res;
     const xavs2gpu_pu_t p = pus[i];
     const PuState st = state[i];
     const unsigned long long key = keys[i];
@@ -625,18 +659,22 @@ __global__ void __launch_bounds__(128) refine_thread_kernel(const int *__restric
 }
 
 // One warp per search for the larger PUs, over a list.
-__global__ void __launch_bounds__(128) refine_warp_list_kernel(const int *__restrict__ list, int n,
-                                                               const xavs2gpu_pu_t *__restrict__ pus,
-                                                               const PuState *__restrict__ state,
-                                                               const unsigned long long *__restrict__ keys,
-                                                               const uint8_t *__restrict__ cur,
-                                                               const uint8_t *const *ref_planes, Geometry g, int R,
-                                                               xavs2gpu_me_params_t prm,
-                                                               xavs2gpu_me_result_t *__restrict__ out)
+__global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *__restrict__ list, int n,
+                                                               const SessView *__restrict__ views, int R,
+                                                               xavs2gpu_me_params_t prm)
 {
     const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (wt >= n) return;
-    const int i = list[wt];
+    const uint32_t e = list[wt];
+    const SessView &v = views[e >> kSessShift];
+    const int i = (int)(e & kIdxMask);
+    const xavs2gpu_pu_t *__restrict__ pus = v.pus;
+    const PuState *__restrict__ state = v.state;
+    const unsigned long long *__restrict__ keys = v.keys;
+    const uint8_t *__restrict__ cur = v.cur;
+    const uint8_t *const *ref_planes = v.planes;
+    const Geometry g = v.g;
+    xavs2gpu_me_result_t *__restrict__ out = v.res;
     const xavs2gpu_pu_t p = pus[i];
     const PuState st = state[i];
     const unsigned long long key = keys[i];
@@ -739,9 +777,52 @@ struct MeSessionImpl {
     int n_small = 0, n_large = 0;
     bool profiling = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // launch shapes (results do not depend on them): searches of at most
+    // tune_split pixels refine one per thread, larger ones one per warp;
+    // tune_block threads per refinement CTA
+    int tune_split = 256, tune_block = 128;
+    // reference slot r lives in plane buffer set slot_buf[r] (rotated by
+    // xavs2gpu_me_rotate_refs without moving pixels)
+    int slot_buf[16] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15};
+    cudaStream_t own_st = nullptr;   // the stream the session created
+    SessView h_view{};
+    SessView *d_view = nullptr;      // this session as the kernels see it
+    std::vector<uint32_t> h_generic, h_small, h_large;
 
     uint8_t *plane(int idx) { return d_planes + (size_t)idx * plane_bytes + (size_t)kPad * stride + kPad; }
+    uint8_t *ref_plane(int slot, int k) { return plane(1 + 16 * slot_buf[slot] + k); }
 };
+
+// Uploads the plane pointer tables of the current slot assignment and the
+// session view (stream-ordered).
+static void refresh_tables(MeSessionImpl &m)
+{
+    std::vector<uint8_t *> ptrs(1 + 16 * m.nrefs);
+    ptrs[0] = m.plane(0);
+    for (int r = 0; r < m.nrefs; r++)
+        for (int k = 0; k < 16; k++) ptrs[1 + 16 * r + k] = m.ref_plane(r, k);
+    std::vector<const uint8_t *> r0(m.nrefs);
+    for (int r = 0; r < m.nrefs; r++) r0[r] = m.ref_plane(r, 0);
+    XG_CUDA(cudaMemcpyAsync(m.d_plane_ptrs, ptrs.data(), sizeof(uint8_t *) * ptrs.size(), cudaMemcpyHostToDevice, m.st));
+    XG_CUDA(cudaMemcpyAsync(m.d_ref0, r0.data(), sizeof(uint8_t *) * r0.size(), cudaMemcpyHostToDevice, m.st));
+}
+
+static void refresh_view(MeSessionImpl &m)
+{
+    SessView v;
+    v.cur = m.plane(0);
+    v.ref0 = m.d_ref0;
+    v.planes = (const uint8_t *const *)(m.d_plane_ptrs + 1);
+    v.pus = m.d_pus;
+    v.state = m.d_state;
+    v.keys = m.d_keys;
+    v.res = m.d_res;
+    v.slots = m.plan.d_slots;
+    v.g = Geometry{m.W, m.H, m.stride};
+    v.n = m.n;
+    m.h_view = v;
+    XG_CUDA(cudaMemcpyAsync(m.d_view, &m.h_view, sizeof(SessView), cudaMemcpyHostToDevice, m.st));
+}
 
 }  // namespace xg
 
@@ -766,7 +847,8 @@ extern "C" void xavs2gpu_pu_set_limits(xavs2gpu_pu_t *pu, int width, int height,
 
 extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int num_refs, int max_pus)
 {
-    if (width < 8 || height < 8 || width > 8192 || height > 8192 || num_refs < 1 || num_refs > 16 || max_pus < 1) {
+    if (width < 8 || height < 8 || width > 8192 || height > 8192 || num_refs < 1 || num_refs > 16 || max_pus < 1 ||
+        max_pus > (int)kIdxMask) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_create", "bad size, reference count or PU capacity");
         return nullptr;
     }
@@ -779,7 +861,8 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     m.rows = height + 2 * kPad;
     m.plane_bytes = align_up((size_t)m.stride * m.rows, 256);
     const int nplanes = 1 + 16 * num_refs;
-    XG_CUDA(cudaStreamCreateWithFlags(&m.st, cudaStreamNonBlocking));
+    XG_CUDA(cudaStreamCreateWithFlags(&m.own_st, cudaStreamNonBlocking));
+    m.st = m.own_st;
     XG_CUDA(cudaMalloc((void **)&m.d_planes, m.plane_bytes * nplanes));
     XG_CUDA(cudaMemsetAsync(m.d_planes, 0, m.plane_bytes * nplanes, m.st));
     std::vector<uint8_t *> ptrs(nplanes);
@@ -803,6 +886,8 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     XG_CUDA(cudaMalloc((void **)&m.d_tasks, sizeof(RefineTask) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_small, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_large, sizeof(int) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_view, sizeof(SessView)));
+    refresh_view(m);
     XG_CUDA(cudaStreamSynchronize(m.st));
     return s;
 }
@@ -813,6 +898,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     MeSessionImpl &m = s->impl;
     cudaSetDevice(m.device);
     if (m.st) cudaStreamSynchronize(m.st);
+    cudaFree(m.d_view);
     ctu_plan_free(m.plan);
     cudaFree(m.d_planes); cudaFree(m.d_plane_ptrs); cudaFree(m.d_ref0);
     cudaFreeHost(m.h_stage); cudaFree(m.d_upload);
@@ -821,7 +907,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     cudaFree(m.d_small); cudaFree(m.d_large);
     for (auto &e : m.ev)
         if (e) cudaEventDestroy(e);
-    if (m.st) cudaStreamDestroy(m.st);
+    if (m.own_st) cudaStreamDestroy(m.own_st);
     delete s;
 }
 
@@ -829,7 +915,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
 // replicates its border; for references also computes the 15 sub-pel planes
 static int load_picture(MeSessionImpl &m, int slot, const uint8_t *dsrc, intptr_t stride)
 {
-    const int idx = slot < 0 ? 0 : 1 + 16 * slot;
+    const int idx = slot < 0 ? 0 : 1 + 16 * m.slot_buf[slot];
     XG_CUDA(cudaMemcpy2DAsync(m.plane(idx), m.stride, dsrc, stride, m.W, m.H, cudaMemcpyDeviceToDevice, m.st));
     if (xavs2gpu_expand_border(m.plane(idx), m.stride, m.W, m.H, kPad, m.st) != XAVS2GPU_OK) return XAVS2GPU_ERR_CUDA;
     if (slot >= 0) {
@@ -891,6 +977,7 @@ extern "C" int xavs2gpu_me_set_pus(xavs2gpu_me_session_t *s, const xavs2gpu_pu_t
     m.h_pus.assign(pus, pus + n);
     XG_CUDA(cudaStreamSynchronize(m.st));
     if (n) XG_CUDA(cudaMemcpyAsync(m.d_pus, pus, sizeof(xavs2gpu_pu_t) * n, cudaMemcpyHostToDevice, m.st));
+    refresh_view(m);
     XG_CUDA(cudaStreamSynchronize(m.st));
     m.plan_R = -1;
     return XAVS2GPU_OK;
@@ -904,6 +991,7 @@ static void ensure_plan(MeSessionImpl &m, int R)
     ctu_plan_build(m.plan, m.h_pus, m.W, m.H, m.nrefs, R, generic, m.st);
     m.n_generic = (int)generic.size();
     m.n_ctu_pus = m.n - m.n_generic;
+    m.h_generic.assign(generic.begin(), generic.end());
     if (m.n_generic)
         XG_CUDA(cudaMemcpyAsync(m.d_generic, generic.data(), sizeof(int) * m.n_generic, cudaMemcpyHostToDevice, m.st));
     // PUs of the CTU plan have the single candidate (0,0), which is also the
@@ -946,15 +1034,18 @@ static void ensure_plan(MeSessionImpl &m, int R)
     std::vector<int> small, large;
     for (int k = 0; k < m.n; k++) {
         const int i = order[k];
-        (h_pu_w[m.h_pus[i].part] * h_pu_h[m.h_pus[i].part] <= 256 ? small : large).push_back(i);
+        (h_pu_w[m.h_pus[i].part] * h_pu_h[m.h_pus[i].part] <= m.tune_split ? small : large).push_back(i);
     }
     m.n_small = (int)small.size();
     m.n_large = (int)large.size();
+    m.h_small.assign(small.begin(), small.end());
+    m.h_large.assign(large.begin(), large.end());
     if (m.n_small) XG_CUDA(cudaMemcpyAsync(m.d_small, small.data(), sizeof(int) * m.n_small, cudaMemcpyHostToDevice, m.st));
     if (m.n_large) XG_CUDA(cudaMemcpyAsync(m.d_large, large.data(), sizeof(int) * m.n_large, cudaMemcpyHostToDevice, m.st));
     if (m.n) XG_CUDA(cudaMemcpyAsync(m.d_order, order.data(), sizeof(int) * m.n, cudaMemcpyHostToDevice, m.st));
     if (m.n_tasks)
         XG_CUDA(cudaMemcpyAsync(m.d_tasks, tasks.data(), sizeof(RefineTask) * m.n_tasks, cudaMemcpyHostToDevice, m.st));
+    refresh_view(m);
     XG_CUDA(cudaStreamSynchronize(m.st));
     m.plan_R = R;
 }
@@ -969,40 +1060,86 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     MeSessionImpl &m = s->impl;
     if (m.n == 0) return XAVS2GPU_OK;
     XG_CUDA(cudaSetDevice(m.device));
-    Geometry g{m.W, m.H, m.stride};
     const int R = prm->search_range, lam = prm->lambda_factor;
     ensure_plan(m, R);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[0], m.st));
     XG_CUDA(cudaMemsetAsync(m.d_keys, 0xff, sizeof(unsigned long long) * m.n, m.st));
+    const uint32_t *gen = reinterpret_cast<const uint32_t *>(m.d_generic);
     if (m.n_generic) {
-        me_init_list_kernel<<<(m.n_generic * 32 + 127) / 128, 128, 0, m.st>>>(
-            m.d_generic, m.n_generic, m.d_pus, m.plane(0), m.d_ref0, g, lam, m.d_state, m.d_keys);
+        me_init_list_kernel<<<(m.n_generic * 32 + 127) / 128, 128, 0, m.st>>>(gen, m.n_generic, m.d_view, lam);
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[1], m.st));
-    ctu_plan_run(m.plan, *prm, m.plane(0), m.d_ref0, g, m.d_state, m.d_keys, m.st);
+    ctu_jobs_run(m.plan.d_jobs, m.plan.n_jobs, m.d_view, *prm, m.st);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
     if (m.n_generic) {
         int grid = m.n_generic < 152 * 8 ? m.n_generic : 152 * 8;
-        fs_generic_kernel<<<grid, 256, 0, m.st>>>(m.d_generic, m.n_generic, m.d_pus, m.d_state, m.plane(0), m.d_ref0,
-                                                  g, R, lam, m.d_keys);
+        fs_generic_kernel<<<grid, 256, 0, m.st>>>(gen, m.n_generic, m.d_view, R, lam);
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
     if (m.n_small) {
-        refine_thread_kernel<<<(m.n_small + 127) / 128, 128, 0, m.st>>>(
-            m.d_small, m.n_small, m.d_pus, m.d_state, m.d_keys, m.plane(0),
-            (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm, m.d_res);
+        refine_thread_kernel<<<(m.n_small + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
+            reinterpret_cast<const uint32_t *>(m.d_small), m.n_small, m.d_view, R, *prm);
         count_launch();
     }
     if (m.n_large) {
-        refine_warp_list_kernel<<<(m.n_large * 32 + 127) / 128, 128, 0, m.st>>>(
-            m.d_large, m.n_large, m.d_pus, m.d_state, m.d_keys, m.plane(0),
-            (const uint8_t *const *)(m.d_plane_ptrs + 1), g, R, *prm, m.d_res);
+        refine_warp_list_kernel<<<(m.n_large * 32 + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
+            reinterpret_cast<const uint32_t *>(m.d_large), m.n_large, m.d_view, R, *prm);
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[4], m.st));
     XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+extern "C" void xavs2gpu_me_session_info(const xavs2gpu_me_session_t *s, int *width, int *height, int *num_refs,
+                                         int *n_pus)
+{
+    if (!s) return;
+    if (width) *width = s->impl.W;
+    if (height) *height = s->impl.H;
+    if (num_refs) *num_refs = s->impl.nrefs;
+    if (n_pus) *n_pus = s->impl.n;
+}
+
+extern "C" int xavs2gpu_me_session_pus(const xavs2gpu_me_session_t *s, xavs2gpu_pu_t *out)
+{
+    if (!s || !out) return XAVS2GPU_ERR_ARG;
+    for (int i = 0; i < s->impl.n; i++) out[i] = s->impl.h_pus[i];
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_me_set_tuning(xavs2gpu_me_session_t *s, const xavs2gpu_me_tuning_t *t)
+{
+    if (!s || !t || t->refine_split_px < 0 || t->refine_split_px > 4096 ||
+        (t->refine_block != 32 && t->refine_block != 64 && t->refine_block != 128)) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_tuning", "refine_split_px must be 0..4096, refine_block 32/64/128");
+        return XAVS2GPU_ERR_ARG;
+    }
+    MeSessionImpl &m = s->impl;
+    if (t->refine_split_px != m.tune_split) m.plan_R = -1;   // the refinement lists change
+    m.tune_split = t->refine_split_px;
+    m.tune_block = t->refine_block;
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_me_get_tuning(const xavs2gpu_me_session_t *s, xavs2gpu_me_tuning_t *t)
+{
+    if (!s || !t) return XAVS2GPU_ERR_ARG;
+    t->refine_split_px = s->impl.tune_split;
+    t->refine_block = s->impl.tune_block;
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_me_prepare(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm)
+{
+    if (!s || !prm || prm->search_range < 1 || prm->search_range > 128) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_prepare", "bad parameters");
+        return XAVS2GPU_ERR_ARG;
+    }
+    XG_CUDA(cudaSetDevice(s->impl.device));
+    ensure_plan(s->impl, prm->search_range);
     return XAVS2GPU_OK;
 }
 
@@ -1053,7 +1190,7 @@ extern "C" const xavs2gpu_me_result_t *xavs2gpu_me_results_device(xavs2gpu_me_se
 extern "C" uint8_t *xavs2gpu_me_plane_device(xavs2gpu_me_session_t *s, int slot, int k)
 {
     if (!s || slot < -1 || slot >= s->impl.nrefs || k < 0 || k > 15 || (slot < 0 && k != 0)) return nullptr;
-    return s->impl.plane(slot < 0 ? 0 : 1 + 16 * slot + k);
+    return slot < 0 ? s->impl.plane(0) : s->impl.ref_plane(slot, k);
 }
 
 extern "C" int xavs2gpu_me_plane_stride(xavs2gpu_me_session_t *s) { return s ? s->impl.stride : 0; }
@@ -1083,6 +1220,157 @@ extern "C" void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus,
     if (n_ctu_jobs) *n_ctu_jobs = s->impl.plan.n_jobs;
 }
 
+// ---- several sessions per launch ------------------------------------------------
+extern "C" int xavs2gpu_me_set_stream(xavs2gpu_me_session_t *s, void *stream)
+{
+    if (!s) return XAVS2GPU_ERR_ARG;
+    MeSessionImpl &m = s->impl;
+    m.st = stream ? (cudaStream_t)stream : m.own_st;
+    return XAVS2GPU_OK;
+}
+
+extern "C" const uint8_t *const *xavs2gpu_me_plane_table_device(xavs2gpu_me_session_t *s)
+{
+    return s ? (const uint8_t *const *)(s->impl.d_plane_ptrs + 1) : nullptr;
+}
+
+extern "C" int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s)
+{
+    if (!s) return XAVS2GPU_ERR_ARG;
+    MeSessionImpl &m = s->impl;
+    XG_CUDA(cudaSetDevice(m.device));
+    const int last = m.slot_buf[m.nrefs - 1];
+    for (int r = m.nrefs - 1; r > 0; r--) m.slot_buf[r] = m.slot_buf[r - 1];
+    m.slot_buf[0] = last;
+    refresh_tables(m);
+    return XAVS2GPU_OK;
+}
+
+struct BatchBuf {
+    CtuJob *d_jobs = nullptr;
+    uint32_t *d_lists = nullptr;    // generic | small | large
+    SessView *d_views = nullptr;
+    size_t cap_jobs = 0, cap_lists = 0, cap_views = 0;
+    cudaEvent_t done = nullptr;
+    bool used = false;
+};
+
+struct xavs2gpu_me_batch {
+    int device = 0;
+    BatchBuf buf[2];
+    int next = 0;
+    std::vector<CtuJob> jobs;
+    std::vector<uint32_t> lists;
+    std::vector<SessView> views;
+};
+
+extern "C" xavs2gpu_me_batch_t *xavs2gpu_me_batch_create(void)
+{
+    auto *b = new xavs2gpu_me_batch();
+    b->device = current_device();
+    for (auto &x : b->buf) XG_CUDA(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+    return b;
+}
+
+extern "C" void xavs2gpu_me_batch_destroy(xavs2gpu_me_batch_t *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    for (auto &x : b->buf) {
+        if (x.used) cudaEventSynchronize(x.done);
+        cudaEventDestroy(x.done);
+        cudaFree(x.d_jobs); cudaFree(x.d_lists); cudaFree(x.d_views);
+    }
+    delete b;
+}
+
+template <typename T>
+static void grow(T *&p, size_t &cap, size_t need)
+{
+    if (need <= cap) return;
+    cudaFree(p);
+    cap = need + need / 4 + 64;
+    XG_CUDA(cudaMalloc((void **)&p, sizeof(T) * cap));
+}
+
+extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session_t *const *sessions, int n,
+                                     const xavs2gpu_me_params_t *prm, void *stream)
+{
+    if (!b || !sessions || n < 0 || n > 256 || !prm || prm->search_range < 1 || prm->search_range > 128 ||
+        prm->fractional_me < 0 || prm->fractional_me > 2 || prm->lambda_factor < 0) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_batch_run", "bad parameters or more than 256 sessions");
+        return XAVS2GPU_ERR_ARG;
+    }
+    if (n == 0) return XAVS2GPU_OK;
+    XG_CUDA(cudaSetDevice(b->device));
+    const int R = prm->search_range, lam = prm->lambda_factor;
+    cudaStream_t st = (cudaStream_t)stream;
+    b->jobs.clear();
+    b->views.clear();
+    std::vector<uint32_t> gen, small, large;
+    int block = 128;
+    for (int k = 0; k < n; k++) {
+        MeSessionImpl &m = sessions[k]->impl;
+        if (m.device != b->device) {
+            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_batch_run", "sessions on different devices");
+            return XAVS2GPU_ERR_ARG;
+        }
+        ensure_plan(m, R);
+        b->views.push_back(m.h_view);
+        const uint32_t tag = (uint32_t)k << kSessShift;
+        for (CtuJob j : m.plan.h_jobs) {
+            j.sess = (uint8_t)k;
+            b->jobs.push_back(j);
+        }
+        for (uint32_t i : m.h_generic) gen.push_back(tag | i);
+        for (uint32_t i : m.h_small) small.push_back(tag | i);
+        for (uint32_t i : m.h_large) large.push_back(tag | i);
+        if (k == 0) block = m.tune_block;
+    }
+    BatchBuf &bb = b->buf[b->next];
+    b->next ^= 1;
+    if (bb.used) XG_CUDA(cudaEventSynchronize(bb.done));   // its lists may still be read
+    b->lists.clear();
+    b->lists.insert(b->lists.end(), gen.begin(), gen.end());
+    b->lists.insert(b->lists.end(), small.begin(), small.end());
+    b->lists.insert(b->lists.end(), large.begin(), large.end());
+    grow(bb.d_jobs, bb.cap_jobs, b->jobs.size());
+    grow(bb.d_lists, bb.cap_lists, b->lists.size());
+    grow(bb.d_views, bb.cap_views, b->views.size());
+    if (!b->jobs.empty())
+        XG_CUDA(cudaMemcpyAsync(bb.d_jobs, b->jobs.data(), sizeof(CtuJob) * b->jobs.size(), cudaMemcpyHostToDevice, st));
+    if (!b->lists.empty())
+        XG_CUDA(cudaMemcpyAsync(bb.d_lists, b->lists.data(), sizeof(uint32_t) * b->lists.size(),
+                                cudaMemcpyHostToDevice, st));
+    XG_CUDA(cudaMemcpyAsync(bb.d_views, b->views.data(), sizeof(SessView) * b->views.size(), cudaMemcpyHostToDevice,
+                            st));
+    const int ng = (int)gen.size(), ns = (int)small.size(), nl = (int)large.size();
+    const uint32_t *d_gen = bb.d_lists, *d_small = bb.d_lists + ng, *d_large = bb.d_lists + ng + ns;
+    reset_keys_kernel<<<152 * 4, 256, 0, st>>>(bb.d_views, n);
+    count_launch();
+    if (ng) {
+        me_init_list_kernel<<<(ng * 32 + 127) / 128, 128, 0, st>>>(d_gen, ng, bb.d_views, lam);
+        count_launch();
+    }
+    ctu_jobs_run(bb.d_jobs, (int)b->jobs.size(), bb.d_views, *prm, st);
+    if (ng) {
+        fs_generic_kernel<<<ng < 152 * 8 ? ng : 152 * 8, 256, 0, st>>>(d_gen, ng, bb.d_views, R, lam);
+        count_launch();
+    }
+    if (ns) {
+        refine_thread_kernel<<<(ns + block - 1) / block, block, 0, st>>>(d_small, ns, bb.d_views, R, *prm);
+        count_launch();
+    }
+    if (nl) {
+        refine_warp_list_kernel<<<(nl * 32 + block - 1) / block, block, 0, st>>>(d_large, nl, bb.d_views, R, *prm);
+        count_launch();
+    }
+    XG_CUDA(cudaEventRecord(bb.done, st));
+    bb.used = true;
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
 // ---- allocation-free search ------------------------------------------------------
 // For callers that cannot allocate device memory while they run: an encoder
 // embedded in a host process whose GPU memory is handed out by the host's
@@ -1105,6 +1393,7 @@ struct NoAllocScratch {
     int list[kNoAllocMaxPus];
     const uint8_t *planes[16 * kNoAllocMaxRefs];
     const uint8_t *ref0[kNoAllocMaxRefs];
+    SessView view;            // the call as the list kernels see it
 };
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
@@ -1116,12 +1405,25 @@ struct PlaneTable { const uint8_t *p[16 * kNoAllocMaxRefs]; };
 // replaced by one that has no admissible candidate, so it is never searched
 // and reports bcost = 1 << 30.  Also writes the plane tables and the index list.
 __global__ void noalloc_prepare_kernel(const xavs2gpu_pu_t *__restrict__ in, int n, NoAllocScratch *s, PlaneTable t,
-                                       int nrefs, int W, int H)
+                                       int nrefs, int W, int H, const uint8_t *cur, int stride,
+                                       xavs2gpu_me_result_t *out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         for (int k = 0; k < 16 * nrefs; k++) s->planes[k] = t.p[k];
         for (int r = 0; r < nrefs; r++) s->ref0[r] = t.p[16 * r];
+        SessView v;
+        v.cur = cur;
+        v.ref0 = s->ref0;
+        v.planes = s->planes;
+        v.pus = s->pus;
+        v.state = s->state;
+        v.keys = s->keys;
+        v.res = out;
+        v.slots = nullptr;
+        v.g = Geometry{W, H, stride};
+        v.n = n;
+        s->view = v;
     }
     if (i >= n) return;
     xavs2gpu_pu_t p = in[i];
@@ -1198,10 +1500,10 @@ extern "C" int xavs2gpu_me_search_noalloc(const uint8_t *cur, int stride, int wi
     cudaStream_t st = (cudaStream_t)stream;
     const Geometry g{width, height, stride};
     const int R = prm->search_range, lam = prm->lambda_factor;
-    noalloc_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(pus, n, s, t, num_refs, width, height);
+    noalloc_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(pus, n, s, t, num_refs, width, height, cur, stride, out);
     me_init_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, cur, s->ref0, g, lam, s->state, s->keys);
     const int grid = n < 152 * 8 ? n : 152 * 8;
-    fs_generic_kernel<<<grid, 256, 0, st>>>(s->list, n, s->pus, s->state, cur, s->ref0, g, R, lam, s->keys);
+    fs_generic_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint32_t *>(s->list), n, &s->view, R, lam);
     refine_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, s->state, s->keys, cur, s->planes, g, R, *prm,
                                                         out);
     count_launch(4);

@@ -128,4 +128,16 @@ uint64_t xavs2gpu_kernel_launches(void) { return xg::g_launches.load(); }
 
 const char *xavs2gpu_version(void) { return "xavs2-gb300 0.1 (sm_103a)"; }
 
+int xavs2gpu_copy_d2h(void *dst, const void *src, size_t bytes)
+{
+    XG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return xavs2gpu_get_status();
+}
+
+int xavs2gpu_copy_h2d(void *dst, const void *src, size_t bytes)
+{
+    XG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return xavs2gpu_get_status();
+}
+
 }  // extern "C"

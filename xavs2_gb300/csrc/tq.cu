@@ -1,0 +1,526 @@
+// tq.cu -- the batched TU reconstruction chain for sm_103a:
+// dct (or the 4x4 secondary transform) -> quant -> [dequant -> idct when a
+// level is non-zero] for every block of a batch, the order of the
+// reference's TU reconstruction (rdo.c:1333-1370, 876-947) with the
+// transforms of transform.c:1123-1587 and the quantiser of quant.c:108-184.
+//
+// Three launches per batch:
+//   1. count the blocks of every TU shape (invalid descriptors get nnz = -1);
+//   2. scatter the block indices into one list grouped by shape, largest
+//      shapes first, so that at any moment the warps of the persistent
+//      kernel run the code of one shape (a mixed order thrashes the
+//      instruction cache);
+//   3. the persistent chain kernel: a warp takes G = 32 / L TUs of one shape
+//      at a time (L lanes per TU: one lane per line of the larger side).
+// Every 1-D pass runs with one line per lane: the line's 16-bit values are
+// packed in pairs and each output is a dot product with a byte-packed basis
+// row, two products per dp2a instruction.  All pass inputs are 16-bit (the
+// residual, the forward first pass's int16 output, the clipped dequantised
+// levels, the inverse first pass's 16-bit clip), so the 32-bit sums are
+// exactly the reference's sums before its rounding shifts.  Passes hand over
+// through shared memory (transposes).  The 64-point shapes run the 5/3
+// wavelet around the 32-point core (wavelet_fwd_d / wavelet_inv_d in
+// transform.cu; transform.c:586-951).
+#include "transform_tables.cuh"
+
+namespace xg {
+namespace tqw {
+
+// ---- byte-packed basis rows --------------------------------------------------
+// Forward table of an N-point transform: row k holds T_N[k][0..N) as N/4
+// words (byte j of word w = T_N[k][4w + j]).  Inverse table: row n holds
+// T_N[0..N)[n].  N = 4, 8, 16, 32 at word offsets 0, 4, 20, 84; then the 4x4
+// secondary transform M (rows of M, resp. of M^T) at 340.
+constexpr int kTabWords = 344;
+struct PackedTab { uint32_t w[kTabWords]; };
+
+__host__ __device__ constexpr int tab_off(int N) { return N == 4 ? 0 : N == 8 ? 4 : N == 16 ? 20 : 84; }
+constexpr int kSec = 340;
+
+constexpr int sec4c(int i, int k)
+{
+    constexpr int8_t m[16] = {34, 58, 72, 81, 77, 69, -7, -75, 79, -33, -75, 58, 55, -84, 73, -28};
+    return m[i * 4 + k];
+}
+
+constexpr PackedTab make_tab(bool inverse)
+{
+    PackedTab t{};
+    for (int N = 4; N <= 32; N *= 2)
+        for (int r = 0; r < N; r++)
+            for (int j = 0; j < N; j++) {
+                const int v = inverse ? basis32(j * (32 / N), r) : basis32(r * (32 / N), j);
+                const int word = tab_off(N) + r * (N / 4) + j / 4;
+                t.w[word] |= (uint32_t)(uint8_t)(int8_t)v << (8 * (j % 4));
+            }
+    for (int r = 0; r < 4; r++)
+        for (int j = 0; j < 4; j++) {
+            const int v = inverse ? sec4c(j, r) : sec4c(r, j);
+            t.w[kSec + r] |= (uint32_t)(uint8_t)(int8_t)v << (8 * j);
+        }
+    return t;
+}
+
+static __constant__ PackedTab c_fwd = make_tab(false);
+static __constant__ PackedTab c_inv = make_tab(true);
+
+__device__ __forceinline__ uint32_t pack16(int a, int b) { return (uint32_t)(a & 0xFFFF) | ((uint32_t)b << 16); }
+__device__ __forceinline__ int clipb(int v, int bits)
+{
+    const int hi = (1 << (bits - 1)) - 1;
+    return min(max(v, -hi - 1), hi);
+}
+
+// sum_j row[j] * x[j] for the N values packed in pairs in xp; row = N/4 words
+template <int N>
+__device__ __forceinline__ int dot_row(const uint32_t (&xp)[N / 2], const uint32_t *row)
+{
+    int s = 0;
+#pragma unroll
+    for (int w = 0; w < N / 4; w++) {
+        const uint32_t b = row[w];
+        s = __dp2a_lo((int)xp[2 * w], (int)b, s);
+        s = __dp2a_hi((int)xp[2 * w + 1], (int)b, s);
+    }
+    return s;
+}
+
+// pairs of a shared-memory line of N int16 (4-byte aligned)
+template <int N>
+__device__ __forceinline__ void load_pairs(const int16_t *p, uint32_t (&xp)[N / 2])
+{
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
+#pragma unroll
+    for (int i = 0; i < N / 2; i++) xp[i] = w[i];
+}
+
+// pairs of a global line of N int16 (16-byte aligned when `al` and N >= 8,
+// 8-byte aligned when `al` and N == 4)
+template <int N>
+__device__ __forceinline__ void load_pairs_global(const int16_t *p, bool al, uint32_t (&xp)[N / 2])
+{
+    if constexpr (N >= 8) {
+        if (al) {
+#pragma unroll
+            for (int q = 0; q < N / 8; q++) {
+                const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p) + q);
+                xp[4 * q] = v.x; xp[4 * q + 1] = v.y; xp[4 * q + 2] = v.z; xp[4 * q + 3] = v.w;
+            }
+            return;
+        }
+    } else {
+        if (al) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
+            xp[0] = v.x; xp[1] = v.y;
+            return;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < N / 2; i++) xp[i] = pack16(p[2 * i], p[2 * i + 1]);
+}
+
+// ---- shapes ------------------------------------------------------------------
+template <int PART> struct Shape;
+#define XG_TQ_SHAPE(P, IW_, IH_, TW_, TH_, S1_, S2_)                                                               \
+    template <> struct Shape<P> {                                                                                  \
+        static constexpr int IW = IW_, IH = IH_, TW = TW_, TH = TH_, S1 = S1_, S2 = S2_;                           \
+        static constexpr bool WAV = IW_ != TW_ || IH_ != TH_;                                                      \
+        static constexpr int L = WAV ? 32 : (TW_ > TH_ ? TW_ : TH_);                                               \
+        static constexpr int G = 32 / L;                                                                           \
+    };
+XG_TQ_SHAPE(0, 4, 4, 4, 4, 0, 7)
+XG_TQ_SHAPE(1, 8, 8, 8, 8, 1, 8)
+XG_TQ_SHAPE(2, 16, 16, 16, 16, 2, 9)
+XG_TQ_SHAPE(3, 32, 32, 32, 32, 3, 10)
+XG_TQ_SHAPE(15, 16, 4, 16, 4, 2, 7)
+XG_TQ_SHAPE(16, 4, 16, 4, 16, 0, 9)
+XG_TQ_SHAPE(19, 32, 8, 32, 8, 3, 8)
+XG_TQ_SHAPE(20, 8, 32, 8, 32, 1, 10)
+XG_TQ_SHAPE(4, 64, 64, 32, 32, 4, 10)
+XG_TQ_SHAPE(23, 64, 16, 32, 8, 3, 7)
+XG_TQ_SHAPE(24, 16, 64, 8, 32, 2, 10)
+#undef XG_TQ_SHAPE
+
+// processing order: largest shapes first; TUs per warp of each class
+constexpr int kNumClasses = 11;
+__constant__ int c_class_part[kNumClasses] = {4, 23, 24, 3, 19, 20, 2, 15, 16, 1, 0};
+__host__ __device__ constexpr int class_g(int c) { return c < 6 ? 1 : c < 9 ? 2 : c == 9 ? 4 : 8; }
+
+__device__ __forceinline__ int class_of(int part)
+{
+    switch (part) {
+    case 4: return 0; case 23: return 1; case 24: return 2; case 3: return 3; case 19: return 4; case 20: return 5;
+    case 2: return 6; case 15: return 7; case 16: return 8; case 1: return 9; case 0: return 10;
+    default: return -1;
+    }
+}
+
+__host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v / 2); }
+
+// Per-warp shared memory: region A holds the wavelet input (64 rows, pitch
+// 66 int16) or the transposes and the output staging of the warp's G TUs;
+// region B the wavelet's horizontal low band (64 rows, pitch 34 int16) and
+// later the inverse transform's output for the upsampling.
+constexpr int kRegionA = 64 * 66 * 2, kRegionB = 64 * 34 * 2;
+constexpr int kWarpSmem = kRegionA + kRegionB;
+
+struct Ctx {
+    const xavs2gpu_tq_block_t *blocks;
+    const int16_t *residual;
+    int16_t *coef, *recon;
+    int32_t *nnz;
+};
+
+// One group of up to G TUs of shape PART; `idx` = the block index of this
+// lane's sub-warp (-1: no TU).
+template <int PART>
+__device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t *smem)
+{
+    using S = Shape<PART>;
+    constexpr int IW = S::IW, IH = S::IH, TW = S::TW, TH = S::TH, L = S::L;
+    constexpr int P1 = TH + 2, P2 = TW + 2;       // transpose pitches (int16, even)
+    constexpr int F = S::WAV ? 1 : 0;
+    constexpr int LEVEL = (ilog2c(IW) + ilog2c(IH)) >> 1;
+    const int sub = lane / L, l = lane % L;
+    const bool act = idx >= 0;
+    xavs2gpu_tq_block_t b{};
+    if (act) b = cx.blocks[idx];
+    const bool sec = PART == 0 && (b.flags & 2);
+    int16_t *tA = reinterpret_cast<int16_t *>(smem) + sub * (kRegionA / 2 / S::G);
+    int16_t *tB = reinterpret_cast<int16_t *>(smem + kRegionA);
+    const int16_t *src = cx.residual + b.offset;
+    const bool al_in = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+
+    // ---- forward rows -> T1[k][j] (pitch P1) in region A
+    uint32_t xp[TW / 2];
+    if constexpr (S::WAV) {
+        constexpr int PX = 66, HP = 34, PL = TW + 2;
+        if (act) {
+            if (al_in) {
+                for (int e = lane; e < IW * IH / 8; e += 32) {
+                    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src) + e);
+                    uint32_t *d = reinterpret_cast<uint32_t *>(tA + ((e * 8) / IW) * PX + (e * 8) % IW);
+                    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+                }
+            } else {
+                for (int e = lane; e < IW * IH; e += 32) tA[(e / IW) * PX + e % IW] = src[e];
+            }
+        }
+        __syncwarp();
+        // horizontal lifting, one row per lane: odd[m] = p[2m+1] - (p[2m] +
+        // p[2m+2]) >> 1, H[m] = p[2m] + (odd[m-1] + odd[m] + 2) >> 2, int16
+        // after each step, mirrored ends (p[IW] = p[IW-2], odd[-1] = odd[0])
+        if (act) {
+            for (int r = lane; r < IH; r += 32) {
+                const int16_t *p = tA + r * PX;
+                int prev_odd = 0, pe = p[0];
+                for (int m = 0; m < IW / 2; m++) {
+                    const int po = p[2 * m + 1], pn = m + 1 < IW / 2 ? p[2 * m + 2] : p[IW - 2];
+                    const int odd = (int16_t)(po - ((pe + pn) >> 1));
+                    if (m == 0) prev_odd = odd;
+                    tB[r * HP + m] = (int16_t)(pe + ((prev_odd + odd + 2) >> 2));
+                    prev_odd = odd;
+                    pe = pn;
+                }
+            }
+        }
+        __syncwarp();
+        // vertical lifting, one LL row per lane (j < TH), into region A:
+        // odd'[m] = q[2m+1] - (q[2m] + q[2m+2]) >> 1,
+        // LL[m] = 2 q[2m] + (odd'[m-1] + odd'[m] + 1) >> 1
+        if (act && lane < TH) {
+            const int j = lane;
+            const int rm2 = j == 0 ? 2 : 2 * j - 2, rm1 = j == 0 ? 1 : 2 * j - 1;
+            const int rp1 = 2 * j + 1, rp2 = j == TH - 1 ? 2 * j : 2 * j + 2;
+            for (int i = 0; i < TW; i++) {
+                const int qa = tB[rm2 * HP + i], qb = tB[rm1 * HP + i], qc = tB[2 * j * HP + i];
+                const int qd = tB[rp1 * HP + i], qe = tB[rp2 * HP + i];
+                const int oa = (int16_t)(qb - ((qa + qc) >> 1));
+                const int ob = (int16_t)(qd - ((qc + qe) >> 1));
+                tA[j * PL + i] = (int16_t)((qc << 1) + ((oa + ob + 1) >> 1));
+            }
+        }
+        __syncwarp();
+        if (act && lane < TH) load_pairs<TW>(tA + lane * PL, xp);
+        __syncwarp();
+    } else {
+        if (act && l < TH) load_pairs_global<TW>(src + l * TW, al_in, xp);
+    }
+    if (act && l < TH) {
+        bool done = false;
+        if constexpr (PART == 0) {
+            if (sec) {
+                for (int k = 0; k < 4; k++)
+                    tA[k * P1 + l] = (int16_t)clipb((dot_row<4>(xp, &c_fwd.w[kSec + k]) + 1) >> 1, 16);
+                done = true;
+            }
+        }
+        if (!done) {
+            const uint32_t *rows = &c_fwd.w[tab_off(TW)];
+#pragma unroll 2
+            for (int k = 0; k < TW; k++)
+                tA[k * P1 + l] = (int16_t)((dot_row<TW>(xp, rows + k * (TW / 4)) + ((1 << S::S1) >> 1)) >> S::S1);
+        }
+    }
+    __syncwarp();
+
+    // ---- forward columns + quant (lane l < TW holds column l): levels to
+    // global, dequantised levels back into T1 row l
+    const int qshift = 22 - LEVEL;
+    const int qadd = (int)(((int64_t)1 << (qshift + (b.flags & 1))) * 5 / 31);
+    const int qscale = c_q_scale[b.qp & 127];
+    const int dqshift = iq_shift_of(b.qp) + 9 + LEVEL - 16;
+    const int dqscale = c_iq_scale[b.qp & 127];
+    int nz = 0;
+    if (act && l < TW) {
+        uint32_t cp[TH / 2];
+        load_pairs<TH>(tA + l * P1, cp);
+        int16_t *co = cx.coef + b.coef_offset + l;
+        const uint32_t *rows = sec ? &c_fwd.w[kSec] : &c_fwd.w[tab_off(TH)];
+#pragma unroll 2
+        for (int m = 0; m < TH; m++) {
+            const int s = dot_row<TH>(cp, rows + m * (TH / 4));
+            const int y = sec ? clipb((s + 128) >> 8, 16) : (int)(int16_t)((s + ((1 << S::S2) >> 1)) >> S::S2);
+            const int a = (y < 0 ? -y : y) * qscale + qadd;
+            const int q = y < 0 ? -(a >> qshift) : (a >> qshift);
+            co[m * TW] = (int16_t)q;
+            nz += q != 0;
+            tA[l * P1 + m] = (int16_t)clipb((q * dqscale + (1 << (dqshift - 1))) >> dqshift, 16);
+        }
+    }
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) nz += __shfl_xor_sync(0xffffffffu, nz, o);
+    if (act && l == 0) cx.nnz[idx] = nz;
+    int16_t *dst = cx.recon + b.offset;
+    const bool al_out = (reinterpret_cast<uintptr_t>(dst) & 15) == 0;
+    if (act && nz == 0) {
+        if (al_out)
+            for (int i = l; i < IW * IH / 8; i += L) reinterpret_cast<uint4 *>(dst)[i] = make_uint4(0, 0, 0, 0);
+        else
+            for (int i = l; i < IW * IH; i += L) dst[i] = 0;
+    }
+    const bool inv = act && nz != 0;
+    __syncwarp();
+
+    // ---- inverse columns: lane l < TW -> T2[n][l] (pitch P2) after T1
+    int16_t *t2 = tA + TW * P1;
+    if (inv && l < TW) {
+        uint32_t cp[TH / 2];
+        load_pairs<TH>(tA + l * P1, cp);
+        const uint32_t *rows = sec ? &c_inv.w[kSec] : &c_inv.w[tab_off(TH)];
+#pragma unroll 2
+        for (int n = 0; n < TH; n++)
+            t2[n * P2 + l] = (int16_t)clipb((dot_row<TH>(cp, rows + n * (TH / 4)) + 16) >> 5, 16);
+    }
+    __syncwarp();
+
+    // ---- inverse rows: lane l < TH; rows staged after T2 (or, for the
+    // wavelet shapes, into region B for the upsampling)
+    int16_t *stage = S::WAV ? tB : t2 + TH * P2;
+    constexpr int PS = S::WAV ? TW + 2 : TW;
+    if (inv && l < TH) {
+        uint32_t vp[TW / 2];
+        load_pairs<TW>(t2 + l * P2, vp);
+        const uint32_t *rows = sec ? &c_inv.w[kSec] : &c_inv.w[tab_off(TW)];
+        const int sh = sec ? 14 : 12 - F, bits = sec ? 9 : 9 + F;
+        int16_t *o = stage + l * PS;
+#pragma unroll 2
+        for (int x = 0; x < TW; x++)
+            o[x] = (int16_t)clipb((dot_row<TW>(vp, rows + x * (TW / 4)) + (1 << (sh - 1))) >> sh, bits);
+    }
+    __syncwarp();
+    if constexpr (!S::WAV) {
+        if (inv) {
+            if (al_out) {
+                for (int i = l; i < TW * TH / 8; i += L) {
+                    const uint32_t *w = reinterpret_cast<const uint32_t *>(stage + 8 * i);
+                    reinterpret_cast<uint4 *>(dst)[i] = make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            } else {
+                for (int i = l; i < TW * TH; i += L) dst[i] = stage[i];
+            }
+        }
+    } else {
+        // upsampling of the TW x TH low band in region B (pitch TW+2):
+        // V[2y] = h[y], V[2y+1] = (h[y] + h[y+1]) >> 1 with h = LL >> 1 and
+        // h[TH] = h[TH-1]; D[2i] = V[i], D[2i+1] = (V[i] + V[i+1]) >> 1 with
+        // V[TW] = V[TW-1].  One output word (2 samples) per lane and step.
+        if (inv) {
+            for (int e = lane; e < IH * TW; e += 32) {
+                const int r = e / TW, i = e % TW, in1 = i + 1 < TW ? i + 1 : i;
+                const int y = r >> 1, yn = y + 1 < TH ? y + 1 : y;
+                int v0 = stage[y * PS + i] >> 1, v1 = stage[y * PS + in1] >> 1;
+                if (r & 1) {
+                    v0 = (v0 + (stage[yn * PS + i] >> 1)) >> 1;
+                    v1 = (v1 + (stage[yn * PS + in1] >> 1)) >> 1;
+                }
+                const uint32_t w = pack16(v0, (v0 + v1) >> 1);
+                if (al_out) {
+                    reinterpret_cast<uint32_t *>(dst)[e] = w;
+                } else {
+                    dst[2 * e] = (int16_t)(w & 0xFFFF);
+                    dst[2 * e + 1] = (int16_t)(w >> 16);
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// 1. per-class counts (warp-aggregated atomics)
+__global__ void tq_count_kernel(const xavs2gpu_tq_block_t *__restrict__ blocks, int n, int *__restrict__ counts,
+                                int32_t *__restrict__ nnz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1;
+    if (i < n) {
+        const xavs2gpu_tq_block_t b = blocks[i];
+        c = (b.qp >= 0 && b.qp <= 79) ? class_of(b.part) : -1;
+        if (c < 0) nnz[i] = -1;
+    }
+    const unsigned valid = __ballot_sync(0xffffffffu, c >= 0);
+    if (c >= 0) {
+        const unsigned same = __match_any_sync(valid, c);
+        if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&counts[c], __popc(same));
+    }
+}
+
+// 2. scatter into the class-ordered list (the order inside a class does not
+//    matter: every TU writes only its own outputs)
+__global__ void tq_scatter_kernel(const xavs2gpu_tq_block_t *__restrict__ blocks, int n, const int *__restrict__ counts,
+                                  int *__restrict__ cursor, int *__restrict__ sorted)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int c = -1;
+    if (i < n) {
+        const xavs2gpu_tq_block_t b = blocks[i];
+        c = (b.qp >= 0 && b.qp <= 79) ? class_of(b.part) : -1;
+    }
+    const unsigned valid = __ballot_sync(0xffffffffu, c >= 0);
+    if (c < 0) return;
+    const unsigned same = __match_any_sync(valid, c);
+    const int leader = __ffs(same) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&cursor[c], __popc(same));
+    base = __shfl_sync(same, base, leader);
+    int start = 0;
+    for (int k = 0; k < c; k++) start += counts[k];
+    sorted[start + base + __popc(same & ((1u << lane) - 1))] = i;
+}
+
+// 3. the chain, persistent: warp-strided over the groups of all classes
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) tq_chain_kernel(Ctx cx, const int *__restrict__ counts,
+                                                               const int *__restrict__ sorted)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    uint8_t *smem = smem_raw + (threadIdx.x >> 5) * kWarpSmem;
+    const int lane = threadIdx.x & 31;
+    int cnt[kNumClasses], gstart[kNumClasses + 1], istart[kNumClasses];
+    gstart[0] = 0;
+    int acc = 0;
+#pragma unroll
+    for (int c = 0; c < kNumClasses; c++) {
+        cnt[c] = counts[c];
+        istart[c] = acc;
+        acc += cnt[c];
+        gstart[c + 1] = gstart[c] + (cnt[c] + class_g(c) - 1) / class_g(c);
+    }
+    const int total = gstart[kNumClasses];
+    const int nw = gridDim.x * WARPS;
+    for (int item = blockIdx.x * WARPS + (threadIdx.x >> 5); item < total; item += nw) {
+        int c = 0, gs = 0, is = istart[0], cn = cnt[0], G = class_g(0);
+#pragma unroll
+        for (int k = 1; k < kNumClasses; k++)
+            if (item >= gstart[k]) {
+                c = k; gs = gstart[k]; is = istart[k]; cn = cnt[k]; G = class_g(k);
+            }
+        const int pos = (item - gs) * G + lane / (32 / G);
+        const int idx = pos < cn ? sorted[is + pos] : -1;
+        switch (c_class_part[c]) {
+        case 4: tu_group<4>(cx, idx, lane, smem); break;
+        case 23: tu_group<23>(cx, idx, lane, smem); break;
+        case 24: tu_group<24>(cx, idx, lane, smem); break;
+        case 3: tu_group<3>(cx, idx, lane, smem); break;
+        case 19: tu_group<19>(cx, idx, lane, smem); break;
+        case 20: tu_group<20>(cx, idx, lane, smem); break;
+        case 2: tu_group<2>(cx, idx, lane, smem); break;
+        case 15: tu_group<15>(cx, idx, lane, smem); break;
+        case 16: tu_group<16>(cx, idx, lane, smem); break;
+        case 1: tu_group<1>(cx, idx, lane, smem); break;
+        default: tu_group<0>(cx, idx, lane, smem); break;
+        }
+    }
+}
+
+}  // namespace tqw
+
+template <int WARPS>
+static int tq_launch_w(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
+                       int16_t *recon, int32_t *nnz, cudaStream_t stream)
+{
+    constexpr int smem = WARPS * tqw::kWarpSmem;
+    static bool attr_set[64] = {false};
+    static int ctas_per_sm[64] = {0}, sms[64] = {0};
+    const int dev = current_device();
+    if (dev < 0 || dev >= 64) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch", "device index out of range");
+        return XAVS2GPU_ERR_ARG;
+    }
+    if (!attr_set[dev]) {
+        XG_CUDA(cudaFuncSetAttribute(tqw::tq_chain_kernel<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas_per_sm[dev], tqw::tq_chain_kernel<WARPS>,
+                                                              WARPS * 32, smem));
+        XG_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev));
+        if (ctas_per_sm[dev] < 1) ctas_per_sm[dev] = 1;
+        // keep freed stream-ordered scratch in the pool between batches
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        attr_set[dev] = true;
+    }
+    // scratch: class counts and cursors (32 ints each), then the ordered list
+    int *scratch = nullptr;
+    XG_CUDA(cudaMallocAsync((void **)&scratch, sizeof(int) * (64 + (size_t)n), stream));
+    if (!scratch) return XAVS2GPU_ERR_CUDA;
+    int *counts = scratch, *cursor = scratch + 32, *sorted = scratch + 64;
+    XG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 64, stream));
+    const int nb = (n + 255) / 256;
+    tqw::tq_count_kernel<<<nb, 256, 0, stream>>>(blocks, n, counts, nnz);
+    tqw::tq_scatter_kernel<<<nb, 256, 0, stream>>>(blocks, n, counts, cursor, sorted);
+    long long grid = (long long)sms[dev] * ctas_per_sm[dev];
+    const long long ctas_needed = ((long long)n + WARPS - 1) / WARPS;
+    if (grid > ctas_needed) grid = ctas_needed;
+    tqw::Ctx cx{blocks, residual, coef, recon, nnz};
+    tqw::tq_chain_kernel<WARPS><<<(int)grid, WARPS * 32, smem, stream>>>(cx, counts, sorted);
+    count_launch(3);
+    XG_CUDA(cudaFreeAsync(scratch, stream));
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+// The batched TU chain with `warps` (4 or 8) warps per CTA.
+int tq_batch_launch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
+                    int16_t *recon, int32_t *nnz, int warps, cudaStream_t stream)
+{
+    if (n < 0) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch", "negative count");
+        return XAVS2GPU_ERR_ARG;
+    }
+    if (n == 0) return XAVS2GPU_OK;
+    if (warps == 8) return tq_launch_w<8>(blocks, n, residual, coef, recon, nnz, stream);
+    return tq_launch_w<4>(blocks, n, residual, coef, recon, nnz, stream);
+}
+
+}  // namespace xg
+
+using namespace xg;
+
+extern "C" int xavs2gpu_tq_batch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
+                                 int16_t *recon, int32_t *nnz, void *stream)
+{
+    return tq_batch_launch(blocks, n, residual, coef, recon, nnz, 4, (cudaStream_t)stream);
+}

@@ -2,62 +2,13 @@
 // the 64-point 5/3-wavelet path), the 4x4 and mode-dependent secondary
 // transforms, and quant/dequant for sm_103a: per-call drop-ins of the
 // reference's dct_funcs_t (source/common/primitives.h:101-119; C versions
-// transform.c:1123-1757 and quant.c:108-247) and the batched
-// dct -> quant -> dequant -> idct chain.
-#include "xavs2gpu_common.cuh"
+// transform.c:1123-1757 and quant.c:108-247).  The batched
+// dct -> quant -> dequant -> idct chain is in tq.cu.
+#include "transform_tables.cuh"
 
 #include <cstring>
 
 namespace xg {
-
-// ---- DCT basis ------------------------------------------------------------
-// Every AVS2 basis entry is +-c[a] for the reduced angle a = k(2n+1) mod 128
-// (units of pi/64); the N-point matrix is rows k*32/N of the 32-point one.
-struct Basis32 { int8_t v[32][32]; };
-
-static constexpr int8_t kCos[32] = {32, 45, 45, 45, 44, 44, 43, 43, 42, 41, 40, 39, 38, 36, 35, 34,
-                                    32, 30, 29, 27, 25, 23, 21, 19, 17, 15, 13, 11, 9,  7,  4,  2};
-
-static constexpr Basis32 make_basis()
-{
-    Basis32 b{};
-    for (int k = 0; k < 32; k++)
-        for (int n = 0; n < 32; n++) {
-            int a = (k * (2 * n + 1)) % 128, s = 1;
-            if (a > 64) a = 128 - a;
-            if (a > 32) { a = 64 - a; s = -1; }
-            b.v[k][n] = (int8_t)(k == 0 ? 32 : s * kCos[a]);
-        }
-    return b;
-}
-
-__constant__ Basis32 c_basis = make_basis();
-
-// Secondary transform matrices (transform.c:140-155), fixed by the standard.
-__constant__ int16_t c_sec_mode[16] = {123, -35, -8, -3, -32, -120, 30, 10, 14, 25, 123, -22, 8, 13, 19, 126};
-__constant__ int16_t c_sec_4x4[16] = {34, 58, 72, 81, 77, 69, -7, -75, 79, -33, -75, 58, 55, -84, 73, -28};
-
-// Quant tables (quant.c:55-81).  IQ shift: 15 - qp/8, except that qp 16,
-// 32, 40 and 48 keep the previous group's shift (quant.c:85-96).
-__constant__ uint16_t c_q_scale[80] = {
-    32768, 29775, 27554, 25268, 23170, 21247, 19369, 17770, 16302, 15024, 13777, 12634, 11626, 10624, 9742, 8958,
-    8192,  7512,  6889,  6305,  5793,  5303,  4878,  4467,  4091,  3756,  3444,  3161,  2894,  2654,  2435, 2235,
-    2048,  1878,  1722,  1579,  1449,  1329,  1218,  1117,  1024,  939,   861,   790,   724,   664,   609,  558,
-    512,   470,   430,   395,   362,   332,   304,   279,   256,   235,   215,   197,   181,   166,   152,  140,
-    128,   116,   108,   99,    91,    83,    76,    69,    64,    59,    54,    49,    45,    41,    38,   35};
-__constant__ uint16_t c_iq_scale[80] = {
-    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933,
-    65535, 35734, 38968, 42577, 46341, 50617, 55027, 60097, 32809, 35734, 38968, 42454, 46382, 50576, 55109, 60056,
-    65535, 35734, 38968, 42495, 46320, 50515, 55109, 60076, 65535, 35744, 38968, 42495, 46341, 50535, 55099, 60087,
-    65535, 35734, 38973, 42500, 46341, 50535, 55109, 60097, 32771, 35734, 38965, 42497, 46341, 50535, 55109, 60099,
-    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933};
-
-__host__ __device__ inline int iq_shift_of(int qp)
-{
-    int s = 15 - (qp >> 3);
-    if (qp == 16 || qp == 32 || qp == 40 || qp == 48) s += 1;
-    return s;
-}
 
 // ---- TU geometry -------------------------------------------------------------
 // Shift parameters of one TU shape for 8-bit input (transform.c:1123-1587).
@@ -362,70 +313,6 @@ __global__ void __launch_bounds__(256) quant_percall_kernel(int op, int16_t *c, 
     if (threadIdx.x == 0) result[0] = nz;
 }
 
-// ---- batched chain (one CTA per TU) -------------------------------------------
-// dct (or the 4x4 secondary transform) -> quant -> [dequant -> idct when any
-// level is non-zero], the order of rdo.c:1333-1370 / 876-947.
-__global__ void __launch_bounds__(256) tq_chain_kernel(const xavs2gpu_tq_block_t *__restrict__ blocks, int n,
-                                                       const int16_t *__restrict__ residual, int16_t *__restrict__ coef,
-                                                       int16_t *__restrict__ recon, int32_t *__restrict__ nnz)
-{
-    extern __shared__ __align__(16) uint8_t smem_raw[];
-    TuSmem &s = *reinterpret_cast<TuSmem *>(smem_raw);
-    load_basis(s);
-    for (int bi = blockIdx.x; bi < n; bi += gridDim.x) {
-        const xavs2gpu_tq_block_t b = blocks[bi];
-        TuGeom g;
-        if (!tu_geom(b.part, 0, g) || b.qp < 0 || b.qp > 79) {
-            if (threadIdx.x == 0) nnz[bi] = -1;
-            continue;
-        }
-        const bool sec = b.part == 0 && (b.flags & 2);
-        const int nin = g.iw * g.ih, ncoef = g.w * g.h;
-        const int16_t *src = residual + b.offset;
-        for (int i = threadIdx.x; i < nin; i += blockDim.x) s.a[i] = src[i];
-        __syncthreads();
-        if (sec) {
-            if (threadIdx.x == 0) sec_4x4_fwd_d(s.a, 4);
-            __syncthreads();
-        } else {
-            tu_forward_d(s, g);
-        }
-        // i_level: log2 of the side for squares (64 -> 6), the mean of the two
-        // side logs for the split shapes
-        const int level = ((31 - __clz(g.iw)) + (31 - __clz(g.ih))) >> 1;
-        const int qshift = 15 + 16 - 9 - level;
-        const int qadd = (int)(((int64_t)1 << (qshift + (b.flags & 1 ? 1 : 0))) * 5 / 31);
-        const int qscale = c_q_scale[b.qp];
-        int nz = 0;
-        for (int i = threadIdx.x; i < ncoef; i += blockDim.x) {
-            int16_t q = quant1(s.a[i], qscale, qshift, qadd);
-            s.a[i] = q;
-            coef[b.coef_offset + i] = q;
-            nz += q != 0;
-        }
-        nz = block_sum(nz, s.red);
-        if (threadIdx.x == 0) nnz[bi] = nz;
-        int16_t *rec = recon + b.offset;
-        if (nz == 0) {
-            for (int i = threadIdx.x; i < nin; i += blockDim.x) rec[i] = 0;
-            __syncthreads();
-            continue;
-        }
-        const int dqshift = iq_shift_of(b.qp) + 9 + level - 16;
-        const int dqscale = c_iq_scale[b.qp];
-        for (int i = threadIdx.x; i < ncoef; i += blockDim.x) s.a[i] = dequant1(s.a[i], dqscale, dqshift);
-        __syncthreads();
-        if (sec) {
-            if (threadIdx.x == 0) sec_4x4_inv_d(s.a, 4);
-            __syncthreads();
-        } else {
-            tu_inverse_d(s, g, 0);
-        }
-        for (int i = threadIdx.x; i < nin; i += blockDim.x) rec[i] = s.a[i];
-        __syncthreads();
-    }
-}
-
 }  // namespace xg
 
 using namespace xg;
@@ -568,26 +455,4 @@ extern "C" void xavs2gpu_quant_init(uint32_t cpuid, xavs2gpu_dct_funcs_t *dctf)
     dctf->wquant = xavs2gpu_quant_weighted;
     dctf->abs_coeff = xavs2gpu_abs_coeff;
     dctf->add_sign = xavs2gpu_add_sign;
-}
-
-extern "C" int xavs2gpu_tq_batch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
-                                 int16_t *recon, int32_t *nnz, void *stream)
-{
-    if (n < 0) {
-        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch", "negative count");
-        return XAVS2GPU_ERR_ARG;
-    }
-    if (n == 0) return XAVS2GPU_OK;
-    static bool attr_set[8] = {false};
-    int dev = current_device();
-    if (!attr_set[dev]) {
-        XG_CUDA(cudaFuncSetAttribute(tq_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TuSmem)));
-        XG_CUDA(cudaFuncSetAttribute(tu_percall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TuSmem)));
-        attr_set[dev] = true;
-    }
-    int grid = n < 152 * 16 ? n : 152 * 16;
-    tq_chain_kernel<<<grid, 256, sizeof(TuSmem), (cudaStream_t)stream>>>(blocks, n, residual, coef, recon, nnz);
-    count_launch();
-    XG_CUDA(cudaGetLastError());
-    return XAVS2GPU_OK;
 }

@@ -68,3 +68,49 @@ def me_workload(seed=1, width=1920, height=1080, n_motions=16, max_px=32):
     f1 = next_picture(rng, f0, n_motions, max_px)
     f2 = next_picture(rng, f1, n_motions, max_px)
     return f2, [f1, f0]
+
+
+TQ_BLOCK_DTYPE = np.dtype([("offset", "<i8"), ("coef_offset", "<i8"), ("part", "<i4"), ("qp", "<i4"),
+                           ("flags", "<i4"), ("pad_", "<i4")])
+
+
+def tq_blocks(n, seed=3, parts=(0, 1, 2, 3, 4)):
+    """Descriptors of the batched transform+quant workload: TU shape uniform
+    over `parts` (LumaPU indices; default the squares 4..64), QP uniform in
+    [22, 51], half of the 4x4 blocks through the intra 4x4 secondary
+    transform (b_intra set with it), blocks packed back to back.  Returns
+    (blocks, residual elements, level elements, per-block zero mask: 10 % of
+    the blocks are all-zero)."""
+    from . import PU_W, PU_H
+    rng = np.random.default_rng(seed)
+    part = rng.choice(np.asarray(parts), n)
+    w, h = np.asarray(PU_W)[part], np.asarray(PU_H)[part]
+    size = (w * h).astype(np.int64)
+    ncoef = np.where((w == 64) | (h == 64), size // 4, size)
+    blocks = np.zeros(n, TQ_BLOCK_DTYPE)
+    blocks["part"] = part
+    blocks["qp"] = rng.integers(22, 52, n)
+    sec = (part == 0) & (rng.random(n) < 0.5)
+    blocks["flags"] = np.where(sec, 3, 0)
+    blocks["offset"] = np.cumsum(size) - size
+    blocks["coef_offset"] = np.cumsum(ncoef) - ncoef
+    zero = rng.random(n) < 0.1
+    return blocks, int(size.sum()), int(ncoef.sum()), zero
+
+
+def tq_residual(blocks, zero, total, seed=4, device="cpu"):
+    """int16 residuals for `blocks` as a torch tensor on `device`: Laplacian
+    (scale 12) by inverse CDF of a seeded uniform, rounded, clipped to
+    [-255, 255]; blocks flagged in `zero` are all zero."""
+    import torch
+    from . import PU_W, PU_H
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    u = torch.rand(total, generator=g, device=device, dtype=torch.float32) - 0.5
+    x = -12.0 * torch.sign(u) * torch.log1p(-2.0 * u.abs().clamp(max=0.4999999))
+    res = x.round().clamp(-255, 255).to(torch.int16)
+    part = blocks["part"]
+    size = (np.asarray(PU_W)[part] * np.asarray(PU_H)[part]).astype(np.int64)
+    keep = torch.from_numpy((~zero).astype(np.int16)).to(device)
+    res *= torch.repeat_interleave(keep, torch.from_numpy(size).to(device), output_size=total)
+    return res
