@@ -127,6 +127,26 @@ def cpu_sample_search(pus, cur, refs, prm_tuple, fraction, seed, threads):
     return count_evals(sel, prm_tuple[0]), dt, len(sel)
 
 
+def reduce_max(value, device):
+    """Max of a per-rank scalar over all ranks (replicas: the slowest rank
+    sets the job's time); the value itself without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank, seconds_per_rank, device):
+    """Whole-job throughput of independent replicas: all ranks' units over
+    the slowest rank's time."""
+    import torch.distributed as dist
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    return units_per_rank * world / reduce_max(seconds_per_rank, device)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -233,10 +253,7 @@ def run_ours(args):
     launches = lib.xavs2gpu_kernel_launches() - launches0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(total_ms, "cuda")
     value = evals * world * args.steps / (total_ms / 1e3)
 
     # ---- per-kernel timing on the session stream (separate pass)
@@ -283,10 +300,7 @@ def run_ours(args):
         out = sess.results()
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(e2e_s, "cuda")
     e2e = evals * world * args.steps / e2e_s
     same = bool(np.array_equal(out, res))
 
@@ -401,7 +415,8 @@ def run_tq(args):
 
     rank, world, local = dist_env()
     n = args.tq_blocks
-    blocks, nres, ncoef, zero = synth.tq_blocks(n, seed=3 + rank)
+    parts = tuple(int(x) for x in args.tq_parts.split(","))
+    blocks, nres, ncoef, zero = synth.tq_blocks(n, seed=3 + rank, parts=parts)
     algo_bytes = tq_bytes(blocks)
     cfg = {"workload": "tq_batch_1e6_tu4to64", "blocks": n, "tu_sizes": "4,8,16,32,64 uniform",
            "qp": "uniform 22..51", "secondary_4x4": "50% of 4x4 blocks", "zero_blocks": "10%",
@@ -475,12 +490,14 @@ def run_tq(args):
     launches = lib.xavs2gpu_kernel_launches() - launches0
     step_ms = [s_.elapsed_time(e) for s_, e in zip(starts, ends)]
     total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(total_ms, dev)
     value = n * world * args.steps / (total_ms / 1e3)
     kernel_ms = min(step_ms)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": TQ_METRIC, "value": value, "unit": "blocks/s", "ms_per_step": kernel_ms,
+                              "GBs": algo_bytes / (kernel_ms / 1e3) / 1e9, "parts": args.tq_parts, "blocks": n}))
+        return
 
     # end to end with host buffers: pinned residual in, levels + recon + nnz out
     h_res = d_res.cpu().pin_memory()
@@ -501,10 +518,7 @@ def run_tq(args):
         stream.synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(e2e_s, dev)
     e2e = n * world * args.steps / e2e_s
     if rank != 0:
         return
@@ -549,6 +563,246 @@ def run_tq(args):
     print(json.dumps(line))
 
 
+# ---- serving: 64 concurrent streams, continuous batching --------------------
+SERVE_METRIC = "served p99 frame latency (64 streams 360p..2160p, 30 fps Poisson arrivals, continuous batching)"
+SERVE_RES = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
+
+
+def serve_content(width, height, n, seed):
+    """Config-0 style pictures: a blurred-noise base picture, then one global
+    quarter-pel translation U[-8, 8] px per picture plus noise."""
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(seed)
+    frames = [synth.base_picture(rng, width, height)]
+    for _ in range(n - 1):
+        frames.append(synth.next_picture(rng, frames[-1], 1, 8))
+    return frames
+
+
+def serve_trace(xg, srv, streams, pools, duration, warm, rate, seed):
+    """Submits every stream's pictures at Poisson arrival times for
+    `duration` s while a collector polls; returns the results of the
+    pictures submitted after `warm` s and the submission failures."""
+    import threading
+    rng = np.random.default_rng(seed)
+    events = []
+    for sid, (res, off) in enumerate(streams):
+        t = rng.uniform(0, 1.0 / rate)
+        k = 0
+        while t < duration:
+            events.append((t, sid, res, off + k))
+            t += rng.exponential(1.0 / rate)
+            k += 1
+    events.sort()
+    results = []
+    done = threading.Event()
+
+    def collect():
+        while not done.is_set() or len(results) < submitted[0]:
+            r = srv.poll(4096, 20)
+            if len(r):
+                results.extend(r.tolist())
+            elif done.is_set() and time.time() > deadline[0]:
+                break
+
+    submitted = [0]
+    deadline = [0.0]
+    fails = 0
+    th = threading.Thread(target=collect)
+    th.start()
+    t0 = time.perf_counter()
+    t0_ns = time.monotonic_ns()
+    for (t, sid, res, k) in events:
+        dt = t - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        pool = pools[res]
+        if srv.submit(sid, pool[k % len(pool)], tag=int(t * 1e9)) == 0:
+            submitted[0] += 1
+        else:
+            fails += 1
+    deadline[0] = time.time() + 30.0
+    done.set()
+    th.join()
+    arr = np.array(results, dtype=xg.SERVER_RESULT_DTYPE)
+    keep = (arr["ref_only"] == 0) & (arr["tag"] >= int(warm * 1e9))
+    return arr[keep], fails, len(events), t0_ns
+
+
+def serve_summary(arr, window):
+    lat = (arr["t_done_ns"] - arr["t_submit_ns"]) / 1e6
+    if len(lat) == 0:
+        return {"frames": 0}
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "frames": int(len(lat)), "frames_per_s": float(len(lat) / window),
+            "mean_batch_frames": float(arr["batch_frames"].mean())}
+
+
+def run_serve(args):
+    import torch
+    import xavs2_gb300 as xg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    rng = np.random.default_rng(11 + rank)
+    nstreams, rate = args.serve_streams, 30.0
+    res_idx = rng.choice(4, nstreams, p=[0.3, 0.3, 0.3, 0.1])
+    pools = {r: serve_content(*SERVE_RES[r], args.serve_pool, 50 + r) for r in sorted(set(res_idx.tolist()))}
+    prm = xg.MeParams(args.serve_range, lambda_factor(QP), 1, 2, 0, 0)
+    layouts = []
+    for sid in range(nstreams):
+        w, h = SERVE_RES[res_idx[sid]]
+        layouts.append(xg.cu_pus(xg.split_map_cus(w, h, 1000 + sid), w, h, 2))
+
+    def make_server(max_frames):
+        cfg = xg.ServerConfig(args.serve_hbm_gb << 30, 48 << 20, max_frames, QP, prm)
+        srv = xg.Server(cfg)
+        streams = []
+        for sid in range(nstreams):
+            w, h = SERVE_RES[res_idx[sid]]
+            pus, cus = layouts[sid]
+            got = srv.open_stream(w, h, pus, cus, ring=16)
+            assert got == sid, got
+            streams.append((int(res_idx[sid]), int(rng.integers(0, args.serve_pool))))
+        return srv, streams
+
+    window = args.serve_seconds - args.serve_warm
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    srv, streams = make_server(args.serve_batch)
+    clk.start()
+    arr, fails, n_events, _ = serve_trace(xg, srv, streams, pools, args.serve_seconds, args.serve_warm, rate, 5)
+    clocks = clk.stop()
+    stats = srv.stats()
+    srv.close()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    batched = serve_summary(arr, window)
+    # the same trace, each picture alone (one picture per batch)
+    srv1, streams1 = make_server(1)
+    arr1, fails1, _, _ = serve_trace(xg, srv1, streams1, pools, args.serve_seconds, args.serve_warm, rate, 5)
+    srv1.close()
+    alone = serve_summary(arr1, window)
+    if rank != 0:
+        return
+    px = {r: SERVE_RES[r][0] * SERVE_RES[r][1] for r in range(4)}
+    mean_px = float(np.mean([px[r] for r in res_idx]))
+    line = {
+        "metric": SERVE_METRIC, "value": batched.get("p99_ms"), "unit": "ms", "n_gpus": world,
+        "steps": batched.get("frames"), "warmup": args.serve_warm, "ms_per_step": batched.get("mean_ms"),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "serve_64_streams_mixed", "streams": nstreams,
+                   "resolutions": {"%dx%d" % SERVE_RES[r]: int((res_idx == r).sum()) for r in range(4)},
+                   "arrivals": "Poisson 30 fps per stream", "seconds": args.serve_seconds, "warm_s": args.serve_warm,
+                   "search_range": args.serve_range, "qp": QP, "refs": 2,
+                   "picture_job": "reference update + sub-pel planes, FS +-%d + quarter-pel SATD over the leaf-CU "
+                                  "PUs of a seeded split map, MC residual, TU chain, reconstruction" % args.serve_range},
+        "batched": batched, "unbatched_same_trace": alone,
+        "submit_failures": {"batched": fails, "unbatched": fails1}, "offered_pictures": n_events,
+        "server": stats,
+        "e2e": {"value": batched.get("frames_per_s"), "unit": "pictures/s",
+                "h2d_bytes_per_step": int(mean_px), "d2h_bytes_per_step": 8},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+# ---- full-picture chain at 4K ------------------------------------------------
+CHAIN_METRIC = "P pictures/s, 3840x2160 hot-path chain (4 refs, FS +-64 + quarter-pel SATD, MC, TU chain, recon; CUDA graph)"
+
+
+def run_chain(args):
+    import torch
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    W, H, NR, R = args.chain_width, args.chain_height, 4, RANGE
+    frames = synth.chain_pictures(NR + 2, W, H, seed=21 + rank)
+    cus_list = xg.split_map_cus(W, H, 31 + rank)
+    pus, cus = xg.cu_pus(cus_list, W, H, NR)
+    sess = xg.MeSession(W, H, NR, len(pus))
+    sess.set_pus(pus)
+    chain = xg.Chain(sess, cus, QP, feedback=True)
+    prm = xg.MeParams(R, lambda_factor(QP), 1, 2, 0, 0)
+    order = [frames[NR]] + [frames[NR - 1 - r] for r in range(NR)]   # current, then refs k-1 .. k-4
+    for idx, img in enumerate(order):
+        assert lib.xavs2gpu_copy_h2d(ctypes.c_void_p(chain.source(idx)), xg.ptr(img), img.nbytes) == 0
+    tune_ms = chain.autotune(prm, reps=1)
+    tun = chain.tuning()
+    chain.capture(prm)
+    nk = chain.graph_kernels()
+    stream = torch.cuda.ExternalStream(sess.stream())
+    for _ in range(args.warmup):
+        chain.launch()
+    sess.sync()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    clk.start()
+    ev[0].record(stream)
+    for _ in range(args.steps):
+        chain.launch()
+    ev[1].record(stream)
+    sess.sync()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    total_ms = ev[0].elapsed_time(ev[1])
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    total_ms = reduce_max(total_ms, "cuda")
+    fps = args.steps * world / (total_ms / 1e3)
+    # end to end: each picture uploaded from pinned host memory, the
+    # reconstruction read back
+    h_in = torch.from_numpy(frames[NR + 1]).pin_memory()
+    h_out = torch.empty(W * H, dtype=torch.uint8).pin_memory()
+    o = chain.outputs()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lib.xavs2gpu_me_sync(sess.h)
+        assert lib.xavs2gpu_copy_h2d(ctypes.c_void_p(chain.source(0)), ctypes.c_void_p(h_in.data_ptr()), W * H) == 0
+        chain.launch()
+        lib.xavs2gpu_me_sync(sess.h)
+        assert lib.xavs2gpu_copy_d2h(ctypes.c_void_p(h_out.data_ptr()), ctypes.c_void_p(o.recon), W * H) == 0
+    e2e_fps = args.steps / (time.perf_counter() - t0)
+    # CPU baseline: the oracle's search over a sample of the picture's PU
+    # searches (the search is ~99 % of the chain's work), scaled to pictures
+    evals = count_evals(pus, R)
+    cpu_e, cpu_s, cpu_n = cpu_sample_search(pus, order[0], order[1:], (R, prm.lambda_factor, 1, 2, 0, 0),
+                                            args.cpu_fraction / 8, 9, os.cpu_count() or 1)
+    cpu_fps = (cpu_e / cpu_s) / evals
+    if rank != 0:
+        return
+    line = {
+        "metric": CHAIN_METRIC, "value": fps, "unit": "pictures/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "chain_2160p_4ref", "width": W, "height": H, "refs": NR, "search_range": R, "qp": QP,
+                   "leaf_cus": int(len(cus)), "pu_searches": int(len(pus)), "evals_per_picture": evals,
+                   "content": "pan 12 px/picture + 2 block-local motions, seeded split map 64..8",
+                   "l2": "inputs larger than L2 (%d MB of reference planes)" % (NR * 16 * (W + 160) * (H + 160) >> 20)},
+        "graph": {"kernels_per_launch": nk, "autotuned": {"refine_split_px": tun.me.refine_split_px,
+                                                            "refine_block": tun.me.refine_block,
+                                                            "tq_warps": tun.tq_warps, "ms_per_picture": tune_ms}},
+        "e2e": {"value": e2e_fps, "unit": "pictures/s", "h2d_bytes_per_step": W * H, "d2h_bytes_per_step": W * H},
+        "gpu_launches": int(launches),
+        "cpu_baseline": {"value": cpu_fps, "unit": "pictures/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": "oracle search over a random %.3f%% (%d) of the picture's PU searches, scaled"
+                                   % (100 * args.cpu_fraction / 8, cpu_n)},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    chain.close()
+    sess.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -559,12 +813,36 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
-    ap.add_argument("--workload", choices=["me", "tq"], default="me",
-                    help="me: batched motion search (default); tq: batched transform+quant")
+    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve"], default="me",
+                    help="me: batched motion search (default); tq: batched transform+quant; chain: 4K full-picture "
+                         "chain; serve: 64-stream serving")
+    ap.add_argument("--chain-width", type=int, default=3840)
+    ap.add_argument("--chain-height", type=int, default=2160)
     ap.add_argument("--tq-blocks", type=int, default=1000000)
+    ap.add_argument("--tq-parts", default="0,1,2,3,4", help="TU shapes (LumaPU indices) of the tq workload")
+    ap.add_argument("--serve-streams", type=int, default=64)
+    ap.add_argument("--serve-seconds", type=float, default=8.0)
+    ap.add_argument("--serve-warm", type=float, default=2.0)
+    ap.add_argument("--serve-range", type=int, default=16)
+    ap.add_argument("--serve-batch", type=int, default=64)
+    ap.add_argument("--serve-pool", type=int, default=4)
+    ap.add_argument("--serve-hbm-gb", type=int, default=64)
     args = ap.parse_args()
     if args.workload == "tq":
         run_tq(args)
+    elif args.workload == "chain":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "metric": CHAIN_METRIC,
+                              "unavailable": "timed as the cpu_baseline of this workload's own line"}))
+        else:
+            run_chain(args)
+    elif args.workload == "serve":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "metric": SERVE_METRIC,
+                              "unavailable": "the reference has no serving path; its per-picture CPU cost is the "
+                                             "--workload me reference arm"}))
+        else:
+            run_serve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

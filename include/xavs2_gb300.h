@@ -394,7 +394,8 @@ XAVS2GPU_API int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_sessi
                                        const xavs2gpu_me_params_t *prm, void *stream);
 /* Make the session enqueue on `stream` (NULL: back to its own stream).  No
  * synchronisation: work already enqueued on the previous stream must be
- * ordered before the next by the caller. */
+ * ordered before the next by the caller, and a session must be switched
+ * back (or destroyed) before its external stream is destroyed. */
 XAVS2GPU_API int xavs2gpu_me_set_stream(xavs2gpu_me_session_t *s, void *stream);
 /* Device table of the reference planes in the current slot order: entry
  * 16 r + k = plane k of reference r (updated in place, stream-ordered, by
@@ -525,6 +526,9 @@ XAVS2GPU_API int xavs2gpu_server_submit(xavs2gpu_server_t *s, int stream, const 
 XAVS2GPU_API int xavs2gpu_server_poll(xavs2gpu_server_t *s, xavs2gpu_server_result_t *out, int max, int timeout_ms);
 XAVS2GPU_API void xavs2gpu_server_stats(xavs2gpu_server_t *s, int64_t *hbm_used, int64_t *batches, int64_t *frames,
                                         int64_t *pending);
+/* Sum over completed batches of their device time (first to last command)
+ * and of the scheduler's time to enqueue them, in ms. */
+XAVS2GPU_API void xavs2gpu_server_timing(xavs2gpu_server_t *s, double *gpu_ms, double *host_ms);
 
 /* ---- allocation-free motion search ---------------------------------------
  * No counterpart in the reference.  The same search as xavs2gpu_me_run

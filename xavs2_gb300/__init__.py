@@ -130,6 +130,14 @@ _SIGS = {
     "xavs2gpu_me_batch_run": (_I, [_P, _P, _I, _P, _P]),
     "xavs2gpu_me_set_stream": (_I, [_P, _P]),
     "xavs2gpu_me_rotate_refs": (_I, [_P]),
+    "xavs2gpu_me_plane_table_device": (_P, [_P]),
+    "xavs2gpu_server_create": (_P, [_P]),
+    "xavs2gpu_server_destroy": (None, [_P]),
+    "xavs2gpu_server_open_stream": (_I, [_P, _I, _I, _P, _I, _P, _I, _I]),
+    "xavs2gpu_server_submit": (_I, [_P, _I, _P, _S, ctypes.c_int64]),
+    "xavs2gpu_server_poll": (_I, [_P, _P, _I, _I]),
+    "xavs2gpu_server_stats": (None, [_P, _P, _P, _P, _P]),
+    "xavs2gpu_server_timing": (None, [_P, _P, _P]),
 }
 
 _PIXEL_CMP = ["sad", "satd", "sa8d", "ssd"]
@@ -300,6 +308,77 @@ class MeBatch:
     def close(self):
         if self.h:
             self.lib.xavs2gpu_me_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_pixels", ctypes.c_int64),
+                ("max_batch_frames", ctypes.c_int32), ("qp", ctypes.c_int32), ("me", MeParams)]
+
+
+SERVER_RESULT_DTYPE = np.dtype([("stream", "<i4"), ("frame", "<i4"), ("tag", "<i8"), ("t_submit_ns", "<i8"),
+                                ("t_done_ns", "<i8"), ("hash", "<u8"), ("batch_frames", "<i4"),
+                                ("ref_only", "<i4")])
+
+
+def output_hash(recon, coef, results):
+    """The serving checksum of a picture (xavs2gpu_server_result_t.hash):
+    sum over the 32-bit words w_i of [reconstruction | levels | search
+    results] of (w_i + 1) * (2 i + 1), modulo 2^64."""
+    words = np.concatenate([np.ascontiguousarray(recon).view(np.uint32).ravel(),
+                            np.ascontiguousarray(coef).view(np.uint32).ravel(),
+                            np.ascontiguousarray(results).view(np.uint32).ravel()]).astype(np.uint64)
+    idx = np.arange(len(words), dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        return int(np.sum((words + np.uint64(1)) * (np.uint64(2) * idx + np.uint64(1)), dtype=np.uint64))
+
+
+class Server:
+    """Continuous-batching server over many streams (xavs2gpu_server_*)."""
+
+    def __init__(self, cfg):
+        self.lib = load()
+        self.cfg = cfg
+        self.h = self.lib.xavs2gpu_server_create(ctypes.byref(cfg))
+        if not self.h:
+            raise RuntimeError("xavs2gpu_server_create failed: %s" % self.lib.xavs2gpu_get_error())
+        self._keep = []
+
+    def open_stream(self, width, height, pus, cus, ring=8):
+        pus = np.ascontiguousarray(pus, dtype=PU_DTYPE)
+        cus = np.ascontiguousarray(cus, dtype=CU_DTYPE)
+        sid = self.lib.xavs2gpu_server_open_stream(self.h, width, height, ptr(pus), len(pus), ptr(cus), len(cus),
+                                                   ring)
+        return sid
+
+    def submit(self, sid, img, tag=0):
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        return self.lib.xavs2gpu_server_submit(self.h, sid, ptr(img), img.shape[1], tag)
+
+    def poll(self, max_results=4096, timeout_ms=0):
+        out = np.zeros(max_results, SERVER_RESULT_DTYPE)
+        k = self.lib.xavs2gpu_server_poll(self.h, ptr(out), max_results, timeout_ms)
+        if k < 0:
+            raise RuntimeError("server_poll failed (%d)" % k)
+        return out[:k]
+
+    def stats(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        self.lib.xavs2gpu_server_stats(self.h, *[ctypes.byref(x) for x in v])
+        g, h = ctypes.c_double(), ctypes.c_double()
+        self.lib.xavs2gpu_server_timing(self.h, ctypes.byref(g), ctypes.byref(h))
+        return {"hbm_used": v[0].value, "batches": v[1].value, "frames": v[2].value, "pending": v[3].value,
+                "gpu_ms": g.value, "host_enqueue_ms": h.value}
+
+    def close(self):
+        if self.h:
+            self.lib.xavs2gpu_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

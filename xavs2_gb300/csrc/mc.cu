@@ -187,7 +187,9 @@ __device__ __forceinline__ void planes_rows(const uint8_t (*s_src)[PS_C], const 
     for (int j = 0; j < 8; j++) fetch(cur + j, win[j]);
     uint32_t out[4] = {0, 0, 0, 0};
     bool have = false;
-#pragma unroll
+    // rolled: the body is the whole per-row filter, and the four phases' code
+    // must stay small enough for the instruction cache
+#pragma unroll 1
     for (int t = 0; t < 8; t++) {
         const int y = ys + t;
         if (y >= H + pad) break;

@@ -1234,6 +1234,19 @@ extern "C" const uint8_t *const *xavs2gpu_me_plane_table_device(xavs2gpu_me_sess
     return s ? (const uint8_t *const *)(s->impl.d_plane_ptrs + 1) : nullptr;
 }
 
+// Rotates the reference tables on the device (stream-ordered, no host
+// staging): reference r takes reference r-1's planes, reference 0 the last's.
+__global__ void rotate_tables_kernel(uint8_t **plane_ptrs, const uint8_t **ref0, int nrefs)
+{
+    const int k = threadIdx.x;   // one thread per sub-pel position, 16 threads
+    uint8_t *last = plane_ptrs[1 + 16 * (nrefs - 1) + k];
+    for (int r = nrefs - 1; r > 0; r--) plane_ptrs[1 + 16 * r + k] = plane_ptrs[1 + 16 * (r - 1) + k];
+    plane_ptrs[1 + k] = last;
+    __syncthreads();
+    if (k == 0)
+        for (int r = 0; r < nrefs; r++) ref0[r] = plane_ptrs[1 + 16 * r];
+}
+
 extern "C" int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s)
 {
     if (!s) return XAVS2GPU_ERR_ARG;
@@ -1242,7 +1255,9 @@ extern "C" int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s)
     const int last = m.slot_buf[m.nrefs - 1];
     for (int r = m.nrefs - 1; r > 0; r--) m.slot_buf[r] = m.slot_buf[r - 1];
     m.slot_buf[0] = last;
-    refresh_tables(m);
+    rotate_tables_kernel<<<1, 16, 0, m.st>>>(m.d_plane_ptrs, m.d_ref0, m.nrefs);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
 }
 
@@ -1251,6 +1266,8 @@ struct BatchBuf {
     uint32_t *d_lists = nullptr;    // generic | small | large
     SessView *d_views = nullptr;
     size_t cap_jobs = 0, cap_lists = 0, cap_views = 0;
+    uint8_t *h_stage = nullptr;     // pinned: jobs | lists | views (uploads without a stream wait)
+    size_t cap_stage = 0;
     cudaEvent_t done = nullptr;
     bool used = false;
 };
@@ -1279,7 +1296,7 @@ extern "C" void xavs2gpu_me_batch_destroy(xavs2gpu_me_batch_t *b)
     for (auto &x : b->buf) {
         if (x.used) cudaEventSynchronize(x.done);
         cudaEventDestroy(x.done);
-        cudaFree(x.d_jobs); cudaFree(x.d_lists); cudaFree(x.d_views);
+        cudaFree(x.d_jobs); cudaFree(x.d_lists); cudaFree(x.d_views); cudaFreeHost(x.h_stage);
     }
     delete b;
 }
@@ -1337,13 +1354,20 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     grow(bb.d_jobs, bb.cap_jobs, b->jobs.size());
     grow(bb.d_lists, bb.cap_lists, b->lists.size());
     grow(bb.d_views, bb.cap_views, b->views.size());
-    if (!b->jobs.empty())
-        XG_CUDA(cudaMemcpyAsync(bb.d_jobs, b->jobs.data(), sizeof(CtuJob) * b->jobs.size(), cudaMemcpyHostToDevice, st));
-    if (!b->lists.empty())
-        XG_CUDA(cudaMemcpyAsync(bb.d_lists, b->lists.data(), sizeof(uint32_t) * b->lists.size(),
-                                cudaMemcpyHostToDevice, st));
-    XG_CUDA(cudaMemcpyAsync(bb.d_views, b->views.data(), sizeof(SessView) * b->views.size(), cudaMemcpyHostToDevice,
-                            st));
+    const size_t bj = sizeof(CtuJob) * b->jobs.size(), bl = sizeof(uint32_t) * b->lists.size();
+    const size_t bv = sizeof(SessView) * b->views.size();
+    const size_t oj = 0, ol = align_up(bj), ov = ol + align_up(bl), need = ov + align_up(bv);
+    if (need > bb.cap_stage) {
+        cudaFreeHost(bb.h_stage);
+        bb.cap_stage = need + need / 4 + 4096;
+        XG_CUDA(cudaMallocHost((void **)&bb.h_stage, bb.cap_stage));
+    }
+    memcpy(bb.h_stage + oj, b->jobs.data(), bj);
+    memcpy(bb.h_stage + ol, b->lists.data(), bl);
+    memcpy(bb.h_stage + ov, b->views.data(), bv);
+    if (bj) XG_CUDA(cudaMemcpyAsync(bb.d_jobs, bb.h_stage + oj, bj, cudaMemcpyHostToDevice, st));
+    if (bl) XG_CUDA(cudaMemcpyAsync(bb.d_lists, bb.h_stage + ol, bl, cudaMemcpyHostToDevice, st));
+    XG_CUDA(cudaMemcpyAsync(bb.d_views, bb.h_stage + ov, bv, cudaMemcpyHostToDevice, st));
     const int ng = (int)gen.size(), ns = (int)small.size(), nl = (int)large.size();
     const uint32_t *d_gen = bb.d_lists, *d_small = bb.d_lists + ng, *d_large = bb.d_lists + ng + ns;
     reset_keys_kernel<<<152 * 4, 256, 0, st>>>(bb.d_views, n);

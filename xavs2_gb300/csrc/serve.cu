@@ -183,7 +183,7 @@ struct Job {
 
 struct BatchSet {
     cudaStream_t st = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr, done = nullptr;
     int16_t *d_res = nullptr, *d_rres = nullptr, *d_coef = nullptr;
     uint8_t *d_recon = nullptr;
     int32_t *d_nnz = nullptr;
@@ -221,6 +221,7 @@ struct xavs2gpu_server {
     bool stop = false;
     std::thread sched, comp;
     int64_t batches = 0, frames_batched = 0;
+    double gpu_ms = 0.0, host_ms = 0.0;       // batch start->done on the device; scheduler enqueue time
 };
 
 namespace {
@@ -232,6 +233,7 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
     // per picture: upload, reference update, planes (all on the set's stream)
     std::vector<xavs2gpu_me_session_t *> sess;
     b.searched.clear();
+    XG_CUDA(cudaEventRecord(b.start, b.st));
     int64_t res_off = 0, coef_off = 0, cu_start = 0, rec_off = 0;
     int nv = 0;
     for (size_t k = 0; k < b.jobs.size(); k++) {
@@ -327,8 +329,11 @@ void scheduler(xavs2gpu_server_t *s)
         for (auto &j : take) s->streams[j.stream]->in_flight = true;
         s->next_set = (int)(&b - s->sets) ^ 1;
         lk.unlock();
+        const int64_t t0 = now_ns();
         enqueue_batch(s, b);
+        const int64_t t1 = now_ns();
         lk.lock();
+        s->host_ms += (t1 - t0) / 1e6;
         s->inflight.push_back((int)(&b - s->sets));
         s->batches++;
         s->frames_batched += (int64_t)take.size();
@@ -348,7 +353,10 @@ void completer(xavs2gpu_server_t *s)
         lk.unlock();
         cudaEventSynchronize(b.done);
         const int64_t t = now_ns();
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b.start, b.done);
         lk.lock();
+        s->gpu_ms += ms;
         s->inflight.pop_front();
         std::vector<int> hidx(b.jobs.size(), -1);
         for (size_t q = 0; q < b.searched.size(); q++) hidx[b.searched[q]] = (int)q;
@@ -381,6 +389,7 @@ void free_set(BatchSet &b)
     cudaFreeHost(b.h_hash); cudaFreeHost(b.h_views);
     if (b.me) xavs2gpu_me_batch_destroy(b.me);
     if (b.done) cudaEventDestroy(b.done);
+    if (b.start) cudaEventDestroy(b.start);
     if (b.st) cudaStreamDestroy(b.st);
 }
 
@@ -400,7 +409,8 @@ extern "C" xavs2gpu_server_t *xavs2gpu_server_create(const xavs2gpu_server_confi
     s->max_cus = frame_cap_cus(px);
     for (auto &b : s->sets) {
         XG_CUDA(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
-        XG_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
+        XG_CUDA(cudaEventCreate(&b.start));
+        XG_CUDA(cudaEventCreate(&b.done));
         XG_CUDA(cudaMalloc((void **)&b.d_res, sizeof(int16_t) * px));
         XG_CUDA(cudaMalloc((void **)&b.d_rres, sizeof(int16_t) * px));
         XG_CUDA(cudaMalloc((void **)&b.d_coef, sizeof(int16_t) * px));
@@ -437,16 +447,16 @@ extern "C" void xavs2gpu_server_destroy(xavs2gpu_server_t *s)
     s->sched.join();
     s->comp.join();
     cudaSetDevice(s->device);
-    for (auto &b : s->sets) {
-        cudaStreamSynchronize(b.st);
-        free_set(b);
-    }
+    for (auto &b : s->sets) cudaStreamSynchronize(b.st);
+    // sessions first: they may still point at the batch streams
     for (Stream *S : s->streams) {
         if (!S) continue;
+        xavs2gpu_me_set_stream(S->sess, nullptr);
         xavs2gpu_me_destroy(S->sess);
         cudaFree(S->d_cus); cudaFree(S->d_in); cudaFree(S->d_prev); cudaFreeHost(S->h_ring);
         delete S;
     }
+    for (auto &b : s->sets) free_set(b);
     delete s;
 }
 
@@ -556,4 +566,12 @@ extern "C" void xavs2gpu_server_stats(xavs2gpu_server_t *s, int64_t *hbm_used, i
     if (batches) *batches = s->batches;
     if (frames) *frames = s->frames_batched;
     if (pending) *pending = (int64_t)s->pending.size();
+}
+
+extern "C" void xavs2gpu_server_timing(xavs2gpu_server_t *s, double *gpu_ms, double *host_ms)
+{
+    if (!s) return;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (gpu_ms) *gpu_ms = s->gpu_ms;
+    if (host_ms) *host_ms = s->host_ms;
 }

@@ -30,11 +30,15 @@ namespace tqw {
 // Forward table of an N-point transform: row k holds T_N[k][0..N) as N/4
 // words (byte j of word w = T_N[k][4w + j]).  Inverse table: row n holds
 // T_N[0..N)[n].  N = 4, 8, 16, 32 at word offsets 0, 4, 20, 84; then the 4x4
-// secondary transform M (rows of M, resp. of M^T) at 340.
-constexpr int kTabWords = 344;
+// secondary transform M (rows of M, resp. of M^T) at 340; then, for the
+// even/odd split of N = 8, 16, 32 (at 344, 348, 364), the odd rows on half a
+// line: forward row k < N/2 holds T_N[2k+1][0..N/2), inverse row n < N/2
+// holds T_N[2k+1][n] over k < N/2.
+constexpr int kTabWords = 428;
 struct PackedTab { uint32_t w[kTabWords]; };
 
 __host__ __device__ constexpr int tab_off(int N) { return N == 4 ? 0 : N == 8 ? 4 : N == 16 ? 20 : 84; }
+__host__ __device__ constexpr int odd_off(int N) { return N == 8 ? 344 : N == 16 ? 348 : 364; }
 constexpr int kSec = 340;
 
 constexpr int sec4c(int i, int k)
@@ -58,6 +62,13 @@ constexpr PackedTab make_tab(bool inverse)
             const int v = inverse ? sec4c(j, r) : sec4c(r, j);
             t.w[kSec + r] |= (uint32_t)(uint8_t)(int8_t)v << (8 * j);
         }
+    for (int N = 8; N <= 32; N *= 2)
+        for (int r = 0; r < N / 2; r++)
+            for (int j = 0; j < N / 2; j++) {
+                const int v = inverse ? basis32((2 * j + 1) * (32 / N), r) : basis32((2 * r + 1) * (32 / N), j);
+                const int word = odd_off(N) + r * (N / 8) + j / 4;
+                t.w[word] |= (uint32_t)(uint8_t)(int8_t)v << (8 * (j % 4));
+            }
     return t;
 }
 
@@ -117,6 +128,65 @@ __device__ __forceinline__ void load_pairs_global(const int16_t *p, bool al, uin
     }
 #pragma unroll
     for (int i = 0; i < N / 2; i++) xp[i] = pack16(p[2 * i], p[2 * i + 1]);
+}
+
+// Forward N-point transform (N >= 8) of one line by a single even/odd split:
+// y[2k] = T_{N/2} (x[n] + x[N-1-n]), y[2k+1] = odd rows . (x[n] - x[N-1-n]),
+// both as dp2a dot products over the folded values packed in pairs.  The
+// folded values must fit 16 bits; `bad` reports a line where they do not
+// (the caller then takes the full-matrix product).  out(k, y[k]).
+template <int N>
+__device__ __forceinline__ void fold_line(const uint32_t (&xp)[N / 2], uint32_t (&ep)[N / 4], uint32_t (&op)[N / 4],
+                                          bool &bad)
+{
+    int x[N];
+#pragma unroll
+    for (int i = 0; i < N / 2; i++) {
+        x[2 * i] = (int)(int16_t)(xp[i] & 0xFFFFu);
+        x[2 * i + 1] = ((int)xp[i]) >> 16;
+    }
+#pragma unroll
+    for (int m = 0; m < N / 4; m++) {
+        const int e0 = x[2 * m] + x[N - 1 - 2 * m], e1 = x[2 * m + 1] + x[N - 2 - 2 * m];
+        const int o0 = x[2 * m] - x[N - 1 - 2 * m], o1 = x[2 * m + 1] - x[N - 2 - 2 * m];
+        bad |= (unsigned)(e0 + 32768) > 65535u || (unsigned)(e1 + 32768) > 65535u ||
+               (unsigned)(o0 + 32768) > 65535u || (unsigned)(o1 + 32768) > 65535u;
+        ep[m] = pack16(e0, e1);
+        op[m] = pack16(o0, o1);
+    }
+}
+
+template <int N, typename Out>
+__device__ __forceinline__ void fwd_folded(const uint32_t (&ep)[N / 4], const uint32_t (&op)[N / 4], Out out)
+{
+    const uint32_t *fe = &c_fwd.w[tab_off(N / 2)], *fo = &c_fwd.w[odd_off(N)];
+#pragma unroll 2
+    for (int k = 0; k < N / 2; k++) {
+        out(2 * k, dot_row<N / 2>(ep, fe + k * (N / 8)));
+        out(2 * k + 1, dot_row<N / 2>(op, fo + k * (N / 8)));
+    }
+}
+
+// Inverse N-point transform (N >= 8) of one line of 16-bit coefficients
+// (always exact): x[n] = E[n] + O[n], x[N-1-n] = E[n] - O[n] with E the
+// N/2-point inverse of the even coefficients and O the odd rows.
+template <int N, typename Out>
+__device__ __forceinline__ void inv_split(const uint32_t (&cp)[N / 2], Out out)
+{
+    uint32_t ce[N / 4], co[N / 4];
+#pragma unroll
+    for (int m = 0; m < N / 4; m++) {
+        ce[m] = __byte_perm(cp[2 * m], cp[2 * m + 1], 0x5410);
+        co[m] = __byte_perm(cp[2 * m], cp[2 * m + 1], 0x7632);
+    }
+    const uint32_t *ie = &c_inv.w[tab_off(N / 2)], *io = &c_inv.w[odd_off(N)];
+#pragma unroll 2
+    for (int n = 0; n < N / 2; n++) {
+        const int e = dot_row<N / 2>(ce, ie + n * (N / 8));
+        const int o = dot_row<N / 2>(co, io + n * (N / 8));
+        out(n, e + o);
+        out(N - 1 - n, e - o);
+    }
 }
 
 // ---- shapes ------------------------------------------------------------------
@@ -256,10 +326,20 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
             }
         }
         if (!done) {
-            const uint32_t *rows = &c_fwd.w[tab_off(TW)];
+            auto put = [&](int k, int v) { tA[k * P1 + l] = (int16_t)((v + ((1 << S::S1) >> 1)) >> S::S1); };
+            bool full = TW < 8;
+            if constexpr (TW >= 8) {
+                uint32_t ep[TW / 4], op[TW / 4];
+                bool bad = false;
+                fold_line<TW>(xp, ep, op, bad);
+                full = __any_sync(__activemask(), bad);
+                if (!full) fwd_folded<TW>(ep, op, put);
+            }
+            if (full) {
+                const uint32_t *rows = &c_fwd.w[tab_off(TW)];
 #pragma unroll 2
-            for (int k = 0; k < TW; k++)
-                tA[k * P1 + l] = (int16_t)((dot_row<TW>(xp, rows + k * (TW / 4)) + ((1 << S::S1) >> 1)) >> S::S1);
+                for (int k = 0; k < TW; k++) put(k, dot_row<TW>(xp, rows + k * (TW / 4)));
+            }
         }
     }
     __syncwarp();
@@ -276,16 +356,26 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
         uint32_t cp[TH / 2];
         load_pairs<TH>(tA + l * P1, cp);
         int16_t *co = cx.coef + b.coef_offset + l;
-        const uint32_t *rows = sec ? &c_fwd.w[kSec] : &c_fwd.w[tab_off(TH)];
-#pragma unroll 2
-        for (int m = 0; m < TH; m++) {
-            const int s = dot_row<TH>(cp, rows + m * (TH / 4));
+        auto put = [&](int m, int s) {
             const int y = sec ? clipb((s + 128) >> 8, 16) : (int)(int16_t)((s + ((1 << S::S2) >> 1)) >> S::S2);
             const int a = (y < 0 ? -y : y) * qscale + qadd;
             const int q = y < 0 ? -(a >> qshift) : (a >> qshift);
             co[m * TW] = (int16_t)q;
             nz += q != 0;
             tA[l * P1 + m] = (int16_t)clipb((q * dqscale + (1 << (dqshift - 1))) >> dqshift, 16);
+        };
+        bool full = TH < 8;
+        if constexpr (TH >= 8) {
+            uint32_t ep[TH / 4], op[TH / 4];
+            bool bad = false;
+            fold_line<TH>(cp, ep, op, bad);
+            full = __any_sync(__activemask(), bad);
+            if (!full) fwd_folded<TH>(ep, op, put);
+        }
+        if (full) {
+            const uint32_t *rows = sec ? &c_fwd.w[kSec] : &c_fwd.w[tab_off(TH)];
+#pragma unroll 2
+            for (int m = 0; m < TH; m++) put(m, dot_row<TH>(cp, rows + m * (TH / 4)));
         }
     }
 #pragma unroll
@@ -307,10 +397,14 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
     if (inv && l < TW) {
         uint32_t cp[TH / 2];
         load_pairs<TH>(tA + l * P1, cp);
-        const uint32_t *rows = sec ? &c_inv.w[kSec] : &c_inv.w[tab_off(TH)];
+        auto put = [&](int n, int v) { t2[n * P2 + l] = (int16_t)clipb((v + 16) >> 5, 16); };
+        if constexpr (TH >= 8) {
+            inv_split<TH>(cp, put);
+        } else {
+            const uint32_t *rows = sec ? &c_inv.w[kSec] : &c_inv.w[tab_off(TH)];
 #pragma unroll 2
-        for (int n = 0; n < TH; n++)
-            t2[n * P2 + l] = (int16_t)clipb((dot_row<TH>(cp, rows + n * (TH / 4)) + 16) >> 5, 16);
+            for (int n = 0; n < TH; n++) put(n, dot_row<TH>(cp, rows + n * (TH / 4)));
+        }
     }
     __syncwarp();
 
@@ -324,9 +418,13 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
         const uint32_t *rows = sec ? &c_inv.w[kSec] : &c_inv.w[tab_off(TW)];
         const int sh = sec ? 14 : 12 - F, bits = sec ? 9 : 9 + F;
         int16_t *o = stage + l * PS;
+        auto put = [&](int x, int v) { o[x] = (int16_t)clipb((v + (1 << (sh - 1))) >> sh, bits); };
+        if constexpr (TW >= 8) {
+            inv_split<TW>(vp, put);
+        } else {
 #pragma unroll 2
-        for (int x = 0; x < TW; x++)
-            o[x] = (int16_t)clipb((dot_row<TW>(vp, rows + x * (TW / 4)) + (1 << (sh - 1))) >> sh, bits);
+            for (int x = 0; x < TW; x++) put(x, dot_row<TW>(vp, rows + x * (TW / 4)));
+        }
     }
     __syncwarp();
     if constexpr (!S::WAV) {

@@ -114,3 +114,15 @@ def tq_residual(blocks, zero, total, seed=4, device="cpu"):
     keep = torch.from_numpy((~zero).astype(np.int16)).to(device)
     res *= torch.repeat_interleave(keep, torch.from_numpy(size).to(device), output_size=total)
     return res
+
+
+def chain_pictures(n, width, height, seed=21, pan_px=12, n_motions=2, max_px=4):
+    """Pictures for the full-picture chain: a base picture, then each picture
+    = the previous one panned by `pan_px` pixels to the left plus
+    `n_motions` block-local quarter-pel motions U[-max_px, max_px] and noise."""
+    rng = np.random.default_rng(seed)
+    frames = [base_picture(rng, width, height)]
+    for _ in range(n - 1):
+        panned = shift_qpel(frames[-1], 4 * pan_px, 0)
+        frames.append(next_picture(rng, panned, n_motions, max_px))
+    return frames
