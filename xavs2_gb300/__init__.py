@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libxavs2gpu.so")
+LIB_PATH = os.environ.get("XAVS2GPU_LIB") or os.path.join(HERE, "libxavs2gpu.so")
 
 # LumaPU order (source/common/pixel.h:50-65)
 PU_W = [4, 8, 16, 32, 64, 8, 4, 16, 8, 32, 16, 64, 32, 16, 12, 16, 4, 32, 24, 32, 8, 64, 48, 64, 16]

@@ -319,8 +319,13 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
     }
 }
 
+// resident CTAs per SM the register budget is sized for (4: 128 registers)
+#ifndef XG_CTU_MINB
+#define XG_CTU_MINB 4
+#endif
+
 template <bool BORDER>
-__global__ void __launch_bounds__(kCtuThreads, 4) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
+__global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
                                                             const SessView *__restrict__ views, int R, int lambda,
                                                             int ww)
 {

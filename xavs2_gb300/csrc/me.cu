@@ -561,7 +561,13 @@ __device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, c
     }
 }
 
-__global__ void __launch_bounds__(128) refine_thread_kernel(const uint32_t *__restrict__ list, int n,
+// resident CTAs per SM the register budget of the per-thread refinement is
+// sized for (0: the compiler's choice)
+#ifndef XG_REFINE_MINB
+#define XG_REFINE_MINB 0
+#endif
+
+__global__ void __launch_bounds__(128, XG_REFINE_MINB) refine_thread_kernel(const uint32_t *__restrict__ list, int n,
                                                             const SessView *__restrict__ views, int R,
                                                             xavs2gpu_me_params_t prm)
 {
@@ -658,6 +664,31 @@ __global__ void __launch_bounds__(128) refine_thread_kernel(const uint32_t *__re
     out[i] = res;
 }
 
+// Warp-cooperative cost of the PU at quarter-pel (mx, my): lanes take the
+// PU's rounding units (4x4 or 8x4; the same tiling sums the SAD) in turn,
+// rows read as aligned words.
+__device__ int qpel_cost_warp_vec(const xavs2gpu_pu_t &p, int w, int h, bool had, const uint8_t *o,
+                                  const uint8_t *const *planes, int stride, int mx, int my, int lane)
+{
+    const bool u4 = had ? satd_unit4(w, h) : (w == 4 || w == 12);
+    const int uw = u4 ? 4 : 8, nux = w / uw, nu = nux * (h >> 2);
+    const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(p.y + (my >> 2)) * stride + p.x + (mx >> 2);
+    int s = 0;
+    for (int u = lane; u < nu; u += 32) {
+        const int uy = u / nux, ux = u - uy * nux;
+        const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * uw;
+        int c[4][8];
+        if (u4) {
+            load_unit<true>(o + off, stride, c);
+            s += unit_cost_pre<true>(had, c, r + off, stride);
+        } else {
+            load_unit<false>(o + off, stride, c);
+            s += unit_cost_pre<false>(had, c, r + off, stride);
+        }
+    }
+    return warp_sum_i(s);
+}
+
 // One warp per search for the larger PUs, over a list.
 __global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *__restrict__ list, int n,
                                                                const SessView *__restrict__ views, int R,
@@ -705,10 +736,10 @@ __global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *_
         const uint8_t *const *planes = ref_planes + 16 * p.ref;
         const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
         int cx = bx, cy = by;
-        if (had) best = qpel_cost_warp(p, w, h, true, o, planes, g, cx, cy, lane) + mv_cost_hd(lam, cx, cy, pmx, pmy);
+        if (had) best = qpel_cost_warp_vec(p, w, h, true, o, planes, g.stride, cx, cy, lane) + mv_cost_hd(lam, cx, cy, pmx, pmy);
         for (int pos = 1; pos < 9; pos += step) {
             int mx = cx + 2 * c_spiral[pat][pos][0], my = cy + 2 * c_spiral[pat][pos][1];
-            int c = qpel_cost_warp(p, w, h, had, o, planes, g, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
+            int c = qpel_cost_warp_vec(p, w, h, had, o, planes, g.stride, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
             if (c < best) { best = c; bx = mx; by = my; }
         }
         if (prm.fractional_me > 1) {
@@ -727,7 +758,7 @@ __global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *_
                 } else {
                     mx = cx + sx; my = cy + sy;
                 }
-                int c = qpel_cost_warp(p, w, h, had, o, planes, g, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
+                int c = qpel_cost_warp_vec(p, w, h, had, o, planes, g.stride, mx, my, lane) + mv_cost_hd(lam, mx, my, pmx, pmy);
                 if (c < best) { best = c; bx = mx; by = my; }
             }
         }
