@@ -378,6 +378,12 @@ XAVS2GPU_API int xavs2gpu_me_get_tuning(const xavs2gpu_me_session_t *s, xavs2gpu
  * stream synchronisation) so that the next xavs2gpu_me_run only enqueues
  * device work -- required before capturing a run into a CUDA graph. */
 XAVS2GPU_API int xavs2gpu_me_prepare(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm);
+/* Autotuner (no counterpart in the reference): runs the search `reps` times
+ * for every candidate refinement split (0..4096 px) and CTA size (64, 128),
+ * keeps the fastest and returns its time per run in ms.  The results of a
+ * run never depend on the choice. */
+XAVS2GPU_API int xavs2gpu_me_autotune(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm, int reps,
+                                      float *best_ms);
 
 /* ---- several pictures per launch -------------------------------------------
  * No counterpart in the reference (its search runs one PU at a time).  The

@@ -112,6 +112,7 @@ _SIGS = {
     "xavs2gpu_me_set_tuning": (_I, [_P, _P]),
     "xavs2gpu_me_get_tuning": (_I, [_P, _P]),
     "xavs2gpu_me_prepare": (_I, [_P, _P]),
+    "xavs2gpu_me_autotune": (_I, [_P, _P, _I, _P]),
     "xavs2gpu_me_session_info": (None, [_P, _P, _P, _P, _P]),
     "xavs2gpu_me_session_pus": (_I, [_P, _P]),
     "xavs2gpu_chain_create": (_P, [_P, _P, _I, _I, _I]),
@@ -277,6 +278,14 @@ class MeSession:
         out = (ctypes.c_float * 4)()
         self._check(self.lib.xavs2gpu_me_phase_ms(self.h, out), "phase_ms")
         return list(out)
+
+    def autotune(self, params, reps=2):
+        """Picks the fastest refinement launch shapes (results unchanged)."""
+        ms = ctypes.c_float()
+        self._check(self.lib.xavs2gpu_me_autotune(self.h, ctypes.byref(params), reps, ctypes.byref(ms)), "autotune")
+        t = MeTuning()
+        self.lib.xavs2gpu_me_get_tuning(self.h, ctypes.byref(t))
+        return ms.value, (t.refine_split_px, t.refine_block)
 
     def set_stream(self, stream):
         self._check(self.lib.xavs2gpu_me_set_stream(self.h, ctypes.c_void_p(stream) if stream else None),

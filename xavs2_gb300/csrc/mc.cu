@@ -127,6 +127,25 @@ __constant__ int8_t c_luma_taps[4][8] = {
     {-1, 3, -7, 19, 57, -10, 4, -1},
 };
 
+// The three sub-pel phases of one axis from the 8 samples v[0..7] around a
+// position.  The AVS2 taps are symmetric (half-pel) and mirror images of
+// each other (quarter-pels: t3[k] = t1[7-k]), so with a_k = v[k] + v[7-k] and
+// d_k = v[k] - v[7-k]:
+//   p2      = -a0 + 4 a1 - 11 a2 + 40 a3
+//   2 p1    = S + D,  2 p3 = S - D,
+//   S = -2 a0 + 7 a1 - 17 a2 + 76 a3,  D = d1 - 3 d2 + 38 d3
+// (exactly the 8-tap sums; 11 multiply-adds for the three phases instead
+// of 24).  Returned: p2 and the doubled quarter-pel sums 2 p1, 2 p3.
+__device__ __forceinline__ void phases3(const int (&v)[8], int &p2, int &p1x2, int &p3x2)
+{
+    const int a0 = v[0] + v[7], a1 = v[1] + v[6], a2 = v[2] + v[5], a3 = v[3] + v[4];
+    const int d1 = v[1] - v[6], d2 = v[2] - v[5], d3 = v[3] - v[4];
+    p2 = -a0 + 4 * a1 - 11 * a2 + 40 * a3;
+    const int S = -2 * a0 + 7 * a1 - 17 * a2 + 76 * a3, D = d1 - 3 * d2 + 38 * d3;
+    p1x2 = S + D;
+    p3x2 = S - D;
+}
+
 constexpr int PT_W = 128, PT_H = 16;            // output tile of a padded plane
 constexpr int PS_R = PT_H + 7, PS_C = PT_W + 16; // source window (rows, pitch)
 
@@ -204,26 +223,28 @@ __device__ __forceinline__ void planes_rows(const uint8_t (*s_src)[PS_C], const 
             have = false;
         }
         if (!have) {
+            // rounding: fx = 0 (bytes) (s + 32) >> 6, else (s + 2048) >> 12;
+            // the quarter-pel sums come doubled, one more shift
+            constexpr int SH = FX == 0 ? 6 : 12;
+            uint32_t pk[4] = {0, 0, 0, 0};
 #pragma unroll
-            for (int fy = 0; fy < 4; fy++) {
-                if (FX == 0 && fy == 0) continue;
-                if (mode < 2 && fy != 0 && fy != 2) continue;
-                uint32_t pk = 0;
+            for (int c = 0; c < 4; c++) {
+                int v[8];
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    int v;
-                    if (fy == 0) {
-                        v = (win[3][c] + 32) >> 6;
-                    } else {
-                        int s = 0;
-#pragma unroll
-                        for (int j = 0; j < 8; j++) s += c_luma_taps[fy][j] * win[j][c];
-                        v = FX == 0 ? (s + 32) >> 6 : (s + 2048) >> 12;
-                    }
-                    pk |= (uint32_t)clip_pel_d(v) << (8 * c);
-                }
-                out[fy] = pk;
+                for (int j = 0; j < 8; j++) v[j] = win[j][c];
+                int p2, p1x2, p3x2;
+                phases3(v, p2, p1x2, p3x2);
+                const int q0 = (win[3][c] + 32) >> 6;
+                const int q1 = (p1x2 + (1 << SH)) >> (SH + 1);
+                const int q2 = (p2 + (1 << (SH - 1))) >> SH;
+                const int q3 = (p3x2 + (1 << SH)) >> (SH + 1);
+                pk[0] |= (uint32_t)clip_pel_d(q0) << (8 * c);
+                pk[1] |= (uint32_t)clip_pel_d(q1) << (8 * c);
+                pk[2] |= (uint32_t)clip_pel_d(q2) << (8 * c);
+                pk[3] |= (uint32_t)clip_pel_d(q3) << (8 * c);
             }
+#pragma unroll
+            for (int fy = 0; fy < 4; fy++) out[fy] = pk[fy];
             have = true;
         }
         const ptrdiff_t ro = (ptrdiff_t)y * stride + xg;
@@ -246,8 +267,13 @@ __device__ __forceinline__ void planes_rows(const uint8_t (*s_src)[PS_C], const 
 //   phase 3: thread = (row half, fx, 4-column group): slides an 8-row window
 //            down its 8 output rows and emits planes 4*fy + fx for fy = 0..3
 //            as 32-bit stores (a warp writes 128 contiguous bytes of a row).
+// resident 256-thread CTAs per SM the register budget is sized for
+#ifndef XG_PLANES_MINB
+#define XG_PLANES_MINB 3
+#endif
+
 template <bool VEC>
-__global__ void __launch_bounds__(256) frame_planes_kernel(const uint8_t *__restrict__ src, int stride, int W, int H,
+__global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const uint8_t *__restrict__ src, int stride, int W, int H,
                                                            int pad, PlaneSet planes, int mode)
 {
     __shared__ __align__(16) uint8_t s_src[PS_R][PS_C];
@@ -271,20 +297,24 @@ __global__ void __launch_bounds__(256) frame_planes_kernel(const uint8_t *__rest
 #pragma unroll
             for (int e = 0; e < 4; e++) b[4 * q + e] = (v >> (8 * e)) & 0xFF;
         }
+        int o[3][4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            int v[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = b[c + k];
+            int p2, p1x2, p3x2;
+            phases3(v, p2, p1x2, p3x2);
+            o[0][c] = p1x2 >> 1;
+            o[1][c] = p2;
+            o[2][c] = p3x2 >> 1;
+        }
 #pragma unroll
         for (int f = 0; f < 3; f++) {
             if (mode < 2 && f != 1) continue;
-            int o[4];
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                int v = 0;
-#pragma unroll
-                for (int k = 0; k < 8; k++) v += c_luma_taps[f + 1][k] * b[c + k];
-                o[c] = v;
-            }
             uint2 pk;
-            pk.x = (uint32_t)(o[0] & 0xFFFF) | ((uint32_t)o[1] << 16);
-            pk.y = (uint32_t)(o[2] & 0xFFFF) | ((uint32_t)o[3] << 16);
+            pk.x = (uint32_t)(o[f][0] & 0xFFFF) | ((uint32_t)o[f][1] << 16);
+            pk.y = (uint32_t)(o[f][2] & 0xFFFF) | ((uint32_t)o[f][3] << 16);
             *reinterpret_cast<uint2 *>(&s_hor[f][r][4 * g]) = pk;
         }
     }

@@ -442,23 +442,30 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
         // upsampling of the TW x TH low band in region B (pitch TW+2):
         // V[2y] = h[y], V[2y+1] = (h[y] + h[y+1]) >> 1 with h = LL >> 1 and
         // h[TH] = h[TH-1]; D[2i] = V[i], D[2i+1] = (V[i] + V[i+1]) >> 1 with
-        // V[TW] = V[TW-1].  One output word (2 samples) per lane and step.
-        if (inv) {
-            for (int e = lane; e < IH * TW; e += 32) {
-                const int r = e / TW, i = e % TW, in1 = i + 1 < TW ? i + 1 : i;
-                const int y = r >> 1, yn = y + 1 < TH ? y + 1 : y;
-                int v0 = stage[y * PS + i] >> 1, v1 = stage[y * PS + in1] >> 1;
-                if (r & 1) {
-                    v0 = (v0 + (stage[yn * PS + i] >> 1)) >> 1;
-                    v1 = (v1 + (stage[yn * PS + in1] >> 1)) >> 1;
-                }
-                const uint32_t w = pack16(v0, (v0 + v1) >> 1);
+        // V[TW] = V[TW-1].  Lane i walks low-band column i down the rows and
+        // writes output word i (samples 2i, 2i+1) of rows 2y and 2y+1: a
+        // warp stores whole rows.
+        if (inv && lane < TW) {
+            const int i = lane, in1 = i + 1 < TW ? i + 1 : i;
+            uint32_t *dw = reinterpret_cast<uint32_t *>(dst);
+            int h0 = stage[i] >> 1, h1 = stage[in1] >> 1;
+            for (int y = 0; y < TH; y++) {
+                const int yn = y + 1 < TH ? y + 1 : y;
+                const int n0 = stage[yn * PS + i] >> 1, n1 = stage[yn * PS + in1] >> 1;
+                const int v0 = (h0 + n0) >> 1, v1 = (h1 + n1) >> 1;
+                const uint32_t we = pack16(h0, (h0 + h1) >> 1), wo = pack16(v0, (v0 + v1) >> 1);
+                const int e = 2 * y * TW + i;
                 if (al_out) {
-                    reinterpret_cast<uint32_t *>(dst)[e] = w;
+                    dw[e] = we;
+                    dw[e + TW] = wo;
                 } else {
-                    dst[2 * e] = (int16_t)(w & 0xFFFF);
-                    dst[2 * e + 1] = (int16_t)(w >> 16);
+                    dst[2 * e] = (int16_t)(we & 0xFFFF);
+                    dst[2 * e + 1] = (int16_t)(we >> 16);
+                    dst[2 * (e + TW)] = (int16_t)(wo & 0xFFFF);
+                    dst[2 * (e + TW) + 1] = (int16_t)(wo >> 16);
                 }
+                h0 = n0;
+                h1 = n1;
             }
         }
     }
