@@ -290,18 +290,27 @@ def run_ours(args):
                               "config": {"width": WIDTH, "height": HEIGHT}, "plan": [n_ctu, n_gen, n_jobs]}))
         sess.close()
         return
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: the pictures and
+    # the result array live in page-locked host memory
     h2d = WIDTH * HEIGHT * (1 + NREFS)
     d2h = len(pus) * xg.RESULT_DTYPE.itemsize
-    out = np.zeros(len(pus), xg.RESULT_DTYPE)
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory()
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return t, v
+
+    keep = [pinned(cur)] + [pinned(r) for r in refs] + [pinned(np.zeros(len(pus), xg.RESULT_DTYPE))]
+    h_cur, h_refs, out = keep[0][1], [k[1] for k in keep[1:1 + NREFS]], keep[-1][1]
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
-        sess.set_picture(-1, cur)
-        for j, r in enumerate(refs):
+        sess.set_picture(-1, h_cur)
+        for j, r in enumerate(h_refs):
             sess.set_picture(j, r)
         sess.run(prm)
-        out = sess.results()
+        sess.results(out)
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_s = reduce_max(e2e_s, "cuda")

@@ -331,7 +331,10 @@ XAVS2GPU_API xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, in
 XAVS2GPU_API void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s);
 /* Load a picture: slot -1 = the current picture, 0..num_refs-1 = references
  * (their borders are replicated and their sub-pel planes computed on the
- * device).  _host copies from host memory, _device from device memory. */
+ * device).  _host copies from host memory, _device from device memory.  A
+ * page-locked host picture is copied asynchronously on the session stream
+ * (keep it unchanged until the stream has passed it, e.g. until the next
+ * get_results / sync); pageable memory is copied before the call returns. */
 XAVS2GPU_API int xavs2gpu_me_set_picture_host(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride);
 XAVS2GPU_API int xavs2gpu_me_set_picture_device(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride);
 /* Set the PU list (host memory).  The list is uploaded and planned once;

@@ -112,3 +112,41 @@ def test_golden_me(gpu):
     pus = np.ascontiguousarray(g["me_pus"]).view(xg.PU_DTYPE)
     got, _ = _run(g["me_cur"], [g["me_ref"]], pus, prm)
     assert got.tobytes() == g["me_out"].tobytes()
+
+
+def test_pinned_host_pictures_and_results(gpu):
+    """Page-locked host pictures take the asynchronous upload path and a
+    page-locked result array the direct download; results equal the
+    pageable path's."""
+    import torch
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(91)
+    w, h = 160, 96
+    f0 = synth.base_picture(rng, w, h)
+    f1 = synth.next_picture(rng, f0, 4, 5)
+    pus = xg.frame_pus(w, h, 1)
+    prm = xg.MeParams(8, oracle.lambda_factor(32), 1, 2, 0, 0)
+    s = xg.MeSession(w, h, 1, len(pus))
+    s.set_pus(pus)
+    s.set_picture(-1, f1)
+    s.set_picture(0, f0)
+    s.run(prm)
+    want = s.results()
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory()
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return t, v
+
+    keep = [pinned(f1), pinned(f0), pinned(np.zeros(len(pus), xg.RESULT_DTYPE))]
+    s2 = xg.MeSession(w, h, 1, len(pus))
+    s2.set_pus(pus)
+    s2.set_picture(-1, keep[0][1])
+    s2.set_picture(0, keep[1][1])
+    s2.run(prm)
+    got = s2.results(keep[2][1])
+    assert got.tobytes() == want.tobytes()
+    s.close()
+    s2.close()

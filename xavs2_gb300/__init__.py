@@ -248,8 +248,10 @@ class MeSession:
     def run(self, params):
         self._check(self.lib.xavs2gpu_me_run(self.h, ctypes.byref(params)), "run")
 
-    def results(self):
-        out = np.zeros(self.n, RESULT_DTYPE)
+    def results(self, out=None):
+        """The results (one per PU) into `out` (e.g. a page-locked array) or a new array."""
+        if out is None:
+            out = np.zeros(self.n, RESULT_DTYPE)
         self._check(self.lib.xavs2gpu_me_get_results(self.h, ptr(out)), "get_results")
         return out
 

@@ -943,12 +943,11 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     delete s;
 }
 
-// copies a W x H picture (device memory, `stride`) into plane `idx`, then
-// replicates its border; for references also computes the 15 sub-pel planes
-static int load_picture(MeSessionImpl &m, int slot, const uint8_t *dsrc, intptr_t stride)
+// replicates the border of the picture just copied into the slot's plane;
+// for references also computes the 15 sub-pel planes
+static int finish_picture(MeSessionImpl &m, int slot)
 {
     const int idx = slot < 0 ? 0 : 1 + 16 * m.slot_buf[slot];
-    XG_CUDA(cudaMemcpy2DAsync(m.plane(idx), m.stride, dsrc, stride, m.W, m.H, cudaMemcpyDeviceToDevice, m.st));
     if (xavs2gpu_expand_border(m.plane(idx), m.stride, m.W, m.H, kPad, m.st) != XAVS2GPU_OK) return XAVS2GPU_ERR_CUDA;
     if (slot >= 0) {
         uint8_t *planes[16];
@@ -956,6 +955,15 @@ static int load_picture(MeSessionImpl &m, int slot, const uint8_t *dsrc, intptr_
         return xavs2gpu_interpolate_frame(m.plane(idx), m.stride, m.W, m.H, kPad, planes, 2, m.st);
     }
     return XAVS2GPU_OK;
+}
+
+// copies a W x H picture (device memory, `stride`) into the slot's plane,
+// then finishes it as above
+static int load_picture(MeSessionImpl &m, int slot, const uint8_t *dsrc, intptr_t stride)
+{
+    const int idx = slot < 0 ? 0 : 1 + 16 * m.slot_buf[slot];
+    XG_CUDA(cudaMemcpy2DAsync(m.plane(idx), m.stride, dsrc, stride, m.W, m.H, cudaMemcpyDeviceToDevice, m.st));
+    return finish_picture(m, slot);
 }
 
 extern "C" int xavs2gpu_me_set_picture_device(xavs2gpu_me_session_t *s, int slot, const uint8_t *luma, intptr_t stride)
@@ -976,6 +984,14 @@ extern "C" int xavs2gpu_me_set_picture_host(xavs2gpu_me_session_t *s, int slot, 
     }
     MeSessionImpl &m = s->impl;
     XG_CUDA(cudaSetDevice(m.device));
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, luma) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
+        // page-locked: one asynchronous 2-D copy into the plane, no staging
+        const int idx = slot < 0 ? 0 : 1 + 16 * m.slot_buf[slot];
+        XG_CUDA(cudaMemcpy2DAsync(m.plane(idx), m.stride, luma, stride, m.W, m.H, cudaMemcpyHostToDevice, m.st));
+        return finish_picture(m, slot);
+    }
+    cudaGetLastError();   // pageable memory is reported as an error by some drivers
     // the staging buffer may still feed an earlier upload on the stream
     XG_CUDA(cudaStreamSynchronize(m.st));
     pack_rows(m.h_stage, luma, stride, m.W, m.H);
@@ -1243,9 +1259,10 @@ extern "C" int xavs2gpu_me_get_results(xavs2gpu_me_session_t *s, xavs2gpu_me_res
     MeSessionImpl &m = s->impl;
     XG_CUDA(cudaSetDevice(m.device));
     if (m.n) {
-        XG_CUDA(cudaMemcpyAsync(m.h_res, m.d_res, sizeof(xavs2gpu_me_result_t) * m.n, cudaMemcpyDeviceToHost, m.st));
+        // straight into the caller's buffer (one DMA when it is pinned; the
+        // driver stages pageable memory itself)
+        XG_CUDA(cudaMemcpyAsync(out, m.d_res, sizeof(xavs2gpu_me_result_t) * m.n, cudaMemcpyDeviceToHost, m.st));
         XG_CUDA(cudaStreamSynchronize(m.st));
-        memcpy(out, m.h_res, sizeof(xavs2gpu_me_result_t) * m.n);
     }
     return XAVS2GPU_OK;
 }
