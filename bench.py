@@ -577,6 +577,183 @@ def run_tq(args):
     print(json.dumps(line))
 
 
+# ---- intra rough mode decision over every CU level of a 1080p picture --------
+INTRA_METRIC = ("bit-exact intra RMD mode-samples/s (1080p, every CU level 64..4 + SDIP strips, 33 modes, "
+                "SATD + lambda*bits, rough candidate search)")
+# integer-op model of one mode-sample: 4-tap filter (4 multiply-adds + round /
+# shift), difference, 2-D 4-point Hadamard (4 add/sub), |x| accumulate
+INTRA_OPS_PER_SAMPLE = 11
+
+
+def intra_workload(rank, width, height):
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(61 + rank)
+    src = synth.base_picture(rng, width, height)
+    recon = np.clip(src.astype(np.int32) + rng.integers(-3, 4, src.shape), 0, 255).astype(np.uint8)
+    rects = synth.intra_level_blocks(width, height)
+    blocks, edges = synth.intra_pack(rects, recon, rng, xg.INTRA_BLOCK_DTYPE)
+    prm = xg.IntraParams(np.sqrt(2.0 ** ((QP - 11) / 4.0) * 0.68), 1, 1, synth.INTRA_DIST2, synth.INTRA_DIST1)
+    return src, blocks, edges, prm
+
+
+def cpu_sample_intra(blocks, edges, src, prm, fraction, seed, threads):
+    """The oracle's batched RMD over a random sample of the blocks; returns
+    (mode-samples done, seconds, sample indices, results)."""
+    import oracle
+    import xavs2_gb300 as xg
+    rng = np.random.default_rng(seed)
+    idx = np.nonzero(rng.random(len(blocks)) < fraction)[0]
+    sel = np.ascontiguousarray(blocks[idx])
+    out = np.zeros(len(sel), xg.INTRA_RESULT_DTYPE)
+    t0 = time.perf_counter()
+    oracle.lib().xo_intra_rmd_batch(oracle.ptr(sel), len(sel), oracle.ptr(edges), oracle.ptr(src), src.shape[1],
+                                    prm.lambda_, prm.use_hadamard, prm.rough, prm.dist2, prm.dist1,
+                                    oracle.ptr(out), threads)
+    dt = time.perf_counter() - t0
+    done = int((sel["width"].astype(np.int64) * sel["height"]).sum()) * 33
+    return done, dt, idx, out
+
+
+def run_intra(args):
+    import torch
+    import xavs2_gb300 as xg
+
+    rank, world, local = dist_env()
+    W, H = args.width, args.height
+    src, blocks, edges, prm = intra_workload(rank, W, H)
+    n = len(blocks)
+    mode_samples = int((blocks["width"].astype(np.int64) * blocks["height"]).sum()) * 33
+    cfg = {"workload": "intra_rmd_1080p_all_levels", "width": W, "height": H, "blocks": n,
+           "shapes": "64x64,32x32,16x16,8x8,4x4,32x8,8x32,16x4,4x16 tiling the picture", "qp": QP,
+           "rough": {"dist2": prm.dist2, "dist1": prm.dist1}, "cost": "SATD",
+           "content": "blurred-noise picture, edges from a +-3 noisy reconstruction",
+           "l2": "flushed between steps (512 MB write)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        frac = min(1.0, 8 * args.cpu_fraction)
+        cpu_sample_intra(blocks, edges, src, prm, frac / 4, 100, threads)
+        done, tt = 0, 0.0
+        for i in range(args.steps):
+            k, dt, *_ = cpu_sample_intra(blocks, edges, src, prm, frac, 200 + i, threads)
+            done += k
+            tt += dt
+        value = done / tt
+        print(json.dumps({"impl": "reference", "metric": INTRA_METRIC, "value": value, "unit": "mode-samples/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+                          "cpu_baseline": {"value": value, "unit": "mode-samples/s", "cores": threads,
+                                           "kind": "port", "sample": "per step a random %.2f%% of the %d blocks"
+                                                                     % (100 * frac, n)},
+                          "e2e": {"value": value, "unit": "mode-samples/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    dev = torch.device("cuda", local)
+    h_blocks = torch.from_numpy(blocks.view(np.uint8).copy()).pin_memory()
+    h_edges = torch.from_numpy(edges).pin_memory()
+    h_src = torch.from_numpy(np.ascontiguousarray(src).reshape(-1)).pin_memory()
+    out_bytes = n * xg.INTRA_RESULT_DTYPE.itemsize
+    h_out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+    d_blocks, d_edges, d_src = h_blocks.to(dev), h_edges.to(dev), h_src.to(dev)
+    d_out = torch.empty(out_bytes, dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(dev)
+    rmd = lib.xavs2gpu_intra_rmd_batch
+
+    def step(s):
+        rc = rmd(ctypes.c_void_p(d_blocks.data_ptr()), n, ctypes.c_void_p(d_edges.data_ptr()),
+                 ctypes.c_void_p(d_src.data_ptr()), W, ctypes.byref(prm), ctypes.c_void_p(d_out.data_ptr()),
+                 ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step(stream)
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    clk.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step(stream)
+            ends[i].record(stream)
+    barrier()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = reduce_max(float(sum(step_ms)), dev)
+    value = mode_samples * world * args.steps / (total_ms / 1e3)
+    kernel_ms = float(np.median(step_ms))
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": INTRA_METRIC, "value": value, "ms_per_step": kernel_ms, "blocks": n}))
+        return
+
+    # end to end with host buffers: descriptors, edges and source in, results out
+    barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            d_blocks.copy_(h_blocks, non_blocking=True)
+            d_edges.copy_(h_edges, non_blocking=True)
+            d_src.copy_(h_src, non_blocking=True)
+            step(stream)
+            h_out.copy_(d_out, non_blocking=True)
+        stream.synchronize()
+    barrier()
+    e2e_s = reduce_max(time.perf_counter() - t0, dev)
+    e2e = mode_samples * world * args.steps / e2e_s
+    if rank != 0:
+        return
+    got = h_out.numpy().view(xg.INTRA_RESULT_DTYPE)
+    done, cpu_s, idx, want = cpu_sample_intra(blocks, edges, src, prm, args.cpu_fraction, 7, os.cpu_count() or 1)
+    exact = bool(np.array_equal(got[idx]["cost"], want["cost"]) and
+                 np.array_equal(got[idx]["cand_mode"], want["cand_mode"]) and
+                 np.array_equal(got[idx]["num_for_rdo"], want["num_for_rdo"]))
+    peaks, peak_src = measured_peaks()
+    achieved = mode_samples / (kernel_ms / 1e3) / 1e12
+    peak = 152 * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / INTRA_OPS_PER_SAMPLE / 1e12
+    line = {
+        "metric": INTRA_METRIC, "value": value, "unit": "mode-samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+        "e2e": {"value": e2e, "unit": "mode-samples/s",
+                "h2d_bytes_per_step": int(h_blocks.numel() + h_edges.numel() + h_src.numel()),
+                "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "int", "kernel": "rmd_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "T mode-samples/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per mode-sample (%s)"
+                                    % (INTRA_OPS_PER_SAMPLE, peak_src),
+                     "work_per_launch": "%d blocks, %d mode-samples" % (n, mode_samples), "kernel_ms": kernel_ms},
+        "sample_bit_exact": exact,
+        "cpu_baseline": {"value": done / cpu_s, "unit": "mode-samples/s", "cores": os.cpu_count() or 1,
+                         "kind": "port", "sample": "random %.2f%% (%d) of the blocks, oracle C RMD, OpenMP"
+                                                   % (100 * args.cpu_fraction, len(idx))},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 # ---- serving: 64 concurrent streams, continuous batching --------------------
 SERVE_METRIC = "served p99 frame latency (64 streams 360p..2160p, 30 fps Poisson arrivals, continuous batching)"
 SERVE_RES = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
@@ -827,9 +1004,9 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
-    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve"], default="me",
+    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra"], default="me",
                     help="me: batched motion search (default); tq: batched transform+quant; chain: 4K full-picture "
-                         "chain; serve: 64-stream serving")
+                         "chain; serve: 64-stream serving; intra: rough intra mode decision")
     ap.add_argument("--chain-width", type=int, default=3840)
     ap.add_argument("--chain-height", type=int, default=2160)
     ap.add_argument("--tq-blocks", type=int, default=1000000)
@@ -844,6 +1021,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "tq":
         run_tq(args)
+    elif args.workload == "intra":
+        run_intra(args)
     elif args.workload == "chain":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "metric": CHAIN_METRIC,

@@ -262,6 +262,62 @@ XAVS2GPU_API int xavs2gpu_interpolate_frame(const uint8_t *src, int stride, int 
  * (plane_expand_border, frame.c:471-507, both bands). */
 XAVS2GPU_API int xavs2gpu_expand_border(uint8_t *pix, int stride, int width, int height, int pad, void *stream);
 
+/* ---- intra prediction (primitives.h:84, 186-188; intra.c) ----------------
+ * intra_pred_t: src = the top-left edge sample (src[1..] top / top-right,
+ * src[-1..] left / left-down), dst a bsx x bsy block with stride i_dst;
+ * dir_mode is the mode (3..32 for the angular entry) or, for DC, the
+ * availability (top << 8) | left (md_intra.c:170-185).  The predictors read
+ * src[-(bsy + 11*bsx/4 + 6) .. bsx + 11*bsy/4 + 6].  Like the reference,
+ * mode 31 on 16x64 writes columns 0-3 only. */
+typedef void (*xavs2gpu_intra_pred_t)(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+XAVS2GPU_API void xavs2gpu_intra_pred_dc(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+XAVS2GPU_API void xavs2gpu_intra_pred_plane(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+XAVS2GPU_API void xavs2gpu_intra_pred_bilinear(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+XAVS2GPU_API void xavs2gpu_intra_pred_ver(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+XAVS2GPU_API void xavs2gpu_intra_pred_hor(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+XAVS2GPU_API void xavs2gpu_intra_pred_ang(uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy);
+/* Fills intraf[0..32] (the layout of intrinsic_func_t.intraf). */
+XAVS2GPU_API void xavs2gpu_intra_pred_init(uint32_t cpuid, xavs2gpu_intra_pred_t intraf[33]);
+
+/* Batched rough mode decision (no single counterpart: the encoder's
+ * rdo_get_pred_intra_luma / _rmd per block, md_intra.c:216-380).  For every
+ * block: each mode's prediction, cost = lambda * (2 for an MPM, else 6) +
+ * SATD (use_hadamard) or SAD against the source block (rdcost_t, double,
+ * rounded as the reference's  lambda * bits + cost), and the 9-entry
+ * candidate list with the number of modes for RDO the encoder derives from
+ * them -- all 33 modes (rough = 0) or the rough three-phase search
+ * (rough = 1, dist2 / dist1 = num_intra_rmd_dist2 / _dist1).  Mode 31 on
+ * 16x64 is predicted in all 16 columns (the reference leaves 12 of them as
+ * they were in its buffer).  Device pointers; edges + edge_offset is the
+ * block's top-left edge sample and samples -(height + 11*width/4 + 6) ..
+ * width + 11*height/4 + 6 around it are read.
+ * A block whose size is not 4..64 or whose MPMs are not modes reports
+ * num_for_rdo = -1. */
+typedef struct xavs2gpu_intra_block {
+    int64_t edge_offset;
+    int64_t fenc_offset;     /* source block: fenc + fenc_offset, stride fenc_stride */
+    int16_t width, height;
+    int16_t dc_avail;        /* (top available << 8) | left available */
+    int8_t mpm[2];
+    int32_t num_for_rdo;     /* tab_num_intra_rdo entry of the block's level */
+    int32_t pad_;
+} xavs2gpu_intra_block_t;
+typedef struct xavs2gpu_intra_params {
+    double lambda;           /* h->f_lambda_mode */
+    int32_t use_hadamard;
+    int32_t rough;
+    int32_t dist2, dist1;
+} xavs2gpu_intra_params_t;
+typedef struct xavs2gpu_intra_result {
+    double cost[33];
+    double cand_cost[9];
+    int32_t cand_mode[9];
+    int32_t num_for_rdo;
+} xavs2gpu_intra_result_t;
+XAVS2GPU_API int xavs2gpu_intra_rmd_batch(const xavs2gpu_intra_block_t *blocks, int n, const uint8_t *edges,
+                                          const uint8_t *fenc, int fenc_stride, const xavs2gpu_intra_params_t *prm,
+                                          xavs2gpu_intra_result_t *out, void *stream);
+
 /* ---- batched transform + quant chain -----------------------------------
  * For every block: dct (or, for a 4x4 block with flag bit 1, the 4x4
  * secondary transform) -> quant -> when any level is non-zero, dequant ->

@@ -106,6 +106,10 @@ _ORACLE_SIGS = {
     "xo_me_search": (_I, [_P, _P, _P, _S, _P, _S, _P]),
     "xo_me_search_list": (None, [_P, _P, _I, _P, _S, _P, _S, _P, _I]),
     "xo_pu_set_limits": (None, [_P, _I, _I, _I, _I]),
+    "xo_intra_pred": (None, [_I, _P, _P, _I, _I, _I, _I]),
+    "xo_intra_mode_costs": (None, [_P, _P, _I, _I, _I, _I, _P, ctypes.c_double, _I, _P]),
+    "xo_intra_candidates": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
+    "xo_intra_rmd_batch": (None, [_P, _I, _P, _P, _I, ctypes.c_double, _I, _I, _I, _I, _P, _I]),
 }
 _REF_SIGS = {
     "xr_cmp": (_I, [_I, _I, _P, _S, _P, _S]),
@@ -128,6 +132,8 @@ _REF_SIGS = {
     "xr_dequant": (None, [_P, _I, _I, _I]), "xr_abs_coeff": (None, [_P, _P, _I]),
     "xr_add_sign": (_I, [_P, _P, _I]),
     "xr_me_search": (_I, [_P, _P, _P, _S, _P, _I, _P]),
+    "xr_intra_pred": (None, [_I, _P, _P, _I, _I, _I, _I]),
+    "xr_intra_fill_edge": (None, [_I, _P, _I, _P, _P, ctypes.c_uint32, _I, _I]),
 }
 
 

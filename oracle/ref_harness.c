@@ -42,6 +42,7 @@ void xr_init(void)
     xavs2_dct_init(0, &g_funcs.dctf);
     xavs2_quant_init(0, &g_funcs.dctf);
     xavs2_mad_init(0, g_funcs.pixf.madf);
+    xavs2_intra_pred_init(0, &g_funcs);
     g_inited = 1;
 }
 
@@ -357,4 +358,24 @@ int xr_mvbits(int d)
         xavs2_me_init(h, &mb);
     }
     return h->mvbits[d];
+}
+
+/* ---- intra prediction (intra.c) ---------------------------------------- */
+/* One table entry: `ep` is the top-left edge sample (intra.c's src), the
+ * block is written to dst with stride i_dst; dir_mode as the encoder passes
+ * it (the availability word for DC, md_intra.c:170-185). */
+void xr_intra_pred(int mode, pel_t *ep, pel_t *dst, int i_dst, int dir_mode, int bsx, int bsy)
+{
+    xr_init();
+    g_funcs.intraf[mode](ep, dst, i_dst, dir_mode, bsx, bsy);
+}
+
+/* fill_edge_f[xy] (intra.c:1580-1840): builds the edge samples of a block
+ * whose top-left neighbour is pTL (stride i_TL), with the top border line
+ * pLcuEP for blocks on the CTU's top edge. */
+void xr_intra_fill_edge(int xy, const pel_t *pTL, int i_TL, const pel_t *pLcuEP, pel_t *EP, uint32_t avail, int bsx,
+                        int bsy)
+{
+    xr_init();
+    g_funcs.fill_edge_f[xy](pTL, i_TL, pLcuEP, EP, avail, bsx, bsy);
 }

@@ -1102,3 +1102,307 @@ void xo_me_search_list(const xo_me_params_t *prm, const xo_pu_t *pus, int n_pus,
                      &out[i]);
     }
 }
+
+/* ==========================================================================
+ * Intra prediction (common/intra.c) and the rough mode decision
+ * (encoder/md_intra.c).  `ep` points at the top-left edge sample: ep[1..]
+ * is the top row continuing into the top-right, ep[-1..] the left column
+ * continuing downwards (intra.c:1590-1594).
+ * ======================================================================== */
+
+/* Angle steps of the angular modes as (multiplier, shift) pairs, for the
+ * step along x per row (index 0) and along y per column (index 1)
+ * (intra.c:98-120, normative AVS2 geometry). */
+static const int8_t k_ang_ms[2][33][2] = {
+    {{0, 0}, {0, 0}, {0, 0},
+     {11, 2}, {2, 0}, {11, 3}, {1, 0}, {93, 7}, {1, 1}, {93, 8}, {1, 2}, {1, 3},
+     {0, 0},
+     {1, 3}, {1, 2}, {93, 8}, {1, 1}, {93, 7}, {1, 0}, {11, 3}, {2, 0}, {11, 2}, {4, 0}, {8, 0},
+     {0, 0},
+     {8, 0}, {4, 0}, {11, 2}, {2, 0}, {11, 3}, {1, 0}, {93, 7}, {1, 1}},
+    {{0, 0}, {0, 0}, {0, 0},
+     {93, 8}, {1, 1}, {93, 7}, {1, 0}, {11, 3}, {2, 0}, {11, 2}, {4, 0}, {8, 0},
+     {0, 0},
+     {8, 0}, {4, 0}, {11, 2}, {2, 0}, {11, 3}, {1, 0}, {93, 7}, {1, 1}, {93, 8}, {1, 2}, {1, 3},
+     {0, 0},
+     {1, 3}, {1, 2}, {93, 8}, {1, 1}, {93, 7}, {1, 0}, {11, 3}, {2, 0}}};
+
+/* integer step and 1/32 fraction of displacement d (intra.c:295-306) */
+static int ang_step(int mode, int axis, int d, int *frac)
+{
+    const int t = d * k_ang_ms[axis][mode][0], sh = k_ang_ms[axis][mode][1];
+    const int n = t >> sh;
+    *frac = ((t << 5) >> sh) - (n << 5);
+    return n;
+}
+
+static int ilog2_pos(int v) { int r = 0; while (v > 1) { v >>= 1; r++; } return r; }
+
+/* The reference's table entry for mode 5 on the narrow 4x16 and 8x32 shapes
+ * (intra_pred_ang_x_5_c, intra.c:455-605): the first 4 (8) rows follow the
+ * angular formula, the rest of the block is one edge sample (ep[8], ep[16])
+ * except a few samples just below those rows. */
+static void mode5_narrow(const uint8_t *ep, uint8_t *dst, int i_dst, int bsx, int bsy)
+{
+    int x, y;
+    const int rows = bsx == 4 ? 4 : 8;
+    for (y = 0; y < rows; y++) {
+        int f, ix = ang_step(5, 0, y + 1, &f);
+        for (x = 0; x < bsx; x++, ix++)
+            dst[y * i_dst + x] = (uint8_t)((ep[ix] * (32 - f) + ep[ix + 1] * (64 - f) + ep[ix + 2] * (32 + f) +
+                                            ep[ix + 3] * f + 64) >> 7);
+    }
+    const uint8_t pad = ep[2 * rows];
+    for (y = rows; y < bsy; y++)
+        for (x = 0; x < bsx; x++) dst[y * i_dst + x] = pad;
+    if (bsx == 4) {
+        const uint8_t *s = ep + 8;
+        dst[4 * i_dst + 0] = (uint8_t)((s[-2] + 9 * s[-1] + 15 * s[0] + 7 * s[1] + 16) >> 5);
+        dst[4 * i_dst + 1] = (uint8_t)((s[-1] + 9 * s[0] + 15 * s[1] + 7 * s[2] + 16) >> 5);
+    } else {
+        const uint8_t *s = ep + 12;
+        for (x = 0; x < 4; x++)
+            dst[8 * i_dst + x] = (uint8_t)((5 * s[x] + 13 * s[x + 1] + 11 * s[x + 2] + 3 * s[x + 3] + 16) >> 5);
+        for (x = 0; x < 3; x++)
+            dst[9 * i_dst + x] = (uint8_t)((s[x + 1] + 5 * s[x + 2] + 7 * s[x + 3] + 3 * s[x + 4] + 8) >> 4);
+        dst[10 * i_dst] = (uint8_t)((7 * s[3] + 15 * s[4] + 9 * s[5] + s[6] + 16) >> 5);
+    }
+}
+
+static void pred_ang_left(int mode, const uint8_t *ep, uint8_t *dst, int i_dst, int bsx, int bsy)
+{
+    int x, y;
+    for (x = 0; x < bsx; x++) {
+        int f, s = ang_step(mode, 1, x + 1, &f);
+        for (y = 0; y < bsy; y++) {
+            const int iy = y + s;
+            dst[y * i_dst + x] = (uint8_t)((ep[-iy] * (32 - f) + ep[-iy - 1] * (64 - f) + ep[-iy - 2] * (32 + f) +
+                                            ep[-iy - 3] * f + 64) >> 7);
+        }
+    }
+}
+
+void xo_intra_pred(int mode, const uint8_t *ep, uint8_t *dst, int i_dst, int dc_avail, int bsx, int bsy)
+{
+    int x, y;
+    if (mode == 5 && ((bsx == 4 && bsy == 16) || (bsx == 8 && bsy == 32))) {
+        mode5_narrow(ep, dst, i_dst, bsx, bsy);
+        return;
+    }
+    if (mode == 31 && ((bsx == 16 && bsy == 4) || (bsx == 32 && bsy == 8))) {
+        /* intra_pred_ang_y_31_c (intra.c:1147-1161): mode 5 on the
+         * transposed edge and block */
+        uint8_t et[2 * 64 + 8], tb[64 * 64];
+        const int n = bsy + bsx * 11 / 8 + 3;
+        for (x = 0; x < n; x++) et[x] = ep[-x];
+        mode5_narrow(et, tb, bsy, bsy, bsx);
+        for (y = 0; y < bsy; y++)
+            for (x = 0; x < bsx; x++) dst[y * i_dst + x] = tb[x * bsy + y];
+        return;
+    }
+    if (mode == 31 && bsx == 16 && bsy == 64) {
+        /* the reference writes columns 0-3 only (intra.c:1176-1183) and
+         * leaves the rest of the block as it was */
+        for (x = 0; x < 4; x++) {
+            int f, sy = ang_step(31, 1, x + 1, &f);
+            for (y = 0; y < bsy; y++) {
+                const int iy = y + sy;
+                dst[y * i_dst + x] = (uint8_t)((ep[-iy] * (32 - f) + ep[-iy - 1] * (64 - f) +
+                                                ep[-iy - 2] * (32 + f) + ep[-iy - 3] * f + 64) >> 7);
+            }
+        }
+        return;
+    }
+    if (mode == 0) {                                           /* DC, intra.c:153-190 */
+        const int top = dc_avail >> 8, left = dc_avail & 0xFF;
+        int sl = 0, sa = 0, v;
+        for (y = 0; y < bsy; y++) sl += ep[-1 - y];
+        for (x = 0; x < bsx; x++) sa += ep[1 + x];
+        if (top && left) v = ((sl + sa + ((bsx + bsy) >> 1)) * (512 / (bsx + bsy))) >> 9;
+        else if (left) v = (sl + (bsy >> 1)) >> ilog2_pos(bsy);
+        else if (top) v = (sa + (bsx >> 1)) >> ilog2_pos(bsx);
+        else v = 128;
+        for (y = 0; y < bsy; y++)
+            for (x = 0; x < bsx; x++) dst[y * i_dst + x] = (uint8_t)v;
+    } else if (mode == 1) {                                    /* plane, intra.c:192-236 */
+        static const int mult[7] = {0, 0, 13, 17, 5, 11, 23}, shf[7] = {0, 0, 7, 10, 11, 15, 19};
+        const int lx = ilog2_pos(bsx), ly = ilog2_pos(bsy), w2 = bsx >> 1, h2 = bsy >> 1;
+        int H = 0, V = 0, a, b, c;
+        for (x = 1; x <= w2; x++) H += x * (ep[w2 + x] - ep[w2 - x]);
+        for (y = 1; y <= h2; y++) V += y * (ep[-h2 - y] - ep[-h2 + y]);
+        a = (ep[-bsy] + ep[bsx]) << 4;
+        b = ((H << 5) * mult[lx] + (1 << (shf[lx] - 1))) >> shf[lx];
+        c = ((V << 5) * mult[ly] + (1 << (shf[ly] - 1))) >> shf[ly];
+        a += 16 - b * (w2 - 1) - c * (h2 - 1);
+        for (y = 0; y < bsy; y++)
+            for (x = 0; x < bsx; x++) {
+                const int v = (a + b * x + c * y) >> 5;
+                dst[y * i_dst + x] = (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+            }
+    } else if (mode == 2) {                                    /* bilinear, intra.c:238-293 */
+        const int lx = ilog2_pos(bsx), ly = ilog2_pos(bsy), sh = lx < ly ? lx : ly, shxy = lx + ly + 1;
+        const int a = ep[bsx], b = ep[-bsy];
+        const int c = bsx == bsy ? (a + b + 1) >> 1 : (((a << lx) + (b << ly)) * 13 + (1 << (sh + 5))) >> (sh + 6);
+        const int t = 2 * c - a - b;
+        for (y = 0; y < bsy; y++)
+            for (x = 0; x < bsx; x++) {
+                /* the reference accumulates these terms row by row and
+                 * column by column; the closed forms are equal */
+                const int top = ep[1 + x], left = ep[-1 - y];
+                const int predx = (left << lx) + (x + 1) * (a - left);
+                const int predy = (top << ly) + (y + 1) * (b - top);
+                const int wxy = x * y * t;
+                int v = ((predx << ly) + (predy << lx) + wxy + (1 << (lx + ly))) >> shxy;
+                dst[y * i_dst + x] = (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+            }
+    } else if (mode == 12) {                                   /* vertical */
+        for (y = 0; y < bsy; y++)
+            for (x = 0; x < bsx; x++) dst[y * i_dst + x] = ep[1 + x];
+    } else if (mode == 24) {                                   /* horizontal */
+        for (y = 0; y < bsy; y++)
+            for (x = 0; x < bsx; x++) dst[y * i_dst + x] = ep[-1 - y];
+    } else if (mode < 12) {                                    /* angular, from the top row (intra.c:310-331) */
+        for (y = 0; y < bsy; y++) {
+            int f, ix = ang_step(mode, 0, y + 1, &f);
+            for (x = 0; x < bsx; x++, ix++)
+                dst[y * i_dst + x] = (uint8_t)((ep[ix] * (32 - f) + ep[ix + 1] * (64 - f) + ep[ix + 2] * (32 + f) +
+                                                ep[ix + 3] * f + 64) >> 7);
+        }
+    } else if (mode > 24) {                                    /* angular, from the left column (intra.c:336-358) */
+        pred_ang_left(mode, ep, dst, i_dst, bsx, bsy);
+    } else {                                                   /* angular, both edges (intra.c:363-397) */
+        for (y = 0; y < bsy; y++) {
+            int fx, ixx = -ang_step(mode, 0, y + 1, &fx);
+            for (x = 0; x < bsx; x++, ixx++) {
+                int fy, sy = ang_step(mode, 1, x + 1, &fy);
+                const int iyy = y - sy;
+                int v;
+                if (iyy <= -1)
+                    v = ep[ixx + 2] * (32 - fx) + ep[ixx + 1] * (64 - fx) + ep[ixx] * (32 + fx) + ep[ixx - 1] * fx;
+                else
+                    v = ep[-iyy - 2] * (32 - fy) + ep[-iyy - 1] * (64 - fy) + ep[-iyy] * (32 + fy) + ep[-iyy + 1] * fy;
+                dst[y * i_dst + x] = (uint8_t)((v + 64) >> 7);
+            }
+        }
+    }
+}
+
+/* Cost of every mode for a block (md_intra.c:216-226): lambda * mode bits
+ * (2 for the two most probable modes, else 6) + SATD (or SAD) of the
+ * prediction against the source block, as rdcost_t (double). */
+void xo_intra_mode_costs(const uint8_t *ep, const uint8_t *fenc, int i_fenc, int bsx, int bsy, int dc_avail,
+                         const int mpm[2], double lambda, int hadamard, double cost[33])
+{
+    uint8_t pred[64 * 64];
+    int m, part = -1;
+    for (m = 0; m < 25; m++)
+        if (k_pu_w[m] == bsx && k_pu_h[m] == bsy) part = m;
+    for (m = 0; m < 33; m++) {
+        const int bits = (mpm[0] == m || mpm[1] == m) ? 2 : 6;
+        int32_t d;
+        if (m == 31 && bsx == 16 && bsy == 64)
+            pred_ang_left(m, ep, pred, bsx, bsx, bsy);   /* every column predicted (the table entry writes 4) */
+        else
+            xo_intra_pred(m, ep, pred, bsx, m == 0 ? dc_avail : m, bsx, bsy);
+        d = hadamard ? xo_satd(part, fenc, i_fenc, pred, bsx) : xo_sad(part, fenc, i_fenc, pred, bsx);
+        cost[m] = lambda * bits + (double)d;
+    }
+}
+
+/* update_candidate_list (md_intra.c:195-210): insertion into a list kept
+ * sorted by cost, a new entry going after equal costs */
+static void cand_insert(int mode, double cost, int n, int *modes, double *costs)
+{
+    int i = n - 1;
+    if (!(cost < costs[i])) return;
+    while (i > 0 && cost < costs[i - 1]) {
+        modes[i] = modes[i - 1];
+        costs[i] = costs[i - 1];
+        i--;
+    }
+    modes[i] = mode;
+    costs[i] = cost;
+}
+
+int xo_intra_candidates(const double cost[33], int rough, int dist2, int dist1, int num_for_rdo, const int mpm[2],
+                        int *modes, double *costs)
+{
+    const int N = 9;   /* INTRA_MODE_NUM_FOR_RDO (defines.h:290) */
+    int visited[33] = {0}, i, j, m, num_angle;
+    for (i = 0; i < N; i++) {
+        modes[i] = 0;
+        costs[i] = (double)(1LL << 50);   /* MAX_COST (defines.h:299) */
+    }
+#define XO_VISIT(k) do { cand_insert((k), cost[(k)], N, modes, costs); visited[(k)] = 1; } while (0)
+    if (!rough) {                                              /* md_intra.c:231-256 */
+        for (m = 0; m < 33; m++) XO_VISIT(m);
+        return num_for_rdo;
+    }
+    /* md_intra.c:258-380 */
+    for (m = 0; m < 3; m++) XO_VISIT(m);
+    for (m = 4; m < 33; m += 4) XO_VISIT(m);
+    for (i = 0; i < dist2; i++) {
+        m = modes[i];
+        if (m <= 2) continue;
+        if (m > 3 && !visited[m - 2]) XO_VISIT(m - 2);
+        if (m < 31 && !visited[m + 2]) XO_VISIT(m + 2);
+    }
+    for (i = 0, num_angle = 0; num_angle < dist1 && i < N; i++) {
+        m = modes[i];
+        if (m <= 2) continue;
+        if (m > 3 && !visited[m - 1]) { XO_VISIT(m - 1); num_angle++; }
+        if (m < 32 && !visited[m + 1]) { XO_VISIT(m + 1); num_angle++; }
+    }
+    if (!visited[mpm[0]]) XO_VISIT(mpm[0]);
+    if (!visited[mpm[1]]) XO_VISIT(mpm[1]);
+#undef XO_VISIT
+    if (modes[0] == mpm[0] || modes[0] == mpm[1] || modes[1] == mpm[0] || modes[1] == mpm[1])
+        return num_for_rdo < 3 ? num_for_rdo : 3;
+    visited[modes[0]] = 2;
+    visited[modes[1]] = 2;
+    for (i = 2, j = 2; i < N && j < num_for_rdo; i++) {
+        m = modes[i];
+        if (!visited[m]) continue;
+        if (m <= 2) {
+            modes[j++] = m;
+            visited[m] = 2;
+        } else if (m == 3) {
+            if (visited[4] == 1) { modes[j++] = 3; visited[3] = 2; }
+        } else if (m == 32) {
+            if (visited[31] == 1) { modes[j++] = 32; visited[32] = 2; }
+        } else if (visited[m - 1] == 1 && visited[m + 1] == 1) {
+            modes[j++] = m;
+            visited[m] = 2;
+        }
+        if (visited[0] == 2 && visited[1] == 2 && visited[2] == 2) break;
+    }
+    return num_for_rdo < j ? num_for_rdo : j;
+}
+
+static void rmd_one(const xo_intra_block_t *b, const uint8_t *edges, const uint8_t *fenc, int fenc_stride,
+                    double lambda, int hadamard, int rough, int dist2, int dist1, xo_intra_result_t *r)
+{
+    const int mpm[2] = {b->mpm[0], b->mpm[1]};
+    xo_intra_mode_costs(edges + b->edge_offset, fenc + b->fenc_offset, fenc_stride, b->width, b->height,
+                        b->dc_avail, mpm, lambda, hadamard, r->cost);
+    r->num_for_rdo = xo_intra_candidates(r->cost, rough, dist2, dist1, b->num_for_rdo, mpm, r->cand_mode,
+                                         r->cand_cost);
+}
+
+void xo_intra_rmd_batch(const xo_intra_block_t *blocks, int n, const uint8_t *edges, const uint8_t *fenc,
+                        int fenc_stride, double lambda, int hadamard, int rough, int dist2, int dist1,
+                        xo_intra_result_t *out, int threads)
+{
+    int i;
+#ifdef _OPENMP
+    if (threads > 1) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+        for (i = 0; i < n; i++)
+            rmd_one(&blocks[i], edges, fenc, fenc_stride, lambda, hadamard, rough, dist2, dist1, &out[i]);
+        return;
+    }
+#endif
+    (void)threads;
+    for (i = 0; i < n; i++)
+        rmd_one(&blocks[i], edges, fenc, fenc_stride, lambda, hadamard, rough, dist2, dist1, &out[i]);
+}

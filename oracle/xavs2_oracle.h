@@ -166,4 +166,39 @@ void xo_pu_set_limits(xo_pu_t *pu, int width, int height, int vmin_qpel, int vma
 }
 #endif
 
+
+/* ---- intra prediction (intra.c) and rough mode decision (md_intra.c) ---- */
+/* Prediction of a bsx x bsy block in mode 0..32 from the edge samples
+ * around ep (ep[0] top-left, ep[1..] top / top-right, ep[-1..] left /
+ * left-down); dc_avail = (top available << 8) | left available. */
+void xo_intra_pred(int mode, const uint8_t *ep, uint8_t *dst, int i_dst, int dc_avail, int bsx, int bsy);
+/* lambda * mode bits + SATD (hadamard) or SAD of every mode's prediction. */
+void xo_intra_mode_costs(const uint8_t *ep, const uint8_t *fenc, int i_fenc, int bsx, int bsy, int dc_avail,
+                         const int mpm[2], double lambda, int hadamard, double cost[33]);
+/* The candidate list (9 entries) and the number of modes for RDO the
+ * encoder derives from those costs: all modes (rough = 0,
+ * rdo_get_pred_intra_luma) or the rough three-phase search (rough = 1,
+ * rdo_get_pred_intra_luma_rmd) with dist2 / dist1 neighbours. */
+int xo_intra_candidates(const double cost[33], int rough, int dist2, int dist1, int num_for_rdo, const int mpm[2],
+                        int *modes, double *costs);
+
+/* Batched form of the two above with the GPU entry's block / result
+ * layouts (xavs2gpu_intra_block_t / _result_t): edges + edge_offset is a
+ * block's top-left edge sample, the source block is fenc + fenc_offset. */
+typedef struct xo_intra_block {
+    int64_t edge_offset, fenc_offset;
+    int16_t width, height, dc_avail;
+    int8_t mpm[2];
+    int32_t num_for_rdo, pad_;
+} xo_intra_block_t;
+typedef struct xo_intra_result {
+    double cost[33];
+    double cand_cost[9];
+    int32_t cand_mode[9];
+    int32_t num_for_rdo;
+} xo_intra_result_t;
+void xo_intra_rmd_batch(const xo_intra_block_t *blocks, int n, const uint8_t *edges, const uint8_t *fenc,
+                        int fenc_stride, double lambda, int hadamard, int rough, int dist2, int dist1,
+                        xo_intra_result_t *out, int threads);
+
 #endif

@@ -23,6 +23,29 @@ from oracle import PU_W, PU_H, TU_PARTS, ptr  # noqa: E402
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
 
 
+# intra block shapes (square CUs, SDIP / NSQT partitions) and the DC
+# availability words (top << 8 | left); entries 33..35 of a digest row are DC
+# with the first three availabilities, entry 0 with both neighbours
+INTRA_SHAPES = [(4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (4, 16), (16, 4), (8, 32), (32, 8), (16, 64), (64, 16)]
+INTRA_DC_AVAIL = [0x000, 0x001, 0x100, 0x101]
+
+
+def intra_edges(rng):
+    """512-sample edge arrays (top-left sample at 256): random, a smooth ramp
+    with noise, and alternating 0 / 255 runs."""
+    a = rng.integers(0, 256, 512).astype(np.uint8)
+    t = np.arange(512)
+    b = np.clip(128 + 100 * np.sin(t / 37.0) + rng.integers(-6, 7, 512), 0, 255).astype(np.uint8)
+    c = np.where((t // 3) % 2 == 0, 255, 0).astype(np.uint8)
+    return [a, b, c]
+
+
+def intra_prefill(bw, bh):
+    """Destination with stride bw + 8, pre-filled so that samples a mode
+    leaves alone are visible."""
+    return ((np.arange(bh * (bw + 8)) * 7 + 3) % 251).astype(np.uint8).reshape(bh, bw + 8)
+
+
 def main():
     r = oracle.ref_lib()
     if r is None:
@@ -128,6 +151,18 @@ def main():
     g["me_params"] = np.array([16, oracle.lambda_factor(32), 1, 2, 0, 0], np.int32)
     g["me_pus"] = np.frombuffer(b"".join(pus), oracle.PU_DTYPE)
     g["me_out"] = np.frombuffer(b"".join(outs), oracle.RESULT_DTYPE)
+
+    # --- intra prediction: every mode and shape on three edge sets (digests)
+    edges = intra_edges(rng)
+    dig = np.zeros((len(edges), len(INTRA_SHAPES), 33 + 3), "<U64")
+    for e, edge in enumerate(edges):
+        for s_, (bw, bh) in enumerate(INTRA_SHAPES):
+            for m in range(36):
+                mode, dir_mode = (0, INTRA_DC_AVAIL[m - 33]) if m >= 33 else (m, INTRA_DC_AVAIL[3] if m == 0 else m)
+                dst = intra_prefill(bw, bh)
+                r.xr_intra_pred(mode, ptr(edge, 256), ptr(dst), bw + 8, dir_mode, bw, bh)
+                dig[e, s_, m] = hashlib.sha256(dst.tobytes()).hexdigest()
+    g["intra_edges"], g["intra_sha"] = np.stack(edges), dig
 
     np.savez_compressed(OUT, **g)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

@@ -93,3 +93,27 @@ def test_motion_search(olib, g):
     out = np.zeros(len(pus), oracle.RESULT_DTYPE)
     olib.xo_me_search_list(ctypes.byref(prm), ptr(pus), len(pus), ptr(cur), w, frefs, stride, ptr(out), 1)
     assert np.array_equal(out, g["me_out"])
+
+
+def _intra_golden():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_intra_prediction(olib, g):
+    """Every intra mode on every block shape, three edge sets, DC with all
+    four availabilities, destination pre-filled (the reference's mode 31 on
+    16x64 leaves columns 4..15 alone)."""
+    mg = _intra_golden()
+    for e, edge in enumerate(g["intra_edges"]):
+        edge = np.ascontiguousarray(edge)
+        for s, (bw, bh) in enumerate(mg.INTRA_SHAPES):
+            for m in range(36):
+                mode, avail = (0, mg.INTRA_DC_AVAIL[m - 33]) if m >= 33 else (m, mg.INTRA_DC_AVAIL[3])
+                dst = mg.intra_prefill(bw, bh)
+                olib.xo_intra_pred(mode, ptr(edge, 256), ptr(dst), bw + 8, avail, bw, bh)
+                assert hashlib.sha256(dst.tobytes()).hexdigest() == g["intra_sha"][e, s, m], (e, bw, bh, m)

@@ -315,3 +315,50 @@ def test_me_search(olib, rlib, hadamard, frac, fast, pmvr):
             assert cr == co and got == exp, (part, x, y, exp, got)
             n += 1
     assert n == 75
+
+
+INTRA_SHAPES = [(4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (4, 16), (16, 4), (8, 32), (32, 8), (16, 64), (64, 16)]
+
+
+def test_intra_prediction(olib, rlib):
+    """xo_intra_pred against the reference's intraf[] table on seeded edges,
+    with edge buffers built by the reference's own fill_edge_f for random
+    neighbour availabilities as well as plain random edges."""
+    rng = np.random.default_rng(77)
+    edges = []
+    for i in range(6):
+        edges.append(rng.integers(0, 256, 512).astype(np.uint8))
+    for i in range(6):
+        t = np.arange(512)
+        edges.append(np.clip(120 + 90 * np.sin(t / (5.0 + 7 * i)) + rng.integers(-9, 10, 512), 0, 255).astype(np.uint8))
+    for edge in edges:
+        for bw, bh in INTRA_SHAPES:
+            for mode in range(33):
+                for avail in ((0x000, 0x001, 0x100, 0x101) if mode == 0 else (mode,)):
+                    fill = rng.integers(0, 256, (bh, bw + 5), dtype=np.uint8)
+                    a, b = fill.copy(), fill.copy()
+                    olib.xo_intra_pred(mode, ptr(edge, 256), ptr(a), bw + 5, avail, bw, bh)
+                    rlib.xr_intra_pred(mode, ptr(edge, 256), ptr(b), bw + 5, avail, bw, bh)
+                    assert np.array_equal(a, b), (bw, bh, mode, avail)
+
+
+def test_intra_fill_edge_prediction(olib, rlib):
+    """Edges as the encoder builds them (fill_edge_f, every availability
+    combination of left / top / top-right / left-down / top-left), then
+    every mode through both."""
+    rng = np.random.default_rng(78)
+    pic = rng.integers(0, 256, (320, 320), dtype=np.uint8)
+    pic = np.ascontiguousarray((pic.astype(np.int32) + np.roll(pic, 1, 0) + np.roll(pic, 1, 1)) // 3).astype(np.uint8)
+    lcu_ep = rng.integers(0, 256, 512).astype(np.uint8)
+    for bw, bh in [(8, 8), (16, 16), (32, 8), (4, 16), (64, 64)]:
+        for avail in range(32):
+            for xy in range(4):
+                ebuf = np.zeros(1024, np.uint8)
+                rlib.xr_intra_fill_edge(xy, ptr(pic, 40 * 320 + 40), 320, ptr(lcu_ep, 200), ptr(ebuf, 512),
+                                        avail, bw, bh)
+                for mode in range(33):
+                    a = np.zeros((bh, bw), np.uint8)
+                    b = np.zeros((bh, bw), np.uint8)
+                    olib.xo_intra_pred(mode, ptr(ebuf, 512), ptr(a), bw, 0x101, bw, bh)
+                    rlib.xr_intra_pred(mode, ptr(ebuf, 512), ptr(b), bw, 0x101 if mode == 0 else mode, bw, bh)
+                    assert np.array_equal(a, b), (bw, bh, avail, xy, mode)

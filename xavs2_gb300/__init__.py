@@ -139,6 +139,14 @@ _SIGS = {
     "xavs2gpu_server_poll": (_I, [_P, _P, _I, _I]),
     "xavs2gpu_server_stats": (None, [_P, _P, _P, _P, _P]),
     "xavs2gpu_server_timing": (None, [_P, _P, _P]),
+    "xavs2gpu_intra_pred_dc": (None, [_P, _P, _I, _I, _I, _I]),
+    "xavs2gpu_intra_pred_plane": (None, [_P, _P, _I, _I, _I, _I]),
+    "xavs2gpu_intra_pred_bilinear": (None, [_P, _P, _I, _I, _I, _I]),
+    "xavs2gpu_intra_pred_ver": (None, [_P, _P, _I, _I, _I, _I]),
+    "xavs2gpu_intra_pred_hor": (None, [_P, _P, _I, _I, _I, _I]),
+    "xavs2gpu_intra_pred_ang": (None, [_P, _P, _I, _I, _I, _I]),
+    "xavs2gpu_intra_pred_init": (None, [ctypes.c_uint32, _P]),
+    "xavs2gpu_intra_rmd_batch": (_I, [_P, _I, _P, _P, _I, _P, _P, _P]),
 }
 
 _PIXEL_CMP = ["sad", "satd", "sa8d", "ssd"]
@@ -410,6 +418,17 @@ class ChainTuning(ctypes.Structure):
 class ChainOutputs(ctypes.Structure):
     _fields_ = [("coef", _P), ("recon_residual", _P), ("nnz", _P), ("blocks", _P), ("recon", _P),
                 ("choice", _P), ("n_residual", ctypes.c_int64), ("n_coef", ctypes.c_int64)]
+
+
+INTRA_BLOCK_DTYPE = np.dtype([("edge_offset", "<i8"), ("fenc_offset", "<i8"), ("width", "<i2"), ("height", "<i2"),
+                              ("dc_avail", "<i2"), ("mpm", "i1", (2,)), ("num_for_rdo", "<i4"), ("pad_", "<i4")])
+INTRA_RESULT_DTYPE = np.dtype([("cost", "<f8", (33,)), ("cand_cost", "<f8", (9,)), ("cand_mode", "<i4", (9,)),
+                               ("num_for_rdo", "<i4")])
+
+
+class IntraParams(ctypes.Structure):
+    _fields_ = [("lambda_", ctypes.c_double), ("use_hadamard", ctypes.c_int32), ("rough", ctypes.c_int32),
+                ("dist2", ctypes.c_int32), ("dist1", ctypes.c_int32)]
 
 
 CHOICE_DTYPE = np.dtype([("ref", "<i4"), ("mv_x", "<i2"), ("mv_y", "<i2")])

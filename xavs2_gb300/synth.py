@@ -126,3 +126,117 @@ def chain_pictures(n, width, height, seed=21, pan_px=12, n_motions=2, max_px=4):
         panned = shift_qpel(frames[-1], 4 * pan_px, 0)
         frames.append(next_picture(rng, panned, n_motions, max_px))
     return frames
+
+
+# ---- intra blocks --------------------------------------------------------------
+INTRA_ENC_SHAPES = [(4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (4, 16), (16, 4), (8, 32), (32, 8)]
+INTRA_ALL_SHAPES = INTRA_ENC_SHAPES + [(16, 64), (64, 16)]
+# modes for RDO per block level (a preset-5 row of the encoder's table:
+# 4x4 .. 64x64) and the rough search's neighbour counts of that preset
+INTRA_RDO_NUM = {2: 6, 3: 6, 4: 6, 5: 4, 6: 3}
+INTRA_DIST2, INTRA_DIST1 = 4, 2
+
+
+def _intra_partition(rng, x0, y0, size, out, all_shapes):
+    """Quad-tree split of a CTU into CUs (64 .. 8), each predicted as one
+    block, as four SDIP strips (32 / 16 CUs) or four 4x4 blocks (8x8 CUs)."""
+    if size > 8 and rng.random() < 0.55:
+        h = size // 2
+        for dy in (0, h):
+            for dx in (0, h):
+                _intra_partition(rng, x0 + dx, y0 + dy, h, out, all_shapes)
+        return
+    r = rng.random()
+    if size in (16, 32) and r < 0.3:
+        q = size // 4
+        if rng.random() < 0.5:
+            out.extend((x0, y0 + i * q, size, q) for i in range(4))
+        else:
+            out.extend((x0 + i * q, y0, q, size) for i in range(4))
+    elif size == 64 and all_shapes and r < 0.3:
+        if rng.random() < 0.5:
+            out.extend((x0, y0 + i * 16, 64, 16) for i in range(4))
+        else:
+            out.extend((x0 + i * 16, y0, 16, 64) for i in range(4))
+    elif size == 8 and r < 0.3:
+        out.extend((x0 + dx, y0 + dy, 4, 4) for dy in (0, 4) for dx in (0, 4))
+    else:
+        out.append((x0, y0, size, size))
+
+
+def intra_edge_window(bw, bh):
+    """Samples below / above the top-left edge sample that the predictors of
+    a bw x bh block read (fill_reference_samples pads this far)."""
+    return bh + (11 * bw) // 4 + 6, bw + (11 * bh) // 4 + 6
+
+
+def intra_pack(rects, recon, rng, block_dtype):
+    """Descriptors and packed edge samples for blocks (x0, y0, w, h) of a
+    picture: top row / top-right from the reconstruction row above, left
+    column / left-down from the column to the left, coordinates clamped into
+    the picture; a missing side repeats the other one (128 when neither
+    exists).  Each block's window is 16-byte aligned in `edges`."""
+    height, width = recon.shape
+    rects = np.asarray(rects, np.int64).reshape(-1, 4)
+    n = len(rects)
+    lo = np.array([intra_edge_window(int(w), int(h))[0] for _, _, w, h in rects], np.int64)
+    hi = np.array([intra_edge_window(int(w), int(h))[1] for _, _, w, h in rects], np.int64)
+    size = (lo + hi + 1 + 15) // 16 * 16
+    start = np.cumsum(size) - size
+    edges = np.full(int(size.sum()) if n else 0, 128, np.uint8)
+    blocks = np.zeros(n, block_dtype)
+    for (bw, bh) in sorted(set(map(tuple, rects[:, 2:].tolist()))):
+        sel = np.nonzero((rects[:, 2] == bw) & (rects[:, 3] == bh))[0]
+        if not len(sel):
+            continue
+        x0, y0 = rects[sel, 0][:, None], rects[sel, 1][:, None]
+        L, H = intra_edge_window(bw, bh)
+        top_ok, left_ok = y0 > 0, x0 > 0
+        k = np.arange(1, H + 1)[None, :]
+        j = np.arange(1, L + 1)[None, :]
+        top = recon[np.maximum(y0 - 1, 0), np.clip(x0 + k - 1, 0, width - 1)]
+        left = recon[np.clip(y0 + j - 1, 0, height - 1), np.maximum(x0 - 1, 0)]
+        rep_l = recon[y0[:, 0], np.maximum(x0[:, 0] - 1, 0)][:, None]
+        rep_t = recon[np.maximum(y0[:, 0] - 1, 0), x0[:, 0]][:, None]
+        top = np.where(top_ok, top, np.where(left_ok, rep_l, 128))
+        left = np.where(left_ok, left, np.where(top_ok, rep_t, 128))
+        corner = np.where(top_ok[:, 0] & left_ok[:, 0], recon[np.maximum(y0[:, 0] - 1, 0), np.maximum(x0[:, 0] - 1, 0)],
+                          np.where(top_ok[:, 0], rep_t[:, 0], np.where(left_ok[:, 0], rep_l[:, 0], 128)))
+        ep = start[sel] + L
+        edges[ep] = corner
+        edges[ep[:, None] + k] = top
+        edges[ep[:, None] - j] = left
+        blocks["edge_offset"][sel] = ep
+    blocks["fenc_offset"] = rects[:, 1] * width + rects[:, 0]
+    blocks["width"], blocks["height"] = rects[:, 2], rects[:, 3]
+    blocks["dc_avail"] = ((rects[:, 1] > 0).astype(np.int16) << 8) | (rects[:, 0] > 0)
+    m0 = rng.integers(0, 33, n)
+    m1 = rng.integers(0, 32, n)
+    blocks["mpm"][:, 0] = m0
+    blocks["mpm"][:, 1] = m1 + (m1 >= m0)
+    level = np.log2(np.maximum(rects[:, 2], rects[:, 3])).astype(int)
+    blocks["num_for_rdo"] = np.array([INTRA_RDO_NUM.get(v, 6) for v in range(7)])[level]
+    return blocks, edges
+
+
+def intra_blocks(rng, src, recon, all_shapes=False, block_dtype=None):
+    """One partition of the picture (width, height multiples of 64) into
+    intra blocks of every shape, with packed edges (see intra_pack)."""
+    height, width = src.shape
+    rects = []
+    for y0 in range(0, height, 64):
+        for x0 in range(0, width, 64):
+            _intra_partition(rng, x0, y0, 64, rects, all_shapes)
+    return intra_pack(rects, recon, rng, block_dtype)
+
+
+def intra_level_blocks(width, height, shapes=None):
+    """Every block an encoder's intra mode decision visits on a picture: the
+    CUs of each level (64 .. 8) that lie inside it, the 4x4 blocks, and the
+    SDIP strips of the 32 / 16 CUs, each set tiling the picture."""
+    shapes = shapes or INTRA_ENC_SHAPES
+    rects = []
+    for bw, bh in shapes:
+        ys, xs = np.meshgrid(np.arange(0, height - bh + 1, bh), np.arange(0, width - bw + 1, bw), indexing="ij")
+        rects.append(np.stack([xs.ravel(), ys.ravel(), np.full(xs.size, bw), np.full(xs.size, bh)], 1))
+    return np.concatenate(rects)
