@@ -291,8 +291,10 @@ XAVS2GPU_API void xavs2gpu_intra_pred_init(uint32_t cpuid, xavs2gpu_intra_pred_t
  * they were in its buffer).  Device pointers; edges + edge_offset is the
  * block's top-left edge sample and samples -(height + 11*width/4 + 6) ..
  * width + 11*height/4 + 6 around it are read.
- * A block whose size is not 4..64 or whose MPMs are not modes reports
- * num_for_rdo = -1. */
+ * A block whose sides are not powers of two in 4..64 with an aspect ratio of
+ * at most 4, or whose MPMs are not modes, reports num_for_rdo = -1 (and no
+ * costs).  Blocks are processed sorted by shape; the order of the batch is
+ * free. */
 typedef struct xavs2gpu_intra_block {
     int64_t edge_offset;
     int64_t fenc_offset;     /* source block: fenc + fenc_offset, stride fenc_stride */

@@ -144,9 +144,35 @@ def test_intra_rmd_edges(gpu, olib):
     cost, modes, ccost, nrdo = _rmd_expected(olib, blocks, edges, src, prm)
     assert np.array_equal(got["cost"], cost) and np.array_equal(got["cand_mode"], modes)
     assert np.array_equal(got["num_for_rdo"], nrdo)
-    bad = blocks[:4].copy()
-    bad["width"] = (12, 4, 128, 8)
-    bad["height"] = (4, 0, 64, 8)
+    bad = blocks[:5].copy()
+    bad["width"] = (12, 4, 128, 8, 4)
+    bad["height"] = (4, 0, 64, 8, 32)
     bad["mpm"][3] = (40, 2)
     got = _rmd_gpu(gpu, bad, edges, src, prm)
-    assert list(got["num_for_rdo"]) == [-1, -1, -1, -1]
+    assert list(got["num_for_rdo"]) == [-1] * 5
+
+
+def test_intra_rmd_every_shape(gpu, olib):
+    """All 19 shapes with power-of-two sides and aspect ratio <= 4 in one
+    shuffled batch (classes of 1 .. 40 blocks, partial tiles)."""
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(12)
+    src = synth.base_picture(rng, 256, 256)
+    recon = np.clip(src.astype(np.int32) + rng.integers(-6, 7, src.shape), 0, 255).astype(np.uint8)
+    rects = []
+    for a in range(5):
+        for b in range(5):
+            if abs(a - b) > 2:
+                continue
+            w, h = 4 << a, 4 << b
+            for _ in range(int(rng.integers(1, 41))):
+                rects.append((int(rng.integers(0, (256 - w) // 4 + 1)) * 4, int(rng.integers(0, 256 - h + 1)), w, h))
+    rects = [rects[i] for i in rng.permutation(len(rects))]
+    blocks, edges = synth.intra_pack(rects, recon, rng, xg.INTRA_BLOCK_DTYPE)
+    for hadamard in (1, 0):
+        prm = xg.IntraParams(7.25, hadamard, 1, 4, 2)
+        got = _rmd_gpu(gpu, blocks, edges, src, prm)
+        cost, modes, ccost, nrdo = _rmd_expected(olib, blocks, edges, src, prm)
+        assert np.array_equal(got["cost"], cost), hadamard
+        assert np.array_equal(got["cand_mode"], modes) and np.array_equal(got["num_for_rdo"], nrdo)

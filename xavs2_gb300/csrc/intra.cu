@@ -194,47 +194,230 @@ __global__ void __launch_bounds__(256) pred_block_kernel(int mode, const uint8_t
     }
 }
 
-// ---- batched rough mode decision -----------------------------------------------
-constexpr int kWarps = 8;
-constexpr int kEdge = 256;        // staged edge: ep at edge[256], windows up to 246 below / 198 above
+// ---- batched rough mode decision ---------------------------------------------
+// Blocks are sorted by shape class ((log2 w - 2) * 5 + log2 h - 2); a CTA
+// takes a tile of G blocks of one class and all 33 modes.  A warp handles
+// one mode at a time for the whole tile, so its branches are uniform: a lane
+// owns one SATD unit (8x4, or 4x4 for width-4 blocks) of one block, predicts
+// it in registers straight from the edge samples and scores it; the lanes of
+// a block then sum their units with shuffles.  Every prediction tap is a
+// 4-sample window of the edge array (in ascending address order for all
+// directions) taken with a funnel shift and weighted with one dp4a.
 constexpr int kN = 9;             // INTRA_MODE_NUM_FOR_RDO (defines.h:290)
+constexpr int kTW = 11;           // warps per CTA: 3 modes each
+constexpr int kTT = kTW * 32;
+constexpr int kCls = 25;
+constexpr int kEdgeArea = 1984;   // max over classes of G * align4(edge window), plus word-read slack
 
-struct Smem {
-    uint8_t edge[2 * kEdge];
-    uint8_t fenc[64 * 64];
-    uint8_t pred[kWarps][64 * 64];
-    double cost[33];
+struct Geo {
+    int w, h, uw, nux, lanes, iters, G, lo, hi, R;
+};
+__host__ __device__ __forceinline__ int side_log(int v)
+{
+    return v == 4 ? 0 : v == 8 ? 1 : v == 16 ? 2 : v == 32 ? 3 : v == 64 ? 4 : -1;
+}
+__host__ __device__ __forceinline__ Geo geo_of(int c)
+{
+    Geo g;
+    g.w = 4 << (c / 5);
+    g.h = 4 << (c % 5);
+    g.uw = g.w == 4 ? 4 : 8;   // satd_unit4 (pixel.c:354-407)
+    g.nux = g.w / g.uw;
+    const int units = g.nux * (g.h >> 2);
+    g.lanes = units < 32 ? units : 32;
+    g.iters = units / g.lanes;
+    g.G = 32 / g.lanes;
+    g.lo = edge_below(g.w, g.h);
+    g.hi = edge_above(g.w, g.h);
+    g.R = (g.lo + g.hi + 1 + 3) & ~3;
+    return g;
+}
+
+struct TileSmem {
+    uint8_t edge[kEdgeArea];          // block b: edge samples -lo..hi at b * R
+    uint8_t fenc[4096];               // block b: w x h source samples at b * w * h
+    double cost[32][33];
+    int satd[32][33];
+    int kc[32][8];                    // dc, plane a / b / c, bilinear corner term
+    int64_t eoff[32], foff[32];
+    int idx[32], dc_avail[32], mpm[32][2], nrdo[32];
+    int tile_base[kCls + 1], order[kCls], start[kCls], count[kCls];
 };
 
+// 4 edge samples p[0..3] as one word (any byte alignment)
+__device__ __forceinline__ uint32_t win4(const uint8_t *p)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    return __funnelshift_r(w[0], w[1], (unsigned)(a & 3) * 8u);
+}
+__device__ __forceinline__ uint32_t wts(int b0, int b1, int b2, int b3)
+{
+    return (uint32_t)b0 | ((uint32_t)b1 << 8) | ((uint32_t)b2 << 16) | ((uint32_t)b3 << 24);
+}
+__device__ __forceinline__ int tap(const uint8_t *ep, int s, uint32_t w)
+{
+    return (int)(__dp4a(win4(ep + s), w, 64u) >> 7);
+}
+
+// Hadamard sum of a 4x4 difference block held in registers
+__device__ __forceinline__ int hsum4_reg(int (&d)[4][4])
+{
+#pragma unroll
+    for (int r = 0; r < 4; r++) fwht4_d(d[r][0], d[r][1], d[r][2], d[r][3]);
+    int s = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        fwht4_d(d[0][c], d[1][c], d[2][c], d[3][c]);
+        s += iabs_d(d[0][c]) + iabs_d(d[1][c]) + iabs_d(d[2][c]) + iabs_d(d[3][c]);
+    }
+    return s;
+}
+
+// |H (src - pred) H^T| of the 4x4 sub-block at (x0, y0) of a block in `mode`
+__device__ __forceinline__ int sub4_hsum(int mode, const uint8_t *ep, const uint8_t *fb, const Geo &g, int x0, int y0,
+                                         const int *kc, bool narrow5, bool narrow31)
+{
+    int p[4][4];
+    if (mode == 0) {
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) p[r][c] = kc[0];
+    } else if (mode == 1) {
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) p[r][c] = min(max((kc[1] + kc[2] * (x0 + c) + kc[3] * (y0 + r)) >> 5, 0), 255);
+    } else if (mode == 2) {
+        const int lx = ilog2d(g.w), ly = ilog2d(g.h), a = ep[g.w], b = ep[-g.h];
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int x = x0 + c, y = y0 + r, top = ep[1 + x], left = ep[-1 - y];
+                const int predx = (left << lx) + (x + 1) * (a - left);
+                const int predy = (top << ly) + (y + 1) * (b - top);
+                const int v = ((predx << ly) + (predy << lx) + x * y * kc[4] + (1 << (lx + ly))) >> (lx + ly + 1);
+                p[r][c] = min(max(v, 0), 255);
+            }
+    } else if (mode == 12) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int v = ep[1 + x0 + c];
+#pragma unroll
+            for (int r = 0; r < 4; r++) p[r][c] = v;
+        }
+    } else if (mode == 24) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int v = ep[-1 - y0 - r];
+#pragma unroll
+            for (int c = 0; c < 4; c++) p[r][c] = v;
+        }
+    } else if (narrow5 || narrow31) {
+        // the reference's tabulated mode-5 / mode-31 variants (intra.c:455-605, 1147-1161)
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                p[r][c] = narrow5 ? mode5_narrow([ep](int i) { return (int)ep[i]; }, x0 + c, y0 + r, g.w)
+                                  : mode5_narrow([ep](int i) { return (int)ep[-i]; }, y0 + r, x0 + c, g.h);
+    } else if (mode < 12) {
+        // from the top row: row y reads ep[ix .. ix + 3], ix = step + x
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int f;
+            const int ix = ang_step(mode, 0, y0 + r + 1, f) + x0;
+            const uint32_t w = wts(32 - f, 64 - f, 32 + f, f);
+#pragma unroll
+            for (int c = 0; c < 4; c++) p[r][c] = tap(ep, ix + c, w);
+        }
+    } else if (mode > 24) {
+        // from the left column: column x reads ep[-iy - 3 .. -iy], iy = y + step
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            int f;
+            const int iy = ang_step(mode, 1, x0 + c + 1, f) + y0;
+            const uint32_t w = wts(f, 32 + f, 64 - f, 32 - f);
+#pragma unroll
+            for (int r = 0; r < 4; r++) p[r][c] = tap(ep, -iy - r - 3, w);
+        }
+    } else {
+        // both edges (intra.c:363-397)
+        int sx[4], sy[4];
+        uint32_t wx[4], wy[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int f;
+            sx[r] = ang_step(mode, 0, y0 + r + 1, f);
+            wx[r] = wts(f, 32 + f, 64 - f, 32 - f);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            int f;
+            sy[c] = ang_step(mode, 1, x0 + c + 1, f);
+            wy[c] = wts(32 - f, 64 - f, 32 + f, f);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int x = x0 + c, y = y0 + r, iyy = y - sy[c];
+                p[r][c] = iyy <= -1 ? tap(ep, x - sx[r] - 1, wx[r]) : tap(ep, -iyy - 2, wy[c]);
+            }
+    }
+    int d[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const uint32_t f = *reinterpret_cast<const uint32_t *>(fb + (y0 + r) * g.w + x0);
+#pragma unroll
+        for (int c = 0; c < 4; c++) d[r][c] = (int)((f >> (8 * c)) & 0xFFu) - p[r][c];
+    }
+    return hsum4_reg(d);
+}
+
+// SAD of the same sub-block (use_hadamard = 0)
+__device__ __forceinline__ int sub4_sad(int mode, const uint8_t *ep, const uint8_t *fb, const Geo &g, int x0, int y0,
+                                        const ModeConst &k)
+{
+    int s = 0;
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++)
+            s += iabs_d((int)fb[(y0 + r) * g.w + x0 + c] - pred_sample(mode, ep, x0 + c, y0 + r, g.w, g.h, k));
+    return s;
+}
+
 // update_candidate_list (md_intra.c:195-210): insertion into the list kept
-// sorted by cost, after equal costs
-__device__ void cand_insert(int mode, double cost, int *modes, double *costs)
+// sorted by cost, after equal costs.  Costs are non-negative doubles, so
+// their bit patterns order like the values.
+__device__ void cand_insert(int mode, long long key, int *modes, long long *keys)
 {
     int i = kN - 1;
-    if (!(cost < costs[i])) return;
-    while (i > 0 && cost < costs[i - 1]) {
+    if (!(key < keys[i])) return;
+    while (i > 0 && key < keys[i - 1]) {
         modes[i] = modes[i - 1];
-        costs[i] = costs[i - 1];
+        keys[i] = keys[i - 1];
         i--;
     }
     modes[i] = mode;
-    costs[i] = cost;
+    keys[i] = key;
 }
 
 // The candidate list of rdo_get_pred_intra_luma (all modes) or of the rough
 // three-phase search rdo_get_pred_intra_luma_rmd (md_intra.c:258-380),
 // replayed on the per-mode costs; returns the number of modes for RDO.
 __device__ int candidates(const double *cost, int rough, int dist2, int dist1, int num_for_rdo, const int *mpm,
-                          int *modes, double *costs)
+                          int *modes, long long *keys)
 {
     int visited[33];
     for (int m = 0; m < 33; m++) visited[m] = 0;
     for (int i = 0; i < kN; i++) {
         modes[i] = 0;
-        costs[i] = (double)(1LL << 50);   // MAX_COST (defines.h:299)
+        keys[i] = __double_as_longlong((double)(1LL << 50));   // MAX_COST (defines.h:299)
     }
     auto visit = [&](int m) {
-        cand_insert(m, cost[m], modes, costs);
+        cand_insert(m, __double_as_longlong(cost[m]), modes, keys);
         visited[m] = 1;
     };
     if (!rough) {
@@ -281,71 +464,193 @@ __device__ int candidates(const double *cost, int rough, int dist2, int dist1, i
     return num_for_rdo < j ? num_for_rdo : j;
 }
 
-__global__ void __launch_bounds__(kWarps * 32) rmd_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks, int n,
-                                                          const uint8_t *__restrict__ edges,
-                                                          const uint8_t *__restrict__ fenc, int fenc_stride,
-                                                          xavs2gpu_intra_params_t prm,
-                                                          xavs2gpu_intra_result_t *__restrict__ out)
+__device__ __forceinline__ int block_class(const xavs2gpu_intra_block_t &b)
+{
+    const int a = side_log(b.width), c = side_log(b.height);
+    if (a < 0 || c < 0 || a - c > 2 || c - a > 2) return -1;   // sides 4..64, aspect ratio at most 4
+    if (b.mpm[0] < 0 || b.mpm[0] > 32 || b.mpm[1] < 0 || b.mpm[1] > 32) return -1;
+    return a * 5 + c;
+}
+
+// 1. per-class counts (warp-aggregated atomics); other blocks are reported
+__global__ void rmd_count_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks, int n, int *__restrict__ counts,
+                                 xavs2gpu_intra_result_t *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1;
+    if (i < n) {
+        c = block_class(blocks[i]);
+        if (c < 0) out[i].num_for_rdo = -1;   // not a block the encoder predicts
+    }
+    const unsigned valid = __ballot_sync(0xffffffffu, c >= 0);
+    if (c >= 0) {
+        const unsigned same = __match_any_sync(valid, c);
+        if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&counts[c], __popc(same));
+    }
+}
+
+// 2. scatter into the class-ordered list
+__global__ void rmd_scatter_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks, int n,
+                                   const int *__restrict__ counts, int *__restrict__ cursor, int *__restrict__ sorted)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int c = i < n ? block_class(blocks[i]) : -1;
+    const unsigned valid = __ballot_sync(0xffffffffu, c >= 0);
+    if (c < 0) return;
+    const unsigned same = __match_any_sync(valid, c);
+    const int leader = __ffs(same) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&cursor[c], __popc(same));
+    base = __shfl_sync(same, base, leader);
+    int start = 0;
+    for (int k = 0; k < c; k++) start += counts[k];
+    sorted[start + base + __popc(same & ((1u << lane) - 1))] = i;
+}
+
+// 3. the tiles, persistent; classes with the most work per tile first
+__global__ void __launch_bounds__(kTT) rmd_tile_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks,
+                                                        const int *__restrict__ counts, const int *__restrict__ sorted,
+                                                        const uint8_t *__restrict__ edges,
+                                                        const uint8_t *__restrict__ fenc, int fenc_stride,
+                                                        xavs2gpu_intra_params_t prm,
+                                                        xavs2gpu_intra_result_t *__restrict__ out)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    Smem &s = *reinterpret_cast<Smem *>(smem_raw);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int bi = blockIdx.x; bi < n; bi += gridDim.x) {
-        const xavs2gpu_intra_block_t b = blocks[bi];
-        const int bsx = b.width, bsy = b.height;
-        const auto ok_side = [](int v) { return v == 4 || v == 8 || v == 16 || v == 32 || v == 64; };
-        if (!ok_side(bsx) || !ok_side(bsy) || b.mpm[0] < 0 || b.mpm[0] > 32 || b.mpm[1] < 0 || b.mpm[1] > 32) {
-            if (threadIdx.x == 0) out[bi].num_for_rdo = -1;   // not a block the encoder predicts
-            continue;
+    TileSmem &s = *reinterpret_cast<TileSmem *>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        int acc = 0;
+        for (int c = 0; c < kCls; c++) {
+            s.count[c] = counts[c];
+            s.start[c] = acc;
+            acc += s.count[c];
         }
-        const uint8_t *ep_g = edges + b.edge_offset;
-        const int lo = edge_below(bsx, bsy), hi = edge_above(bsx, bsy);
-        for (int i = threadIdx.x - lo; i <= hi; i += blockDim.x) s.edge[kEdge + i] = ep_g[i];
-        const uint8_t *src = fenc + b.fenc_offset;
-        for (int i = threadIdx.x; i < bsx * bsy; i += blockDim.x) s.fenc[i] = src[(i / bsx) * fenc_stride + i % bsx];
+        // order: tile work (G * w * h) descending, ties by class
+        for (int c = 0; c < kCls; c++) s.order[c] = c;
+        for (int i = 1; i < kCls; i++) {
+            const int c = s.order[i];
+            const Geo gc = geo_of(c);
+            const int wc = gc.G * gc.w * gc.h;
+            int j = i;
+            while (j > 0) {
+                const Geo gp = geo_of(s.order[j - 1]);
+                if (gp.G * gp.w * gp.h >= wc) break;
+                s.order[j] = s.order[j - 1];
+                j--;
+            }
+            s.order[j] = c;
+        }
+        s.tile_base[0] = 0;
+        for (int k = 0; k < kCls; k++) {
+            const Geo g = geo_of(s.order[k]);
+            s.tile_base[k + 1] = s.tile_base[k] + (s.count[s.order[k]] + g.G - 1) / g.G;
+        }
+    }
+    __syncthreads();
+    const int total = s.tile_base[kCls];
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        int k = 0;
+        while (t >= s.tile_base[k + 1]) k++;
+        const int c = s.order[k];
+        const Geo g = geo_of(c);
+        const int first = s.start[c] + (t - s.tile_base[k]) * g.G;
+        const int rem = s.start[c] + s.count[c] - first;
+        const int nb = rem < g.G ? rem : g.G;
+        if (tid < nb) {
+            const int bi = sorted[first + tid];
+            const xavs2gpu_intra_block_t b = blocks[bi];
+            s.idx[tid] = bi;
+            s.eoff[tid] = b.edge_offset;
+            s.foff[tid] = b.fenc_offset;
+            s.dc_avail[tid] = b.dc_avail;
+            s.mpm[tid][0] = b.mpm[0];
+            s.mpm[tid][1] = b.mpm[1];
+            s.nrdo[tid] = b.num_for_rdo;
+        }
         __syncthreads();
-        const uint8_t *ep = s.edge + kEdge;
-        uint8_t *pred = s.pred[warp];
-        const bool u4 = prm.use_hadamard ? satd_unit4(bsx, bsy) : (bsx == 4);
-        const int uw = u4 ? 4 : 8, nux = bsx / uw, nu = nux * (bsy >> 2);
-        for (int mode = warp; mode < 33; mode += kWarps) {
-            const ModeConst k = mode_const(mode, ep, b.dc_avail, bsx, bsy, lane);
-            for (int i = lane; i < bsx * bsy; i += 32) {
-                const int y = i / bsx, x = i - y * bsx;
-                pred[i] = (uint8_t)pred_sample(mode, ep, x, y, bsx, bsy, k);
-            }
-            __syncwarp();
-            int d = 0;
-            for (int u = lane; u < nu; u += 32) {
-                const int uy = u / nux, ux = u - uy * nux;
-                const int off = uy * 4 * bsx + ux * uw;
-                if (prm.use_hadamard) {
-                    d += satd_unit_d(u4, s.fenc + off, bsx, pred + off, bsx);
-                } else {
-                    for (int r = 0; r < 4; r++)
-                        for (int c = 0; c < uw; c++) d += iabs_d((int)s.fenc[off + r * bsx + c] - (int)pred[off + r * bsx + c]);
-                }
-            }
-            d = warp_sum(d);
+        // stage the edge windows and the source blocks
+        const int ew = g.lo + g.hi + 1;
+        for (int e = tid; e < nb * ew; e += kTT) {
+            const int b = e / ew, r = e - b * ew;
+            s.edge[b * g.R + r] = edges[s.eoff[b] - g.lo + r];
+        }
+        const int area = g.w * g.h;
+        const int lw = ilog2d(g.w);
+        for (int e = tid; e < nb * area; e += kTT) {
+            const int b = e / area, r = e - b * area, y = r >> lw, x = r & (g.w - 1);
+            s.fenc[e] = fenc[s.foff[b] + (int64_t)y * fenc_stride + x];
+        }
+        __syncthreads();
+        // DC / plane / bilinear constants, a warp per block
+        for (int b = warp; b < nb; b += kTW) {
+            const uint8_t *ep = s.edge + b * g.R + g.lo;
+            const ModeConst k0 = mode_const(0, ep, s.dc_avail[b], g.w, g.h, lane);
+            const ModeConst k1 = mode_const(1, ep, 0, g.w, g.h, lane);
+            const ModeConst k2 = mode_const(2, ep, 0, g.w, g.h, lane);
             if (lane == 0) {
-                const int bits = (b.mpm[0] == mode || b.mpm[1] == mode) ? 2 : 6;
-                s.cost[mode] = __dadd_rn(__dmul_rn(prm.lambda, (double)bits), (double)d);
+                s.kc[b][0] = k0.dc;
+                s.kc[b][1] = k1.pa;
+                s.kc[b][2] = k1.pb;
+                s.kc[b][3] = k1.pc;
+                s.kc[b][4] = k2.bt;
             }
-            __syncwarp();
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            xavs2gpu_intra_result_t &r = out[bi];
-            const int mpm[2] = {b.mpm[0], b.mpm[1]};
+        // every mode: a warp per mode, a lane per SATD unit
+        {
+            const int b = lane / g.lanes, u0 = lane - b * g.lanes;
+            const bool live = b < nb;
+            const int bb = live ? b : 0;
+            const uint8_t *ep = s.edge + bb * g.R + g.lo;
+            const uint8_t *fb = s.fenc + bb * area;
+            const int *kc = s.kc[bb];
+            for (int mode = warp; mode < 33; mode += kTW) {
+                const bool n5 = mode == 5 && ((g.w == 4 && g.h == 16) || (g.w == 8 && g.h == 32));
+                const bool n31 = mode == 31 && ((g.w == 16 && g.h == 4) || (g.w == 32 && g.h == 8));
+                int acc = 0;
+                if (live) {
+                    for (int it = 0; it < g.iters; it++) {
+                        const int u = u0 + it * g.lanes, uy = (u / g.nux) * 4, ux = (u - (u / g.nux) * g.nux) * g.uw;
+                        if (prm.use_hadamard) {
+                            int hs = sub4_hsum(mode, ep, fb, g, ux, uy, kc, n5, n31);
+                            if (g.uw == 8) hs += sub4_hsum(mode, ep, fb, g, ux + 4, uy, kc, n5, n31);
+                            acc += hs >> 1;
+                        } else {
+                            ModeConst k{};
+                            k.dc = kc[0]; k.pa = kc[1]; k.pb = kc[2]; k.pc = kc[3]; k.bt = kc[4];
+                            k.ba = ep[g.w]; k.bb = ep[-g.h]; k.lx = ilog2d(g.w); k.ly = ilog2d(g.h);
+                            acc += sub4_sad(mode, ep, fb, g, ux, uy, k);
+                            if (g.uw == 8) acc += sub4_sad(mode, ep, fb, g, ux + 4, uy, k);
+                        }
+                    }
+                }
+                for (int o = g.lanes >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (live && u0 == 0) s.satd[b][mode] = acc;
+            }
+        }
+        __syncthreads();
+        // costs (rdcost_t, md_intra.c:216-226) and the candidate lists
+        for (int e = tid; e < nb * 33; e += kTT) {
+            const int b = e / 33, m = e - b * 33;
+            const int bits = (s.mpm[b][0] == m || s.mpm[b][1] == m) ? 2 : 6;
+            const double cst = __dadd_rn(__dmul_rn(prm.lambda, (double)bits), (double)s.satd[b][m]);
+            s.cost[b][m] = cst;
+            out[s.idx[b]].cost[m] = cst;
+        }
+        __syncthreads();
+        if (tid < nb) {
             int modes[kN];
-            double costs[kN];
-            r.num_for_rdo = candidates(s.cost, prm.rough, prm.dist2, prm.dist1, b.num_for_rdo, mpm, modes, costs);
+            long long keys[kN];
+            const int nr = candidates(s.cost[tid], prm.rough, prm.dist2, prm.dist1, s.nrdo[tid], s.mpm[tid], modes,
+                                      keys);
+            xavs2gpu_intra_result_t &r = out[s.idx[tid]];
+            r.num_for_rdo = nr;
             for (int i = 0; i < kN; i++) {
                 r.cand_mode[i] = modes[i];
-                r.cand_cost[i] = costs[i];
+                r.cand_cost[i] = __longlong_as_double(keys[i]);
             }
         }
-        for (int m = threadIdx.x; m < 33; m += blockDim.x) out[bi].cost[m] = s.cost[m];
         __syncthreads();
     }
 }
@@ -419,24 +724,50 @@ extern "C" void xavs2gpu_intra_pred_init(uint32_t cpuid, xavs2gpu_intra_pred_t i
 
 extern "C" int xavs2gpu_intra_rmd_batch(const xavs2gpu_intra_block_t *blocks, int n, const uint8_t *edges,
                                         const uint8_t *fenc, int fenc_stride, const xavs2gpu_intra_params_t *prm,
-                                        xavs2gpu_intra_result_t *out, void *stream)
+                                        xavs2gpu_intra_result_t *out, void *stream_)
 {
     if (n < 0 || !prm || prm->dist1 < 0 || prm->dist2 < 0) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_intra_rmd_batch", "bad count or parameters");
         return XAVS2GPU_ERR_ARG;
     }
     if (n == 0) return XAVS2GPU_OK;
-    static bool attr[64] = {false};
+    const cudaStream_t stream = (cudaStream_t)stream_;
+    constexpr int smem = (int)sizeof(intra::TileSmem);
+    static bool attr_set[64] = {false};
+    static int ctas_per_sm[64] = {0}, sms[64] = {0};
     const int dev = current_device();
-    if (dev >= 0 && dev < 64 && !attr[dev]) {
-        XG_CUDA(cudaFuncSetAttribute(intra::rmd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(intra::Smem)));
-        attr[dev] = true;
+    if (dev < 0 || dev >= 64) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_intra_rmd_batch", "device index out of range");
+        return XAVS2GPU_ERR_ARG;
     }
-    const int grid = n < 152 * 8 ? n : 152 * 8;
-    intra::rmd_kernel<<<grid, intra::kWarps * 32, sizeof(intra::Smem), (cudaStream_t)stream>>>(
-        blocks, n, edges, fenc, fenc_stride, *prm, out);
-    count_launch();
+    if (!attr_set[dev]) {
+        XG_CUDA(cudaFuncSetAttribute(intra::rmd_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas_per_sm[dev], intra::rmd_tile_kernel, intra::kTT,
+                                                              smem));
+        XG_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev));
+        if (ctas_per_sm[dev] < 1) ctas_per_sm[dev] = 1;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        attr_set[dev] = true;
+    }
+    // scratch: class counts and cursors (32 ints each), then the ordered list
+    int *scratch = nullptr;
+    XG_CUDA(cudaMallocAsync((void **)&scratch, sizeof(int) * (64 + (size_t)n), stream));
+    if (!scratch) return XAVS2GPU_ERR_CUDA;
+    int *counts = scratch, *cursor = scratch + 32, *sorted = scratch + 64;
+    XG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * 64, stream));
+    const int nb = (n + 255) / 256;
+    intra::rmd_count_kernel<<<nb, 256, 0, stream>>>(blocks, n, counts, out);
+    intra::rmd_scatter_kernel<<<nb, 256, 0, stream>>>(blocks, n, counts, cursor, sorted);
+    long long grid = (long long)sms[dev] * ctas_per_sm[dev];
+    if (grid > n) grid = n;
+    intra::rmd_tile_kernel<<<(int)grid, intra::kTT, smem, stream>>>(blocks, counts, sorted, edges, fenc, fenc_stride,
+                                                                     *prm, out);
+    count_launch(3);
+    XG_CUDA(cudaFreeAsync(scratch, stream));
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
 }

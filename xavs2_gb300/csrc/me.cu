@@ -825,20 +825,6 @@ struct MeSessionImpl {
     uint8_t *ref_plane(int slot, int k) { return plane(1 + 16 * slot_buf[slot] + k); }
 };
 
-// Uploads the plane pointer tables of the current slot assignment and the
-// session view (stream-ordered).
-static void refresh_tables(MeSessionImpl &m)
-{
-    std::vector<uint8_t *> ptrs(1 + 16 * m.nrefs);
-    ptrs[0] = m.plane(0);
-    for (int r = 0; r < m.nrefs; r++)
-        for (int k = 0; k < 16; k++) ptrs[1 + 16 * r + k] = m.ref_plane(r, k);
-    std::vector<const uint8_t *> r0(m.nrefs);
-    for (int r = 0; r < m.nrefs; r++) r0[r] = m.ref_plane(r, 0);
-    XG_CUDA(cudaMemcpyAsync(m.d_plane_ptrs, ptrs.data(), sizeof(uint8_t *) * ptrs.size(), cudaMemcpyHostToDevice, m.st));
-    XG_CUDA(cudaMemcpyAsync(m.d_ref0, r0.data(), sizeof(uint8_t *) * r0.size(), cudaMemcpyHostToDevice, m.st));
-}
-
 static void refresh_view(MeSessionImpl &m)
 {
     SessView v;
