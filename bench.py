@@ -740,7 +740,7 @@ def run_intra(args):
                 "h2d_bytes_per_step": int(h_blocks.numel() + h_edges.numel() + h_src.numel()),
                 "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "int", "kernel": "rmd_kernel", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "int", "kernel": "intra_rmd_batch (sort, tiles, candidates)", "achieved": achieved, "peak": peak,
                      "unit": "T mode-samples/s", "frac": achieved / peak, "traffic": None,
                      "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per mode-sample (%s)"
                                     % (INTRA_OPS_PER_SAMPLE, peak_src),

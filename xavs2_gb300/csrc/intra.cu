@@ -49,6 +49,10 @@ __device__ __forceinline__ int ilog2d(int v) { return 31 - __clz(v); }
 __host__ __device__ __forceinline__ int edge_below(int bsx, int bsy) { return bsy + (11 * bsx) / 4 + 6; }
 __host__ __device__ __forceinline__ int edge_above(int bsx, int bsy) { return bsx + (11 * bsy) / 4 + 6; }
 
+// Plane-mode multiplier and shift per log2 block side 2..6 (intra.c:194-195)
+__device__ __forceinline__ int plane_mult(int l) { return (int)((0x170B05110DULL >> (8 * (l - 2))) & 0xFF); }
+__device__ __forceinline__ int plane_shift(int l) { return (int)((0x130F0B0A07ULL >> (8 * (l - 2))) & 0xFF); }
+
 // Per-(block, mode) constants of the non-angular modes.
 struct ModeConst {
     int dc;                  // DC value
@@ -152,15 +156,14 @@ __device__ ModeConst mode_const(int mode, const uint8_t *ep, int dc_avail, int b
         else if (top) k.dc = (sa + (bsx >> 1)) >> ilog2d(bsx);
         else k.dc = 128;
     } else if (mode == 1) {   // intra.c:192-236
-        const int mult[7] = {0, 0, 13, 17, 5, 11, 23}, shf[7] = {0, 0, 7, 10, 11, 15, 19};
         const int lx = ilog2d(bsx), ly = ilog2d(bsy), w2 = bsx >> 1, h2 = bsy >> 1;
         int H = 0, V = 0;
         for (int i = lane + 1; i <= w2; i += 32) H += i * (ep[w2 + i] - ep[w2 - i]);
         for (int i = lane + 1; i <= h2; i += 32) V += i * (ep[-h2 - i] - ep[-h2 + i]);
         H = warp_sum(H);
         V = warp_sum(V);
-        k.pb = ((H << 5) * mult[lx] + (1 << (shf[lx] - 1))) >> shf[lx];
-        k.pc = ((V << 5) * mult[ly] + (1 << (shf[ly] - 1))) >> shf[ly];
+        k.pb = ((H << 5) * plane_mult(lx) + (1 << (plane_shift(lx) - 1))) >> plane_shift(lx);
+        k.pc = ((V << 5) * plane_mult(ly) + (1 << (plane_shift(ly) - 1))) >> plane_shift(ly);
         k.pa = ((ep[-bsy] + ep[bsx]) << 4) + 16 - k.pb * (w2 - 1) - k.pc * (h2 - 1);
     } else if (mode == 2) {   // intra.c:238-293
         const int lx = ilog2d(bsx), ly = ilog2d(bsy), sh = min(lx, ly);
@@ -235,13 +238,22 @@ __host__ __device__ __forceinline__ Geo geo_of(int c)
 
 struct TileSmem {
     uint8_t edge[kEdgeArea];          // block b: edge samples -lo..hi at b * R
-    uint8_t fenc[4096];               // block b: w x h source samples at b * w * h
-    double cost[32][33];
+    uint8_t fenc[4096 + 64];          // block b: w x h source samples at b * (w * h + 4)
     int satd[32][33];
-    int kc[32][8];                    // dc, plane a / b / c, bilinear corner term
     int64_t eoff[32], foff[32];
-    int idx[32], dc_avail[32], mpm[32][2], nrdo[32];
+    int idx[32], dc_avail[32], mpm[32][2];
+    int next_mode;
     int tile_base[kCls + 1], order[kCls], start[kCls], count[kCls];
+};
+
+// Modes in the order warps take them: the per-sample two-edge modes first,
+// then the one-edge angles, then the cheap ones (longest work first).
+__constant__ int8_t c_mode_order[33] = {13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 3, 4, 5, 6, 7, 8,
+                                        9,  10, 11, 25, 26, 27, 28, 29, 30, 31, 32, 2, 1, 0, 12, 24};
+
+// Per-lane constants of the non-angular modes for the lane's block
+struct LaneConst {
+    int dc, pa, pb, pc, bt;
 };
 
 // 4 edge samples p[0..3] as one word (any byte alignment)
@@ -275,20 +287,20 @@ __device__ __forceinline__ int hsum4_reg(int (&d)[4][4])
 }
 
 // |H (src - pred) H^T| of the 4x4 sub-block at (x0, y0) of a block in `mode`
-__device__ __forceinline__ int sub4_hsum(int mode, const uint8_t *ep, const uint8_t *fb, const Geo &g, int x0, int y0,
-                                         const int *kc, bool narrow5, bool narrow31)
+__device__ __forceinline__ int sub4_hsum(int mode, const uint8_t *ep, const uint8_t *fb, int fstride, const Geo &g,
+                                         int x0, int y0, const LaneConst &kc, bool narrow5, bool narrow31)
 {
     int p[4][4];
     if (mode == 0) {
 #pragma unroll
         for (int r = 0; r < 4; r++)
 #pragma unroll
-            for (int c = 0; c < 4; c++) p[r][c] = kc[0];
+            for (int c = 0; c < 4; c++) p[r][c] = kc.dc;
     } else if (mode == 1) {
 #pragma unroll
         for (int r = 0; r < 4; r++)
 #pragma unroll
-            for (int c = 0; c < 4; c++) p[r][c] = min(max((kc[1] + kc[2] * (x0 + c) + kc[3] * (y0 + r)) >> 5, 0), 255);
+            for (int c = 0; c < 4; c++) p[r][c] = min(max((kc.pa + kc.pb * (x0 + c) + kc.pc * (y0 + r)) >> 5, 0), 255);
     } else if (mode == 2) {
         const int lx = ilog2d(g.w), ly = ilog2d(g.h), a = ep[g.w], b = ep[-g.h];
 #pragma unroll
@@ -298,7 +310,7 @@ __device__ __forceinline__ int sub4_hsum(int mode, const uint8_t *ep, const uint
                 const int x = x0 + c, y = y0 + r, top = ep[1 + x], left = ep[-1 - y];
                 const int predx = (left << lx) + (x + 1) * (a - left);
                 const int predy = (top << ly) + (y + 1) * (b - top);
-                const int v = ((predx << ly) + (predy << lx) + x * y * kc[4] + (1 << (lx + ly))) >> (lx + ly + 1);
+                const int v = ((predx << ly) + (predy << lx) + x * y * kc.bt + (1 << (lx + ly))) >> (lx + ly + 1);
                 p[r][c] = min(max(v, 0), 255);
             }
     } else if (mode == 12) {
@@ -370,7 +382,7 @@ __device__ __forceinline__ int sub4_hsum(int mode, const uint8_t *ep, const uint
     int d[4][4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-        const uint32_t f = *reinterpret_cast<const uint32_t *>(fb + (y0 + r) * g.w + x0);
+        const uint32_t f = *reinterpret_cast<const uint32_t *>(fb + (y0 + r) * fstride + x0);
 #pragma unroll
         for (int c = 0; c < 4; c++) d[r][c] = (int)((f >> (8 * c)) & 0xFFu) - p[r][c];
     }
@@ -388,78 +400,97 @@ __device__ __forceinline__ int sub4_sad(int mode, const uint8_t *ep, const uint8
     return s;
 }
 
-// update_candidate_list (md_intra.c:195-210): insertion into the list kept
-// sorted by cost, after equal costs.  Costs are non-negative doubles, so
-// their bit patterns order like the values.
-__device__ void cand_insert(int mode, long long key, int *modes, long long *keys)
+// update_candidate_list (md_intra.c:195-210): insertion into the 9-entry
+// list kept sorted by cost, after equal costs; a cost not below the last
+// entry is dropped.  Costs are non-negative doubles, so their bit patterns
+// order like the values.  Unrolled over the positions: the list stays in
+// registers.
+struct CandList {
+    long long k[kN];
+    int m[kN];
+};
+__device__ __forceinline__ void cand_insert(CandList &L, int mode, long long key)
 {
-    int i = kN - 1;
-    if (!(key < keys[i])) return;
-    while (i > 0 && key < keys[i - 1]) {
-        modes[i] = modes[i - 1];
-        keys[i] = keys[i - 1];
-        i--;
+#pragma unroll
+    for (int i = kN - 1; i >= 0; i--) {
+        const bool lt_prev = i > 0 && key < L.k[i > 0 ? i - 1 : 0];
+        if (lt_prev) {
+            L.k[i] = L.k[i - 1];
+            L.m[i] = L.m[i - 1];
+        } else if (key < L.k[i]) {
+            L.k[i] = key;
+            L.m[i] = mode;
+        }
     }
-    modes[i] = mode;
-    keys[i] = key;
 }
 
 // The candidate list of rdo_get_pred_intra_luma (all modes) or of the rough
 // three-phase search rdo_get_pred_intra_luma_rmd (md_intra.c:258-380),
 // replayed on the per-mode costs; returns the number of modes for RDO.
-__device__ int candidates(const double *cost, int rough, int dist2, int dist1, int num_for_rdo, const int *mpm,
-                          int *modes, long long *keys)
+// `vis` / `fin` are the reference's visited[] states 1 / 2 as bit masks.
+__device__ __forceinline__ int candidates(const long long *key, int rough, int dist2, int dist1, int num_for_rdo,
+                                          int mpm0, int mpm1, CandList &L)
 {
-    int visited[33];
-    for (int m = 0; m < 33; m++) visited[m] = 0;
+    const long long kMax = __double_as_longlong((double)(1LL << 50));   // MAX_COST (defines.h:299)
+#pragma unroll
     for (int i = 0; i < kN; i++) {
-        modes[i] = 0;
-        keys[i] = __double_as_longlong((double)(1LL << 50));   // MAX_COST (defines.h:299)
+        L.m[i] = 0;
+        L.k[i] = kMax;
     }
-    auto visit = [&](int m) {
-        cand_insert(m, __double_as_longlong(cost[m]), modes, keys);
-        visited[m] = 1;
-    };
     if (!rough) {
-        for (int m = 0; m < 33; m++) visit(m);
+        for (int m = 0; m < 33; m++) cand_insert(L, m, key[m]);
         return num_for_rdo;
     }
+    uint64_t vis = 0, fin = 0;
+    auto visit = [&](int m) {
+        cand_insert(L, m, key[m]);
+        vis |= 1ull << m;
+    };
+    auto seen = [&](int m) { return (vis >> m) & 1ull; };
     for (int m = 0; m < 3; m++) visit(m);
     for (int m = 4; m < 33; m += 4) visit(m);
-    for (int i = 0; i < dist2; i++) {
-        const int m = modes[i];
+#pragma unroll
+    for (int i = 0; i < kN; i++) {
+        if (i >= dist2) break;
+        const int m = L.m[i];
         if (m <= 2) continue;
-        if (m > 3 && !visited[m - 2]) visit(m - 2);
-        if (m < 31 && !visited[m + 2]) visit(m + 2);
+        if (m > 3 && !seen(m - 2)) visit(m - 2);
+        if (m < 31 && !seen(m + 2)) visit(m + 2);
     }
-    for (int i = 0, na = 0; na < dist1 && i < kN; i++) {
-        const int m = modes[i];
+    int na = 0;
+#pragma unroll
+    for (int i = 0; i < kN; i++) {
+        if (na >= dist1) break;
+        const int m = L.m[i];
         if (m <= 2) continue;
-        if (m > 3 && !visited[m - 1]) { visit(m - 1); na++; }
-        if (m < 32 && !visited[m + 1]) { visit(m + 1); na++; }
+        if (m > 3 && !seen(m - 1)) { visit(m - 1); na++; }
+        if (m < 32 && !seen(m + 1)) { visit(m + 1); na++; }
     }
-    if (!visited[mpm[0]]) visit(mpm[0]);
-    if (!visited[mpm[1]]) visit(mpm[1]);
-    if (modes[0] == mpm[0] || modes[0] == mpm[1] || modes[1] == mpm[0] || modes[1] == mpm[1])
+    if (!seen(mpm0)) visit(mpm0);
+    if (!seen(mpm1)) visit(mpm1);
+    if (L.m[0] == mpm0 || L.m[0] == mpm1 || L.m[1] == mpm0 || L.m[1] == mpm1)
         return num_for_rdo < 3 ? num_for_rdo : 3;
-    visited[modes[0]] = 2;
-    visited[modes[1]] = 2;
+    fin |= (1ull << L.m[0]) | (1ull << L.m[1]);
+    auto one = [&](int m) { return ((vis >> m) & 1ull) && !((fin >> m) & 1ull); };   // visited == 1
     int j = 2;
-    for (int i = 2; i < kN && j < num_for_rdo; i++) {
-        const int m = modes[i];
-        if (!visited[m]) continue;
-        if (m <= 2) {
-            modes[j++] = m;
-            visited[m] = 2;
-        } else if (m == 3) {
-            if (visited[4] == 1) { modes[j++] = 3; visited[3] = 2; }
-        } else if (m == 32) {
-            if (visited[31] == 1) { modes[j++] = 32; visited[32] = 2; }
-        } else if (visited[m - 1] == 1 && visited[m + 1] == 1) {
-            modes[j++] = m;
-            visited[m] = 2;
+#pragma unroll
+    for (int i = 2; i < kN; i++) {
+        if (j >= num_for_rdo) break;
+        const int m = L.m[i];
+        if (!seen(m)) continue;
+        bool take;
+        if (m <= 2) take = true;
+        else if (m == 3) take = one(4);
+        else if (m == 32) take = one(31);
+        else take = one(m - 1) && one(m + 1);
+        if (take) {
+#pragma unroll
+            for (int p = 2; p < kN; p++)
+                if (p == j) L.m[p] = m;
+            j++;
+            fin |= 1ull << m;
         }
-        if (visited[0] == 2 && visited[1] == 2 && visited[2] == 2) break;
+        if (((fin & 7ull) == 7ull)) break;
     }
     return num_for_rdo < j ? num_for_rdo : j;
 }
@@ -509,7 +540,10 @@ __global__ void rmd_scatter_kernel(const xavs2gpu_intra_block_t *__restrict__ bl
 }
 
 // 3. the tiles, persistent; classes with the most work per tile first
-__global__ void __launch_bounds__(kTT) rmd_tile_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks,
+#ifndef XG_RMD_MINB
+#define XG_RMD_MINB 3
+#endif
+__global__ void __launch_bounds__(kTT, XG_RMD_MINB) rmd_tile_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks,
                                                         const int *__restrict__ counts, const int *__restrict__ sorted,
                                                         const uint8_t *__restrict__ edges,
                                                         const uint8_t *__restrict__ fenc, int fenc_stride,
@@ -519,6 +553,7 @@ __global__ void __launch_bounds__(kTT) rmd_tile_kernel(const xavs2gpu_intra_bloc
     extern __shared__ __align__(16) uint8_t smem_raw[];
     TileSmem &s = *reinterpret_cast<TileSmem *>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    (void)warp;
     if (tid == 0) {
         int acc = 0;
         for (int c = 0; c < kCls; c++) {
@@ -566,92 +601,128 @@ __global__ void __launch_bounds__(kTT) rmd_tile_kernel(const xavs2gpu_intra_bloc
             s.dc_avail[tid] = b.dc_avail;
             s.mpm[tid][0] = b.mpm[0];
             s.mpm[tid][1] = b.mpm[1];
-            s.nrdo[tid] = b.num_for_rdo;
         }
+        if (tid == 0) s.next_mode = 0;
         __syncthreads();
-        // stage the edge windows and the source blocks
+        // stage the edge windows and the source blocks (one padding word
+        // after each block keeps the lanes' rows in distinct banks)
         const int ew = g.lo + g.hi + 1;
         for (int e = tid; e < nb * ew; e += kTT) {
             const int b = e / ew, r = e - b * ew;
             s.edge[b * g.R + r] = edges[s.eoff[b] - g.lo + r];
         }
-        const int area = g.w * g.h;
+        const int area = g.w * g.h, fpitch = area + 4;
         const int lw = ilog2d(g.w);
         for (int e = tid; e < nb * area; e += kTT) {
             const int b = e / area, r = e - b * area, y = r >> lw, x = r & (g.w - 1);
-            s.fenc[e] = fenc[s.foff[b] + (int64_t)y * fenc_stride + x];
+            s.fenc[b * fpitch + r] = fenc[s.foff[b] + (int64_t)y * fenc_stride + x];
         }
         __syncthreads();
-        // DC / plane / bilinear constants, a warp per block
-        for (int b = warp; b < nb; b += kTW) {
-            const uint8_t *ep = s.edge + b * g.R + g.lo;
-            const ModeConst k0 = mode_const(0, ep, s.dc_avail[b], g.w, g.h, lane);
-            const ModeConst k1 = mode_const(1, ep, 0, g.w, g.h, lane);
-            const ModeConst k2 = mode_const(2, ep, 0, g.w, g.h, lane);
-            if (lane == 0) {
-                s.kc[b][0] = k0.dc;
-                s.kc[b][1] = k1.pa;
-                s.kc[b][2] = k1.pb;
-                s.kc[b][3] = k1.pc;
-                s.kc[b][4] = k2.bt;
-            }
-        }
-        __syncthreads();
-        // every mode: a warp per mode, a lane per SATD unit
+        // modes, taken by the warps in c_mode_order; a lane per SATD unit
         {
             const int b = lane / g.lanes, u0 = lane - b * g.lanes;
             const bool live = b < nb;
             const int bb = live ? b : 0;
             const uint8_t *ep = s.edge + bb * g.R + g.lo;
-            const uint8_t *fb = s.fenc + bb * area;
-            const int *kc = s.kc[bb];
-            for (int mode = warp; mode < 33; mode += kTW) {
+            const uint8_t *fb = s.fenc + bb * fpitch;
+            const int lx = ilog2d(g.w), ly = ilog2d(g.h);
+            int mi = 0;
+            if (lane == 0) mi = atomicAdd(&s.next_mode, 1);
+            mi = __shfl_sync(0xffffffffu, mi, 0);
+            while (mi < 33) {
+                const int mode = c_mode_order[mi];
+                LaneConst kc{0, 0, 0, 0, 0};
+                if (mode == 0) {                       // DC (intra.c:153-190)
+                    int sl = 0, sa = 0;
+                    for (int i = u0; i < g.h; i += g.lanes) sl += ep[-1 - i];
+                    for (int i = u0; i < g.w; i += g.lanes) sa += ep[1 + i];
+                    for (int o = g.lanes >> 1; o > 0; o >>= 1) {
+                        sl += __shfl_xor_sync(0xffffffffu, sl, o);
+                        sa += __shfl_xor_sync(0xffffffffu, sa, o);
+                    }
+                    const int top = s.dc_avail[bb] >> 8, left = s.dc_avail[bb] & 0xFF;
+                    if (top && left) kc.dc = ((sl + sa + ((g.w + g.h) >> 1)) * (512 / (g.w + g.h))) >> 9;
+                    else if (left) kc.dc = (sl + (g.h >> 1)) >> ly;
+                    else if (top) kc.dc = (sa + (g.w >> 1)) >> lx;
+                    else kc.dc = 128;
+                } else if (mode == 1) {                // plane (intra.c:192-236)
+                    const int w2 = g.w >> 1, h2 = g.h >> 1;
+                    int H = 0, V = 0;
+                    for (int i = u0 + 1; i <= w2; i += g.lanes) H += i * (ep[w2 + i] - ep[w2 - i]);
+                    for (int i = u0 + 1; i <= h2; i += g.lanes) V += i * (ep[-h2 - i] - ep[-h2 + i]);
+                    for (int o = g.lanes >> 1; o > 0; o >>= 1) {
+                        H += __shfl_xor_sync(0xffffffffu, H, o);
+                        V += __shfl_xor_sync(0xffffffffu, V, o);
+                    }
+                    kc.pb = ((H << 5) * plane_mult(lx) + (1 << (plane_shift(lx) - 1))) >> plane_shift(lx);
+                    kc.pc = ((V << 5) * plane_mult(ly) + (1 << (plane_shift(ly) - 1))) >> plane_shift(ly);
+                    kc.pa = ((ep[-g.h] + ep[g.w]) << 4) + 16 - kc.pb * (w2 - 1) - kc.pc * (h2 - 1);
+                } else if (mode == 2) {                // bilinear (intra.c:238-293)
+                    const int a = ep[g.w], bl = ep[-g.h], sh = min(lx, ly);
+                    const int cc = g.w == g.h ? (a + bl + 1) >> 1
+                                              : (((a << lx) + (bl << ly)) * 13 + (1 << (sh + 5))) >> (sh + 6);
+                    kc.bt = 2 * cc - a - bl;
+                }
                 const bool n5 = mode == 5 && ((g.w == 4 && g.h == 16) || (g.w == 8 && g.h == 32));
                 const bool n31 = mode == 31 && ((g.w == 16 && g.h == 4) || (g.w == 32 && g.h == 8));
                 int acc = 0;
                 if (live) {
                     for (int it = 0; it < g.iters; it++) {
-                        const int u = u0 + it * g.lanes, uy = (u / g.nux) * 4, ux = (u - (u / g.nux) * g.nux) * g.uw;
+                        const int u = u0 + it * g.lanes, uq = u / g.nux;
+                        const int uy = uq * 4, ux = (u - uq * g.nux) * g.uw;
+                        int hs = 0;
                         if (prm.use_hadamard) {
-                            int hs = sub4_hsum(mode, ep, fb, g, ux, uy, kc, n5, n31);
-                            if (g.uw == 8) hs += sub4_hsum(mode, ep, fb, g, ux + 4, uy, kc, n5, n31);
+#pragma unroll 1
+                            for (int x0 = ux; x0 < ux + g.uw; x0 += 4)
+                                hs += sub4_hsum(mode, ep, fb, g.w, g, x0, uy, kc, n5, n31);
                             acc += hs >> 1;
                         } else {
                             ModeConst k{};
-                            k.dc = kc[0]; k.pa = kc[1]; k.pb = kc[2]; k.pc = kc[3]; k.bt = kc[4];
-                            k.ba = ep[g.w]; k.bb = ep[-g.h]; k.lx = ilog2d(g.w); k.ly = ilog2d(g.h);
-                            acc += sub4_sad(mode, ep, fb, g, ux, uy, k);
-                            if (g.uw == 8) acc += sub4_sad(mode, ep, fb, g, ux + 4, uy, k);
+                            k.dc = kc.dc; k.pa = kc.pa; k.pb = kc.pb; k.pc = kc.pc; k.bt = kc.bt;
+                            k.ba = ep[g.w]; k.bb = ep[-g.h]; k.lx = lx; k.ly = ly;
+                            for (int r = 0; r < 4; r++)
+                                for (int x = ux; x < ux + g.uw; x++)
+                                    acc += iabs_d((int)fb[(uy + r) * g.w + x] - pred_sample(mode, ep, x, uy + r, g.w, g.h, k));
                         }
                     }
                 }
                 for (int o = g.lanes >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                 if (live && u0 == 0) s.satd[b][mode] = acc;
+                if (lane == 0) mi = atomicAdd(&s.next_mode, 1);
+                mi = __shfl_sync(0xffffffffu, mi, 0);
             }
         }
         __syncthreads();
-        // costs (rdcost_t, md_intra.c:216-226) and the candidate lists
+        // costs: lambda * mode bits + distortion as rdcost_t (md_intra.c:216-226)
         for (int e = tid; e < nb * 33; e += kTT) {
             const int b = e / 33, m = e - b * 33;
             const int bits = (s.mpm[b][0] == m || s.mpm[b][1] == m) ? 2 : 6;
-            const double cst = __dadd_rn(__dmul_rn(prm.lambda, (double)bits), (double)s.satd[b][m]);
-            s.cost[b][m] = cst;
-            out[s.idx[b]].cost[m] = cst;
+            out[s.idx[b]].cost[m] = __dadd_rn(__dmul_rn(prm.lambda, (double)bits), (double)s.satd[b][m]);
         }
         __syncthreads();
-        if (tid < nb) {
-            int modes[kN];
-            long long keys[kN];
-            const int nr = candidates(s.cost[tid], prm.rough, prm.dist2, prm.dist1, s.nrdo[tid], s.mpm[tid], modes,
-                                      keys);
-            xavs2gpu_intra_result_t &r = out[s.idx[tid]];
-            r.num_for_rdo = nr;
-            for (int i = 0; i < kN; i++) {
-                r.cand_mode[i] = modes[i];
-                r.cand_cost[i] = __longlong_as_double(keys[i]);
-            }
-        }
-        __syncthreads();
+    }
+}
+
+// 4. the candidate lists, a thread per block
+__global__ void __launch_bounds__(128) rmd_cand_kernel(const xavs2gpu_intra_block_t *__restrict__ blocks, int n,
+                                                        xavs2gpu_intra_params_t prm,
+                                                        xavs2gpu_intra_result_t *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const xavs2gpu_intra_block_t b = blocks[i];
+    if (block_class(b) < 0) return;
+    xavs2gpu_intra_result_t &r = out[i];
+    long long key[33];
+#pragma unroll
+    for (int m = 0; m < 33; m++) key[m] = __double_as_longlong(r.cost[m]);
+    CandList L;
+    const int nr = candidates(key, prm.rough, prm.dist2, prm.dist1, b.num_for_rdo, b.mpm[0], b.mpm[1], L);
+    r.num_for_rdo = nr;
+#pragma unroll
+    for (int k = 0; k < kN; k++) {
+        r.cand_mode[k] = L.m[k];
+        r.cand_cost[k] = __longlong_as_double(L.k[k]);
     }
 }
 
@@ -726,7 +797,7 @@ extern "C" int xavs2gpu_intra_rmd_batch(const xavs2gpu_intra_block_t *blocks, in
                                         const uint8_t *fenc, int fenc_stride, const xavs2gpu_intra_params_t *prm,
                                         xavs2gpu_intra_result_t *out, void *stream_)
 {
-    if (n < 0 || !prm || prm->dist1 < 0 || prm->dist2 < 0) {
+    if (n < 0 || !prm || prm->dist1 < 0 || prm->dist2 < 0 || prm->dist2 > 9) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_intra_rmd_batch", "bad count or parameters");
         return XAVS2GPU_ERR_ARG;
     }
@@ -766,7 +837,8 @@ extern "C" int xavs2gpu_intra_rmd_batch(const xavs2gpu_intra_block_t *blocks, in
     if (grid > n) grid = n;
     intra::rmd_tile_kernel<<<(int)grid, intra::kTT, smem, stream>>>(blocks, counts, sorted, edges, fenc, fenc_stride,
                                                                      *prm, out);
-    count_launch(3);
+    intra::rmd_cand_kernel<<<(n + 127) / 128, 128, 0, stream>>>(blocks, n, *prm, out);
+    count_launch(4);
     XG_CUDA(cudaFreeAsync(scratch, stream));
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
