@@ -754,6 +754,173 @@ def run_intra(args):
     print(json.dumps(line))
 
 
+# ---- in-loop filters: 4K 4:2:0 deblocking + SAO -----------------------------------
+LF_METRIC = "bit-exact 3840x2160 4:2:0 pictures/s (deblocking + SAO, per-8x8 edge parameters, LCU 64)"
+
+
+def lf_workload(rank, width, height):
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(71 + rank)
+    y, u, v, scus = synth.deblock_picture(rng, width, height)
+    lcus = synth.sao_params(rng, width, height, 6)
+    return y, u, v, scus, lcus
+
+
+def cpu_lf(y, u, v, scus, lcus, width, height):
+    """The oracle's picture deblocking (reference LCU order), the copy and the
+    SAO of one picture on one core; returns (seconds, y, u, v)."""
+    import oracle
+    olib = oracle.lib()
+    ey, eu, ev = y.copy(), u.copy(), v.copy()
+    t0 = time.perf_counter()
+    olib.xo_deblock_picture(oracle.ptr(ey), width, oracle.ptr(eu), oracle.ptr(ev), width // 2, width, height,
+                            oracle.ptr(scus), 6, 1)
+    src = [ey.copy(), eu.copy(), ev.copy()]
+    dptr = (ctypes.c_void_p * 3)(*[oracle.ptr(p).value for p in (ey, eu, ev)])
+    sptr = (ctypes.c_void_p * 3)(*[oracle.ptr(p).value for p in src])
+    olib.xo_sao_picture(dptr, sptr, width, width // 2, width, height, 6, oracle.ptr(lcus))
+    return time.perf_counter() - t0, ey, eu, ev
+
+
+def run_loopfilter(args):
+    import torch
+    import xavs2_gb300 as xg
+
+    rank, world, local = dist_env()
+    W, H = args.chain_width, args.chain_height
+    y, u, v, scus, lcus = lf_workload(rank, W, H)
+    pic_bytes = y.nbytes + u.nbytes + v.nbytes
+    cfg = {"workload": "loopfilter_2160p", "width": W, "height": H, "chroma": "4:2:0", "lcu": 64,
+           "edges": "per 8x8 block: type none/luma/both (0.2/0.2/0.6), half-edge flags 0.9, alpha 4..64, beta 1..27",
+           "sao": "per LCU and component: off 10 %, else EO_0/EO_90/EO_135/EO_45/BO uniform",
+           "content": "blurred noise plus a random offset per 8x8 block (blocking artefacts)",
+           "l2": "flushed between steps (512 MB write)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cpu_lf(y, u, v, scus, lcus, W, H)
+        tt = 0.0
+        for i in range(args.steps):
+            dt, *_ = cpu_lf(y, u, v, scus, lcus, W, H)
+            tt += dt
+        value = args.steps / tt
+        print(json.dumps({"impl": "reference", "metric": LF_METRIC, "value": value, "unit": "pictures/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+                          "cpu_baseline": {"value": value, "unit": "pictures/s", "cores": 1, "kind": "port",
+                                           "sample": "whole pictures, oracle C (one thread)"},
+                          "e2e": {"value": value, "unit": "pictures/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    dev = torch.device("cuda", local)
+    h_pic = [torch.from_numpy(p).pin_memory() for p in (y, u, v)]
+    h_scus = torch.from_numpy(scus.view(np.uint8).copy()).pin_memory()
+    h_lcus = torch.from_numpy(lcus.view(np.uint8).copy()).pin_memory()
+    pristine = [t.to(dev) for t in h_pic]
+    work = [t.clone() for t in pristine]
+    out = [torch.empty_like(t) for t in pristine]
+    d_scus, d_lcus = h_scus.to(dev), h_lcus.to(dev)
+    h_out = [torch.empty_like(t).pin_memory() for t in h_pic]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(dev)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def step(s):
+        # deblock in place, then SAO into a second picture written whole
+        # (the reference copies the deblocked picture and filters into it)
+        rc = lib.xavs2gpu_deblock_picture(P(work[0]), W, P(work[1]), P(work[2]), W // 2, W, H, 6, P(d_scus),
+                                          ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0
+        rc = lib.xavs2gpu_sao_picture(P(out[0]), P(out[1]), P(out[2]), P(work[0]), P(work[1]), P(work[2]), W,
+                                      W // 2, W, H, 6, P(d_lcus), 1, ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0
+
+    def restore():
+        for k in range(3):
+            work[k].copy_(pristine[k], non_blocking=True)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            restore()
+            step(stream)
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    clk.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            restore()
+            flush.zero_()
+            starts[i].record(stream)
+            step(stream)
+            ends[i].record(stream)
+    barrier()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = reduce_max(float(sum(step_ms)), dev)
+    value = world * args.steps / (total_ms / 1e3)
+    kernel_ms = float(np.median(step_ms))
+    # end to end: host picture and edge / SAO parameters in, filtered picture out
+    barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            for k in range(3):
+                work[k].copy_(h_pic[k], non_blocking=True)
+            d_scus.copy_(h_scus, non_blocking=True)
+            d_lcus.copy_(h_lcus, non_blocking=True)
+            step(stream)
+            for k in range(3):
+                h_out[k].copy_(out[k], non_blocking=True)
+        stream.synchronize()
+    barrier()
+    e2e_s = reduce_max(time.perf_counter() - t0, dev)
+    e2e = world * args.steps / e2e_s
+    if rank != 0:
+        return
+    cpu_s, ey, eu, ev = cpu_lf(y, u, v, scus, lcus, W, H)
+    exact = all(np.array_equal(h_out[k].numpy(), e) for k, e in enumerate((ey, eu, ev)))
+    peaks, peak_src = measured_peaks()
+    # algorithmic bytes: each deblocking pass and the SAO read and write the
+    # picture once, plus the per-8x8 and per-LCU parameters
+    algo = 6 * pic_bytes + h_scus.numel() + h_lcus.numel()
+    achieved = algo / (kernel_ms / 1e3) / 1e9
+    line = {
+        "metric": LF_METRIC, "value": value, "unit": "pictures/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+        "e2e": {"value": e2e, "unit": "pictures/s",
+                "h2d_bytes_per_step": int(pic_bytes + h_scus.numel() + h_lcus.numel()),
+                "d2h_bytes_per_step": int(pic_bytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "deblock_ver + deblock_hor + sao_picture",
+                     "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None, "peak_source": peak_src,
+                     "algorithmic_bytes_per_step": int(algo), "kernel_ms": kernel_ms},
+        "sample_bit_exact": bool(exact),
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "pictures/s", "cores": 1, "kind": "port",
+                         "sample": "one whole picture, oracle C (reference LCU order), one thread"},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 # ---- serving: 64 concurrent streams, continuous batching --------------------
 SERVE_METRIC = "served p99 frame latency (64 streams 360p..2160p, 30 fps Poisson arrivals, continuous batching)"
 SERVE_RES = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
@@ -1004,9 +1171,9 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
-    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra"], default="me",
+    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter"], default="me",
                     help="me: batched motion search (default); tq: batched transform+quant; chain: 4K full-picture "
-                         "chain; serve: 64-stream serving; intra: rough intra mode decision")
+                         "chain; serve: 64-stream serving; intra: rough intra mode decision; loopfilter: 4K deblocking + SAO")
     ap.add_argument("--chain-width", type=int, default=3840)
     ap.add_argument("--chain-height", type=int, default=2160)
     ap.add_argument("--tq-blocks", type=int, default=1000000)
@@ -1023,6 +1190,8 @@ def main():
         run_tq(args)
     elif args.workload == "intra":
         run_intra(args)
+    elif args.workload == "loopfilter":
+        run_loopfilter(args)
     elif args.workload == "chain":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "metric": CHAIN_METRIC,

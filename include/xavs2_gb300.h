@@ -320,6 +320,86 @@ XAVS2GPU_API int xavs2gpu_intra_rmd_batch(const xavs2gpu_intra_block_t *blocks, 
                                           const uint8_t *fenc, int fenc_stride, const xavs2gpu_intra_params_t *prm,
                                           xavs2gpu_intra_result_t *out, void *stream);
 
+/* ---- in-loop filters (primitives.h:202-208; filter_deblock.c, filter_sao.c)
+ * Deblocking of one edge: src is the first sample on the Q side (right of a
+ * vertical edge, below a horizontal one); 8 lines for luma, 4 per chroma
+ * plane; flt_flag[0] / [1] enable the first / second half of the lines.
+ * Members in the layout of intrinsic_func_t.deblock_luma[2] /
+ * deblock_chroma[2] ([0] vertical edge, [1] horizontal edge). */
+typedef struct xavs2gpu_deblock_funcs {
+    void (*deblock_luma[2])(uint8_t *src, int stride, int alpha, int beta, uint8_t *flt_flag);
+    void (*deblock_chroma[2])(uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta, uint8_t *flt_flag);
+} xavs2gpu_deblock_funcs_t;
+XAVS2GPU_API void xavs2gpu_deblock_luma_ver(uint8_t *src, int stride, int alpha, int beta, uint8_t *flt_flag);
+XAVS2GPU_API void xavs2gpu_deblock_luma_hor(uint8_t *src, int stride, int alpha, int beta, uint8_t *flt_flag);
+XAVS2GPU_API void xavs2gpu_deblock_chroma_ver(uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta,
+                                              uint8_t *flt_flag);
+XAVS2GPU_API void xavs2gpu_deblock_chroma_hor(uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta,
+                                              uint8_t *flt_flag);
+XAVS2GPU_API void xavs2gpu_deblock_init(uint32_t cpuid, xavs2gpu_deblock_funcs_t *f);
+
+/* SAOBlkParam (basic_types.h:88-94): type_idc -1 off, 0 EO_0, 1 EO_90,
+ * 2 EO_135, 3 EO_45, 4 BO; offset[] by edge class (EO) or band (BO). */
+typedef struct xavs2gpu_sao_param {
+    int merge_idx, type_idc, start_band, delta_band;
+    int offset[32];
+} xavs2gpu_sao_param_t;
+/* sao_flt_t (primitives.h:123-125): filters a w x h block of p_src into
+ * p_dst; lcu_avail[8] = top, down, left, right, top-left, top-right,
+ * down-left, down-right; samples outside the filtered range keep p_dst.
+ * One sample around the source block is read (the reference's frames have
+ * a margin). */
+typedef void (*xavs2gpu_sao_flt_t)(uint8_t *p_dst, int i_dst, uint8_t *p_src, int i_src, int i_block_w,
+                                   int i_block_h, int *lcu_avail, xavs2gpu_sao_param_t *sao_param);
+XAVS2GPU_API void xavs2gpu_sao_block(uint8_t *p_dst, int i_dst, uint8_t *p_src, int i_src, int i_block_w,
+                                     int i_block_h, int *lcu_avail, xavs2gpu_sao_param_t *sao_param);
+XAVS2GPU_API void xavs2gpu_sao_init(uint32_t cpuid, xavs2gpu_sao_flt_t *f);
+
+/* Picture-level deblocking (no single counterpart: xavs2_lcu_deblock,
+ * filter_deblock.c:497-546, over every LCU).  Per 8x8 block (raster order,
+ * width/8 per row) and direction (0 its left edge, 1 its top edge): the edge
+ * type (0 none, 1 luma only, 2 luma and chroma; edges on the picture border
+ * are never filtered), the half-edge flags (lf_skip_filter), and alpha /
+ * beta for luma and chroma (tab_deblock_alpha / _beta at the edge's QP,
+ * lf_scu_deblock).  4:2:0, in place, device pointers; width and height
+ * multiples of 8, planes and strides 4-byte aligned, lcu_level 3..6.
+ * Result = the reference's LCU-order result (including, in a picture one
+ * LCU wide, the horizontal edges of the last 8x8 column left unfiltered). */
+typedef struct xavs2gpu_deblock_scu {
+    uint8_t type[2];
+    uint8_t flag[2][2];
+    uint8_t alpha[2], beta[2];
+    uint8_t alpha_c[2], beta_c[2];
+    uint8_t pad_[2];
+} xavs2gpu_deblock_scu_t;
+XAVS2GPU_API int xavs2gpu_deblock_picture(uint8_t *y, int stride, uint8_t *u, uint8_t *v, int stride_c, int width,
+                                          int height, int lcu_level, const xavs2gpu_deblock_scu_t *scus,
+                                          void *stream);
+/* Picture-level SAO (sao_filter_lcu, sao.c:1170-1200, over every LCU): per
+ * LCU (raster order) the type per component (-1 off), the offsets per
+ * component and the availability of the top / down / left / right LCUs
+ * (bits 0..3; diagonals are their conjunctions).  Each LCU's region is the
+ * LCU moved 4 samples up and left inside the picture (sao.c:898-975); src
+ * (the deblocked picture) and dst must not overlap; dst samples outside the
+ * filtered ranges keep their values, or, with XAVS2GPU_SAO_COPY_UNFILTERED
+ * in flags, get src's (dst is then written whole: the encoder's result
+ * without its copy of the picture; this mode requires availabilities
+ * consistent between neighbours -- a side is available exactly when the
+ * neighbour there sees this LCU as available, none on the picture border --
+ * as the encoder derives them).  Without the flag any availabilities are
+ * accepted and overlapping regions resolve as in the reference's LCU loop.
+ * 4:2:0, device pointers, LCU 16..64. */
+#define XAVS2GPU_SAO_COPY_UNFILTERED 1
+typedef struct xavs2gpu_sao_lcu {
+    int8_t type[3];
+    uint8_t avail;
+    int8_t offset[3][32];
+} xavs2gpu_sao_lcu_t;
+XAVS2GPU_API int xavs2gpu_sao_picture(uint8_t *dst_y, uint8_t *dst_u, uint8_t *dst_v, const uint8_t *src_y,
+                                      const uint8_t *src_u, const uint8_t *src_v, int stride, int stride_c,
+                                      int width, int height, int lcu_level, const xavs2gpu_sao_lcu_t *lcus,
+                                      int flags, void *stream);
+
 /* ---- batched transform + quant chain -----------------------------------
  * For every block: dct (or, for a 4x4 block with flag bit 1, the 4x4
  * secondary transform) -> quant -> when any level is non-zero, dequant ->

@@ -110,6 +110,11 @@ _ORACLE_SIGS = {
     "xo_intra_mode_costs": (None, [_P, _P, _I, _I, _I, _I, _P, ctypes.c_double, _I, _P]),
     "xo_intra_candidates": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "xo_intra_rmd_batch": (None, [_P, _I, _P, _P, _I, ctypes.c_double, _I, _I, _I, _I, _P, _I]),
+    "xo_deblock_luma": (None, [_I, _P, _I, _I, _I, _P]),
+    "xo_deblock_chroma": (None, [_I, _P, _P, _I, _I, _I, _P]),
+    "xo_deblock_picture": (None, [_P, _I, _P, _P, _I, _I, _I, _P, _I, _I]),
+    "xo_sao_block": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
+    "xo_sao_picture": (None, [_P, _P, _I, _I, _I, _I, _I, _P]),
 }
 _REF_SIGS = {
     "xr_cmp": (_I, [_I, _I, _P, _S, _P, _S]),
@@ -134,6 +139,9 @@ _REF_SIGS = {
     "xr_me_search": (_I, [_P, _P, _P, _S, _P, _I, _P]),
     "xr_intra_pred": (None, [_I, _P, _P, _I, _I, _I, _I]),
     "xr_intra_fill_edge": (None, [_I, _P, _I, _P, _P, ctypes.c_uint32, _I, _I]),
+    "xr_deblock_luma": (None, [_I, _P, _I, _I, _I, _P]),
+    "xr_deblock_chroma": (None, [_I, _P, _P, _I, _I, _I, _P]),
+    "xr_sao_block": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
 }
 
 

@@ -12,6 +12,7 @@
 #include "primitives.h"
 #include "mc.h"
 #include "me.h"
+#include "filter.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -27,6 +28,10 @@ void xavs2_log(void *p, int i_log_level, const char *psz_fmt, ...)
     (void)p; (void)i_log_level; (void)psz_fmt;
 }
 void *xavs2_malloc(size_t i_size) { return calloc(1, i_size); }
+/* Placeholder for the chroma QP table (avs2tab.h:68) that the picture-level
+ * deblocking loop (xavs2_lcu_deblock, never called here) references; the
+ * per-edge filters driven below do not read it. */
+const uint8_t tab_qp_scale_chroma[64] = {0};
 void xavs2_free(void *ptr) { free(ptr); }
 
 static int g_inited = 0;
@@ -43,6 +48,8 @@ void xr_init(void)
     xavs2_quant_init(0, &g_funcs.dctf);
     xavs2_mad_init(0, g_funcs.pixf.madf);
     xavs2_intra_pred_init(0, &g_funcs);
+    xavs2_deblock_init(0, &g_funcs);
+    xavs2_sao_init(0, &g_funcs);
     g_inited = 1;
 }
 
@@ -378,4 +385,24 @@ void xr_intra_fill_edge(int xy, const pel_t *pTL, int i_TL, const pel_t *pLcuEP,
 {
     xr_init();
     g_funcs.fill_edge_f[xy](pTL, i_TL, pLcuEP, EP, avail, bsx, bsy);
+}
+
+/* ---- in-loop filters (filter_deblock.c, filter_sao.c) -------------------- */
+/* deblock_luma[dir] / deblock_chroma[dir] (filter_deblock.c:400-431): one
+ * 8-sample edge (4 per chroma plane), dir 0 = vertical edge, 1 = horizontal. */
+void xr_deblock_luma(int dir, pel_t *src, int stride, int alpha, int beta, uint8_t *flt_flag)
+{
+    xr_init();
+    g_funcs.deblock_luma[dir](src, stride, alpha, beta, flt_flag);
+}
+void xr_deblock_chroma(int dir, pel_t *src_u, pel_t *src_v, int stride, int alpha, int beta, uint8_t *flt_flag)
+{
+    xr_init();
+    g_funcs.deblock_chroma[dir](src_u, src_v, stride, alpha, beta, flt_flag);
+}
+/* sao_block (filter_sao.c:50-226) */
+void xr_sao_block(pel_t *p_dst, int i_dst, pel_t *p_src, int i_src, int w, int h, int *avail, SAOBlkParam *prm)
+{
+    xr_init();
+    g_funcs.sao_block(p_dst, i_dst, p_src, i_src, w, h, avail, prm);
 }

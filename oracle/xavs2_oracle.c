@@ -1406,3 +1406,237 @@ void xo_intra_rmd_batch(const xo_intra_block_t *blocks, int n, const uint8_t *ed
     for (i = 0; i < n; i++)
         rmd_one(&blocks[i], edges, fenc, fenc_stride, lambda, hadamard, rough, dist2, dist1, &out[i]);
 }
+
+/* ------------------------------------------------------------------------
+ * in-loop filters (filter_deblock.c, filter_sao.c, encoder/sao.c)
+ * ---------------------------------------------------------------------- */
+/* One line across an edge (lf_edge_core, filter_deblock.c:254-360): s points
+ * at the first sample of the Q side, `a` steps across the edge.  The filter
+ * strength fs comes from the flatness of both sides; the formulas are the
+ * reference's written as weighted sums. */
+static void deblock_line(uint8_t *s, int a, int alpha, int beta, int chroma)
+{
+    const int L0 = s[-a], L1 = s[-2 * a], L2 = s[-3 * a];
+    const int R0 = s[0], R1 = s[a], R2 = s[2 * a];
+    const int d = iabs(R0 - L0);
+    int fl, fr, fs;
+    if (d >= alpha || d <= 1) return;
+    fl = (iabs(L1 - L0) < beta ? 2 : 0) + (iabs(L2 - L0) < beta ? 1 : 0);
+    fr = (iabs(R0 - R1) < beta ? 2 : 0) + (iabs(R0 - R2) < beta ? 1 : 0);
+    switch (fl + fr) {
+    case 6: fs = (R1 == R0 && L0 == L1) ? 4 : 3; break;
+    case 5: fs = (R1 == R0 && L0 == L1) ? 3 : 2; break;
+    case 4: fs = fl == 2 ? 2 : 1; break;
+    case 3: fs = iabs(L1 - R1) < beta ? 1 : 0; break;
+    default: fs = 0; break;
+    }
+    if (chroma && fs > 0) fs--;
+    if (fs == 4) {
+        s[-a] = (uint8_t)((9 * L0 + 9 * L2 + 8 * R0 + 6 * R2 + 16) >> 5);
+        s[-2 * a] = (uint8_t)((7 * L0 + 6 * L2 + 3 * R0 + 8) >> 4);
+        s[-3 * a] = (uint8_t)((4 * L0 + 3 * L2 + R0 + 4) >> 3);
+        s[0] = (uint8_t)((9 * R0 + 9 * R2 + 8 * L0 + 6 * L2 + 16) >> 5);
+        s[a] = (uint8_t)((7 * R0 + 6 * R2 + 3 * L0 + 8) >> 4);
+        s[2 * a] = (uint8_t)((4 * R0 + 3 * R2 + L0 + 4) >> 3);
+    } else if (fs == 3) {
+        s[-a] = (uint8_t)((L2 + 4 * L1 + 6 * L0 + 4 * R0 + R1 + 8) >> 4);
+        s[0] = (uint8_t)((L1 + 4 * L0 + 6 * R0 + 4 * R1 + R2 + 8) >> 4);
+        s[-2 * a] = (uint8_t)((3 * L2 + 8 * L1 + 4 * L0 + R0 + 8) >> 4);
+        s[a] = (uint8_t)((3 * R2 + 8 * R1 + 4 * R0 + L0 + 8) >> 4);
+    } else if (fs == 2) {
+        s[-a] = (uint8_t)((3 * L1 + 10 * L0 + 3 * R0 + 8) >> 4);
+        s[0] = (uint8_t)((3 * L0 + 10 * R0 + 3 * R1 + 8) >> 4);
+    } else if (fs == 1) {
+        s[-a] = (uint8_t)((3 * L0 + R0 + 2) >> 2);
+        s[0] = (uint8_t)((3 * R0 + L0 + 2) >> 2);
+    }
+}
+
+/* n lines of an edge, `along` apart; the first half uses flt_flag[0] */
+static void deblock_edge(uint8_t *src, int n, int along, int across, int alpha, int beta, int chroma,
+                         const uint8_t *flt_flag)
+{
+    int k;
+    for (k = 0; k < n; k++)
+        if (flt_flag[k >= n / 2]) deblock_line(src + k * along, across, alpha, beta, chroma);
+}
+
+void xo_deblock_luma(int dir, uint8_t *src, int stride, int alpha, int beta, const uint8_t *flt_flag)
+{
+    if (dir == 0) deblock_edge(src, 8, stride, 1, alpha, beta, 0, flt_flag);
+    else deblock_edge(src, 8, 1, stride, alpha, beta, 0, flt_flag);
+}
+
+void xo_deblock_chroma(int dir, uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta,
+                       const uint8_t *flt_flag)
+{
+    if (dir == 0) {
+        deblock_edge(src_u, 4, stride, 1, alpha, beta, 1, flt_flag);
+        deblock_edge(src_v, 4, stride, 1, alpha, beta, 1, flt_flag);
+    } else {
+        deblock_edge(src_u, 4, 1, stride, alpha, beta, 1, flt_flag);
+        deblock_edge(src_v, 4, 1, stride, alpha, beta, 1, flt_flag);
+    }
+}
+
+/* the edge of one 8x8 block in one direction (lf_scu_deblock,
+ * filter_deblock.c:434-486); no edge on the picture border */
+static void deblock_scu(uint8_t *y, int stride, uint8_t *u, uint8_t *v, int stride_c, int sx, int sy, int w_scu,
+                        const xo_deblock_scu_t *scus, int dir)
+{
+    const xo_deblock_scu_t *e = &scus[sy * w_scu + sx];
+    if (!e->type[dir] || (dir == 0 && sx == 0) || (dir == 1 && sy == 0)) return;
+    if (!e->flag[dir][0] && !e->flag[dir][1]) return;
+    xo_deblock_luma(dir, y + (sy * 8) * stride + sx * 8, stride, e->alpha[dir], e->beta[dir], e->flag[dir]);
+    if (e->type[dir] == 2 && ((dir == 1 && !(sy & 1)) || (dir == 0 && !(sx & 1)))) {
+        const int o = (sy * 4) * stride_c + sx * 4;
+        xo_deblock_chroma(dir, u + o, v + o, stride_c, e->alpha_c[dir], e->beta_c[dir], e->flag[dir]);
+    }
+}
+
+void xo_deblock_picture(uint8_t *y, int stride, uint8_t *u, uint8_t *v, int stride_c, int width, int height,
+                        const xo_deblock_scu_t *scus, int lcu_level, int lcu_order)
+{
+    const int w_scu = width / 8, h_scu = height / 8;
+    int i, j;
+    if (!lcu_order) {
+        /* a picture one LCU wide: the LCU loop leaves the horizontal edges
+         * of its last 8x8 column for a next LCU that does not exist */
+        const int n_hor = w_scu <= (1 << (lcu_level - 3)) ? w_scu - 1 : w_scu;
+        for (j = 0; j < h_scu; j++)
+            for (i = 0; i < w_scu; i++) deblock_scu(y, stride, u, v, stride_c, i, j, w_scu, scus, 0);
+        for (j = 0; j < h_scu; j++)
+            for (i = 0; i < n_hor; i++) deblock_scu(y, stride, u, v, stride_c, i, j, w_scu, scus, 1);
+        return;
+    } else {
+        /* xavs2_lcu_deblock (filter_deblock.c:497-546) for each LCU in raster
+         * order: its vertical edges, then its horizontal edges one 8x8 column
+         * to the left (the last column waits for the next LCU's vertical
+         * edges, except in the last LCU of a row) */
+        const int lcu_scu = 1 << (lcu_level - 3);
+        int lx, ly;
+        for (ly = 0; ly < h_scu; ly += lcu_scu)
+            for (lx = 0; lx < w_scu; lx += lcu_scu) {
+                const int nh = lcu_scu < w_scu - lx ? lcu_scu : w_scu - lx;
+                const int nv = lcu_scu < h_scu - ly ? lcu_scu : h_scu - ly;
+                int x0 = lx, n = nh;
+                for (j = 0; j < nv; j++)
+                    for (i = 0; i < nh; i++) deblock_scu(y, stride, u, v, stride_c, lx + i, ly + j, w_scu, scus, 0);
+                if (lx == 0) {
+                    n--;
+                } else {
+                    if (lx + nh == w_scu) n++;
+                    x0--;
+                }
+                for (j = 0; j < nv; j++)
+                    for (i = 0; i < n; i++) deblock_scu(y, stride, u, v, stride_c, x0 + i, ly + j, w_scu, scus, 1);
+            }
+    }
+}
+
+static int sign3(int v) { return (v > 0) - (v < 0); }
+
+/* sao_block_c (filter_sao.c:50-226) in closed form: a sample's edge class
+ * is sign(s - n1) + sign(s - n2) + 2 over its two neighbours along the EO
+ * direction, its band (BO) the top 5 bits.  The filtered range of each row
+ * follows the reference's availability rules; samples outside it keep dst.
+ * (When a diagonal neighbour is available but an adjacent side is not --
+ * never the case in the encoder, whose diagonals are conjunctions of the
+ * sides -- the reference reads a line-buffer entry it has not set; this
+ * restatement uses the true neighbour there.) */
+void xo_sao_block(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w, int h, const int *avail,
+                  const xo_sao_param_t *prm)
+{
+    const int T = avail[0], D = avail[1], L = avail[2], R = avail[3];
+    const int TL = avail[4], TR = avail[5], DL = avail[6], DR = avail[7];
+    static const int nb[4][4] = {{-1, 0, 1, 0}, {0, -1, 0, 1}, {-1, -1, 1, 1}, {1, -1, -1, 1}};
+    const int type = prm->type_idc;
+    const int sx = L ? 0 : 1, ex = R ? w : w - 1;
+    int x, y;
+    if (type == 4) {                                           /* BO */
+        for (y = 0; y < h; y++)
+            for (x = 0; x < w; x++) {
+                const int s = src[y * i_src + x];
+                dst[y * i_dst + x] = clip_pel(s + prm->offset[s >> 3]);
+            }
+        return;
+    }
+    if (type < 0 || type > 3) return;
+    for (y = 0; y < h; y++) {
+        int x0 = sx, x1 = ex;
+        if (type == 1) {                                       /* EO_90: rows limited, all columns */
+            if ((y == 0 && !T) || (y == h - 1 && !D)) continue;
+            x0 = 0;
+            x1 = w;
+        } else if (type == 2 && y == 0) {                      /* EO_135 first / last row */
+            x0 = TL ? 0 : 1;
+            x1 = T ? (R ? w : w - 1) : 1;
+        } else if (type == 2 && y == h - 1) {
+            x0 = D ? (L ? 0 : 1) : w - 1;
+            x1 = DR ? w : w - 1;
+        } else if (type == 3 && y == 0) {                      /* EO_45 first / last row */
+            x0 = T ? (L ? 0 : 1) : w - 1;
+            x1 = TR ? w : w - 1;
+        } else if (type == 3 && y == h - 1) {
+            x0 = DL ? 0 : 1;
+            x1 = D ? (R ? w : w - 1) : 1;
+        }
+        for (x = x0; x < x1; x++) {
+            const uint8_t *p = src + y * i_src + x;
+            const int s = p[0];
+            const int c = sign3(s - p[nb[type][1] * i_src + nb[type][0]]) +
+                          sign3(s - p[nb[type][3] * i_src + nb[type][2]]) + 2;
+            dst[y * i_dst + x] = clip_pel(s + prm->offset[c]);
+        }
+    }
+}
+
+/* the filtered region of an LCU (sao_get_neighbor_avail, sao.c:898-975):
+ * comp 0 luma, 1/2 chroma; returns 0 when empty */
+static int sao_region(int lx, int ly, int lcu_level, int width, int height, int avail, int comp, int *px, int *py,
+                      int *pw, int *ph)
+{
+    const int T = avail & 1, D = (avail >> 1) & 1, L = (avail >> 2) & 1, R = (avail >> 3) & 1;
+    const int S = 1 << lcu_level, c = comp > 0;
+    int x = lx * S, y = ly * S;
+    int w = (S < width - x ? S : width - x), h = (S < height - y ? S : height - y);
+    const int W = c ? width >> 1 : width, H = c ? height >> 1 : height;
+    if (c) {
+        x >>= 1; y >>= 1; w >>= 1; h >>= 1;
+    }
+    if (!R) w += 4;
+    if (!D) h += 4;
+    if (L) x -= 4; else w -= 4;
+    if (T) y -= 4; else h -= 4;
+    if (w > W - x) w = W - x;
+    if (h > H - y) h = H - y;
+    *px = x; *py = y; *pw = w; *ph = h;
+    return w > 0 && h > 0;
+}
+
+void xo_sao_picture(uint8_t *const dst[3], const uint8_t *const src[3], int stride, int stride_c, int width,
+                    int height, int lcu_level, const xo_sao_lcu_t *lcus)
+{
+    const int S = 1 << lcu_level;
+    const int wl = (width + S - 1) / S, hl = (height + S - 1) / S;
+    int lx, ly, comp, k;
+    for (ly = 0; ly < hl; ly++)
+        for (lx = 0; lx < wl; lx++) {
+            const xo_sao_lcu_t *p = &lcus[ly * wl + lx];
+            const int a = p->avail;
+            const int av[8] = {a & 1, (a >> 1) & 1, (a >> 2) & 1, (a >> 3) & 1, (a & 1) && ((a >> 2) & 1),
+                               (a & 1) && ((a >> 3) & 1), ((a >> 1) & 1) && ((a >> 2) & 1),
+                               ((a >> 1) & 1) && ((a >> 3) & 1)};
+            for (comp = 0; comp < 3; comp++) {
+                xo_sao_param_t prm;
+                int x, y, w, h;
+                const int st = comp ? stride_c : stride;
+                if (p->type[comp] < 0 || !sao_region(lx, ly, lcu_level, width, height, a, comp, &x, &y, &w, &h))
+                    continue;
+                memset(&prm, 0, sizeof(prm));
+                prm.type_idc = p->type[comp];
+                for (k = 0; k < 32; k++) prm.offset[k] = p->offset[comp][k];
+                xo_sao_block(dst[comp] + y * st + x, st, src[comp] + y * st + x, st, w, h, av, &prm);
+            }
+        }
+}

@@ -201,4 +201,54 @@ void xo_intra_rmd_batch(const xo_intra_block_t *blocks, int n, const uint8_t *ed
                         int fenc_stride, double lambda, int hadamard, int rough, int dist2, int dist1,
                         xo_intra_result_t *out, int threads);
 
+/* ---- in-loop filters (filter_deblock.c, filter_sao.c) ------------------ */
+/* One deblocking edge: dir 0 = vertical edge (lines run down, samples across
+ * are horizontal neighbours), 1 = horizontal edge; 8 lines for luma, 4 per
+ * chroma plane; flt_flag[0] / [1] enable the first / second half. */
+void xo_deblock_luma(int dir, uint8_t *src, int stride, int alpha, int beta, const uint8_t *flt_flag);
+void xo_deblock_chroma(int dir, uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta,
+                       const uint8_t *flt_flag);
+/* Per-8x8-block edge parameters of a picture (the values lf_scu_deblock
+ * derives from the CU data, filter_deblock.c:434-486): per direction the edge
+ * type (0 none, 1 luma only, 2 luma and chroma), the two half-edge filter
+ * flags, and alpha / beta for luma and for chroma. */
+typedef struct xo_deblock_scu {
+    uint8_t type[2];
+    uint8_t flag[2][2];
+    uint8_t alpha[2], beta[2];
+    uint8_t alpha_c[2], beta_c[2];
+    uint8_t pad_[2];
+} xo_deblock_scu_t;
+/* Deblocks a 4:2:0 picture in place (width, height multiples of 8), in the
+ * reference's LCU order (lcu_order = 1, xavs2_lcu_deblock per LCU) or as two
+ * picture-wide passes (all vertical edges, then all horizontal edges; in a
+ * picture one LCU wide the horizontal edges of the last 8x8 column are left
+ * unfiltered, as the LCU loop leaves them). */
+void xo_deblock_picture(uint8_t *y, int stride, uint8_t *u, uint8_t *v, int stride_c, int width, int height,
+                        const xo_deblock_scu_t *scus, int lcu_level, int lcu_order);
+
+/* SAOBlkParam (basic_types.h:88-94) */
+typedef struct xo_sao_param {
+    int merge_idx, type_idc, start_band, delta_band;
+    int offset[32];
+} xo_sao_param_t;
+/* sao_block: dst = clip(src + offset[class]) over the block's filtered
+ * range; avail[8] = top, down, left, right, top-left, top-right, down-left,
+ * down-right (lcu_neighbor_e, filter.h). */
+void xo_sao_block(uint8_t *dst, int i_dst, const uint8_t *src, int i_src, int w, int h, const int *avail,
+                  const xo_sao_param_t *prm);
+/* Per-LCU SAO parameters of a picture: type per component (-1 off, EO_0,
+ * EO_90, EO_135, EO_45, BO), offsets per component, and the availability of
+ * the top / down / left / right LCUs (bits 0..3; the diagonals are their
+ * conjunctions, sao.c:898-929). */
+typedef struct xo_sao_lcu {
+    int8_t type[3];
+    uint8_t avail;
+    int8_t offset[3][32];
+} xo_sao_lcu_t;
+/* SAO of a 4:2:0 picture: every LCU's region (the LCU moved 4 samples up
+ * and left inside the picture, sao.c:898-975) filtered from src into dst. */
+void xo_sao_picture(uint8_t *const dst[3], const uint8_t *const src[3], int stride, int stride_c, int width,
+                    int height, int lcu_level, const xo_sao_lcu_t *lcus);
+
 #endif

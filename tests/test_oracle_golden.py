@@ -117,3 +117,22 @@ def test_intra_prediction(olib, g):
                 dst = mg.intra_prefill(bw, bh)
                 olib.xo_intra_pred(mode, ptr(edge, 256), ptr(dst), bw + 8, avail, bw, bh)
                 assert hashlib.sha256(dst.tobytes()).hexdigest() == g["intra_sha"][e, s, m], (e, bw, bh, m)
+
+
+def test_deblock_lcu_order_equals_two_passes(olib):
+    """The picture deblocked in the reference's LCU order equals all vertical
+    edges then all horizontal edges (edges 8 samples apart, each reading 3
+    and writing at most 3 samples on either side), for LCU sizes 16..64."""
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(93)
+    for (w, h, lcu) in ((128, 96, 6), (136, 72, 5), (64, 48, 4), (200, 120, 6), (64, 48, 6), (56, 40, 6),
+                        (32, 64, 5)):
+        y, u, v, scus = synth.deblock_picture(rng, w, h)
+        outs = []
+        for lcu_order in (1, 0):
+            yy, uu, vv = y.copy(), u.copy(), v.copy()
+            olib.xo_deblock_picture(ptr(yy), w, ptr(uu), ptr(vv), w // 2, w, h, ptr(scus), lcu, lcu_order)
+            outs.append((yy, uu, vv))
+        for a, b in zip(*outs):
+            assert np.array_equal(a, b), (w, h, lcu)
+        assert not np.array_equal(outs[0][0], y)      # something was filtered

@@ -362,3 +362,75 @@ def test_intra_fill_edge_prediction(olib, rlib):
                     olib.xo_intra_pred(mode, ptr(ebuf, 512), ptr(a), bw, 0x101, bw, bh)
                     rlib.xr_intra_pred(mode, ptr(ebuf, 512), ptr(b), bw, 0x101 if mode == 0 else mode, bw, bh)
                     assert np.array_equal(a, b), (bw, bh, avail, xy, mode)
+
+
+ALPHA_TAB_SAMPLES = [(2, 1), (6, 2), (13, 3), (24, 5), (36, 8), (50, 15), (64, 27), (0, 0), (255, 255)]
+
+
+def _deblock_area(rng, n):
+    """n 16x16 areas (a vertical and a horizontal edge through the centre)
+    with flat or ramped sides, a step of random size and small noise, so that
+    every filter strength occurs."""
+    out = []
+    for i in range(n):
+        base = int(rng.integers(20, 230))
+        a = np.full((16, 16), base, np.int32)
+        kind = i % 4
+        if kind == 1:
+            a += np.arange(16)[None, :] * int(rng.integers(-3, 4))
+        elif kind == 2:
+            a += rng.integers(-2, 3, (16, 16))
+        elif kind == 3:
+            a += rng.integers(-12, 13, (16, 16))
+        step = int(rng.integers(-30, 31))
+        a[:, 8:] += step
+        a[8:, :] += int(rng.integers(-30, 31))
+        if i % 7 == 0:
+            a[:, 7] = a[:, 6]          # L0 == L1 / R0 == R1 patterns
+            a[:, 8] = a[:, 9]
+        out.append(np.clip(a, 0, 255).astype(np.uint8))
+    return out
+
+
+def test_deblock_edges(olib, rlib):
+    rng = np.random.default_rng(91)
+    for area in _deblock_area(rng, 160):
+        for alpha, beta in ALPHA_TAB_SAMPLES:
+            for flags in ((1, 1), (1, 0), (0, 1)):
+                fl = np.array(flags, np.uint8)
+                for d in (0, 1):
+                    a, b = area.copy(), area.copy()
+                    olib.xo_deblock_luma(d, ptr(a, 4 * 16 + 8 if d == 0 else 8 * 16 + 4), 16, alpha, beta, ptr(fl))
+                    rlib.xr_deblock_luma(d, ptr(b, 4 * 16 + 8 if d == 0 else 8 * 16 + 4), 16, alpha, beta, ptr(fl))
+                    assert np.array_equal(a, b), (d, alpha, beta, flags)
+                    u1, v1 = area.copy(), area[::-1].copy()
+                    u2, v2 = u1.copy(), v1.copy()
+                    o = 4 * 16 + 8 if d == 0 else 8 * 16 + 4
+                    olib.xo_deblock_chroma(d, ptr(u1, o), ptr(v1, o), 16, alpha, beta, ptr(fl))
+                    rlib.xr_deblock_chroma(d, ptr(u2, o), ptr(v2, o), 16, alpha, beta, ptr(fl))
+                    assert np.array_equal(u1, u2) and np.array_equal(v1, v2), (d, alpha, beta, flags)
+
+
+def test_sao_block(olib, rlib):
+    """Every SAO type over every combination of the four side
+    availabilities (diagonals are the conjunctions, as the encoder derives
+    them), several block sizes, random offsets."""
+    rng = np.random.default_rng(92)
+    for trial in range(6):
+        img = rng.integers(0, 256, (80, 96), dtype=np.uint8)
+        if trial % 2:
+            img = np.clip(128 + np.cumsum(rng.integers(-3, 4, (80, 96)), 1), 0, 255).astype(np.uint8)
+        for w, h in ((64, 64), (68, 60), (60, 68), (8, 8), (36, 4), (4, 36)):
+            for sides in range(16):
+                T, D, L, R = sides & 1, (sides >> 1) & 1, (sides >> 2) & 1, (sides >> 3) & 1
+                avail = np.array([T, D, L, R, T & L, T & R, D & L, D & R], np.int32)
+                for typ in range(5):
+                    prm = np.zeros(36, np.int32)
+                    prm[1] = typ
+                    prm[4:] = rng.integers(-7, 8, 32)
+                    dst1 = rng.integers(0, 256, (80, 96), dtype=np.uint8)
+                    dst2 = dst1.copy()
+                    o = 6 * 96 + 8
+                    olib.xo_sao_block(ptr(dst1, o), 96, ptr(img, o), 96, w, h, ptr(avail), ptr(prm))
+                    rlib.xr_sao_block(ptr(dst2, o), 96, ptr(img, o), 96, w, h, ptr(avail), ptr(prm))
+                    assert np.array_equal(dst1, dst2), (trial, w, h, sides, typ)

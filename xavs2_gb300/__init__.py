@@ -147,6 +147,15 @@ _SIGS = {
     "xavs2gpu_intra_pred_ang": (None, [_P, _P, _I, _I, _I, _I]),
     "xavs2gpu_intra_pred_init": (None, [ctypes.c_uint32, _P]),
     "xavs2gpu_intra_rmd_batch": (_I, [_P, _I, _P, _P, _I, _P, _P, _P]),
+    "xavs2gpu_deblock_luma_ver": (None, [_P, _I, _I, _I, _P]),
+    "xavs2gpu_deblock_luma_hor": (None, [_P, _I, _I, _I, _P]),
+    "xavs2gpu_deblock_chroma_ver": (None, [_P, _P, _I, _I, _I, _P]),
+    "xavs2gpu_deblock_chroma_hor": (None, [_P, _P, _I, _I, _I, _P]),
+    "xavs2gpu_deblock_init": (None, [ctypes.c_uint32, _P]),
+    "xavs2gpu_sao_block": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
+    "xavs2gpu_sao_init": (None, [ctypes.c_uint32, _P]),
+    "xavs2gpu_deblock_picture": (_I, [_P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
+    "xavs2gpu_sao_picture": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _I, _P]),
 }
 
 _PIXEL_CMP = ["sad", "satd", "sa8d", "ssd"]
@@ -424,6 +433,12 @@ INTRA_BLOCK_DTYPE = np.dtype([("edge_offset", "<i8"), ("fenc_offset", "<i8"), ("
                               ("dc_avail", "<i2"), ("mpm", "i1", (2,)), ("num_for_rdo", "<i4"), ("pad_", "<i4")])
 INTRA_RESULT_DTYPE = np.dtype([("cost", "<f8", (33,)), ("cand_cost", "<f8", (9,)), ("cand_mode", "<i4", (9,)),
                                ("num_for_rdo", "<i4")])
+
+
+DEBLOCK_SCU_DTYPE = np.dtype([("type", "u1", (2,)), ("flag", "u1", (2, 2)), ("alpha", "u1", (2,)),
+                              ("beta", "u1", (2,)), ("alpha_c", "u1", (2,)), ("beta_c", "u1", (2,)),
+                              ("pad_", "u1", (2,))])
+SAO_LCU_DTYPE = np.dtype([("type", "i1", (3,)), ("avail", "u1"), ("offset", "i1", (3, 32))])
 
 
 class IntraParams(ctypes.Structure):

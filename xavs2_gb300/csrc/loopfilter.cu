@@ -1,0 +1,605 @@
+// loopfilter.cu -- AVS2 in-loop filters for sm_103a: deblocking
+// (filter_deblock.c) and sample adaptive offset (filter_sao.c, encoder/sao.c).
+//
+// Drop-ins for the reference's table entries (deblock_luma[2],
+// deblock_chroma[2], sao_block; primitives.h:202-208) and picture-level
+// batched forms.  Deblocking edges lie 8 samples apart and a filter reads 3
+// and writes at most 3 samples on either side, so all vertical edges of a
+// picture are independent of each other, and so are all horizontal edges; the
+// reference's LCU-by-LCU order (xavs2_lcu_deblock) filters every sample's
+// vertical edge before its horizontal edge, so the picture is done in two
+// passes: every vertical edge, then every horizontal edge.  SAO reads the
+// deblocked picture and writes another buffer, so every sample is
+// independent.
+#include "xavs2gpu_common.cuh"
+
+#include <cstring>
+
+namespace xg {
+namespace lf {
+
+// ---- one line across an edge (lf_edge_core, filter_deblock.c:254-360) ------
+// p[0..5] = L2 L1 L0 R0 R1 R2; returns true when a sample changed.
+__device__ __forceinline__ bool filter_line(int (&p)[6], int alpha, int beta, bool chroma)
+{
+    const int L2 = p[0], L1 = p[1], L0 = p[2], R0 = p[3], R1 = p[4], R2 = p[5];
+    const int d = abs(R0 - L0);
+    if (d >= alpha || d <= 1) return false;
+    const int fl = (abs(L1 - L0) < beta ? 2 : 0) + (abs(L2 - L0) < beta ? 1 : 0);
+    const int fr = (abs(R0 - R1) < beta ? 2 : 0) + (abs(R0 - R2) < beta ? 1 : 0);
+    int fs;
+    switch (fl + fr) {
+    case 6: fs = (R1 == R0 && L0 == L1) ? 4 : 3; break;
+    case 5: fs = (R1 == R0 && L0 == L1) ? 3 : 2; break;
+    case 4: fs = fl == 2 ? 2 : 1; break;
+    case 3: fs = abs(L1 - R1) < beta ? 1 : 0; break;
+    default: fs = 0; break;
+    }
+    if (chroma && fs > 0) fs--;
+    switch (fs) {
+    case 4:
+        p[2] = (9 * L0 + 9 * L2 + 8 * R0 + 6 * R2 + 16) >> 5;
+        p[1] = (7 * L0 + 6 * L2 + 3 * R0 + 8) >> 4;
+        p[0] = (4 * L0 + 3 * L2 + R0 + 4) >> 3;
+        p[3] = (9 * R0 + 9 * R2 + 8 * L0 + 6 * L2 + 16) >> 5;
+        p[4] = (7 * R0 + 6 * R2 + 3 * L0 + 8) >> 4;
+        p[5] = (4 * R0 + 3 * R2 + L0 + 4) >> 3;
+        return true;
+    case 3:
+        p[2] = (L2 + 4 * L1 + 6 * L0 + 4 * R0 + R1 + 8) >> 4;
+        p[3] = (L1 + 4 * L0 + 6 * R0 + 4 * R1 + R2 + 8) >> 4;
+        p[1] = (3 * L2 + 8 * L1 + 4 * L0 + R0 + 8) >> 4;
+        p[4] = (3 * R2 + 8 * R1 + 4 * R0 + L0 + 8) >> 4;
+        return true;
+    case 2:
+        p[2] = (3 * L1 + 10 * L0 + 3 * R0 + 8) >> 4;
+        p[3] = (3 * L0 + 10 * R0 + 3 * R1 + 8) >> 4;
+        return true;
+    case 1:
+        p[2] = (3 * L0 + R0 + 2) >> 2;
+        p[3] = (3 * R0 + L0 + 2) >> 2;
+        return true;
+    default:
+        return false;
+    }
+}
+
+__device__ __forceinline__ int byte_of(uint32_t w, int k) { return (int)((w >> (8 * k)) & 0xFFu); }
+__device__ __forceinline__ uint32_t set_byte(uint32_t w, int k, int v)
+{
+    return (w & ~(0xFFu << (8 * k))) | ((uint32_t)v << (8 * k));
+}
+
+// ---- per-call kernel: n lines of one edge ------------------------------------
+// `src` points at the Q-side sample of line 0; lines `along` apart, samples
+// across `across` apart; line k uses flag[k >= n / 2].
+__global__ void edge_kernel(uint8_t *src, int n, int along, int across, int alpha, int beta, int chroma, int f0,
+                            int f1)
+{
+    const int k = threadIdx.x;
+    if (k >= n || !(k >= n / 2 ? f1 : f0)) return;
+    uint8_t *s = src + k * along;
+    int p[6];
+    for (int i = 0; i < 6; i++) p[i] = s[(i - 3) * across];
+    if (filter_line(p, alpha, beta, chroma != 0))
+        for (int i = 0; i < 6; i++) s[(i - 3) * across] = (uint8_t)p[i];
+}
+
+// ---- picture deblocking --------------------------------------------------------
+struct Pic {
+    uint8_t *y, *u, *v;
+    int stride, stride_c, width, height, w_scu, h_scu;
+    int n_hor;   // 8x8 columns whose horizontal edges are filtered
+    const xavs2gpu_deblock_scu_t *scus;
+};
+
+// Pass 1: every vertical edge.  A thread filters one half of one edge (the
+// 4 luma / 2 chroma lines sharing a filter flag): per line the 8 samples
+// [x-4, x+4) as two words.  Consecutive threads take consecutive edges of
+// the same lines, so a warp reads 256 contiguous bytes per line.
+__global__ void __launch_bounds__(256) deblock_ver_kernel(Pic pc)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ne = pc.w_scu - 1;                         // luma edges per row (x = 8 .. width - 8)
+    const int nec = (pc.w_scu - 1) >> 1;                 // chroma edges per row (x_c = 8, 16, ..)
+    const long long n_luma = (long long)(pc.height >> 2) * ne;
+    const long long n_chroma = (long long)(pc.height >> 2) * nec;   // 2-line groups of height / 2 rows
+    uint8_t *row;
+    int e, x, sx, sy, half, lines, stride;
+    bool chroma;
+    if (i < n_luma) {
+        const int g = (int)(i / ne);                     // 4-line group
+        e = 1 + (int)(i - (long long)g * ne);
+        x = 8 * e;
+        sx = e;
+        sy = g >> 1;
+        half = g & 1;
+        lines = 4;
+        stride = pc.stride;
+        row = pc.y + (long long)(4 * g) * stride;
+        chroma = false;
+    } else if (i < n_luma + 2 * n_chroma) {
+        const long long j = i - n_luma;
+        const int plane = j >= n_chroma;
+        const long long jj = j - (plane ? n_chroma : 0);
+        const int g = (int)(jj / nec);                   // 2-line group
+        e = 1 + (int)(jj - (long long)g * nec);
+        x = 8 * e;
+        sx = 2 * e;
+        sy = g >> 1;
+        half = g & 1;
+        lines = 2;
+        stride = pc.stride_c;
+        row = (plane ? pc.v : pc.u) + (long long)(2 * g) * stride;
+        chroma = true;
+    } else {
+        return;
+    }
+    const xavs2gpu_deblock_scu_t q = pc.scus[sy * pc.w_scu + sx];
+    if (q.type[0] == 0 || (chroma && q.type[0] != 2) || !q.flag[0][half]) return;
+    const int alpha = chroma ? q.alpha_c[0] : q.alpha[0];
+    const int beta = chroma ? q.beta_c[0] : q.beta[0];
+    for (int k = 0; k < lines; k++) {
+        uint32_t *w = reinterpret_cast<uint32_t *>(row + (long long)k * stride + x - 4);
+        uint32_t a = w[0], b = w[1];
+        int p[6] = {byte_of(a, 1), byte_of(a, 2), byte_of(a, 3), byte_of(b, 0), byte_of(b, 1), byte_of(b, 2)};
+        if (!filter_line(p, alpha, beta, chroma)) continue;
+        w[0] = set_byte(set_byte(set_byte(a, 1, p[0]), 2, p[1]), 3, p[2]);
+        w[1] = set_byte(set_byte(set_byte(b, 0, p[3]), 1, p[4]), 2, p[5]);
+    }
+}
+
+// filters columns of one word of a horizontal edge (rows y-3 .. y+2);
+// returns true when a sample changed
+__device__ __forceinline__ bool hor_word(uint8_t *col, int stride, int alpha, int beta, bool chroma, bool f_lo,
+                                         bool f_hi)
+{
+    uint32_t w[6];
+#pragma unroll
+    for (int r = 0; r < 6; r++) w[r] = *reinterpret_cast<const uint32_t *>(col + (long long)(r - 3) * stride);
+    bool any = false;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        if (!(c < 2 ? f_lo : f_hi)) continue;
+        int p[6];
+#pragma unroll
+        for (int r = 0; r < 6; r++) p[r] = byte_of(w[r], c);
+        if (filter_line(p, alpha, beta, chroma)) {
+            any = true;
+#pragma unroll
+            for (int r = 0; r < 6; r++) w[r] = set_byte(w[r], c, p[r]);
+        }
+    }
+    if (any) {
+#pragma unroll
+        for (int r = 0; r < 6; r++) *reinterpret_cast<uint32_t *>(col + (long long)(r - 3) * stride) = w[r];
+    }
+    return any;
+}
+
+// Pass 2: every horizontal edge.  A thread filters one 8x8 block's edge: 8
+// luma columns (two words of rows y-3 .. y+2, one per half) or the 4 chroma
+// columns (one word; columns 0-1 and 2-3 are the halves).
+__global__ void __launch_bounds__(256) deblock_hor_kernel(Pic pc)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ne = pc.h_scu - 1;                         // luma edges (y = 8 .. height - 8)
+    const int nec = (pc.h_scu - 1) >> 1;                 // chroma edges (y_c = 8, 16, ..)
+    const long long n_luma = (long long)ne * pc.w_scu;
+    const long long n_chroma = (long long)nec * pc.w_scu;
+    int sx, sy;
+    if (i < n_luma) {
+        const int j = (int)(i / pc.w_scu);
+        sx = (int)(i - (long long)j * pc.w_scu);
+        sy = j + 1;
+        if (sx >= pc.n_hor) return;
+        const xavs2gpu_deblock_scu_t q = pc.scus[sy * pc.w_scu + sx];
+        if (q.type[1] == 0) return;
+        uint8_t *col = pc.y + (long long)(8 * sy) * pc.stride + 8 * sx;
+        if (q.flag[1][0]) hor_word(col, pc.stride, q.alpha[1], q.beta[1], false, true, true);
+        if (q.flag[1][1]) hor_word(col + 4, pc.stride, q.alpha[1], q.beta[1], false, true, true);
+    } else if (i < n_luma + 2 * n_chroma) {
+        const long long t = i - n_luma;
+        const int plane = t >= n_chroma;
+        const long long tt = t - (plane ? n_chroma : 0);
+        const int j = (int)(tt / pc.w_scu);
+        sx = (int)(tt - (long long)j * pc.w_scu);
+        sy = 2 * (j + 1);
+        if (sx >= pc.n_hor) return;
+        const xavs2gpu_deblock_scu_t q = pc.scus[sy * pc.w_scu + sx];
+        if (q.type[1] != 2 || (!q.flag[1][0] && !q.flag[1][1])) return;
+        uint8_t *col = (plane ? pc.v : pc.u) + (long long)(8 * (j + 1)) * pc.stride_c + 4 * sx;
+        hor_word(col, pc.stride_c, q.alpha_c[1], q.beta_c[1], true, q.flag[1][0] != 0, q.flag[1][1] != 0);
+    }
+}
+
+// ---- SAO -------------------------------------------------------------------------
+__device__ __forceinline__ int sign3(int v) { return (v > 0) - (v < 0); }
+
+// The filtered column range [x0, x1) of row y of a w x h SAO block
+// (filter_sao.c:50-226) for type t; avail bits: 0 T, 1 D, 2 L, 3 R, 4 TL,
+// 5 TR, 6 DL, 7 DR.  Returns false for rows not filtered.
+__host__ __device__ __forceinline__ bool sao_row_range(int t, int av, int y, int w, int h, int &x0, int &x1)
+{
+    const bool T = av & 1, D = av & 2, L = av & 4, R = av & 8, TL = av & 16, TR = av & 32, DL = av & 64,
+               DR = av & 128;
+    x0 = L ? 0 : 1;
+    x1 = R ? w : w - 1;
+    if (t == 4) {
+        x0 = 0;
+        x1 = w;
+    } else if (t == 1) {
+        if ((y == 0 && !T) || (y == h - 1 && !D)) return false;
+        x0 = 0;
+        x1 = w;
+    } else if (t == 2 && y == 0) {
+        x0 = TL ? 0 : 1;
+        x1 = T ? (R ? w : w - 1) : 1;
+    } else if (t == 2 && y == h - 1) {
+        x0 = D ? (L ? 0 : 1) : w - 1;
+        x1 = DR ? w : w - 1;
+    } else if (t == 3 && y == 0) {
+        x0 = T ? (L ? 0 : 1) : w - 1;
+        x1 = TR ? w : w - 1;
+    } else if (t == 3 && y == h - 1) {
+        x0 = DL ? 0 : 1;
+        x1 = D ? (R ? w : w - 1) : 1;
+    }
+    return x1 > x0;
+}
+
+// neighbour offsets (dx1, dy1, dx2, dy2) of the EO types
+__constant__ int8_t c_eo_nb[4][4] = {{-1, 0, 1, 0}, {0, -1, 0, 1}, {-1, -1, 1, 1}, {1, -1, -1, 1}};
+
+// per-call: one block, dst pre-filled with the caller's samples
+__global__ void __launch_bounds__(256) sao_block_kernel(uint8_t *dst, int i_dst, const uint8_t *src, int i_src,
+                                                        int w, int h, int av, xavs2gpu_sao_param_t prm)
+{
+    for (int i = threadIdx.x; i < w * h; i += blockDim.x) {
+        const int y = i / w, x = i - y * w;
+        int x0, x1;
+        if (!sao_row_range(prm.type_idc, av, y, w, h, x0, x1) || x < x0 || x >= x1) continue;
+        const uint8_t *p = src + y * i_src + x;
+        const int s = p[0];
+        int c;
+        if (prm.type_idc == 4) {
+            c = s >> 3;
+        } else {
+            const int8_t *nb = c_eo_nb[prm.type_idc];
+            c = sign3(s - p[nb[1] * i_src + nb[0]]) + sign3(s - p[nb[3] * i_src + nb[2]]) + 2;
+        }
+        dst[y * i_dst + x] = (uint8_t)min(max(s + prm.offset[c], 0), 255);
+    }
+}
+
+// The region of an LCU (sao_get_neighbor_avail, sao.c:898-975) for
+// component c: the LCU moved 4 samples up / left where that side is
+// available, grown by 4 where the right / lower side is not, kept inside the
+// picture.
+__host__ __device__ __forceinline__ bool sao_region(int lx, int ly, int lcu_level, int width, int height, int av,
+                                                    int c, int &x, int &y, int &w, int &h)
+{
+    const int S = 1 << lcu_level;
+    x = lx * S;
+    y = ly * S;
+    w = S < width - x ? S : width - x;
+    h = S < height - y ? S : height - y;
+    const int W = c ? width >> 1 : width, H = c ? height >> 1 : height;
+    if (c) {
+        x >>= 1; y >>= 1; w >>= 1; h >>= 1;
+    }
+    if (!(av & 8)) w += 4;
+    if (!(av & 2)) h += 4;
+    if (av & 4) x -= 4; else w -= 4;
+    if (av & 1) y -= 4; else h -= 4;
+    if (w > W - x) w = W - x;
+    if (h > H - y) h = H - y;
+    return w > 0 && h > 0;
+}
+
+struct SaoPic {
+    uint8_t *dst[3];
+    const uint8_t *src[3];
+    int stride, stride_c, width, height, lcu_level, wl, hl, copy_rest;
+    const xavs2gpu_sao_lcu_t *lcus;
+};
+
+__device__ __forceinline__ int full_avail(int a)
+{
+    const int T = a & 1, D = (a >> 1) & 1, L = (a >> 2) & 1, R = (a >> 3) & 1;
+    return a & 15 | ((T & L) << 4) | ((T & R) << 5) | ((D & L) << 6) | ((D & R) << 7);
+}
+
+// A CTA filters one LCU's region of one component; a thread takes 4
+// horizontally adjacent samples (one word) at a time.  Region boundaries are
+// multiples of 4, so a word never straddles two regions.  Where regions
+// overlap (availabilities inconsistent between neighbours, which the
+// encoder's derivation never produces) the result is the reference's LCU
+// loop's: a sample keeps the value of the last LCU in raster order that
+// filters it, so a CTA leaves alone the samples that one of its later
+// neighbours filters.
+constexpr int kSaoThreads = 128;
+
+__global__ void __launch_bounds__(kSaoThreads, 8) sao_lcu_kernel(SaoPic sp)
+{
+    const int l = blockIdx.x, c = blockIdx.y;
+    const int lx = l % sp.wl, ly = l / sp.wl;
+    const xavs2gpu_sao_lcu_t &q = sp.lcus[l];
+    int rx, ry, rw, rh;
+    if (!sao_region(lx, ly, sp.lcu_level, sp.width, sp.height, q.avail, c, rx, ry, rw, rh)) return;
+    // neighbours whose regions overlap this one: x, y, w, h, type,
+    // availability, later in raster order
+    __shared__ int off[32];
+    __shared__ int nb[8][7];
+    __shared__ int n_nb;
+    if (threadIdx.x < 32) off[threadIdx.x] = q.offset[c][threadIdx.x];
+    if (threadIdx.x == 0) {
+        int no = 0;
+        for (int my = ly - 1; my <= ly + 1; my++)
+            for (int mx = lx - 1; mx <= lx + 1; mx++) {
+                if (mx < 0 || mx >= sp.wl || my < 0 || my >= sp.hl || (mx == lx && my == ly)) continue;
+                int x, y, w, h;
+                const xavs2gpu_sao_lcu_t &m = sp.lcus[my * sp.wl + mx];
+                if (!sao_region(mx, my, sp.lcu_level, sp.width, sp.height, m.avail, c, x, y, w, h)) continue;
+                if (x >= rx + rw || x + w <= rx || y >= ry + rh || y + h <= ry) continue;
+                nb[no][0] = x; nb[no][1] = y; nb[no][2] = w; nb[no][3] = h;
+                nb[no][4] = m.type[c];
+                nb[no][5] = full_avail(m.avail);
+                nb[no][6] = my * sp.wl + mx > l;
+                no++;
+            }
+        n_nb = no;
+    }
+    __syncthreads();
+    const int no = n_nb;
+    const int t = q.type[c];
+    const int av = full_avail(q.avail);
+    const int W = c ? sp.width >> 1 : sp.width, H = c ? sp.height >> 1 : sp.height;
+    const int st = c ? sp.stride_c : sp.stride;
+    const uint8_t *s = c == 0 ? sp.src[0] : c == 1 ? sp.src[1] : sp.src[2];
+    uint8_t *dp = c == 0 ? sp.dst[0] : c == 1 ? sp.dst[1] : sp.dst[2];
+    const int nwords = rw >> 2;
+    for (int i = threadIdx.x; i < nwords * rh; i += kSaoThreads) {
+        const int yy = i / nwords, x = rx + 4 * (i - yy * nwords), y = ry + yy;
+        // samples of this word that a later neighbour filters (copy mode:
+        // every sample a later neighbour's region holds); a word that
+        // another region also holds is written byte by byte
+        unsigned later = 0;
+        bool shared = false;
+        for (int k = 0; k < no; k++) {
+            const int *o = nb[k];
+            if (x < o[0] || x >= o[0] + o[2] || y < o[1] || y >= o[1] + o[3]) continue;
+            shared = true;
+            if (!o[6]) continue;
+            int a0, a1;
+            if (sp.copy_rest) {
+                later = 15u;
+            } else if (o[4] >= 0 && o[4] <= 4 && sao_row_range(o[4], o[5], y - o[1], o[2], o[3], a0, a1)) {
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (x + j >= o[0] + a0 && x + j < o[0] + a1) later |= 1u << j;
+            }
+        }
+        if (later == 15u) continue;
+        uint8_t *d = dp + (long long)y * st + x;
+        int x0 = 0, x1 = 0;
+        const bool filt = t >= 0 && t <= 4 && sao_row_range(t, av, yy, rw, rh, x0, x1) && x + 4 > rx + x0 &&
+                          x < rx + x1;
+        if (!filt) {
+            // samples SAO leaves alone: the source value, or untouched
+            if (sp.copy_rest && !shared)
+                *reinterpret_cast<uint32_t *>(d) = *reinterpret_cast<const uint32_t *>(s + (long long)y * st + x);
+            continue;
+        }
+        x0 += rx;
+        x1 += rx;
+        // source words: rows y-1, y, y+1 at x-4, x, x+4 (0 outside the
+        // picture: the availability rules keep filtered samples' neighbours
+        // inside)
+        uint32_t win[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const int yr = y + r - 1;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const int xx = x + 4 * (k - 1);
+                win[r][k] = (yr >= 0 && yr < H && xx >= 0 && xx < W)
+                                ? *reinterpret_cast<const uint32_t *>(s + (long long)yr * st + xx) : 0u;
+            }
+        }
+        const uint32_t old = sp.copy_rest ? win[1][1] : shared ? 0u : *reinterpret_cast<const uint32_t *>(d);
+        uint32_t out = old;
+        unsigned wrote = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int xs = x + k;
+            if (xs < x0 || xs >= x1 || ((later >> k) & 1u)) continue;
+            const int sv = byte_of(win[1][1], k);
+            // neighbour (dx, dy) of sample k: byte 4 + k + dx of the 12-byte
+            // window of row 1 + dy (indices constant after unrolling)
+            auto nbv = [&](int dx, int dy) {
+                const int o = 4 + k + dx;
+                return byte_of(win[1 + dy][o >> 2], o & 3);
+            };
+            int cls;
+            if (t == 4) {
+                cls = sv >> 3;
+            } else {
+                int n1, n2;
+                switch (t) {
+                case 0: n1 = nbv(-1, 0); n2 = nbv(1, 0); break;
+                case 1: n1 = nbv(0, -1); n2 = nbv(0, 1); break;
+                case 2: n1 = nbv(-1, -1); n2 = nbv(1, 1); break;
+                default: n1 = nbv(1, -1); n2 = nbv(-1, 1); break;
+                }
+                cls = sign3(sv - n1) + sign3(sv - n2) + 2;
+            }
+            out = set_byte(out, k, min(max(sv + off[cls], 0), 255));
+            wrote |= 1u << k;
+        }
+        if (shared) {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if ((wrote >> k) & 1u) d[k] = (uint8_t)byte_of(out, k);
+        } else if (sp.copy_rest || out != old) {
+            *reinterpret_cast<uint32_t *>(d) = out;
+        }
+    }
+}
+
+}  // namespace lf
+}  // namespace xg
+
+using namespace xg;
+
+// ---- per-call drop-ins ----------------------------------------------------------
+// One edge through the per-thread staging area: the samples the filter can
+// read (3 on the P side, 3 on the Q side) of each line are packed, filtered
+// and unpacked.
+static void deblock_call(uint8_t *const planes[2], int nplanes, int dir, int stride, int alpha, int beta,
+                         const uint8_t *flt_flag, bool chroma)
+{
+    const int n = chroma ? 4 : 8;
+    // a rectangle of `rows` x `cols` samples starting 3 before the edge
+    const int rows = dir == 0 ? n : 6, cols = dir == 0 ? 6 : n;
+    const size_t bytes = (size_t)rows * cols;
+    CallCtx &c = call_ctx(align_up(bytes) * nplanes);
+    for (int p = 0; p < nplanes; p++) {
+        const uint8_t *o = dir == 0 ? planes[p] - 3 : planes[p] - 3 * (intptr_t)stride;
+        pack_rows(c.h_stage + align_up(bytes) * p, o, stride, cols, rows);
+    }
+    XG_CUDA(cudaMemcpyAsync(c.d_stage, c.h_stage, align_up(bytes) * nplanes, cudaMemcpyHostToDevice, c.stream));
+    for (int p = 0; p < nplanes; p++) {
+        uint8_t *base = c.d_stage + align_up(bytes) * p;
+        uint8_t *q = dir == 0 ? base + 3 : base + 3 * cols;
+        lf::edge_kernel<<<1, 32, 0, c.stream>>>(q, n, dir == 0 ? cols : 1, dir == 0 ? 1 : cols, alpha, beta,
+                                               chroma ? 1 : 0, flt_flag[0], flt_flag[1]);
+        count_launch();
+    }
+    XG_CUDA(cudaMemcpyAsync(c.h_stage, c.d_stage, align_up(bytes) * nplanes, cudaMemcpyDeviceToHost, c.stream));
+    XG_CUDA(cudaStreamSynchronize(c.stream));
+    for (int p = 0; p < nplanes; p++) {
+        uint8_t *o = dir == 0 ? planes[p] - 3 : planes[p] - 3 * (intptr_t)stride;
+        unpack_rows(o, stride, c.h_stage + align_up(bytes) * p, cols, rows);
+    }
+}
+
+extern "C" void xavs2gpu_deblock_luma_ver(uint8_t *src, int stride, int alpha, int beta, uint8_t *flt_flag)
+{
+    uint8_t *p[2] = {src, nullptr};
+    deblock_call(p, 1, 0, stride, alpha, beta, flt_flag, false);
+}
+extern "C" void xavs2gpu_deblock_luma_hor(uint8_t *src, int stride, int alpha, int beta, uint8_t *flt_flag)
+{
+    uint8_t *p[2] = {src, nullptr};
+    deblock_call(p, 1, 1, stride, alpha, beta, flt_flag, false);
+}
+extern "C" void xavs2gpu_deblock_chroma_ver(uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta,
+                                            uint8_t *flt_flag)
+{
+    uint8_t *p[2] = {src_u, src_v};
+    deblock_call(p, 2, 0, stride, alpha, beta, flt_flag, true);
+}
+extern "C" void xavs2gpu_deblock_chroma_hor(uint8_t *src_u, uint8_t *src_v, int stride, int alpha, int beta,
+                                            uint8_t *flt_flag)
+{
+    uint8_t *p[2] = {src_u, src_v};
+    deblock_call(p, 2, 1, stride, alpha, beta, flt_flag, true);
+}
+
+extern "C" void xavs2gpu_deblock_init(uint32_t cpuid, xavs2gpu_deblock_funcs_t *f)
+{
+    (void)cpuid;
+    f->deblock_luma[0] = xavs2gpu_deblock_luma_ver;
+    f->deblock_luma[1] = xavs2gpu_deblock_luma_hor;
+    f->deblock_chroma[0] = xavs2gpu_deblock_chroma_ver;
+    f->deblock_chroma[1] = xavs2gpu_deblock_chroma_hor;
+}
+
+extern "C" void xavs2gpu_sao_block(uint8_t *p_dst, int i_dst, uint8_t *p_src, int i_src, int i_block_w,
+                                   int i_block_h, int *lcu_avail, xavs2gpu_sao_param_t *sao_param)
+{
+    if (sao_param->type_idc < 0 || sao_param->type_idc > 4 || i_block_w < 1 || i_block_h < 1) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_sao_block", "not a supported SAO type or empty block");
+        return;
+    }
+    int av = 0;
+    for (int k = 0; k < 8; k++) av |= (lcu_avail[k] ? 1 : 0) << k;
+    // source with a one-sample ring (neighbours), destination block
+    const int sw = i_block_w + 2, sh = i_block_h + 2;
+    const size_t o_dst = align_up((size_t)sw * sh);
+    CallCtx &c = call_ctx(o_dst + (size_t)i_block_w * i_block_h);
+    pack_rows(c.h_stage, p_src - i_src - 1, i_src, sw, sh);
+    pack_rows(c.h_stage + o_dst, p_dst, i_dst, i_block_w, i_block_h);
+    XG_CUDA(cudaMemcpyAsync(c.d_stage, c.h_stage, o_dst + (size_t)i_block_w * i_block_h, cudaMemcpyHostToDevice,
+                            c.stream));
+    lf::sao_block_kernel<<<1, 256, 0, c.stream>>>(c.d_stage + o_dst, i_block_w, c.d_stage + sw + 1, sw, i_block_w,
+                                                 i_block_h, av, *sao_param);
+    count_launch();
+    XG_CUDA(cudaMemcpyAsync(c.h_stage + o_dst, c.d_stage + o_dst, (size_t)i_block_w * i_block_h,
+                            cudaMemcpyDeviceToHost, c.stream));
+    XG_CUDA(cudaStreamSynchronize(c.stream));
+    unpack_rows(p_dst, i_dst, c.h_stage + o_dst, i_block_w, i_block_h);
+}
+
+extern "C" void xavs2gpu_sao_init(uint32_t cpuid, xavs2gpu_sao_flt_t *f)
+{
+    (void)cpuid;
+    *f = xavs2gpu_sao_block;
+}
+
+// ---- picture-level forms ---------------------------------------------------------
+static bool aligned4(const void *p) { return ((uintptr_t)p & 3) == 0; }
+
+extern "C" int xavs2gpu_deblock_picture(uint8_t *y, int stride, uint8_t *u, uint8_t *v, int stride_c, int width,
+                                        int height, int lcu_level, const xavs2gpu_deblock_scu_t *scus, void *stream)
+{
+    if (width < 8 || height < 8 || (width & 7) || (height & 7) || stride < width || stride_c < width / 2 ||
+        (stride & 3) || (stride_c & 3) || !aligned4(y) || !aligned4(u) || !aligned4(v) || !scus ||
+        lcu_level < 3 || lcu_level > 6) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_deblock_picture",
+             "sizes must be multiples of 8, LCU 8..64, planes and strides 4-byte aligned");
+        return XAVS2GPU_ERR_ARG;
+    }
+    // a picture one LCU wide: xavs2_lcu_deblock leaves the horizontal edges
+    // of the last 8x8 column for a next LCU in the row, which does not exist
+    const int w_scu = width / 8;
+    const int n_hor = w_scu <= (1 << (lcu_level - 3)) ? w_scu - 1 : w_scu;
+    lf::Pic pc{y, u, v, stride, stride_c, width, height, w_scu, height / 8, n_hor, scus};
+    const cudaStream_t st = (cudaStream_t)stream;
+    const long long nv = (long long)(height / 4) * (pc.w_scu - 1) + 2LL * (height / 4) * ((pc.w_scu - 1) >> 1);
+    const long long nh = (long long)(pc.h_scu - 1) * pc.w_scu + 2LL * ((pc.h_scu - 1) >> 1) * pc.w_scu;
+    if (nv > 0) {
+        lf::deblock_ver_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(pc);
+        count_launch();
+    }
+    if (nh > 0) {
+        lf::deblock_hor_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, st>>>(pc);
+        count_launch();
+    }
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_sao_picture(uint8_t *dst_y, uint8_t *dst_u, uint8_t *dst_v, const uint8_t *src_y,
+                                    const uint8_t *src_u, const uint8_t *src_v, int stride, int stride_c, int width,
+                                    int height, int lcu_level, const xavs2gpu_sao_lcu_t *lcus, int flags,
+                                    void *stream)
+{
+    const void *ptrs[6] = {dst_y, dst_u, dst_v, src_y, src_u, src_v};
+    bool ok = width >= 8 && height >= 8 && !(width & 7) && !(height & 7) && stride >= width &&
+              stride_c >= width / 2 && !(stride & 3) && !(stride_c & 3) && lcu_level >= 4 && lcu_level <= 6 && lcus;
+    for (int k = 0; k < 6; k++) ok = ok && ptrs[k] && aligned4(ptrs[k]);
+    if (!ok) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_sao_picture",
+             "sizes must be multiples of 8, LCU 16..64, planes and strides 4-byte aligned");
+        return XAVS2GPU_ERR_ARG;
+    }
+    const int S = 1 << lcu_level;
+    lf::SaoPic sp{{dst_y, dst_u, dst_v}, {src_y, src_u, src_v}, stride, stride_c, width, height, lcu_level,
+                  (width + S - 1) / S, (height + S - 1) / S, (flags & XAVS2GPU_SAO_COPY_UNFILTERED) ? 1 : 0, lcus};
+    lf::sao_lcu_kernel<<<dim3((unsigned)(sp.wl * sp.hl), 3), lf::kSaoThreads, 0, (cudaStream_t)stream>>>(sp);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}

@@ -240,3 +240,67 @@ def intra_level_blocks(width, height, shapes=None):
         ys, xs = np.meshgrid(np.arange(0, height - bh + 1, bh), np.arange(0, width - bw + 1, bw), indexing="ij")
         rects.append(np.stack([xs.ravel(), ys.ravel(), np.full(xs.size, bw), np.full(xs.size, bh)], 1))
     return np.concatenate(rects)
+
+
+# ---- in-loop filters --------------------------------------------------------------
+def _blocky(rng, w, h, amp):
+    from scipy.ndimage import gaussian_filter
+    img = gaussian_filter(rng.integers(0, 256, (h, w)).astype(np.float64), 2.0)
+    img = 40 + (img - img.min()) * (170.0 / max(np.ptp(img), 1e-9))
+    off = rng.integers(-amp, amp + 1, ((h + 7) // 8, (w + 7) // 8))
+    img += np.kron(off, np.ones((8, 8)))[:h, :w]
+    return np.clip(np.round(img), 0, 255).astype(np.uint8)
+
+
+def deblock_picture(rng, w, h, p_edge=0.8):
+    """A 4:2:0 picture with 8x8 blocking artefacts (blurred noise plus a
+    random offset per 8x8 block) and per-8x8-block edge parameters: edge type
+    (none / luma only / both) per direction with none on the picture border,
+    half-edge flags, and alpha / beta in the ranges of the AVS2 tables."""
+    from . import DEBLOCK_SCU_DTYPE
+    y = _blocky(rng, w, h, 6)
+    u = _blocky(rng, w // 2, h // 2, 4)
+    v = _blocky(rng, w // 2, h // 2, 4)
+    n = (w // 8) * (h // 8)
+    scus = np.zeros(n, DEBLOCK_SCU_DTYPE)
+    t = rng.random((n, 2))
+    scus["type"] = np.where(t < p_edge * 0.75, 2, np.where(t < p_edge, 1, 0))
+    sx = np.arange(n) % (w // 8)
+    sy = np.arange(n) // (w // 8)
+    scus["type"][sx == 0, 0] = 0
+    scus["type"][sy == 0, 1] = 0
+    scus["flag"] = (rng.random((n, 2, 2)) < 0.9).astype(np.uint8)
+    scus["alpha"] = rng.integers(4, 65, (n, 2))
+    scus["beta"] = rng.integers(1, 28, (n, 2))
+    scus["alpha_c"] = rng.integers(4, 65, (n, 2))
+    scus["beta_c"] = rng.integers(1, 28, (n, 2))
+    return y, u, v, scus
+
+
+def sao_params(rng, w, h, lcu_level, p_off=0.1):
+    """Per-LCU SAO parameters: per component a type (off with probability
+    p_off, else EO_0 / EO_90 / EO_135 / EO_45 / BO uniformly), EO offsets in
+    the AVS2 ranges (class 0, 1 >= 0; class 3, 4 <= 0; class 2 zero), BO
+    offsets on four bands from a random start band, and the side
+    availabilities of a single-slice picture."""
+    from . import SAO_LCU_DTYPE
+    S = 1 << lcu_level
+    wl, hl = (w + S - 1) // S, (h + S - 1) // S
+    lcus = np.zeros(wl * hl, SAO_LCU_DTYPE)
+    lx = np.arange(wl * hl) % wl
+    ly = np.arange(wl * hl) // wl
+    lcus["avail"] = (ly > 0) | ((ly < hl - 1) << 1) | ((lx > 0) << 2) | ((lx < wl - 1) << 3)
+    for i in range(wl * hl):
+        for c in range(3):
+            if rng.random() < p_off:
+                lcus["type"][i, c] = -1
+                continue
+            t = int(rng.integers(0, 5))
+            lcus["type"][i, c] = t
+            if t < 4:
+                lcus["offset"][i, c, :5] = (rng.integers(0, 7), rng.integers(0, 2), 0, -rng.integers(0, 2),
+                                            -rng.integers(0, 7))
+            else:
+                b = int(rng.integers(0, 29))
+                lcus["offset"][i, c, b:b + 4] = rng.integers(-7, 8, 4)
+    return lcus
