@@ -921,6 +921,136 @@ def run_loopfilter(args):
     print(json.dumps(line))
 
 
+# ---- lookahead analysis: 4K half-resolution picture + MAD maps -------------------
+LA_METRIC = "bit-exact 3840x2160 pictures/s (lookahead: half-resolution picture + 16/32/64 MAD maps)"
+
+
+def cpu_lookahead(img, W, H):
+    import oracle
+    lw = W // 2
+    low = np.zeros((H // 2, lw), np.uint8)
+    n = [((W + s - 1) // s) * ((H + s - 1) // s) for s in (16, 32, 64)]
+    mads = [np.zeros(k, np.int32) for k in n]
+    t0 = time.perf_counter()
+    oracle.lib().xo_lookahead_picture(oracle.ptr(img), W, W, H, oracle.ptr(low), lw, *[oracle.ptr(m) for m in mads])
+    return time.perf_counter() - t0, low, mads
+
+
+def run_lookahead(args):
+    import torch
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+
+    rank, world, local = dist_env()
+    W, H = args.chain_width, args.chain_height
+    img = synth.chain_pictures(1, W, H, seed=81 + rank)[0]
+    n = [((W + s - 1) // s) * ((H + s - 1) // s) for s in (16, 32, 64)]
+    cfg = {"workload": "lookahead_2160p", "width": W, "height": H,
+           "outputs": "width/2 x height/2 lowres picture, MAD of every aligned 16x16 / 32x32 / 64x64 block",
+           "content": "blurred-noise picture", "l2": "flushed between steps (512 MB write)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cpu_lookahead(img, W, H)
+        tt = sum(cpu_lookahead(img, W, H)[0] for _ in range(args.steps))
+        value = args.steps / tt
+        print(json.dumps({"impl": "reference", "metric": LA_METRIC, "value": value, "unit": "pictures/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+                          "cpu_baseline": {"value": value, "unit": "pictures/s", "cores": 1, "kind": "port",
+                                           "sample": "whole pictures, oracle C (one thread)"},
+                          "e2e": {"value": value, "unit": "pictures/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    dev = torch.device("cuda", local)
+    h_img = torch.from_numpy(img).pin_memory()
+    d_img = h_img.to(dev)
+    d_low = torch.empty((H // 2, W // 2), dtype=torch.uint8, device=dev)
+    d_mad = [torch.empty(k, dtype=torch.int32, device=dev) for k in n]
+    h_low = torch.empty_like(d_low, device="cpu").pin_memory()
+    h_mad = [torch.empty(k, dtype=torch.int32).pin_memory() for k in n]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(dev)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def step(s):
+        rc = lib.xavs2gpu_lookahead_picture(P(d_img), W, W, H, P(d_low), W // 2, *[P(m) for m in d_mad],
+                                            ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step(stream)
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    clk.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step(stream)
+            ends[i].record(stream)
+    barrier()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = reduce_max(float(sum(step_ms)), dev)
+    value = world * args.steps / (total_ms / 1e3)
+    kernel_ms = float(np.median(step_ms))
+    barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            d_img.copy_(h_img, non_blocking=True)
+            step(stream)
+            h_low.copy_(d_low, non_blocking=True)
+            for k in range(3):
+                h_mad[k].copy_(d_mad[k], non_blocking=True)
+        stream.synchronize()
+    barrier()
+    e2e = world * args.steps / reduce_max(time.perf_counter() - t0, dev)
+    if rank != 0:
+        return
+    cpu_s, low, mads = cpu_lookahead(img, W, H)
+    exact = bool(np.array_equal(h_low.numpy(), low) and all(np.array_equal(h_mad[k].numpy(), mads[k])
+                                                           for k in range(3)))
+    peaks, peak_src = measured_peaks()
+    out_bytes = d_low.numel() + 4 * sum(n)
+    algo = img.nbytes + out_bytes
+    achieved = algo / (kernel_ms / 1e3) / 1e9
+    print(json.dumps({
+        "metric": LA_METRIC, "value": value, "unit": "pictures/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+        "e2e": {"value": e2e, "unit": "pictures/s", "h2d_bytes_per_step": int(img.nbytes),
+                "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "lookahead_kernel", "achieved": achieved,
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0),
+                     "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_step": int(algo),
+                     "kernel_ms": kernel_ms},
+        "sample_bit_exact": exact,
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "pictures/s", "cores": 1, "kind": "port",
+                         "sample": "one whole picture, oracle C, one thread"},
+        "clocks": clocks,
+    }))
+
+
 # ---- serving: 64 concurrent streams, continuous batching --------------------
 SERVE_METRIC = "served p99 frame latency (64 streams 360p..2160p, 30 fps Poisson arrivals, continuous batching)"
 SERVE_RES = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
@@ -1171,9 +1301,11 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
-    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter"], default="me",
+    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter", "lookahead"],
+                    default="me",
                     help="me: batched motion search (default); tq: batched transform+quant; chain: 4K full-picture "
-                         "chain; serve: 64-stream serving; intra: rough intra mode decision; loopfilter: 4K deblocking + SAO")
+                         "chain; serve: 64-stream serving; intra: rough intra mode decision; loopfilter: 4K deblocking + SAO; "
+                         "lookahead: 4K half-resolution picture + MAD maps")
     ap.add_argument("--chain-width", type=int, default=3840)
     ap.add_argument("--chain-height", type=int, default=2160)
     ap.add_argument("--tq-blocks", type=int, default=1000000)
@@ -1192,6 +1324,8 @@ def main():
         run_intra(args)
     elif args.workload == "loopfilter":
         run_loopfilter(args)
+    elif args.workload == "lookahead":
+        run_lookahead(args)
     elif args.workload == "chain":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "metric": CHAIN_METRIC,

@@ -400,6 +400,24 @@ XAVS2GPU_API int xavs2gpu_sao_picture(uint8_t *dst_y, uint8_t *dst_u, uint8_t *d
                                       int width, int height, int lcu_level, const xavs2gpu_sao_lcu_t *lcus,
                                       int flags, void *stream);
 
+/* ---- lookahead analysis (mc.c:838-855, pixel.c:1620-1649, rdo.c:3286-3297)
+ * lowres_filter (intrinsic_func_t.lowres_filter, primitives.h:140): the
+ * width x height output from 2*width x 2*height source samples, each output
+ * the rounded average of the rounded vertical averages of a 2x2 quad. */
+XAVS2GPU_API void xavs2gpu_lowres_filter(uint8_t *src, int i_src, uint8_t *dst, int i_dst, int width, int height);
+/* The same over device buffers, stream-ordered. */
+XAVS2GPU_API int xavs2gpu_lowres_picture(const uint8_t *src, int i_src, uint8_t *dst, int i_dst, int width,
+                                         int height, void *stream);
+/* One pass over a luma picture (device pointers): the width/2 x height/2
+ * low-resolution picture and the MAD (mad_NxN_c) of every aligned 16x16,
+ * 32x32 and 64x64 block, raster order over ceil(width/N) x ceil(height/N)
+ * positions per size, -1 for blocks not fully inside the picture.  The
+ * encoder's CU-depth prediction splits a CU when its MAD reaches 512 (16x16),
+ * 2048 (32x32) or 12288 (64x64) (ctu_intra_depth_pred_mad). */
+XAVS2GPU_API int xavs2gpu_lookahead_picture(const uint8_t *src, int stride, int width, int height, uint8_t *lowres,
+                                            int lowres_stride, int32_t *mad16, int32_t *mad32, int32_t *mad64,
+                                            void *stream);
+
 /* ---- batched transform + quant chain -----------------------------------
  * For every block: dct (or, for a 4x4 block with flag bit 1, the 4x4
  * secondary transform) -> quant -> when any level is non-zero, dequant ->

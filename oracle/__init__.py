@@ -115,6 +115,8 @@ _ORACLE_SIGS = {
     "xo_deblock_picture": (None, [_P, _I, _P, _P, _I, _I, _I, _P, _I, _I]),
     "xo_sao_block": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
     "xo_sao_picture": (None, [_P, _P, _I, _I, _I, _I, _I, _P]),
+    "xo_lowres_filter": (None, [_P, _I, _P, _I, _I, _I]),
+    "xo_lookahead_picture": (None, [_P, _I, _I, _I, _P, _I, _P, _P, _P]),
 }
 _REF_SIGS = {
     "xr_cmp": (_I, [_I, _I, _P, _S, _P, _S]),
@@ -142,6 +144,7 @@ _REF_SIGS = {
     "xr_deblock_luma": (None, [_I, _P, _I, _I, _I, _P]),
     "xr_deblock_chroma": (None, [_I, _P, _P, _I, _I, _I, _P]),
     "xr_sao_block": (None, [_P, _I, _P, _I, _I, _I, _P, _P]),
+    "xr_lowres_filter": (None, [_P, _I, _P, _I, _I, _I]),
 }
 
 

@@ -406,3 +406,10 @@ void xr_sao_block(pel_t *p_dst, int i_dst, pel_t *p_src, int i_src, int w, int h
     xr_init();
     g_funcs.sao_block(p_dst, i_dst, p_src, i_src, w, h, avail, prm);
 }
+
+/* lowres_filter (mc.c:838-855, table member primitives.h:140) */
+void xr_lowres_filter(pel_t *src, int i_src, pel_t *dst, int i_dst, int width, int height)
+{
+    xr_init();
+    g_funcs.lowres_filter(src, i_src, dst, i_dst, width, height);
+}

@@ -1640,3 +1640,34 @@ void xo_sao_picture(uint8_t *const dst[3], const uint8_t *const src[3], int stri
             }
         }
 }
+
+/* ------------------------------------------------------------------------
+ * lookahead analysis
+ * ---------------------------------------------------------------------- */
+/* lowres_filter_core_c (mc.c:838-855) */
+void xo_lowres_filter(const uint8_t *src, int i_src, uint8_t *dst, int i_dst, int width, int height)
+{
+    int x, y;
+    for (y = 0; y < height; y++) {
+        const uint8_t *a = src + 2 * y * i_src, *b = a + i_src;
+        for (x = 0; x < width; x++) {
+            const int l = (a[2 * x] + b[2 * x] + 1) >> 1, r = (a[2 * x + 1] + b[2 * x + 1] + 1) >> 1;
+            dst[y * i_dst + x] = (uint8_t)((l + r + 1) >> 1);
+        }
+    }
+}
+
+void xo_lookahead_picture(const uint8_t *src, int stride, int width, int height, uint8_t *lowres, int lowres_stride,
+                          int32_t *mad16, int32_t *mad32, int32_t *mad64)
+{
+    int32_t *out[3] = {mad16, mad32, mad64};
+    int k, x, y;
+    xo_lowres_filter(src, stride, lowres, lowres_stride, width / 2, height / 2);
+    for (k = 0; k < 3; k++) {
+        const int n = 16 << k, nx = (width + n - 1) / n, ny = (height + n - 1) / n;
+        for (y = 0; y < ny; y++)
+            for (x = 0; x < nx; x++)
+                out[k][y * nx + x] = ((x + 1) * n <= width && (y + 1) * n <= height)
+                                         ? xo_mad(src + (size_t)y * n * stride + x * n, stride, n) : -1;
+    }
+}

@@ -251,4 +251,15 @@ typedef struct xo_sao_lcu {
 void xo_sao_picture(uint8_t *const dst[3], const uint8_t *const src[3], int stride, int stride_c, int width,
                     int height, int lcu_level, const xo_sao_lcu_t *lcus);
 
+/* ---- lookahead analysis (mc.c:838-855, pixel.c:1620-1649, rdo.c:3286-3297) */
+/* lowres_filter: dst[y][x] = avg(avg(s[2y][2x], s[2y+1][2x]), avg(s[2y][2x+1],
+ * s[2y+1][2x+1])), each avg rounding up; width, height = output size. */
+void xo_lowres_filter(const uint8_t *src, int i_src, uint8_t *dst, int i_dst, int width, int height);
+/* The half-resolution picture (width/2 x height/2) and the MAD of every
+ * aligned 16x16, 32x32, 64x64 block fully inside the picture (raster order
+ * per size over ceil(width/N) x ceil(height/N) positions; -1 where a block
+ * leaves the picture). */
+void xo_lookahead_picture(const uint8_t *src, int stride, int width, int height, uint8_t *lowres, int lowres_stride,
+                          int32_t *mad16, int32_t *mad32, int32_t *mad64);
+
 #endif

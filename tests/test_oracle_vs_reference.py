@@ -434,3 +434,14 @@ def test_sao_block(olib, rlib):
                     olib.xo_sao_block(ptr(dst1, o), 96, ptr(img, o), 96, w, h, ptr(avail), ptr(prm))
                     rlib.xr_sao_block(ptr(dst2, o), 96, ptr(img, o), 96, w, h, ptr(avail), ptr(prm))
                     assert np.array_equal(dst1, dst2), (trial, w, h, sides, typ)
+
+
+def test_lowres_filter(olib, rlib):
+    rng = np.random.default_rng(94)
+    for w, h in ((32, 18), (7, 5), (64, 64), (1, 1)):
+        src = rng.integers(0, 256, (2 * h + 3, 2 * w + 5), dtype=np.uint8)
+        a = np.zeros((h, w + 3), np.uint8)
+        b = a.copy()
+        olib.xo_lowres_filter(ptr(src), src.shape[1], ptr(a), w + 3, w, h)
+        rlib.xr_lowres_filter(ptr(src), src.shape[1], ptr(b), w + 3, w, h)
+        assert np.array_equal(a, b), (w, h)
