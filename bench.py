@@ -1051,6 +1051,192 @@ def run_lookahead(args):
     }))
 
 
+# ---- skip / direct rough cost: every CU of a 1080p picture, 5 candidates -------
+SKIP_METRIC = ("bit-exact skip/direct candidate costs/s (1080p, CUs 8..64, 5 candidates per CU incl. 4-PU and "
+               "bi-predicted, SA8D + lambda*rate, best per CU)")
+SKIP_OPS_PER_SAMPLE = 10   # prediction 1, difference 1, 8x8 Hadamard 6, |x| accumulate 2
+
+
+def skip_workload(rank, W, H):
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(91 + rank)
+    frames = synth.chain_pictures(3, W, H, seed=93 + rank, pan_px=3)
+    cur, refs = frames[2], [frames[1], frames[0]]
+    cands, n_cu = synth.skip_candidates(rng, W, H, 2, motion=(-12, 0), cand_dtype=xg.SKIP_CAND_DTYPE)
+    return cur, refs, cands, n_cu
+
+
+def cpu_skip(olib, cur, tab, stride, W, H, cands, n_cu, lam, fraction, seed):
+    """The oracle over a random sample of the CUs (all their candidates);
+    returns (candidates, samples evaluated, seconds, CU ids, dist, cost, best)."""
+    rng = np.random.default_rng(seed)
+    pick = np.nonzero(rng.random(n_cu) < fraction)[0]
+    sel = np.ascontiguousarray(cands[np.isin(cands["cu"], pick)])
+    remap = np.full(n_cu, -1, np.int64)
+    remap[pick] = np.arange(len(pick))
+    sub = sel.copy()
+    sub["cu"] = remap[sel["cu"]]
+    d = np.zeros(len(sub), np.int32)
+    c = np.zeros(len(sub))
+    b = np.zeros(len(pick), np.int32)
+    t0 = time.perf_counter()
+    olib.xo_skip_costs(oracle_ptr(cur), W, tab, stride, W, H, 2, oracle_ptr(sub), len(sub), lam, len(pick),
+                       oracle_ptr(d), oracle_ptr(c), oracle_ptr(b))
+    dt = time.perf_counter() - t0
+    samples = int((1 << (2 * sub["size_log2"].astype(np.int64))).sum())
+    return len(sub), samples, dt, pick, sel, d, c, b
+
+
+def oracle_ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def run_skip(args):
+    import torch
+    import oracle
+    import xavs2_gb300 as xg
+
+    rank, world, local = dist_env()
+    W, H = args.width, args.height
+    cur, refs, cands, n_cu = skip_workload(rank, W, H)
+    n = len(cands)
+    lam = float(np.sqrt(2.0 ** ((QP - 11) / 4.0) * 0.68))
+    samples = int((1 << (2 * cands["size_log2"].astype(np.int64))).sum())
+    cfg = {"workload": "skip_direct_1080p", "width": W, "height": H, "refs": 2, "cus": n_cu, "candidates": n,
+           "candidates_per_cu": "1 four-PU temporal-style + 4 single-PU (35 % bi-predicted, some repeated)",
+           "motion": "pan 3 px/picture + local motion; candidate vectors around (-3, 0) px", "qp": QP,
+           "l2": "flushed between steps (512 MB write)"}
+    olib = oracle.lib()
+    stride = W + 160
+    flats = [np.ascontiguousarray(oracle.interpolate_frame(olib, r, mode=2).reshape(16, -1)) for r in refs]
+    tab = (ctypes.c_void_p * 32)(*[oracle.ptr(f[k], 80 * stride + 80).value for f in flats for k in range(16)])
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        frac = min(1.0, 8 * args.cpu_fraction)
+        cpu_skip(olib, cur, tab, stride, W, H, cands, n_cu, lam, frac / 4, 100)
+        done, tt = 0, 0.0
+        for i in range(args.steps):
+            k, _, dt, *_ = cpu_skip(olib, cur, tab, stride, W, H, cands, n_cu, lam, frac, 200 + i)
+            done += k
+            tt += dt
+        value = done / tt
+        print(json.dumps({"impl": "reference", "metric": SKIP_METRIC, "value": value, "unit": "candidates/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+                          "cpu_baseline": {"value": value, "unit": "candidates/s", "cores": 1, "kind": "port",
+                                           "sample": "per step the candidates of a random %.1f%% of the CUs, "
+                                                     "oracle C (one thread)" % (100 * frac)},
+                          "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = xg.load()
+    lib.xavs2gpu_init(local)
+    dev = torch.device("cuda", local)
+    sess = xg.MeSession(W, H, 2, 1)
+    sess.set_picture(-1, cur)
+    for i, r in enumerate(refs):
+        sess.set_picture(i, r)
+    sess.sync()
+    stream = torch.cuda.ExternalStream(sess.stream())
+    h_c = torch.from_numpy(cands.view(np.uint8).copy()).pin_memory()
+    d_c = h_c.to(dev)
+    d_dist = torch.empty(n, dtype=torch.int32, device=dev)
+    d_cost = torch.empty(n, dtype=torch.float64, device=dev)
+    d_best = torch.empty(n_cu, dtype=torch.int32, device=dev)
+    h_dist = torch.empty(n, dtype=torch.int32).pin_memory()
+    h_cost = torch.empty(n, dtype=torch.float64).pin_memory()
+    h_best = torch.empty(n_cu, dtype=torch.int32).pin_memory()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def step():
+        rc = lib.xavs2gpu_skip_costs(ctypes.c_void_p(sess.h), P(d_c), n, lam, n_cu, P(d_dist), P(d_cost), P(d_best),
+                                     None)
+        assert rc == 0
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    sess.sync()
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    launches0 = lib.xavs2gpu_kernel_launches()
+    clk.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+    sess.sync()
+    barrier()
+    clocks = clk.stop()
+    launches = lib.xavs2gpu_kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = reduce_max(float(sum(step_ms)), dev)
+    value = n * world * args.steps / (total_ms / 1e3)
+    kernel_ms = float(np.median(step_ms))
+    barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            d_c.copy_(h_c, non_blocking=True)
+            step()
+            h_dist.copy_(d_dist, non_blocking=True)
+            h_cost.copy_(d_cost, non_blocking=True)
+            h_best.copy_(d_best, non_blocking=True)
+    sess.sync()
+    barrier()
+    e2e = n * world * args.steps / reduce_max(time.perf_counter() - t0, dev)
+    dist_h, cost_h, best_h = h_dist.numpy().copy(), h_cost.numpy().copy(), h_best.numpy().copy()
+    # release the tensors that were used on the session's stream before the
+    # session (and its stream) goes away
+    del h_c, d_c, d_dist, d_cost, d_best, h_dist, h_cost, h_best, flush, stream
+    torch.cuda.synchronize()
+    sess.close()
+    if rank != 0:
+        return
+    k, smp, cpu_s, pick, sel, d, c, b = cpu_skip(olib, cur, tab, stride, W, H, cands, n_cu, lam, args.cpu_fraction, 7)
+    gi = np.nonzero(np.isin(cands["cu"], pick))[0]
+    gb = best_h[pick]
+    exact = bool(np.array_equal(dist_h[gi], d) and np.array_equal(cost_h[gi], c) and
+                 np.array_equal(np.where(gb >= 0, np.searchsorted(gi, gb), -1), b))
+    peaks, peak_src = measured_peaks()
+    peak = 152 * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / SKIP_OPS_PER_SAMPLE / 1e12
+    achieved = samples / (kernel_ms / 1e3) / 1e12
+    print(json.dumps({
+        "metric": SKIP_METRIC, "value": value, "unit": "candidates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+        "e2e": {"value": e2e, "unit": "candidates/s", "h2d_bytes_per_step": int(cands.nbytes),
+                "d2h_bytes_per_step": int(12 * n + 4 * n_cu)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "int", "kernel": "skip_count + skip_scatter + skip_cost + skip_best", "achieved": achieved,
+                     "peak": peak, "unit": "T candidate-samples/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per sample (%s)"
+                                    % (SKIP_OPS_PER_SAMPLE, peak_src),
+                     "work_per_launch": "%d candidates, %d predicted samples" % (n, samples), "kernel_ms": kernel_ms},
+        "sample_bit_exact": exact,
+        "cpu_baseline": {"value": k / cpu_s, "unit": "candidates/s", "cores": 1, "kind": "port",
+                         "sample": "the candidates of a random %.2f%% (%d) of the CUs, oracle C (one thread)"
+                                   % (100 * args.cpu_fraction, len(pick))},
+        "clocks": clocks,
+    }), flush=True)
+
+
 # ---- serving: 64 concurrent streams, continuous batching --------------------
 SERVE_METRIC = "served p99 frame latency (64 streams 360p..2160p, 30 fps Poisson arrivals, continuous batching)"
 SERVE_RES = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
@@ -1301,11 +1487,11 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
-    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter", "lookahead"],
+    ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter", "lookahead", "skip"],
                     default="me",
                     help="me: batched motion search (default); tq: batched transform+quant; chain: 4K full-picture "
                          "chain; serve: 64-stream serving; intra: rough intra mode decision; loopfilter: 4K deblocking + SAO; "
-                         "lookahead: 4K half-resolution picture + MAD maps")
+                         "lookahead: 4K half-resolution picture + MAD maps; skip: skip/direct candidate costs")
     ap.add_argument("--chain-width", type=int, default=3840)
     ap.add_argument("--chain-height", type=int, default=2160)
     ap.add_argument("--tq-blocks", type=int, default=1000000)
@@ -1326,6 +1512,8 @@ def main():
         run_loopfilter(args)
     elif args.workload == "lookahead":
         run_lookahead(args)
+    elif args.workload == "skip":
+        run_skip(args)
     elif args.workload == "chain":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "metric": CHAIN_METRIC,

@@ -544,6 +544,31 @@ XAVS2GPU_API int xavs2gpu_me_prepare(xavs2gpu_me_session_t *s, const xavs2gpu_me
 XAVS2GPU_API int xavs2gpu_me_autotune(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm, int reps,
                                       float *best_ms);
 
+/* ---- skip / direct rough cost (rdo.c:2366-2480) ---------------------------
+ * One candidate of a CU (skip or direct mode, motion derived by the host):
+ * the CU (size_log2 3..6, inside the picture), one PU or four quadrant PUs
+ * (z-order), per PU the reference slot of list 0 / 1 (-1 unused; both: the
+ * average of the two predictions) and quarter-pel vectors, and the mode's
+ * header bits.  A CU's candidates are contiguous, in evaluation order. */
+typedef struct xavs2gpu_skip_cand {
+    int16_t x, y;
+    uint8_t size_log2, n_pu;
+    int16_t pad_;
+    int32_t cu;
+    int32_t rate;
+    int8_t ref[4][2];
+    int16_t mv[4][2][2];
+} xavs2gpu_skip_cand_t;
+/* Against the current picture and reference planes of a motion-search
+ * session: dist[i] = luma SA8D of candidate i's prediction (-1: not
+ * evaluated -- same motion as an earlier candidate of its CU, or a bad
+ * candidate), cost[i] = dist + lambda * rate (rdcost_t rounding),
+ * best[cu] = the first candidate with the strictly smallest cost (-1:
+ * none).  Device arrays; stream NULL = the session's stream. */
+XAVS2GPU_API int xavs2gpu_skip_costs(xavs2gpu_me_session_t *s, const xavs2gpu_skip_cand_t *cands, int n,
+                                     double lambda, int n_cus, int32_t *dist, double *cost, int32_t *best,
+                                     void *stream);
+
 /* ---- several pictures per launch -------------------------------------------
  * No counterpart in the reference (its search runs one PU at a time).  The
  * session's work (CTU jobs, per-PU searches, refinements) of up to 256

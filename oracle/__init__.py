@@ -117,6 +117,7 @@ _ORACLE_SIGS = {
     "xo_sao_picture": (None, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "xo_lowres_filter": (None, [_P, _I, _P, _I, _I, _I]),
     "xo_lookahead_picture": (None, [_P, _I, _I, _I, _P, _I, _P, _P, _P]),
+    "xo_skip_costs": (None, [_P, _I, _P, _I, _I, _I, _I, _P, _I, ctypes.c_double, _I, _P, _P, _P]),
 }
 _REF_SIGS = {
     "xr_cmp": (_I, [_I, _I, _P, _S, _P, _S]),

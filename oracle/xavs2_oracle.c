@@ -1671,3 +1671,85 @@ void xo_lookahead_picture(const uint8_t *src, int stride, int width, int height,
                                          ? xo_mad(src + (size_t)y * n * stride + x * n, stride, n) : -1;
     }
 }
+
+/* ------------------------------------------------------------------------
+ * skip / direct rough cost (cu_check_skip_direct_rough2, rdo.c:2395-2480)
+ * ---------------------------------------------------------------------- */
+static int skip_same_motion(const xo_skip_cand_t *a, const xo_skip_cand_t *b)
+{
+    int q, l;
+    if (a->n_pu != b->n_pu) return 0;
+    for (q = 0; q < a->n_pu; q++)
+        for (l = 0; l < 2; l++) {
+            if (a->ref[q][l] != b->ref[q][l]) return 0;
+            if (a->ref[q][l] >= 0 && (a->mv[q][l][0] != b->mv[q][l][0] || a->mv[q][l][1] != b->mv[q][l][1]))
+                return 0;
+        }
+    return 1;
+}
+
+void xo_skip_costs(const uint8_t *cur, int cur_stride, const uint8_t *const *planes, int stride, int width,
+                   int height, int nrefs, const xo_skip_cand_t *cands, int n, double lambda, int n_cus,
+                   int32_t *dist, double *cost, int32_t *best)
+{
+    static uint8_t pred[64 * 64];
+    const double max_cost = (double)(1LL << 50);   /* MAX_COST (defines.h:299) */
+    int i, j, q, l, x, y;
+    for (i = 0; i < n; i++) {
+        const xo_skip_cand_t *k = &cands[i];
+        const int S = 1 << k->size_log2;
+        int ok = k->size_log2 >= 3 && k->size_log2 <= 6 && (k->n_pu == 1 || k->n_pu == 4) && k->x >= 0 &&
+                 k->y >= 0 && k->x + S <= width && k->y + S <= height;
+        /* update_skip_mv_list (rdo.c:2366-2389): repeated motion is skipped */
+        for (j = i - 1; ok && j >= 0 && cands[j].cu == k->cu; j--)
+            if (skip_same_motion(&cands[j], k)) ok = 0;
+        if (ok) {
+            const int hp = k->n_pu == 4 ? S / 2 : S;
+            for (q = 0; q < k->n_pu; q++) {
+                if (k->ref[q][0] < 0 && k->ref[q][1] < 0) ok = 0;
+                for (l = 0; l < 2; l++) {
+                    const int r = k->ref[q][l];
+                    int px, py;
+                    if (r < 0) continue;
+                    px = k->x + (q & 1) * hp + (k->mv[q][l][0] >> 2);
+                    py = k->y + (q >> 1) * hp + (k->mv[q][l][1] >> 2);
+                    if (r >= nrefs || px < -80 || py < -80 || px + hp > width + 80 || py + hp > height + 80) ok = 0;
+                }
+            }
+        }
+        if (!ok) {
+            dist[i] = -1;
+            cost[i] = max_cost;
+            continue;
+        }
+        for (y = 0; y < S; y++)
+            for (x = 0; x < S; x++) {
+                const int qq = k->n_pu == 4 ? (x >= S / 2) + 2 * (y >= S / 2) : 0;
+                int v[2], nv = 0;
+                for (l = 0; l < 2; l++) {
+                    const int r = k->ref[qq][l];
+                    const int mx = k->mv[qq][l][0], my = k->mv[qq][l][1];
+                    const uint8_t *pl;
+                    if (r < 0) continue;
+                    /* frame sub-pel plane of the fractional position (mc.c:570-574) */
+                    pl = planes[16 * r + ((my & 3) << 2) + (mx & 3)];
+                    v[nv++] = pl[(intptr_t)(k->y + y + (my >> 2)) * stride + k->x + x + (mx >> 2)];
+                }
+                /* bi-prediction: pixel_avg (pixel.c:680-719) */
+                pred[y * 64 + x] = (uint8_t)(nv == 2 ? (v[0] + v[1] + 1) >> 1 : v[0]);
+            }
+        dist[i] = xo_sa8d(k->size_log2 - 2, cur + (intptr_t)k->y * cur_stride + k->x, cur_stride, pred, 64);
+        cost[i] = (double)dist[i] + lambda * (double)k->rate;
+    }
+    for (i = 0; i < n_cus; i++) best[i] = -1;
+    for (i = 0; i < n; i++) {
+        const int cu = cands[i].cu;
+        double m = max_cost;
+        if (cu < 0 || cu >= n_cus || (i > 0 && cands[i - 1].cu == cu)) continue;
+        for (j = i; j < n && cands[j].cu == cu; j++)
+            if (cost[j] < m) {
+                m = cost[j];
+                best[cu] = j;
+            }
+    }
+}

@@ -262,4 +262,23 @@ void xo_lowres_filter(const uint8_t *src, int i_src, uint8_t *dst, int i_dst, in
 void xo_lookahead_picture(const uint8_t *src, int stride, int width, int height, uint8_t *lowres, int lowres_stride,
                           int32_t *mad16, int32_t *mad32, int32_t *mad64);
 
+/* ---- skip / direct rough cost (rdo.c:2366-2480) ------------------------ */
+typedef struct xo_skip_cand {
+    int16_t x, y;
+    uint8_t size_log2, n_pu;
+    int16_t pad_;
+    int32_t cu, rate;
+    int8_t ref[4][2];
+    int16_t mv[4][2][2];
+} xo_skip_cand_t;
+/* Per candidate: the luma prediction from the reference planes (planes[16 r
+ * + k] at pixel (0,0), margin 80, stride `stride`; one list or the rounded
+ * average of two), its SA8D against cur, cost = dist + lambda * rate; per CU
+ * the first candidate with the strictly smallest cost.  Candidates whose
+ * motion repeats an earlier one of their CU, or that are malformed, get
+ * dist -1 and cost MAX_COST. */
+void xo_skip_costs(const uint8_t *cur, int cur_stride, const uint8_t *const *planes, int stride, int width,
+                   int height, int nrefs, const xo_skip_cand_t *cands, int n, double lambda, int n_cus,
+                   int32_t *dist, double *cost, int32_t *best);
+
 #endif

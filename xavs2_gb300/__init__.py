@@ -156,6 +156,7 @@ _SIGS = {
     "xavs2gpu_sao_init": (None, [ctypes.c_uint32, _P]),
     "xavs2gpu_deblock_picture": (_I, [_P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
     "xavs2gpu_lowres_filter": (None, [_P, _I, _P, _I, _I, _I]),
+    "xavs2gpu_skip_costs": (_I, [_P, _P, _I, ctypes.c_double, _I, _P, _P, _P, _P]),
     "xavs2gpu_lowres_picture": (_I, [_P, _I, _P, _I, _I, _I, _P]),
     "xavs2gpu_lookahead_picture": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "xavs2gpu_sao_picture": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _I, _P]),
@@ -441,6 +442,8 @@ INTRA_RESULT_DTYPE = np.dtype([("cost", "<f8", (33,)), ("cand_cost", "<f8", (9,)
 DEBLOCK_SCU_DTYPE = np.dtype([("type", "u1", (2,)), ("flag", "u1", (2, 2)), ("alpha", "u1", (2,)),
                               ("beta", "u1", (2,)), ("alpha_c", "u1", (2,)), ("beta_c", "u1", (2,)),
                               ("pad_", "u1", (2,))])
+SKIP_CAND_DTYPE = np.dtype([("x", "<i2"), ("y", "<i2"), ("size_log2", "u1"), ("n_pu", "u1"), ("pad_", "<i2"),
+                            ("cu", "<i4"), ("rate", "<i4"), ("ref", "i1", (4, 2)), ("mv", "<i2", (4, 2, 2))])
 SAO_LCU_DTYPE = np.dtype([("type", "i1", (3,)), ("avail", "u1"), ("offset", "i1", (3, 32))])
 
 

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libxavs2gpu.so")
-SOURCES = ["runtime.cu", "pixel.cu", "mc.cu", "transform.cu", "tq.cu", "me.cu", "chain.cu", "serve.cu", "intra.cu", "loopfilter.cu", "analysis.cu"]
+SOURCES = ["runtime.cu", "pixel.cu", "mc.cu", "transform.cu", "tq.cu", "me.cu", "chain.cu", "serve.cu", "intra.cu", "loopfilter.cu", "analysis.cu", "skip.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -304,3 +304,48 @@ def sao_params(rng, w, h, lcu_level, p_off=0.1):
                 b = int(rng.integers(0, 29))
                 lcus["offset"][i, c, b:b + 4] = rng.integers(-7, 8, 4)
     return lcus
+
+
+# ---- skip / direct candidates -----------------------------------------------------
+def skip_candidates(rng, width, height, nrefs, per_cu=5, motion=(0, 0), levels=(3, 4, 5, 6), cand_dtype=None):
+    """Candidates for every aligned CU of the given levels inside the
+    picture: first a temporal-style candidate with four quadrant PUs, then
+    single-PU candidates around `motion` (quarter-pel), a third of them
+    bi-predicted from two references, some repeating an earlier candidate's
+    motion (the encoder skips those); header bits 1..12.  Returns
+    (candidates, number of CUs)."""
+    rects = []
+    for lv in levels:
+        S = 1 << lv
+        for y in range(0, height - S + 1, S):
+            for x in range(0, width - S + 1, S):
+                rects.append((x, y, lv))
+    n_cu = len(rects)
+    cands = np.zeros(n_cu * per_cu, cand_dtype)
+    cands["ref"] = -1
+    mx0, my0 = motion
+    k = 0
+    for cu, (x, y, lv) in enumerate(rects):
+        for j in range(per_cu):
+            c = cands[k]
+            c["x"], c["y"], c["size_log2"], c["cu"] = x, y, lv, cu
+            c["rate"] = int(rng.integers(1, 13))
+            if j == 0:
+                c["n_pu"] = 4
+                for q in range(4):
+                    c["ref"][q, 0] = int(rng.integers(0, nrefs))
+                    c["mv"][q, 0] = (mx0 + int(rng.integers(-6, 7)), my0 + int(rng.integers(-6, 7)))
+            elif j >= 3 and rng.random() < 0.3:
+                c["n_pu"] = cands[k - 1]["n_pu"]
+                c["ref"] = cands[k - 1]["ref"]
+                c["mv"] = cands[k - 1]["mv"]
+            else:
+                c["n_pu"] = 1
+                c["ref"][0, 0] = int(rng.integers(0, nrefs))
+                c["mv"][0, 0] = (mx0 + int(rng.integers(-12, 13)), my0 + int(rng.integers(-12, 13)))
+                if nrefs > 1 and rng.random() < 0.35:
+                    c["ref"][0, 1] = int(rng.integers(0, nrefs))
+                    c["mv"][0, 1] = (mx0 + int(rng.integers(-12, 13)), my0 + int(rng.integers(-12, 13)))
+            cands[k] = c
+            k += 1
+    return cands, n_cu
