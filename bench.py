@@ -98,6 +98,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch / step
+# of the dominant kernels at the default configurations, from one ncu capture
+# of each workload; None for other configurations
+MEASURED_TRAFFIC = {
+    "me": 15083008 + 5165824,          # fs_ctu_kernel<0> + <1>, one picture
+    "tq": 5013000000,                  # tq_chain_kernel, 10^6 blocks (scaled from 10^5)
+    "intra": 39612928 + 31689984,      # rmd_tile_kernel
+    "lookahead": 8306176,              # lookahead_kernel
+    "skip": 104250368 + 4567808,       # skip_cost_kernel
+    "loopfilter": 15775488 + 11389440 + 12672256,   # deblock_ver + deblock_hor + sao_lcu
+}
+
+
+def measured_traffic(name, default_config):
+    return MEASURED_TRAFFIC.get(name) if default_config else None
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -360,7 +377,8 @@ def run_ours(args):
                 "results_equal_device_run": same},
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "fs_ctu_kernel", "achieved": achieved, "peak": peak,
-                     "unit": "Tpx-absdiff/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "Tpx-absdiff/s", "frac": achieved / peak,
+                     "traffic": measured_traffic("me", (WIDTH, HEIGHT, RANGE) == (1920, 1080, 64)),
                      "peak_source": "152 SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % peak_src,
                      "work_per_launch": "%d CTU-ref jobs x %d displacements x 4096 px" % (n_jobs, n_pos),
                      "kernel_ms": ctu_ms},
@@ -565,7 +583,8 @@ def run_tq(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "tq_batch", "achieved": achieved,
                      "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
+                     "frac": achieved / peaks.get("hbm_gbs", 6800.0),
+                     "traffic": measured_traffic("tq", n == 1000000 and args.tq_parts == "0,1,2,3,4"),
                      "peak_source": peak_src, "algorithmic_bytes_per_launch": algo_bytes,
                      "kernel_ms": kernel_ms},
         "sample_bit_exact": exact,
@@ -741,7 +760,8 @@ def run_intra(args):
                 "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "intra_rmd_batch (sort, tiles, candidates)", "achieved": achieved, "peak": peak,
-                     "unit": "T mode-samples/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "T mode-samples/s", "frac": achieved / peak,
+                     "traffic": measured_traffic("intra", (W, H) == (1920, 1080)),
                      "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per mode-sample (%s)"
                                     % (INTRA_OPS_PER_SAMPLE, peak_src),
                      "work_per_launch": "%d blocks, %d mode-samples" % (n, mode_samples), "kernel_ms": kernel_ms},
@@ -911,7 +931,8 @@ def run_loopfilter(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "deblock_ver + deblock_hor + sao_picture",
                      "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None, "peak_source": peak_src,
+                     "frac": achieved / peaks.get("hbm_gbs", 6800.0),
+                     "traffic": measured_traffic("loopfilter", (W, H) == (3840, 2160)), "peak_source": peak_src,
                      "algorithmic_bytes_per_step": int(algo), "kernel_ms": kernel_ms},
         "sample_bit_exact": bool(exact),
         "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "pictures/s", "cores": 1, "kind": "port",
@@ -1042,7 +1063,8 @@ def run_lookahead(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "lookahead_kernel", "achieved": achieved,
                      "peak": peaks.get("hbm_gbs"), "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0),
-                     "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_step": int(algo),
+                     "traffic": measured_traffic("lookahead", (W, H) == (3840, 2160)), "peak_source": peak_src,
+                     "algorithmic_bytes_per_step": int(algo),
                      "kernel_ms": kernel_ms},
         "sample_bit_exact": exact,
         "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "pictures/s", "cores": 1, "kind": "port",
@@ -1225,7 +1247,8 @@ def run_skip(args):
                 "d2h_bytes_per_step": int(12 * n + 4 * n_cu)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "skip_count + skip_scatter + skip_cost + skip_best", "achieved": achieved,
-                     "peak": peak, "unit": "T candidate-samples/s", "frac": achieved / peak, "traffic": None,
+                     "peak": peak, "unit": "T candidate-samples/s", "frac": achieved / peak,
+                     "traffic": measured_traffic("skip", (W, H) == (1920, 1080)),
                      "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per sample (%s)"
                                     % (SKIP_OPS_PER_SAMPLE, peak_src),
                      "work_per_launch": "%d candidates, %d predicted samples" % (n, samples), "kernel_ms": kernel_ms},
