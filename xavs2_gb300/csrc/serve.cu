@@ -138,21 +138,24 @@ __device__ __forceinline__ unsigned long long mixw(uint32_t w, uint64_t i)
     return (unsigned long long)((uint64_t)w + 1) * (unsigned long long)(2 * i + 1);
 }
 
+// The checksum of a picture: sum over its words i (reconstruction, then
+// levels, then search results) of (w_i + 1)(2i + 1) mod 2^64.  The grid is
+// sized for the largest picture of the batch; each region is walked by its
+// own grid-stride loop.
 __global__ void hash_kernel(const JobView *__restrict__ views, const int16_t *__restrict__ coef)
 {
     const JobView &v = views[blockIdx.y];
     const uint64_t nrec = (uint64_t)v.width * v.height / 4;
     const uint64_t ncw = (uint64_t)v.n_coef / 2;
     const uint64_t nres = (uint64_t)v.n_pus * 5;
-    const uint64_t total = nrec + ncw + nres;
     const uint32_t *rec = reinterpret_cast<const uint32_t *>(v.recon);
     const uint32_t *cw = reinterpret_cast<const uint32_t *>(coef + v.coef_off);
     const uint32_t *rw = reinterpret_cast<const uint32_t *>(v.res);
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, step = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long h = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t w = i < nrec ? rec[i] : (i < nrec + ncw ? cw[i - nrec] : rw[i - nrec - ncw]);
-        h += mixw(w, i);
-    }
+    for (uint64_t i = t0; i < nrec; i += step) h += mixw(rec[i], i);
+    for (uint64_t i = t0; i < ncw; i += step) h += mixw(cw[i], nrec + i);
+    for (uint64_t i = t0; i < nres; i += step) h += mixw(rw[i], nrec + ncw + i);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(v.hash, h);
@@ -284,7 +287,14 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
         mc_residual_kernel<<<blocks, 128, 0, b.st>>>(b.d_views, nv, n, s->cfg.qp, b.d_res, b.d_blocks, b.d_choice);
         tq_batch_launch(b.d_blocks, (int)n, b.d_res, b.d_coef, b.d_rres, b.d_nnz, 4, b.st);
         reconstruct_kernel<<<blocks, 128, 0, b.st>>>(b.d_views, nv, n, b.d_choice, b.d_rres);
-        hash_kernel<<<dim3(16, nv), 256, 0, b.st>>>(b.d_views, b.d_coef);
+        int64_t max_words = 0;
+        for (int k = 0; k < nv; k++) {
+            const JobView &v = b.h_views[k];
+            max_words = std::max<int64_t>(max_words, (int64_t)v.width * v.height / 4 + v.n_coef / 2 + 5LL * v.n_pus);
+        }
+        // about 8 words of the largest picture per thread
+        const unsigned hx = (unsigned)std::min<int64_t>(std::max<int64_t>((max_words + 2047) / 2048, 1), 4096);
+        hash_kernel<<<dim3(hx, nv), 256, 0, b.st>>>(b.d_views, b.d_coef);
         count_launch(3);
         XG_CUDA(cudaMemcpyAsync(b.h_hash, b.d_hash, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, b.st));
     }
