@@ -777,6 +777,12 @@ __global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *_
 namespace xg {
 
 // ---- session ---------------------------------------------------------------------
+// default refinement split (pixels): searches of PUs up to this size refine
+// one per thread, larger ones one per warp (xavs2gpu_me_set_tuning changes it)
+#ifndef XG_REFINE_SPLIT
+#define XG_REFINE_SPLIT 256
+#endif
+
 struct MeSessionImpl {
     int W = 0, H = 0, nrefs = 0, max_pus = 0;
     int stride = 0, rows = 0;
@@ -812,7 +818,7 @@ struct MeSessionImpl {
     // launch shapes (results do not depend on them): searches of at most
     // tune_split pixels refine one per thread, larger ones one per warp;
     // tune_block threads per refinement CTA
-    int tune_split = 256, tune_block = 128;
+    int tune_split = XG_REFINE_SPLIT, tune_block = 128;
     // reference slot r lives in plane buffer set slot_buf[r] (rotated by
     // xavs2gpu_me_rotate_refs without moving pixels)
     int slot_buf[16] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15};
