@@ -400,6 +400,21 @@ XAVS2GPU_API int xavs2gpu_sao_picture(uint8_t *dst_y, uint8_t *dst_u, uint8_t *d
                                       int width, int height, int lcu_level, const xavs2gpu_sao_lcu_t *lcus,
                                       int flags, void *stream);
 
+/* Deblocking and SAO of a picture in one pass (both loops of the encoder,
+ * xavs2_lcu_deblock and sao_filter_lcu, over every LCU): dst = SAO of the
+ * deblocked src, written whole; src is left unchanged and must not overlap
+ * dst.  The same per-8x8 edge parameters and per-LCU SAO parameters as
+ * xavs2gpu_deblock_picture / xavs2gpu_sao_picture, one LCU size for both;
+ * the availabilities must be consistent between neighbours (as the
+ * encoder derives them), so that the SAO regions tile the picture.  4:2:0,
+ * device pointers, width and height multiples of 8, LCU 16..64, planes and
+ * strides 4-byte aligned. */
+XAVS2GPU_API int xavs2gpu_loopfilter_picture(const uint8_t *src_y, const uint8_t *src_u, const uint8_t *src_v,
+                                             uint8_t *dst_y, uint8_t *dst_u, uint8_t *dst_v, int stride,
+                                             int stride_c, int width, int height, int lcu_level,
+                                             const xavs2gpu_deblock_scu_t *scus, const xavs2gpu_sao_lcu_t *lcus,
+                                             void *stream);
+
 /* ---- lookahead analysis (mc.c:838-855, pixel.c:1620-1649, rdo.c:3286-3297)
  * lowres_filter (intrinsic_func_t.lowres_filter, primitives.h:140): the
  * width x height output from 2*width x 2*height source samples, each output

@@ -169,3 +169,32 @@ def test_sao_picture_inconsistent_avail(gpu, olib):
     torch.cuda.synchronize()
     for k in range(3):
         assert np.array_equal(dd[k].cpu().numpy(), exp[k]), k
+
+
+@pytest.mark.parametrize("w,h,lcu", [(128, 96, 6), (136, 72, 5), (200, 120, 6), (64, 48, 6), (56, 40, 6),
+                                     (64, 48, 4), (1920, 1080, 6)])
+def test_loopfilter_fused(gpu, olib, w, h, lcu):
+    """Deblocking + SAO in one pass equals the reference's two loops: the
+    picture deblocked in LCU order, then SAO over every LCU region with the
+    deblocked picture as both source and starting destination."""
+    import torch
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(w * 3 + h + lcu)
+    y, u, v, scus = synth.deblock_picture(rng, w, h)
+    lcus = synth.sao_params(rng, w, h, lcu)
+    dy, du, dv = y.copy(), u.copy(), v.copy()
+    olib.xo_deblock_picture(oracle.ptr(dy), w, oracle.ptr(du), oracle.ptr(dv), w // 2, w, h, oracle.ptr(scus), lcu, 1)
+    exp = [dy.copy(), du.copy(), dv.copy()]
+    dptr = (ctypes.c_void_p * 3)(*[oracle.ptr(p).value for p in exp])
+    sptr = (ctypes.c_void_p * 3)(*[oracle.ptr(p).value for p in (dy, du, dv)])
+    olib.xo_sao_picture(dptr, sptr, w, w // 2, w, h, lcu, oracle.ptr(lcus))
+    src = [_dev(p) for p in (y, u, v)]
+    out = [torch.full(p.shape, 7, dtype=torch.uint8, device="cuda") for p in (y, u, v)]
+    ds, dl = _dev(scus.view(np.uint8)), _dev(lcus.view(np.uint8))
+    rc = gpu.xavs2gpu_loopfilter_picture(*[ctypes.c_void_p(t.data_ptr()) for t in src + out], w, w // 2, w, h, lcu,
+                                         ctypes.c_void_p(ds.data_ptr()), ctypes.c_void_p(dl.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert np.array_equal(out[k].cpu().numpy(), exp[k]), k
+        assert np.array_equal(src[k].cpu().numpy(), (y, u, v)[k])   # source untouched

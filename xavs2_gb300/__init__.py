@@ -156,6 +156,7 @@ _SIGS = {
     "xavs2gpu_sao_init": (None, [ctypes.c_uint32, _P]),
     "xavs2gpu_deblock_picture": (_I, [_P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
     "xavs2gpu_lowres_filter": (None, [_P, _I, _P, _I, _I, _I]),
+    "xavs2gpu_loopfilter_picture": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P]),
     "xavs2gpu_skip_costs": (_I, [_P, _P, _I, ctypes.c_double, _I, _P, _P, _P, _P]),
     "xavs2gpu_lowres_picture": (_I, [_P, _I, _P, _I, _I, _I, _P]),
     "xavs2gpu_lookahead_picture": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),

@@ -447,6 +447,162 @@ __global__ void __launch_bounds__(kSaoThreads, 8) sao_lcu_kernel(SaoPic sp)
     }
 }
 
+// ---- fused deblocking + SAO --------------------------------------------------
+// A CTA takes the SAO region of one LCU for one component and produces its
+// final samples in one pass: the region plus an 8-sample margin (clamped to
+// the picture) is loaded into shared memory, the vertical edges and then the
+// horizontal edges whose filter window lies inside the tile are filtered
+// there, and SAO writes the region.  A deblocked sample depends on source
+// samples at most 5 away in each direction and SAO reads 1 around the region,
+// so the margin holds everything the region needs and the result equals the
+// picture-wide two-pass deblocking followed by SAO.
+constexpr int kLfPitch = 96, kLfRows = 88;   // tile: region (<= 68) + 2 x 8
+constexpr int kLfScus = 256;                  // 8x8 blocks the tile touches (<= 15 x 15)
+#ifndef XG_LF_THREADS
+#define XG_LF_THREADS 256
+#endif
+
+struct FusedPic {
+    const uint8_t *src[3];
+    uint8_t *dst[3];
+    int stride, stride_c, width, height, lcu_level, wl, hl, w_scu, n_hor;
+    const xavs2gpu_deblock_scu_t *scus;
+    const xavs2gpu_sao_lcu_t *lcus;
+};
+
+// Per 8x8 block and direction, the edge as one word for the component:
+// bit 0 filter the first half, bit 1 the second half (type and flag
+// combined), alpha in bits 8-15, beta in bits 16-23.
+__device__ __forceinline__ uint32_t edge_word(const xavs2gpu_deblock_scu_t &e, int dir, bool chroma)
+{
+    const bool on = chroma ? e.type[dir] == 2 : e.type[dir] != 0;
+    if (!on) return 0;
+    return (e.flag[dir][0] ? 1u : 0u) | (e.flag[dir][1] ? 2u : 0u) |
+           ((uint32_t)(chroma ? e.alpha_c[dir] : e.alpha[dir]) << 8) |
+           ((uint32_t)(chroma ? e.beta_c[dir] : e.beta[dir]) << 16);
+}
+
+__device__ __forceinline__ void filter_smem_line(uint8_t *s0, int step, uint32_t ew, bool chroma)
+{
+    int p[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) p[k] = s0[k * step];
+    if (filter_line(p, (int)((ew >> 8) & 0xFF), (int)((ew >> 16) & 0xFF), chroma)) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) s0[k * step] = (uint8_t)p[k];
+    }
+}
+
+__global__ void __launch_bounds__(XG_LF_THREADS) loopfilter_lcu_kernel(FusedPic fp)
+{
+    __shared__ __align__(16) uint8_t t[kLfRows][kLfPitch];
+    __shared__ uint32_t ev[kLfScus], eh[kLfScus];   // edge words, vertical / horizontal
+    __shared__ int off[32];
+    const int l = blockIdx.x, c = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+    const bool chroma = c != 0;
+    const int lx = l % fp.wl, ly = l / fp.wl;
+    const xavs2gpu_sao_lcu_t &q = fp.lcus[l];
+    int rx, ry, rw, rh;
+    if (!sao_region(lx, ly, fp.lcu_level, fp.width, fp.height, q.avail, c, rx, ry, rw, rh)) return;
+    const int W = chroma ? fp.width >> 1 : fp.width, H = chroma ? fp.height >> 1 : fp.height;
+    const int st = chroma ? fp.stride_c : fp.stride;
+    const uint8_t *src = c == 0 ? fp.src[0] : c == 1 ? fp.src[1] : fp.src[2];
+    uint8_t *dst = c == 0 ? fp.dst[0] : c == 1 ? fp.dst[1] : fp.dst[2];
+    const int tx0 = max(rx - 8, 0), tx1 = min(rx + rw + 8, W), ty0 = max(ry - 8, 0), ty1 = min(ry + rh + 8, H);
+    const int tw = tx1 - tx0, th = ty1 - ty0, nw = tw >> 2;
+    if (tid < 32) off[tid] = q.offset[c][tid];
+    // edge words of the 8x8 blocks the tile touches
+    const int sh = chroma ? 2 : 3;
+    const int sx0 = tx0 >> sh, sy0 = ty0 >> sh, nsx = ((tx1 - 1) >> sh) - sx0 + 1, nsy = ((ty1 - 1) >> sh) - sy0 + 1;
+    for (int i = tid; i < nsx * nsy; i += nt) {
+        const int r = i / nsx, sx = sx0 + i - r * nsx;
+        const xavs2gpu_deblock_scu_t e = fp.scus[(sy0 + r) * fp.w_scu + sx];
+        ev[i] = edge_word(e, 0, chroma);
+        eh[i] = sx < fp.n_hor ? edge_word(e, 1, chroma) : 0u;
+    }
+    // the tile: a thread keeps one word column and walks the rows
+    {
+        const int w = tid % nw, r0 = tid / nw, rs = nt / nw;
+        if (r0 < rs)
+            for (int r = r0; r < th; r += rs)
+                *reinterpret_cast<uint32_t *>(&t[r][4 * w]) =
+                    *reinterpret_cast<const uint32_t *>(src + (long long)(ty0 + r) * st + tx0 + 4 * w);
+    }
+    __syncthreads();
+    // vertical edges with the whole filter window inside the tile; a thread
+    // keeps one edge and walks the rows
+    {
+        const int ex0 = max(8, (tx0 + 3 + 7) & ~7), ex1 = tx1 - 3;
+        const int nex = ex1 >= ex0 ? (ex1 - ex0) / 8 + 1 : 0;
+        if (nex > 0) {
+            const int e = tid % nex, r0 = tid / nex, rs = nt / nex;
+            const int ex = ex0 + 8 * e, sxl = (ex >> sh) - sx0;
+            if (r0 < rs)
+                for (int r = r0; r < th; r += rs) {
+                    const int y = ty0 + r;
+                    const uint32_t ew = ev[((y >> sh) - sy0) * nsx + sxl];
+                    const int half = chroma ? (y & 3) >= 2 : (y & 7) >= 4;
+                    if ((ew >> half) & 1u) filter_smem_line(&t[r][ex - tx0 - 3], 1, ew, chroma);
+                }
+        }
+    }
+    __syncthreads();
+    // horizontal edges with the whole filter window inside the tile, on the
+    // columns SAO reads (the region and one around it); a thread keeps one
+    // column and walks the edges
+    {
+        const int ey0 = max(8, (ty0 + 3 + 7) & ~7), ey1 = ty1 - 3;
+        const int ney = ey1 >= ey0 ? (ey1 - ey0) / 8 + 1 : 0;
+        const int cx0 = max(rx - 1, tx0), cx1 = min(rx + rw + 1, tx1), ncol = cx1 - cx0;
+        if (ney > 0 && ncol > 0) {
+            const int xi = tid % ncol, j0 = tid / ncol, js = nt / ncol;
+            const int x = cx0 + xi, sxl = (x >> sh) - sx0;
+            const int half = chroma ? (x & 3) >= 2 : (x & 7) >= 4;
+            if (j0 < js)
+                for (int j = j0; j < ney; j += js) {
+                    const int ey = ey0 + 8 * j;
+                    const uint32_t ew = eh[((ey >> sh) - sy0) * nsx + sxl];
+                    if ((ew >> half) & 1u) filter_smem_line(&t[ey - ty0 - 3][x - tx0], kLfPitch, ew, chroma);
+                }
+        }
+    }
+    __syncthreads();
+    // SAO of the region from the deblocked tile; dst written whole; a thread
+    // keeps one word column and walks the rows
+    const int ty = q.type[c], av = full_avail(q.avail), rwords = rw >> 2;
+    const int wi = tid % rwords, r0 = tid / rwords, rs = nt / rwords;
+    if (r0 >= rs) return;
+    for (int yy = r0; yy < rh; yy += rs) {
+        const int x = rx + 4 * wi, y = ry + yy;
+        const uint8_t *d = &t[y - ty0][x - tx0];
+        uint32_t out = *reinterpret_cast<const uint32_t *>(d);
+        int x0 = 0, x1 = 0;
+        if (ty >= 0 && ty <= 4 && sao_row_range(ty, av, yy, rw, rh, x0, x1)) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int xs = x + k - rx;
+                if (xs < x0 || xs >= x1) continue;
+                const int sv = d[k];
+                int cls;
+                if (ty == 4) {
+                    cls = sv >> 3;
+                } else {
+                    int n1, n2;
+                    switch (ty) {
+                    case 0: n1 = d[k - 1]; n2 = d[k + 1]; break;
+                    case 1: n1 = d[k - kLfPitch]; n2 = d[k + kLfPitch]; break;
+                    case 2: n1 = d[k - kLfPitch - 1]; n2 = d[k + kLfPitch + 1]; break;
+                    default: n1 = d[k - kLfPitch + 1]; n2 = d[k + kLfPitch - 1]; break;
+                    }
+                    cls = sign3(sv - n1) + sign3(sv - n2) + 2;
+                }
+                out = set_byte(out, k, min(max(sv + off[cls], 0), 255));
+            }
+        }
+        *reinterpret_cast<uint32_t *>(dst + (long long)y * st + x) = out;
+    }
+}
+
 }  // namespace lf
 }  // namespace xg
 
@@ -599,6 +755,31 @@ extern "C" int xavs2gpu_sao_picture(uint8_t *dst_y, uint8_t *dst_u, uint8_t *dst
     lf::SaoPic sp{{dst_y, dst_u, dst_v}, {src_y, src_u, src_v}, stride, stride_c, width, height, lcu_level,
                   (width + S - 1) / S, (height + S - 1) / S, (flags & XAVS2GPU_SAO_COPY_UNFILTERED) ? 1 : 0, lcus};
     lf::sao_lcu_kernel<<<dim3((unsigned)(sp.wl * sp.hl), 3), lf::kSaoThreads, 0, (cudaStream_t)stream>>>(sp);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+extern "C" int xavs2gpu_loopfilter_picture(const uint8_t *src_y, const uint8_t *src_u, const uint8_t *src_v,
+                                           uint8_t *dst_y, uint8_t *dst_u, uint8_t *dst_v, int stride, int stride_c,
+                                           int width, int height, int lcu_level, const xavs2gpu_deblock_scu_t *scus,
+                                           const xavs2gpu_sao_lcu_t *lcus, void *stream)
+{
+    const void *ptrs[6] = {src_y, src_u, src_v, dst_y, dst_u, dst_v};
+    bool ok = width >= 8 && height >= 8 && !(width & 7) && !(height & 7) && stride >= width &&
+              stride_c >= width / 2 && !(stride & 3) && !(stride_c & 3) && lcu_level >= 4 && lcu_level <= 6 && scus &&
+              lcus;
+    for (int k = 0; k < 6; k++) ok = ok && ptrs[k] && aligned4(ptrs[k]);
+    if (!ok) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_loopfilter_picture",
+             "sizes must be multiples of 8, LCU 16..64, planes and strides 4-byte aligned");
+        return XAVS2GPU_ERR_ARG;
+    }
+    const int S = 1 << lcu_level, w_scu = width / 8;
+    const int n_hor = w_scu <= (1 << (lcu_level - 3)) ? w_scu - 1 : w_scu;
+    lf::FusedPic fp{{src_y, src_u, src_v}, {dst_y, dst_u, dst_v}, stride, stride_c, width, height, lcu_level,
+                    (width + S - 1) / S, (height + S - 1) / S, w_scu, n_hor, scus, lcus};
+    lf::loopfilter_lcu_kernel<<<dim3((unsigned)(fp.wl * fp.hl), 3), XG_LF_THREADS, 0, (cudaStream_t)stream>>>(fp);
     count_launch();
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
