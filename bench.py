@@ -1488,6 +1488,23 @@ def run_chain(args):
         lib.xavs2gpu_me_sync(sess.h)
         assert lib.xavs2gpu_copy_d2h(ctypes.c_void_p(h_out.data_ptr()), ctypes.c_void_p(o.recon), W * H) == 0
     e2e_fps = args.steps / (time.perf_counter() - t0)
+    # phase timing of one eager search of the picture's PUs (the graph's
+    # search kernels), for the roofline of the dominant kernel
+    sess.set_profiling(True)
+    ph = np.zeros(4)
+    for _ in range(3):
+        sess.run(prm)
+        sess.sync()
+        ph += np.array(sess.phase_ms())
+    sess.set_profiling(False)
+    ph /= 3
+    n_ctu_pus, n_gen, n_jobs = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib.xavs2gpu_me_plan_stats(ctypes.c_void_p(sess.h), ctypes.byref(n_ctu_pus), ctypes.byref(n_gen),
+                               ctypes.byref(n_jobs))
+    peaks, peak_src = measured_peaks()
+    ctu_px = n_jobs.value * (2 * R) * (2 * R) * 4096
+    ctu_ach = ctu_px / (ph[1] / 1e3) / 1e12
+    ctu_peak = 152 * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     # CPU baseline: the oracle's search over a sample of the picture's PU
     # searches (the search is ~99 % of the chain's work), scaled to pictures
     evals = count_evals(pus, R)
@@ -1509,6 +1526,11 @@ def run_chain(args):
                                                             "tq_warps": tun.tq_warps, "ms_per_picture": tune_ms}},
         "e2e": {"value": e2e_fps, "unit": "pictures/s", "h2d_bytes_per_step": W * H, "d2h_bytes_per_step": W * H},
         "gpu_launches": int(launches),
+        "roofline": {"bound": "int", "kernel": "fs_ctu_kernel", "achieved": ctu_ach, "peak": ctu_peak,
+                     "unit": "Tpx-absdiff/s", "frac": ctu_ach / ctu_peak, "traffic": None,
+                     "peak_source": "152 SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % peak_src,
+                     "work_per_launch": "%d CTU-ref jobs x %d displacements x 4096 px" % (n_jobs.value, 4 * R * R),
+                     "kernel_ms": float(ph[1]), "eager_search_phases_ms": [float(v) for v in ph]},
         "cpu_baseline": {"value": cpu_fps, "unit": "pictures/s", "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": "oracle search over a random %.3f%% (%d) of the picture's PU searches, scaled"
                                    % (100 * args.cpu_fraction / 8, cpu_n)},
