@@ -51,7 +51,9 @@ def count_evals(pus, R, frac=2, hadamard=1):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """nvidia-smi clock/throttle samples during the timed region.  start()
+    returns once the first sample has arrived, so that a timed region
+    shorter than the sampling interval still has the sample that opens it."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -60,24 +62,38 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
+        self.lines = []
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line)
 
     def start(self):
+        import threading
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
+        t0 = time.time()
+        while not self.lines and self.proc.poll() is None and time.time() - t0 < 10:
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
         try:
-            text, _ = self.proc.communicate(timeout=5)
+            self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-            text, _ = self.proc.communicate()
+            self.proc.wait()
+        self.reader.join(timeout=5)
+        text = "".join(self.lines)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in text.splitlines():
@@ -611,24 +627,29 @@ def intra_workload(rank, width, height):
     src = synth.base_picture(rng, width, height)
     recon = np.clip(src.astype(np.int32) + rng.integers(-3, 4, src.shape), 0, 255).astype(np.uint8)
     rects = synth.intra_level_blocks(width, height)
-    blocks, edges = synth.intra_pack(rects, recon, rng, xg.INTRA_BLOCK_DTYPE)
+    blocks, jobs, size = synth.intra_fill_jobs(rects, width, height, rng, xg.INTRA_BLOCK_DTYPE,
+                                               xg.INTRA_EDGE_JOB_DTYPE)
     prm = xg.IntraParams(np.sqrt(2.0 ** ((QP - 11) / 4.0) * 0.68), 1, 1, synth.INTRA_DIST2, synth.INTRA_DIST1)
-    return src, blocks, edges, prm
+    return src, recon, blocks, jobs, size, prm
 
 
-def cpu_sample_intra(blocks, edges, src, prm, fraction, seed, threads):
-    """The oracle's batched RMD over a random sample of the blocks; returns
-    (mode-samples done, seconds, sample indices, results)."""
+def cpu_sample_intra(blocks, jobs, size, recon, src, prm, fraction, seed, threads):
+    """The oracle's edge filling and batched RMD over a random sample of the
+    blocks; returns (mode-samples done, seconds, sample indices, results)."""
     import oracle
     import xavs2_gb300 as xg
     rng = np.random.default_rng(seed)
     idx = np.nonzero(rng.random(len(blocks)) < fraction)[0]
     sel = np.ascontiguousarray(blocks[idx])
+    sjobs = np.ascontiguousarray(jobs[idx])
+    edges = np.zeros(size, np.uint8)
     out = np.zeros(len(sel), xg.INTRA_RESULT_DTYPE)
+    lib = oracle.lib()
     t0 = time.perf_counter()
-    oracle.lib().xo_intra_rmd_batch(oracle.ptr(sel), len(sel), oracle.ptr(edges), oracle.ptr(src), src.shape[1],
-                                    prm.lambda_, prm.use_hadamard, prm.rough, prm.dist2, prm.dist1,
-                                    oracle.ptr(out), threads)
+    lib.xo_intra_fill_edges(oracle.ptr(sjobs), len(sjobs), oracle.ptr(recon), recon.shape[1], recon.shape[1],
+                            recon.shape[0], oracle.ptr(edges), size)
+    lib.xo_intra_rmd_batch(oracle.ptr(sel), len(sel), oracle.ptr(edges), oracle.ptr(src), src.shape[1],
+                           prm.lambda_, prm.use_hadamard, prm.rough, prm.dist2, prm.dist1, oracle.ptr(out), threads)
     dt = time.perf_counter() - t0
     done = int((sel["width"].astype(np.int64) * sel["height"]).sum()) * 33
     return done, dt, idx, out
@@ -640,23 +661,25 @@ def run_intra(args):
 
     rank, world, local = dist_env()
     W, H = args.width, args.height
-    src, blocks, edges, prm = intra_workload(rank, W, H)
+    src, recon, blocks, jobs, esize, prm = intra_workload(rank, W, H)
     n = len(blocks)
     mode_samples = int((blocks["width"].astype(np.int64) * blocks["height"]).sum()) * 33
     cfg = {"workload": "intra_rmd_1080p_all_levels", "width": W, "height": H, "blocks": n,
            "shapes": "64x64,32x32,16x16,8x8,4x4,32x8,8x32,16x4,4x16 tiling the picture", "qp": QP,
            "rough": {"dist2": prm.dist2, "dist1": prm.dist1}, "cost": "SATD",
            "content": "blurred-noise picture, edges from a +-3 noisy reconstruction",
+           "edges": "built on the device from the reconstruction each step (fill_reference_samples, "
+                    "encoder availability: picture bounds + z-scan within the 64x64 LCU)",
            "l2": "flushed between steps (512 MB write)"}
     if args.impl == "reference":
         if rank != 0:
             return
         threads = os.cpu_count() or 1
         frac = min(1.0, 8 * args.cpu_fraction)
-        cpu_sample_intra(blocks, edges, src, prm, frac / 4, 100, threads)
+        cpu_sample_intra(blocks, jobs, esize, recon, src, prm, frac / 4, 100, threads)
         done, tt = 0, 0.0
         for i in range(args.steps):
-            k, dt, *_ = cpu_sample_intra(blocks, edges, src, prm, frac, 200 + i, threads)
+            k, dt, *_ = cpu_sample_intra(blocks, jobs, esize, recon, src, prm, frac, 200 + i, threads)
             done += k
             tt += dt
         value = done / tt
@@ -665,8 +688,9 @@ def run_intra(args):
                           "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
                           "cpu_baseline": {"value": value, "unit": "mode-samples/s", "cores": threads,
-                                           "kind": "port", "sample": "per step a random %.2f%% of the %d blocks"
-                                                                     % (100 * frac, n)},
+                                           "kind": "port",
+                                           "sample": "per step a random %.2f%% of the %d blocks (edge fill + RMD)"
+                                                     % (100 * frac, n)},
                           "e2e": {"value": value, "unit": "mode-samples/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}))
         return
@@ -679,17 +703,26 @@ def run_intra(args):
     lib.xavs2gpu_init(local)
     dev = torch.device("cuda", local)
     h_blocks = torch.from_numpy(blocks.view(np.uint8).copy()).pin_memory()
-    h_edges = torch.from_numpy(edges).pin_memory()
+    h_jobs = torch.from_numpy(jobs.view(np.uint8).copy()).pin_memory()
+    h_recon = torch.from_numpy(np.ascontiguousarray(recon).reshape(-1)).pin_memory()
     h_src = torch.from_numpy(np.ascontiguousarray(src).reshape(-1)).pin_memory()
     out_bytes = n * xg.INTRA_RESULT_DTYPE.itemsize
     h_out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
-    d_blocks, d_edges, d_src = h_blocks.to(dev), h_edges.to(dev), h_src.to(dev)
+    d_blocks, d_jobs, d_recon, d_src = h_blocks.to(dev), h_jobs.to(dev), h_recon.to(dev), h_src.to(dev)
+    d_edges = torch.zeros(esize, dtype=torch.uint8, device=dev)
     d_out = torch.empty(out_bytes, dtype=torch.uint8, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(dev)
     rmd = lib.xavs2gpu_intra_rmd_batch
+    fill = lib.xavs2gpu_intra_fill_edges
+
+    def fill_step(s):
+        rc = fill(ctypes.c_void_p(d_jobs.data_ptr()), n, ctypes.c_void_p(d_recon.data_ptr()), W, W, H,
+                  ctypes.c_void_p(d_edges.data_ptr()), esize, ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0
 
     def step(s):
+        fill_step(s)
         rc = rmd(ctypes.c_void_p(d_blocks.data_ptr()), n, ctypes.c_void_p(d_edges.data_ptr()),
                  ctypes.c_void_p(d_src.data_ptr()), W, ctypes.byref(prm), ctypes.c_void_p(d_out.data_ptr()),
                  ctypes.c_void_p(s.cuda_stream))
@@ -722,18 +755,31 @@ def run_intra(args):
     total_ms = reduce_max(float(sum(step_ms)), dev)
     value = mode_samples * world * args.steps / (total_ms / 1e3)
     kernel_ms = float(np.median(step_ms))
+    # the edge filling alone (events around it, L2 flushed before each)
+    f0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    f1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            f0[i].record(stream)
+            fill_step(stream)
+            f1[i].record(stream)
+    barrier()
+    fill_ms = float(np.median([x.elapsed_time(y) for x, y in zip(f0, f1)]))
     if args.quick:
         if rank == 0:
-            print(json.dumps({"metric": INTRA_METRIC, "value": value, "ms_per_step": kernel_ms, "blocks": n}))
+            print(json.dumps({"metric": INTRA_METRIC, "value": value, "ms_per_step": kernel_ms, "fill_ms": fill_ms,
+                              "blocks": n}))
         return
 
-    # end to end with host buffers: descriptors, edges and source in, results out
+    # end to end with host buffers: descriptors, reconstruction and source in, results out
     barrier()
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for i in range(args.steps):
             d_blocks.copy_(h_blocks, non_blocking=True)
-            d_edges.copy_(h_edges, non_blocking=True)
+            d_jobs.copy_(h_jobs, non_blocking=True)
+            d_recon.copy_(h_recon, non_blocking=True)
             d_src.copy_(h_src, non_blocking=True)
             step(stream)
             h_out.copy_(d_out, non_blocking=True)
@@ -744,30 +790,38 @@ def run_intra(args):
     if rank != 0:
         return
     got = h_out.numpy().view(xg.INTRA_RESULT_DTYPE)
-    done, cpu_s, idx, want = cpu_sample_intra(blocks, edges, src, prm, args.cpu_fraction, 7, os.cpu_count() or 1)
+    import oracle
+    want_edges = np.zeros(esize, np.uint8)
+    oracle.lib().xo_intra_fill_edges(oracle.ptr(jobs), n, oracle.ptr(recon), W, W, H, oracle.ptr(want_edges), esize)
+    edges_exact = bool(np.array_equal(d_edges.cpu().numpy(), want_edges))
+    done, cpu_s, idx, want = cpu_sample_intra(blocks, jobs, esize, recon, src, prm, args.cpu_fraction, 7,
+                                              os.cpu_count() or 1)
     exact = bool(np.array_equal(got[idx]["cost"], want["cost"]) and
                  np.array_equal(got[idx]["cand_mode"], want["cand_mode"]) and
                  np.array_equal(got[idx]["num_for_rdo"], want["num_for_rdo"]))
     peaks, peak_src = measured_peaks()
-    achieved = mode_samples / (kernel_ms / 1e3) / 1e12
+    rmd_ms = max(kernel_ms - fill_ms, 1e-6)
+    achieved = mode_samples / (rmd_ms / 1e3) / 1e12
     peak = 152 * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / INTRA_OPS_PER_SAMPLE / 1e12
     line = {
         "metric": INTRA_METRIC, "value": value, "unit": "mode-samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
         "e2e": {"value": e2e, "unit": "mode-samples/s",
-                "h2d_bytes_per_step": int(h_blocks.numel() + h_edges.numel() + h_src.numel()),
+                "h2d_bytes_per_step": int(h_blocks.numel() + h_jobs.numel() + h_recon.numel() + h_src.numel()),
                 "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": int(launches),
+        "fill_edges_ms": fill_ms, "edges_bit_exact": edges_exact,
         "roofline": {"bound": "int", "kernel": "intra_rmd_batch (sort, tiles, candidates)", "achieved": achieved, "peak": peak,
                      "unit": "T mode-samples/s", "frac": achieved / peak,
                      "traffic": measured_traffic("intra", (W, H) == (1920, 1080)),
                      "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per mode-sample (%s)"
                                     % (INTRA_OPS_PER_SAMPLE, peak_src),
-                     "work_per_launch": "%d blocks, %d mode-samples" % (n, mode_samples), "kernel_ms": kernel_ms},
+                     "work_per_launch": "%d blocks, %d mode-samples" % (n, mode_samples),
+                     "kernel_ms": rmd_ms},
         "sample_bit_exact": exact,
         "cpu_baseline": {"value": done / cpu_s, "unit": "mode-samples/s", "cores": os.cpu_count() or 1,
-                         "kind": "port", "sample": "random %.2f%% (%d) of the blocks, oracle C RMD, OpenMP"
+                         "kind": "port", "sample": "random %.2f%% (%d) of the blocks, oracle C edge fill + RMD, OpenMP"
                                                    % (100 * args.cpu_fraction, len(idx))},
         "clocks": clocks,
     }

@@ -320,6 +320,29 @@ XAVS2GPU_API int xavs2gpu_intra_rmd_batch(const xavs2gpu_intra_block_t *blocks, 
                                           const uint8_t *fenc, int fenc_stride, const xavs2gpu_intra_params_t *prm,
                                           xavs2gpu_intra_result_t *out, void *stream);
 
+/* Edge samples of a batch of blocks from one reconstructed picture, as
+ * fill_reference_samples builds them (intra.c:1580-1860; the encoder's call
+ * fill_ref_samples_luma, md_intra.c:137-160) when every neighbour sample is
+ * the picture's: for each job, edges + edge_offset receives the block's
+ * edge, samples -(height + 11*width/4 + 6) .. width + 11*height/4 + 6 around
+ * it (the window xavs2gpu_intra_rmd_batch reads; beyond the reference's
+ * padding the run's last sample repeats).  avail holds the MD_I_* bits of
+ * get_intra_neighbors (md_intra.c:60-83): bit 0 left, 1 top, 2 left-down,
+ * 3 top-right, 4 top-left; a side whose samples are not inside the
+ * width x height picture is treated as missing.  Jobs with an invalid shape
+ * (as for the RMD batch) or a window outside [0, edges_size) are skipped.
+ * Device pointers; the jobs are independent and run in parallel, so windows
+ * must not overlap. */
+typedef struct xavs2gpu_intra_edge_job {
+    int64_t edge_offset;     /* the block's top-left edge sample in edges */
+    int32_t x, y;            /* the block's top-left sample in the picture */
+    int16_t width, height;
+    int32_t avail;           /* MD_I_* availability bits */
+} xavs2gpu_intra_edge_job_t;
+XAVS2GPU_API int xavs2gpu_intra_fill_edges(const xavs2gpu_intra_edge_job_t *jobs, int n, const uint8_t *pic,
+                                           int stride, int width, int height, uint8_t *edges, int64_t edges_size,
+                                           void *stream);
+
 /* ---- in-loop filters (primitives.h:202-208; filter_deblock.c, filter_sao.c)
  * Deblocking of one edge: src is the first sample on the Q side (right of a
  * vertical edge, below a horizontal one); 8 lines for luma, 4 per chroma

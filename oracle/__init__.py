@@ -107,6 +107,8 @@ _ORACLE_SIGS = {
     "xo_me_search_list": (None, [_P, _P, _I, _P, _S, _P, _S, _P, _I]),
     "xo_pu_set_limits": (None, [_P, _I, _I, _I, _I]),
     "xo_intra_pred": (None, [_I, _P, _P, _I, _I, _I, _I]),
+    "xo_intra_fill_edge": (None, [_P, _I, _I, _I, _I, _I, _I, _P]),
+    "xo_intra_fill_edges": (None, [_P, _I, _P, _I, _I, _I, _P, ctypes.c_int64]),
     "xo_intra_mode_costs": (None, [_P, _P, _I, _I, _I, _I, _P, ctypes.c_double, _I, _P]),
     "xo_intra_candidates": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "xo_intra_rmd_batch": (None, [_P, _I, _P, _P, _I, ctypes.c_double, _I, _I, _I, _I, _P, _I]),

@@ -1753,3 +1753,72 @@ void xo_skip_costs(const uint8_t *cur, int cur_stride, const uint8_t *const *pla
             }
     }
 }
+
+/* fill_reference_samples_{0,x,y,xy}_c (intra.c:1580-1860) with the neighbour
+ * samples taken from one picture (the four variants differ only in whether
+ * the top row / left column come from the CTU's border buffers or from the
+ * CTU's reconstruction) */
+void xo_intra_fill_edge(const uint8_t *pic, int stride, int x0, int y0, int bsx, int bsy, int avail, uint8_t *ep)
+{
+    const int L = avail & 1, T = (avail >> 1) & 1, LD = (avail >> 2) & 1, TR = (avail >> 3) & 1, TL = (avail >> 4) & 1;
+    const uint8_t *top = pic + (intptr_t)(y0 - 1) * stride + x0 - 1;   /* top[k] = edge sample k > 0 */
+    int k, npad;
+    for (k = -2 * bsy; k <= 2 * bsx; k++) ep[k] = 128;               /* g_dc_value, 8-bit */
+    if (T)
+        for (k = 1; k <= bsx; k++) ep[k] = top[k];
+    for (k = bsx + 1; k <= 2 * bsx; k++) ep[k] = TR ? top[k] : ep[bsx];
+    npad = bsy * 11 / 4 - bsx + 4;
+    for (k = 1; k <= npad; k++) ep[2 * bsx + k] = ep[2 * bsx];
+    if (L)
+        for (k = 1; k <= bsy; k++) ep[-k] = pic[(intptr_t)(y0 + k - 1) * stride + x0 - 1];
+    for (k = bsy + 1; k <= 2 * bsy; k++) ep[-k] = LD ? pic[(intptr_t)(y0 + k - 1) * stride + x0 - 1] : ep[-bsy];
+    if (TL) ep[0] = top[0];
+    else if (T) ep[0] = top[1];
+    else if (L) ep[0] = pic[(intptr_t)y0 * stride + x0 - 1];
+    npad = bsx * 11 / 4 - bsy + 4;
+    for (k = 1; k <= npad; k++) ep[-2 * bsy - k] = ep[-2 * bsy];
+}
+
+static int xo_side_log(int v)
+{
+    int l;
+    for (l = 2; l <= 6; l++)
+        if (v == (1 << l)) return l;
+    return -1;
+}
+
+/* the picture-bounds part of is_block_available (md_intra.c:44-56) applied
+ * to each side's samples */
+static int xo_usable_sides(int avail, int x, int y, int bsx, int bsy, int width, int height)
+{
+    const int l = x >= 1 && y >= 0 && y + bsy <= height, t = y >= 1 && x >= 0 && x + bsx <= width;
+    int ok = (l ? 1 : 0) | (t ? 2 : 0);
+    if (l && y + 2 * bsy <= height) ok |= 4;
+    if (t && x + 2 * bsx <= width) ok |= 8;
+    if (l && t) ok |= 16;
+    return avail & ok;
+}
+
+void xo_intra_fill_edges(const xo_intra_edge_job_t *jobs, int n, const uint8_t *pic, int stride, int width, int height,
+                         uint8_t *edges, int64_t edges_size)
+{
+    int i, k;
+    uint8_t buf[1024];
+    for (i = 0; i < n; i++) {
+        const xo_intra_edge_job_t *j = &jobs[i];
+        const int bsx = j->width, bsy = j->height, a = xo_side_log(bsx), c = xo_side_log(bsy);
+        int lo, hi, lo_ref, hi_ref;
+        if (a < 0 || c < 0 || a - c > 2 || c - a > 2) continue;
+        lo = bsy + 11 * bsx / 4 + 6;
+        hi = bsx + 11 * bsy / 4 + 6;
+        if (j->edge_offset < lo || j->edge_offset > edges_size - 1 - hi) continue;
+        xo_intra_fill_edge(pic, stride, j->x, j->y, bsx, bsy,
+                           xo_usable_sides(j->avail, j->x, j->y, bsx, bsy, width, height), buf + 512);
+        /* last sample the reference writes on each side */
+        hi_ref = 2 * bsx + (bsy * 11 / 4 - bsx + 4 > 0 ? bsy * 11 / 4 - bsx + 4 : 0);
+        lo_ref = 2 * bsy + (bsx * 11 / 4 - bsy + 4 > 0 ? bsx * 11 / 4 - bsy + 4 : 0);
+        for (k = hi_ref + 1; k <= hi; k++) buf[512 + k] = buf[512 + hi_ref];
+        for (k = lo_ref + 1; k <= lo; k++) buf[512 - k] = buf[512 - lo_ref];
+        memcpy(edges + j->edge_offset - lo, buf + 512 - lo, (size_t)(lo + hi + 1));
+    }
+}

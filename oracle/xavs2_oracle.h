@@ -172,6 +172,24 @@ void xo_pu_set_limits(xo_pu_t *pu, int width, int height, int vmin_qpel, int vma
  * around ep (ep[0] top-left, ep[1..] top / top-right, ep[-1..] left /
  * left-down); dc_avail = (top available << 8) | left available. */
 void xo_intra_pred(int mode, const uint8_t *ep, uint8_t *dst, int i_dst, int dc_avail, int bsx, int bsy);
+/* The edge samples of a bsx x bsy block at (x0, y0) of a picture, as
+ * fill_reference_samples builds them (intra.c:1580-1860) when its neighbour
+ * samples are the picture's: avail bits 0 left, 1 top, 2 left-down, 3
+ * top-right, 4 top-left (MD_I_*); ep is the top-left edge sample. */
+void xo_intra_fill_edge(const uint8_t *pic, int stride, int x0, int y0, int bsx, int bsy, int avail, uint8_t *ep);
+/* A batch of xo_intra_fill_edge over one picture (job layout of
+ * xavs2gpu_intra_edge_job_t): the window -(h + 11w/4 + 6) .. w + 11h/4 + 6
+ * around each edge_offset, beyond the reference's padding repeating the
+ * run's last sample; sides outside the picture count as missing; jobs with
+ * an invalid shape or window outside [0, edges_size) are skipped. */
+typedef struct {
+    int64_t edge_offset;
+    int32_t x, y;
+    int16_t width, height;
+    int32_t avail;
+} xo_intra_edge_job_t;
+void xo_intra_fill_edges(const xo_intra_edge_job_t *jobs, int n, const uint8_t *pic, int stride, int width, int height,
+                         uint8_t *edges, int64_t edges_size);
 /* lambda * mode bits + SATD (hadamard) or SAD of every mode's prediction. */
 void xo_intra_mode_costs(const uint8_t *ep, const uint8_t *fenc, int i_fenc, int bsx, int bsy, int dc_avail,
                          const int mpm[2], double lambda, int hadamard, double cost[33]);

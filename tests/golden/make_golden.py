@@ -40,6 +40,28 @@ def intra_edges(rng):
     return [a, b, c]
 
 
+def intra_fill_picture():
+    """272x272 picture for the edge-fill digests (a closed formula, so the
+    fixture stores only digests)."""
+    y, x = np.mgrid[0:272, 0:272]
+    return ((x * 37 + y * 101 + (x * y) // 3) % 251).astype(np.uint8)
+
+
+def intra_fill_windows(fill, bw, bh):
+    """The edges of a bw x bh block at (72, 72) of intra_fill_picture for
+    availability masks 0..31, the window the reference writes
+    (-(bh + 11*bw/4 + 4) .. bw + 11*bh/4 + 4), concatenated; fill(pic, ep,
+    avail) writes one edge around ep (an index into a 1024-sample array)."""
+    pic = intra_fill_picture()
+    lo, hi = bh + (11 * bw) // 4 + 4, bw + (11 * bh) // 4 + 4
+    out = []
+    for avail in range(32):
+        buf = np.zeros(1024, np.uint8)
+        fill(pic, buf, avail)
+        out.append(buf[512 - lo:512 + hi + 1])
+    return np.concatenate(out)
+
+
 def intra_prefill(bw, bh):
     """Destination with stride bw + 8, pre-filled so that samples a mode
     leaves alone are visible."""
@@ -163,6 +185,15 @@ def main():
                 r.xr_intra_pred(mode, ptr(edge, 256), ptr(dst), bw + 8, dir_mode, bw, bh)
                 dig[e, s_, m] = hashlib.sha256(dst.tobytes()).hexdigest()
     g["intra_edges"], g["intra_sha"] = np.stack(edges), dig
+
+    # --- intra edge filling: a block inside a picture, every availability
+    fill_dig = []
+    for bw, bh in INTRA_SHAPES:
+        def fill(pic, buf, avail, bw=bw, bh=bh):
+            ptl = ptr(pic, 71 * 272 + 71)
+            r.xr_intra_fill_edge(3, ptl, 272, ptr(buf, 512), ptr(buf, 512), avail, bw, bh)
+        fill_dig.append(hashlib.sha256(intra_fill_windows(fill, bw, bh).tobytes()).hexdigest())
+    g["intra_fill_sha"] = np.array(fill_dig)
 
     np.savez_compressed(OUT, **g)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

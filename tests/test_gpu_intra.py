@@ -176,3 +176,82 @@ def test_intra_rmd_every_shape(gpu, olib):
         cost, modes, ccost, nrdo = _rmd_expected(olib, blocks, edges, src, prm)
         assert np.array_equal(got["cost"], cost), hadamard
         assert np.array_equal(got["cand_mode"], modes) and np.array_equal(got["num_for_rdo"], nrdo)
+
+
+def _fill_gpu(gpu, jobs, pic, size, width=None, height=None, prefill=0):
+    import torch
+    dev = torch.device("cuda:0")
+    d_jobs = torch.from_numpy(jobs.view(np.uint8).copy()).to(dev)
+    d_pic = torch.from_numpy(np.ascontiguousarray(pic)).to(dev)
+    d_edges = torch.full((size,), prefill, dtype=torch.uint8, device=dev)
+    h, w = pic.shape
+    rc = gpu.xavs2gpu_intra_fill_edges(ctypes.c_void_p(d_jobs.data_ptr()), len(jobs), ctypes.c_void_p(d_pic.data_ptr()),
+                                       w, width or w, height or h, ctypes.c_void_p(d_edges.data_ptr()), size, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    return d_edges.cpu().numpy()
+
+
+def _fill_oracle(olib, jobs, pic, size, width=None, height=None, prefill=0):
+    edges = np.full(size, prefill, np.uint8)
+    h, w = pic.shape
+    olib.xo_intra_fill_edges(oracle.ptr(jobs), len(jobs), oracle.ptr(pic), w, width or w, height or h,
+                             oracle.ptr(edges), size)
+    return edges
+
+
+def test_intra_fill_edges(gpu, olib):
+    """Edges of every block of every shape of a 320x256 picture, with the
+    encoder's availability, built on the device from the reconstruction:
+    equal to the oracle's fill_reference_samples; then the rough mode
+    decision on those edges equals the oracle's on the oracle's edges."""
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(31)
+    W, H = 320, 256
+    src = synth.base_picture(rng, W, H)
+    recon = np.clip(src.astype(np.int32) + rng.integers(-5, 6, src.shape), 0, 255).astype(np.uint8)
+    rects = synth.intra_level_blocks(W, H, synth.INTRA_ALL_SHAPES)
+    blocks, jobs, size = synth.intra_fill_jobs(rects, W, H, rng, xg.INTRA_BLOCK_DTYPE, xg.INTRA_EDGE_JOB_DTYPE)
+    assert len(np.unique(jobs["avail"])) > 8
+    got = _fill_gpu(gpu, jobs, recon, size, prefill=0xA5)
+    want = _fill_oracle(olib, jobs, recon, size, prefill=0xA5)
+    assert np.array_equal(got, want)
+    sel = rng.choice(len(blocks), 600, replace=False)
+    prm = xg.IntraParams(9.5, 1, 1, synth.INTRA_DIST2, synth.INTRA_DIST1)
+    res = _rmd_gpu(gpu, blocks[sel], got, src, prm)
+    cost, modes, ccost, nrdo = _rmd_expected(olib, blocks[sel], want, src, prm)
+    assert np.array_equal(res["cost"], cost) and np.array_equal(res["cand_mode"], modes)
+    assert np.array_equal(res["num_for_rdo"], nrdo)
+
+
+def test_intra_fill_edges_edge_cases(gpu, olib):
+    """Empty batch; availability claimed outside the picture (treated as
+    missing), every mask at the picture's corners, a picture smaller than
+    its stride; jobs with a bad shape or a window outside the buffer are
+    skipped (their samples keep the buffer's value)."""
+    import xavs2_gb300 as xg
+    assert gpu.xavs2gpu_intra_fill_edges(None, 0, None, 64, 64, 64, None, 0, None) == 0
+    rng = np.random.default_rng(8)
+    pic = rng.integers(0, 256, (136, 200), dtype=np.uint8)
+    W, H = 184, 128                    # inside a 200-stride, 136-row allocation
+    shapes = [(4, 4), (8, 8), (64, 64), (16, 64), (64, 16), (4, 16), (32, 8)]
+    pos = [(0, 0), (W - 64, 0), (0, H - 64), (W - 64, H - 64), (8, 8), (W - 4, H - 4), (60, 36)]
+    jobs = []
+    off = 256
+    for bw, bh in shapes:
+        for x, y in pos:
+            if x + bw > W or y + bh > H:
+                x, y = min(x, W - bw), min(y, H - bh)
+            for avail in range(32):
+                jobs.append((off, x, y, bw, bh, avail))
+                off += 512
+    bad = [(off, 8, 8, 12, 4, 31), (off + 512, 8, 8, 4, 32, 31), (3, 8, 8, 8, 8, 31),
+           (off + 1024 + 400, 8, 8, 64, 64, 31)]
+    size = off + 1024 + 500
+    arr = np.array(jobs + bad, dtype=[("edge_offset", "<i8"), ("x", "<i4"), ("y", "<i4"), ("width", "<i2"),
+                                      ("height", "<i2"), ("avail", "<i4")]).astype(xg.INTRA_EDGE_JOB_DTYPE)
+    got = _fill_gpu(gpu, arr, pic, size, W, H, prefill=0x3C)
+    want = _fill_oracle(olib, arr, pic, size, W, H, prefill=0x3C)
+    assert np.array_equal(got, want)
+    assert (got[off:] == 0x3C).all() and (got[:100] == 0x3C).all()

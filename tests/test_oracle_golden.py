@@ -136,3 +136,36 @@ def test_deblock_lcu_order_equals_two_passes(olib):
         for a, b in zip(*outs):
             assert np.array_equal(a, b), (w, h, lcu)
         assert not np.array_equal(outs[0][0], y)      # something was filtered
+
+
+def test_intra_fill_edges(olib, g):
+    """Edge filling of a block inside a picture, every availability mask,
+    against digests of the reference's fill_reference_samples; the batch
+    entry writes the same samples and repeats each run's last one out to
+    the RMD window."""
+    import xavs2_gb300 as xg
+    mg = _intra_golden()
+    pic = mg.intra_fill_picture()
+    for s, (bw, bh) in enumerate(mg.INTRA_SHAPES):
+        def fill(p, buf, avail):
+            olib.xo_intra_fill_edge(ptr(p), 272, 72, 72, bw, bh, avail, ptr(buf, 512))
+        win = mg.intra_fill_windows(fill, bw, bh)
+        assert hashlib.sha256(win.tobytes()).hexdigest() == g["intra_fill_sha"][s], (bw, bh)
+        lo, hi = bh + (11 * bw) // 4 + 6, bw + (11 * bh) // 4 + 6
+        jobs = np.zeros(32, xg.INTRA_EDGE_JOB_DTYPE)
+        jobs["edge_offset"] = 512 + 1024 * np.arange(32)
+        jobs["x"], jobs["y"], jobs["width"], jobs["height"], jobs["avail"] = 72, 72, bw, bh, np.arange(32)
+        edges = np.zeros(32 * 1024, np.uint8)
+        olib.xo_intra_fill_edges(ptr(jobs), 32, ptr(pic), 272, 272, 272, ptr(edges), len(edges))
+        rlo, rhi = lo - 2, hi - 2
+        ref = win.reshape(32, rlo + rhi + 1)
+        for a in range(32):
+            ep = 512 + 1024 * a
+            got = edges[ep - lo:ep + hi + 1]
+            assert np.array_equal(got[2:-2], ref[a]), (bw, bh, a)
+            hi_ref = 2 * bw + max(bh * 11 // 4 - bw + 4, 0)
+            lo_ref = 2 * bh + max(bw * 11 // 4 - bh + 4, 0)
+            if hi > hi_ref:
+                assert (edges[ep + hi_ref:ep + hi + 1] == edges[ep + hi_ref]).all()
+            if lo > lo_ref:
+                assert (edges[ep - lo:ep - lo_ref + 1] == edges[ep - lo_ref]).all()

@@ -445,3 +445,64 @@ def test_lowres_filter(olib, rlib):
         olib.xo_lowres_filter(ptr(src), src.shape[1], ptr(a), w + 3, w, h)
         rlib.xr_lowres_filter(ptr(src), src.shape[1], ptr(b), w + 3, w, h)
         assert np.array_equal(a, b), (w, h)
+
+
+def test_intra_fill_edge_restated(olib, rlib):
+    """xo_intra_fill_edge against the reference's fill_edge_f: variant xy
+    (block inside its CTU: neighbours from the reconstruction) and variant 0
+    (block at the CTU's corner: neighbours from the border buffer, here
+    built from the same picture), every availability mask, several shapes."""
+    rng = np.random.default_rng(79)
+    pic = rng.integers(0, 256, (320, 320), dtype=np.uint8)
+    x0, y0 = 120, 96
+    for bw, bh in INTRA_SHAPES:
+        # border buffer of variant 0: [k] = top row (k >= 0, k = 0 the corner), [-j] = left column
+        buf = np.zeros(1024, np.uint8)
+        for k in range(0, 2 * bw + 1):
+            buf[512 + k] = pic[y0 - 1, x0 - 1 + k]
+        for j in range(1, 2 * bh + 1):
+            buf[512 - j] = pic[y0 + j - 1, x0 - 1]
+        for avail in range(32):
+            want = np.zeros(1024, np.uint8)
+            olib.xo_intra_fill_edge(ptr(pic), 320, x0, y0, bw, bh, avail, ptr(want, 512))
+            lo, hi = 512 - (bh + (11 * bw) // 4 + 4), 512 + bw + (11 * bh) // 4 + 4
+            for xy, ptl, lcu in ((3, ptr(pic, (y0 - 1) * 320 + x0 - 1), ptr(buf, 512)),
+                                 (0, ptr(pic, (y0 - 1) * 320 + x0 - 1), ptr(buf, 512))):
+                got = np.zeros(1024, np.uint8)
+                rlib.xr_intra_fill_edge(xy, ptl, 320, lcu, ptr(got, 512), avail, bw, bh)
+                assert np.array_equal(got[lo:hi + 1], want[lo:hi + 1]), (bw, bh, avail, xy)
+
+
+def test_intra_neighbor_rule(rlib):
+    """The synthetic availability (xavs2_gb300.synth.intra_neighbors: picture
+    bounds plus the z-scan of 4x4 units) equals get_intra_neighbors' lookup
+    in the reference's tab_TR_Avail / tab_DL_Avail tables (block_info.c),
+    read from its source, for every block of every shape of a 256x192
+    picture and every LCU size."""
+    import os
+    import re
+    import xavs2_gb300.synth as synth
+    path = os.path.join(oracle.REF_SRC, "common", "block_info.c")
+    src = open(path, encoding="latin-1").read()
+
+    def table(name, n):
+        body = re.search(r"%s\[[^\]]*\] = \{(.*?)\};" % name, src, re.S).group(1)
+        return np.array([int(v) for v in re.findall(r"\b[01]\b", re.sub(r"//.*", "", body))]).reshape(n, n)
+
+    W, H = 256, 192
+    for lcu in (16, 32, 64):
+        n = lcu // 4
+        tr, dl = table("tab_TR_Avail%d" % lcu, n), table("tab_DL_Avail%d" % lcu, n)
+        rects = [(x, y, bw, bh) for bw, bh in synth.INTRA_ALL_SHAPES if bw <= lcu and bh <= lcu
+                 for y in range(0, H - bh + 1, bh) for x in range(0, W - bw + 1, bw)]
+        got = synth.intra_neighbors(rects, W, H, lcu)
+        for (x, y, bw, bh), a in zip(rects, got):
+            x4, y4 = x // 4, y // 4
+
+            def inside(dx, dy):
+                return 0 <= x4 + dx < W // 4 and 0 <= y4 + dy < H // 4
+            ld = inside(-1, bh // 2 - 1) and dl[(y4 % n) + bh // 4 - 1][x4 % n]
+            trr = inside(bw // 2 - 1, -1) and tr[y4 % n][(x4 % n) + bw // 4 - 1]
+            want = int(inside(-1, 0)) | int(inside(0, -1)) << 1 | int(bool(ld)) << 2 | int(bool(trr)) << 3 \
+                | int(inside(-1, -1)) << 4
+            assert want == int(a), (lcu, x, y, bw, bh)

@@ -147,6 +147,7 @@ _SIGS = {
     "xavs2gpu_intra_pred_ang": (None, [_P, _P, _I, _I, _I, _I]),
     "xavs2gpu_intra_pred_init": (None, [ctypes.c_uint32, _P]),
     "xavs2gpu_intra_rmd_batch": (_I, [_P, _I, _P, _P, _I, _P, _P, _P]),
+    "xavs2gpu_intra_fill_edges": (_I, [_P, _I, _P, _I, _I, _I, _P, ctypes.c_int64, _P]),
     "xavs2gpu_deblock_luma_ver": (None, [_P, _I, _I, _I, _P]),
     "xavs2gpu_deblock_luma_hor": (None, [_P, _I, _I, _I, _P]),
     "xavs2gpu_deblock_chroma_ver": (None, [_P, _P, _I, _I, _I, _P]),
@@ -438,6 +439,9 @@ INTRA_BLOCK_DTYPE = np.dtype([("edge_offset", "<i8"), ("fenc_offset", "<i8"), ("
                               ("dc_avail", "<i2"), ("mpm", "i1", (2,)), ("num_for_rdo", "<i4"), ("pad_", "<i4")])
 INTRA_RESULT_DTYPE = np.dtype([("cost", "<f8", (33,)), ("cand_cost", "<f8", (9,)), ("cand_mode", "<i4", (9,)),
                                ("num_for_rdo", "<i4")])
+# xavs2gpu_intra_edge_job_t; avail = MD_I_* bits (0 left, 1 top, 2 left-down, 3 top-right, 4 top-left)
+INTRA_EDGE_JOB_DTYPE = np.dtype([("edge_offset", "<i8"), ("x", "<i4"), ("y", "<i4"), ("width", "<i2"),
+                                 ("height", "<i2"), ("avail", "<i4")])
 
 
 DEBLOCK_SCU_DTYPE = np.dtype([("type", "u1", (2,)), ("flag", "u1", (2, 2)), ("alpha", "u1", (2,)),

@@ -726,10 +726,91 @@ __global__ void __launch_bounds__(128) rmd_cand_kernel(const xavs2gpu_intra_bloc
     }
 }
 
+// ---- edge samples of a batch of blocks from one reconstructed picture ---------------
+// fill_reference_samples_{0,x,y,xy} (intra.c:1580-1860) as the encoder calls
+// them (fill_ref_samples_luma, md_intra.c:137-160) with every neighbour sample
+// in the picture.  The sides a block may use are the availability bits that
+// lie inside the picture (the picture-bounds half of is_block_available,
+// md_intra.c:44-56); a side claimed outside it is treated as missing.
+__device__ __forceinline__ int usable_sides(int avail, int x, int y, int bsx, int bsy, int width, int height)
+{
+    const bool l = x >= 1 && y >= 0 && y + bsy <= height, t = y >= 1 && x >= 0 && x + bsx <= width;
+    int ok = 0;
+    if (l) ok |= 1 << 0;
+    if (t) ok |= 1 << 1;
+    if (l && y + 2 * bsy <= height) ok |= 1 << 2;   // left-down
+    if (t && x + 2 * bsx <= width) ok |= 1 << 3;    // top-right
+    if (l && t) ok |= 1 << 4;                       // top-left
+    return avail & ok;
+}
+
+// A warp per block writes ep[-edge_below .. edge_above]: the top row and
+// top-right run (the last top sample repeated when the top-right is
+// missing), the left column and left-down run likewise, 128 for a missing
+// side, the corner from the top-left, else the first top, else the first
+// left sample, and the padding beyond 2 * bsx / 2 * bsy repeating the run's
+// last sample.
+__global__ void __launch_bounds__(256) fill_edges_kernel(const xavs2gpu_intra_edge_job_t *__restrict__ jobs, int n,
+                                                         const uint8_t *__restrict__ pic, int stride, int width,
+                                                         int height, uint8_t *__restrict__ edges, long long edges_size)
+{
+    const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const xavs2gpu_intra_edge_job_t j = jobs[w];
+    const int bsx = j.width, bsy = j.height, a = side_log(bsx), c = side_log(bsy);
+    if (a < 0 || c < 0 || a - c > 2 || c - a > 2) return;
+    const int lo = edge_below(bsx, bsy), hi = edge_above(bsx, bsy);
+    if (j.edge_offset < lo || j.edge_offset > edges_size - 1 - hi) return;
+    const int av = usable_sides(j.avail, j.x, j.y, bsx, bsy, width, height);
+    const bool L = av & 1, T = av & 2, LD = av & 4, TR = av & 8, TL = av & 16;
+    const long long row = (long long)(j.y - 1) * stride + j.x - 1;   // the corner's position
+    uint8_t *ep = edges + j.edge_offset;
+    for (int k = -lo + lane; k <= hi; k += 32) {
+        int v = 128;
+        if (k > 0) {
+            const int kk = min(k, 2 * bsx);
+            if (kk <= bsx) {
+                if (T) v = pic[row + kk];
+            } else if (TR) {
+                v = pic[row + kk];
+            } else if (T) {
+                v = pic[row + bsx];
+            }
+        } else if (k < 0) {
+            const int jj = min(-k, 2 * bsy);
+            if (jj <= bsy) {
+                if (L) v = pic[row + (long long)jj * stride];
+            } else if (LD) {
+                v = pic[row + (long long)jj * stride];
+            } else if (L) {
+                v = pic[row + (long long)bsy * stride];
+            }
+        } else {
+            v = TL ? pic[row] : T ? pic[row + 1] : L ? pic[row + stride] : 128;
+        }
+        ep[k] = (uint8_t)v;
+    }
+}
+
 }  // namespace intra
 }  // namespace xg
 
 using namespace xg;
+
+extern "C" int xavs2gpu_intra_fill_edges(const xavs2gpu_intra_edge_job_t *jobs, int n, const uint8_t *pic, int stride,
+                                         int width, int height, uint8_t *edges, int64_t edges_size, void *stream)
+{
+    if (n < 0 || width < 1 || height < 1 || stride < width || edges_size < 0 || (n > 0 && (!jobs || !pic || !edges))) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_intra_fill_edges", "bad count, size or pointer");
+        return XAVS2GPU_ERR_ARG;
+    }
+    if (n == 0) return XAVS2GPU_OK;
+    intra::fill_edges_kernel<<<(unsigned)((n + 7) / 8), 256, 0, (cudaStream_t)stream>>>(jobs, n, pic, stride, width,
+                                                                                         height, edges, edges_size);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
 
 // ---- per-call drop-ins (intra_pred_t, primitives.h:84) -----------------------------
 static void intra_call(int mode, uint8_t *src, uint8_t *dst, int i_dst, int dir_mode, int bsx, int bsy)

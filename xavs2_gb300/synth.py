@@ -230,6 +230,68 @@ def intra_blocks(rng, src, recon, all_shapes=False, block_dtype=None):
     return intra_pack(rects, recon, rng, block_dtype)
 
 
+def _zorder(ux, uy):
+    r = np.zeros_like(ux)
+    for b in range(5):
+        r |= ((ux >> b) & 1) << (2 * b) | ((uy >> b) & 1) << (2 * b + 1)
+    return r
+
+
+def intra_neighbors(rects, width, height, lcu_size=64):
+    """MD_I_* availability of blocks (x0, y0, w, h) of a one-slice picture as
+    get_intra_neighbors derives it (md_intra.c:60-83): a side is available
+    when its last 4x4 unit lies inside the picture and, for the top-right and
+    left-down runs, when it precedes the block in the z-scan of 4x4 units
+    within the LCU (the rule the tab_TR_Avail / tab_DL_Avail tables of
+    block_info.c:50-160 hold; the row above the LCU counts as coded, the LCU
+    to the right and the row below it as not)."""
+    rects = np.asarray(rects, np.int64).reshape(-1, 4)
+    x, y, w, h = rects.T
+    n = lcu_size // 4
+    left = x >= 4
+    top = y >= 4
+    tl = left & top
+    # the top-right run's last unit, the left-down run's last unit
+    tr = top & (x + 2 * w - 4 < width)
+    ld = left & (y + 2 * h - 4 < height)
+    ux, uy = ((x + w) // 4 - 1) % n, (y // 4) % n                    # the block's top-right 4x4 unit
+    tr_z = np.where(uy == 0, True, np.where(ux == n - 1, False, _zorder(ux + 1, uy - 1) < _zorder(ux, uy)))
+    vx, vy = (x // 4) % n, ((y + h) // 4 - 1) % n                    # the block's bottom-left 4x4 unit
+    ld_z = np.where(vy == n - 1, False, np.where(vx == 0, True, _zorder(vx - 1, vy + 1) < _zorder(vx, vy)))
+    return (left.astype(np.int32) | top << 1 | (ld & ld_z) << 2 | (tr & tr_z) << 3 | tl << 4).astype(np.int32)
+
+
+def intra_fill_jobs(rects, width, height, rng, block_dtype, job_dtype, lcu_size=64):
+    """Descriptors for building every block's edge on the device from a
+    reconstructed picture (xavs2gpu_intra_fill_edges) and for the RMD batch
+    that reads them: each window 16-byte aligned in an edge buffer of
+    `size` bytes, availability from intra_neighbors, the DC availability
+    word from its top / left bits, random MPMs.  Returns (blocks, jobs, size)."""
+    rects = np.asarray(rects, np.int64).reshape(-1, 4)
+    n = len(rects)
+    win = np.array([intra_edge_window(int(w), int(h)) for _, _, w, h in rects], np.int64).reshape(-1, 2)
+    size = (win[:, 0] + win[:, 1] + 1 + 15) // 16 * 16
+    start = np.cumsum(size) - size
+    avail = intra_neighbors(rects, width, height, lcu_size)
+    jobs = np.zeros(n, job_dtype)
+    jobs["edge_offset"] = start + win[:, 0]
+    jobs["x"], jobs["y"] = rects[:, 0], rects[:, 1]
+    jobs["width"], jobs["height"] = rects[:, 2], rects[:, 3]
+    jobs["avail"] = avail
+    blocks = np.zeros(n, block_dtype)
+    blocks["edge_offset"] = jobs["edge_offset"]
+    blocks["fenc_offset"] = rects[:, 1] * width + rects[:, 0]
+    blocks["width"], blocks["height"] = rects[:, 2], rects[:, 3]
+    blocks["dc_avail"] = (((avail >> 1) & 1) << 8) | (avail & 1)
+    m0 = rng.integers(0, 33, n)
+    m1 = rng.integers(0, 32, n)
+    blocks["mpm"][:, 0] = m0
+    blocks["mpm"][:, 1] = m1 + (m1 >= m0)
+    level = np.log2(np.maximum(rects[:, 2], rects[:, 3])).astype(int)
+    blocks["num_for_rdo"] = np.array([INTRA_RDO_NUM.get(v, 6) for v in range(7)])[level]
+    return blocks, jobs, int(size.sum())
+
+
 def intra_level_blocks(width, height, shapes=None):
     """Every block an encoder's intra mode decision visits on a picture: the
     CUs of each level (64 .. 8) that lie inside it, the 4x4 blocks, and the
