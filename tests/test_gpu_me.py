@@ -150,3 +150,31 @@ def test_pinned_host_pictures_and_results(gpu):
     assert got.tobytes() == want.tobytes()
     s.close()
     s2.close()
+
+
+@pytest.mark.parametrize("had,frac,fast,pmvr", [(1, 2, 0, 0), (0, 2, 0, 0), (1, 1, 0, 0), (1, 2, 1, 0), (0, 0, 0, 0),
+                                                (1, 2, 0, 1)])
+def test_cu_partition_refinement(gpu, olib, had, frac, fast, pmvr):
+    """The partitions of leaf CUs (every mode of 16..64 CUs, 8x8 CUs),
+    searched and refined together per CU (CU-grouped refinement; per-PU
+    kernels with PMVR), predictors varying between the partitions of a CU,
+    content with several motions (partitions that disagree on the centre),
+    duplicated searches (groups split at 32 members): equal to the oracle."""
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(300 + 8 * had + 4 * frac + 2 * fast + pmvr)
+    w, h = 256, 192
+    f0 = synth.base_picture(rng, w, h)
+    f1 = synth.next_picture(rng, f0, 6, 6)
+    f2 = synth.next_picture(rng, f1, 6, 6)
+    pus, _ = xg.cu_pus(xg.split_map_cus(w, h, 17), w, h, 2)
+    pus["mvp_x"] = rng.integers(-12, 13, len(pus))
+    pus["mvp_y"] = rng.integers(-12, 13, len(pus))
+    pus = xg.set_limits(pus, w, h)
+    big = np.nonzero(np.array(xg.PU_W)[pus["part"]] == 64)[0][:1]
+    dup = np.repeat(pus[big], 40) if len(big) else pus[:0]
+    allp = np.concatenate([pus, pus[:200], dup])
+    prm = xg.MeParams(10, oracle.lambda_factor(30), had, frac, fast, pmvr)
+    got, _ = _run(f2, [f1, f0], allp, prm)
+    exp = _oracle(olib, f2, [f1, f0], allp, prm)
+    _assert_same(got, exp, allp)

@@ -18,8 +18,10 @@
 // and refine_kernel.
 #include "xavs2gpu_common.cuh"
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <unordered_map>
 #include <vector>
 
 namespace xg {
@@ -770,6 +772,253 @@ __global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *_
     if (lane == 0) out[i] = res;
 }
 
+// ---- refinement v4: the partitions of one CU together -----------------------------
+// The searches of the canonical partitions of one aligned CU (16x16 and up:
+// 2Nx2N, 2NxN, Nx2N and the four AMP modes) against one reference usually
+// share their integer motion vector and often the half-pel winner.  Their
+// SATD / SAD sums over the same units at the same positions are then the
+// same numbers, so a warp takes all partitions of a CU: per refinement stage
+// it groups the members by their current centre, computes the cost of every
+// unit of the CU that a member of the group covers at each of the stage's
+// positions once (a table in shared memory), sums each member's units, and
+// lets each member pick its winner in the reference's order (the first
+// strictly smaller cost in spiral order).  Unit tilings are the ones the
+// per-PU kernels use: 8x4 units (4x4 for 4-wide and 12x16 PUs with SATD,
+// 4- and 12-wide with SAD), aligned to the CU, since every partition of a
+// CU starts at a multiple of its unit width.
+struct RefineGroup {
+    uint32_t first;     // first member in the member list
+    int16_t cx, cy;     // CU origin
+    uint8_t count;      // members, 1..32
+    uint8_t lg;         // log2 of the CU size, 4..6
+    uint8_t ref;
+    uint8_t pad_;
+};
+constexpr int kGrpWarps = 4;
+constexpr int kGrpMaxPos = 9;
+constexpr int kGrpU8 = 128;   // 8x4 units of a 64x64 CU
+constexpr int kGrpU4 = 16;    // 4x4 units of a 16x16 CU (the only size with 4- or 12-wide partitions)
+
+struct GroupSmem {
+    int t8[kGrpU8][kGrpMaxPos];
+    int t4[kGrpU4][kGrpMaxPos];
+    int16_t rx[32], ry[32], rw[32], rh[32];
+    int8_t ru4[32];
+};
+
+// floor(q / d) for q < 4096, d <= 16, with m = ceil(65536 / d)
+__device__ __forceinline__ int div_small(int q, int m) { return (q * m) >> 16; }
+
+// is unit (x, y, type u4) of the CU inside a member of `grp`?
+__device__ __forceinline__ bool unit_covered(const GroupSmem &S, unsigned grp, int x, int y, int u4)
+{
+    while (grp) {
+        const int m = __ffs(grp) - 1;
+        grp &= grp - 1;
+        if (S.ru4[m] == u4 && x >= S.rx[m] && x < S.rx[m] + S.rw[m] && y >= S.ry[m] && y < S.ry[m] + S.rh[m])
+            return true;
+    }
+    return false;
+}
+
+// Costs of the covered units of one type at the P positions (qpel, absolute)
+// ccx + offx[k], ccy + offy[k].
+template <bool U4>
+__device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had, int cs, const uint8_t *o,
+                                            const uint8_t *const *planes, int stride, int px, int py, int ccx,
+                                            int ccy, const int (&offx)[kGrpMaxPos], const int (&offy)[kGrpMaxPos],
+                                            int P, int lane)
+{
+    constexpr int UW = U4 ? 4 : 8;
+    const int cols = cs / UW, nu = cols * (cs >> 2);
+    const int mcols = (65536 + cols - 1) / cols;
+    int(*T)[kGrpMaxPos] = U4 ? S.t4 : S.t8;
+    if (nu >= 32) {
+        // a lane per unit, its current block loaded once for all positions
+        for (int u = lane; u < nu; u += 32) {
+            const int uy = div_small(u, mcols), ux = u - uy * cols;
+            if (!unit_covered(S, grp, ux * UW, uy * 4, U4)) continue;
+            int c[4][8];
+            const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * UW;
+            load_unit<U4>(o + off, stride, c);
+#pragma unroll
+            for (int k = 0; k < kGrpMaxPos; k++) {
+                if (k < P) {
+                    const int mx = ccx + offx[k], my = ccy + offy[k];
+                    const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(py + (my >> 2)) * stride +
+                                       px + (mx >> 2) + off;
+                    T[u][k] = unit_cost_pre<U4>(had, c, r, stride);
+                }
+            }
+        }
+    } else {
+        // a lane per (unit, position)
+        const int mp = (65536 + P - 1) / P;
+        for (int e = lane; e < nu * P; e += 32) {
+            const int u = div_small(e, mp), k = e - u * P;
+            const int uy = div_small(u, mcols), ux = u - uy * cols;
+            if (!unit_covered(S, grp, ux * UW, uy * 4, U4)) continue;
+            int c[4][8];
+            const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * UW;
+            load_unit<U4>(o + off, stride, c);
+            int dx = offx[0], dy = offy[0];
+#pragma unroll
+            for (int q = 1; q < kGrpMaxPos; q++)
+                if (q == k) { dx = offx[q]; dy = offy[q]; }
+            const int mx = ccx + dx, my = ccy + dy;
+            const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(py + (my >> 2)) * stride + px +
+                               (mx >> 2) + off;
+            T[u][k] = unit_cost_pre<U4>(had, c, r, stride);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kGrpWarps) refine_group_kernel(const RefineGroup *__restrict__ groups,
+                                                                      int ngroups,
+                                                                      const uint32_t *__restrict__ members,
+                                                                      const SessView *__restrict__ views, int R,
+                                                                      xavs2gpu_me_params_t prm)
+{
+    __shared__ GroupSmem smem[kGrpWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gi = blockIdx.x * kGrpWarps + warp;
+    if (gi >= ngroups) return;   // the whole warp
+    GroupSmem &S = smem[warp];
+    const RefineGroup G = groups[gi];
+    const uint32_t e0 = members[G.first];
+    const SessView &v = views[e0 >> kSessShift];
+    const Geometry g = v.g;
+    const int M = G.count, cs = 1 << G.lg;
+    const bool had = prm.use_hadamard != 0;
+    const int lam = prm.lambda_factor;
+    const bool mem = lane < M;
+    int i = 0, pmx = 0, pmy = 0, bx = 0, by = 0, best = 0;
+    bool valid = false;
+    xavs2gpu_me_result_t res;
+    if (mem) {
+        i = (int)(members[G.first + lane] & kIdxMask);
+        const xavs2gpu_pu_t p = v.pus[i];
+        const PuState st = v.state[i];
+        const unsigned long long key = v.keys[i];
+        valid = st.valid && key != kNoKey;
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        S.rx[lane] = (int16_t)(p.x - G.cx);
+        S.ry[lane] = (int16_t)(p.y - G.cy);
+        S.rw[lane] = (int16_t)w;
+        S.rh[lane] = (int16_t)h;
+        S.ru4[lane] = (int8_t)(had ? satd_unit4(w, h) : (w == 4 || w == 12));
+        pmx = p.mvp_x;
+        pmy = p.mvp_y;
+        if (!valid) {
+            res.bmv_x = res.bmv_y = res.imv_x = res.imv_y = 0;
+            res.bcost = res.icost = 1 << 30;
+            res.mvcost = 0;
+            v.res[i] = res;
+        } else {
+            const int icost = (int)(key >> 32);
+            const unsigned order_ = (unsigned)(key & 0xffffffffu);
+            int bmx, bmy;
+            if (order_ < 2) { bmx = st.cand[order_][0]; bmy = st.cand[order_][1]; }
+            else {
+                const int q = (int)order_ - 2;
+                bmx = st.cx + q % (2 * R) - R;
+                bmy = st.cy + q / (2 * R) - R;
+            }
+            res.imv_x = (int16_t)bmx; res.imv_y = (int16_t)bmy; res.icost = icost;
+            bx = bmx * 4; by = bmy * 4; best = icost;
+        }
+    }
+    __syncwarp();
+    const uint8_t *o = v.cur + (ptrdiff_t)G.cy * g.stride + G.cx;
+    const uint8_t *const *planes = v.planes + 16 * G.ref;
+    if (prm.fractional_me) {
+        const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
+        for (int stage = 0; stage < (prm.fractional_me > 1 ? 2 : 1); stage++) {
+            // the stage's positions relative to the centre, in the reference's order
+            int offx[kGrpMaxPos], offy[kGrpMaxPos], P = 0;
+            const int k0 = (stage == 0 && had) ? 1 : 0;
+#pragma unroll
+            for (int k = 0; k < kGrpMaxPos; k++) { offx[k] = 0; offy[k] = 0; }
+            P = k0;
+#pragma unroll
+            for (int pos = 1; pos < 9; pos++) {
+                if ((pos - 1) % step) continue;
+                const int mult = stage == 0 ? 2 : 1;
+#pragma unroll
+                for (int k = 0; k < kGrpMaxPos; k++)
+                    if (k == P) { offx[k] = mult * c_spiral[pat][pos][0]; offy[k] = mult * c_spiral[pat][pos][1]; }
+                P++;
+            }
+            unsigned pending = __ballot_sync(0xffffffffu, mem && valid);
+            while (pending) {
+                const int leader = __ffs(pending) - 1;
+                const int ccx = __shfl_sync(0xffffffffu, bx, leader), ccy = __shfl_sync(0xffffffffu, by, leader);
+                const unsigned grp = __ballot_sync(0xffffffffu, mem && valid && bx == ccx && by == ccy) & pending;
+                pending &= ~grp;
+                const bool need8 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && !S.ru4[lane]);
+                const bool need4 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && S.ru4[lane]);
+                if (need8)
+                    group_table<false>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
+                                       lane);
+                if (need4)
+                    group_table<true>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
+                                      lane);
+                __syncwarp();
+                // each member's sums over its units
+                int acc[kGrpMaxPos];
+#pragma unroll
+                for (int k = 0; k < kGrpMaxPos; k++) acc[k] = 0;
+                for (unsigned left = grp; left;) {
+                    const int m = __ffs(left) - 1;
+                    left &= left - 1;
+                    const int u4 = S.ru4[m], uw = u4 ? 4 : 8;
+                    const int nux = S.rw[m] / uw, n = nux * (S.rh[m] >> 2);
+                    const int mnux = (65536 + nux - 1) / nux, cols = cs / uw;
+                    const int base = (S.ry[m] >> 2) * cols + S.rx[m] / uw;
+                    int part[kGrpMaxPos];
+#pragma unroll
+                    for (int k = 0; k < kGrpMaxPos; k++) part[k] = 0;
+                    for (int q = lane; q < n; q += 32) {
+                        const int qy = div_small(q, mnux), qx = q - qy * nux;
+                        const int u = base + qy * cols + qx;
+                        const int *row = u4 ? S.t4[u] : S.t8[u];
+#pragma unroll
+                        for (int k = 0; k < kGrpMaxPos; k++)
+                            if (k < P) part[k] += row[k];
+                    }
+#pragma unroll
+                    for (int k = 0; k < kGrpMaxPos; k++) {
+                        if (k < P) {
+                            const int t = __reduce_add_sync(0xffffffffu, part[k]);
+                            if (lane == m) acc[k] = t;
+                        }
+                    }
+                }
+                __syncwarp();   // the tables are rebuilt for the next centre
+                if ((grp >> lane) & 1) {
+                    int nbx = bx, nby = by;
+                    if (k0) best = acc[0] + mv_cost_hd(lam, ccx, ccy, pmx, pmy);
+#pragma unroll
+                    for (int k = 0; k < kGrpMaxPos; k++) {
+                        if (k < k0 || k >= P) continue;
+                        const int mx = ccx + offx[k], my = ccy + offy[k];
+                        const int c = acc[k] + mv_cost_hd(lam, mx, my, pmx, pmy);
+                        if (c < best) { best = c; nbx = mx; nby = my; }
+                    }
+                    bx = nbx;
+                    by = nby;
+                }
+            }
+        }
+    }
+    if (mem && valid) {
+        res.bmv_x = (int16_t)bx; res.bmv_y = (int16_t)by;
+        res.bcost = best;
+        res.mvcost = mv_cost_hd(lam, bx, by, pmx, pmy);
+        v.res[i] = res;
+    }
+}
+
 }  // namespace xg
 
 #include "fs_ctu.cuh"
@@ -777,6 +1026,13 @@ __global__ void __launch_bounds__(128) refine_warp_list_kernel(const uint32_t *_
 namespace xg {
 
 // ---- session ---------------------------------------------------------------------
+// CU-grouped refinement on (1) or per-PU kernels only (0); the results are
+// the same either way
+#ifndef XG_REFINE_GROUPS
+#define XG_REFINE_GROUPS 1
+#endif
+static constexpr bool use_groups() { return XG_REFINE_GROUPS != 0; }
+
 // default refinement split (pixels): searches of PUs up to this size refine
 // one per thread, larger ones one per warp (xavs2gpu_me_set_tuning changes it)
 #ifndef XG_REFINE_SPLIT
@@ -826,6 +1082,14 @@ struct MeSessionImpl {
     SessView h_view{};
     SessView *d_view = nullptr;      // this session as the kernels see it
     std::vector<uint32_t> h_generic, h_small, h_large;
+    // CU-grouped refinement: the groups, their members, and the thread /
+    // warp lists of the searches no group covers
+    RefineGroup *d_groups = nullptr;
+    uint32_t *d_members = nullptr;
+    int *d_small_g = nullptr, *d_large_g = nullptr;
+    int n_groups = 0, n_small_g = 0, n_large_g = 0;
+    std::vector<RefineGroup> h_groups;
+    std::vector<uint32_t> h_members, h_small_g, h_large_g;
 
     uint8_t *plane(int idx) { return d_planes + (size_t)idx * plane_bytes + (size_t)kPad * stride + kPad; }
     uint8_t *ref_plane(int slot, int k) { return plane(1 + 16 * slot_buf[slot] + k); }
@@ -910,6 +1174,10 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     XG_CUDA(cudaMalloc((void **)&m.d_tasks, sizeof(RefineTask) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_small, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_large, sizeof(int) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_groups, sizeof(RefineGroup) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_members, sizeof(uint32_t) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_small_g, sizeof(int) * max_pus));
+    XG_CUDA(cudaMalloc((void **)&m.d_large_g, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_view, sizeof(SessView)));
     refresh_view(m);
     XG_CUDA(cudaStreamSynchronize(m.st));
@@ -929,6 +1197,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     cudaFree(m.d_pus); cudaFree(m.d_res); cudaFreeHost(m.h_res); cudaFree(m.d_keys);
     cudaFree(m.d_state); cudaFree(m.d_generic); cudaFree(m.d_order); cudaFree(m.d_tasks);
     cudaFree(m.d_small); cudaFree(m.d_large);
+    cudaFree(m.d_groups); cudaFree(m.d_members); cudaFree(m.d_small_g); cudaFree(m.d_large_g);
     for (auto &e : m.ev)
         if (e) cudaEventDestroy(e);
     if (m.own_st) cudaStreamDestroy(m.own_st);
@@ -1023,6 +1292,82 @@ extern "C" int xavs2gpu_me_set_pus(xavs2gpu_me_session_t *s, const xavs2gpu_pu_t
     return XAVS2GPU_OK;
 }
 
+// Groups the searches that are canonical partitions of an aligned CU of
+// 16x16 or larger by (reference, CU); larger CUs first.  The searches left
+// over keep the thread / warp lists.
+static void build_groups(MeSessionImpl &m, const std::vector<int> &small, const std::vector<int> &large)
+{
+    std::unordered_map<uint64_t, int> open;   // key -> group index (the one still filling)
+    std::vector<std::vector<int>> gm;
+    std::vector<RefineGroup> gd;
+    std::vector<char> grouped(m.n, 0);
+    for (int i = 0; i < m.n; i++) {
+        const xavs2gpu_pu_t &p = m.h_pus[i];
+        const int w = h_pu_w[p.part], h = h_pu_h[p.part], S = w > h ? w : h;
+        const int lg = S == 16 ? 4 : S == 32 ? 5 : S == 64 ? 6 : 0;
+        if (!lg) continue;
+        const int cx = p.x & ~(S - 1), cy = p.y & ~(S - 1);
+        bool canon = false;
+        for (int mo = 0; mo < 13 && !canon; mo++) {
+            const SlotGeom g = cu_mode_geom(S, cx, cy, mo);
+            canon = g.part == p.part && g.ox == p.x && g.oy == p.y;
+        }
+        if (!canon) continue;
+        const uint64_t key = ((uint64_t)p.ref << 40) | ((uint64_t)lg << 32) | ((uint64_t)(uint16_t)cx << 16) |
+                             (uint64_t)(uint16_t)cy;
+        auto it = open.find(key);
+        int gi;
+        if (it == open.end() || gm[it->second].size() >= 32) {
+            gi = (int)gm.size();
+            gm.emplace_back();
+            RefineGroup d{};
+            d.cx = (int16_t)cx;
+            d.cy = (int16_t)cy;
+            d.lg = (uint8_t)lg;
+            d.ref = p.ref;
+            gd.push_back(d);
+            open[key] = gi;
+        } else {
+            gi = it->second;
+        }
+        gm[gi].push_back(i);
+        grouped[i] = 1;
+    }
+    std::vector<int> ord(gd.size());
+    for (size_t k = 0; k < ord.size(); k++) ord[k] = (int)k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return gd[a].lg > gd[b].lg; });
+    m.h_groups.clear();
+    m.h_members.clear();
+    for (int k : ord) {
+        RefineGroup d = gd[k];
+        d.first = (uint32_t)m.h_members.size();
+        d.count = (uint8_t)gm[k].size();
+        for (int i : gm[k]) m.h_members.push_back((uint32_t)i);
+        m.h_groups.push_back(d);
+    }
+    m.h_small_g.clear();
+    m.h_large_g.clear();
+    for (int i : small)
+        if (!grouped[i]) m.h_small_g.push_back((uint32_t)i);
+    for (int i : large)
+        if (!grouped[i]) m.h_large_g.push_back((uint32_t)i);
+    m.n_groups = (int)m.h_groups.size();
+    m.n_small_g = (int)m.h_small_g.size();
+    m.n_large_g = (int)m.h_large_g.size();
+    if (m.n_groups) {
+        XG_CUDA(cudaMemcpyAsync(m.d_groups, m.h_groups.data(), sizeof(RefineGroup) * m.n_groups,
+                                cudaMemcpyHostToDevice, m.st));
+        XG_CUDA(cudaMemcpyAsync(m.d_members, m.h_members.data(), sizeof(uint32_t) * m.h_members.size(),
+                                cudaMemcpyHostToDevice, m.st));
+    }
+    if (m.n_small_g)
+        XG_CUDA(cudaMemcpyAsync(m.d_small_g, m.h_small_g.data(), sizeof(int) * m.n_small_g, cudaMemcpyHostToDevice,
+                                m.st));
+    if (m.n_large_g)
+        XG_CUDA(cudaMemcpyAsync(m.d_large_g, m.h_large_g.data(), sizeof(int) * m.n_large_g, cudaMemcpyHostToDevice,
+                                m.st));
+}
+
 // (Re)builds the split into CTU jobs and per-PU searches for window size R.
 static void ensure_plan(MeSessionImpl &m, int R)
 {
@@ -1083,6 +1428,7 @@ static void ensure_plan(MeSessionImpl &m, int R)
     if (m.n_small) XG_CUDA(cudaMemcpyAsync(m.d_small, small.data(), sizeof(int) * m.n_small, cudaMemcpyHostToDevice, m.st));
     if (m.n_large) XG_CUDA(cudaMemcpyAsync(m.d_large, large.data(), sizeof(int) * m.n_large, cudaMemcpyHostToDevice, m.st));
     if (m.n) XG_CUDA(cudaMemcpyAsync(m.d_order, order.data(), sizeof(int) * m.n, cudaMemcpyHostToDevice, m.st));
+    build_groups(m, small, large);
     if (m.n_tasks)
         XG_CUDA(cudaMemcpyAsync(m.d_tasks, tasks.data(), sizeof(RefineTask) * m.n_tasks, cudaMemcpyHostToDevice, m.st));
     refresh_view(m);
@@ -1118,14 +1464,24 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
-    if (m.n_small) {
-        refine_thread_kernel<<<(m.n_small + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
-            reinterpret_cast<const uint32_t *>(m.d_small), m.n_small, m.d_view, R, *prm);
+    // the CU-grouped refinement follows the reference's per-PU order, which
+    // with PMVR depends on each PU's predictor; PMVR keeps the per-PU kernels
+    const bool grouped = !prm->enable_pmvr && m.n_groups > 0 && use_groups();
+    const int ns = grouped ? m.n_small_g : m.n_small, nl = grouped ? m.n_large_g : m.n_large;
+    const int *lst_s = grouped ? m.d_small_g : m.d_small, *lst_l = grouped ? m.d_large_g : m.d_large;
+    if (grouped) {
+        refine_group_kernel<<<(m.n_groups + kGrpWarps - 1) / kGrpWarps, 32 * kGrpWarps, 0, m.st>>>(
+            m.d_groups, m.n_groups, m.d_members, m.d_view, R, *prm);
         count_launch();
     }
-    if (m.n_large) {
-        refine_warp_list_kernel<<<(m.n_large * 32 + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
-            reinterpret_cast<const uint32_t *>(m.d_large), m.n_large, m.d_view, R, *prm);
+    if (ns) {
+        refine_thread_kernel<<<(ns + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
+            reinterpret_cast<const uint32_t *>(lst_s), ns, m.d_view, R, *prm);
+        count_launch();
+    }
+    if (nl) {
+        refine_warp_list_kernel<<<(nl * 32 + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
+            reinterpret_cast<const uint32_t *>(lst_l), nl, m.d_view, R, *prm);
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[4], m.st));
@@ -1347,9 +1703,10 @@ extern "C" int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s)
 
 struct BatchBuf {
     CtuJob *d_jobs = nullptr;
-    uint32_t *d_lists = nullptr;    // generic | small | large
+    uint32_t *d_lists = nullptr;    // generic | small | large | group members
     SessView *d_views = nullptr;
-    size_t cap_jobs = 0, cap_lists = 0, cap_views = 0;
+    RefineGroup *d_groups = nullptr;
+    size_t cap_jobs = 0, cap_lists = 0, cap_views = 0, cap_groups = 0;
     uint8_t *h_stage = nullptr;     // pinned: jobs | lists | views (uploads without a stream wait)
     size_t cap_stage = 0;
     cudaEvent_t done = nullptr;
@@ -1380,7 +1737,7 @@ extern "C" void xavs2gpu_me_batch_destroy(xavs2gpu_me_batch_t *b)
     for (auto &x : b->buf) {
         if (x.used) cudaEventSynchronize(x.done);
         cudaEventDestroy(x.done);
-        cudaFree(x.d_jobs); cudaFree(x.d_lists); cudaFree(x.d_views); cudaFreeHost(x.h_stage);
+        cudaFree(x.d_jobs); cudaFree(x.d_lists); cudaFree(x.d_views); cudaFree(x.d_groups); cudaFreeHost(x.h_stage);
     }
     delete b;
 }
@@ -1408,7 +1765,9 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     cudaStream_t st = (cudaStream_t)stream;
     b->jobs.clear();
     b->views.clear();
-    std::vector<uint32_t> gen, small, large;
+    std::vector<uint32_t> gen, small, large, members;
+    std::vector<RefineGroup> groups;
+    const bool grouped = !prm->enable_pmvr && use_groups();
     int block = 128;
     for (int k = 0; k < n; k++) {
         MeSessionImpl &m = sessions[k]->impl;
@@ -1424,8 +1783,18 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
             b->jobs.push_back(j);
         }
         for (uint32_t i : m.h_generic) gen.push_back(tag | i);
-        for (uint32_t i : m.h_small) small.push_back(tag | i);
-        for (uint32_t i : m.h_large) large.push_back(tag | i);
+        if (grouped) {
+            for (uint32_t i : m.h_small_g) small.push_back(tag | i);
+            for (uint32_t i : m.h_large_g) large.push_back(tag | i);
+            for (RefineGroup d : m.h_groups) {
+                d.first += (uint32_t)members.size();
+                groups.push_back(d);
+            }
+            for (uint32_t i : m.h_members) members.push_back(tag | i);
+        } else {
+            for (uint32_t i : m.h_small) small.push_back(tag | i);
+            for (uint32_t i : m.h_large) large.push_back(tag | i);
+        }
         if (k == 0) block = m.tune_block;
     }
     BatchBuf &bb = b->buf[b->next];
@@ -1435,12 +1804,14 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     b->lists.insert(b->lists.end(), gen.begin(), gen.end());
     b->lists.insert(b->lists.end(), small.begin(), small.end());
     b->lists.insert(b->lists.end(), large.begin(), large.end());
+    b->lists.insert(b->lists.end(), members.begin(), members.end());
     grow(bb.d_jobs, bb.cap_jobs, b->jobs.size());
     grow(bb.d_lists, bb.cap_lists, b->lists.size());
     grow(bb.d_views, bb.cap_views, b->views.size());
+    grow(bb.d_groups, bb.cap_groups, groups.size());
     const size_t bj = sizeof(CtuJob) * b->jobs.size(), bl = sizeof(uint32_t) * b->lists.size();
-    const size_t bv = sizeof(SessView) * b->views.size();
-    const size_t oj = 0, ol = align_up(bj), ov = ol + align_up(bl), need = ov + align_up(bv);
+    const size_t bv = sizeof(SessView) * b->views.size(), bg = sizeof(RefineGroup) * groups.size();
+    const size_t oj = 0, ol = align_up(bj), ov = ol + align_up(bl), og = ov + align_up(bv), need = og + align_up(bg);
     if (need > bb.cap_stage) {
         cudaFreeHost(bb.h_stage);
         bb.cap_stage = need + need / 4 + 4096;
@@ -1449,11 +1820,14 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     memcpy(bb.h_stage + oj, b->jobs.data(), bj);
     memcpy(bb.h_stage + ol, b->lists.data(), bl);
     memcpy(bb.h_stage + ov, b->views.data(), bv);
+    if (bg) memcpy(bb.h_stage + og, groups.data(), bg);
     if (bj) XG_CUDA(cudaMemcpyAsync(bb.d_jobs, bb.h_stage + oj, bj, cudaMemcpyHostToDevice, st));
     if (bl) XG_CUDA(cudaMemcpyAsync(bb.d_lists, bb.h_stage + ol, bl, cudaMemcpyHostToDevice, st));
     XG_CUDA(cudaMemcpyAsync(bb.d_views, bb.h_stage + ov, bv, cudaMemcpyHostToDevice, st));
-    const int ng = (int)gen.size(), ns = (int)small.size(), nl = (int)large.size();
+    if (bg) XG_CUDA(cudaMemcpyAsync(bb.d_groups, bb.h_stage + og, bg, cudaMemcpyHostToDevice, st));
+    const int ng = (int)gen.size(), ns = (int)small.size(), nl = (int)large.size(), ngr = (int)groups.size();
     const uint32_t *d_gen = bb.d_lists, *d_small = bb.d_lists + ng, *d_large = bb.d_lists + ng + ns;
+    const uint32_t *d_members = bb.d_lists + ng + ns + nl;
     reset_keys_kernel<<<152 * 4, 256, 0, st>>>(bb.d_views, n);
     count_launch();
     if (ng) {
@@ -1463,6 +1837,11 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     ctu_jobs_run(bb.d_jobs, (int)b->jobs.size(), bb.d_views, *prm, st);
     if (ng) {
         fs_generic_kernel<<<ng < 152 * 8 ? ng : 152 * 8, 256, 0, st>>>(d_gen, ng, bb.d_views, R, lam);
+        count_launch();
+    }
+    if (ngr) {
+        refine_group_kernel<<<(ngr + kGrpWarps - 1) / kGrpWarps, 32 * kGrpWarps, 0, st>>>(bb.d_groups, ngr, d_members,
+                                                                                         bb.d_views, R, *prm);
         count_launch();
     }
     if (ns) {
