@@ -387,7 +387,8 @@ def run_ours(args):
         "config": {"workload": "me_1080p_2ref_fs64_qpel_satd", "width": WIDTH, "height": HEIGHT, "refs": NREFS,
                    "search_range": RANGE, "qp": QP, "pus_per_picture": int(len(pus)),
                    "evals_per_step": evals, "l2": "flushed between steps (512 MiB write)",
-                   "autotuned": {"refine_split_px": tuning[0], "refine_block": tuning[1], "search_ms": tune_ms},
+                   "autotuned": {"refine_split_px": tuning[0], "refine_block": tuning[1], "cu_groups": tuning[2],
+                                 "search_ms": tune_ms},
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "results_equal_device_run": same},
@@ -1577,6 +1578,7 @@ def run_chain(args):
                    "l2": "inputs larger than L2 (%d MB of reference planes)" % (NR * 16 * (W + 160) * (H + 160) >> 20)},
         "graph": {"kernels_per_launch": nk, "autotuned": {"refine_split_px": tun.me.refine_split_px,
                                                             "refine_block": tun.me.refine_block,
+                                                            "cu_groups": tun.me.cu_groups,
                                                             "tq_warps": tun.tq_warps, "ms_per_picture": tune_ms}},
         "e2e": {"value": e2e_fps, "unit": "pictures/s", "h2d_bytes_per_step": W * H, "d2h_bytes_per_step": W * H},
         "gpu_launches": int(launches),

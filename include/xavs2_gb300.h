@@ -564,10 +564,15 @@ XAVS2GPU_API int xavs2gpu_me_phase_ms(xavs2gpu_me_session_t *s, float ms[4]);
 /* Launch shapes of the sub-pel refinement (no counterpart in the reference;
  * results never depend on them): searches of at most refine_split_px
  * pixels refine one per thread, larger ones one per warp; refine_block
- * threads per CTA (32, 64 or 128). */
+ * threads per CTA (32, 64 or 128); cu_groups = 1 refines the partitions of
+ * each 16x16..64x64 CU together, sharing the unit costs of partitions with
+ * a common centre (faster when partitions agree on their motion, the
+ * default), 0 refines every search on its own. */
 typedef struct xavs2gpu_me_tuning {
     int32_t refine_split_px;
     int32_t refine_block;
+    int32_t cu_groups;
+    int32_t pad_;
 } xavs2gpu_me_tuning_t;
 XAVS2GPU_API int xavs2gpu_me_set_tuning(xavs2gpu_me_session_t *s, const xavs2gpu_me_tuning_t *t);
 XAVS2GPU_API int xavs2gpu_me_get_tuning(const xavs2gpu_me_session_t *s, xavs2gpu_me_tuning_t *t);

@@ -178,3 +178,38 @@ def test_cu_partition_refinement(gpu, olib, had, frac, fast, pmvr):
     got, _ = _run(f2, [f1, f0], allp, prm)
     exp = _oracle(olib, f2, [f1, f0], allp, prm)
     _assert_same(got, exp, allp)
+
+
+def test_tuning_cu_groups(gpu, olib):
+    """The CU-grouped refinement on and off (xavs2gpu_me_set_tuning) give the
+    same results; bad tuning values are refused."""
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(5150)
+    w, h = 192, 128
+    f0 = synth.base_picture(rng, w, h)
+    f1 = synth.next_picture(rng, f0, 3, 5)
+    pus, _ = xg.cu_pus(xg.split_map_cus(w, h, 23), w, h, 1)
+    prm = xg.MeParams(12, oracle.lambda_factor(32), 1, 2, 0, 0)
+    s = xg.MeSession(w, h, 1, len(pus))
+    s.set_pus(pus)
+    s.set_picture(-1, f1)
+    s.set_picture(0, f0)
+    outs = []
+    for groups in (1, 0, 1):
+        assert s.lib.xavs2gpu_me_set_tuning(s.h, ctypes.byref(xg.MeTuning(256, 128, groups))) == 0
+        t = xg.MeTuning()
+        s.lib.xavs2gpu_me_get_tuning(s.h, ctypes.byref(t))
+        assert (t.refine_split_px, t.refine_block, t.cu_groups) == (256, 128, groups)
+        s.run(prm)
+        outs.append(s.results().tobytes())
+    assert outs[0] == outs[1] == outs[2]
+    s.lib.xavs2gpu_set_abort_on_error(0)
+    try:
+        assert s.lib.xavs2gpu_me_set_tuning(s.h, ctypes.byref(xg.MeTuning(256, 128, 2))) != 0
+    finally:
+        s.lib.xavs2gpu_clear_error()
+        s.lib.xavs2gpu_set_abort_on_error(1)
+    s.close()
+    exp = _oracle(olib, f1, [f0], pus, prm)
+    assert outs[0] == exp.tobytes()

@@ -310,7 +310,7 @@ class MeSession:
         self._check(self.lib.xavs2gpu_me_autotune(self.h, ctypes.byref(params), reps, ctypes.byref(ms)), "autotune")
         t = MeTuning()
         self.lib.xavs2gpu_me_get_tuning(self.h, ctypes.byref(t))
-        return ms.value, (t.refine_split_px, t.refine_block)
+        return ms.value, (t.refine_split_px, t.refine_block, t.cu_groups)
 
     def set_stream(self, stream):
         self._check(self.lib.xavs2gpu_me_set_stream(self.h, ctypes.c_void_p(stream) if stream else None),
@@ -423,7 +423,8 @@ class Server:
 
 
 class MeTuning(ctypes.Structure):
-    _fields_ = [("refine_split_px", ctypes.c_int32), ("refine_block", ctypes.c_int32)]
+    _fields_ = [("refine_split_px", ctypes.c_int32), ("refine_block", ctypes.c_int32), ("cu_groups", ctypes.c_int32),
+                ("pad_", ctypes.c_int32)]
 
 
 class ChainTuning(ctypes.Structure):

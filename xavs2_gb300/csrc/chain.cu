@@ -370,10 +370,11 @@ extern "C" int xavs2gpu_chain_autotune(xavs2gpu_chain_t *c, const xavs2gpu_me_pa
     }
     for (int split : {64, 128, 256, 512}) {
         if (rc != XAVS2GPU_OK) break;
-        for (int blk : {64, 128}) {
+        for (int cfg = 0; cfg < 4; cfg++) {
             xavs2gpu_chain_tuning_t cand = best;
             cand.me.refine_split_px = split;
-            cand.me.refine_block = blk;
+            cand.me.refine_block = cfg & 1 ? 128 : 64;
+            cand.me.cu_groups = cfg >> 1;
             if ((rc = time_cfg(cand, t)) != XAVS2GPU_OK) break;
             if (t < best_t) { best_t = t; best = cand; }
         }

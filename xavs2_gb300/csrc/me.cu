@@ -827,15 +827,15 @@ template <bool U4>
 __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had, int cs, const uint8_t *o,
                                             const uint8_t *const *planes, int stride, int px, int py, int ccx,
                                             int ccy, const int (&offx)[kGrpMaxPos], const int (&offy)[kGrpMaxPos],
-                                            int P, int t, int nt)
+                                            int P, int lane)
 {
     constexpr int UW = U4 ? 4 : 8;
     const int cols = cs / UW, nu = cols * (cs >> 2);
     const int mcols = (65536 + cols - 1) / cols;
     int(*T)[kGrpMaxPos] = U4 ? S.t4 : S.t8;
-    if (nu >= nt) {
-        // a thread per unit, its current block loaded once for all positions
-        for (int u = t; u < nu; u += nt) {
+    if (nu >= 32) {
+        // a lane per unit, its current block loaded once for all positions
+        for (int u = lane; u < nu; u += 32) {
             const int uy = div_small(u, mcols), ux = u - uy * cols;
             if (!unit_covered(S, grp, ux * UW, uy * 4, U4)) continue;
             int c[4][8];
@@ -852,9 +852,9 @@ __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had
             }
         }
     } else {
-        // a thread per (unit, position)
+        // a lane per (unit, position)
         const int mp = (65536 + P - 1) / P;
-        for (int e = t; e < nu * P; e += nt) {
+        for (int e = lane; e < nu * P; e += 32) {
             const int u = div_small(e, mp), k = e - u * P;
             const int uy = div_small(u, mcols), ux = u - uy * cols;
             if (!unit_covered(S, grp, ux * UW, uy * 4, U4)) continue;
@@ -873,131 +873,6 @@ __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had
     }
 }
 
-// Member `slot` of group G: its rectangle in the CU, unit type and predictor,
-// the integer search's result; an invalid search gets its result here.
-struct GroupMember {
-    int i, pmx, pmy, bx, by, best;
-    bool valid;
-    xavs2gpu_me_result_t res;
-};
-
-__device__ __forceinline__ GroupMember init_member(const SessView &v, const RefineGroup &G, const uint32_t *members,
-                                                   int slot, int R, bool had, GroupSmem &S)
-{
-    GroupMember q;
-    q.i = (int)(members[G.first + slot] & kIdxMask);
-    const xavs2gpu_pu_t p = v.pus[q.i];
-    const PuState st = v.state[q.i];
-    const unsigned long long key = v.keys[q.i];
-    q.valid = st.valid && key != kNoKey;
-    const int w = c_pu_w[p.part], h = c_pu_h[p.part];
-    S.rx[slot] = (int16_t)(p.x - G.cx);
-    S.ry[slot] = (int16_t)(p.y - G.cy);
-    S.rw[slot] = (int16_t)w;
-    S.rh[slot] = (int16_t)h;
-    S.ru4[slot] = (int8_t)(had ? satd_unit4(w, h) : (w == 4 || w == 12));
-    q.pmx = p.mvp_x;
-    q.pmy = p.mvp_y;
-    q.bx = q.by = q.best = 0;
-    if (!q.valid) {
-        q.res.bmv_x = q.res.bmv_y = q.res.imv_x = q.res.imv_y = 0;
-        q.res.bcost = q.res.icost = 1 << 30;
-        q.res.mvcost = 0;
-        v.res[q.i] = q.res;
-    } else {
-        const int icost = (int)(key >> 32);
-        const unsigned order_ = (unsigned)(key & 0xffffffffu);
-        int bmx, bmy;
-        if (order_ < 2) { bmx = st.cand[order_][0]; bmy = st.cand[order_][1]; }
-        else {
-            const int qq = (int)order_ - 2;
-            bmx = st.cx + qq % (2 * R) - R;
-            bmy = st.cy + qq / (2 * R) - R;
-        }
-        q.res.imv_x = (int16_t)bmx; q.res.imv_y = (int16_t)bmy; q.res.icost = icost;
-        q.bx = bmx * 4; q.by = bmy * 4; q.best = icost;
-    }
-    return q;
-}
-
-// The positions of a refinement stage relative to its centre, in the
-// reference's order: the centre first (half-pel stage with SATD), then the
-// spiral (every neighbour, or every other with fast_sub_me), 2 quarter-pels
-// apart in the half-pel stage and 1 in the quarter-pel stage.  Returns the
-// count; k0 = 1 when position 0 is the centre.
-__device__ __forceinline__ int stage_positions(const xavs2gpu_me_params_t &prm, int stage, bool had,
-                                               int (&offx)[kGrpMaxPos], int (&offy)[kGrpMaxPos], int &k0)
-{
-    const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1, mult = stage == 0 ? 2 : 1;
-    k0 = (stage == 0 && had) ? 1 : 0;
-#pragma unroll
-    for (int k = 0; k < kGrpMaxPos; k++) { offx[k] = 0; offy[k] = 0; }
-    int P = k0;
-#pragma unroll
-    for (int pos = 1; pos < 9; pos++) {
-        if ((pos - 1) % step) continue;
-#pragma unroll
-        for (int k = 0; k < kGrpMaxPos; k++)
-            if (k == P) { offx[k] = mult * c_spiral[pat][pos][0]; offy[k] = mult * c_spiral[pat][pos][1]; }
-        P++;
-    }
-    return P;
-}
-
-// Sums of member m's units at the P positions, reduced over the warp (every
-// lane gets the totals in part[]).
-__device__ __forceinline__ void member_sums(const GroupSmem &S, int m, int cs, int P, int lane,
-                                            int (&part)[kGrpMaxPos])
-{
-    const int u4 = S.ru4[m], uw = u4 ? 4 : 8;
-    const int nux = S.rw[m] / uw, n = nux * (S.rh[m] >> 2);
-    const int mnux = (65536 + nux - 1) / nux, cols = cs / uw;
-    const int base = (S.ry[m] >> 2) * cols + S.rx[m] / uw;
-#pragma unroll
-    for (int k = 0; k < kGrpMaxPos; k++) part[k] = 0;
-    for (int q = lane; q < n; q += 32) {
-        const int qy = div_small(q, mnux), qx = q - qy * nux;
-        const int u = base + qy * cols + qx;
-        const int *row = u4 ? S.t4[u] : S.t8[u];
-#pragma unroll
-        for (int k = 0; k < kGrpMaxPos; k++)
-            if (k < P) part[k] += row[k];
-    }
-#pragma unroll
-    for (int k = 0; k < kGrpMaxPos; k++)
-        if (k < P) part[k] = __reduce_add_sync(0xffffffffu, part[k]);
-}
-
-// The member's winner among the stage's positions around (ccx, ccy): the
-// first strictly smaller cost in order (the centre, with SATD, replaces the
-// integer search's SAD cost).
-__device__ __forceinline__ void member_pick(const int (&acc)[kGrpMaxPos], int P, int k0, const int (&offx)[kGrpMaxPos],
-                                            const int (&offy)[kGrpMaxPos], int ccx, int ccy, int lam, int pmx,
-                                            int pmy, int &bx, int &by, int &best)
-{
-    int nbx = bx, nby = by;
-    if (k0) best = acc[0] + mv_cost_hd(lam, ccx, ccy, pmx, pmy);
-#pragma unroll
-    for (int k = 0; k < kGrpMaxPos; k++) {
-        if (k < k0 || k >= P) continue;
-        const int mx = ccx + offx[k], my = ccy + offy[k];
-        const int c = acc[k] + mv_cost_hd(lam, mx, my, pmx, pmy);
-        if (c < best) { best = c; nbx = mx; nby = my; }
-    }
-    bx = nbx;
-    by = nby;
-}
-
-__device__ __forceinline__ void write_member(const SessView &v, const GroupMember &q, int lam)
-{
-    xavs2gpu_me_result_t res = q.res;
-    res.bmv_x = (int16_t)q.bx; res.bmv_y = (int16_t)q.by;
-    res.bcost = q.best;
-    res.mvcost = mv_cost_hd(lam, q.bx, q.by, q.pmx, q.pmy);
-    v.res[q.i] = res;
-}
-
-// A warp per group (16x16 CUs): lanes are the members.
 __global__ void __launch_bounds__(32 * kGrpWarps) refine_group_kernel(const RefineGroup *__restrict__ groups,
                                                                       int ngroups,
                                                                       const uint32_t *__restrict__ members,
@@ -1010,150 +885,149 @@ __global__ void __launch_bounds__(32 * kGrpWarps) refine_group_kernel(const Refi
     if (gi >= ngroups) return;   // the whole warp
     GroupSmem &S = smem[warp];
     const RefineGroup G = groups[gi];
-    const SessView &v = views[members[G.first] >> kSessShift];
+    const uint32_t e0 = members[G.first];
+    const SessView &v = views[e0 >> kSessShift];
     const Geometry g = v.g;
-    const int cs = 1 << G.lg;
+    const int M = G.count, cs = 1 << G.lg;
     const bool had = prm.use_hadamard != 0;
     const int lam = prm.lambda_factor;
-    const bool mem = lane < G.count;
-    GroupMember q{};
-    if (mem) q = init_member(v, G, members, lane, R, had, S);
+    const bool mem = lane < M;
+    int i = 0, pmx = 0, pmy = 0, bx = 0, by = 0, best = 0;
+    bool valid = false;
+    xavs2gpu_me_result_t res;
+    if (mem) {
+        i = (int)(members[G.first + lane] & kIdxMask);
+        const xavs2gpu_pu_t p = v.pus[i];
+        const PuState st = v.state[i];
+        const unsigned long long key = v.keys[i];
+        valid = st.valid && key != kNoKey;
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
+        S.rx[lane] = (int16_t)(p.x - G.cx);
+        S.ry[lane] = (int16_t)(p.y - G.cy);
+        S.rw[lane] = (int16_t)w;
+        S.rh[lane] = (int16_t)h;
+        S.ru4[lane] = (int8_t)(had ? satd_unit4(w, h) : (w == 4 || w == 12));
+        pmx = p.mvp_x;
+        pmy = p.mvp_y;
+        if (!valid) {
+            res.bmv_x = res.bmv_y = res.imv_x = res.imv_y = 0;
+            res.bcost = res.icost = 1 << 30;
+            res.mvcost = 0;
+            v.res[i] = res;
+        } else {
+            const int icost = (int)(key >> 32);
+            const unsigned order_ = (unsigned)(key & 0xffffffffu);
+            int bmx, bmy;
+            if (order_ < 2) { bmx = st.cand[order_][0]; bmy = st.cand[order_][1]; }
+            else {
+                const int q = (int)order_ - 2;
+                bmx = st.cx + q % (2 * R) - R;
+                bmy = st.cy + q / (2 * R) - R;
+            }
+            res.imv_x = (int16_t)bmx; res.imv_y = (int16_t)bmy; res.icost = icost;
+            bx = bmx * 4; by = bmy * 4; best = icost;
+        }
+    }
     __syncwarp();
     const uint8_t *o = v.cur + (ptrdiff_t)G.cy * g.stride + G.cx;
     const uint8_t *const *planes = v.planes + 16 * G.ref;
     if (prm.fractional_me) {
+        const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
         for (int stage = 0; stage < (prm.fractional_me > 1 ? 2 : 1); stage++) {
-            int offx[kGrpMaxPos], offy[kGrpMaxPos], k0;
-            const int P = stage_positions(prm, stage, had, offx, offy, k0);
-            unsigned pending = __ballot_sync(0xffffffffu, mem && q.valid);
+            // the stage's positions relative to the centre, in the reference's order
+            int offx[kGrpMaxPos], offy[kGrpMaxPos], P = 0;
+            const int k0 = (stage == 0 && had) ? 1 : 0;
+#pragma unroll
+            for (int k = 0; k < kGrpMaxPos; k++) { offx[k] = 0; offy[k] = 0; }
+            P = k0;
+#pragma unroll
+            for (int pos = 1; pos < 9; pos++) {
+                if ((pos - 1) % step) continue;
+                const int mult = stage == 0 ? 2 : 1;
+#pragma unroll
+                for (int k = 0; k < kGrpMaxPos; k++)
+                    if (k == P) { offx[k] = mult * c_spiral[pat][pos][0]; offy[k] = mult * c_spiral[pat][pos][1]; }
+                P++;
+            }
+            unsigned pending = __ballot_sync(0xffffffffu, mem && valid);
             while (pending) {
                 const int leader = __ffs(pending) - 1;
-                const int ccx = __shfl_sync(0xffffffffu, q.bx, leader), ccy = __shfl_sync(0xffffffffu, q.by, leader);
-                const unsigned grp =
-                    __ballot_sync(0xffffffffu, mem && q.valid && q.bx == ccx && q.by == ccy) & pending;
+                const int ccx = __shfl_sync(0xffffffffu, bx, leader), ccy = __shfl_sync(0xffffffffu, by, leader);
+                const unsigned grp = __ballot_sync(0xffffffffu, mem && valid && bx == ccx && by == ccy) & pending;
                 pending &= ~grp;
                 const bool need8 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && !S.ru4[lane]);
                 const bool need4 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && S.ru4[lane]);
                 if (need8)
                     group_table<false>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
-                                       lane, 32);
+                                       lane);
                 if (need4)
                     group_table<true>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
-                                      lane, 32);
+                                      lane);
                 __syncwarp();
+                // each member's sums over its units
                 int acc[kGrpMaxPos];
 #pragma unroll
                 for (int k = 0; k < kGrpMaxPos; k++) acc[k] = 0;
                 for (unsigned left = grp; left;) {
                     const int m = __ffs(left) - 1;
                     left &= left - 1;
+                    const int u4 = S.ru4[m], uw = u4 ? 4 : 8;
+                    const int nux = S.rw[m] / uw, n = nux * (S.rh[m] >> 2);
+                    const int mnux = (65536 + nux - 1) / nux, cols = cs / uw;
+                    const int base = (S.ry[m] >> 2) * cols + S.rx[m] / uw;
                     int part[kGrpMaxPos];
-                    member_sums(S, m, cs, P, lane, part);
-                    if (lane == m) {
 #pragma unroll
-                        for (int k = 0; k < kGrpMaxPos; k++) acc[k] = part[k];
+                    for (int k = 0; k < kGrpMaxPos; k++) part[k] = 0;
+                    for (int q = lane; q < n; q += 32) {
+                        const int qy = div_small(q, mnux), qx = q - qy * nux;
+                        const int u = base + qy * cols + qx;
+                        const int *row = u4 ? S.t4[u] : S.t8[u];
+#pragma unroll
+                        for (int k = 0; k < kGrpMaxPos; k++)
+                            if (k < P) part[k] += row[k];
+                    }
+#pragma unroll
+                    for (int k = 0; k < kGrpMaxPos; k++) {
+                        if (k < P) {
+                            const int t = __reduce_add_sync(0xffffffffu, part[k]);
+                            if (lane == m) acc[k] = t;
+                        }
                     }
                 }
                 __syncwarp();   // the tables are rebuilt for the next centre
-                if ((grp >> lane) & 1)
-                    member_pick(acc, P, k0, offx, offy, ccx, ccy, lam, q.pmx, q.pmy, q.bx, q.by, q.best);
+                if ((grp >> lane) & 1) {
+                    int nbx = bx, nby = by;
+                    if (k0) best = acc[0] + mv_cost_hd(lam, ccx, ccy, pmx, pmy);
+#pragma unroll
+                    for (int k = 0; k < kGrpMaxPos; k++) {
+                        if (k < k0 || k >= P) continue;
+                        const int mx = ccx + offx[k], my = ccy + offy[k];
+                        const int c = acc[k] + mv_cost_hd(lam, mx, my, pmx, pmy);
+                        if (c < best) { best = c; nbx = mx; nby = my; }
+                    }
+                    bx = nbx;
+                    by = nby;
+                }
             }
         }
     }
-    if (mem && q.valid) write_member(v, q, lam);
+    if (mem && valid) {
+        res.bmv_x = (int16_t)bx; res.bmv_y = (int16_t)by;
+        res.bcost = best;
+        res.mvcost = mv_cost_hd(lam, bx, by, pmx, pmy);
+        v.res[i] = res;
+    }
 }
 
-// A CTA per group (32x32 and 64x64 CUs): the table of a centre is spread
-// over all 128 threads, members' sums over the four warps; warp 0 lanes
-// hold the members.
-constexpr int kGrpCtaThreads = 128;
-struct GroupCtaSmem {
-    GroupSmem S;
-    int bx[32], by[32];
-    int acc[32][kGrpMaxPos];
-    unsigned valid;
-};
-
-__global__ void __launch_bounds__(kGrpCtaThreads) refine_group_cta_kernel(const RefineGroup *__restrict__ groups,
-                                                                          int ngroups,
-                                                                          const uint32_t *__restrict__ members,
-                                                                          const SessView *__restrict__ views, int R,
-                                                                          xavs2gpu_me_params_t prm)
+// The CU-grouped refinement: a warp per group.
+static void launch_groups(const RefineGroup *groups, int n, const uint32_t *members, const SessView *views, int R,
+                          const xavs2gpu_me_params_t &prm, cudaStream_t st)
 {
-    __shared__ GroupCtaSmem sm;
-    const int gi = blockIdx.x;
-    if (gi >= ngroups) return;   // the whole CTA
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const RefineGroup G = groups[gi];
-    const SessView &v = views[members[G.first] >> kSessShift];
-    const Geometry g = v.g;
-    const int cs = 1 << G.lg;
-    const bool had = prm.use_hadamard != 0;
-    const int lam = prm.lambda_factor;
-    GroupMember q{};
-    const bool mem = warp == 0 && lane < G.count;
-    if (mem) q = init_member(v, G, members, lane, R, had, sm.S);
-    if (warp == 0) {
-        const unsigned vm = __ballot_sync(0xffffffffu, mem && q.valid);
-        if (lane == 0) sm.valid = vm;
-        if (mem) { sm.bx[lane] = q.bx; sm.by[lane] = q.by; }
+    if (n) {
+        refine_group_kernel<<<(n + kGrpWarps - 1) / kGrpWarps, 32 * kGrpWarps, 0, st>>>(groups, n, members, views, R,
+                                                                                      prm);
+        count_launch();
     }
-    __syncthreads();
-    const uint8_t *o = v.cur + (ptrdiff_t)G.cy * g.stride + G.cx;
-    const uint8_t *const *planes = v.planes + 16 * G.ref;
-    if (prm.fractional_me) {
-        for (int stage = 0; stage < (prm.fractional_me > 1 ? 2 : 1); stage++) {
-            int offx[kGrpMaxPos], offy[kGrpMaxPos], k0;
-            const int P = stage_positions(prm, stage, had, offx, offy, k0);
-            unsigned pending = sm.valid;
-            while (pending) {
-                // every thread derives the same centre group from shared memory
-                const int leader = __ffs(pending) - 1;
-                const int ccx = sm.bx[leader], ccy = sm.by[leader];
-                unsigned grp = 0;
-                bool need8 = false, need4 = false;
-                for (unsigned left = pending; left;) {
-                    const int m = __ffs(left) - 1;
-                    left &= left - 1;
-                    if (sm.bx[m] == ccx && sm.by[m] == ccy) {
-                        grp |= 1u << m;
-                        if (sm.S.ru4[m]) need4 = true;
-                        else need8 = true;
-                    }
-                }
-                pending &= ~grp;
-                if (need8)
-                    group_table<false>(sm.S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
-                                       tid, kGrpCtaThreads);
-                if (need4)
-                    group_table<true>(sm.S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
-                                      tid, kGrpCtaThreads);
-                __syncthreads();
-                // member j of the centre group is summed by warp j % 4
-                int j = 0;
-                for (unsigned left = grp; left; j++) {
-                    const int m = __ffs(left) - 1;
-                    left &= left - 1;
-                    if ((j & 3) != warp) continue;
-                    int part[kGrpMaxPos];
-                    member_sums(sm.S, m, cs, P, lane, part);
-                    if (lane == 0) {
-#pragma unroll
-                        for (int k = 0; k < kGrpMaxPos; k++)
-                            if (k < P) sm.acc[m][k] = part[k];
-                    }
-                }
-                __syncthreads();
-                if (mem && ((grp >> lane) & 1)) {
-                    member_pick(sm.acc[lane], P, k0, offx, offy, ccx, ccy, lam, q.pmx, q.pmy, q.bx, q.by, q.best);
-                    sm.bx[lane] = q.bx;
-                    sm.by[lane] = q.by;
-                }
-                __syncthreads();   // centres updated; the tables are rebuilt for the next centre
-            }
-        }
-    }
-    if (mem && q.valid) write_member(v, q, lam);
 }
 
 }  // namespace xg
@@ -1169,11 +1043,7 @@ namespace xg {
 #define XG_REFINE_GROUPS 1
 #endif
 static constexpr bool use_groups() { return XG_REFINE_GROUPS != 0; }
-// CUs of at least 2^XG_GROUP_CTA_LG pixels a side refine a CTA per group,
-// smaller ones a warp per group
-#ifndef XG_GROUP_CTA_LG
-#define XG_GROUP_CTA_LG 5
-#endif
+
 
 // default refinement split (pixels): searches of PUs up to this size refine
 // one per thread, larger ones one per warp (xavs2gpu_me_set_tuning changes it)
@@ -1217,6 +1087,7 @@ struct MeSessionImpl {
     // tune_split pixels refine one per thread, larger ones one per warp;
     // tune_block threads per refinement CTA
     int tune_split = XG_REFINE_SPLIT, tune_block = 128;
+    int cu_groups = 1;   // CU-grouped refinement (when PMVR is off)
     // reference slot r lives in plane buffer set slot_buf[r] (rotated by
     // xavs2gpu_me_rotate_refs without moving pixels)
     int slot_buf[16] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15};
@@ -1229,7 +1100,7 @@ struct MeSessionImpl {
     RefineGroup *d_groups = nullptr;
     uint32_t *d_members = nullptr;
     int *d_small_g = nullptr, *d_large_g = nullptr;
-    int n_groups = 0, n_heavy = 0, n_small_g = 0, n_large_g = 0;   // groups [0, n_heavy): 32x32 / 64x64 CUs
+    int n_groups = 0, n_heavy = 0, n_small_g = 0, n_large_g = 0;   // groups [0, n_heavy): 32x32 and 64x64 CUs
     std::vector<RefineGroup> h_groups;
     std::vector<uint32_t> h_members, h_small_g, h_large_g;
 
@@ -1434,22 +1305,6 @@ extern "C" int xavs2gpu_me_set_pus(xavs2gpu_me_session_t *s, const xavs2gpu_pu_t
     return XAVS2GPU_OK;
 }
 
-// The CU-grouped refinement of groups [0, heavy) (a CTA each) and
-// [heavy, n) (a warp each).
-static void launch_groups(const RefineGroup *groups, int heavy, int n, const uint32_t *members, const SessView *views,
-                          int R, const xavs2gpu_me_params_t &prm, cudaStream_t st)
-{
-    if (heavy) {
-        refine_group_cta_kernel<<<heavy, kGrpCtaThreads, 0, st>>>(groups, heavy, members, views, R, prm);
-        count_launch();
-    }
-    if (n > heavy) {
-        refine_group_kernel<<<(n - heavy + kGrpWarps - 1) / kGrpWarps, 32 * kGrpWarps, 0, st>>>(
-            groups + heavy, n - heavy, members, views, R, prm);
-        count_launch();
-    }
-}
-
 // Groups the searches that are canonical partitions of an aligned CU of
 // 16x16 or larger by (reference, CU); larger CUs first.  The searches left
 // over keep the thread / warp lists.
@@ -1511,7 +1366,7 @@ static void build_groups(MeSessionImpl &m, const std::vector<int> &small, const 
         if (!grouped[i]) m.h_large_g.push_back((uint32_t)i);
     m.n_groups = (int)m.h_groups.size();
     m.n_heavy = 0;
-    while (m.n_heavy < m.n_groups && m.h_groups[m.n_heavy].lg >= XG_GROUP_CTA_LG) m.n_heavy++;
+    while (m.n_heavy < m.n_groups && m.h_groups[m.n_heavy].lg >= 5) m.n_heavy++;
     m.n_small_g = (int)m.h_small_g.size();
     m.n_large_g = (int)m.h_large_g.size();
     if (m.n_groups) {
@@ -1626,10 +1481,10 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
     // the CU-grouped refinement follows the reference's per-PU order, which
     // with PMVR depends on each PU's predictor; PMVR keeps the per-PU kernels
-    const bool grouped = !prm->enable_pmvr && m.n_groups > 0 && use_groups();
+    const bool grouped = !prm->enable_pmvr && m.cu_groups && m.n_groups > 0 && use_groups();
     const int ns = grouped ? m.n_small_g : m.n_small, nl = grouped ? m.n_large_g : m.n_large;
     const int *lst_s = grouped ? m.d_small_g : m.d_small, *lst_l = grouped ? m.d_large_g : m.d_large;
-    if (grouped) launch_groups(m.d_groups, m.n_heavy, m.n_groups, m.d_members, m.d_view, R, *prm, m.st);
+    if (grouped) launch_groups(m.d_groups, m.n_groups, m.d_members, m.d_view, R, *prm, m.st);
     if (ns) {
         refine_thread_kernel<<<(ns + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
             reinterpret_cast<const uint32_t *>(lst_s), ns, m.d_view, R, *prm);
@@ -1665,14 +1520,17 @@ extern "C" int xavs2gpu_me_session_pus(const xavs2gpu_me_session_t *s, xavs2gpu_
 extern "C" int xavs2gpu_me_set_tuning(xavs2gpu_me_session_t *s, const xavs2gpu_me_tuning_t *t)
 {
     if (!s || !t || t->refine_split_px < 0 || t->refine_split_px > 4096 ||
-        (t->refine_block != 32 && t->refine_block != 64 && t->refine_block != 128)) {
-        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_tuning", "refine_split_px must be 0..4096, refine_block 32/64/128");
+        (t->refine_block != 32 && t->refine_block != 64 && t->refine_block != 128) ||
+        (t->cu_groups != 0 && t->cu_groups != 1)) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_set_tuning",
+             "refine_split_px must be 0..4096, refine_block 32/64/128, cu_groups 0/1");
         return XAVS2GPU_ERR_ARG;
     }
     MeSessionImpl &m = s->impl;
     if (t->refine_split_px != m.tune_split) m.plan_R = -1;   // the refinement lists change
     m.tune_split = t->refine_split_px;
     m.tune_block = t->refine_block;
+    m.cu_groups = t->cu_groups;
     return XAVS2GPU_OK;
 }
 
@@ -1681,6 +1539,8 @@ extern "C" int xavs2gpu_me_get_tuning(const xavs2gpu_me_session_t *s, xavs2gpu_m
     if (!s || !t) return XAVS2GPU_ERR_ARG;
     t->refine_split_px = s->impl.tune_split;
     t->refine_block = s->impl.tune_block;
+    t->cu_groups = s->impl.cu_groups;
+    t->pad_ = 0;
     return XAVS2GPU_OK;
 }
 
@@ -1693,13 +1553,14 @@ extern "C" int xavs2gpu_me_autotune(xavs2gpu_me_session_t *s, const xavs2gpu_me_
     cudaEvent_t e0, e1;
     XG_CUDA(cudaEventCreate(&e0));
     XG_CUDA(cudaEventCreate(&e1));
-    xavs2gpu_me_tuning_t best{m.tune_split, m.tune_block}, cand;
+    xavs2gpu_me_tuning_t best{m.tune_split, m.tune_block, m.cu_groups, 0}, cand{};
     float best_t = 1e30f;
     int rc = XAVS2GPU_OK;
     for (int split : {0, 64, 128, 256, 512, 1024, 4096}) {
-        for (int blk : {64, 128}) {
+        for (int cfg = 0; cfg < 4; cfg++) {
             cand.refine_split_px = split;
-            cand.refine_block = blk;
+            cand.refine_block = cfg & 1 ? 128 : 64;
+            cand.cu_groups = cfg >> 1;
             if ((rc = xavs2gpu_me_set_tuning(s, &cand)) != XAVS2GPU_OK) break;
             ensure_plan(m, prm->search_range);
             if ((rc = xavs2gpu_me_run(s, prm)) != XAVS2GPU_OK) break;   // warm-up
@@ -1922,7 +1783,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     b->jobs.clear();
     b->views.clear();
     std::vector<uint32_t> gen, small, large, members;
-    std::vector<RefineGroup> groups, light;   // CTA-per-group ones first
+    std::vector<RefineGroup> groups, light;   // 32x32 and 64x64 CUs first (longest work first)
     const bool grouped = !prm->enable_pmvr && use_groups();
     int block = 128;
     for (int k = 0; k < n; k++) {
@@ -1939,7 +1800,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
             b->jobs.push_back(j);
         }
         for (uint32_t i : m.h_generic) gen.push_back(tag | i);
-        if (grouped) {
+        if (grouped && m.cu_groups) {
             for (uint32_t i : m.h_small_g) small.push_back(tag | i);
             for (uint32_t i : m.h_large_g) large.push_back(tag | i);
             for (int k = 0; k < m.n_groups; k++) {
@@ -1954,7 +1815,6 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         }
         if (k == 0) block = m.tune_block;
     }
-    const int n_heavy = (int)groups.size();
     groups.insert(groups.end(), light.begin(), light.end());
     BatchBuf &bb = b->buf[b->next];
     b->next ^= 1;
@@ -1998,7 +1858,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         fs_generic_kernel<<<ng < 152 * 8 ? ng : 152 * 8, 256, 0, st>>>(d_gen, ng, bb.d_views, R, lam);
         count_launch();
     }
-    if (ngr) launch_groups(bb.d_groups, n_heavy, ngr, d_members, bb.d_views, R, *prm, st);
+    if (ngr) launch_groups(bb.d_groups, ngr, d_members, bb.d_views, R, *prm, st);
     if (ns) {
         refine_thread_kernel<<<(ns + block - 1) / block, block, 0, st>>>(d_small, ns, bb.d_views, R, *prm);
         count_launch();
