@@ -239,9 +239,21 @@ def run_ours(args):
     lib.xavs2gpu_init(local)
 
     cur, refs = synth.me_workload(seed=1 + rank, width=WIDTH, height=HEIGHT)
-    pus = xg.frame_pus(WIDTH, HEIGHT, NREFS)
-    prm = xg.MeParams(RANGE, lambda_factor(QP), 1, 2, 0, 0)
-    evals = count_evals(pus, RANGE)
+    if args.me_leaf:
+        # the serving-shaped search (device timing only): every partition of
+        # the leaf CUs of a seeded split map, FS +-16, content panned by a
+        # global quarter-pel motion
+        if not args.quick:
+            raise SystemExit("--me-leaf is a --quick (device timing) workload")
+        frames = serve_content(WIDTH, HEIGHT, 3, 52)
+        cur, refs = frames[2], [frames[1], frames[0]]
+        pus, _ = xg.cu_pus(xg.split_map_cus(WIDTH, HEIGHT, 1002), WIDTH, HEIGHT, NREFS)
+        prm = xg.MeParams(16, lambda_factor(QP), 1, 2, 0, 0)
+        evals = count_evals(pus, 16)
+    else:
+        pus = xg.frame_pus(WIDTH, HEIGHT, NREFS)
+        prm = xg.MeParams(RANGE, lambda_factor(QP), 1, 2, 0, 0)
+        evals = count_evals(pus, RANGE)
     sess = xg.MeSession(WIDTH, HEIGHT, NREFS, len(pus))
     sess.set_pus(pus)
     stream = torch.cuda.ExternalStream(sess.stream())
@@ -320,7 +332,9 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": total_ms / args.steps,
                               "kernels_ms": list(phases), "interp_ms": interp_ms,
-                              "config": {"width": WIDTH, "height": HEIGHT}, "plan": [n_ctu, n_gen, n_jobs]}))
+                              "config": {"width": WIDTH, "height": HEIGHT, "leaf_partitions": bool(args.me_leaf),
+                                         "search_range": prm.search_range, "pus": int(len(pus))},
+                              "autotuned": list(tuning), "plan": [n_ctu, n_gen, n_jobs]}))
         sess.close()
         return
     # ---- end to end through the C ABI with host buffers: the pictures and
@@ -1607,6 +1621,8 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
+    ap.add_argument("--me-leaf", action="store_true",
+                    help="with --quick: the serving-shaped search (leaf-CU partitions, FS +-16) instead of every PU")
     ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter", "lookahead", "skip"],
                     default="me",
                     help="me: batched motion search (default); tq: batched transform+quant; chain: 4K full-picture "
