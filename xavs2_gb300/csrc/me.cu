@@ -804,6 +804,7 @@ struct GroupSmem {
     int t4[kGrpU4][kGrpMaxPos];
     int16_t rx[32], ry[32], rw[32], rh[32];
     int8_t ru4[32];
+    int offx[kGrpMaxPos], offy[kGrpMaxPos];   // the stage's positions relative to the centre
 };
 
 // floor(q / d) for q < 4096, d <= 16, with m = ceil(65536 / d)
@@ -826,10 +827,10 @@ __device__ __forceinline__ bool unit_covered(const GroupSmem &S, unsigned grp, i
 template <bool U4>
 __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had, int cs, const uint8_t *o,
                                             const uint8_t *const *planes, int stride, int px, int py, int ccx,
-                                            int ccy, const int (&offx)[kGrpMaxPos], const int (&offy)[kGrpMaxPos],
-                                            int P, int lane)
+                                            int ccy, int P, int lane)
 {
     constexpr int UW = U4 ? 4 : 8;
+    const int *offx = S.offx, *offy = S.offy;
     const int cols = cs / UW, nu = cols * (cs >> 2);
     const int mcols = (65536 + cols - 1) / cols;
     int(*T)[kGrpMaxPos] = U4 ? S.t4 : S.t8;
@@ -841,14 +842,14 @@ __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had
             int c[4][8];
             const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * UW;
             load_unit<U4>(o + off, stride, c);
-#pragma unroll
-            for (int k = 0; k < kGrpMaxPos; k++) {
-                if (k < P) {
-                    const int mx = ccx + offx[k], my = ccy + offy[k];
-                    const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(py + (my >> 2)) * stride +
-                                       px + (mx >> 2) + off;
-                    T[u][k] = unit_cost_pre<U4>(had, c, r, stride);
-                }
+            // one copy of the unit's cost code (the kernel stays small in
+            // the instruction cache)
+#pragma unroll 1
+            for (int k = 0; k < P; k++) {
+                const int mx = ccx + offx[k], my = ccy + offy[k];
+                const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(py + (my >> 2)) * stride + px +
+                                   (mx >> 2) + off;
+                T[u][k] = unit_cost_pre<U4>(had, c, r, stride);
             }
         }
     } else {
@@ -861,11 +862,7 @@ __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had
             int c[4][8];
             const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * UW;
             load_unit<U4>(o + off, stride, c);
-            int dx = offx[0], dy = offy[0];
-#pragma unroll
-            for (int q = 1; q < kGrpMaxPos; q++)
-                if (q == k) { dx = offx[q]; dy = offy[q]; }
-            const int mx = ccx + dx, my = ccy + dy;
+            const int mx = ccx + offx[k], my = ccy + offy[k];
             const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] + (ptrdiff_t)(py + (my >> 2)) * stride + px +
                                (mx >> 2) + off;
             T[u][k] = unit_cost_pre<U4>(had, c, r, stride);
@@ -955,6 +952,11 @@ __global__ void __launch_bounds__(32 * kGrpWarps, XG_GROUP_MINB) refine_group_ke
                     if (k == P) { offx[k] = mult * c_spiral[pat][pos][0]; offy[k] = mult * c_spiral[pat][pos][1]; }
                 P++;
             }
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < kGrpMaxPos; k++) { S.offx[k] = offx[k]; S.offy[k] = offy[k]; }
+            }
+            __syncwarp();
             unsigned pending = __ballot_sync(0xffffffffu, mem && valid);
             while (pending) {
                 const int leader = __ffs(pending) - 1;
@@ -964,11 +966,9 @@ __global__ void __launch_bounds__(32 * kGrpWarps, XG_GROUP_MINB) refine_group_ke
                 const bool need8 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && !S.ru4[lane]);
                 const bool need4 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && S.ru4[lane]);
                 if (need8)
-                    group_table<false>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
-                                       lane);
+                    group_table<false>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, P, lane);
                 if (need4)
-                    group_table<true>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, offx, offy, P,
-                                      lane);
+                    group_table<true>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, P, lane);
                 __syncwarp();
                 // each member's sums over its units
                 int acc[kGrpMaxPos];
