@@ -1740,9 +1740,6 @@ struct xavs2gpu_me_batch {
     int device = 0;
     BatchBuf buf[2];
     int next = 0;
-    std::vector<CtuJob> jobs;
-    std::vector<uint32_t> lists;
-    std::vector<SessView> views;
 };
 
 extern "C" xavs2gpu_me_batch_t *xavs2gpu_me_batch_create(void)
@@ -1750,6 +1747,13 @@ extern "C" xavs2gpu_me_batch_t *xavs2gpu_me_batch_create(void)
     auto *b = new xavs2gpu_me_batch();
     b->device = current_device();
     for (auto &x : b->buf) XG_CUDA(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+    // the batch buffers grow with stream-ordered allocations: keep freed
+    // blocks in the device's pool
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, b->device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     return b;
 }
 
@@ -1765,13 +1769,16 @@ extern "C" void xavs2gpu_me_batch_destroy(xavs2gpu_me_batch_t *b)
     delete b;
 }
 
+// Stream-ordered growth of a batch buffer: no device-wide synchronisation
+// (the buffer's previous launch has completed: its done event was waited
+// for), freed blocks stay in the device's pool.
 template <typename T>
-static void grow(T *&p, size_t &cap, size_t need)
+static void grow(T *&p, size_t &cap, size_t need, cudaStream_t st)
 {
     if (need <= cap) return;
-    cudaFree(p);
-    cap = need + need / 4 + 64;
-    XG_CUDA(cudaMalloc((void **)&p, sizeof(T) * cap));
+    if (p) XG_CUDA(cudaFreeAsync(p, st));
+    cap = need + need / 2 + 64;
+    XG_CUDA(cudaMallocAsync((void **)&p, sizeof(T) * cap, st));
 }
 
 extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session_t *const *sessions, int n,
@@ -1786,11 +1793,9 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     XG_CUDA(cudaSetDevice(b->device));
     const int R = prm->search_range, lam = prm->lambda_factor;
     cudaStream_t st = (cudaStream_t)stream;
-    b->jobs.clear();
-    b->views.clear();
-    std::vector<uint32_t> gen, small, large, members;
-    std::vector<RefineGroup> groups, light;   // 32x32 and 64x64 CUs first (longest work first)
+    // pass 1: plans and sizes
     const bool grouped = !prm->enable_pmvr && use_groups();
+    size_t nj = 0, ng = 0, ns = 0, nl = 0, nm = 0, nheavy = 0, ngr = 0;
     int block = 128;
     for (int k = 0; k < n; k++) {
         MeSessionImpl &m = sessions[k]->impl;
@@ -1799,78 +1804,97 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
             return XAVS2GPU_ERR_ARG;
         }
         ensure_plan(m, R);
-        b->views.push_back(m.h_view);
-        const uint32_t tag = (uint32_t)k << kSessShift;
-        for (CtuJob j : m.plan.h_jobs) {
-            j.sess = (uint8_t)k;
-            b->jobs.push_back(j);
-        }
-        for (uint32_t i : m.h_generic) gen.push_back(tag | i);
-        if (grouped && m.cu_groups) {
-            for (uint32_t i : m.h_small_g) small.push_back(tag | i);
-            for (uint32_t i : m.h_large_g) large.push_back(tag | i);
-            for (int k = 0; k < m.n_groups; k++) {
-                RefineGroup d = m.h_groups[k];
-                d.first += (uint32_t)members.size();
-                (k < m.n_heavy ? groups : light).push_back(d);
-            }
-            for (uint32_t i : m.h_members) members.push_back(tag | i);
-        } else {
-            for (uint32_t i : m.h_small) small.push_back(tag | i);
-            for (uint32_t i : m.h_large) large.push_back(tag | i);
+        const bool g = grouped && m.cu_groups;
+        nj += m.plan.h_jobs.size();
+        ng += m.h_generic.size();
+        ns += g ? m.h_small_g.size() : m.h_small.size();
+        nl += g ? m.h_large_g.size() : m.h_large.size();
+        if (g) {
+            nm += m.h_members.size();
+            nheavy += (size_t)m.n_heavy;
+            ngr += (size_t)m.n_groups;
         }
         if (k == 0) block = m.tune_block;
     }
-    groups.insert(groups.end(), light.begin(), light.end());
     BatchBuf &bb = b->buf[b->next];
     b->next ^= 1;
-    if (bb.used) XG_CUDA(cudaEventSynchronize(bb.done));   // its lists may still be read
-    b->lists.clear();
-    b->lists.insert(b->lists.end(), gen.begin(), gen.end());
-    b->lists.insert(b->lists.end(), small.begin(), small.end());
-    b->lists.insert(b->lists.end(), large.begin(), large.end());
-    b->lists.insert(b->lists.end(), members.begin(), members.end());
-    grow(bb.d_jobs, bb.cap_jobs, b->jobs.size());
-    grow(bb.d_lists, bb.cap_lists, b->lists.size());
-    grow(bb.d_views, bb.cap_views, b->views.size());
-    grow(bb.d_groups, bb.cap_groups, groups.size());
-    const size_t bj = sizeof(CtuJob) * b->jobs.size(), bl = sizeof(uint32_t) * b->lists.size();
-    const size_t bv = sizeof(SessView) * b->views.size(), bg = sizeof(RefineGroup) * groups.size();
+    if (bb.used) XG_CUDA(cudaEventSynchronize(bb.done));   // its staging and lists may still be read
+    const size_t nlist = ng + ns + nl + nm;
+    grow(bb.d_jobs, bb.cap_jobs, nj, st);
+    grow(bb.d_lists, bb.cap_lists, nlist, st);
+    grow(bb.d_views, bb.cap_views, (size_t)n, st);
+    grow(bb.d_groups, bb.cap_groups, ngr, st);
+    const size_t bj = sizeof(CtuJob) * nj, bl = sizeof(uint32_t) * nlist;
+    const size_t bv = sizeof(SessView) * n, bg = sizeof(RefineGroup) * ngr;
     const size_t oj = 0, ol = align_up(bj), ov = ol + align_up(bl), og = ov + align_up(bv), need = og + align_up(bg);
     if (need > bb.cap_stage) {
         cudaFreeHost(bb.h_stage);
-        bb.cap_stage = need + need / 4 + 4096;
+        bb.cap_stage = need + need / 2 + 4096;
         XG_CUDA(cudaMallocHost((void **)&bb.h_stage, bb.cap_stage));
     }
-    memcpy(bb.h_stage + oj, b->jobs.data(), bj);
-    memcpy(bb.h_stage + ol, b->lists.data(), bl);
-    memcpy(bb.h_stage + ov, b->views.data(), bv);
-    if (bg) memcpy(bb.h_stage + og, groups.data(), bg);
+    // pass 2: written straight into the pinned staging buffer, list entries
+    // tagged with their session's index in this launch; groups of 32x32 and
+    // 64x64 CUs first (longest work first)
+    CtuJob *J = reinterpret_cast<CtuJob *>(bb.h_stage + oj);
+    uint32_t *Lg = reinterpret_cast<uint32_t *>(bb.h_stage + ol), *Ls = Lg + ng, *Ll = Ls + ns, *Lm = Ll + nl;
+    SessView *V = reinterpret_cast<SessView *>(bb.h_stage + ov);
+    RefineGroup *Gh = reinterpret_cast<RefineGroup *>(bb.h_stage + og), *Gl = Gh + nheavy;
+    uint32_t mbase = 0;
+    auto put = [](uint32_t *&dst, const std::vector<uint32_t> &src, uint32_t tag) {
+        const uint32_t *p = src.data();
+        const size_t c = src.size();
+        for (size_t i = 0; i < c; i++) dst[i] = tag | p[i];
+        dst += c;
+    };
+    for (int k = 0; k < n; k++) {
+        MeSessionImpl &m = sessions[k]->impl;
+        const bool g = grouped && m.cu_groups;
+        const uint32_t tag = (uint32_t)k << kSessShift;
+        V[k] = m.h_view;
+        for (const CtuJob &j0 : m.plan.h_jobs) {
+            *J = j0;
+            J->sess = (uint8_t)k;
+            J++;
+        }
+        put(Lg, m.h_generic, tag);
+        put(Ls, g ? m.h_small_g : m.h_small, tag);
+        put(Ll, g ? m.h_large_g : m.h_large, tag);
+        if (g) {
+            for (int q = 0; q < m.n_groups; q++) {
+                RefineGroup d = m.h_groups[q];
+                d.first += mbase;
+                *(q < m.n_heavy ? Gh++ : Gl++) = d;
+            }
+            put(Lm, m.h_members, tag);
+            mbase += (uint32_t)m.h_members.size();
+        }
+    }
     if (bj) XG_CUDA(cudaMemcpyAsync(bb.d_jobs, bb.h_stage + oj, bj, cudaMemcpyHostToDevice, st));
     if (bl) XG_CUDA(cudaMemcpyAsync(bb.d_lists, bb.h_stage + ol, bl, cudaMemcpyHostToDevice, st));
     XG_CUDA(cudaMemcpyAsync(bb.d_views, bb.h_stage + ov, bv, cudaMemcpyHostToDevice, st));
     if (bg) XG_CUDA(cudaMemcpyAsync(bb.d_groups, bb.h_stage + og, bg, cudaMemcpyHostToDevice, st));
-    const int ng = (int)gen.size(), ns = (int)small.size(), nl = (int)large.size(), ngr = (int)groups.size();
     const uint32_t *d_gen = bb.d_lists, *d_small = bb.d_lists + ng, *d_large = bb.d_lists + ng + ns;
     const uint32_t *d_members = bb.d_lists + ng + ns + nl;
     reset_keys_kernel<<<152 * 4, 256, 0, st>>>(bb.d_views, n);
     count_launch();
     if (ng) {
-        me_init_list_kernel<<<(ng * 32 + 127) / 128, 128, 0, st>>>(d_gen, ng, bb.d_views, lam);
+        me_init_list_kernel<<<(unsigned)((ng * 32 + 127) / 128), 128, 0, st>>>(d_gen, (int)ng, bb.d_views, lam);
         count_launch();
     }
-    ctu_jobs_run(bb.d_jobs, (int)b->jobs.size(), bb.d_views, *prm, st);
+    ctu_jobs_run(bb.d_jobs, (int)nj, bb.d_views, *prm, st);
     if (ng) {
-        fs_generic_kernel<<<ng < 152 * 8 ? ng : 152 * 8, 256, 0, st>>>(d_gen, ng, bb.d_views, R, lam);
+        fs_generic_kernel<<<(unsigned)(ng < 152 * 8 ? ng : 152 * 8), 256, 0, st>>>(d_gen, (int)ng, bb.d_views, R, lam);
         count_launch();
     }
-    if (ngr) launch_groups(bb.d_groups, ngr, d_members, bb.d_views, R, *prm, st);
+    if (ngr) launch_groups(bb.d_groups, (int)ngr, d_members, bb.d_views, R, *prm, st);
     if (ns) {
-        refine_thread_kernel<<<(ns + block - 1) / block, block, 0, st>>>(d_small, ns, bb.d_views, R, *prm);
+        refine_thread_kernel<<<(unsigned)((ns + block - 1) / block), block, 0, st>>>(d_small, (int)ns, bb.d_views, R,
+                                                                                  *prm);
         count_launch();
     }
     if (nl) {
-        refine_warp_list_kernel<<<(nl * 32 + block - 1) / block, block, 0, st>>>(d_large, nl, bb.d_views, R, *prm);
+        refine_warp_list_kernel<<<(unsigned)((nl * 32 + block - 1) / block), block, 0, st>>>(d_large, (int)nl,
+                                                                                          bb.d_views, R, *prm);
         count_launch();
     }
     XG_CUDA(cudaEventRecord(bb.done, st));
