@@ -1442,7 +1442,7 @@ def run_serve(args):
         layouts.append(xg.cu_pus(xg.split_map_cus(w, h, 1000 + sid), w, h, 2))
 
     def make_server(max_frames):
-        cfg = xg.ServerConfig(args.serve_hbm_gb << 30, 48 << 20, max_frames, QP, prm)
+        cfg = xg.ServerConfig(args.serve_hbm_gb << 30, args.serve_batch_mpx << 20, max_frames, QP, prm)
         srv = xg.Server(cfg)
         streams = []
         for sid in range(nstreams):
@@ -1481,6 +1481,7 @@ def run_serve(args):
                    "resolutions": {"%dx%d" % SERVE_RES[r]: int((res_idx == r).sum()) for r in range(4)},
                    "arrivals": "Poisson 30 fps per stream", "seconds": args.serve_seconds, "warm_s": args.serve_warm,
                    "search_range": args.serve_range, "qp": QP, "refs": 2,
+                   "batch_cap": {"pictures": args.serve_batch, "luma_mpx": args.serve_batch_mpx},
                    "picture_job": "reference update + sub-pel planes, FS +-%d + quarter-pel SATD over the leaf-CU "
                                   "PUs of a seeded split map, MC residual, TU chain, reconstruction" % args.serve_range},
         "batched": batched, "unbatched_same_trace": alone,
@@ -1637,6 +1638,10 @@ def main():
     ap.add_argument("--serve-warm", type=float, default=2.0)
     ap.add_argument("--serve-range", type=int, default=16)
     ap.add_argument("--serve-batch", type=int, default=64)
+    # luma pixels per batch (MiB): about one and a half 2160p pictures keeps a
+    # burst of arrivals from forming one long batch (p99 11.7 ms against 16-19
+    # ms with 48 MiB batches at 64 streams)
+    ap.add_argument("--serve-batch-mpx", type=int, default=12)
     ap.add_argument("--serve-pool", type=int, default=4)
     ap.add_argument("--serve-hbm-gb", type=int, default=64)
     args = ap.parse_args()
