@@ -29,6 +29,12 @@
 #include <thread>
 #include <vector>
 
+// batch buffer sets (each with its own CUDA stream): while one batch runs,
+// the next ones are formed and enqueued
+#ifndef XG_SERVE_SETS
+#define XG_SERVE_SETS 2
+#endif
+
 namespace xg {
 
 int tq_batch_launch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
@@ -213,7 +219,7 @@ struct xavs2gpu_server {
     int64_t hbm_used = 0;
     int64_t max_cus = 0;
     std::vector<Stream *> streams;
-    BatchSet sets[2];
+    BatchSet sets[XG_SERVE_SETS];
     int next_set = 0;
     std::mutex mu;
     std::condition_variable cv;
@@ -307,8 +313,8 @@ void scheduler(xavs2gpu_server_t *s)
     std::unique_lock<std::mutex> lk(s->mu);
     while (!s->stop) {
         BatchSet *free_set = nullptr;
-        for (int t = 0; t < 2 && !free_set; t++) {
-            BatchSet &c = s->sets[(s->next_set + t) & 1];
+        for (int t = 0; t < XG_SERVE_SETS && !free_set; t++) {
+            BatchSet &c = s->sets[(s->next_set + t) % XG_SERVE_SETS];
             if (!c.busy) free_set = &c;
         }
         // take the arrived pictures whose stream is idle, oldest first
@@ -337,7 +343,7 @@ void scheduler(xavs2gpu_server_t *s)
         b.busy = true;
         b.jobs = take;
         for (auto &j : take) s->streams[j.stream]->in_flight = true;
-        s->next_set = (int)(&b - s->sets) ^ 1;
+        s->next_set = ((int)(&b - s->sets) + 1) % XG_SERVE_SETS;
         lk.unlock();
         const int64_t t0 = now_ns();
         enqueue_batch(s, b);
