@@ -1051,6 +1051,10 @@ namespace xg {
 static constexpr bool use_groups() { return XG_REFINE_GROUPS != 0; }
 
 
+#ifndef XG_REFINE_LPT
+#define XG_REFINE_LPT 1
+#endif
+
 // default refinement split (pixels): searches of PUs up to this size refine
 // one per thread, larger ones one per warp (xavs2gpu_me_set_tuning changes it)
 #ifndef XG_REFINE_SPLIT
@@ -1442,6 +1446,13 @@ static void ensure_plan(MeSessionImpl &m, int R)
         const int i = order[k];
         (h_pu_w[m.h_pus[i].part] * h_pu_h[m.h_pus[i].part] <= m.tune_split ? small : large).push_back(i);
     }
+#if XG_REFINE_LPT
+    // largest searches first (shape groups kept together): the long ones
+    // start early instead of forming the launch's tail
+    auto area = [&](int i) { return h_pu_w[m.h_pus[i].part] * h_pu_h[m.h_pus[i].part]; };
+    std::stable_sort(small.begin(), small.end(), [&](int a, int b) { return area(a) > area(b); });
+    std::stable_sort(large.begin(), large.end(), [&](int a, int b) { return area(a) > area(b); });
+#endif
     m.n_small = (int)small.size();
     m.n_large = (int)large.size();
     m.h_small.assign(small.begin(), small.end());
