@@ -316,154 +316,6 @@ __global__ void __launch_bounds__(128) refine_kernel(const xavs2gpu_pu_t *__rest
     if (lane == 0) out[i] = res;
 }
 
-// Shape-grouped refinement.  PU searches are sorted by shape; a warp takes G
-// searches of one shape and spreads every (search, position, SATD unit) item
-// of a refinement step over its lanes, accumulating unit costs in shared
-// memory, so small PUs do not leave most lanes idle.
-struct RefineTask {
-    int32_t first;    // index of the first search in the shape-sorted order
-    int16_t count;    // G searches of the same shape
-    int16_t part;
-};
-
-constexpr int kRefineWarps = 4;
-constexpr int kRefineMaxG = 3;
-
-// cost of one rounding unit (SATD) or one 4x4/8x4 tile (SAD) of a PU at
-// quarter-pel (mx, my)
-__device__ __forceinline__ int unit_cost(bool had, bool u4, const uint8_t *o, const uint8_t *r, int stride, int uw)
-{
-    if (had) return satd_unit_d(u4, o, stride, r, stride);
-    int s = 0;
-    for (int y = 0; y < 4; y++)
-        for (int x = 0; x < uw; x++) s += iabs_d((int)o[y * stride + x] - (int)r[y * stride + x]);
-    return s;
-}
-
-__global__ void __launch_bounds__(32 * kRefineWarps) refine_grouped_kernel(
-    const RefineTask *__restrict__ tasks, int ntasks, const int *__restrict__ order,
-    const xavs2gpu_pu_t *__restrict__ pus, const PuState *__restrict__ state,
-    const unsigned long long *__restrict__ keys, const uint8_t *__restrict__ cur,
-    const uint8_t *const *ref_planes, Geometry g, int R, xavs2gpu_me_params_t prm,
-    xavs2gpu_me_result_t *__restrict__ out)
-{
-    __shared__ int acc[kRefineWarps][kRefineMaxG][9];
-    __shared__ int s_x[kRefineWarps][kRefineMaxG], s_y[kRefineWarps][kRefineMaxG];
-    __shared__ int s_cx[kRefineWarps][kRefineMaxG], s_cy[kRefineWarps][kRefineMaxG];
-    __shared__ int s_ref[kRefineWarps][kRefineMaxG], s_ok[kRefineWarps][kRefineMaxG];
-    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t = blockIdx.x * kRefineWarps + wi;
-    if (t >= ntasks) return;
-    const RefineTask task = tasks[t];
-    const int G = task.count, part = task.part;
-    const int w = c_pu_w[part], h = c_pu_h[part];
-    const bool had = prm.use_hadamard != 0;
-    const bool u4 = had ? satd_unit4(w, h) : (w == 4 || w == 12);
-    const int uw = u4 ? 4 : 8, nux = w / uw, nu = nux * (h >> 2);
-    const int lam = prm.lambda_factor;
-    const int pat = prm.fast_sub_me ? 1 : 0, step = prm.fast_sub_me ? 2 : 1;
-    int i_pu = -1, icost = 0, bx = 0, by = 0, best = 0, pmx = 0, pmy = 0;
-    xavs2gpu_me_result_t res;
-    if (lane < G) {
-        i_pu = order[task.first + lane];
-        const xavs2gpu_pu_t p = pus[i_pu];
-        const PuState st = state[i_pu];
-        const unsigned long long key = keys[i_pu];
-        const bool ok = st.valid && key != kNoKey;
-        pmx = p.mvp_x; pmy = p.mvp_y;
-        if (ok) {
-            icost = (int)(key >> 32);
-            const unsigned order_ = (unsigned)(key & 0xffffffffu);
-            int mx, my;
-            if (order_ < 2) { mx = st.cand[order_][0]; my = st.cand[order_][1]; }
-            else {
-                const int q = (int)order_ - 2;
-                mx = st.cx + q % (2 * R) - R;
-                my = st.cy + q / (2 * R) - R;
-            }
-            res.imv_x = (int16_t)mx; res.imv_y = (int16_t)my; res.icost = icost;
-            bx = mx * 4; by = my * 4; best = icost;
-        }
-        s_x[wi][lane] = p.x; s_y[wi][lane] = p.y; s_ref[wi][lane] = p.ref;
-        s_cx[wi][lane] = bx; s_cy[wi][lane] = by; s_ok[wi][lane] = ok;
-        for (int k = 0; k < 9; k++) acc[wi][lane][k] = 0;
-    }
-    __syncwarp();
-    if (prm.fractional_me) {
-        // step 1: centre (SATD only) + half-pel positions; step 2: quarter-pel
-        for (int stage = 0; stage < (prm.fractional_me > 1 ? 2 : 1); stage++) {
-            const int mul = stage == 0 ? 2 : 1;
-            const int items = G * 9 * nu;
-            for (int q = lane; q < items; q += 32) {
-                const int gg = q / (9 * nu), rem = q - gg * 9 * nu, pos = rem / nu, u = rem - pos * nu;
-                if (!s_ok[wi][gg]) continue;
-                if (pos == 0 && (stage == 1 || !had)) continue;          // centre cost already known
-                if (pos > 0 && ((pos - 1) % step) != 0) continue;        // spiral-2 uses every other point
-                const int cx = s_cx[wi][gg], cy = s_cy[wi][gg];
-                const int mx = cx + mul * c_spiral[pat][pos][0], my = cy + mul * c_spiral[pat][pos][1];
-                const int uy = u / nux, ux = u - uy * nux;
-                const int px = s_x[wi][gg] + ux * uw, py = s_y[wi][gg] + uy * 4;
-                const uint8_t *o = cur + (ptrdiff_t)py * g.stride + px;
-                const uint8_t *r = ref_planes[16 * s_ref[wi][gg] + ((my & 3) << 2) + (mx & 3)] +
-                                   (ptrdiff_t)(py + (my >> 2)) * g.stride + px + (mx >> 2);
-                atomicAdd(&acc[wi][gg][pos], unit_cost(had, u4, o, r, g.stride, uw));
-            }
-            __syncwarp();
-            if (lane < G && s_ok[wi][lane]) {
-                const int cx = s_cx[wi][lane], cy = s_cy[wi][lane];
-                if (stage == 0 && had) best = acc[wi][lane][0] + mv_cost_hd(lam, cx, cy, pmx, pmy);
-                const int ctr_x = (pmx >> 1) << 1, ctr_y = (pmy >> 1) << 1;
-                for (int pos = 1; pos < 9; pos += step) {
-                    const int sx = c_spiral[pat][pos][0], sy = c_spiral[pat][pos][1];
-                    int mx = cx + mul * sx, my = cy + mul * sy;
-                    if (stage == 1 && prm.enable_pmvr) {
-                        // pmvr_adapt_mv (me.c:412-424), TH_PMVR = 2; such positions
-                        // were computed at the plain quarter-pel offset, so the
-                        // adapted ones are evaluated here directly
-                        if (abs(cx - ctr_x) > 2 || abs(cy - ctr_y) > 2) {
-                            mx = cx + 2 * sx; my = cy + 2 * sy;
-                            if (abs(mx - ctr_x) <= 2 && abs(my - ctr_y) <= 2) continue;
-                        } else {
-                            if (abs(mx - ctr_x) > 2 || abs(my - ctr_y) > 2) continue;
-                        }
-                    }
-                    int c;
-                    if (stage == 1 && prm.enable_pmvr && (mx != cx + sx || my != cy + sy)) {
-                        c = 0;
-                        const uint8_t *o = cur + (ptrdiff_t)s_y[wi][lane] * g.stride + s_x[wi][lane];
-                        const uint8_t *r = ref_planes[16 * s_ref[wi][lane] + ((my & 3) << 2) + (mx & 3)] +
-                                           (ptrdiff_t)(s_y[wi][lane] + (my >> 2)) * g.stride + s_x[wi][lane] + (mx >> 2);
-                        for (int u = 0; u < nu; u++) {
-                            const int uy = u / nux, ux = u - uy * nux;
-                            c += unit_cost(had, u4, o + (ptrdiff_t)uy * 4 * g.stride + ux * uw,
-                                           r + (ptrdiff_t)uy * 4 * g.stride + ux * uw, g.stride, uw);
-                        }
-                    } else {
-                        c = acc[wi][lane][pos];
-                    }
-                    c += mv_cost_hd(lam, mx, my, pmx, pmy);
-                    if (c < best) { best = c; bx = mx; by = my; }
-                }
-                s_cx[wi][lane] = bx; s_cy[wi][lane] = by;
-                for (int k = 0; k < 9; k++) acc[wi][lane][k] = 0;
-            }
-            __syncwarp();
-        }
-    }
-    if (lane < G) {
-        if (!s_ok[wi][lane]) {
-            res.bmv_x = res.bmv_y = res.imv_x = res.imv_y = 0;
-            res.bcost = res.icost = 1 << 30;
-            res.mvcost = 0;
-        } else {
-            res.bmv_x = (int16_t)bx; res.bmv_y = (int16_t)by;
-            res.bcost = best;
-            res.mvcost = mv_cost_hd(lam, bx, by, pmx, pmy);
-        }
-        out[i_pu] = res;
-    }
-}
-
 // ---- refinement v3: one thread per search (PUs up to 256 pixels) ---------------
 // The thread runs the reference's sequential loop itself: the positions of a
 // step are fixed by the centre, so their costs are accumulated unit by unit
@@ -1086,9 +938,6 @@ struct MeSessionImpl {
     int plan_R = -1;               // search range the plan was built for (-1: stale)
     int n_ctu_pus = 0;
     std::vector<xavs2gpu_pu_t> h_pus;
-    int *d_order = nullptr;                 // PU indices sorted by shape
-    RefineTask *d_tasks = nullptr;          // refinement warp tasks
-    int n_tasks = 0;
     int *d_small = nullptr, *d_large = nullptr;   // refinement lists: thread / warp per search
     int n_small = 0, n_large = 0;
     bool profiling = false;
@@ -1193,8 +1042,6 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     XG_CUDA(cudaMalloc((void **)&m.d_keys, sizeof(unsigned long long) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_state, sizeof(PuState) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_generic, sizeof(int) * max_pus));
-    XG_CUDA(cudaMalloc((void **)&m.d_order, sizeof(int) * max_pus));
-    XG_CUDA(cudaMalloc((void **)&m.d_tasks, sizeof(RefineTask) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_small, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_large, sizeof(int) * max_pus));
     XG_CUDA(cudaMalloc((void **)&m.d_groups, sizeof(RefineGroup) * max_pus));
@@ -1218,7 +1065,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     cudaFree(m.d_planes); cudaFree(m.d_plane_ptrs); cudaFree(m.d_ref0);
     cudaFreeHost(m.h_stage); cudaFree(m.d_upload);
     cudaFree(m.d_pus); cudaFree(m.d_res); cudaFreeHost(m.h_res); cudaFree(m.d_keys);
-    cudaFree(m.d_state); cudaFree(m.d_generic); cudaFree(m.d_order); cudaFree(m.d_tasks);
+    cudaFree(m.d_state); cudaFree(m.d_generic); 
     cudaFree(m.d_small); cudaFree(m.d_large);
     cudaFree(m.d_groups); cudaFree(m.d_members); cudaFree(m.d_small_g); cudaFree(m.d_large_g);
     for (auto &e : m.ev)
@@ -1420,27 +1267,12 @@ static void ensure_plan(MeSessionImpl &m, int R)
         if (m.n) XG_CUDA(cudaMemcpyAsync(m.d_state, st.data(), sizeof(PuState) * m.n, cudaMemcpyHostToDevice, m.st));
         XG_CUDA(cudaStreamSynchronize(m.st));
     }
-    // refinement order: PU searches grouped by shape, G per warp task
+    // refinement order: PU searches grouped by shape
     std::vector<int> order(m.n), start(kNumParts + 1, 0);
     for (const auto &p : m.h_pus) start[p.part + 1]++;
     for (int k = 0; k < kNumParts; k++) start[k + 1] += start[k];
     std::vector<int> fill(start.begin(), start.end() - 1);
     for (int i = 0; i < m.n; i++) order[fill[m.h_pus[i].part]++] = i;
-    std::vector<RefineTask> tasks;
-    for (int k = 0; k < kNumParts; k++) {
-        const int w = h_pu_w[k], h = h_pu_h[k];
-        const int units = (w * h) / 32 > 0 ? (w * h) / 32 : 1;     // 8x4 units (4x4 shapes: about the same)
-        int G = 32 / (9 * units);
-        G = G < 1 ? 1 : (G > kRefineMaxG ? kRefineMaxG : G);
-        for (int f = start[k]; f < start[k + 1]; f += G) {
-            RefineTask t;
-            t.first = f;
-            t.count = (int16_t)(start[k + 1] - f < G ? start[k + 1] - f : G);
-            t.part = (int16_t)k;
-            tasks.push_back(t);
-        }
-    }
-    m.n_tasks = (int)tasks.size();
     std::vector<int> small, large;
     for (int k = 0; k < m.n; k++) {
         const int i = order[k];
@@ -1459,10 +1291,7 @@ static void ensure_plan(MeSessionImpl &m, int R)
     m.h_large.assign(large.begin(), large.end());
     if (m.n_small) XG_CUDA(cudaMemcpyAsync(m.d_small, small.data(), sizeof(int) * m.n_small, cudaMemcpyHostToDevice, m.st));
     if (m.n_large) XG_CUDA(cudaMemcpyAsync(m.d_large, large.data(), sizeof(int) * m.n_large, cudaMemcpyHostToDevice, m.st));
-    if (m.n) XG_CUDA(cudaMemcpyAsync(m.d_order, order.data(), sizeof(int) * m.n, cudaMemcpyHostToDevice, m.st));
     build_groups(m, small, large);
-    if (m.n_tasks)
-        XG_CUDA(cudaMemcpyAsync(m.d_tasks, tasks.data(), sizeof(RefineTask) * m.n_tasks, cudaMemcpyHostToDevice, m.st));
     refresh_view(m);
     XG_CUDA(cudaStreamSynchronize(m.st));
     m.plan_R = R;
