@@ -210,7 +210,9 @@ constexpr int kN = 9;             // INTRA_MODE_NUM_FOR_RDO (defines.h:290)
 constexpr int kTW = 11;           // warps per CTA: 3 modes each
 constexpr int kTT = kTW * 32;
 constexpr int kCls = 25;
-constexpr int kEdgeArea = 1984;   // max over classes of G * align4(edge window), plus word-read slack
+// max over classes of G * (align4(edge window) + 4: the window's offset in
+// its first word), plus word-read slack
+constexpr int kEdgeArea = 2112;
 
 struct Geo {
     int w, h, uw, nux, lanes, iters, G, lo, hi, R;
@@ -236,15 +238,28 @@ __host__ __device__ __forceinline__ Geo geo_of(int c)
     return g;
 }
 
-struct TileSmem {
-    uint8_t edge[kEdgeArea];          // block b: edge samples -lo..hi at b * R
+// Two tile buffers: the next tile is copied in (cp.async) while the warps
+// score the current one.
+struct TileBuf {
+    uint8_t edge[kEdgeArea];          // block b: the words holding edge samples -lo..hi at b * (R + 4)
     uint8_t fenc[4096 + 64];          // block b: w x h source samples at b * (w * h + 4)
-    int satd[32][33];
     int64_t eoff[32], foff[32];
     int idx[32], dc_avail[32], mpm[32][2];
+    int emis[32];                     // byte offset of sample -lo in its first word
+};
+struct TileSmem {
+    TileBuf buf[2];
+    int satd[32][33];
     int next_mode;
     int tile_base[kCls + 1], order[kCls], start[kCls], count[kCls];
 };
+
+__device__ __forceinline__ void cp_async4(void *dst_smem, const void *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Modes in the order warps take them: the per-sample two-edge modes first,
 // then the one-edge angles, then the cheap ones (longest work first).
@@ -584,47 +599,96 @@ __global__ void __launch_bounds__(kTT, XG_RMD_MINB) rmd_tile_kernel(const xavs2g
     }
     __syncthreads();
     const int total = s.tile_base[kCls];
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        int k = 0;
+    // tile t's class, its first block and its block count
+    auto tile_of = [&](int t, int &k, Geo &g, int &first, int &nb) {
+        k = 0;
         while (t >= s.tile_base[k + 1]) k++;
         const int c = s.order[k];
-        const Geo g = geo_of(c);
-        const int first = s.start[c] + (t - s.tile_base[k]) * g.G;
+        g = geo_of(c);
+        first = s.start[c] + (t - s.tile_base[k]) * g.G;
         const int rem = s.start[c] + s.count[c] - first;
-        const int nb = rem < g.G ? rem : g.G;
+        nb = rem < g.G ? rem : g.G;
+    };
+    // descriptors of tile t into buffer p (threads < nb)
+    auto stage_desc = [&](int p, int first, int nb) {
+        TileBuf &B = s.buf[p];
         if (tid < nb) {
             const int bi = sorted[first + tid];
             const xavs2gpu_intra_block_t b = blocks[bi];
-            s.idx[tid] = bi;
-            s.eoff[tid] = b.edge_offset;
-            s.foff[tid] = b.fenc_offset;
-            s.dc_avail[tid] = b.dc_avail;
-            s.mpm[tid][0] = b.mpm[0];
-            s.mpm[tid][1] = b.mpm[1];
+            B.idx[tid] = bi;
+            B.eoff[tid] = b.edge_offset;
+            B.foff[tid] = b.fenc_offset;
+            B.dc_avail[tid] = b.dc_avail;
+            B.mpm[tid][0] = b.mpm[0];
+            B.mpm[tid][1] = b.mpm[1];
+            B.emis[tid] = (int)((uintptr_t)(edges + b.edge_offset - edge_below(b.width, b.height)) & 3);
         }
-        if (tid == 0) s.next_mode = 0;
-        __syncthreads();
-        // stage the edge windows and the source blocks (one padding word
-        // after each block keeps the lanes' rows in distinct banks)
-        const int ew = g.lo + g.hi + 1;
-        for (int e = tid; e < nb * ew; e += kTT) {
-            const int b = e / ew, r = e - b * ew;
-            s.edge[b * g.R + r] = edges[s.eoff[b] - g.lo + r];
+    };
+    // samples of tile t into buffer p: the edge windows as the aligned words
+    // holding them, the source rows as words when they are 4-byte aligned
+    // (else bytes); asynchronous copies (cp.async) where possible
+    auto stage_data = [&](int p, const Geo &g, int nb) {
+        TileBuf &B = s.buf[p];
+        const int ew = g.lo + g.hi + 1, RB = g.R + 4;
+        const int nw = (ew + 3 + 3) >> 2;   // words covering the window at any offset
+        for (int e = tid; e < nb * nw; e += kTT) {
+            const int b = e / nw, q = e - b * nw;
+            const uint8_t *src = edges + B.eoff[b] - g.lo;
+            const uint8_t *w0 = reinterpret_cast<const uint8_t *>((uintptr_t)src & ~(uintptr_t)3);
+            cp_async4(B.edge + b * RB + 4 * q, w0 + 4 * q);
         }
         const int area = g.w * g.h, fpitch = area + 4;
         const int lw = ilog2d(g.w);
-        for (int e = tid; e < nb * area; e += kTT) {
-            const int b = e / area, r = e - b * area, y = r >> lw, x = r & (g.w - 1);
-            s.fenc[b * fpitch + r] = fenc[s.foff[b] + (int64_t)y * fenc_stride + x];
+        bool al = (fenc_stride & 3) == 0;
+        for (int b = 0; b < nb; b++) al = al && ((uintptr_t)(fenc + B.foff[b]) & 3) == 0;
+        if (al) {
+            const int wpr = g.w >> 2, lwr = ilog2d(wpr);
+            for (int e = tid; e < nb * (area >> 2); e += kTT) {
+                const int b = e / (area >> 2), r = e - b * (area >> 2), y = r >> lwr, x = (r & (wpr - 1)) << 2;
+                cp_async4(B.fenc + b * fpitch + (y << lw) + x, fenc + B.foff[b] + (int64_t)y * fenc_stride + x);
+            }
+        } else {
+            for (int e = tid; e < nb * area; e += kTT) {
+                const int b = e / area, r = e - b * area, y = r >> lw, x = r & (g.w - 1);
+                B.fenc[b * fpitch + r] = fenc[B.foff[b] + (int64_t)y * fenc_stride + x];
+            }
         }
+    };
+    int t = blockIdx.x, p = 0;
+    if (t < total) {
+        int k, first, nb;
+        Geo g;
+        tile_of(t, k, g, first, nb);
+        stage_desc(0, first, nb);
         __syncthreads();
+        stage_data(0, g, nb);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    for (; t < total; t += gridDim.x, p ^= 1) {
+        int k, first, nb;
+        Geo g;
+        tile_of(t, k, g, first, nb);
+        TileBuf &B = s.buf[p];
+        // the next tile's descriptors, then its samples in flight while this one is scored
+        const int tn = t + gridDim.x;
+        int kn = 0, firstn = 0, nbn = 0;
+        Geo gn;
+        if (tn < total) {
+            tile_of(tn, kn, gn, firstn, nbn);
+            stage_desc(p ^ 1, firstn, nbn);
+        }
+        if (tid == 0) s.next_mode = 0;
+        __syncthreads();
+        if (tn < total) stage_data(p ^ 1, gn, nbn);
+        const int area = g.w * g.h, fpitch = area + 4;
         // modes, taken by the warps in c_mode_order; a lane per SATD unit
         {
             const int b = lane / g.lanes, u0 = lane - b * g.lanes;
             const bool live = b < nb;
             const int bb = live ? b : 0;
-            const uint8_t *ep = s.edge + bb * g.R + g.lo;
-            const uint8_t *fb = s.fenc + bb * fpitch;
+            const uint8_t *ep = B.edge + bb * (g.R + 4) + B.emis[bb] + g.lo;
+            const uint8_t *fb = B.fenc + bb * fpitch;
             const int lx = ilog2d(g.w), ly = ilog2d(g.h);
             int mi = 0;
             if (lane == 0) mi = atomicAdd(&s.next_mode, 1);
@@ -640,7 +704,7 @@ __global__ void __launch_bounds__(kTT, XG_RMD_MINB) rmd_tile_kernel(const xavs2g
                         sl += __shfl_xor_sync(0xffffffffu, sl, o);
                         sa += __shfl_xor_sync(0xffffffffu, sa, o);
                     }
-                    const int top = s.dc_avail[bb] >> 8, left = s.dc_avail[bb] & 0xFF;
+                    const int top = B.dc_avail[bb] >> 8, left = B.dc_avail[bb] & 0xFF;
                     if (top && left) kc.dc = ((sl + sa + ((g.w + g.h) >> 1)) * (512 / (g.w + g.h))) >> 9;
                     else if (left) kc.dc = (sl + (g.h >> 1)) >> ly;
                     else if (top) kc.dc = (sa + (g.w >> 1)) >> lx;
@@ -692,14 +756,15 @@ __global__ void __launch_bounds__(kTT, XG_RMD_MINB) rmd_tile_kernel(const xavs2g
                 mi = __shfl_sync(0xffffffffu, mi, 0);
             }
         }
+        cp_async_wait_all();   // the next tile's samples have landed
         __syncthreads();
         // costs: lambda * mode bits + distortion as rdcost_t (md_intra.c:216-226)
         for (int e = tid; e < nb * 33; e += kTT) {
             const int b = e / 33, m = e - b * 33;
-            const int bits = (s.mpm[b][0] == m || s.mpm[b][1] == m) ? 2 : 6;
-            out[s.idx[b]].cost[m] = __dadd_rn(__dmul_rn(prm.lambda, (double)bits), (double)s.satd[b][m]);
+            const int bits = (B.mpm[b][0] == m || B.mpm[b][1] == m) ? 2 : 6;
+            out[B.idx[b]].cost[m] = __dadd_rn(__dmul_rn(prm.lambda, (double)bits), (double)s.satd[b][m]);
         }
-        __syncthreads();
+        __syncthreads();   // this buffer is refilled two tiles on
     }
 }
 
