@@ -44,7 +44,8 @@ constexpr int kLimitMargin = 58;               // 64-pixel margin minus 6 (md_in
 
 struct CtuJob {
     int16_t x0, y0;       // CTU origin
-    int16_t ref;
+    uint8_t ref;
+    uint8_t levels;       // CU sizes with a PU in the job: 1 8x8, 2 16x16, 4 32x32, 8 64x64
     int16_t mvp_x, mvp_y;
     uint8_t border;       // 1: limits may bind inside the window
     uint8_t sess;         // index into the session views of the launch
@@ -53,6 +54,7 @@ struct CtuJob {
 
 struct CtuPlan {
     int n_jobs = 0, cap_jobs = 0;
+    int n_border = 0;             // jobs whose search limits may bind (border variant)
     CtuJob *d_jobs = nullptr;
     int32_t *d_slots = nullptr;   // [n_jobs][kSlots]: PU index or -1
     std::vector<CtuJob> h_jobs;   // host copy (sess = 0), for multi-session launches
@@ -200,7 +202,9 @@ struct LaneRole {
 // Folds the costs of one displacement into the lane's keys.  `raw` are the
 // lane's eight 4x4 SADs; `mks` = (mvc << 11) | (row << 8) | dx+R for the
 // small keys, `mkl` = (mvc << 8) | dx+R for the large ones.
-template <bool BORDER>
+// LV (a compile-time set of CU sizes, as CtuJob::levels) drops the key
+// updates of the CU sizes a job has no PU of.
+template <bool BORDER, int LV>
 __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (&raw)[2][4], uint32_t mks,
                                                   uint32_t mkl, int dx, bool brow0, bool brow1, const Geometry &g,
                                                   uint32_t (&ks)[25], uint32_t (&rowl)[3])
@@ -231,6 +235,7 @@ __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (
         vl[sd] = t[0][c0] + t[1][c0];
         vr[sd] = t[0][c0 + 1] + t[1][c0 + 1];
         qv[sd] = at[sd] + ab[sd];
+        if (!(LV & 1)) continue;
         const int kb = 9 * sd;
         ks[kb + 0] = addmin(qv[sd], mks, ks[kb + 0]);
         ks[kb + 1] = addmin(at[sd], mks, ks[kb + 1]);
@@ -253,13 +258,15 @@ __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (
     const uint32_t xs_o = __shfl_xor_sync(0xffffffffu, xs, 1);
     const uint32_t F = Fh + Fh_o, L = Lh + Lh_o;
     const uint32_t cc = (half ? c3h : c0h) + xs_o;          // col 3 (half 1) / col 0 (half 0)
-    ks[18] = addmin(F - (half ? L : 0u), mks, ks[18]);     // 16x16 | 8x16 right
-    ks[19] = addmin(Fh, mks, ks[19]);                      // 16x8 top | bottom
-    ks[20] = addmin(half ? Fh : L, mks, ks[20]);           // 8x16 left | (dup)
-    ks[21] = addmin(rr_, mks, ks[21]);                     // 16x4 y0 | y12
-    ks[22] = addmin(F - rr_, mks, ks[22]);                 // 16x12 y4 | y0
-    ks[23] = addmin(cc, mks, ks[23]);                      // 4x16 x0 | x12
-    ks[24] = addmin(F - cc, mks, ks[24]);                  // 12x16 x4 | x0
+    if (LV & 2) {
+        ks[18] = addmin(F - (half ? L : 0u), mks, ks[18]);     // 16x16 | 8x16 right
+        ks[19] = addmin(Fh, mks, ks[19]);                      // 16x8 top | bottom
+        ks[20] = addmin(half ? Fh : L, mks, ks[20]);           // 8x16 left | (dup)
+        ks[21] = addmin(rr_, mks, ks[21]);                     // 16x4 y0 | y12
+        ks[22] = addmin(F - rr_, mks, ks[22]);                 // 16x12 y4 | y0
+        ks[23] = addmin(cc, mks, ks[23]);                      // 4x16 x0 | x12
+        ks[24] = addmin(F - cc, mks, ks[24]);                  // 12x16 x4 | x0
+    }
     // large PUs in the raw domain
     uint32_t Fr, Tr, Lr;
     if (BORDER) {
@@ -295,9 +302,11 @@ __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (
     const uint32_t P = RS + __shfl_xor_sync(0xffffffffu, RS, LR.pr4);      // row | column pairs
     const uint32_t TOT = P + __shfl_xor_sync(0xffffffffu, P, LR.pr5);
     const int v64 = LR.c64[0] * (int)TOT + LR.c64[1] * (int)P + LR.c64[2] * (int)RS;
-    rowl[0] = min(rowl[0], (min((uint32_t)va, kCapLarge) << 8) + mkl);
-    rowl[1] = min(rowl[1], (min((uint32_t)vb, kCapLarge) << 8) + mkl);
-    rowl[2] = min(rowl[2], (min((uint32_t)v64, kCapLarge) << 8) + mkl);
+    if (LV & 4) {
+        rowl[0] = min(rowl[0], (min((uint32_t)va, kCapLarge) << 8) + mkl);
+        rowl[1] = min(rowl[1], (min((uint32_t)vb, kCapLarge) << 8) + mkl);
+    }
+    if (LV & 8) rowl[2] = min(rowl[2], (min((uint32_t)v64, kCapLarge) << 8) + mkl);
 }
 
 // 4x4 SADs of the lane's half-region against window rows wrow0.. at byte
@@ -330,15 +339,10 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
 #define XG_CTU_MINB 3
 #endif
 
-template <bool BORDER>
-__global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
-                                                            const SessView *__restrict__ views, int R, int lambda,
-                                                            int ww)
+template <bool BORDER, int LV>
+__device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const SessView *__restrict__ views, int R,
+                                           int lambda, int ww, uint8_t *smem)
 {
-    extern __shared__ __align__(16) uint8_t smem[];
-    const int job_idx = blockIdx.x / nchunks, chunk = blockIdx.x % nchunks;
-    const CtuJob job = jobs[job_idx];
-    if (BORDER != (job.border != 0)) return;
     const SessView &view = views[job.sess];
     const int32_t *__restrict__ slots = view.slots;
     const uint8_t *__restrict__ cur = view.cur;
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const 
             b0 = L.by0 >= -kLimitMargin && L.by0 + 4 <= g.H + kLimitMargin;
             b1 = L.by0 + 4 >= -kLimitMargin && L.by0 + 8 <= g.H + kLimitMargin;
         }
-        fold_displacement<BORDER>(L, raw, mvc0 << 11, mvc0 << 8, 0, b0, b1, g, ks0, rowl0);
+        fold_displacement<BORDER, LV>(L, raw, mvc0 << 11, mvc0 << 8, 0, b0, b1, g, ks0, rowl0);
 #pragma unroll
         for (int k = 0; k < 25; k++) {
             const uint32_t cost = ks0[k] >> 11;
@@ -505,7 +509,7 @@ __global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const 
                 const int dxr = j0 + o;
                 const uint32_t mks = mrow[dxr];
                 const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
-                fold_displacement<BORDER>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+                fold_displacement<BORDER, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
             }
         }
         // fold this row's large-PU minima into 64-bit (cost, order) keys
@@ -537,6 +541,30 @@ __global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const 
         const int pu = smap[slot];
         if (pu >= 0) atomicMin(&keys[pu], kl[k]);
     }
+}
+
+// CU sizes with separate compiled folds (serving's leaf CUs often have no
+// 8x8 / 16x16 CU in a CTU): 1 on, 0 every job with the full fold
+#ifndef XG_CTU_LEVELS
+#define XG_CTU_LEVELS 1
+#endif
+
+template <bool BORDER>
+__global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
+                                                            const SessView *__restrict__ views, int R, int lambda,
+                                                            int ww)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int job_idx = blockIdx.x / nchunks, chunk = blockIdx.x % nchunks;
+    const CtuJob job = jobs[job_idx];
+    if (BORDER != (job.border != 0)) return;
+#if XG_CTU_LEVELS
+    if (job.levels & 1) ctu_search<BORDER, 15>(job, chunk, views, R, lambda, ww, smem);
+    else if (job.levels & 2) ctu_search<BORDER, 14>(job, chunk, views, R, lambda, ww, smem);
+    else ctu_search<BORDER, 12>(job, chunk, views, R, lambda, ww, smem);
+#else
+    ctu_search<BORDER, 15>(job, chunk, views, R, lambda, ww, smem);
+#endif
 }
 
 // ---- host planning -----------------------------------------------------------------
@@ -584,6 +612,7 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
             group_job[gidx] = j;
             CtuJob cj;
             cj.x0 = (int16_t)(u.x & ~63); cj.y0 = (int16_t)(u.y & ~63); cj.ref = u.ref;
+            cj.levels = 0;
             cj.mvp_x = u.mvp_x; cj.mvp_y = u.mvp_y;
             // can the edge rule bind for any block of this CTU inside the window?
             cj.border = (cj.x0 - R < -kLimitMargin || cj.x0 + 64 + R > W + kLimitMargin ||
@@ -597,6 +626,7 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
         int32_t &slot = slots[(size_t)cj.slot_base + s];
         if (cj.mvp_x != u.mvp_x || cj.mvp_y != u.mvp_y || slot >= 0) { generic.push_back(i); continue; }
         slot = i;
+        cj.levels |= (uint8_t)(s < 576 ? 1 : s < 784 ? 2 : s < 836 ? 4 : 8);
     }
     if ((int)jobs.size() > p.cap_jobs) {
         if (p.d_jobs) cudaFree(p.d_jobs);
@@ -606,6 +636,8 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
         XG_CUDA(cudaMalloc((void **)&p.d_slots, sizeof(int32_t) * kSlots * p.cap_jobs));
     }
     p.n_jobs = (int)jobs.size();
+    p.n_border = 0;
+    for (const CtuJob &j : jobs) p.n_border += j.border ? 1 : 0;
     p.h_jobs = jobs;
     if (p.n_jobs) {
         XG_CUDA(cudaMemcpyAsync(p.d_jobs, jobs.data(), sizeof(CtuJob) * p.n_jobs, cudaMemcpyHostToDevice, st));
@@ -623,8 +655,10 @@ static inline size_t ctu_smem_bytes(int R, int &ww)
 }
 
 // One launch of each variant over `n_jobs` jobs (sessions per job.sess).
-static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, const SessView *d_views, const xavs2gpu_me_params_t &prm,
-                         cudaStream_t st)
+// n_border of the jobs need the border variant; a variant with no job of
+// its kind is not launched.
+static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const SessView *d_views,
+                         const xavs2gpu_me_params_t &prm, cudaStream_t st)
 {
     if (n_jobs == 0) return;
     const int R = prm.search_range;
@@ -641,9 +675,14 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, const SessView *d_vie
     }
     const int nchunks = (2 * R + kDyChunk - 1) / kDyChunk;
     const int grid = n_jobs * nchunks;
-    fs_ctu_kernel<false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
-    fs_ctu_kernel<true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
-    count_launch(2);
+    if (n_border < n_jobs) {
+        fs_ctu_kernel<false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        count_launch();
+    }
+    if (n_border > 0) {
+        fs_ctu_kernel<true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        count_launch();
+    }
 }
 
 }  // namespace xg

@@ -1317,7 +1317,7 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[1], m.st));
-    ctu_jobs_run(m.plan.d_jobs, m.plan.n_jobs, m.d_view, *prm, m.st);
+    ctu_jobs_run(m.plan.d_jobs, m.plan.n_jobs, m.plan.n_border, m.d_view, *prm, m.st);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
     if (m.n_generic) {
         int grid = m.n_generic < 152 * 8 ? m.n_generic : 152 * 8;
@@ -1636,6 +1636,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     // pass 1: plans and sizes
     const bool grouped = !prm->enable_pmvr && use_groups();
     size_t nj = 0, ng = 0, ns = 0, nl = 0, nm = 0, nheavy = 0, ngr = 0;
+    int nborder = 0;
     int block = 128;
     for (int k = 0; k < n; k++) {
         MeSessionImpl &m = sessions[k]->impl;
@@ -1646,6 +1647,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         ensure_plan(m, R);
         const bool g = grouped && m.cu_groups;
         nj += m.plan.h_jobs.size();
+        nborder += m.plan.n_border;
         ng += m.h_generic.size();
         ns += g ? m.h_small_g.size() : m.h_small.size();
         nl += g ? m.h_large_g.size() : m.h_large.size();
@@ -1721,7 +1723,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         me_init_list_kernel<<<(unsigned)((ng * 32 + 127) / 128), 128, 0, st>>>(d_gen, (int)ng, bb.d_views, lam);
         count_launch();
     }
-    ctu_jobs_run(bb.d_jobs, (int)nj, bb.d_views, *prm, st);
+    ctu_jobs_run(bb.d_jobs, (int)nj, nborder, bb.d_views, *prm, st);
     if (ng) {
         fs_generic_kernel<<<(unsigned)(ng < 152 * 8 ? ng : 152 * 8), 256, 0, st>>>(d_gen, (int)ng, bb.d_views, R, lam);
         count_launch();
