@@ -1349,7 +1349,7 @@ def run_skip(args):
 
 
 # ---- serving: 64 concurrent streams, continuous batching --------------------
-SERVE_METRIC = "served p99 frame latency (64 streams 360p..2160p, 30 fps Poisson arrivals, continuous batching)"
+SERVE_METRIC = "served p99 frame latency (%d streams %s, 30 fps Poisson arrivals, continuous batching)"
 SERVE_RES = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
 
 
@@ -1434,6 +1434,8 @@ def run_serve(args):
     rng = np.random.default_rng(11 + rank)
     nstreams, rate = args.serve_streams, 30.0
     res_idx = rng.choice(4, nstreams, p=[0.3, 0.3, 0.3, 0.1])
+    if args.serve_res != "mix":
+        res_idx = np.full(nstreams, ["360p", "720p", "1080p", "2160p"].index(args.serve_res))
     pools = {r: serve_content(*SERVE_RES[r], args.serve_pool, 50 + r) for r in sorted(set(res_idx.tolist()))}
     prm = xg.MeParams(args.serve_range, lambda_factor(QP), 1, 2, 0, 0)
     layouts = []
@@ -1474,10 +1476,12 @@ def run_serve(args):
     px = {r: SERVE_RES[r][0] * SERVE_RES[r][1] for r in range(4)}
     mean_px = float(np.mean([px[r] for r in res_idx]))
     line = {
-        "metric": SERVE_METRIC, "value": batched.get("p99_ms"), "unit": "ms", "n_gpus": world,
+        "metric": SERVE_METRIC % (nstreams, "360p..2160p" if args.serve_res == "mix" else args.serve_res),
+        "value": batched.get("p99_ms"), "unit": "ms", "n_gpus": world,
         "steps": batched.get("frames"), "warmup": args.serve_warm, "ms_per_step": batched.get("mean_ms"),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "serve_64_streams_mixed", "streams": nstreams,
+        "config": {"workload": "serve_%d_streams_%s" % (nstreams, "mixed" if args.serve_res == "mix" else args.serve_res),
+                   "streams": nstreams,
                    "resolutions": {"%dx%d" % SERVE_RES[r]: int((res_idx == r).sum()) for r in range(4)},
                    "arrivals": "Poisson 30 fps per stream", "seconds": args.serve_seconds, "warm_s": args.serve_warm,
                    "search_range": args.serve_range, "qp": QP, "refs": 2,
@@ -1642,6 +1646,8 @@ def main():
     # burst of arrivals from forming one long batch (p99 11.7 ms against 16-19
     # ms with 48 MiB batches at 64 streams)
     ap.add_argument("--serve-batch-mpx", type=int, default=12)
+    ap.add_argument("--serve-res", choices=["mix", "360p", "720p", "1080p", "2160p"], default="mix",
+                    help="stream resolutions: the 360p..2160p mix, or every stream at one size")
     ap.add_argument("--serve-pool", type=int, default=4)
     ap.add_argument("--serve-hbm-gb", type=int, default=64)
     args = ap.parse_args()
@@ -1663,7 +1669,9 @@ def main():
             run_chain(args)
     elif args.workload == "serve":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "metric": SERVE_METRIC,
+            print(json.dumps({"impl": "reference",
+                              "metric": SERVE_METRIC % (args.serve_streams, "360p..2160p" if args.serve_res == "mix"
+                                                        else args.serve_res),
                               "unavailable": "the reference has no serving path; its per-picture CPU cost is the "
                                              "--workload me reference arm"}))
         else:
