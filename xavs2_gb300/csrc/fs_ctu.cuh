@@ -328,6 +328,11 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
     }
 }
 
+// border jobs: the interior fold for displacements that need no limit
+#ifndef XG_CTU_SAFE_SPLIT
+#define XG_CTU_SAFE_SPLIT 1
+#endif
+
 // window fill with 16-byte loads when the window lies inside the padded plane
 #ifndef XG_CTU_VEC_FILL
 #define XG_CTU_VEC_FILL 1
@@ -480,6 +485,9 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
             brow0 = yb >= -kLimitMargin && yb + 4 <= g.H + kLimitMargin;
             brow1 = yb + 4 >= -kLimitMargin && yb + 8 <= g.H + kLimitMargin;
         }
+        // every block of the CTU inside the vertical limits at this dy
+        const bool row_safe = job.y0 + dy >= -kLimitMargin && job.y0 + 64 + dy <= g.H + kLimitMargin;
+        (void)row_safe;
         for (int j0 = 0; j0 < nd; j0 += 4) {
             uint32_t s[4][2][4];
 #pragma unroll
@@ -504,6 +512,29 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
                     }
                 }
             }
+#if XG_CTU_SAFE_SPLIT
+            // in a border job, displacements whose every block stays inside
+            // the limits take the interior fold (same keys: nothing to poison)
+            const bool safe = !BORDER || (row_safe && job.x0 + j0 - R >= -kLimitMargin &&
+                                          job.x0 + 64 + j0 + 3 - R <= g.W + kLimitMargin);
+            if (BORDER && !safe) {
+#pragma unroll
+                for (int o = 0; o < 4; o++) {
+                    const int dxr = j0 + o;
+                    const uint32_t mks = mrow[dxr];
+                    const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
+                    fold_displacement<true, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+                }
+            } else {
+#pragma unroll
+                for (int o = 0; o < 4; o++) {
+                    const int dxr = j0 + o;
+                    const uint32_t mks = mrow[dxr];
+                    const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;
+                    fold_displacement<false, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+                }
+            }
+#else
 #pragma unroll
             for (int o = 0; o < 4; o++) {
                 const int dxr = j0 + o;
@@ -511,6 +542,7 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
                 const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
                 fold_displacement<BORDER, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
             }
+#endif
         }
         // fold this row's large-PU minima into 64-bit (cost, order) keys
 #pragma unroll
