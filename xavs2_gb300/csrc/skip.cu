@@ -179,8 +179,14 @@ __global__ void skip_scatter_kernel(Ctx c, const int *__restrict__ counts, int *
 // of 8x8 blocks) lanes each; lane s of a candidate takes 8x8 blocks s and
 // s + 32 in z-order, so the four blocks of a 16x16 SA8D unit sit in four
 // consecutive lanes (their sums are rounded together, pixel.c:470-500).
-__global__ void __launch_bounds__(128) skip_cost_kernel(Ctx c, const int *__restrict__ counts,
-                                                        const int *__restrict__ sorted)
+// resident 128-thread CTAs per SM the register budget is sized for (4: 128
+// registers; the kernel waits on plane gathers, and 4 CTAs measured faster
+// than 3 (the compiler's own 134 registers), 5 and 6)
+#ifndef XG_SKIP_MINB
+#define XG_SKIP_MINB 4
+#endif
+__global__ void __launch_bounds__(128, XG_SKIP_MINB) skip_cost_kernel(Ctx c, const int *__restrict__ counts,
+                                                                      const int *__restrict__ sorted)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     int start = 0, first = 0, cl = -1;
