@@ -819,7 +819,9 @@ __global__ void __launch_bounds__(32 * kGrpWarps, XG_GROUP_MINB) refine_group_ke
                 const bool need4 = __any_sync(0xffffffffu, ((grp >> lane) & 1) && S.ru4[lane]);
                 if (need8)
                     group_table<false>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, P, lane);
-                if (need4)
+                // 4x4 units occur only in 16x16 CUs (4- and 12-wide partitions);
+                // the 4x4 table holds one 16x16 CU
+                if (need4 && cs == 16)
                     group_table<true>(S, grp, had, cs, o, planes, g.stride, G.cx, G.cy, ccx, ccy, P, lane);
                 __syncwarp();
                 // each member's sums over its units
