@@ -92,9 +92,24 @@ __device__ __forceinline__ PuSrc pu_src(const Ctx &c, const xavs2gpu_skip_cand_t
     return s;
 }
 
+// 4 samples at any byte address, from the two aligned words holding them
+// (the word after the last sample is read too: planes and pictures have an
+// 80-sample margin, so it is inside the allocation)
+__device__ __forceinline__ uint32_t ld4u(const uint8_t *p)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    return __funnelshift_r(w[0], w[1], (unsigned)(a & 3) * 8u);
+}
+
+// bytewise (a + b + 1) >> 1 of four packed samples (pixel_avg, pixel.c:680-700)
+__device__ __forceinline__ uint32_t avg4(uint32_t a, uint32_t b) { return (a | b) - (((a ^ b) >> 1) & 0x7F7F7F7Fu); }
+
 // |H8 (src - pred) H8^T| of the 8x8 block at (X, Y); the prediction of
 // sample (x, y) comes from src4[(y >= 4) * 2 + (x >= 4)] (four 4x4 PUs of an
 // 8x8 CU) or from src4[0] everywhere, relative to each PU's own corner.
+// Rows are read as words: the current block's aligned, the prediction's at
+// any alignment.
 template <bool QUAD>
 __device__ int hsum8_pred(const Ctx &c, int X, int Y, const PuSrc *src4)
 {
@@ -102,14 +117,20 @@ __device__ int hsum8_pred(const Ctx &c, int X, int Y, const PuSrc *src4)
 #pragma unroll
     for (int y = 0; y < 8; y++) {
         const uint8_t *cur = c.cur + (long long)(Y + y) * c.stride + X;
+        const uint32_t c0 = ld4u(cur), c1 = ld4u(cur + 4);
+        uint32_t pw[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const PuSrc &ps = src4[QUAD ? (y >= 4) * 2 + h : 0];
+            const long long o = (long long)(QUAD ? (y & 3) : y) * c.stride + (QUAD ? 0 : 4 * h);
+            const uint32_t a = ld4u(ps.p[0] + o);
+            pw[h] = ps.n == 2 ? avg4(a, ld4u(ps.p[1] + o)) : a;   // one list: the plane's samples
+        }
         int t[8];
 #pragma unroll
         for (int x = 0; x < 8; x++) {
-            const PuSrc &ps = src4[QUAD ? (y >= 4) * 2 + (x >= 4) : 0];
-            const int ox = QUAD ? (x & 3) : x, oy = QUAD ? (y & 3) : y;
-            const long long o = (long long)oy * c.stride + ox;
-            const int a = ps.p[0][o], b = ps.p[1][o];
-            t[x] = (int)cur[x] - ((a + b + 1) >> 1);   // one list: a == b
+            const uint32_t cv = x < 4 ? c0 : c1, pv = pw[x >> 2];
+            t[x] = (int)((cv >> (8 * (x & 3))) & 0xFFu) - (int)((pv >> (8 * (x & 3))) & 0xFFu);
         }
         int u[8];
 #pragma unroll
