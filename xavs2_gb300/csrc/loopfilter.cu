@@ -449,17 +449,20 @@ __global__ void __launch_bounds__(kSaoThreads, 8) sao_lcu_kernel(SaoPic sp)
 
 // ---- fused deblocking + SAO --------------------------------------------------
 // A CTA takes the SAO region of one LCU for one component and produces its
-// final samples in one pass: the region plus an 8-sample margin (clamped to
-// the picture) is loaded into shared memory, the vertical edges and then the
-// horizontal edges whose filter window lies inside the tile are filtered
-// there, and SAO writes the region.  A deblocked sample depends on source
+// final samples in one pass: the part of the region plus an 8-sample margin
+// (clamped to the picture) that the filters read is loaded into shared
+// memory, the vertical edges and then the horizontal edges that change a
+// sample SAO reads are filtered there, four lines per thread, and SAO writes
+// the region, four samples per thread.  A deblocked sample depends on source
 // samples at most 5 away in each direction and SAO reads 1 around the region,
 // so the margin holds everything the region needs and the result equals the
-// picture-wide two-pass deblocking followed by SAO.
+// picture-wide two-pass deblocking followed by SAO.  With most of the
+// deblocking branch-free, 128 threads a CTA keep more CTAs in flight than
+// 256 (0.043 against 0.055 ms for a 3840x2160 picture).
 constexpr int kLfPitch = 96, kLfRows = 88;   // tile: region (<= 68) + 2 x 8
 constexpr int kLfScus = 256;                  // 8x8 blocks the tile touches (<= 15 x 15)
 #ifndef XG_LF_THREADS
-#define XG_LF_THREADS 256
+#define XG_LF_THREADS 128
 #endif
 
 struct FusedPic {
@@ -469,6 +472,42 @@ struct FusedPic {
     const xavs2gpu_deblock_scu_t *scus;
     const xavs2gpu_sao_lcu_t *lcus;
 };
+
+// ---- four samples per word (SWAR, Hacker's Delight ch. 2) ---------------------
+// bit 7 of each byte: a >= b, bytewise unsigned.  The low 7 bits are compared
+// through (a | 0x80) - (b & 0x7F), which cannot borrow across bytes.
+__device__ __forceinline__ uint32_t ge_bytes(uint32_t a, uint32_t b)
+{
+    const uint32_t t = (a | 0x80808080u) - (b & 0x7F7F7F7Fu);
+    return ((a & ~b) | (~(a ^ b) & t)) & 0x80808080u;
+}
+// bytewise min(a + b, 255): the sum without carries between bytes, the
+// carry out of each byte, and a byte of ones where it is set
+__device__ __forceinline__ uint32_t addus_bytes(uint32_t a, uint32_t b)
+{
+    const uint32_t s = ((a & 0x7F7F7F7Fu) + (b & 0x7F7F7F7Fu)) ^ ((a ^ b) & 0x80808080u);
+    const uint32_t cy = ((a & b) | ((a | b) & ~s)) & 0x80808080u;
+    return s | cy | (cy - (cy >> 7));
+}
+// bytewise max(a - b, 0) = 255 - min(255 - a + b, 255)
+__device__ __forceinline__ uint32_t subus_bytes(uint32_t a, uint32_t b) { return ~addus_bytes(~a, b); }
+
+// SAO edge class per byte: sign(s - n1) + sign(s - n2) + 2, each term
+// sign(s - n) + 1 = [s >= n] + (1 - [n >= s]); the sum is at most 4
+__device__ __forceinline__ uint32_t eo_class(uint32_t s, uint32_t n1, uint32_t n2)
+{
+    const uint32_t H = 0x80808080u;
+    return ((ge_bytes(s, n1) >> 7) + (ge_bytes(s, n2) >> 7)) +
+           (((ge_bytes(n1, s) ^ H) >> 7) + ((ge_bytes(n2, s) ^ H) >> 7));
+}
+// clip(s + offset[class], 0, 255) per byte: the classes (0..4) packed into
+// the 4 selector nibbles of a byte permute over the offsets' positive and
+// negative parts (each clipped to 255, which leaves the clipped sum exact)
+__device__ __forceinline__ uint32_t eo_apply(uint32_t s, uint32_t cls, const uint32_t *tab)
+{
+    const uint32_t sel = __byte_perm(cls | (cls >> 4), 0, 0x0020);
+    return subus_bytes(addus_bytes(s, __byte_perm(tab[0], tab[1], sel)), __byte_perm(tab[2], tab[3], sel));
+}
 
 // Per 8x8 block and direction, the edge as one word for the component:
 // bit 0 filter the first half, bit 1 the second half (type and flag
@@ -482,14 +521,171 @@ __device__ __forceinline__ uint32_t edge_word(const xavs2gpu_deblock_scu_t &e, i
            ((uint32_t)(chroma ? e.beta_c[dir] : e.beta[dir]) << 16);
 }
 
-__device__ __forceinline__ void filter_smem_line(uint8_t *s0, int step, uint32_t ew, bool chroma)
+// Four lines across one edge at once, a line per byte lane: w[0..5] hold
+// L2 L1 L0 R0 R1 R2 of the four lines, `lanes` has bit 7 of each byte set for
+// the lines the edge filters.  The filter-strength decision of filter_line
+// becomes byte masks (no divergence between lines) and its sums are formed in
+// 16-bit halves, the even and the odd lanes.  Returns false when no line
+// changes.
+__device__ __forceinline__ uint32_t lt_bytes(uint32_t a, uint32_t b) { return ge_bytes(a, b) ^ 0x80808080u; }
+__device__ __forceinline__ uint32_t byte_mask(uint32_t m7) { return (m7 >> 7) * 0xFFu; }
+__device__ __forceinline__ uint32_t pick(uint32_t a, uint32_t b, uint32_t m) { return (a & ~m) | (b & m); }
+
+template <bool CHROMA>
+__device__ __forceinline__ bool filter_lines4(uint32_t (&w)[6], uint32_t ew, uint32_t lanes)
 {
-    int p[6];
+    const uint32_t alpha = ((ew >> 8) & 0xFFu) * 0x01010101u, beta = ((ew >> 16) & 0xFFu) * 0x01010101u;
+    const uint32_t L2 = w[0], L1 = w[1], L0 = w[2], R0 = w[3], R1 = w[4], R2 = w[5];
+    const uint32_t d = __vabsdiffu4(R0, L0);
+    const uint32_t on = lt_bytes(d, alpha) & ge_bytes(d, 0x02020202u) & lanes;
+    if (!on) return false;
+    const uint32_t dl1 = __vabsdiffu4(L1, L0), dr1 = __vabsdiffu4(R0, R1);
+    const uint32_t a1 = lt_bytes(dl1, beta), a2 = lt_bytes(__vabsdiffu4(L2, L0), beta);
+    const uint32_t b1 = lt_bytes(dr1, beta), b2 = lt_bytes(__vabsdiffu4(R0, R2), beta);
+    const uint32_t eq = lt_bytes(dl1 | dr1, 0x01010101u);              // L1 == L0 and R1 == R0
+    const uint32_t c3 = lt_bytes(__vabsdiffu4(L1, R1), beta);
+    // fl = 2 a1 + a2, fr = 2 b1 + b2; strength by fl + fr
+    const uint32_t s6 = a1 & a2 & b1 & b2;
+    const uint32_t s5 = a1 & b1 & (a2 ^ b2);
+    const uint32_t s4_2 = a1 & b1 & ~(a2 | b2);                            // fl = fr = 2
+    const uint32_t s4_1 = a2 & b2 & (a1 ^ b1);                             // (3, 1), (1, 3)
+    const uint32_t s3 = (a1 & a2 & ~(b1 | b2)) | (b1 & b2 & ~(a1 | a2)) | (a1 & b2 & ~(a2 | b1)) |
+                        (a2 & b1 & ~(a1 | b2));
+    const uint32_t f4 = s6 & eq, f3 = (s6 & ~eq) | (s5 & eq), f2 = (s5 & ~eq) | s4_2, f1 = s4_1 | (s3 & c3);
+    // chroma filters one step weaker
+    const uint32_t m4 = CHROMA ? 0u : byte_mask(f4 & on), m3 = byte_mask((CHROMA ? f4 : f3) & on),
+                   m2 = byte_mask((CHROMA ? f3 : f2) & on), m1 = byte_mask((CHROMA ? f2 : f1) & on);
+    if (!(m4 | m3 | m2 | m1)) return false;
+    // the six words split into even / odd lanes (16 bits each); a sum's
+    // result byte is bits 0-7 of each lane after the shift
+    uint32_t e[6], o[6];
 #pragma unroll
-    for (int k = 0; k < 6; k++) p[k] = s0[k * step];
-    if (filter_line(p, (int)((ew >> 8) & 0xFF), (int)((ew >> 16) & 0xFF), chroma)) {
+    for (int k = 0; k < 6; k++) {
+        e[k] = w[k] & 0x00FF00FFu;
+        o[k] = __byte_perm(w[k], 0, 0x4341);
+    }
+    auto join = [](uint32_t ev, uint32_t od) { return __byte_perm(ev, od, 0x6240); };
+    const uint32_t K2 = 0x00020002u, K4 = 0x00040004u, K8 = 0x00080008u, K16 = 0x00100010u;
+    uint32_t nL2 = L2, nL1 = L1, nL0 = L0, nR0 = R0, nR1 = R1, nR2 = R2;
+    if (m1) {
+        auto l0 = [&](const uint32_t *v) { return (3 * v[2] + v[3] + K2) >> 2; };
+        auto r0 = [&](const uint32_t *v) { return (3 * v[3] + v[2] + K2) >> 2; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m1);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m1);
+    }
+    if (m2) {
+        auto l0 = [&](const uint32_t *v) { return (3 * v[1] + 10 * v[2] + 3 * v[3] + K8) >> 4; };
+        auto r0 = [&](const uint32_t *v) { return (3 * v[2] + 10 * v[3] + 3 * v[4] + K8) >> 4; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m2);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m2);
+    }
+    if (m3) {
+        auto l0 = [&](const uint32_t *v) { return (v[0] + 4 * v[1] + 6 * v[2] + 4 * v[3] + v[4] + K8) >> 4; };
+        auto r0 = [&](const uint32_t *v) { return (v[1] + 4 * v[2] + 6 * v[3] + 4 * v[4] + v[5] + K8) >> 4; };
+        auto l1 = [&](const uint32_t *v) { return (3 * v[0] + 8 * v[1] + 4 * v[2] + v[3] + K8) >> 4; };
+        auto r1 = [&](const uint32_t *v) { return (3 * v[5] + 8 * v[4] + 4 * v[3] + v[2] + K8) >> 4; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m3);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m3);
+        nL1 = pick(nL1, join(l1(e), l1(o)), m3);
+        nR1 = pick(nR1, join(r1(e), r1(o)), m3);
+    }
+    if (!CHROMA && m4) {
+        auto l0 = [&](const uint32_t *v) { return (9 * v[2] + 9 * v[0] + 8 * v[3] + 6 * v[5] + K16) >> 5; };
+        auto l1 = [&](const uint32_t *v) { return (7 * v[2] + 6 * v[0] + 3 * v[3] + K8) >> 4; };
+        auto l2 = [&](const uint32_t *v) { return (4 * v[2] + 3 * v[0] + v[3] + K4) >> 3; };
+        auto r0 = [&](const uint32_t *v) { return (9 * v[3] + 9 * v[5] + 8 * v[2] + 6 * v[0] + K16) >> 5; };
+        auto r1 = [&](const uint32_t *v) { return (7 * v[3] + 6 * v[5] + 3 * v[2] + K8) >> 4; };
+        auto r2 = [&](const uint32_t *v) { return (4 * v[3] + 3 * v[5] + v[2] + K4) >> 3; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m4);
+        nL1 = pick(nL1, join(l1(e), l1(o)), m4);
+        nL2 = pick(nL2, join(l2(e), l2(o)), m4);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m4);
+        nR1 = pick(nR1, join(r1(e), r1(o)), m4);
+        nR2 = pick(nR2, join(r2(e), r2(o)), m4);
+    }
+    w[0] = nL2; w[1] = nL1; w[2] = nL0; w[3] = nR0; w[4] = nR1; w[5] = nR2;
+    return true;
+}
+
+// 4x4 byte transpose: rows a..d (byte k = column k) to columns
+__device__ __forceinline__ void transpose4(uint32_t &a, uint32_t &b, uint32_t &c, uint32_t &d)
+{
+    const uint32_t x = __byte_perm(a, b, 0x5140), y = __byte_perm(a, b, 0x7362);
+    const uint32_t z = __byte_perm(c, d, 0x5140), v = __byte_perm(c, d, 0x7362);
+    a = __byte_perm(x, z, 0x5410);
+    b = __byte_perm(x, z, 0x7632);
+    c = __byte_perm(y, v, 0x5410);
+    d = __byte_perm(y, v, 0x7632);
+}
+
+// The bit-7 lane mask of four lines of one 8x8 block's edge: luma lines
+// share the half's flag; chroma lines 0-1 are the first half, 2-3 the second.
+__device__ __forceinline__ uint32_t edge_lanes(uint32_t ew, bool chroma, int half)
+{
+    if (chroma) return ((ew & 1u) ? 0x00008080u : 0u) | ((ew & 2u) ? 0x80800000u : 0u);
+    return ((ew >> half) & 1u) ? 0x80808080u : 0u;
+}
+
+// Four rows of one vertical edge: p = the tile at (row 0, edge - 4)
+template <bool CHROMA>
+__device__ __forceinline__ void filter_ver4(uint8_t *p, uint32_t ew, uint32_t lanes)
+{
+    uint32_t A[4], B[4];
 #pragma unroll
-        for (int k = 0; k < 6; k++) s0[k * step] = (uint8_t)p[k];
+    for (int r = 0; r < 4; r++) {
+        A[r] = *reinterpret_cast<const uint32_t *>(p + r * kLfPitch);
+        B[r] = *reinterpret_cast<const uint32_t *>(p + r * kLfPitch + 4);
+    }
+    transpose4(A[0], A[1], A[2], A[3]);   // A[k] = column edge - 4 + k
+    transpose4(B[0], B[1], B[2], B[3]);   // B[k] = column edge + k
+    uint32_t w[6] = {A[1], A[2], A[3], B[0], B[1], B[2]};
+    if (!filter_lines4<CHROMA>(w, ew, lanes)) return;
+    A[1] = w[0]; A[2] = w[1]; A[3] = w[2]; B[0] = w[3]; B[1] = w[4]; B[2] = w[5];
+    transpose4(A[0], A[1], A[2], A[3]);
+    transpose4(B[0], B[1], B[2], B[3]);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        *reinterpret_cast<uint32_t *>(p + r * kLfPitch) = A[r];
+        *reinterpret_cast<uint32_t *>(p + r * kLfPitch + 4) = B[r];
+    }
+}
+
+// Four columns of one horizontal edge: p = the tile at (edge - 3, column 0)
+template <bool CHROMA>
+__device__ __forceinline__ void filter_hor4(uint8_t *p, uint32_t ew, uint32_t lanes)
+{
+    uint32_t w[6];
+#pragma unroll
+    for (int r = 0; r < 6; r++) w[r] = *reinterpret_cast<const uint32_t *>(p + r * kLfPitch);
+    if (!filter_lines4<CHROMA>(w, ew, lanes)) return;
+#pragma unroll
+    for (int r = 0; r < 6; r++) *reinterpret_cast<uint32_t *>(p + r * kLfPitch) = w[r];
+}
+
+// The deblocking of the tile: vertical edges on the rows [vy0, vy1) in
+// 4-row groups, then horizontal edges on the word columns holding
+// [cx0, cx1).  Rows and columns outside those ranges that a group or word
+// also covers get filtered too; nothing after reads them.
+template <bool CHROMA>
+__device__ __forceinline__ void deblock_tile(uint8_t (*t)[kLfPitch], const uint32_t *ev, const uint32_t *eh,
+                                             int tx0, int ty0, int sx0, int sy0, int nsx, int ex0, int nex, int ey0,
+                                             int ney, int vy0, int vy1, int cx0, int cx1)
+{
+    const int sh = CHROMA ? 2 : 3, tid = threadIdx.x, nt = blockDim.x;
+    const int gy0 = vy0 & ~3, ng = (vy1 - gy0 + 3) >> 2;
+    for (int i = tid; i < nex * ng; i += nt) {
+        const int g = i / nex, ex = ex0 + 8 * (i - g * nex), y = gy0 + 4 * g;
+        const uint32_t ew = ev[((y >> sh) - sy0) * nsx + (ex >> sh) - sx0];
+        const uint32_t lanes = edge_lanes(ew, CHROMA, (y & 7) >= 4);
+        if (lanes) filter_ver4<CHROMA>(&t[y - ty0][ex - tx0 - 4], ew, lanes);
+    }
+    __syncthreads();
+    const int wx0 = cx0 & ~3, nwc = (((cx1 + 3) & ~3) - wx0) >> 2;
+    for (int i = tid; i < nwc * ney; i += nt) {
+        const int j = i / nwc, x = wx0 + 4 * (i - j * nwc), ey = ey0 + 8 * j;
+        const uint32_t ew = eh[((ey >> sh) - sy0) * nsx + (x >> sh) - sx0];
+        const uint32_t lanes = edge_lanes(ew, CHROMA, (x & 7) >= 4);
+        if (lanes) filter_hor4<CHROMA>(&t[ey - ty0 - 3][x - tx0], ew, lanes);
     }
 }
 
@@ -498,6 +694,7 @@ __global__ void __launch_bounds__(XG_LF_THREADS) loopfilter_lcu_kernel(FusedPic 
     __shared__ __align__(16) uint8_t t[kLfRows][kLfPitch];
     __shared__ uint32_t ev[kLfScus], eh[kLfScus];   // edge words, vertical / horizontal
     __shared__ int off[32];
+    __shared__ uint32_t eo_tab[4];   // edge-offset classes 0-4: added bytes (words 0-1), subtracted (2-3)
     const int l = blockIdx.x, c = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
     const bool chroma = c != 0;
     const int lx = l % fp.wl, ly = l / fp.wl;
@@ -509,8 +706,16 @@ __global__ void __launch_bounds__(XG_LF_THREADS) loopfilter_lcu_kernel(FusedPic 
     const uint8_t *src = c == 0 ? fp.src[0] : c == 1 ? fp.src[1] : fp.src[2];
     uint8_t *dst = c == 0 ? fp.dst[0] : c == 1 ? fp.dst[1] : fp.dst[2];
     const int tx0 = max(rx - 8, 0), tx1 = min(rx + rw + 8, W), ty0 = max(ry - 8, 0), ty1 = min(ry + rh + 8, H);
-    const int tw = tx1 - tx0, th = ty1 - ty0, nw = tw >> 2;
     if (tid < 32) off[tid] = q.offset[c][tid];
+    if (tid == 32) {
+        uint32_t ad[2] = {0, 0}, sb[2] = {0, 0};
+        for (int k = 0; k < 5; k++) {
+            const int o = q.offset[c][k];
+            ad[k >> 2] |= (uint32_t)min(max(o, 0), 255) << (8 * (k & 3));
+            sb[k >> 2] |= (uint32_t)min(max(-o, 0), 255) << (8 * (k & 3));
+        }
+        eo_tab[0] = ad[0]; eo_tab[1] = ad[1]; eo_tab[2] = sb[0]; eo_tab[3] = sb[1];
+    }
     // edge words of the 8x8 blocks the tile touches
     const int sh = chroma ? 2 : 3;
     const int sx0 = tx0 >> sh, sy0 = ty0 >> sh, nsx = ((tx1 - 1) >> sh) - sx0 + 1, nsy = ((ty1 - 1) >> sh) - sy0 + 1;
@@ -520,83 +725,83 @@ __global__ void __launch_bounds__(XG_LF_THREADS) loopfilter_lcu_kernel(FusedPic 
         ev[i] = edge_word(e, 0, chroma);
         eh[i] = sx < fp.n_hor ? edge_word(e, 1, chroma) : 0u;
     }
-    // the tile: a thread keeps one word column and walks the rows
+    // The samples SAO reads are the region and one around it; only the edges
+    // that change one of them are filtered (a filter changes at most 3
+    // samples on either side of its edge), and only on the rows and columns
+    // that SAO and the horizontal edges read.
+    const int cx0 = max(rx - 1, tx0), cx1 = min(rx + rw + 1, tx1), cy0 = max(ry - 1, ty0),
+              cy1 = min(ry + rh + 1, ty1);
+    const int ex0 = (max(max(8, tx0 + 3), cx0 - 2) + 7) & ~7, ex1 = min(tx1 - 3, cx1 + 2);
+    const int nex = ex1 >= ex0 ? (ex1 - ex0) / 8 + 1 : 0;
+    const int ey0 = (max(max(8, ty0 + 3), cy0 - 2) + 7) & ~7, ey1 = min(ty1 - 3, cy1 + 2);
+    const int ney = ey1 >= ey0 ? (ey1 - ey0) / 8 + 1 : 0;
+    const int vy0 = ney ? min(cy0, ey0 - 3) : cy0, vy1 = ney ? max(cy1, ey0 + 8 * (ney - 1) + 3) : cy1;
+    const int lx0 = (nex ? min(cx0, ex0 - 3) : cx0) & ~3,
+              lx1 = min(((nex ? max(cx1, ex0 + 8 * (nex - 1) + 3) : cx1) + 3) & ~3, tx1);
+    // the tile rows [vy0, vy1), columns [lx0, lx1): a thread keeps one word
+    // column and walks the rows
     {
-        const int w = tid % nw, r0 = tid / nw, rs = nt / nw;
+        const int nw = (lx1 - lx0) >> 2, w = tid % nw, r0 = tid / nw, rs = nt / nw;
         if (r0 < rs)
-            for (int r = r0; r < th; r += rs)
-                *reinterpret_cast<uint32_t *>(&t[r][4 * w]) =
-                    *reinterpret_cast<const uint32_t *>(src + (long long)(ty0 + r) * st + tx0 + 4 * w);
+            for (int y = vy0 + r0; y < vy1; y += rs)
+                *reinterpret_cast<uint32_t *>(&t[y - ty0][lx0 - tx0 + 4 * w]) =
+                    *reinterpret_cast<const uint32_t *>(src + (long long)y * st + lx0 + 4 * w);
     }
     __syncthreads();
-    // vertical edges with the whole filter window inside the tile; a thread
-    // keeps one edge and walks the rows
-    {
-        const int ex0 = max(8, (tx0 + 3 + 7) & ~7), ex1 = tx1 - 3;
-        const int nex = ex1 >= ex0 ? (ex1 - ex0) / 8 + 1 : 0;
-        if (nex > 0) {
-            const int e = tid % nex, r0 = tid / nex, rs = nt / nex;
-            const int ex = ex0 + 8 * e, sxl = (ex >> sh) - sx0;
-            if (r0 < rs)
-                for (int r = r0; r < th; r += rs) {
-                    const int y = ty0 + r;
-                    const uint32_t ew = ev[((y >> sh) - sy0) * nsx + sxl];
-                    const int half = chroma ? (y & 3) >= 2 : (y & 7) >= 4;
-                    if ((ew >> half) & 1u) filter_smem_line(&t[r][ex - tx0 - 3], 1, ew, chroma);
-                }
-        }
-    }
+    if (chroma)
+        deblock_tile<true>(t, ev, eh, tx0, ty0, sx0, sy0, nsx, ex0, nex, ey0, ney, vy0, vy1, cx0, cx1);
+    else
+        deblock_tile<false>(t, ev, eh, tx0, ty0, sx0, sy0, nsx, ex0, nex, ey0, ney, vy0, vy1, cx0, cx1);
     __syncthreads();
-    // horizontal edges with the whole filter window inside the tile, on the
-    // columns SAO reads (the region and one around it); a thread keeps one
-    // column and walks the edges
-    {
-        const int ey0 = max(8, (ty0 + 3 + 7) & ~7), ey1 = ty1 - 3;
-        const int ney = ey1 >= ey0 ? (ey1 - ey0) / 8 + 1 : 0;
-        const int cx0 = max(rx - 1, tx0), cx1 = min(rx + rw + 1, tx1), ncol = cx1 - cx0;
-        if (ney > 0 && ncol > 0) {
-            const int xi = tid % ncol, j0 = tid / ncol, js = nt / ncol;
-            const int x = cx0 + xi, sxl = (x >> sh) - sx0;
-            const int half = chroma ? (x & 3) >= 2 : (x & 7) >= 4;
-            if (j0 < js)
-                for (int j = j0; j < ney; j += js) {
-                    const int ey = ey0 + 8 * j;
-                    const uint32_t ew = eh[((ey >> sh) - sy0) * nsx + sxl];
-                    if ((ew >> half) & 1u) filter_smem_line(&t[ey - ty0 - 3][x - tx0], kLfPitch, ew, chroma);
-                }
-        }
-    }
-    __syncthreads();
-    // SAO of the region from the deblocked tile; dst written whole; a thread
-    // keeps one word column and walks the rows
+    // SAO of the region from the deblocked tile, a word (4 samples) at a
+    // time; dst written whole; a thread keeps one word column and walks the
+    // rows
     const int ty = q.type[c], av = full_avail(q.avail), rwords = rw >> 2;
     const int wi = tid % rwords, r0 = tid / rwords, rs = nt / rwords;
     if (r0 >= rs) return;
+    const int x = rx + 4 * wi;
+    const bool has_left = x - tx0 >= 4;
     for (int yy = r0; yy < rh; yy += rs) {
-        const int x = rx + 4 * wi, y = ry + yy;
+        const int y = ry + yy;
         const uint8_t *d = &t[y - ty0][x - tx0];
-        uint32_t out = *reinterpret_cast<const uint32_t *>(d);
+        const uint32_t cur = *reinterpret_cast<const uint32_t *>(d);
+        uint32_t out = cur;
         int x0 = 0, x1 = 0;
         if (ty >= 0 && ty <= 4 && sao_row_range(ty, av, yy, rw, rh, x0, x1)) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int xs = x + k - rx;
-                if (xs < x0 || xs >= x1) continue;
-                const int sv = d[k];
-                int cls;
+            const int lo = max(x0 - 4 * wi, 0), hi = min(x1 - 4 * wi, 4);
+            if (lo < hi) {
+                uint32_t res;
                 if (ty == 4) {
-                    cls = sv >> 3;
-                } else {
-                    int n1, n2;
-                    switch (ty) {
-                    case 0: n1 = d[k - 1]; n2 = d[k + 1]; break;
-                    case 1: n1 = d[k - kLfPitch]; n2 = d[k + kLfPitch]; break;
-                    case 2: n1 = d[k - kLfPitch - 1]; n2 = d[k + kLfPitch + 1]; break;
-                    default: n1 = d[k - kLfPitch + 1]; n2 = d[k + kLfPitch - 1]; break;
+                    res = cur;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const int sv = byte_of(cur, k);
+                        res = set_byte(res, k, min(max(sv + off[sv >> 3], 0), 255));
                     }
-                    cls = sign3(sv - n1) + sign3(sv - n2) + 2;
+                } else {
+                    // neighbour words of row y + dy: samples x-1 .. x+2 and x+1 .. x+4
+                    auto lft = [&](int dy) {
+                        const uint32_t *r = reinterpret_cast<const uint32_t *>(d + dy * kLfPitch);
+                        return __byte_perm(has_left ? r[-1] : 0u, r[0], 0x6543);
+                    };
+                    auto rgt = [&](int dy) {
+                        const uint32_t *r = reinterpret_cast<const uint32_t *>(d + dy * kLfPitch);
+                        return __byte_perm(r[0], r[1], 0x4321);
+                    };
+                    uint32_t n1, n2;
+                    switch (ty) {
+                    case 0: n1 = lft(0); n2 = rgt(0); break;
+                    case 1:
+                        n1 = *reinterpret_cast<const uint32_t *>(d - kLfPitch);
+                        n2 = *reinterpret_cast<const uint32_t *>(d + kLfPitch);
+                        break;
+                    case 2: n1 = lft(-1); n2 = rgt(1); break;
+                    default: n1 = rgt(-1); n2 = lft(1); break;
+                    }
+                    res = eo_apply(cur, eo_class(cur, n1, n2), eo_tab);
                 }
-                out = set_byte(out, k, min(max(sv + off[cls], 0), 255));
+                const uint32_t m = (0xFFFFFFFFu << (8 * lo)) & (0xFFFFFFFFu >> (8 * (4 - hi)));
+                out = (res & m) | (cur & ~m);
             }
         }
         *reinterpret_cast<uint32_t *>(dst + (long long)y * st + x) = out;
