@@ -85,6 +85,197 @@ __global__ void edge_kernel(uint8_t *src, int n, int along, int across, int alph
         for (int i = 0; i < 6; i++) s[(i - 3) * across] = (uint8_t)p[i];
 }
 
+// ---- four samples per word (SWAR, Hacker's Delight ch. 2) ---------------------
+// bit 7 of each byte: a >= b, bytewise unsigned.  The low 7 bits are compared
+// through (a | 0x80) - (b & 0x7F), which cannot borrow across bytes.
+__device__ __forceinline__ uint32_t ge_bytes(uint32_t a, uint32_t b)
+{
+    const uint32_t t = (a | 0x80808080u) - (b & 0x7F7F7F7Fu);
+    return ((a & ~b) | (~(a ^ b) & t)) & 0x80808080u;
+}
+// bytewise min(a + b, 255): the sum without carries between bytes, the
+// carry out of each byte, and a byte of ones where it is set
+__device__ __forceinline__ uint32_t addus_bytes(uint32_t a, uint32_t b)
+{
+    const uint32_t s = ((a & 0x7F7F7F7Fu) + (b & 0x7F7F7F7Fu)) ^ ((a ^ b) & 0x80808080u);
+    const uint32_t cy = ((a & b) | ((a | b) & ~s)) & 0x80808080u;
+    return s | cy | (cy - (cy >> 7));
+}
+// bytewise max(a - b, 0) = 255 - min(255 - a + b, 255)
+__device__ __forceinline__ uint32_t subus_bytes(uint32_t a, uint32_t b) { return ~addus_bytes(~a, b); }
+
+// SAO edge class per byte: sign(s - n1) + sign(s - n2) + 2, each term
+// sign(s - n) + 1 = [s >= n] + (1 - [n >= s]); the sum is at most 4
+__device__ __forceinline__ uint32_t eo_class(uint32_t s, uint32_t n1, uint32_t n2)
+{
+    const uint32_t H = 0x80808080u;
+    return ((ge_bytes(s, n1) >> 7) + (ge_bytes(s, n2) >> 7)) +
+           (((ge_bytes(n1, s) ^ H) >> 7) + ((ge_bytes(n2, s) ^ H) >> 7));
+}
+// the edge-offset table of eo_apply: the offsets of classes 0-4 clipped to
+// [0, 255] (words 0-1) and their negations clipped likewise (words 2-3)
+__device__ __forceinline__ void eo_table(const int8_t *offset, uint32_t *tab)
+{
+    uint32_t ad[2] = {0, 0}, sb[2] = {0, 0};
+    for (int k = 0; k < 5; k++) {
+        const int o = offset[k];
+        ad[k >> 2] |= (uint32_t)min(max(o, 0), 255) << (8 * (k & 3));
+        sb[k >> 2] |= (uint32_t)min(max(-o, 0), 255) << (8 * (k & 3));
+    }
+    tab[0] = ad[0]; tab[1] = ad[1]; tab[2] = sb[0]; tab[3] = sb[1];
+}
+// clip(s + offset[class], 0, 255) per byte: the classes (0..4) packed into
+// the 4 selector nibbles of a byte permute over the offsets' positive and
+// negative parts (each clipped to 255, which leaves the clipped sum exact)
+__device__ __forceinline__ uint32_t eo_apply(uint32_t s, uint32_t cls, const uint32_t *tab)
+{
+    const uint32_t sel = __byte_perm(cls | (cls >> 4), 0, 0x0020);
+    return subus_bytes(addus_bytes(s, __byte_perm(tab[0], tab[1], sel)), __byte_perm(tab[2], tab[3], sel));
+}
+
+// Four lines across one edge at once, a line per byte lane: w[0..5] hold
+// L2 L1 L0 R0 R1 R2 of the four lines, `lanes` has bit 7 of each byte set for
+// the lines the edge filters.  The filter-strength decision of filter_line
+// becomes byte masks (no divergence between lines) and its sums are formed in
+// 16-bit halves, the even and the odd lanes.  Returns false when no line
+// changes.
+__device__ __forceinline__ uint32_t lt_bytes(uint32_t a, uint32_t b) { return ge_bytes(a, b) ^ 0x80808080u; }
+__device__ __forceinline__ uint32_t byte_mask(uint32_t m7) { return (m7 >> 7) * 0xFFu; }
+__device__ __forceinline__ uint32_t pick(uint32_t a, uint32_t b, uint32_t m) { return (a & ~m) | (b & m); }
+
+template <bool CHROMA>
+__device__ __forceinline__ bool filter_lines4(uint32_t (&w)[6], uint32_t ew, uint32_t lanes)
+{
+    const uint32_t alpha = ((ew >> 8) & 0xFFu) * 0x01010101u, beta = ((ew >> 16) & 0xFFu) * 0x01010101u;
+    const uint32_t L2 = w[0], L1 = w[1], L0 = w[2], R0 = w[3], R1 = w[4], R2 = w[5];
+    const uint32_t d = __vabsdiffu4(R0, L0);
+    const uint32_t on = lt_bytes(d, alpha) & ge_bytes(d, 0x02020202u) & lanes;
+    if (!on) return false;
+    const uint32_t dl1 = __vabsdiffu4(L1, L0), dr1 = __vabsdiffu4(R0, R1);
+    const uint32_t a1 = lt_bytes(dl1, beta), a2 = lt_bytes(__vabsdiffu4(L2, L0), beta);
+    const uint32_t b1 = lt_bytes(dr1, beta), b2 = lt_bytes(__vabsdiffu4(R0, R2), beta);
+    const uint32_t eq = lt_bytes(dl1 | dr1, 0x01010101u);              // L1 == L0 and R1 == R0
+    const uint32_t c3 = lt_bytes(__vabsdiffu4(L1, R1), beta);
+    // fl = 2 a1 + a2, fr = 2 b1 + b2; strength by fl + fr
+    const uint32_t s6 = a1 & a2 & b1 & b2;
+    const uint32_t s5 = a1 & b1 & (a2 ^ b2);
+    const uint32_t s4_2 = a1 & b1 & ~(a2 | b2);                            // fl = fr = 2
+    const uint32_t s4_1 = a2 & b2 & (a1 ^ b1);                             // (3, 1), (1, 3)
+    const uint32_t s3 = (a1 & a2 & ~(b1 | b2)) | (b1 & b2 & ~(a1 | a2)) | (a1 & b2 & ~(a2 | b1)) |
+                        (a2 & b1 & ~(a1 | b2));
+    const uint32_t f4 = s6 & eq, f3 = (s6 & ~eq) | (s5 & eq), f2 = (s5 & ~eq) | s4_2, f1 = s4_1 | (s3 & c3);
+    // chroma filters one step weaker
+    const uint32_t m4 = CHROMA ? 0u : byte_mask(f4 & on), m3 = byte_mask((CHROMA ? f4 : f3) & on),
+                   m2 = byte_mask((CHROMA ? f3 : f2) & on), m1 = byte_mask((CHROMA ? f2 : f1) & on);
+    if (!(m4 | m3 | m2 | m1)) return false;
+    // the six words split into even / odd lanes (16 bits each); a sum's
+    // result byte is bits 0-7 of each lane after the shift
+    uint32_t e[6], o[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        e[k] = w[k] & 0x00FF00FFu;
+        o[k] = __byte_perm(w[k], 0, 0x4341);
+    }
+    auto join = [](uint32_t ev, uint32_t od) { return __byte_perm(ev, od, 0x6240); };
+    const uint32_t K2 = 0x00020002u, K4 = 0x00040004u, K8 = 0x00080008u, K16 = 0x00100010u;
+    uint32_t nL2 = L2, nL1 = L1, nL0 = L0, nR0 = R0, nR1 = R1, nR2 = R2;
+    if (m1) {
+        auto l0 = [&](const uint32_t *v) { return (3 * v[2] + v[3] + K2) >> 2; };
+        auto r0 = [&](const uint32_t *v) { return (3 * v[3] + v[2] + K2) >> 2; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m1);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m1);
+    }
+    if (m2) {
+        auto l0 = [&](const uint32_t *v) { return (3 * v[1] + 10 * v[2] + 3 * v[3] + K8) >> 4; };
+        auto r0 = [&](const uint32_t *v) { return (3 * v[2] + 10 * v[3] + 3 * v[4] + K8) >> 4; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m2);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m2);
+    }
+    if (m3) {
+        auto l0 = [&](const uint32_t *v) { return (v[0] + 4 * v[1] + 6 * v[2] + 4 * v[3] + v[4] + K8) >> 4; };
+        auto r0 = [&](const uint32_t *v) { return (v[1] + 4 * v[2] + 6 * v[3] + 4 * v[4] + v[5] + K8) >> 4; };
+        auto l1 = [&](const uint32_t *v) { return (3 * v[0] + 8 * v[1] + 4 * v[2] + v[3] + K8) >> 4; };
+        auto r1 = [&](const uint32_t *v) { return (3 * v[5] + 8 * v[4] + 4 * v[3] + v[2] + K8) >> 4; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m3);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m3);
+        nL1 = pick(nL1, join(l1(e), l1(o)), m3);
+        nR1 = pick(nR1, join(r1(e), r1(o)), m3);
+    }
+    if (!CHROMA && m4) {
+        auto l0 = [&](const uint32_t *v) { return (9 * v[2] + 9 * v[0] + 8 * v[3] + 6 * v[5] + K16) >> 5; };
+        auto l1 = [&](const uint32_t *v) { return (7 * v[2] + 6 * v[0] + 3 * v[3] + K8) >> 4; };
+        auto l2 = [&](const uint32_t *v) { return (4 * v[2] + 3 * v[0] + v[3] + K4) >> 3; };
+        auto r0 = [&](const uint32_t *v) { return (9 * v[3] + 9 * v[5] + 8 * v[2] + 6 * v[0] + K16) >> 5; };
+        auto r1 = [&](const uint32_t *v) { return (7 * v[3] + 6 * v[5] + 3 * v[2] + K8) >> 4; };
+        auto r2 = [&](const uint32_t *v) { return (4 * v[3] + 3 * v[5] + v[2] + K4) >> 3; };
+        nL0 = pick(nL0, join(l0(e), l0(o)), m4);
+        nL1 = pick(nL1, join(l1(e), l1(o)), m4);
+        nL2 = pick(nL2, join(l2(e), l2(o)), m4);
+        nR0 = pick(nR0, join(r0(e), r0(o)), m4);
+        nR1 = pick(nR1, join(r1(e), r1(o)), m4);
+        nR2 = pick(nR2, join(r2(e), r2(o)), m4);
+    }
+    w[0] = nL2; w[1] = nL1; w[2] = nL0; w[3] = nR0; w[4] = nR1; w[5] = nR2;
+    return true;
+}
+
+// 4x4 byte transpose: rows a..d (byte k = column k) to columns
+__device__ __forceinline__ void transpose4(uint32_t &a, uint32_t &b, uint32_t &c, uint32_t &d)
+{
+    const uint32_t x = __byte_perm(a, b, 0x5140), y = __byte_perm(a, b, 0x7362);
+    const uint32_t z = __byte_perm(c, d, 0x5140), v = __byte_perm(c, d, 0x7362);
+    a = __byte_perm(x, z, 0x5410);
+    b = __byte_perm(x, z, 0x7632);
+    c = __byte_perm(y, v, 0x5410);
+    d = __byte_perm(y, v, 0x7632);
+}
+
+// The bit-7 lane mask of four lines of one 8x8 block's edge: luma lines
+// share the half's flag; chroma lines 0-1 are the first half, 2-3 the second.
+__device__ __forceinline__ uint32_t edge_lanes(uint32_t ew, bool chroma, int half)
+{
+    if (chroma) return ((ew & 1u) ? 0x00008080u : 0u) | ((ew & 2u) ? 0x80800000u : 0u);
+    return ((ew >> half) & 1u) ? 0x80808080u : 0u;
+}
+
+// ROWS (2 or 4) rows of one vertical edge: p = the samples at (row 0,
+// edge - 4), rows `pitch` apart
+template <bool CHROMA, int ROWS = 4>
+__device__ __forceinline__ void filter_ver4(uint8_t *p, long long pitch, uint32_t ew, uint32_t lanes)
+{
+    uint32_t A[4] = {0, 0, 0, 0}, B[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int r = 0; r < ROWS; r++) {
+        A[r] = *reinterpret_cast<const uint32_t *>(p + r * pitch);
+        B[r] = *reinterpret_cast<const uint32_t *>(p + r * pitch + 4);
+    }
+    transpose4(A[0], A[1], A[2], A[3]);   // A[k] = column edge - 4 + k
+    transpose4(B[0], B[1], B[2], B[3]);   // B[k] = column edge + k
+    uint32_t w[6] = {A[1], A[2], A[3], B[0], B[1], B[2]};
+    if (!filter_lines4<CHROMA>(w, ew, lanes)) return;
+    A[1] = w[0]; A[2] = w[1]; A[3] = w[2]; B[0] = w[3]; B[1] = w[4]; B[2] = w[5];
+    transpose4(A[0], A[1], A[2], A[3]);
+    transpose4(B[0], B[1], B[2], B[3]);
+#pragma unroll
+    for (int r = 0; r < ROWS; r++) {
+        *reinterpret_cast<uint32_t *>(p + r * pitch) = A[r];
+        *reinterpret_cast<uint32_t *>(p + r * pitch + 4) = B[r];
+    }
+}
+
+// Four columns of one horizontal edge: p = the samples at (edge - 3,
+// column 0), rows `pitch` apart
+template <bool CHROMA>
+__device__ __forceinline__ void filter_hor4(uint8_t *p, long long pitch, uint32_t ew, uint32_t lanes)
+{
+    uint32_t w[6];
+#pragma unroll
+    for (int r = 0; r < 6; r++) w[r] = *reinterpret_cast<const uint32_t *>(p + r * pitch);
+    if (!filter_lines4<CHROMA>(w, ew, lanes)) return;
+#pragma unroll
+    for (int r = 0; r < 6; r++) *reinterpret_cast<uint32_t *>(p + r * pitch) = w[r];
+}
+
 // ---- picture deblocking --------------------------------------------------------
 struct Pic {
     uint8_t *y, *u, *v;
@@ -105,7 +296,7 @@ __global__ void __launch_bounds__(256) deblock_ver_kernel(Pic pc)
     const long long n_luma = (long long)(pc.height >> 2) * ne;
     const long long n_chroma = (long long)(pc.height >> 2) * nec;   // 2-line groups of height / 2 rows
     uint8_t *row;
-    int e, x, sx, sy, half, lines, stride;
+    int e, x, sx, sy, half, stride;
     bool chroma;
     if (i < n_luma) {
         const int g = (int)(i / ne);                     // 4-line group
@@ -114,7 +305,6 @@ __global__ void __launch_bounds__(256) deblock_ver_kernel(Pic pc)
         sx = e;
         sy = g >> 1;
         half = g & 1;
-        lines = 4;
         stride = pc.stride;
         row = pc.y + (long long)(4 * g) * stride;
         chroma = false;
@@ -128,7 +318,6 @@ __global__ void __launch_bounds__(256) deblock_ver_kernel(Pic pc)
         sx = 2 * e;
         sy = g >> 1;
         half = g & 1;
-        lines = 2;
         stride = pc.stride_c;
         row = (plane ? pc.v : pc.u) + (long long)(2 * g) * stride;
         chroma = true;
@@ -137,44 +326,27 @@ __global__ void __launch_bounds__(256) deblock_ver_kernel(Pic pc)
     }
     const xavs2gpu_deblock_scu_t q = pc.scus[sy * pc.w_scu + sx];
     if (q.type[0] == 0 || (chroma && q.type[0] != 2) || !q.flag[0][half]) return;
-    const int alpha = chroma ? q.alpha_c[0] : q.alpha[0];
-    const int beta = chroma ? q.beta_c[0] : q.beta[0];
-    for (int k = 0; k < lines; k++) {
-        uint32_t *w = reinterpret_cast<uint32_t *>(row + (long long)k * stride + x - 4);
-        uint32_t a = w[0], b = w[1];
-        int p[6] = {byte_of(a, 1), byte_of(a, 2), byte_of(a, 3), byte_of(b, 0), byte_of(b, 1), byte_of(b, 2)};
-        if (!filter_line(p, alpha, beta, chroma)) continue;
-        w[0] = set_byte(set_byte(set_byte(a, 1, p[0]), 2, p[1]), 3, p[2]);
-        w[1] = set_byte(set_byte(set_byte(b, 0, p[3]), 1, p[4]), 2, p[5]);
-    }
+    const uint32_t ew = ((uint32_t)(chroma ? q.alpha_c[0] : q.alpha[0]) << 8) |
+                        ((uint32_t)(chroma ? q.beta_c[0] : q.beta[0]) << 16);
+    // the lines (4 luma, 2 chroma) as byte lanes of transposed words
+    if (chroma)
+        filter_ver4<true, 2>(row + x - 4, stride, ew, 0x00008080u);
+    else
+        filter_ver4<false, 4>(row + x - 4, stride, ew, 0x80808080u);
 }
 
-// filters columns of one word of a horizontal edge (rows y-3 .. y+2);
-// returns true when a sample changed
-__device__ __forceinline__ bool hor_word(uint8_t *col, int stride, int alpha, int beta, bool chroma, bool f_lo,
+// filters the four columns of one word of a horizontal edge (rows y-3 ..
+// y+2); the first two and the last two columns take flags f_lo and f_hi
+__device__ __forceinline__ void hor_word(uint8_t *col, int stride, int alpha, int beta, bool chroma, bool f_lo,
                                          bool f_hi)
 {
-    uint32_t w[6];
-#pragma unroll
-    for (int r = 0; r < 6; r++) w[r] = *reinterpret_cast<const uint32_t *>(col + (long long)(r - 3) * stride);
-    bool any = false;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        if (!(c < 2 ? f_lo : f_hi)) continue;
-        int p[6];
-#pragma unroll
-        for (int r = 0; r < 6; r++) p[r] = byte_of(w[r], c);
-        if (filter_line(p, alpha, beta, chroma)) {
-            any = true;
-#pragma unroll
-            for (int r = 0; r < 6; r++) w[r] = set_byte(w[r], c, p[r]);
-        }
-    }
-    if (any) {
-#pragma unroll
-        for (int r = 0; r < 6; r++) *reinterpret_cast<uint32_t *>(col + (long long)(r - 3) * stride) = w[r];
-    }
-    return any;
+    const uint32_t ew = ((uint32_t)alpha << 8) | ((uint32_t)beta << 16);
+    const uint32_t lanes = (f_lo ? 0x00008080u : 0u) | (f_hi ? 0x80800000u : 0u);
+    if (!lanes) return;
+    if (chroma)
+        filter_hor4<true>(col - 3LL * stride, stride, ew, lanes);
+    else
+        filter_hor4<false>(col - 3LL * stride, stride, ew, lanes);
 }
 
 // Pass 2: every horizontal edge.  A thread filters one 8x8 block's edge: 8
@@ -332,7 +504,9 @@ __global__ void __launch_bounds__(kSaoThreads, 8) sao_lcu_kernel(SaoPic sp)
     __shared__ int off[32];
     __shared__ int nb[8][7];
     __shared__ int n_nb;
+    __shared__ uint32_t eo_tab[4];
     if (threadIdx.x < 32) off[threadIdx.x] = q.offset[c][threadIdx.x];
+    if (threadIdx.x == 32) eo_table(q.offset[c], eo_tab);
     if (threadIdx.x == 0) {
         int no = 0;
         for (int my = ly - 1; my <= ly + 1; my++)
@@ -408,35 +582,36 @@ __global__ void __launch_bounds__(kSaoThreads, 8) sao_lcu_kernel(SaoPic sp)
             }
         }
         const uint32_t old = sp.copy_rest ? win[1][1] : shared ? 0u : *reinterpret_cast<const uint32_t *>(d);
-        uint32_t out = old;
+        // the samples written: inside [x0, x1) and not filtered by a later
+        // neighbour; all four computed at once
         unsigned wrote = 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int xs = x + k;
-            if (xs < x0 || xs >= x1 || ((later >> k) & 1u)) continue;
-            const int sv = byte_of(win[1][1], k);
-            // neighbour (dx, dy) of sample k: byte 4 + k + dx of the 12-byte
-            // window of row 1 + dy (indices constant after unrolling)
-            auto nbv = [&](int dx, int dy) {
-                const int o = 4 + k + dx;
-                return byte_of(win[1 + dy][o >> 2], o & 3);
-            };
-            int cls;
-            if (t == 4) {
-                cls = sv >> 3;
-            } else {
-                int n1, n2;
-                switch (t) {
-                case 0: n1 = nbv(-1, 0); n2 = nbv(1, 0); break;
-                case 1: n1 = nbv(0, -1); n2 = nbv(0, 1); break;
-                case 2: n1 = nbv(-1, -1); n2 = nbv(1, 1); break;
-                default: n1 = nbv(1, -1); n2 = nbv(-1, 1); break;
-                }
-                cls = sign3(sv - n1) + sign3(sv - n2) + 2;
+        for (int k = 0; k < 4; k++)
+            if (x + k >= x0 && x + k < x1 && !((later >> k) & 1u)) wrote |= 1u << k;
+        const uint32_t cur = win[1][1];
+        uint32_t res;
+        if (t == 4) {
+            res = cur;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int sv = byte_of(cur, k);
+                res = set_byte(res, k, min(max(sv + off[sv >> 3], 0), 255));
             }
-            out = set_byte(out, k, min(max(sv + off[cls], 0), 255));
-            wrote |= 1u << k;
+        } else {
+            // samples x-1 .. x+2 and x+1 .. x+4 of source row r
+            auto lft = [&](int r) { return __byte_perm(win[r][0], win[r][1], 0x6543); };
+            auto rgt = [&](int r) { return __byte_perm(win[r][1], win[r][2], 0x4321); };
+            uint32_t n1, n2;
+            switch (t) {
+            case 0: n1 = lft(1); n2 = rgt(1); break;
+            case 1: n1 = win[0][1]; n2 = win[2][1]; break;
+            case 2: n1 = lft(0); n2 = rgt(2); break;
+            default: n1 = rgt(0); n2 = lft(2); break;
+            }
+            res = eo_apply(cur, eo_class(cur, n1, n2), eo_tab);
         }
+        const uint32_t m = ((wrote * 0x00204081u) & 0x01010101u) * 0xFFu;   // bit k -> byte k
+        const uint32_t out = (res & m) | (old & ~m);
         if (shared) {
 #pragma unroll
             for (int k = 0; k < 4; k++)
@@ -473,42 +648,6 @@ struct FusedPic {
     const xavs2gpu_sao_lcu_t *lcus;
 };
 
-// ---- four samples per word (SWAR, Hacker's Delight ch. 2) ---------------------
-// bit 7 of each byte: a >= b, bytewise unsigned.  The low 7 bits are compared
-// through (a | 0x80) - (b & 0x7F), which cannot borrow across bytes.
-__device__ __forceinline__ uint32_t ge_bytes(uint32_t a, uint32_t b)
-{
-    const uint32_t t = (a | 0x80808080u) - (b & 0x7F7F7F7Fu);
-    return ((a & ~b) | (~(a ^ b) & t)) & 0x80808080u;
-}
-// bytewise min(a + b, 255): the sum without carries between bytes, the
-// carry out of each byte, and a byte of ones where it is set
-__device__ __forceinline__ uint32_t addus_bytes(uint32_t a, uint32_t b)
-{
-    const uint32_t s = ((a & 0x7F7F7F7Fu) + (b & 0x7F7F7F7Fu)) ^ ((a ^ b) & 0x80808080u);
-    const uint32_t cy = ((a & b) | ((a | b) & ~s)) & 0x80808080u;
-    return s | cy | (cy - (cy >> 7));
-}
-// bytewise max(a - b, 0) = 255 - min(255 - a + b, 255)
-__device__ __forceinline__ uint32_t subus_bytes(uint32_t a, uint32_t b) { return ~addus_bytes(~a, b); }
-
-// SAO edge class per byte: sign(s - n1) + sign(s - n2) + 2, each term
-// sign(s - n) + 1 = [s >= n] + (1 - [n >= s]); the sum is at most 4
-__device__ __forceinline__ uint32_t eo_class(uint32_t s, uint32_t n1, uint32_t n2)
-{
-    const uint32_t H = 0x80808080u;
-    return ((ge_bytes(s, n1) >> 7) + (ge_bytes(s, n2) >> 7)) +
-           (((ge_bytes(n1, s) ^ H) >> 7) + ((ge_bytes(n2, s) ^ H) >> 7));
-}
-// clip(s + offset[class], 0, 255) per byte: the classes (0..4) packed into
-// the 4 selector nibbles of a byte permute over the offsets' positive and
-// negative parts (each clipped to 255, which leaves the clipped sum exact)
-__device__ __forceinline__ uint32_t eo_apply(uint32_t s, uint32_t cls, const uint32_t *tab)
-{
-    const uint32_t sel = __byte_perm(cls | (cls >> 4), 0, 0x0020);
-    return subus_bytes(addus_bytes(s, __byte_perm(tab[0], tab[1], sel)), __byte_perm(tab[2], tab[3], sel));
-}
-
 // Per 8x8 block and direction, the edge as one word for the component:
 // bit 0 filter the first half, bit 1 the second half (type and flag
 // combined), alpha in bits 8-15, beta in bits 16-23.
@@ -519,147 +658,6 @@ __device__ __forceinline__ uint32_t edge_word(const xavs2gpu_deblock_scu_t &e, i
     return (e.flag[dir][0] ? 1u : 0u) | (e.flag[dir][1] ? 2u : 0u) |
            ((uint32_t)(chroma ? e.alpha_c[dir] : e.alpha[dir]) << 8) |
            ((uint32_t)(chroma ? e.beta_c[dir] : e.beta[dir]) << 16);
-}
-
-// Four lines across one edge at once, a line per byte lane: w[0..5] hold
-// L2 L1 L0 R0 R1 R2 of the four lines, `lanes` has bit 7 of each byte set for
-// the lines the edge filters.  The filter-strength decision of filter_line
-// becomes byte masks (no divergence between lines) and its sums are formed in
-// 16-bit halves, the even and the odd lanes.  Returns false when no line
-// changes.
-__device__ __forceinline__ uint32_t lt_bytes(uint32_t a, uint32_t b) { return ge_bytes(a, b) ^ 0x80808080u; }
-__device__ __forceinline__ uint32_t byte_mask(uint32_t m7) { return (m7 >> 7) * 0xFFu; }
-__device__ __forceinline__ uint32_t pick(uint32_t a, uint32_t b, uint32_t m) { return (a & ~m) | (b & m); }
-
-template <bool CHROMA>
-__device__ __forceinline__ bool filter_lines4(uint32_t (&w)[6], uint32_t ew, uint32_t lanes)
-{
-    const uint32_t alpha = ((ew >> 8) & 0xFFu) * 0x01010101u, beta = ((ew >> 16) & 0xFFu) * 0x01010101u;
-    const uint32_t L2 = w[0], L1 = w[1], L0 = w[2], R0 = w[3], R1 = w[4], R2 = w[5];
-    const uint32_t d = __vabsdiffu4(R0, L0);
-    const uint32_t on = lt_bytes(d, alpha) & ge_bytes(d, 0x02020202u) & lanes;
-    if (!on) return false;
-    const uint32_t dl1 = __vabsdiffu4(L1, L0), dr1 = __vabsdiffu4(R0, R1);
-    const uint32_t a1 = lt_bytes(dl1, beta), a2 = lt_bytes(__vabsdiffu4(L2, L0), beta);
-    const uint32_t b1 = lt_bytes(dr1, beta), b2 = lt_bytes(__vabsdiffu4(R0, R2), beta);
-    const uint32_t eq = lt_bytes(dl1 | dr1, 0x01010101u);              // L1 == L0 and R1 == R0
-    const uint32_t c3 = lt_bytes(__vabsdiffu4(L1, R1), beta);
-    // fl = 2 a1 + a2, fr = 2 b1 + b2; strength by fl + fr
-    const uint32_t s6 = a1 & a2 & b1 & b2;
-    const uint32_t s5 = a1 & b1 & (a2 ^ b2);
-    const uint32_t s4_2 = a1 & b1 & ~(a2 | b2);                            // fl = fr = 2
-    const uint32_t s4_1 = a2 & b2 & (a1 ^ b1);                             // (3, 1), (1, 3)
-    const uint32_t s3 = (a1 & a2 & ~(b1 | b2)) | (b1 & b2 & ~(a1 | a2)) | (a1 & b2 & ~(a2 | b1)) |
-                        (a2 & b1 & ~(a1 | b2));
-    const uint32_t f4 = s6 & eq, f3 = (s6 & ~eq) | (s5 & eq), f2 = (s5 & ~eq) | s4_2, f1 = s4_1 | (s3 & c3);
-    // chroma filters one step weaker
-    const uint32_t m4 = CHROMA ? 0u : byte_mask(f4 & on), m3 = byte_mask((CHROMA ? f4 : f3) & on),
-                   m2 = byte_mask((CHROMA ? f3 : f2) & on), m1 = byte_mask((CHROMA ? f2 : f1) & on);
-    if (!(m4 | m3 | m2 | m1)) return false;
-    // the six words split into even / odd lanes (16 bits each); a sum's
-    // result byte is bits 0-7 of each lane after the shift
-    uint32_t e[6], o[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        e[k] = w[k] & 0x00FF00FFu;
-        o[k] = __byte_perm(w[k], 0, 0x4341);
-    }
-    auto join = [](uint32_t ev, uint32_t od) { return __byte_perm(ev, od, 0x6240); };
-    const uint32_t K2 = 0x00020002u, K4 = 0x00040004u, K8 = 0x00080008u, K16 = 0x00100010u;
-    uint32_t nL2 = L2, nL1 = L1, nL0 = L0, nR0 = R0, nR1 = R1, nR2 = R2;
-    if (m1) {
-        auto l0 = [&](const uint32_t *v) { return (3 * v[2] + v[3] + K2) >> 2; };
-        auto r0 = [&](const uint32_t *v) { return (3 * v[3] + v[2] + K2) >> 2; };
-        nL0 = pick(nL0, join(l0(e), l0(o)), m1);
-        nR0 = pick(nR0, join(r0(e), r0(o)), m1);
-    }
-    if (m2) {
-        auto l0 = [&](const uint32_t *v) { return (3 * v[1] + 10 * v[2] + 3 * v[3] + K8) >> 4; };
-        auto r0 = [&](const uint32_t *v) { return (3 * v[2] + 10 * v[3] + 3 * v[4] + K8) >> 4; };
-        nL0 = pick(nL0, join(l0(e), l0(o)), m2);
-        nR0 = pick(nR0, join(r0(e), r0(o)), m2);
-    }
-    if (m3) {
-        auto l0 = [&](const uint32_t *v) { return (v[0] + 4 * v[1] + 6 * v[2] + 4 * v[3] + v[4] + K8) >> 4; };
-        auto r0 = [&](const uint32_t *v) { return (v[1] + 4 * v[2] + 6 * v[3] + 4 * v[4] + v[5] + K8) >> 4; };
-        auto l1 = [&](const uint32_t *v) { return (3 * v[0] + 8 * v[1] + 4 * v[2] + v[3] + K8) >> 4; };
-        auto r1 = [&](const uint32_t *v) { return (3 * v[5] + 8 * v[4] + 4 * v[3] + v[2] + K8) >> 4; };
-        nL0 = pick(nL0, join(l0(e), l0(o)), m3);
-        nR0 = pick(nR0, join(r0(e), r0(o)), m3);
-        nL1 = pick(nL1, join(l1(e), l1(o)), m3);
-        nR1 = pick(nR1, join(r1(e), r1(o)), m3);
-    }
-    if (!CHROMA && m4) {
-        auto l0 = [&](const uint32_t *v) { return (9 * v[2] + 9 * v[0] + 8 * v[3] + 6 * v[5] + K16) >> 5; };
-        auto l1 = [&](const uint32_t *v) { return (7 * v[2] + 6 * v[0] + 3 * v[3] + K8) >> 4; };
-        auto l2 = [&](const uint32_t *v) { return (4 * v[2] + 3 * v[0] + v[3] + K4) >> 3; };
-        auto r0 = [&](const uint32_t *v) { return (9 * v[3] + 9 * v[5] + 8 * v[2] + 6 * v[0] + K16) >> 5; };
-        auto r1 = [&](const uint32_t *v) { return (7 * v[3] + 6 * v[5] + 3 * v[2] + K8) >> 4; };
-        auto r2 = [&](const uint32_t *v) { return (4 * v[3] + 3 * v[5] + v[2] + K4) >> 3; };
-        nL0 = pick(nL0, join(l0(e), l0(o)), m4);
-        nL1 = pick(nL1, join(l1(e), l1(o)), m4);
-        nL2 = pick(nL2, join(l2(e), l2(o)), m4);
-        nR0 = pick(nR0, join(r0(e), r0(o)), m4);
-        nR1 = pick(nR1, join(r1(e), r1(o)), m4);
-        nR2 = pick(nR2, join(r2(e), r2(o)), m4);
-    }
-    w[0] = nL2; w[1] = nL1; w[2] = nL0; w[3] = nR0; w[4] = nR1; w[5] = nR2;
-    return true;
-}
-
-// 4x4 byte transpose: rows a..d (byte k = column k) to columns
-__device__ __forceinline__ void transpose4(uint32_t &a, uint32_t &b, uint32_t &c, uint32_t &d)
-{
-    const uint32_t x = __byte_perm(a, b, 0x5140), y = __byte_perm(a, b, 0x7362);
-    const uint32_t z = __byte_perm(c, d, 0x5140), v = __byte_perm(c, d, 0x7362);
-    a = __byte_perm(x, z, 0x5410);
-    b = __byte_perm(x, z, 0x7632);
-    c = __byte_perm(y, v, 0x5410);
-    d = __byte_perm(y, v, 0x7632);
-}
-
-// The bit-7 lane mask of four lines of one 8x8 block's edge: luma lines
-// share the half's flag; chroma lines 0-1 are the first half, 2-3 the second.
-__device__ __forceinline__ uint32_t edge_lanes(uint32_t ew, bool chroma, int half)
-{
-    if (chroma) return ((ew & 1u) ? 0x00008080u : 0u) | ((ew & 2u) ? 0x80800000u : 0u);
-    return ((ew >> half) & 1u) ? 0x80808080u : 0u;
-}
-
-// Four rows of one vertical edge: p = the tile at (row 0, edge - 4)
-template <bool CHROMA>
-__device__ __forceinline__ void filter_ver4(uint8_t *p, uint32_t ew, uint32_t lanes)
-{
-    uint32_t A[4], B[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        A[r] = *reinterpret_cast<const uint32_t *>(p + r * kLfPitch);
-        B[r] = *reinterpret_cast<const uint32_t *>(p + r * kLfPitch + 4);
-    }
-    transpose4(A[0], A[1], A[2], A[3]);   // A[k] = column edge - 4 + k
-    transpose4(B[0], B[1], B[2], B[3]);   // B[k] = column edge + k
-    uint32_t w[6] = {A[1], A[2], A[3], B[0], B[1], B[2]};
-    if (!filter_lines4<CHROMA>(w, ew, lanes)) return;
-    A[1] = w[0]; A[2] = w[1]; A[3] = w[2]; B[0] = w[3]; B[1] = w[4]; B[2] = w[5];
-    transpose4(A[0], A[1], A[2], A[3]);
-    transpose4(B[0], B[1], B[2], B[3]);
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        *reinterpret_cast<uint32_t *>(p + r * kLfPitch) = A[r];
-        *reinterpret_cast<uint32_t *>(p + r * kLfPitch + 4) = B[r];
-    }
-}
-
-// Four columns of one horizontal edge: p = the tile at (edge - 3, column 0)
-template <bool CHROMA>
-__device__ __forceinline__ void filter_hor4(uint8_t *p, uint32_t ew, uint32_t lanes)
-{
-    uint32_t w[6];
-#pragma unroll
-    for (int r = 0; r < 6; r++) w[r] = *reinterpret_cast<const uint32_t *>(p + r * kLfPitch);
-    if (!filter_lines4<CHROMA>(w, ew, lanes)) return;
-#pragma unroll
-    for (int r = 0; r < 6; r++) *reinterpret_cast<uint32_t *>(p + r * kLfPitch) = w[r];
 }
 
 // The deblocking of the tile: vertical edges on the rows [vy0, vy1) in
@@ -677,7 +675,7 @@ __device__ __forceinline__ void deblock_tile(uint8_t (*t)[kLfPitch], const uint3
         const int g = i / nex, ex = ex0 + 8 * (i - g * nex), y = gy0 + 4 * g;
         const uint32_t ew = ev[((y >> sh) - sy0) * nsx + (ex >> sh) - sx0];
         const uint32_t lanes = edge_lanes(ew, CHROMA, (y & 7) >= 4);
-        if (lanes) filter_ver4<CHROMA>(&t[y - ty0][ex - tx0 - 4], ew, lanes);
+        if (lanes) filter_ver4<CHROMA>(&t[y - ty0][ex - tx0 - 4], kLfPitch, ew, lanes);
     }
     __syncthreads();
     const int wx0 = cx0 & ~3, nwc = (((cx1 + 3) & ~3) - wx0) >> 2;
@@ -685,7 +683,7 @@ __device__ __forceinline__ void deblock_tile(uint8_t (*t)[kLfPitch], const uint3
         const int j = i / nwc, x = wx0 + 4 * (i - j * nwc), ey = ey0 + 8 * j;
         const uint32_t ew = eh[((ey >> sh) - sy0) * nsx + (x >> sh) - sx0];
         const uint32_t lanes = edge_lanes(ew, CHROMA, (x & 7) >= 4);
-        if (lanes) filter_hor4<CHROMA>(&t[ey - ty0 - 3][x - tx0], ew, lanes);
+        if (lanes) filter_hor4<CHROMA>(&t[ey - ty0 - 3][x - tx0], kLfPitch, ew, lanes);
     }
 }
 
@@ -707,15 +705,7 @@ __global__ void __launch_bounds__(XG_LF_THREADS) loopfilter_lcu_kernel(FusedPic 
     uint8_t *dst = c == 0 ? fp.dst[0] : c == 1 ? fp.dst[1] : fp.dst[2];
     const int tx0 = max(rx - 8, 0), tx1 = min(rx + rw + 8, W), ty0 = max(ry - 8, 0), ty1 = min(ry + rh + 8, H);
     if (tid < 32) off[tid] = q.offset[c][tid];
-    if (tid == 32) {
-        uint32_t ad[2] = {0, 0}, sb[2] = {0, 0};
-        for (int k = 0; k < 5; k++) {
-            const int o = q.offset[c][k];
-            ad[k >> 2] |= (uint32_t)min(max(o, 0), 255) << (8 * (k & 3));
-            sb[k >> 2] |= (uint32_t)min(max(-o, 0), 255) << (8 * (k & 3));
-        }
-        eo_tab[0] = ad[0]; eo_tab[1] = ad[1]; eo_tab[2] = sb[0]; eo_tab[3] = sb[1];
-    }
+    if (tid == 32) eo_table(q.offset[c], eo_tab);
     // edge words of the 8x8 blocks the tile touches
     const int sh = chroma ? 2 : 3;
     const int sx0 = tx0 >> sh, sy0 = ty0 >> sh, nsx = ((tx1 - 1) >> sh) - sx0 + 1, nsy = ((ty1 - 1) >> sh) - sy0 + 1;
