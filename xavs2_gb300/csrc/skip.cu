@@ -116,15 +116,37 @@ __device__ int hsum8_pred(const Ctx &c, int X, int Y, const PuSrc *src4)
     int m[8][8];
 #pragma unroll
     for (int y = 0; y < 8; y++) {
-        const uint8_t *cur = c.cur + (long long)(Y + y) * c.stride + X;
-        const uint32_t c0 = ld4u(cur), c1 = ld4u(cur + 4);
+        // the current picture is the session's plane: stride a multiple of
+        // 64, origin 16-byte aligned, X a multiple of 8
+        const uint2 cw = *reinterpret_cast<const uint2 *>(c.cur + (long long)(Y + y) * c.stride + X);
+        const uint32_t c0 = cw.x, c1 = cw.y;
         uint32_t pw[2];
+        if (QUAD) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const PuSrc &ps = src4[QUAD ? (y >= 4) * 2 + h : 0];
-            const long long o = (long long)(QUAD ? (y & 3) : y) * c.stride + (QUAD ? 0 : 4 * h);
-            const uint32_t a = ld4u(ps.p[0] + o);
-            pw[h] = ps.n == 2 ? avg4(a, ld4u(ps.p[1] + o)) : a;   // one list: the plane's samples
+            for (int h = 0; h < 2; h++) {
+                const PuSrc &ps = src4[(y >= 4) * 2 + h];
+                const long long o = (long long)(y & 3) * c.stride;
+                const uint32_t a = ld4u(ps.p[0] + o);
+                pw[h] = ps.n == 2 ? avg4(a, ld4u(ps.p[1] + o)) : a;   // one list: the plane's samples
+            }
+        } else {
+            // the row's 8 prediction samples from the 3 aligned words holding them
+            auto ld8u = [&](const uint8_t *q, uint32_t &lo, uint32_t &hi) {
+                const uintptr_t a = reinterpret_cast<uintptr_t>(q);
+                const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+                const unsigned sh = (unsigned)(a & 3) * 8u;
+                const uint32_t w0 = w[0], w1 = w[1], w2 = w[2];
+                lo = __funnelshift_r(w0, w1, sh);
+                hi = __funnelshift_r(w1, w2, sh);
+            };
+            const long long o = (long long)y * c.stride;
+            ld8u(src4[0].p[0] + o, pw[0], pw[1]);
+            if (src4[0].n == 2) {
+                uint32_t b0, b1;
+                ld8u(src4[0].p[1] + o, b0, b1);
+                pw[0] = avg4(pw[0], b0);
+                pw[1] = avg4(pw[1], b1);
+            }
         }
         int t[8];
 #pragma unroll
