@@ -198,3 +198,63 @@ def test_loopfilter_fused(gpu, olib, w, h, lcu):
     for k in range(3):
         assert np.array_equal(out[k].cpu().numpy(), exp[k]), k
         assert np.array_equal(src[k].cpu().numpy(), (y, u, v)[k])   # source untouched
+
+
+@pytest.mark.parametrize("w,h,lcu", [(200, 120, 6), (136, 72, 5), (64, 48, 4)])
+def test_loopfilter_extreme_params(gpu, olib, w, h, lcu):
+    """The word-wise filters at the edges of their value ranges: alpha and
+    beta over the whole byte range (0, 1, 2 and 255 included), pictures of
+    flat 8x8 blocks with small steps between them (so every filter strength,
+    including the one that needs L1 == L0 and R1 == R0, occurs), and SAO
+    offsets over the whole int8 range (the saturating byte arithmetic).
+    Both the fused pass and the two picture passes against the oracle."""
+    import torch
+    import xavs2_gb300.synth as synth
+    rng = np.random.default_rng(w * 11 + h + lcu)
+    y, u, v, scus = synth.deblock_picture(rng, w, h, p_edge=0.95)
+    for p, bs in ((y, 8), (u, 4), (v, 4)):
+        # about half the blocks flat: their value plus a step of -3..3
+        for by in range(0, p.shape[0], bs):
+            for bx in range(0, p.shape[1], bs):
+                if rng.random() < 0.5:
+                    blk = p[by:by + bs, bx:bx + bs]
+                    blk[:] = np.clip(int(blk.mean()) + int(rng.integers(-3, 4)), 0, 255)
+    for f in ("alpha", "beta", "alpha_c", "beta_c"):
+        scus[f] = rng.integers(0, 256, scus[f].shape)
+        k = rng.integers(0, len(scus), 8)
+        scus[f][k[:2]] = 0
+        scus[f][k[2:4]] = 1
+        scus[f][k[4:6]] = 2
+        scus[f][k[6:]] = 255
+    lcus = synth.sao_params(rng, w, h, lcu, p_off=0.05)
+    lcus["offset"] = rng.integers(-128, 128, lcus["offset"].shape)
+    lcus["offset"][0::3] = 127
+    lcus["offset"][1::5] = -128
+    dy, du, dv = y.copy(), u.copy(), v.copy()
+    olib.xo_deblock_picture(oracle.ptr(dy), w, oracle.ptr(du), oracle.ptr(dv), w // 2, w, h, oracle.ptr(scus), lcu, 1)
+    assert not np.array_equal(dy, y)
+    exp = [dy.copy(), du.copy(), dv.copy()]
+    dptr = (ctypes.c_void_p * 3)(*[oracle.ptr(p).value for p in exp])
+    sptr = (ctypes.c_void_p * 3)(*[oracle.ptr(p).value for p in (dy, du, dv)])
+    olib.xo_sao_picture(dptr, sptr, w, w // 2, w, h, lcu, oracle.ptr(lcus))
+    ds, dl = _dev(scus.view(np.uint8)), _dev(lcus.view(np.uint8))
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    # fused
+    src = [_dev(p) for p in (y, u, v)]
+    out = [torch.full(p.shape, 7, dtype=torch.uint8, device="cuda") for p in (y, u, v)]
+    rc = gpu.xavs2gpu_loopfilter_picture(*[P(t) for t in src + out], w, w // 2, w, h, lcu, P(ds), P(dl), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert np.array_equal(out[k].cpu().numpy(), exp[k]), ("fused", k)
+    # two passes: deblocking in place, then SAO writing the picture whole
+    work = [_dev(p) for p in (y, u, v)]
+    rc = gpu.xavs2gpu_deblock_picture(P(work[0]), w, P(work[1]), P(work[2]), w // 2, w, h, lcu, P(ds), None)
+    assert rc == 0
+    out2 = [torch.full(p.shape, 7, dtype=torch.uint8, device="cuda") for p in (y, u, v)]
+    rc = gpu.xavs2gpu_sao_picture(*[P(t) for t in out2 + work], w, w // 2, w, h, lcu, P(dl), 1, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert np.array_equal(work[k].cpu().numpy(), (dy, du, dv)[k]), ("deblock", k)
+        assert np.array_equal(out2[k].cpu().numpy(), exp[k]), ("two-pass", k)
