@@ -121,8 +121,8 @@ MEASURED_TRAFFIC = {
     "me": 15083008 + 5165824,          # fs_ctu_kernel<0> + <1>, one picture
     "tq": 5013000000,                  # tq_chain_kernel, 10^6 blocks (scaled from 10^5)
     "intra": 39612928 + 31689984,      # rmd_tile_kernel
-    "lookahead": 8306176,              # lookahead_kernel
-    "skip": 104250368 + 4567808,       # skip_cost_kernel
+    "lookahead": 8311040,              # lookahead_kernel (16x4 strips)
+    "skip": 106347008 + 5720832,       # skip_cost_kernel
     "loopfilter": 14746368,            # loopfilter_lcu_kernel (deblocking + SAO in one pass)
 }
 
