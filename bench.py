@@ -139,13 +139,15 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def cpu_sample_search(pus, cur, refs, prm_tuple, fraction, seed, threads):
+def cpu_sample_search(pus, cur, refs, prm_tuple, fraction, seed, threads, want_results=False):
     """The oracle's restatement of xavs2_me_search over a random sample of
-    the PU list, on `threads` host threads; returns (evals, seconds)."""
+    the PU list, on `threads` host threads; returns (evals, seconds, sample
+    size) and, with want_results, the sampled indices and their results."""
     import oracle
     olib = oracle.lib()
     rng = np.random.default_rng(seed)
-    sel = np.ascontiguousarray(pus[rng.random(len(pus)) < fraction])
+    idx = np.flatnonzero(rng.random(len(pus)) < fraction)
+    sel = np.ascontiguousarray(pus[idx])
     h, w = cur.shape
     stride = w + 160
     flats = [np.ascontiguousarray(oracle.interpolate_frame(olib, r, mode=2).reshape(16, -1)) for r in refs]
@@ -157,7 +159,26 @@ def cpu_sample_search(pus, cur, refs, prm_tuple, fraction, seed, threads):
     olib.xo_me_search_list(ctypes.byref(prm), oracle.ptr(sel), len(sel), oracle.ptr(cur), w, frefs, stride,
                            oracle.ptr(out), threads)
     dt = time.perf_counter() - t0
+    if want_results:
+        return count_evals(sel, prm_tuple[0]), dt, len(sel), idx, out
     return count_evals(sel, prm_tuple[0]), dt, len(sel)
+
+
+def parity_check(gpu_results, idx, oracle_results, what):
+    """Compares the GPU's results at the sampled indices with the oracle's
+    (byte for byte: every field of every result); returns the bench line's
+    parity object."""
+    got = np.ascontiguousarray(gpu_results[idx]).view(np.uint8).reshape(len(idx), -1)
+    exp = np.ascontiguousarray(oracle_results).view(np.uint8).reshape(len(idx), -1)
+    bad = np.flatnonzero((got != exp).any(axis=1))
+    return {"checked": int(len(idx)), "mismatches": int(len(bad)), "against": "oracle", "sample": what,
+            "first_mismatch": int(idx[bad[0]]) if len(bad) else None}
+
+
+def sm_count():
+    """SM count of the current CUDA device (the integer roofs scale with it)."""
+    import torch
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
 
 
 def reduce_max(value, device):
@@ -381,19 +402,26 @@ def run_ours(args):
         return
     # roofline of the dominant kernel (shared-window CTU search): the
     # algorithmic work is 4096 absolute differences (one 64x64 CTU) per
-    # (CTU, reference, displacement); the SM peak is 152 SMs x 64 lanes/clk
-    # of VABSDIFF4 (4 pixels each, half the INT32 issue rate) x max SM clock.
+    # (CTU, reference, displacement); the SM peak is the device's SMs x 64
+    # lanes/clk of VABSDIFF4 (4 pixels each, half the INT32 issue rate) x max
+    # SM clock.
     ctu_px = n_jobs * n_pos * 4096
     ctu_ms = phases[1]
     achieved = ctu_px / (ctu_ms / 1e3) / 1e12
-    peak = 152 * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    peak = sm_count() * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     # interpolation (HBM-bound): 15 planes written with their margin + the source read, per reference
     plane_bytes = (WIDTH + 160) * (HEIGHT + 160)
     interp_bytes = NREFS * (15 * plane_bytes + WIDTH * HEIGHT)
     interp_gbs = interp_bytes / (interp_ms / 1e3) / 1e9
 
-    cpu_e, cpu_s, cpu_n = cpu_sample_search(pus, cur, refs, (RANGE, prm.lambda_factor, 1, 2, 0, 0),
-                                            args.cpu_fraction, 7, os.cpu_count() or 1)
+    cpu_e, cpu_s, cpu_n, cpu_idx, cpu_res = cpu_sample_search(pus, cur, refs, (RANGE, prm.lambda_factor, 1, 2, 0, 0),
+                                                              args.cpu_fraction, 7, os.cpu_count() or 1,
+                                                              want_results=True)
+    # the timed run's results (last warm-up; the e2e run's download equals
+    # it) against the oracle on the CPU sample: every field of every sampled
+    # PU search, border CTUs and the partial bottom CTU row included
+    parity = parity_check(res, cpu_idx, cpu_res, "the CPU baseline's random %.2f%% of the picture's PU searches"
+                          % (100 * args.cpu_fraction))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -410,7 +438,7 @@ def run_ours(args):
         "roofline": {"bound": "int", "kernel": "fs_ctu_kernel", "achieved": achieved, "peak": peak,
                      "unit": "Tpx-absdiff/s", "frac": achieved / peak,
                      "traffic": measured_traffic("me", (WIDTH, HEIGHT, RANGE) == (1920, 1080, 64)),
-                     "peak_source": "152 SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % peak_src,
+                     "peak_source": "%d SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % (sm_count(), peak_src),
                      "work_per_launch": "%d CTU-ref jobs x %d displacements x 4096 px" % (n_jobs, n_pos),
                      "kernel_ms": ctu_ms},
         "kernels_ms": {"candidates": phases[0], "ctu_search": phases[1], "per_pu_search": phases[2],
@@ -422,10 +450,14 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_e / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": "random %.2f%% (%d) of the picture's PU searches, oracle C port, OpenMP"
                                    % (100 * args.cpu_fraction, cpu_n)},
+        "parity": parity,
         "clocks": clocks,
     }
     print(json.dumps(line))
     sess.close()
+    if parity["mismatches"] or not same:
+        sys.exit("bench: motion-search results differ from the oracle on %d of %d sampled PU searches"
+                 " (e2e equal to device run: %s)" % (parity["mismatches"], parity["checked"], same))
 
 
 # ---- batched transform + quant ---------------------------------------------
@@ -817,7 +849,7 @@ def run_intra(args):
     peaks, peak_src = measured_peaks()
     rmd_ms = max(kernel_ms - fill_ms, 1e-6)
     achieved = mode_samples / (rmd_ms / 1e3) / 1e12
-    peak = 152 * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / INTRA_OPS_PER_SAMPLE / 1e12
+    peak = sm_count() * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / INTRA_OPS_PER_SAMPLE / 1e12
     line = {
         "metric": INTRA_METRIC, "value": value, "unit": "mode-samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -830,8 +862,8 @@ def run_intra(args):
         "roofline": {"bound": "int", "kernel": "intra_rmd_batch (sort, tiles, candidates)", "achieved": achieved, "peak": peak,
                      "unit": "T mode-samples/s", "frac": achieved / peak,
                      "traffic": measured_traffic("intra", (W, H) == (1920, 1080)),
-                     "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per mode-sample (%s)"
-                                    % (INTRA_OPS_PER_SAMPLE, peak_src),
+                     "peak_source": "%d SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per mode-sample (%s)"
+                                    % (sm_count(), INTRA_OPS_PER_SAMPLE, peak_src),
                      "work_per_launch": "%d blocks, %d mode-samples" % (n, mode_samples),
                      "kernel_ms": rmd_ms},
         "sample_bit_exact": exact,
@@ -1325,7 +1357,7 @@ def run_skip(args):
     exact = bool(np.array_equal(dist_h[gi], d) and np.array_equal(cost_h[gi], c) and
                  np.array_equal(np.where(gb >= 0, np.searchsorted(gi, gb), -1), b))
     peaks, peak_src = measured_peaks()
-    peak = 152 * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / SKIP_OPS_PER_SAMPLE / 1e12
+    peak = sm_count() * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / SKIP_OPS_PER_SAMPLE / 1e12
     achieved = samples / (kernel_ms / 1e3) / 1e12
     print(json.dumps({
         "metric": SKIP_METRIC, "value": value, "unit": "candidates/s", "n_gpus": world, "steps": args.steps,
@@ -1337,8 +1369,8 @@ def run_skip(args):
         "roofline": {"bound": "int", "kernel": "skip_count + skip_scatter + skip_cost + skip_best", "achieved": achieved,
                      "peak": peak, "unit": "T candidate-samples/s", "frac": achieved / peak,
                      "traffic": measured_traffic("skip", (W, H) == (1920, 1080)),
-                     "peak_source": "152 SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per sample (%s)"
-                                    % (SKIP_OPS_PER_SAMPLE, peak_src),
+                     "peak_source": "%d SMs x 128 INT32 lanes/clk x sm_max_mhz / %d ops per sample (%s)"
+                                    % (sm_count(), SKIP_OPS_PER_SAMPLE, peak_src),
                      "work_per_launch": "%d candidates, %d predicted samples" % (n, samples), "kernel_ms": kernel_ms},
         "sample_bit_exact": exact,
         "cpu_baseline": {"value": k / cpu_s, "unit": "candidates/s", "cores": 1, "kind": "port",
@@ -1578,7 +1610,7 @@ def run_chain(args):
     peaks, peak_src = measured_peaks()
     ctu_px = n_jobs.value * (2 * R) * (2 * R) * 4096
     ctu_ach = ctu_px / (ph[1] / 1e3) / 1e12
-    ctu_peak = 152 * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    ctu_peak = sm_count() * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     # CPU baseline: the oracle's search over a sample of the picture's PU
     # searches (the search is ~99 % of the chain's work), scaled to pictures
     evals = count_evals(pus, R)
@@ -1603,7 +1635,7 @@ def run_chain(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "fs_ctu_kernel", "achieved": ctu_ach, "peak": ctu_peak,
                      "unit": "Tpx-absdiff/s", "frac": ctu_ach / ctu_peak, "traffic": None,
-                     "peak_source": "152 SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % peak_src,
+                     "peak_source": "%d SMs x 64 VABSDIFF4 lanes/clk x 4 px x sm_max_mhz (%s)" % (sm_count(), peak_src),
                      "work_per_launch": "%d CTU-ref jobs x %d displacements x 4096 px" % (n_jobs.value, 4 * R * R),
                      "kernel_ms": float(ph[1]), "eager_search_phases_ms": [float(v) for v in ph]},
         "cpu_baseline": {"value": cpu_fps, "unit": "pictures/s", "cores": os.cpu_count() or 1, "kind": "port",

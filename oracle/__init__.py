@@ -15,7 +15,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libxavs2ref.so")
-REF_SRC = os.environ.get("XAVS2_REF_SRC", "/root/reference/source")
+
+
+def _recipe_ref_src():
+    """The reference source directory the build recipe (Makefile, REF_SRC)
+    names; XAVS2_REF_SRC overrides it."""
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF_SRC") and "?=" in line:
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+REF_SRC = os.environ.get("XAVS2_REF_SRC") or _recipe_ref_src()
 
 # LumaPU order (pixel.h:50-65)
 PU_W = [4, 8, 16, 32, 64, 8, 4, 16, 8, 32, 16, 64, 32, 16, 12, 16, 4, 32, 24, 32, 8, 64, 48, 64, 16]

@@ -9,9 +9,11 @@ import tempfile
 
 import pytest
 
+import oracle
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "xavs2_gb300.h")
-REF_SRC = os.environ.get("XAVS2_REF_SRC", "/root/reference/source")
+REF_SRC = oracle.REF_SRC
 
 
 @pytest.fixture(scope="module")

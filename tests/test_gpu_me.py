@@ -1,6 +1,7 @@
 """Batched motion search on the GPU against the oracle's restatement of
 xavs2_me_search (full search + sub-pel refinement), bit-exact."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -213,3 +214,30 @@ def test_tuning_cu_groups(gpu, olib):
     s.close()
     exp = _oracle(olib, f1, [f0], pus, prm)
     assert outs[0] == exp.tobytes()
+
+
+def test_headline_1080p_sample(gpu, olib):
+    """The benchmark's own workload at its own size: 1920x1080, 2 references,
+    FS +-64, quarter-pel SATD at QP 32, every PU of the CTU layout searched
+    on the GPU; checked against the oracle on a seeded sample of about 3,000
+    PU searches made of every PU of six CTUs at the picture's corners and
+    bottom edge (the partial 56-row CTU row) plus a random draw over the
+    rest."""
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    W, H, R = 1920, 1080, 64
+    cur, refs = synth.me_workload(seed=1, width=W, height=H)
+    pus = xg.frame_pus(W, H, 2)
+    prm = xg.MeParams(R, oracle.lambda_factor(32), 1, 2, 0, 0)
+    got, stats = _run(cur, refs, pus, prm)
+    assert stats[0] == len(pus) and stats[1] == 0, stats
+    ctu = (pus["x"] // 64).astype(int) * 1000 + (pus["y"] // 64).astype(int)
+    corners = [(0, 0), (29, 0), (0, 16), (29, 16), (14, 16), (15, 8)]
+    edge = np.isin(ctu, [cx * 1000 + cy for cx, cy in corners])
+    rng = np.random.default_rng(1080)
+    rest = np.flatnonzero(~edge)
+    idx = np.sort(np.concatenate([np.flatnonzero(edge), rng.choice(rest, 1500, replace=False)]))
+    assert (pus["y"][idx] >= 1024).any() and (pus["x"][idx] >= 1856).any()
+    sel = np.ascontiguousarray(pus[idx])
+    exp = _oracle(olib, cur, refs, sel, prm, threads=os.cpu_count() or 1)
+    _assert_same(np.ascontiguousarray(got[idx]), exp, sel)

@@ -1025,8 +1025,12 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     const int nplanes = 1 + 16 * num_refs;
     XG_CUDA(cudaStreamCreateWithFlags(&m.own_st, cudaStreamNonBlocking));
     m.st = m.own_st;
-    XG_CUDA(cudaMalloc((void **)&m.d_planes, m.plane_bytes * nplanes));
-    XG_CUDA(cudaMemsetAsync(m.d_planes, 0, m.plane_bytes * nplanes, m.st));
+    // 256 bytes of slack after the last plane: word-wise row readers (the skip
+    // costs' 3-word prediction rows) may touch the aligned word after a row
+    // that ends at the right edge of the margin, which lies past the last
+    // plane when its size is already a multiple of 256.
+    XG_CUDA(cudaMalloc((void **)&m.d_planes, m.plane_bytes * nplanes + 256));
+    XG_CUDA(cudaMemsetAsync(m.d_planes, 0, m.plane_bytes * nplanes + 256, m.st));
     std::vector<uint8_t *> ptrs(nplanes);
     for (int k = 0; k < nplanes; k++) ptrs[k] = m.plane(k);
     XG_CUDA(cudaMalloc((void **)&m.d_plane_ptrs, sizeof(uint8_t *) * nplanes));
@@ -1322,7 +1326,8 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     ctu_jobs_run(m.plan.d_jobs, m.plan.n_jobs, m.plan.n_border, m.d_view, *prm, m.st);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
     if (m.n_generic) {
-        int grid = m.n_generic < 152 * 8 ? m.n_generic : 152 * 8;
+        const int cap = sm_count() * 8;
+        int grid = m.n_generic < cap ? m.n_generic : cap;
         fs_generic_kernel<<<grid, 256, 0, m.st>>>(gen, m.n_generic, m.d_view, R, lam);
         count_launch();
     }
@@ -1719,7 +1724,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     if (bg) XG_CUDA(cudaMemcpyAsync(bb.d_groups, bb.h_stage + og, bg, cudaMemcpyHostToDevice, st));
     const uint32_t *d_gen = bb.d_lists, *d_small = bb.d_lists + ng, *d_large = bb.d_lists + ng + ns;
     const uint32_t *d_members = bb.d_lists + ng + ns + nl;
-    reset_keys_kernel<<<152 * 4, 256, 0, st>>>(bb.d_views, n);
+    reset_keys_kernel<<<sm_count() * 4, 256, 0, st>>>(bb.d_views, n);
     count_launch();
     if (ng) {
         me_init_list_kernel<<<(unsigned)((ng * 32 + 127) / 128), 128, 0, st>>>(d_gen, (int)ng, bb.d_views, lam);
@@ -1727,7 +1732,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     }
     ctu_jobs_run(bb.d_jobs, (int)nj, nborder, bb.d_views, *prm, st);
     if (ng) {
-        fs_generic_kernel<<<(unsigned)(ng < 152 * 8 ? ng : 152 * 8), 256, 0, st>>>(d_gen, (int)ng, bb.d_views, R, lam);
+        fs_generic_kernel<<<(unsigned)(ng < (size_t)sm_count() * 8 ? ng : (size_t)sm_count() * 8), 256, 0, st>>>(d_gen, (int)ng, bb.d_views, R, lam);
         count_launch();
     }
     if (ngr) launch_groups(bb.d_groups, (int)ngr, d_members, bb.d_views, R, *prm, st);
@@ -1803,7 +1808,7 @@ __global__ void noalloc_prepare_kernel(const xavs2gpu_pu_t *__restrict__ in, int
     }
     if (i >= n) return;
     xavs2gpu_pu_t p = in[i];
-    bool ok = p.part < kNumParts && p.ref < nrefs;
+    bool ok = (unsigned)p.part < (unsigned)kNumParts && (unsigned)p.ref < (unsigned)nrefs;
     if (ok) {
         const int w = c_pu_w[p.part], h = c_pu_h[p.part];
         ok = p.x >= 0 && p.y >= 0 && p.x + w <= W && p.y + h <= H && p.min_x >= -kPad + 8 - p.x &&
@@ -1821,13 +1826,19 @@ __global__ void noalloc_prepare_kernel(const xavs2gpu_pu_t *__restrict__ in, int
     s->list[i] = i;
 }
 
+constexpr int kNoAllocMaxDevices = 64;
 static std::mutex g_noalloc_mu;
-static NoAllocScratch *g_noalloc_addr[64] = {nullptr};
+static NoAllocScratch *g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
 
 // Device address of the scratch array on `dev` (the current device), looked
-// up once per device.
+// up once per device.  The cached address stays valid until the device is
+// reset (cudaDeviceReset); the library is not meant to outlive a reset.
 static NoAllocScratch *noalloc_scratch(int dev)
 {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_search_noalloc", "device ordinal beyond the 64 the scratch table covers");
+        return nullptr;
+    }
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (!g_noalloc_addr[dev]) {
         void *ptr = nullptr;
@@ -1872,13 +1883,13 @@ extern "C" int xavs2gpu_me_search_noalloc(const uint8_t *cur, int stride, int wi
     int dev = 0;
     XG_CUDA(cudaGetDevice(&dev));
     NoAllocScratch *s = noalloc_scratch(dev);
-    if (!s) return XAVS2GPU_ERR_CUDA;
+    if (!s) return xavs2gpu_get_status();
     cudaStream_t st = (cudaStream_t)stream;
     const Geometry g{width, height, stride};
     const int R = prm->search_range, lam = prm->lambda_factor;
     noalloc_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(pus, n, s, t, num_refs, width, height, cur, stride, out);
     me_init_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, cur, s->ref0, g, lam, s->state, s->keys);
-    const int grid = n < 152 * 8 ? n : 152 * 8;
+    const int grid = n < sm_count() * 8 ? n : sm_count() * 8;
     fs_generic_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint32_t *>(s->list), n, &s->view, R, lam);
     refine_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, s->state, s->keys, cur, s->planes, g, R, *prm,
                                                         out);

@@ -40,6 +40,19 @@ void check_cuda(cudaError_t e, const char *where)
 
 int current_device() { return t_device; }
 
+int sm_count()
+{
+    static int sms[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!sms[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+        sms[dev] = n;
+    }
+    return sms[dev];
+}
+
 // One context per (thread, device).  Buffers grow on demand and live until
 // thread exit.
 struct CtxHolder {

@@ -47,6 +47,8 @@ struct CallCtx {
 };
 CallCtx &call_ctx(size_t need_bytes);
 int current_device();
+// Number of SMs of the current device (queried once per device).
+int sm_count();
 
 // Byte offset rounded up to 256 for staging sub-buffers.
 static inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
