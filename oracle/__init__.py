@@ -70,7 +70,7 @@ def build(with_ref=None):
         with_ref = os.path.isdir(REF_SRC)
     if with_ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, "REF_SRC=" + REF_SRC] + targets, check=True)
+    subprocess.run(["make", "-s", "-j4", "-C", HERE, "REF_SRC=" + REF_SRC] + targets, check=True)
 
 
 _oracle = None

@@ -59,6 +59,46 @@ def next_picture(rng, prev, n_motions=1, max_px=8, block=8, noise=2.0):
     return np.clip(np.round(out), 0, 255).astype(np.uint8)
 
 
+_CTAPS = np.array([[0, 64, 0, 0], [-4, 62, 6, 0], [-6, 56, 15, -1], [-5, 47, 25, -3],
+                   [-4, 36, 36, -4], [-3, 25, 47, -5], [-1, 15, 56, -6], [0, 6, 62, -4]], np.float64)
+
+
+def shift_eighth_chroma(img, mvx, mvy):
+    """A chroma plane displaced by (mvx, mvy) eighth-pels with the AVS2
+    4-tap chroma filter (the luma motion in quarter-pels at half size)."""
+    h, w = img.shape
+    ix, fx = mvx >> 3, mvx & 7
+    iy, fy = mvy >> 3, mvy & 7
+    pad = 2 + max(abs(ix), abs(iy))
+    p = np.pad(img.astype(np.float64), pad, mode="edge")
+    ys = np.arange(h) + pad + iy
+    xs = np.arange(w) + pad + ix
+    rows = p[ys[0] - 1:ys[-1] + 3]
+    hor = sum(_CTAPS[fx][k] * rows[:, xs[0] - 1 + k:xs[-1] - 1 + k + 1] for k in range(4)) / 64.0
+    out = sum(_CTAPS[fy][k] * hor[k:k + h] for k in range(4)) / 64.0
+    return np.clip(np.round(out), 0, 255)
+
+
+def config0_sequence(n=8, width=416, height=240, seed=0, max_px=8, noise=2.0):
+    """The plain-encoder sequence: n 4:2:0 pictures (Y, U, V).  Picture 0 is
+    blurred noise rescaled to [16, 235] (chroma likewise at half size); each
+    later picture is the previous one moved by one translation U[-8, 8] px
+    per axis in quarter-pel steps (AVS2 8-tap luma, 4-tap chroma at the same
+    displacement), plus Gaussian noise, clipped."""
+    rng = np.random.default_rng(seed)
+    y = base_picture(rng, width, height)
+    u = base_picture(rng, width // 2, height // 2)
+    v = base_picture(rng, width // 2, height // 2)
+    seq = [(y, u, v)]
+    for _ in range(n - 1):
+        mvx, mvy = (int(m) for m in rng.integers(-max_px * 4, max_px * 4 + 1, 2))
+        y = np.clip(np.round(shift_qpel(y, mvx, mvy) + rng.normal(0.0, noise, y.shape)), 0, 255).astype(np.uint8)
+        u, v = (np.clip(np.round(shift_eighth_chroma(c, mvx, mvy) + rng.normal(0.0, noise, c.shape)), 0, 255)
+                .astype(np.uint8) for c in (u, v))
+        seq.append((y, u, v))
+    return seq
+
+
 def me_workload(seed=1, width=1920, height=1080, n_motions=16, max_px=32):
     """Current picture and two references (k-1, k-2) for the batched
     motion-search benchmark: 16 block-local motions U[-32, 32] px in
