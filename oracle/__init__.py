@@ -154,6 +154,7 @@ _REF_SIGS = {
     "xr_dequant": (None, [_P, _I, _I, _I]), "xr_abs_coeff": (None, [_P, _P, _I]),
     "xr_add_sign": (_I, [_P, _P, _I]),
     "xr_me_search": (_I, [_P, _P, _P, _S, _P, _I, _P]),
+    "xr_me_search_list": (None, [_P, _P, _I, _P, _S, _P, _I, _P, _I]),
     "xr_intra_pred": (None, [_I, _P, _P, _I, _I, _I, _I]),
     "xr_intra_fill_edge": (None, [_I, _P, _I, _P, _P, ctypes.c_uint32, _I, _I]),
     "xr_deblock_luma": (None, [_I, _P, _I, _I, _I, _P]),

@@ -352,6 +352,25 @@ int32_t xr_me_search(const xr_me_params_t *prm, const xr_pu_t *pu, const pel_t *
     return cost;
 }
 
+/* xr_me_search over a PU list (frefs: 16 planes per reference), on
+ * `threads` OpenMP threads, in the same loop form as the oracle's
+ * xo_me_search_list, so that the two can be timed side by side.  xr_init
+ * runs first on this thread: it fills the shared table once. */
+void xr_me_search_list(const xr_me_params_t *prm, const xr_pu_t *pus, int n, const pel_t *fenc, intptr_t i_fenc,
+                       pel_t *const *frefs, int i_fref, xr_me_result_t *out, int threads)
+{
+    int i;
+    xr_init();
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads > 0 ? threads : 1)
+#endif
+    for (i = 0; i < n; i++) {
+        const xr_pu_t *pu = &pus[i];
+        xr_me_search(prm, pu, fenc + pu->y * i_fenc + pu->x, i_fenc, frefs + 16 * pu->ref, i_fref, &out[i]);
+    }
+    (void)threads;
+}
+
 int xr_mvbits(int d)
 {
     static xavs2_t *h = NULL;

@@ -57,9 +57,38 @@ static int32_t sad_wh(const uint8_t *a, intptr_t sa, const uint8_t *b, intptr_t 
     return s;
 }
 
+/* One SAD function per shape with the block size a compile-time constant,
+ * as the reference instantiates them (PIXEL_SAD_C, pixel.c:93-135), so that
+ * the compiler unrolls and vectorises the rows: the CPU baseline times this
+ * port on hosts where the reference build is absent, and it must run at the
+ * reference C's speed. */
+#define SAD_FIXED(W, H)                                                                          \
+    static int32_t sad_##W##x##H(const uint8_t *a, intptr_t sa, const uint8_t *b, intptr_t sb)   \
+    {                                                                                            \
+        int32_t s = 0;                                                                           \
+        for (int y = 0; y < H; y++, a += sa, b += sb)                                            \
+            for (int x = 0; x < W; x += 4) {                                                     \
+                s += abs(a[x] - b[x]);                                                           \
+                s += abs(a[x + 1] - b[x + 1]);                                                   \
+                s += abs(a[x + 2] - b[x + 2]);                                                   \
+                s += abs(a[x + 3] - b[x + 3]);                                                   \
+            }                                                                                    \
+        return s;                                                                                \
+    }
+SAD_FIXED(4, 4) SAD_FIXED(8, 8) SAD_FIXED(16, 16) SAD_FIXED(32, 32) SAD_FIXED(64, 64)
+SAD_FIXED(8, 4) SAD_FIXED(4, 8) SAD_FIXED(16, 8) SAD_FIXED(8, 16) SAD_FIXED(32, 16) SAD_FIXED(16, 32)
+SAD_FIXED(64, 32) SAD_FIXED(32, 64) SAD_FIXED(16, 12) SAD_FIXED(12, 16) SAD_FIXED(16, 4) SAD_FIXED(4, 16)
+SAD_FIXED(32, 24) SAD_FIXED(24, 32) SAD_FIXED(32, 8) SAD_FIXED(8, 32) SAD_FIXED(64, 48) SAD_FIXED(48, 64)
+SAD_FIXED(64, 16) SAD_FIXED(16, 64)
+typedef int32_t (*sad_fn_t)(const uint8_t *, intptr_t, const uint8_t *, intptr_t);
+static const sad_fn_t k_sad_fn[25] = {
+    sad_4x4, sad_8x8, sad_16x16, sad_32x32, sad_64x64, sad_8x4, sad_4x8, sad_16x8, sad_8x16,
+    sad_32x16, sad_16x32, sad_64x32, sad_32x64, sad_16x12, sad_12x16, sad_16x4, sad_4x16,
+    sad_32x24, sad_24x32, sad_32x8, sad_8x32, sad_64x48, sad_48x64, sad_64x16, sad_16x64};
+
 int32_t xo_sad(int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2)
 {
-    return sad_wh(p1, s1, p2, s2, k_pu_w[part], k_pu_h[part]);
+    return k_sad_fn[part](p1, s1, p2, s2);
 }
 
 /* sad_x3 / sad_x4: the encode block always has stride FENC_STRIDE = 64
@@ -936,10 +965,8 @@ void xo_tq_batch(const xo_tq_block_t *blocks, int n, const int16_t *residual, in
  * 2*bitlen(|d|) + 1 */
 int xo_mvbits(int d)
 {
-    int a = iabs(d), bl = 0;
-    if (a == 0) return 1;
-    while (a) { bl++; a >>= 1; }
-    return 2 * bl + 1;
+    const unsigned a = (unsigned)iabs(d);
+    return a ? 2 * (32 - __builtin_clz(a)) + 1 : 1;   /* 2 * bit length + 1 */
 }
 
 static inline int32_t mv_cost(int lambda, int mvx, int mvy, int pmx, int pmy)
@@ -1013,15 +1040,24 @@ int32_t xo_me_search(const xo_me_params_t *prm, const xo_pu_t *pu, const uint8_t
     /* full search, j outer, i inner, first strictly smaller cost wins
      * (me.c:1156-1164) */
     omx = bmx; omy = bmy;
-    for (j = -prm->search_range; j < prm->search_range; j++)
-        for (i = -prm->search_range; i < prm->search_range; i++) {
-            int mx = omx + i, my = omy + j;
-            if (in_box(pu, mx, my)) {
-                int32_t cost = xo_sad(part, fenc, i_fenc, ref0 + my * i_fref + mx, i_fref) +
-                               mv_cost(lam, mx * 4, my * 4, pmx, pmy);
+    {
+        /* the window clipped to the limits (the positions outside are
+         * skipped in the reference's loop), the vertical MV bits hoisted */
+        const sad_fn_t sad = k_sad_fn[part];
+        const int R = prm->search_range;
+        const int j0 = pu->min_y - omy > -R ? pu->min_y - omy : -R, j1 = pu->max_y - omy < R - 1 ? pu->max_y - omy : R - 1;
+        const int i0 = pu->min_x - omx > -R ? pu->min_x - omx : -R, i1 = pu->max_x - omx < R - 1 ? pu->max_x - omx : R - 1;
+        for (j = j0; j <= j1; j++) {
+            const int my = omy + j, by = xo_mvbits(my * 4 - pmy);
+            const uint8_t *row = ref0 + my * i_fref;
+            for (i = i0; i <= i1; i++) {
+                const int mx = omx + i;
+                const int32_t cost = sad(fenc, i_fenc, row + mx, i_fref) +
+                                     (int32_t)(((int64_t)lam * (xo_mvbits(mx * 4 - pmx) + by)) >> 16);
                 if (cost < bcost) { bcost = cost; bmx = mx; bmy = my; }
             }
         }
+    }
     out->imv_x = (int16_t)bmx; out->imv_y = (int16_t)bmy;
     out->icost = bcost;
     out->bmv_x = (int16_t)(bmx * 4); out->bmv_y = (int16_t)(bmy * 4);

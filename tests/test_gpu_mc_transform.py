@@ -63,7 +63,7 @@ def test_intpl_dropins(gpu, olib):
                 assert np.array_equal(d1, d2), (kind, fx, fy)
 
 
-@pytest.mark.parametrize("w,h", [(136, 72), (64, 8), (200, 120)])
+@pytest.mark.parametrize("w,h", [(136, 72), (64, 8), (200, 120), (416, 240), (330, 190), (1920, 1080)])
 def test_frame_planes(gpu, olib, w, h):
     """The 15 sub-pel planes (with their 80-pixel replicated margin) computed
     on the device when a reference picture is loaded."""
@@ -77,6 +77,40 @@ def test_frame_planes(gpu, olib, w, h):
     for k in range(16):
         assert np.array_equal(s.get_plane(0, k), exp[k]), k
     s.close()
+
+
+@pytest.mark.parametrize("w,h,pad,extra,mode", [(300, 170, 9, 3, 2), (256, 128, 12, 0, 1), (97, 61, 8, 1, 2)])
+def test_interpolate_frame_api(gpu, olib, w, h, pad, extra, mode):
+    """xavs2gpu_interpolate_frame on device buffers with other margins,
+    strides that are not multiples of 4 (byte stores, byte source loads)
+    and the half-pel-only mode: every requested plane equals the oracle's
+    over the whole padded area; planes not requested stay untouched."""
+    import ctypes
+    import torch
+    import xavs2_gb300 as xg
+    lib = xg.load()
+    rng = np.random.default_rng(w * h + pad)
+    img = rng.integers(0, 256, (h, w), dtype=np.uint8)
+    exp = oracle.interpolate_frame(olib, img, mode=2)      # 80-pixel margins
+    stride = w + 2 * pad + extra
+    rows = h + 2 * pad
+    src = np.zeros((rows, stride), np.uint8)
+    src[:, :w + 2 * pad] = exp[0][80 - pad:80 + h + pad, 80 - pad:80 + w + pad]
+    d_src = torch.from_numpy(src.reshape(-1).copy()).cuda()
+    d_planes = torch.full((16, rows * stride + 16), 0x5A, dtype=torch.uint8, device="cuda")
+    org = pad * stride + pad
+    off = 1 if extra else 0          # misaligned planes where the stride is odd anyway
+    ptrs = (ctypes.c_void_p * 16)(*[d_planes[k].data_ptr() + off + org for k in range(16)])
+    rc = lib.xavs2gpu_interpolate_frame(ctypes.c_void_p(d_src.data_ptr() + org), stride, w, h, pad, ptrs, mode, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    got = d_planes.cpu().numpy()
+    for k in range(1, 16):
+        plane = got[k][off:off + rows * stride].reshape(rows, stride)[:, :w + 2 * pad]
+        if mode == 2 or k in (2, 8, 10):
+            assert np.array_equal(plane, exp[k][80 - pad:80 + h + pad, 80 - pad:80 + w + pad]), k
+        else:
+            assert (plane == 0x5A).all(), k
 
 
 @pytest.mark.parametrize("part", TU_PARTS)

@@ -120,34 +120,10 @@ static inline int nblocks(int n, int t = 256) { int b = (n + t - 1) / t; return 
 // clamped into the picture: the reference filters rows [-4, H+4) x columns
 // [-4, W+4) and replicates that region outwards.  One kernel writes the
 // whole padded plane directly, so the replication costs no extra pass.
-__constant__ int8_t c_luma_taps[4][8] = {
-    {0, 0, 0, 64, 0, 0, 0, 0},
-    {-1, 4, -10, 57, 19, -7, 3, -1},
-    {-1, 4, -11, 40, 40, -11, 4, -1},
-    {-1, 3, -7, 19, 57, -10, 4, -1},
-};
-
-// The three sub-pel phases of one axis from the 8 samples v[0..7] around a
-// position.  The AVS2 taps are symmetric (half-pel) and mirror images of
-// each other (quarter-pels: t3[k] = t1[7-k]), so with a_k = v[k] + v[7-k] and
-// d_k = v[k] - v[7-k]:
-//   p2      = -a0 + 4 a1 - 11 a2 + 40 a3
-//   2 p1    = S + D,  2 p3 = S - D,
-//   S = -2 a0 + 7 a1 - 17 a2 + 76 a3,  D = d1 - 3 d2 + 38 d3
-// (exactly the 8-tap sums; 11 multiply-adds for the three phases instead
-// of 24).  Returned: p2 and the doubled quarter-pel sums 2 p1, 2 p3.
-__device__ __forceinline__ void phases3(const int (&v)[8], int &p2, int &p1x2, int &p3x2)
-{
-    const int a0 = v[0] + v[7], a1 = v[1] + v[6], a2 = v[2] + v[5], a3 = v[3] + v[4];
-    const int d1 = v[1] - v[6], d2 = v[2] - v[5], d3 = v[3] - v[4];
-    p2 = -a0 + 4 * a1 - 11 * a2 + 40 * a3;
-    const int S = -2 * a0 + 7 * a1 - 17 * a2 + 76 * a3, D = d1 - 3 * d2 + 38 * d3;
-    p1x2 = S + D;
-    p3x2 = S - D;
-}
-
 constexpr int PT_W = 128, PT_H = 16;            // output tile of a padded plane
-constexpr int PS_R = PT_H + 7, PS_C = PT_W + 16; // source window (rows, pitch)
+constexpr int PS_R = PT_H + 7;                  // source rows a tile reads (23)
+constexpr int PS_C = PT_W + 16;                 // source bytes per row, padded (144)
+constexpr int PP_R = PT_H + 6;                  // row pairs of the vertical pass (22)
 
 struct PlaneSet { uint8_t *p[16]; };
 
@@ -167,164 +143,231 @@ __device__ __forceinline__ void store_group(uint8_t *p, uint32_t v, int x, int e
         if (x + i < end_col) p[i] = (uint8_t)(v >> (8 * i));
 }
 
-// Phase 3 of frame_planes_kernel for one horizontal phase FX: the 4-column
-// group g of output rows [y0 + 8*half, y0 + 8*half + 8).
-template <int FX, bool VEC>
-__device__ __forceinline__ void planes_rows(const uint8_t (*s_src)[PS_C], const int16_t (*s_hor)[PS_R][PT_W],
-                                            const PlaneSet &planes, int stride, int W, int H, int pad, int x0,
-                                            int y0, int cx0, int cy0, int g, int half, int mode)
+// Four unsigned bytes of a times four signed bytes of b, plus c.
+__device__ __forceinline__ int dp4a_us(uint32_t a, uint32_t b, int c)
 {
-    const int xg = x0 + 4 * g;
-    const int end_col = W + pad;
-    if (xg >= end_col) return;
-    int lc[4];
-    bool contiguous = true;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        lc[c] = clampi(xg + c, -4, W + 3) - cx0;
-        contiguous &= lc[c] == 4 * g + c;
-    }
-    // window element (row j, column c): the source byte at column lc+3 for
-    // FX == 0, else the raw horizontal sum of phase FX
-    auto fetch = [&](int row, int (&dst)[4]) {
-        if (FX == 0) {
-#pragma unroll
-            for (int c = 0; c < 4; c++) dst[c] = s_src[row][lc[c] + 3];
-        } else if (contiguous) {
-            const uint2 pk = *reinterpret_cast<const uint2 *>(&s_hor[FX - 1][row][4 * g]);
-            dst[0] = (int16_t)(pk.x & 0xFFFF); dst[1] = (int16_t)(pk.x >> 16);
-            dst[2] = (int16_t)(pk.y & 0xFFFF); dst[3] = (int16_t)(pk.y >> 16);
-        } else {
-#pragma unroll
-            for (int c = 0; c < 4; c++) dst[c] = s_hor[FX - 1][row][lc[c]];
-        }
-    };
-    const int ys = y0 + 8 * half;
-    int cur = clampi(ys, -4, H + 3) - cy0;
-    int win[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; j++) fetch(cur + j, win[j]);
-    uint32_t out[4] = {0, 0, 0, 0};
-    bool have = false;
-    // rolled: the body is the whole per-row filter, and the four phases' code
-    // must stay small enough for the instruction cache
-#pragma unroll 1
-    for (int t = 0; t < 8; t++) {
-        const int y = ys + t;
-        if (y >= H + pad) break;
-        const int l = clampi(y, -4, H + 3) - cy0;
-        if (l != cur) {
-#pragma unroll
-            for (int j = 0; j < 7; j++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) win[j][c] = win[j + 1][c];
-            fetch(l + 7, win[7]);
-            cur = l;
-            have = false;
-        }
-        if (!have) {
-            // rounding: fx = 0 (bytes) (s + 32) >> 6, else (s + 2048) >> 12;
-            // the quarter-pel sums come doubled, one more shift
-            constexpr int SH = FX == 0 ? 6 : 12;
-            uint32_t pk[4] = {0, 0, 0, 0};
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                int v[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = win[j][c];
-                int p2, p1x2, p3x2;
-                phases3(v, p2, p1x2, p3x2);
-                const int q0 = (win[3][c] + 32) >> 6;
-                const int q1 = (p1x2 + (1 << SH)) >> (SH + 1);
-                const int q2 = (p2 + (1 << (SH - 1))) >> SH;
-                const int q3 = (p3x2 + (1 << SH)) >> (SH + 1);
-                pk[0] |= (uint32_t)clip_pel_d(q0) << (8 * c);
-                pk[1] |= (uint32_t)clip_pel_d(q1) << (8 * c);
-                pk[2] |= (uint32_t)clip_pel_d(q2) << (8 * c);
-                pk[3] |= (uint32_t)clip_pel_d(q3) << (8 * c);
-            }
-#pragma unroll
-            for (int fy = 0; fy < 4; fy++) out[fy] = pk[fy];
-            have = true;
-        }
-        const ptrdiff_t ro = (ptrdiff_t)y * stride + xg;
-#pragma unroll
-        for (int fy = 0; fy < 4; fy++) {
-            if (FX == 0 && fy == 0) continue;
-            if (mode < 2 && fy != 0 && fy != 2) continue;
-            store_group<VEC>(planes.p[4 * fy + FX] + ro, out[fy], xg, end_col);
-        }
-    }
+    int d;
+    asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+// The two signed 16-bit halves of a times signed bytes 0, 1 (lo) or 2, 3 (hi)
+// of b, plus c.
+__device__ __forceinline__ int dp2a_lo(uint32_t a, uint32_t b, int c)
+{
+    int d;
+    asm("dp2a.lo.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+__device__ __forceinline__ int dp2a_hi(uint32_t a, uint32_t b, int c)
+{
+    int d;
+    asm("dp2a.hi.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+// x0..x3 clipped to [0, 255] and packed, x0 in the lowest byte.
+__device__ __forceinline__ uint32_t pack_sat_u8(int x0, int x1, int x2, int x3)
+{
+    uint32_t t, d;
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, 0;" : "=r"(t) : "r"(x3), "r"(x2));
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(x1), "r"(x0), "r"(t));
+    return d;
+}
+
+// The AVS2 luma taps (mc.c:73-78) as packed signed bytes: half 0 holds
+// taps 0..3, half 1 taps 4..7.  Phase 0 is the full-pel position (only
+// tap 3 = 64).
+__host__ __device__ constexpr uint32_t pk4(int a, int b, int c, int d)
+{
+    return (uint32_t)(a & 255) | (uint32_t)(b & 255) << 8 | (uint32_t)(c & 255) << 16 | (uint32_t)(d & 255) << 24;
+}
+__host__ __device__ constexpr uint32_t tap_word(int phase, int half)
+{
+    return phase == 0 ? (half ? pk4(0, 0, 0, 0) : pk4(0, 0, 0, 64))
+         : phase == 1 ? (half ? pk4(19, -7, 3, -1) : pk4(-1, 4, -10, 57))
+         : phase == 2 ? (half ? pk4(40, -11, 4, -1) : pk4(-1, 4, -11, 40))
+                      : (half ? pk4(57, -10, 4, -1) : pk4(-1, 3, -7, 19));
+}
+
+// Vertical 8-tap sum at one column from the four row pairs (h[l], h[l+1]),
+// (h[l+2], h[l+3]), (h[l+4], h[l+5]), (h[l+6], h[l+7]) packed as int16 halves.
+__device__ __forceinline__ int vsum(uint32_t a, uint32_t b, uint32_t c, uint32_t d, uint32_t t03, uint32_t t47,
+                                    int init)
+{
+    return dp2a_hi(d, t47, dp2a_lo(c, t47, dp2a_hi(b, t03, dp2a_lo(a, t03, init))));
+}
+
+// The four columns of one row pair (x..w) from shared memory: one 16-byte load
+// when the columns are contiguous and aligned, else one load per column.
+__device__ __forceinline__ uint4 load_pairs(const uint32_t *row, const int (&lc)[4], bool vec)
+{
+    if (vec) return *reinterpret_cast<const uint4 *>(row + lc[0]);
+    return make_uint4(row[lc[0]], row[lc[1]], row[lc[2]], row[lc[3]]);
 }
 
 // One CTA writes a 128 x 16 tile of every requested sub-pel plane over the
 // whole padded area [-pad, W+pad) x [-pad, H+pad).  The sample at (x, y) is
-// the filter output at (cx, cy) = (clamp(x, -4, W+3), clamp(y, -4, H+3)), so
-// the tile only needs the clamped columns [cx(x0), cx(x0+127)] and rows
-// [cy(y0), cy(y0+15)] (at most 128 x 16 distinct values).
-//   phase 1: source window (clamped reads) -> shared memory;
-//   phase 2: raw horizontal 8-tap sums for fx = 1..3, 4 columns per item;
-//   phase 3: thread = (row half, fx, 4-column group): slides an 8-row window
-//            down its 8 output rows and emits planes 4*fy + fx for fy = 0..3
-//            as 32-bit stores (a warp writes 128 contiguous bytes of a row).
-// resident 256-thread CTAs per SM the register budget is sized for
+// the filter output at (cx, cy) = (clamp(x, -4, W+3), clamp(y, -4, H+3)) (the
+// reference filters [-4, W+4) x [-4, H+4) and replicates that region
+// outwards), so a tile needs the filter at the clamped columns cx0 + [0, 128)
+// and rows cy0 + [0, nL), nL <= 16 distinct clamped rows.
+//   1: the source window, 23 rows x 135 bytes, into shared memory (word loads
+//      away from the picture edge, clamped byte loads near it);
+//   2: the raw horizontal 8-tap sums of the three sub-pel phases (two byte
+//      dot products each) and the source bytes themselves, stored as row
+//      pairs (h[s], h[s+1]) of int16 for s = 0..21: thread = (4 columns,
+//      3 rows of pairs);
+//   3: thread = (horizontal phase fx, 4 columns, 8 rows): every vertical
+//      phase of a row is four 16-bit pair dot products on the pairs, the
+//      rounding (+32 >> 6 on bytes, +2048 >> 12 on raw sums) is one shift,
+//      and four samples are clipped and packed by two saturating packs; the
+//      row is stored to every output row that clamps to it (the top and
+//      bottom margins repeat rows -4 and H+3) as 32-bit stores, a warp
+//      writing 128 contiguous bytes of a plane row.
 #ifndef XG_PLANES_MINB
-#define XG_PLANES_MINB 3
+#define XG_PLANES_MINB 4
 #endif
 
 template <bool VEC>
 __global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const uint8_t *__restrict__ src, int stride, int W, int H,
-                                                           int pad, PlaneSet planes, int mode)
+                                                           int pad, PlaneSet planes, int mode, int src_words)
 {
     __shared__ __align__(16) uint8_t s_src[PS_R][PS_C];
-    __shared__ __align__(16) int16_t s_hor[3][PS_R][PT_W];
+    __shared__ __align__(16) uint32_t s_pair[4][PP_R][PT_W];
     const int x0 = -pad + blockIdx.x * PT_W, y0 = -pad + blockIdx.y * PT_H;
     const int cx0 = clampi(x0, -4, W + 3), cy0 = clampi(y0, -4, H + 3);
+    const int nL = clampi(y0 + PT_H - 1, -4, H + 3) - cy0 + 1;
     const int tid = threadIdx.x;
-    for (int i = tid; i < PS_R * (PT_W + 8); i += 256) {
-        const int r = i / (PT_W + 8), m = i - r * (PT_W + 8);
-        const int sy = clampi(cy0 - 3 + r, 0, H - 1), sx = clampi(cx0 - 3 + m, 0, W - 1);
-        s_src[r][m] = src[(ptrdiff_t)sy * stride + sx];
-    }
-    __syncthreads();
-    for (int i = tid; i < PS_R * (PT_W / 4); i += 256) {
-        const int r = i / (PT_W / 4), g = i - r * (PT_W / 4);
-        const uint32_t *w = reinterpret_cast<const uint32_t *>(&s_src[r][4 * g]);
-        int b[12];
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-            const uint32_t v = w[q];
-#pragma unroll
-            for (int e = 0; e < 4; e++) b[4 * q + e] = (v >> (8 * e)) & 0xFF;
+    // ---- 1: source window: s_src[r][m] = src(cy0 - 3 + r, cx0 - 3 + m) for
+    // m < 136 (words 0..33; the filters read bytes 0..134).  Word loads (src
+    // and stride 4-byte aligned) only where every byte they touch, up to
+    // column cx0 + 136, lies inside the picture.
+    constexpr int kWords = (PT_W + 8) / 4;
+    const bool inner = src_words && cx0 - 6 >= 0 && cx0 + PT_W + 12 <= W && cy0 - 3 >= 0 && cy0 + PT_H + 4 <= H;
+    if (inner) {
+        const int xa = cx0 - 3, sh = 8 * (xa & 3);
+        for (int i = tid; i < PS_R * kWords; i += 256) {
+            const int r = i / kWords, q = i - r * kWords;
+            const uint32_t *p =
+                reinterpret_cast<const uint32_t *>(src + (ptrdiff_t)(cy0 - 3 + r) * stride + ((xa + 4 * q) & ~3));
+            const uint32_t lo = __ldg(p), hi = sh ? __ldg(p + 1) : 0u;
+            *reinterpret_cast<uint32_t *>(&s_src[r][4 * q]) = __funnelshift_r(lo, hi, sh);
         }
-        int o[3][4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            int v[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++) v[k] = b[c + k];
-            int p2, p1x2, p3x2;
-            phases3(v, p2, p1x2, p3x2);
-            o[0][c] = p1x2 >> 1;
-            o[1][c] = p2;
-            o[2][c] = p3x2 >> 1;
-        }
-#pragma unroll
-        for (int f = 0; f < 3; f++) {
-            if (mode < 2 && f != 1) continue;
-            uint2 pk;
-            pk.x = (uint32_t)(o[f][0] & 0xFFFF) | ((uint32_t)o[f][1] << 16);
-            pk.y = (uint32_t)(o[f][2] & 0xFFFF) | ((uint32_t)o[f][3] << 16);
-            *reinterpret_cast<uint2 *>(&s_hor[f][r][4 * g]) = pk;
+    } else {
+        for (int i = tid; i < PS_R * PS_C; i += 256) {
+            const int r = i / PS_C, m = i - r * PS_C;
+            const int sy = clampi(cy0 - 3 + r, 0, H - 1), sx = clampi(cx0 - 3 + m, 0, W - 1);
+            s_src[r][m] = src[(ptrdiff_t)sy * stride + sx];
         }
     }
     __syncthreads();
+    // ---- 2: horizontal phases as row pairs
+    {
+        const int g = tid & 31, seg = tid >> 5;
+        const int r0 = 3 * seg, r1 = min(r0 + 3, PS_R - 1);
+        uint32_t prev[4][4] = {};
+        for (int r = r0; r <= r1; r++) {
+            const uint32_t *w = reinterpret_cast<const uint32_t *>(&s_src[r][0]);
+            const uint32_t w0 = w[g], w1 = w[g + 1], w2 = w[g + 2];
+            uint32_t cur[4][4];
+            const uint32_t ctr = __funnelshift_r(w0, w1, 24);   // the centre bytes (tap 3) of the 4 columns
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint32_t lo = __funnelshift_r(w0, w1, 8 * j), hi = __funnelshift_r(w1, w2, 8 * j);
+#pragma unroll
+                for (int f = 1; f < 4; f++) cur[f][j] = (uint32_t)dp4a_us(hi, tap_word(f, 1), dp4a_us(lo, tap_word(f, 0), 0));
+                cur[0][j] = (ctr >> (8 * j)) & 0xFFu;
+            }
+            if (r > r0) {
+                const int s = r - 1;
+#pragma unroll
+                for (int f = 0; f < 4; f++) {
+                    uint4 v;
+                    v.x = __byte_perm(prev[f][0], cur[f][0], 0x5410);
+                    v.y = __byte_perm(prev[f][1], cur[f][1], 0x5410);
+                    v.z = __byte_perm(prev[f][2], cur[f][2], 0x5410);
+                    v.w = __byte_perm(prev[f][3], cur[f][3], 0x5410);
+                    *reinterpret_cast<uint4 *>(&s_pair[f][s][4 * g]) = v;
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < 4; f++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) prev[f][j] = cur[f][j];
+        }
+    }
+    __syncthreads();
+    // ---- 3: vertical phases, 4 columns x 8 rows per thread
     const int g = tid & 31, fx = (tid >> 5) & 3, half = tid >> 7;
-    switch (fx) {
-    case 0: planes_rows<0, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
-    case 1: if (mode == 2) planes_rows<1, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
-    case 2: planes_rows<2, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
-    default: if (mode == 2) planes_rows<3, VEC>(s_src, s_hor, planes, stride, W, H, pad, x0, y0, cx0, cy0, g, half, mode); break;
+    const int l0 = 8 * half;
+    const int xg = x0 + 4 * g, end_col = W + pad;
+    if (l0 >= nL || xg >= end_col) return;
+    // planes this thread writes: fy = 0..3 of column phase fx (plane 0 is the
+    // full-pel picture itself; mode 1 keeps planes 2, 8, 10)
+    int want = 0;
+#pragma unroll
+    for (int fy = 0; fy < 4; fy++) {
+        const int k = 4 * fy + fx;
+        if (k != 0 && (mode == 2 || k == 2 || k == 8 || k == 10)) want |= 1 << fy;
+    }
+    if (!want) return;
+    int lc[4];
+    bool vec = true;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        lc[c] = clampi(xg + c, -4, W + 3) - cx0;
+        vec &= lc[c] == lc[0] + c;
+    }
+    vec &= (lc[0] & 3) == 0;
+    const uint32_t *rows = &s_pair[fx][0][0];
+    const int init = fx ? 2048 : 32, rsh = fx ? 12 : 6;
+    uint8_t *base[4];
+#pragma unroll
+    for (int fy = 0; fy < 4; fy++)   // static parameter indices (a dynamic one copies the table to the stack)
+        base[fy] = (fx == 0 ? planes.p[4 * fy] : fx == 1 ? planes.p[4 * fy + 1] : fx == 2 ? planes.p[4 * fy + 2]
+                                                                                 : planes.p[4 * fy + 3]) + xg;
+    uint4 E[7], O[7];   // E[i] = pairs of row l0 + 2i, O[i] = of row l0 + 1 + 2i
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int l = l0 + t;
+        if (l >= nL) continue;
+        if (t == 0) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) E[i] = load_pairs(rows + (l0 + 2 * i) * PT_W, lc, vec);
+        } else if (t == 1) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) O[i] = load_pairs(rows + (l0 + 1 + 2 * i) * PT_W, lc, vec);
+        } else if ((t & 1) == 0) {
+            E[t / 2 + 3] = load_pairs(rows + (l0 + t + 6) * PT_W, lc, vec);
+        } else {
+            O[t / 2 + 3] = load_pairs(rows + (l0 + t + 6) * PT_W, lc, vec);
+        }
+        uint4 A, B, C, D;
+        if (t & 1) {
+            A = O[t / 2]; B = O[t / 2 + 1]; C = O[t / 2 + 2]; D = O[t / 2 + 3];
+        } else {
+            A = E[t / 2]; B = E[t / 2 + 1]; C = E[t / 2 + 2]; D = E[t / 2 + 3];
+        }
+        uint32_t out[4];
+#pragma unroll
+        for (int fy = 0; fy < 4; fy++) {
+            const uint32_t t03 = tap_word(fy, 0), t47 = tap_word(fy, 1);
+            const int vx = vsum(A.x, B.x, C.x, D.x, t03, t47, init) >> rsh;
+            const int vy = vsum(A.y, B.y, C.y, D.y, t03, t47, init) >> rsh;
+            const int vz = vsum(A.z, B.z, C.z, D.z, t03, t47, init) >> rsh;
+            const int vw = vsum(A.w, B.w, C.w, D.w, t03, t47, init) >> rsh;
+            out[fy] = pack_sat_u8(vx, vy, vz, vw);
+        }
+        // output rows clamping to this row: one inside the picture's band,
+        // the whole margin run at rows -4 and H + 3
+        const int cyl = cy0 + l;
+        const int ya = max(cyl == -4 ? y0 : cyl, y0);
+        const int yb = min(min(cyl == H + 3 ? y0 + PT_H - 1 : cyl, y0 + PT_H - 1), H + pad - 1);
+        for (int y = ya; y <= yb; y++) {
+            const ptrdiff_t ro = (ptrdiff_t)y * stride;
+#pragma unroll
+            for (int fy = 0; fy < 4; fy++)
+                if ((want >> fy) & 1) store_group<VEC>(base[fy] + ro, out[fy], xg, end_col);
+        }
     }
 }
 
@@ -551,11 +594,12 @@ extern "C" int xavs2gpu_interpolate_frame(const uint8_t *src, int stride, int wi
     bool vec = stride % 4 == 0;
     for (int k = 1; k < 16; k++)
         if ((mask >> k) & 1) vec &= ((uintptr_t)planes[k] - (uintptr_t)pad) % 4 == 0;
+    const int src_words = stride % 4 == 0 && (uintptr_t)src % 4 == 0;
     dim3 grid((width + 2 * pad + PT_W - 1) / PT_W, (height + 2 * pad + PT_H - 1) / PT_H);
     if (vec)
-        frame_planes_kernel<true><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode);
+        frame_planes_kernel<true><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode, src_words);
     else
-        frame_planes_kernel<false><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode);
+        frame_planes_kernel<false><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode, src_words);
     count_launch();
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
