@@ -1531,8 +1531,24 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def chain_parity(xg, chain, sess, order, pus, cus, prm_tuple, n_cus, seed):
+    """The last eager picture of a chain against the oracle on n_cus seeded
+    CUs: the search of each of their PUs, every candidate (levels, nnz,
+    reconstructed residual, SSDs, search cost), each CU's choice and block
+    of the reconstruction.  Returns the bench line's parity object."""
+    import oracle
+    out = chain.download()
+    rng = np.random.default_rng(seed)
+    cu_idx = np.sort(rng.choice(len(cus), min(n_cus, len(cus)), replace=False))
+    n_pu, n_cd, bad = oracle.chain_sample_check(oracle.lib(), out, order[0], order[1:], pus, cus, sess.results(),
+                                                prm_tuple, QP, cu_idx, os.cpu_count() or 1)
+    return {"checked_cus": int(len(cu_idx)), "checked_pu_searches": int(n_pu), "checked_candidates": int(n_cd),
+            "mismatches": len(bad), "first": bad[0] if bad else None, "against": "oracle"}
+
+
 # ---- full-picture chain at 4K ------------------------------------------------
-CHAIN_METRIC = "P pictures/s, 3840x2160 hot-path chain (4 refs, FS +-64 + quarter-pel SATD, MC, TU chain, recon; CUDA graph)"
+CHAIN_METRIC = ("P pictures/s, 3840x2160 hot-path chain (4 refs, FS +-64 + quarter-pel SATD, every inter candidate "
+                "through the TU chain incl. TU splits, recon; CUDA graph)")
 
 
 def run_chain(args):
@@ -1553,8 +1569,19 @@ def run_chain(args):
     chain = xg.Chain(sess, cus, QP, feedback=True)
     prm = xg.MeParams(R, lambda_factor(QP), 1, 2, 0, 0)
     order = [frames[NR]] + [frames[NR - 1 - r] for r in range(NR)]   # current, then refs k-1 .. k-4
-    for idx, img in enumerate(order):
-        assert lib.xavs2gpu_copy_h2d(ctypes.c_void_p(chain.source(idx)), xg.ptr(img), img.nbytes) == 0
+
+    def upload_sources():
+        for idx, img in enumerate(order):
+            assert lib.xavs2gpu_copy_h2d(ctypes.c_void_p(chain.source(idx)), xg.ptr(img), img.nbytes) == 0
+
+    # parity at the full size: one eager picture, checked against the oracle
+    # on a seeded sample of CUs (their PU searches, every candidate, choice
+    # and reconstructed block); the feedback then moved the sources, so they
+    # are uploaded again
+    upload_sources()
+    chain.run(prm)
+    parity = chain_parity(xg, chain, sess, order, pus, cus, (R, prm.lambda_factor, 1, 2, 0, 0), 48, 77)
+    upload_sources()
     tune_ms = chain.autotune(prm, reps=1)
     tun = chain.tuning()
     chain.capture(prm)
@@ -1625,6 +1652,7 @@ def run_chain(args):
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": "chain_2160p_4ref", "width": W, "height": H, "refs": NR, "search_range": R, "qp": QP,
                    "leaf_cus": int(len(cus)), "pu_searches": int(len(pus)), "evals_per_picture": evals,
+                   "candidates": int(chain.outputs().n_cands), "tus_per_picture": 5 * int(chain.outputs().n_cands),
                    "content": "pan 12 px/picture + 2 block-local motions, seeded split map 64..8",
                    "l2": "inputs larger than L2 (%d MB of reference planes)" % (NR * 16 * (W + 160) * (H + 160) >> 20)},
         "graph": {"kernels_per_launch": nk, "autotuned": {"refine_split_px": tun.me.refine_split_px,
@@ -1641,11 +1669,14 @@ def run_chain(args):
         "cpu_baseline": {"value": cpu_fps, "unit": "pictures/s", "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": "oracle search over a random %.3f%% (%d) of the picture's PU searches, scaled"
                                    % (100 * args.cpu_fraction / 8, cpu_n)},
+        "parity": parity,
         "clocks": clocks,
     }
     print(json.dumps(line))
     chain.close()
     sess.close()
+    if parity["mismatches"]:
+        sys.exit("bench: chain outputs differ from the oracle: %s" % parity["first"])
 
 
 def main():

@@ -644,21 +644,33 @@ XAVS2GPU_API int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s);
  * No single counterpart in the reference: the device-side sequence of one
  * P picture over its leaf CUs -- sub-pel planes of every reference
  * (interpolate_lcu_row), the current picture, the batched motion search
- * (xavs2_me_search per PU and reference), the motion-compensated residual of
- * each CU's 2Nx2N prediction from its best reference (mc_luma on the
- * frame's sub-pel planes, mc.c:559-589, then pixel_sub_ps), the TU chain of
- * one CU-sized TU per CU (xavs2gpu_tq_batch), and the reconstruction
- * clip(pred + residual) (pixel_add_ps) -- enqueued on the session stream,
- * eagerly or as one captured CUDA graph.  The RDO choices between partition
- * modes, TU splits and intra stay on the host. */
+ * (xavs2_me_search per PU and reference), and every inter candidate of
+ * every leaf CU through the TU chain: each partition mode (2Nx2N, 2NxN,
+ * Nx2N, 2NxnU, 2NxnD, nLx2N, nRx2N; 8x8 CUs the first three) predicted PU by
+ * PU from the reference with the smallest search cost (mc_luma on the
+ * frame's sub-pel planes, mc.c:559-589), its residual (pixel_sub_ps), and
+ * dct -> quant -> dequant -> idct both as one CU-sized TU and as the mode's
+ * four split TUs (tu_recon_inter_luma, rdo.c:1333-1370; NSQT strips for the
+ * asymmetric modes of CUs above 8x8, quarters otherwise, rdo.c:103-192),
+ * with the SSD of each reconstruction -- enqueued on the session stream,
+ * eagerly or as one captured CUDA graph.  The encoder's RDO (rates from the
+ * entropy coder) stays on the host; so that the chain reconstructs a
+ * picture, each CU takes the mode with the smallest sum of its PUs' search
+ * costs and then the TU variant with the smaller SSD (the first on ties).
+ * A CU whose partition PUs are not in the PU list (see below) has the 2Nx2N
+ * candidate only. */
 typedef struct xavs2gpu_cu {
     int16_t x, y;              /* luma position of the CU                          */
     int16_t size;              /* 8, 16, 32 or 64                                  */
     int16_t pad_;
     int32_t pu[4];             /* index of the CU's 2Nx2N PU in the session's PU
-                                  list for reference 0..3 (-1: not searched)       */
-    int64_t offset;            /* residual / recon offset (elements), size*size    */
-    int64_t coef_offset;       /* level offset, size*size (64: 32*32)              */
+                                  list for reference 0..3 (-1: not searched); the
+                                  mode's other PUs follow it: 2NxN top, bottom,
+                                  Nx2N left, right, 2NxnU, 2NxnD, nLx2N, nRx2N
+                                  (two each; 8x8 CUs: 2NxN and Nx2N)               */
+    int64_t offset;            /* unused by the chain and the server (kept for the
+                                  caller's own residual layout)                    */
+    int64_t coef_offset;       /* unused likewise                                   */
 } xavs2gpu_cu_t;
 
 typedef struct xavs2gpu_chain xavs2gpu_chain_t;
@@ -677,12 +689,28 @@ XAVS2GPU_API uint8_t *xavs2gpu_chain_source(xavs2gpu_chain_t *c, int idx);
 XAVS2GPU_API int xavs2gpu_chain_run(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm);
 XAVS2GPU_API int xavs2gpu_chain_capture(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm);
 XAVS2GPU_API int xavs2gpu_chain_launch(xavs2gpu_chain_t *c);
-/* Device outputs of the last picture: levels, reconstructed residual, nnz
- * and TU descriptors per CU (CU order), the reconstructed picture (width x
- * height, stride = width) and per CU the chosen reference and its MV. */
+/* Device outputs of the last picture.  Candidates are numbered CU by CU,
+ * modes in the order above; candidate i owns TU descriptors (and nnz)
+ * 5 i (one TU) and 5 i + 1 .. 5 i + 4 (split TUs, in TU order), SSDs 2 i (one
+ * TU) and 2 i + 1 (split), and the residual / reconstructed-residual / level
+ * regions of its table entry.  The reconstructed picture is width x height,
+ * stride = width. */
+typedef struct xavs2gpu_cand {
+    int32_t cu;                /* CU index                                          */
+    int8_t mode;               /* 0 2Nx2N, 1 2NxN, 2 Nx2N, 3 2NxnU, 4 2NxnD, 5 nLx2N, 6 nRx2N */
+    int8_t split_type;         /* split TUs: 1 quarters, 2 horizontal strips S x S/4,
+                                  3 vertical strips S/4 x S                         */
+    int16_t pad_;
+    int64_t res_offset;        /* residual and reconstructed residual: S*S elements
+                                  of the one TU (row-major), then the four split TUs
+                                  (each contiguous, stride = TU width)              */
+    int64_t coef_offset;       /* levels, without gaps: the one TU's (S*S; 64: 32*32),
+                                  then the split TUs' (each w*h; 64-point: w*h/4)   */
+} xavs2gpu_cand_t;
 typedef struct xavs2gpu_cu_choice {
-    int32_t ref;               /* reference with the smallest 2Nx2N cost (lowest index on ties) */
-    int16_t mv_x, mv_y;        /* its MV, quarter-pel                               */
+    int32_t cand;              /* chosen candidate (index into the candidate table) */
+    int16_t mode;              /* its partition mode                                */
+    int16_t split;             /* 0 one TU, 1 split TUs                             */
 } xavs2gpu_cu_choice_t;
 typedef struct xavs2gpu_chain_outputs {
     int16_t *coef;
@@ -692,6 +720,10 @@ typedef struct xavs2gpu_chain_outputs {
     uint8_t *recon;
     xavs2gpu_cu_choice_t *choice;
     int64_t n_residual, n_coef;
+    const xavs2gpu_cand_t *cands;      /* candidate table (device)                 */
+    int32_t *cand_cost;                /* per candidate: sum of its PUs' search costs */
+    int32_t *dist;                     /* per candidate: SSD one TU, SSD split TUs  */
+    int64_t n_cands;                   /* candidates (TU descriptors: 5 n_cands)    */
 } xavs2gpu_chain_outputs_t;
 XAVS2GPU_API int xavs2gpu_chain_get_outputs(xavs2gpu_chain_t *c, xavs2gpu_chain_outputs_t *o);
 /* Autotuner: times the chain eagerly for every candidate launch shape
@@ -719,8 +751,11 @@ XAVS2GPU_API int xavs2gpu_chain_graph_kernels(const xavs2gpu_chain_t *c);
  * of all pictures (xavs2gpu_me_batch_run), each CU's motion-compensated
  * residual from its best reference, one TU chain over all CUs, the
  * reconstruction and a per-picture checksum.  Each stream keeps its two
- * references and their planes resident; streams are admitted against
- * hbm_budget_bytes.  The first two pictures of a stream only fill its
+ * references and their planes resident; a stream is admitted when its
+ * resident memory fits both hbm_budget_bytes (if set) and the device's free
+ * memory at that moment (cudaMemGetInfo) less hbm_reserve_bytes and less
+ * what streams admitted but not yet allocated will take.  The first two
+ * pictures of a stream only fill its
  * references (ref_only results); every later picture is searched against
  * the two before it. */
 typedef struct xavs2gpu_server_config {
@@ -729,6 +764,7 @@ typedef struct xavs2gpu_server_config {
     int32_t max_batch_frames;    /* pictures per batch, 1..256 */
     int32_t qp;                  /* quantiser of every TU */
     xavs2gpu_me_params_t me;     /* search parameters */
+    int64_t hbm_reserve_bytes;   /* device memory admission leaves free (0: 1/32 of the device, at least 1 GiB) */
 } xavs2gpu_server_config_t;
 
 typedef struct xavs2gpu_server_result {
@@ -748,7 +784,8 @@ XAVS2GPU_API void xavs2gpu_server_destroy(xavs2gpu_server_t *s);
 /* A stream of width x height pictures with its leaf-CU PU list (2
  * references) and CU list (as for xavs2gpu_chain_create) and `ring` pinned
  * picture slots.  Returns the stream id, or minus an error code
- * (-XAVS2GPU_ERR_CAPACITY when the device-memory budget is exhausted). */
+ * (-XAVS2GPU_ERR_CAPACITY when the stream does not fit the budget or the
+ * free device memory). */
 XAVS2GPU_API int xavs2gpu_server_open_stream(xavs2gpu_server_t *s, int width, int height, const xavs2gpu_pu_t *pus,
                                              int n_pus, const xavs2gpu_cu_t *cus, int n_cus, int ring);
 /* Copies the picture into a free slot of the stream and queues it;

@@ -233,3 +233,134 @@ def interpolate_frame(lib_, img, pad=80, mode=2, ref=False, lcu_level=6):
     else:
         lib_.xo_interpolate_frame(arr, ptr(planes[0], off), stride, w, h, pad, mode)
     return planes.reshape(16, h + 2 * pad, w + 2 * pad)
+
+
+# ---- the full-picture chain's inter candidates (rdo.c:1333-1477) -----------
+CAND_DTYPE = np.dtype([("cu", "<i4"), ("mode", "i1"), ("split_type", "i1"), ("pad_", "<i2"),
+                       ("res_offset", "<i8"), ("coef_offset", "<i8")])
+# partition PUs of a CU after its 2Nx2N PU, in quarters of the CU side:
+# (dx, dy, w, h); mode m >= 1 owns PUs 2m - 1 and 2m
+_CU_PARTS = [(0, 0, 4, 4), (0, 0, 4, 2), (0, 2, 4, 2), (0, 0, 2, 4), (2, 0, 2, 4), (0, 0, 4, 1), (0, 1, 4, 3),
+             (0, 0, 4, 3), (0, 3, 4, 1), (0, 0, 1, 4), (1, 0, 3, 4), (0, 0, 3, 4), (3, 0, 1, 4)]
+
+
+def _split_tus(S, split_type):
+    """(x, y, w, h) of the four split TUs of an S x S CU: quarters (1),
+    horizontal strips (2), vertical strips (3) (rdo.c:1419-1463)."""
+    if split_type == 2:
+        return [(0, t * S // 4, S, S // 4) for t in range(4)]
+    if split_type == 3:
+        return [(t * S // 4, 0, S // 4, S) for t in range(4)]
+    h = S // 2
+    return [((t & 1) * h, (t >> 1) * h, h, h) for t in range(4)]
+
+
+def chain_candidate(olib, cur, planes, res, cu, mode, split_type, qp):
+    """One inter candidate of a CU as the chain computes it: each PU of the
+    mode predicted from the reference with its smallest search cost (first
+    on ties) at that search's MV from the sub-pel planes (planes[r] =
+    interpolate_frame(...) of reference r, margin 80), the residual, the TU
+    chain (xo_tq_chain: dct -> quant -> dequant -> idct, i_level from the TU
+    shape) of the one CU-sized TU and of the four split TUs.  Returns a dict:
+    cost (sum of the PUs' search costs), levels / nnz / rres (reconstructed
+    residual, S x S) / dist (SSD of clip(pred + rres)) per variant (0 one TU,
+    1 split)."""
+    x, y, S = int(cu["x"]), int(cu["y"]), int(cu["size"])
+    ks = [0] if mode == 0 else [2 * mode - 1, 2 * mode]
+    pred = np.zeros((S, S), np.int32)
+    cost = 0
+    for k in ks:
+        best = None
+        for r in range(len(planes)):
+            q = res[int(cu["pu"][r]) + k]
+            if best is None or q["bcost"] < best[0]:
+                best = (int(q["bcost"]), r, int(q["bmv_x"]), int(q["bmv_y"]))
+        cost += best[0]
+        _, r, mvx, mvy = best
+        dx, dy, w, h = (v * S // 4 for v in _CU_PARTS[k])
+        pl = planes[r][((mvy & 3) << 2) + (mvx & 3)]
+        oy, ox = 80 + y + dy + (mvy >> 2), 80 + x + dx + (mvx >> 2)
+        pred[dy:dy + h, dx:dx + w] = pl[oy:oy + h, ox:ox + w]
+    src = cur[y:y + S, x:x + S].astype(np.int32)
+    resid = (src - pred).astype(np.int16)
+    out = {"cost": cost, "levels": [], "nnz": [], "rres": [], "dist": []}
+    for variant in (0, 1):
+        tus = [(0, 0, S, S)] if variant == 0 else _split_tus(S, split_type)
+        rres = np.zeros((S, S), np.int16)
+        levels, nnzs = [], []
+        for (tx, ty, tw, th) in tus:
+            blk = np.ascontiguousarray(resid[ty:ty + th, tx:tx + tw]).reshape(-1).copy()
+            coef = np.zeros(tw * th, np.int16)
+            part = PU_W.index(tw) if tw == th else [k for k in range(25) if PU_W[k] == tw and PU_H[k] == th][0]
+            nnzs.append(olib.xo_tq_chain(part, ptr(blk), ptr(coef), qp, 0, 0))
+            nc = tw * th // 4 if (tw == 64 or th == 64) else tw * th
+            levels.append(coef[:nc])
+            rres[ty:ty + th, tx:tx + tw] = blk.reshape(th, tw)
+        rec = np.clip(pred + rres, 0, 255)
+        out["levels"].append(np.concatenate(levels))
+        out["nnz"].append(nnzs)
+        out["rres"].append(rres)
+        out["dist"].append(int(((src - rec) ** 2).sum()))
+    out["pred"] = pred
+    return out
+
+
+def chain_sample_check(olib, out, cur, refs, pus, cus, res_gpu, prm_tuple, qp, cu_idx, threads=1):
+    """Checks a chain's (or a served picture's) outputs for the CUs cu_idx
+    against the oracle: the search of every PU of those CUs (oracle's
+    xo_me_search_list on the same pictures), every candidate of those CUs
+    (chain_candidate with the oracle's search results) and each CU's choice
+    and reconstructed block.  `out` holds the downloaded outputs (cands,
+    nnz, coef, rres, cost, dist, choice, recon).  Returns (PU searches
+    checked, candidates checked, list of mismatch descriptions)."""
+    h, w = cur.shape
+    stride = w + 160
+    cands = out["cands"]
+    first = np.searchsorted(cands["cu"], cu_idx)
+    last = np.searchsorted(cands["cu"], cu_idx, side="right")
+    sel = []
+    for c, a, b in zip(cu_idx, first, last):
+        nk = 1 if b - a == 1 else (5 if int(cus[c]["size"]) == 8 else 13)
+        for r in range(len(refs)):
+            sel.extend(range(int(cus[c]["pu"][r]), int(cus[c]["pu"][r]) + nk))
+    sel = np.array(sorted(set(sel)), np.int64)
+    flats = [np.ascontiguousarray(interpolate_frame(olib, r, mode=2).reshape(16, -1)) for r in refs]
+    frefs = (ctypes.c_void_p * (16 * len(refs)))(*[ptr(f[k], 80 * stride + 80).value for f in flats
+                                                   for k in range(16)])
+    sub = np.ascontiguousarray(pus[sel])
+    got = np.zeros(len(sel), RESULT_DTYPE)
+    olib.xo_me_search_list(ctypes.byref(MeParams(*prm_tuple)), ptr(sub), len(sub), ptr(cur), w, frefs, stride,
+                           ptr(got), threads)
+    bad = []
+    res = np.zeros(len(pus), RESULT_DTYPE)
+    res[sel] = got
+    diff = np.flatnonzero((got.view(np.uint8).reshape(len(sel), -1) !=
+                           np.ascontiguousarray(res_gpu[sel]).view(np.uint8).reshape(len(sel), -1)).any(axis=1))
+    bad += ["search of PU %d" % sel[i] for i in diff[:5]]
+    planes = [f.reshape(16, h + 160, w + 160) for f in flats]
+    n_cands = 0
+    for c, a, b in zip(cu_idx, first, last):
+        exp = {}
+        for i in range(a, b):
+            cd = cands[i]
+            e = chain_candidate(olib, cur, planes, res, cus[c], int(cd["mode"]), int(cd["split_type"]), qp)
+            exp[i] = e
+            n_cands += 1
+            S = int(cus[c]["size"])
+            ro, co = int(cd["res_offset"]), int(cd["coef_offset"])
+            n0, n1 = len(e["levels"][0]), len(e["levels"][1])
+            ok = (int(out["cost"][i]) == e["cost"] and list(out["dist"][i]) == e["dist"] and
+                  list(out["nnz"][5 * i:5 * i + 5]) == [e["nnz"][0][0]] + e["nnz"][1] and
+                  np.array_equal(out["rres"][ro:ro + S * S].reshape(S, S), e["rres"][0]) and
+                  np.array_equal(out["coef"][co:co + n0], e["levels"][0]) and
+                  np.array_equal(out["coef"][co + n0:co + n0 + n1], e["levels"][1]))
+            if not ok:
+                bad.append("candidate %d (CU %d mode %d)" % (i, c, int(cd["mode"])))
+        best = min(range(a, b), key=lambda k: (exp[k]["cost"], k))
+        split = int(exp[best]["dist"][1] < exp[best]["dist"][0])
+        ch = out["choice"][c]
+        x, y, S = int(cus[c]["x"]), int(cus[c]["y"]), int(cus[c]["size"])
+        rec = np.clip(exp[best]["pred"] + exp[best]["rres"][split], 0, 255)
+        if (int(ch["cand"]), int(ch["split"])) != (best, split) or not np.array_equal(out["recon"][y:y + S, x:x + S], rec):
+            bad.append("choice of CU %d" % c)
+    return len(sel), n_cands, bad

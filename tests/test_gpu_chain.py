@@ -1,9 +1,11 @@
 """The full-picture chain (xavs2gpu_chain_*) against the oracle: the motion
-search of every leaf-CU PU, each CU's best reference and prediction, the
-residual through dct -> quant -> dequant -> idct, and the reconstructed
-picture; the captured CUDA graph gives the same outputs as the eager run,
-the autotuner's launch shapes change no output, and the feedback loop makes
-the reconstruction the next reference."""
+search of every leaf-CU PU; for every inter candidate (each partition mode
+of each CU) the prediction from each PU's best reference, the residual
+through dct -> quant -> dequant -> idct as one TU and as the mode's four
+split TUs (levels, nnz, reconstructed residual, SSD); each CU's choice and
+the reconstructed picture; the captured CUDA graph gives the same outputs
+as the eager run, the autotuner's launch shapes change no output, and the
+feedback loop makes the reconstruction the next reference."""
 import ctypes
 
 import numpy as np
@@ -25,59 +27,70 @@ def _pictures(seed=11):
     return f2, [f1, f0]
 
 
-def _oracle_chain(cur, refs, pus, cus, prm_tuple, qp):
+def _oracle_me(cur, refs, pus, prm_tuple):
     olib = oracle.lib()
-    stride = W + 160
+    h, w = cur.shape
+    stride = w + 160
     flats = [np.ascontiguousarray(oracle.interpolate_frame(olib, r, mode=2).reshape(16, -1)) for r in refs]
     frefs = (ctypes.c_void_p * (16 * len(refs)))(*[oracle.ptr(f[k], 80 * stride + 80).value
                                                    for f in flats for k in range(16)])
     res = np.zeros(len(pus), oracle.RESULT_DTYPE)
     prm = oracle.MeParams(*prm_tuple)
-    olib.xo_me_search_list(ctypes.byref(prm), oracle.ptr(pus), len(pus), oracle.ptr(cur), W, frefs, stride,
-                           oracle.ptr(res), 1)
-    planes = [f.reshape(16, H + 160, W + 160) for f in flats]
-    n_res = int((cus["size"].astype(np.int64) ** 2).sum())
-    n_coef = int(cus["coef_offset"][-1]) + (1024 if cus["size"][-1] == 64 else int(cus["size"][-1]) ** 2)
-    coef = np.zeros(n_coef, np.int16)
-    rres = np.zeros(n_res, np.int16)
-    nnz = np.zeros(len(cus), np.int32)
-    recon = np.zeros((H, W), np.uint8)
-    choice = np.zeros(len(cus), [("ref", "<i4"), ("mv_x", "<i2"), ("mv_y", "<i2")])
-    part_of = {8: 1, 16: 2, 32: 3, 64: 4}
-    for i, c in enumerate(cus):
-        x, y, s = int(c["x"]), int(c["y"]), int(c["size"])
-        best = 0
-        for r in range(NREFS):
-            if r == 0 or res["bcost"][c["pu"][r]] < res["bcost"][c["pu"][best]]:
-                best = r
-        q = res[c["pu"][best]]
-        mvx, mvy = int(q["bmv_x"]), int(q["bmv_y"])
-        pl = planes[best][((mvy & 3) << 2) + (mvx & 3)]
-        pred = pl[80 + y + (mvy >> 2):80 + y + (mvy >> 2) + s, 80 + x + (mvx >> 2):80 + x + (mvx >> 2) + s].astype(np.int32)
-        blk = (cur[y:y + s, x:x + s].astype(np.int32) - pred).astype(np.int16).reshape(-1).copy()
-        cf = np.zeros(s * s, np.int16)
-        nnz[i] = olib.xo_tq_chain(part_of[s], oracle.ptr(blk), oracle.ptr(cf), qp, 0, 0)
-        nc = 1024 if s == 64 else s * s
-        coef[int(c["coef_offset"]):int(c["coef_offset"]) + nc] = cf[:nc]
-        rres[int(c["offset"]):int(c["offset"]) + s * s] = blk
-        recon[y:y + s, x:x + s] = np.clip(pred + blk.reshape(s, s), 0, 255)
-        choice[i] = (best, mvx, mvy)
-    return res, coef, rres, nnz, recon, choice
+    olib.xo_me_search_list(ctypes.byref(prm), oracle.ptr(pus), len(pus), oracle.ptr(cur), w, frefs, stride,
+                           oracle.ptr(res), 8)
+    return res, [f.reshape(16, h + 160, w + 160) for f in flats]
+
+
+def check_candidates(out, cur, planes, res, cus, qp, cand_idx):
+    """The GPU outputs of the candidates cand_idx against the oracle's
+    chain_candidate; returns the oracle's per-candidate results."""
+    olib = oracle.lib()
+    exp = {}
+    for i in cand_idx:
+        cd = out["cands"][i]
+        e = oracle.chain_candidate(olib, cur, planes, res, cus[int(cd["cu"])], int(cd["mode"]),
+                                   int(cd["split_type"]), qp)
+        S = int(cus[int(cd["cu"])]["size"])
+        assert out["cost"][i] == e["cost"], i
+        assert list(out["dist"][i]) == e["dist"], (i, out["dist"][i], e["dist"])
+        assert list(out["nnz"][5 * i:5 * i + 5]) == [e["nnz"][0][0]] + e["nnz"][1], i
+        ro, co = int(cd["res_offset"]), int(cd["coef_offset"])
+        assert np.array_equal(out["rres"][ro:ro + S * S].reshape(S, S), e["rres"][0]), i
+        n0 = len(e["levels"][0])
+        assert np.array_equal(out["coef"][co:co + n0], e["levels"][0]), i
+        n1 = len(e["levels"][1])
+        assert np.array_equal(out["coef"][co + n0:co + n0 + n1], e["levels"][1]), i
+        # the split TUs' reconstructed residual, TU by TU
+        split = out["rres"][ro + S * S:ro + 2 * S * S]
+        off = 0
+        for (tx, ty, tw, th) in oracle._split_tus(S, int(cd["split_type"])):
+            assert np.array_equal(split[off:off + tw * th].reshape(th, tw), e["rres"][1][ty:ty + th, tx:tx + tw]), i
+            off += tw * th
+        exp[i] = e
+    return exp
+
+
+def check_choices(out, cur, planes, res, cus, qp):
+    """Every candidate and every CU's choice and reconstruction."""
+    exp = check_candidates(out, cur, planes, res, cus, qp, range(len(out["cands"])))
+    first = np.searchsorted(out["cands"]["cu"], np.arange(len(cus)))
+    last = np.searchsorted(out["cands"]["cu"], np.arange(len(cus)), side="right")
+    recon = np.zeros_like(cur)
+    for c in range(len(cus)):
+        ks = list(range(first[c], last[c]))
+        best = min(ks, key=lambda k: (exp[k]["cost"], k))
+        split = int(exp[best]["dist"][1] < exp[best]["dist"][0])
+        ch = out["choice"][c]
+        assert (int(ch["cand"]), int(ch["mode"]), int(ch["split"])) == (best, int(out["cands"][best]["mode"]), split), c
+        x, y, S = int(cus[c]["x"]), int(cus[c]["y"]), int(cus[c]["size"])
+        recon[y:y + S, x:x + S] = np.clip(exp[best]["pred"] + exp[best]["rres"][split], 0, 255)
+    assert np.array_equal(out["recon"], recon)
 
 
 def _d2h(lib, dev_ptr, n, dtype):
     out = np.zeros(n, dtype)
     assert lib.xavs2gpu_copy_d2h(oracle.ptr(out), ctypes.c_void_p(dev_ptr), out.nbytes) == 0
     return out
-
-
-def _outputs(lib, chain, n_cus):
-    import xavs2_gb300 as xg
-    o = chain.outputs()
-    lib.xavs2gpu_me_sync(chain.sess.h)
-    return (_d2h(lib, o.coef, o.n_coef, np.int16), _d2h(lib, o.recon_residual, o.n_residual, np.int16),
-            _d2h(lib, o.nnz, n_cus, np.int32), _d2h(lib, o.recon, W * H, np.uint8).reshape(H, W),
-            _d2h(lib, o.choice, n_cus, xg.CHOICE_DTYPE))
 
 
 def _setup(feedback=False, seed=11):
@@ -99,31 +112,60 @@ def test_chain_matches_oracle_and_graph(gpu):
     prm_t = (16, oracle.lambda_factor(QP), 1, 2, 0, 0)
     prm = xg.MeParams(*prm_t)
     chain.run(prm)
-    eager = _outputs(lib, chain, len(cus))
+    eager = chain.download()
     me = sess.results()
-    o_me, o_coef, o_rres, o_nnz, o_recon, o_choice = _oracle_chain(cur, refs, pus, cus, prm_t, QP)
+    o_me, planes = _oracle_me(cur, refs, pus, prm_t)
     assert me.tobytes() == o_me.tobytes()
-    coef, rres, nnz, recon, choice = eager
-    assert np.array_equal(choice, o_choice)
-    assert np.array_equal(nnz, o_nnz)
-    assert np.array_equal(coef, o_coef)
-    assert np.array_equal(rres, o_rres)
-    assert np.array_equal(recon, o_recon)
+    # every CU has all of its partition modes (8x8: three)
+    modes = np.bincount(eager["cands"]["cu"], minlength=len(cus))
+    assert (modes == np.where(cus["size"] == 8, 3, 7)).all()
+    assert set(np.unique(eager["cands"]["split_type"])) == {1, 2, 3}
+    check_choices(eager, cur, planes, o_me, cus, QP)
     # the captured graph: same outputs, and it holds the chain's kernels
     chain.capture(prm)
     assert chain.graph_kernels() >= 8
     chain.launch()
-    graph = _outputs(lib, chain, len(cus))
-    for a, b in zip(eager, graph):
-        assert np.array_equal(a, b)
+    graph = chain.download()
+    for k in eager:
+        assert np.array_equal(eager[k], graph[k]), k
     # autotuned launch shapes change nothing
     chain.autotune(prm, reps=1)
     t = chain.tuning()
     assert t.tq_warps in (4, 8) and t.me.refine_block in (64, 128)
     chain.run(prm)
-    tuned = _outputs(lib, chain, len(cus))
-    for a, b in zip(eager, tuned):
-        assert np.array_equal(a, b)
+    tuned = chain.download()
+    for k in eager:
+        assert np.array_equal(eager[k], tuned[k]), k
+    chain.close()
+    sess.close()
+
+
+def test_chain_2nx2n_only_cus(gpu):
+    """CUs whose partition PUs are not in the PU list have the 2Nx2N
+    candidate alone; it is chosen and reconstructed like the others."""
+    import xavs2_gb300 as xg
+    cur, refs = _pictures(seed=4)
+    cus_list = xg.split_map_cus(W, H, seed=9)
+    pus, cus = xg.cu_pus(cus_list, W, H, NREFS)
+    # keep only the 2Nx2N PUs: re-index the CU records
+    keep = np.unique(cus["pu"][:, :NREFS].reshape(-1))
+    remap = -np.ones(len(pus), np.int64)
+    remap[keep] = np.arange(len(keep))
+    pus2 = np.ascontiguousarray(pus[keep])
+    cus2 = cus.copy()
+    cus2["pu"][:, :NREFS] = remap[cus["pu"][:, :NREFS]]
+    sess = xg.MeSession(W, H, NREFS, len(pus2))
+    sess.set_pus(pus2)
+    chain = xg.Chain(sess, cus2, QP)
+    lib = xg.load()
+    for idx, img in enumerate([cur] + refs):
+        assert lib.xavs2gpu_copy_h2d(ctypes.c_void_p(chain.source(idx)), oracle.ptr(img), img.nbytes) == 0
+    prm_t = (8, oracle.lambda_factor(QP), 1, 2, 0, 0)
+    chain.run(xg.MeParams(*prm_t))
+    out = chain.download()
+    assert len(out["cands"]) == len(cus2) and (out["cands"]["mode"] == 0).all()
+    o_me, planes = _oracle_me(cur, refs, pus2, prm_t)
+    check_choices(out, cur, planes, o_me, cus2, QP)
     chain.close()
     sess.close()
 
@@ -134,7 +176,7 @@ def test_chain_feedback_loop(gpu):
     xg, lib, sess, chain, cur, refs, pus, cus = _setup(feedback=True, seed=5)
     prm = xg.MeParams(8, oracle.lambda_factor(QP), 1, 2, 0, 0)
     chain.run(prm)
-    _, _, _, recon, _ = _outputs(lib, chain, len(cus))
+    recon = chain.download()["recon"]
     src1 = _d2h(lib, chain.source(1), W * H, np.uint8).reshape(H, W)
     src2 = _d2h(lib, chain.source(2), W * H, np.uint8).reshape(H, W)
     assert np.array_equal(src1, recon)

@@ -99,3 +99,28 @@ def test_server_admission_budget(gpu):
         lib.xavs2gpu_clear_error()
         lib.xavs2gpu_set_abort_on_error(1)
     srv.close()
+
+
+def test_server_admission_free_memory(gpu):
+    """Streams are admitted against the device's free memory: with a
+    reserve that leaves less free memory than one stream needs, opening it
+    is refused; with the default reserve it is admitted, and a stream
+    refused earlier does not count against later ones."""
+    import torch
+    import xavs2_gb300 as xg
+    w, h, frames, pus, cus = _streams(xg)[1]
+    prm = xg.MeParams(R, oracle.lambda_factor(QP), 1, 2, 0, 0)
+    free_b, _ = torch.cuda.mem_get_info()
+    lib = xg.load()
+    srv = xg.Server(xg.ServerConfig(0, 1 << 18, 4, QP, prm, max(free_b - (1 << 20), 1)))
+    lib.xavs2gpu_set_abort_on_error(0)
+    try:
+        assert srv.open_stream(w, h, pus, cus) == -5      # -XAVS2GPU_ERR_CAPACITY: 1 MiB is not enough
+        assert b"free device memory" in lib.xavs2gpu_get_error()
+    finally:
+        lib.xavs2gpu_clear_error()
+        lib.xavs2gpu_set_abort_on_error(1)
+    srv.close()
+    srv = xg.Server(xg.ServerConfig(0, 1 << 18, 4, QP, prm))
+    assert srv.open_stream(w, h, pus, cus) >= 0
+    srv.close()

@@ -353,7 +353,8 @@ class MeBatch:
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_pixels", ctypes.c_int64),
-                ("max_batch_frames", ctypes.c_int32), ("qp", ctypes.c_int32), ("me", MeParams)]
+                ("max_batch_frames", ctypes.c_int32), ("qp", ctypes.c_int32), ("me", MeParams),
+                ("hbm_reserve_bytes", ctypes.c_int64)]
 
 
 SERVER_RESULT_DTYPE = np.dtype([("stream", "<i4"), ("frame", "<i4"), ("tag", "<i8"), ("t_submit_ns", "<i8"),
@@ -433,7 +434,8 @@ class ChainTuning(ctypes.Structure):
 
 class ChainOutputs(ctypes.Structure):
     _fields_ = [("coef", _P), ("recon_residual", _P), ("nnz", _P), ("blocks", _P), ("recon", _P),
-                ("choice", _P), ("n_residual", ctypes.c_int64), ("n_coef", ctypes.c_int64)]
+                ("choice", _P), ("n_residual", ctypes.c_int64), ("n_coef", ctypes.c_int64),
+                ("cands", _P), ("cand_cost", _P), ("dist", _P), ("n_cands", ctypes.c_int64)]
 
 
 INTRA_BLOCK_DTYPE = np.dtype([("edge_offset", "<i8"), ("fenc_offset", "<i8"), ("width", "<i2"), ("height", "<i2"),
@@ -458,7 +460,11 @@ class IntraParams(ctypes.Structure):
                 ("dist2", ctypes.c_int32), ("dist1", ctypes.c_int32)]
 
 
-CHOICE_DTYPE = np.dtype([("ref", "<i4"), ("mv_x", "<i2"), ("mv_y", "<i2")])
+# xavs2gpu_cu_choice_t: chosen candidate, its partition mode and TU variant
+CHOICE_DTYPE = np.dtype([("cand", "<i4"), ("mode", "<i2"), ("split", "<i2")])
+# xavs2gpu_cand_t
+CAND_DTYPE = np.dtype([("cu", "<i4"), ("mode", "i1"), ("split_type", "i1"), ("pad_", "<i2"),
+                       ("res_offset", "<i8"), ("coef_offset", "<i8")])
 
 
 class Chain:
@@ -522,6 +528,29 @@ class Chain:
         o = ChainOutputs()
         self._check(self.lib.xavs2gpu_chain_get_outputs(self.h, ctypes.byref(o)), "chain_get_outputs")
         return o
+
+    def download(self):
+        """Every output of the last picture on the host (after a session
+        sync): candidate table, TU descriptors, nnz, levels, reconstructed
+        residual, candidate search costs and SSDs, per-CU choices and the
+        reconstructed picture."""
+        o = self.outputs()
+        self.lib.xavs2gpu_me_sync(self.sess.h)
+        n = int(o.n_cands)
+        W, H = self.sess.width, self.sess.height
+
+        def d2h(p, count, dtype):
+            out = np.zeros(count, dtype)
+            if count:
+                rc = self.lib.xavs2gpu_copy_d2h(out.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(p), out.nbytes)
+                self._check(rc, "copy_d2h")
+            return out
+        return {"cands": d2h(o.cands, n, CAND_DTYPE), "blocks": d2h(o.blocks, 5 * n, TQ_DTYPE),
+                "nnz": d2h(o.nnz, 5 * n, np.int32), "coef": d2h(o.coef, int(o.n_coef), np.int16),
+                "rres": d2h(o.recon_residual, int(o.n_residual), np.int16),
+                "cost": d2h(o.cand_cost, n, np.int32), "dist": d2h(o.dist, 2 * n, np.int32).reshape(n, 2),
+                "choice": d2h(o.choice, len(self.cus), CHOICE_DTYPE),
+                "recon": d2h(o.recon, W * H, np.uint8).reshape(H, W)}
 
 
 def set_limits(pus, width, height, vmin=-2048, vmax=2047):

@@ -1,0 +1,251 @@
+// cand.cuh -- the inter candidates of leaf CUs through the transform chain,
+// shared by the full-picture chain (chain.cu) and the server (serve.cu).
+//
+// A candidate is one partition mode of a CU (2Nx2N, 2NxN, Nx2N, 2NxnU, 2NxnD,
+// nLx2N, nRx2N; 8x8 CUs have the first three): every PU of the mode is
+// predicted from the reference whose search returned its smallest cost
+// (lowest index on ties) at that search's MV (mc_luma on the frame's sub-pel
+// planes, mc.c:559-589), the CU's residual is formed (pixel_sub_ps), and the
+// residual goes through dct -> quant -> dequant -> idct both as one CU-sized
+// TU and as the four TUs of the mode's TU split (tu_recon_inter_luma,
+// rdo.c:1333-1370; split type cu_set_tu_split_type, rdo.c:183-192 with
+// TU_SPLIT_TYPE, rdo.c:103-116, NSQT on: horizontal strips for the 2NxN-type
+// modes and vertical strips for the Nx2N-type modes of CUs above 8x8,
+// quarters otherwise; i_level one below the CU's, rdo.c:1440-1463).  For
+// every candidate and TU variant the kernels report the levels, nnz, the
+// reconstructed residual and the SSD of the reconstruction.  The encoder's
+// RDO (rates from the entropy coder) is out of scope; so that the chain has a
+// reconstruction to feed back, each CU takes the mode with the smallest sum
+// of its PUs' search costs and then the TU variant with the smaller SSD (the
+// first on ties).
+#pragma once
+
+#include "xavs2gpu_common.cuh"
+
+namespace xg {
+
+// The picture a group of candidates belongs to.  The chain has one; a
+// serving batch has one per picture, found from the batch-wide indices.
+struct PicView {
+    const uint8_t *cur;                 // current picture (stride `stride`)
+    const uint8_t *const *planes;       // reference planes, 16 r + k (stride `stride`)
+    const xavs2gpu_me_result_t *res;    // search results of the picture's PU list
+    const xavs2gpu_cu_t *cus;           // leaf CUs
+    const xavs2gpu_cand_t *cands;       // candidate table (picture-local offsets)
+    const int32_t *cu_cand;             // per CU: first candidate; [n_cus] = number of candidates
+    uint8_t *recon;                     // reconstructed picture (stride `width`)
+    unsigned long long *hash;           // serving checksum
+    int64_t res_off, coef_off;          // base of the picture in the batch residual / level buffers
+    int64_t cu_start;                   // first batch-wide CU index of the picture
+    int64_t cand_start;                 // first batch-wide candidate index of the picture
+    int64_t n_coef;                     // levels of the picture
+    int n_cus, n_cands, stride, width, height, nrefs, n_pus;
+};
+
+// view holding batch-wide index i of a field with the given start member
+template <int64_t PicView::*START>
+__device__ __forceinline__ int find_view(const PicView *v, int nviews, int64_t i)
+{
+    int lo = 0, hi = nviews - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (v[mid].*START <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// PU k of a mode (0 or 1) covers pixel (xx, yy) of the S x S CU
+__device__ __forceinline__ int mode_pu_of(int mode, int S, int xx, int yy)
+{
+    switch (mode) {
+    case 1: return yy >= S / 2;
+    case 2: return xx >= S / 2;
+    case 3: return yy >= S / 4;
+    case 4: return yy >= 3 * S / 4;
+    case 5: return xx >= S / 4;
+    case 6: return xx >= 3 * S / 4;
+    default: return 0;
+    }
+}
+
+// position of partition PU `k` of `mode` after the CU's 2Nx2N PU in the PU
+// list (2Nx2N; 2NxN top, bottom; Nx2N left, right; then the AMP pairs)
+__device__ __forceinline__ int mode_pu_index(int mode, int k) { return mode == 0 ? 0 : 2 * mode - 1 + k; }
+
+// element offset of CU pixel (xx, yy) inside the four split TUs (each TU
+// contiguous, in TU order)
+__device__ __forceinline__ int split_offset(int split_type, int S, int xx, int yy)
+{
+    if (split_type == 2) {                           // horizontal strips S x S/4
+        const int q = S >> 2;
+        return (yy / q) * (S * q) + (yy % q) * S + xx;
+    }
+    if (split_type == 3) {                           // vertical strips S/4 x S
+        const int q = S >> 2;
+        return (xx / q) * (S * q) + yy * q + (xx % q);
+    }
+    const int h = S >> 1;                            // quarters
+    return ((yy >= h) * 2 + (xx >= h)) * (h * h) + (yy % h) * h + (xx % h);
+}
+
+__device__ __forceinline__ int luma_part(int w, int h)
+{
+    // LumaPU index of the TU shapes (pixel.h:50-65)
+    if (w == h) return w == 4 ? 0 : w == 8 ? 1 : w == 16 ? 2 : w == 32 ? 3 : 4;
+    if (w == 16 && h == 4) return 15;
+    if (w == 4 && h == 16) return 16;
+    if (w == 32 && h == 8) return 19;
+    if (w == 8 && h == 32) return 20;
+    if (w == 64 && h == 16) return 23;
+    return 24;                                       // 16x64
+}
+
+// Best reference of partition PU k of a CU: the CU record holds its 2Nx2N
+// PU per reference and the mode's PUs follow it.  (The record is read from
+// global memory: a local copy indexed by the reference would live on the
+// stack.)
+struct PuPick { int ref, mvx, mvy, cost; };
+__device__ __forceinline__ PuPick best_ref(const PicView &v, const xavs2gpu_cu_t *cp, int k)
+{
+    PuPick p{0, 0, 0, 0};
+    for (int r = 0; r < v.nrefs; r++) {
+        const xavs2gpu_me_result_t q = v.res[cp->pu[r] + k];
+        if (r == 0 || q.bcost < p.cost) p = PuPick{r, q.bmv_x, q.bmv_y, q.bcost};
+    }
+    return p;
+}
+
+__device__ __forceinline__ const uint8_t *pred_ptr(const PicView &v, int cx, int cy, const PuPick &p)
+{
+    return v.planes[p.ref * 16 + ((p.mvy & 3) << 2) + (p.mvx & 3)] + (ptrdiff_t)(cy + (p.mvy >> 2)) * v.stride + cx +
+           (p.mvx >> 2);
+}
+
+// Warp per candidate: prediction, residual in both TU layouts, the five TU
+// descriptors, and the sum of the mode's search costs.
+static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
+                                                            int qp, int16_t *__restrict__ residual,
+                                                            xavs2gpu_tq_block_t *__restrict__ blocks,
+                                                            int32_t *__restrict__ cand_cost)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const PicView &v = views[find_view<&PicView::cand_start>(views, nviews, i)];
+    const xavs2gpu_cand_t cd = v.cands[i - v.cand_start];
+    const xavs2gpu_cu_t *cp = v.cus + cd.cu;
+    const int cx = cp->x, cy = cp->y, S = cp->size, lg = 31 - __clz(S), mode = cd.mode;
+    const PuPick p0 = best_ref(v, cp, mode_pu_index(mode, 0));
+    const PuPick p1 = mode ? best_ref(v, cp, mode_pu_index(mode, 1)) : p0;
+    const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
+    const uint8_t *src = v.cur + (ptrdiff_t)cy * v.stride + cx;
+    int16_t *whole = residual + v.res_off + cd.res_offset, *split = whole + S * S;
+    for (int e = lane; e < S * S; e += 32) {
+        const int yy = e >> lg, xx = e & (S - 1);
+        const uint8_t *pr = mode_pu_of(mode, S, xx, yy) ? pr1 : pr0;
+        const int16_t r = (int16_t)((int)src[(ptrdiff_t)yy * v.stride + xx] - (int)pr[(ptrdiff_t)yy * v.stride + xx]);
+        whole[e] = r;
+        split[split_offset(cd.split_type, S, xx, yy)] = r;
+    }
+    if (lane < 5) {
+        xavs2gpu_tq_block_t b;
+        b.qp = qp;
+        b.flags = 0;
+        b.pad_ = 0;
+        if (lane == 0) {
+            b.offset = v.res_off + cd.res_offset;
+            b.coef_offset = v.coef_off + cd.coef_offset;
+            b.part = luma_part(S, S);
+        } else {
+            const int t = lane - 1;
+            const int tw = cd.split_type == 3 ? S >> 2 : cd.split_type == 2 ? S : S >> 1;
+            const int th = cd.split_type == 2 ? S >> 2 : cd.split_type == 3 ? S : S >> 1;
+            const int wav = (tw == 64 || th == 64) ? 2 : 0;   // 64-point shapes keep a quarter of the levels
+            b.offset = v.res_off + cd.res_offset + S * S + (int64_t)t * tw * th;
+            b.coef_offset = v.coef_off + cd.coef_offset + (S == 64 ? 1024 : S * S) + (int64_t)t * ((tw * th) >> wav);
+            b.part = luma_part(tw, th);
+        }
+        blocks[5 * i + lane] = b;
+    }
+    if (lane == 0) cand_cost[i] = p0.cost + (mode ? p1.cost : 0);
+}
+
+// Warp per candidate: SSD of clip(pred + reconstructed residual) against the
+// current picture for both TU variants (dist[2 i] one TU, dist[2 i + 1] split).
+static __global__ void __launch_bounds__(128) cand_eval_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
+                                                        const int16_t *__restrict__ rres, int32_t *__restrict__ dist)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const PicView &v = views[find_view<&PicView::cand_start>(views, nviews, i)];
+    const xavs2gpu_cand_t cd = v.cands[i - v.cand_start];
+    const xavs2gpu_cu_t *cp = v.cus + cd.cu;
+    const int cx = cp->x, cy = cp->y, S = cp->size, lg = 31 - __clz(S), mode = cd.mode;
+    const PuPick p0 = best_ref(v, cp, mode_pu_index(mode, 0));
+    const PuPick p1 = mode ? best_ref(v, cp, mode_pu_index(mode, 1)) : p0;
+    const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
+    const uint8_t *src = v.cur + (ptrdiff_t)cy * v.stride + cx;
+    const int16_t *whole = rres + v.res_off + cd.res_offset, *split = whole + S * S;
+    int d0 = 0, d1 = 0;
+    for (int e = lane; e < S * S; e += 32) {
+        const int yy = e >> lg, xx = e & (S - 1);
+        const int pv = (mode_pu_of(mode, S, xx, yy) ? pr1 : pr0)[(ptrdiff_t)yy * v.stride + xx];
+        const int sv = src[(ptrdiff_t)yy * v.stride + xx];
+        const int a = sv - clip_pel_d(pv + whole[e]), b = sv - clip_pel_d(pv + split[split_offset(cd.split_type, S, xx, yy)]);
+        d0 += a * a;
+        d1 += b * b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+        d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+    }
+    if (lane == 0) {
+        dist[2 * i] = d0;
+        dist[2 * i + 1] = d1;
+    }
+}
+
+// Warp per CU: the mode with the smallest search cost, then the TU variant
+// with the smaller SSD; its reconstruction into the picture.
+static __global__ void __launch_bounds__(128) cand_choose_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
+                                                          const int32_t *__restrict__ cand_cost,
+                                                          const int32_t *__restrict__ dist,
+                                                          const int16_t *__restrict__ rres,
+                                                          xavs2gpu_cu_choice_t *__restrict__ choice)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const PicView &v = views[find_view<&PicView::cu_start>(views, nviews, i)];
+    const int ci = (int)(i - v.cu_start);
+    const int64_t first = v.cand_start + v.cu_cand[ci], last = v.cand_start + v.cu_cand[ci + 1];
+    int64_t best = first;
+    for (int64_t k = first + 1; k < last; k++)
+        if (cand_cost[k] < cand_cost[best]) best = k;
+    const int split = dist[2 * best + 1] < dist[2 * best];
+    const xavs2gpu_cand_t cd = v.cands[best - v.cand_start];
+    const xavs2gpu_cu_t *cp = v.cus + ci;
+    const int cx = cp->x, cy = cp->y, S = cp->size, lg = 31 - __clz(S), mode = cd.mode;
+    const PuPick p0 = best_ref(v, cp, mode_pu_index(mode, 0));
+    const PuPick p1 = mode ? best_ref(v, cp, mode_pu_index(mode, 1)) : p0;
+    const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
+    const int16_t *r = rres + v.res_off + cd.res_offset + (split ? S * S : 0);
+    uint8_t *o = v.recon + (ptrdiff_t)cy * v.width + cx;
+    for (int e = lane; e < S * S; e += 32) {
+        const int yy = e >> lg, xx = e & (S - 1);
+        const int pv = (mode_pu_of(mode, S, xx, yy) ? pr1 : pr0)[(ptrdiff_t)yy * v.stride + xx];
+        o[(ptrdiff_t)yy * v.width + xx] = clip_pel_d(pv + r[split ? split_offset(cd.split_type, S, xx, yy) : e]);
+    }
+    if (lane == 0) {
+        xavs2gpu_cu_choice_t ch;
+        ch.cand = (int32_t)(best - v.cand_start);
+        ch.mode = (int16_t)mode;
+        ch.split = (int16_t)split;
+        choice[i] = ch;
+    }
+}
+
+}  // namespace xg

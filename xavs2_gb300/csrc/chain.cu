@@ -1,15 +1,14 @@
 // chain.cu -- one P picture of the encoder hot path on the device, over the
 // leaf CUs of its quadtree: sub-pel planes of every reference and the
 // current picture (interpolate_lcu_row, mc.c:593-785), the batched motion
-// search (xavs2_me_search, me.c:879-1183), each CU's motion-compensated
-// 2Nx2N prediction from its best reference (mc_luma on the frame's sub-pel
-// planes, mc.c:559-589) and residual (pixel_sub_ps, pixel.c:780-792), one
-// CU-sized TU per CU through dct -> quant -> dequant -> idct (tq.cu), and
-// the reconstruction clip(pred + residual) (pixel_add_ps, pixel.c:794-806).
-// The sequence is enqueued on the motion-search session's stream, eagerly
-// or as one captured CUDA graph; an autotuner picks launch shapes that do
-// not change any result.
-#include "xavs2gpu_common.cuh"
+// search (xavs2_me_search, me.c:879-1183), and every inter candidate of every
+// CU through the TU chain (cand.cuh: predictions from the sub-pel planes,
+// residuals, dct -> quant -> dequant -> idct as one TU and as the mode's TU
+// split, SSDs, the reconstruction of each CU's chosen candidate).  The
+// sequence is enqueued on the motion-search session's stream, eagerly or as
+// one captured CUDA graph; an autotuner picks launch shapes that do not
+// change any result.
+#include "cand.cuh"
 
 #include <vector>
 
@@ -18,83 +17,69 @@ namespace xg {
 int tq_batch_launch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
                     int16_t *recon, int32_t *nnz, int warps, cudaStream_t stream);
 
-using CuChoice = xavs2gpu_cu_choice_t;
+// Partition PUs of a CU relative to its 2Nx2N PU: (dx, dy, w, h) in units of
+// S/4, in the order the CU record documents.
+static const int8_t k_modes_big[13][4] = {{0, 0, 4, 4}, {0, 0, 4, 2}, {0, 2, 4, 2}, {0, 0, 2, 4}, {2, 0, 2, 4},
+                                          {0, 0, 4, 1}, {0, 1, 4, 3}, {0, 0, 4, 3}, {0, 3, 4, 1},
+                                          {0, 0, 1, 4}, {1, 0, 3, 4}, {0, 0, 3, 4}, {3, 0, 1, 4}};
 
-__device__ __forceinline__ int square_part(int s) { return s == 8 ? 1 : s == 16 ? 2 : s == 32 ? 3 : 4; }
-
-// Warp per CU: the best reference is the one whose 2Nx2N search returned the
-// smallest cost (the lowest index on ties); the prediction is the sub-pel
-// plane (my&3)*4 + (mx&3) of that reference at the integer part of the MV.
-__global__ void __launch_bounds__(128) mc_residual_kernel(const xavs2gpu_cu_t *__restrict__ cus, int n, int nrefs,
-                                                          const xavs2gpu_me_result_t *__restrict__ res,
-                                                          const uint8_t *__restrict__ cur,
-                                                          const uint8_t *const *__restrict__ planes, int stride, int qp,
-                                                          int16_t *__restrict__ residual,
-                                                          xavs2gpu_tq_block_t *__restrict__ blocks,
-                                                          CuChoice *__restrict__ choice)
+static int part_of(int w, int h)
 {
-    const int lane = threadIdx.x & 31;
-    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (i >= n) return;
-    const xavs2gpu_cu_t c = cus[i];
-    int best = 0, bcost = 0, mvx = 0, mvy = 0;
-    for (int r = 0; r < nrefs; r++) {
-        const xavs2gpu_me_result_t q = res[c.pu[r]];
-        if (r == 0 || q.bcost < bcost) {
-            best = r;
-            bcost = q.bcost;
-            mvx = q.bmv_x;
-            mvy = q.bmv_y;
-        }
-    }
-    const int S = c.size, lg = 31 - __clz(S);
-    const uint8_t *pred = planes[best * 16 + ((mvy & 3) << 2) + (mvx & 3)] +
-                          (ptrdiff_t)(c.y + (mvy >> 2)) * stride + c.x + (mvx >> 2);
-    const uint8_t *src = cur + (ptrdiff_t)c.y * stride + c.x;
-    int16_t *dst = residual + c.offset;
-    for (int e = lane; e < S * S; e += 32) {
-        const int yy = e >> lg, xx = e & (S - 1);
-        dst[e] = (int16_t)((int)src[(ptrdiff_t)yy * stride + xx] - (int)pred[(ptrdiff_t)yy * stride + xx]);
-    }
-    if (lane == 0) {
-        xavs2gpu_tq_block_t b;
-        b.offset = c.offset;
-        b.coef_offset = c.coef_offset;
-        b.part = square_part(S);
-        b.qp = qp;
-        b.flags = 0;
-        b.pad_ = 0;
-        blocks[i] = b;
-        CuChoice ch;
-        ch.ref = best;
-        ch.mv_x = (int16_t)mvx;
-        ch.mv_y = (int16_t)mvy;
-        choice[i] = ch;
-    }
+    for (int k = 0; k < kNumParts; k++)
+        if (h_pu_w[k] == w && h_pu_h[k] == h) return k;
+    return -1;
 }
 
-// Warp per CU: recon = clip(pred + reconstructed residual) into a
-// width-strided picture.
-__global__ void __launch_bounds__(128) reconstruct_kernel(const xavs2gpu_cu_t *__restrict__ cus, int n,
-                                                          const CuChoice *__restrict__ choice,
-                                                          const uint8_t *const *__restrict__ planes, int stride,
-                                                          const int16_t *__restrict__ rres, uint8_t *__restrict__ out,
-                                                          int out_stride)
+// The candidate table of a CU list over a PU list: every partition mode
+// whose PUs follow the CU's 2Nx2N PU for every reference, else the 2Nx2N
+// mode alone.  Returns false if a CU or its 2Nx2N PUs are invalid.
+bool build_candidates(const xavs2gpu_cu_t *cus, int n_cus, const xavs2gpu_pu_t *pus, int n_pus, int W, int H,
+                      int nrefs, std::vector<xavs2gpu_cand_t> &cands, std::vector<int32_t> &cu_cand, int64_t &n_res,
+                      int64_t &n_coef)
 {
-    const int lane = threadIdx.x & 31;
-    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (i >= n) return;
-    const xavs2gpu_cu_t c = cus[i];
-    const CuChoice ch = choice[i];
-    const int S = c.size, lg = 31 - __clz(S);
-    const uint8_t *pred = planes[ch.ref * 16 + ((ch.mv_y & 3) << 2) + (ch.mv_x & 3)] +
-                          (ptrdiff_t)(c.y + (ch.mv_y >> 2)) * stride + c.x + (ch.mv_x >> 2);
-    const int16_t *r = rres + c.offset;
-    uint8_t *o = out + (ptrdiff_t)c.y * out_stride + c.x;
-    for (int e = lane; e < S * S; e += 32) {
-        const int yy = e >> lg, xx = e & (S - 1);
-        o[(ptrdiff_t)yy * out_stride + xx] = clip_pel_d((int)pred[(ptrdiff_t)yy * stride + xx] + r[e]);
+    cands.clear();
+    cu_cand.assign(n_cus + 1, 0);
+    n_res = n_coef = 0;
+    for (int i = 0; i < n_cus; i++) {
+        const xavs2gpu_cu_t &c = cus[i];
+        const int S = c.size;
+        if (!(S == 8 || S == 16 || S == 32 || S == 64) || c.x < 0 || c.y < 0 || c.x + S > W || c.y + S > H)
+            return false;
+        const int nk = S == 8 ? 5 : 13;
+        bool all = true;
+        for (int r = 0; r < nrefs; r++) {
+            const int k0 = c.pu[r];
+            if (k0 < 0 || k0 >= n_pus || pus[k0].x != c.x || pus[k0].y != c.y || pus[k0].part != part_of(S, S) ||
+                pus[k0].ref != r)
+                return false;
+            for (int k = 1; k < nk && all; k++) {
+                const int q = S / 4;
+                const int8_t *m = k_modes_big[k];
+                const int dx = m[0] * q, dy = m[1] * q, w = m[2] * q, h = m[3] * q;
+                all = k0 + k < n_pus && pus[k0 + k].x == c.x + dx && pus[k0 + k].y == c.y + dy &&
+                      pus[k0 + k].part == part_of(w, h) && pus[k0 + k].ref == r;
+            }
+        }
+        const int nmodes = all ? (S == 8 ? 3 : 7) : 1;
+        cu_cand[i] = (int32_t)cands.size();
+        for (int m = 0; m < nmodes; m++) {
+            xavs2gpu_cand_t cd;
+            cd.cu = i;
+            cd.mode = (int8_t)m;
+            const bool nsqt = S > 8;
+            cd.split_type = (int8_t)(!nsqt || m == 0 ? 1 : (m == 1 || m == 3 || m == 4) ? 2 : 3);
+            cd.pad_ = 0;
+            cd.res_offset = n_res;
+            cd.coef_offset = n_coef;
+            n_res += 2 * (int64_t)S * S;
+            // levels packed without gaps: the one TU's, then the split TUs'
+            // (64-point shapes keep a quarter)
+            n_coef += (S == 64 ? 1024 : (int64_t)S * S) + (S == 64 && cd.split_type != 1 ? 1024 : (int64_t)S * S);
+            cands.push_back(cd);
+        }
     }
+    cu_cand[n_cus] = (int32_t)cands.size();
+    return true;
 }
 
 }  // namespace xg
@@ -104,14 +89,18 @@ using namespace xg;
 struct xavs2gpu_chain {
     xavs2gpu_me_session_t *s = nullptr;
     int W = 0, H = 0, nrefs = 0, stride = 0, qp = 0, flags = 0, n_cus = 0, device = 0;
+    int64_t n_cands = 0;
     cudaStream_t st = nullptr;
     xavs2gpu_cu_t *d_cus = nullptr;
+    xavs2gpu_cand_t *d_cands = nullptr;
+    int32_t *d_cu_cand = nullptr, *d_cost = nullptr, *d_dist = nullptr;
     int16_t *d_res = nullptr, *d_rres = nullptr, *d_coef = nullptr;
     int32_t *d_nnz = nullptr;
-    CuChoice *d_choice = nullptr;
+    xavs2gpu_cu_choice_t *d_choice = nullptr;
     xavs2gpu_tq_block_t *d_blocks = nullptr;
     uint8_t *d_src = nullptr, *d_recon = nullptr;
     const uint8_t **d_planes = nullptr;
+    PicView *d_view = nullptr;
     int64_t n_res = 0, n_coef = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -130,16 +119,17 @@ int chain_enqueue(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm)
         if ((rc = xavs2gpu_me_set_picture_device(c->s, r, c->src(1 + r), c->W)) != XAVS2GPU_OK) return rc;
     if ((rc = xavs2gpu_me_set_picture_device(c->s, -1, c->src(0), c->W)) != XAVS2GPU_OK) return rc;
     if ((rc = xavs2gpu_me_run(c->s, prm)) != XAVS2GPU_OK) return rc;
-    const int blocks = (c->n_cus * 32 + 127) / 128;
-    mc_residual_kernel<<<blocks, 128, 0, c->st>>>(c->d_cus, c->n_cus, c->nrefs, xavs2gpu_me_results_device(c->s),
-                                                 xavs2gpu_me_plane_device(c->s, -1, 0), c->d_planes, c->stride,
-                                                 c->qp, c->d_res, c->d_blocks, c->d_choice);
+    const unsigned cand_blocks = (unsigned)((c->n_cands * 32 + 127) / 128);
+    cand_residual_kernel<<<cand_blocks, 128, 0, c->st>>>(c->d_view, 1, c->n_cands, c->qp, c->d_res, c->d_blocks,
+                                                         c->d_cost);
     count_launch();
-    if ((rc = tq_batch_launch(c->d_blocks, c->n_cus, c->d_res, c->d_coef, c->d_rres, c->d_nnz, c->tq_warps, c->st)) !=
-        XAVS2GPU_OK)
+    if ((rc = tq_batch_launch(c->d_blocks, (int)(5 * c->n_cands), c->d_res, c->d_coef, c->d_rres, c->d_nnz,
+                              c->tq_warps, c->st)) != XAVS2GPU_OK)
         return rc;
-    reconstruct_kernel<<<blocks, 128, 0, c->st>>>(c->d_cus, c->n_cus, c->d_choice, c->d_planes, c->stride, c->d_rres,
-                                                 c->d_recon, c->W);
+    cand_eval_kernel<<<cand_blocks, 128, 0, c->st>>>(c->d_view, 1, c->n_cands, c->d_rres, c->d_dist);
+    count_launch();
+    cand_choose_kernel<<<(c->n_cus * 32 + 127) / 128, 128, 0, c->st>>>(c->d_view, 1, c->n_cus, c->d_cost, c->d_dist,
+                                                                       c->d_rres, c->d_choice);
     count_launch();
     if (c->flags & 1) {
         const size_t pic = (size_t)c->W * c->H;
@@ -178,29 +168,22 @@ extern "C" xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, con
     }
     std::vector<xavs2gpu_pu_t> pus(n);
     if (n) xavs2gpu_me_session_pus(s, pus.data());
+    std::vector<xavs2gpu_cand_t> cands;
+    std::vector<int32_t> cu_cand;
     int64_t n_res = 0, n_coef = 0;
-    for (int i = 0; i < n_cus; i++) {
-        const xavs2gpu_cu_t &c = cus[i];
-        const int S = c.size;
-        bool ok = (S == 8 || S == 16 || S == 32 || S == 64) && c.x >= 0 && c.y >= 0 && c.x + S <= W &&
-                  c.y + S <= H && c.offset >= 0 && c.coef_offset >= 0;
-        const int part = S == 8 ? 1 : S == 16 ? 2 : S == 32 ? 3 : 4;
-        for (int r = 0; ok && r < nrefs; r++) {
-            const int k = c.pu[r];
-            ok = k >= 0 && k < n && pus[k].x == c.x && pus[k].y == c.y && pus[k].part == part && pus[k].ref == r;
-        }
-        if (!ok) {
-            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_chain_create",
-                 "CU outside the picture, bad size or offsets, or pu[r] is not its 2Nx2N PU for reference r");
-            return nullptr;
-        }
-        const int64_t nc = S == 64 ? 1024 : (int64_t)S * S;
-        if (c.offset + (int64_t)S * S > n_res) n_res = c.offset + (int64_t)S * S;
-        if (c.coef_offset + nc > n_coef) n_coef = c.coef_offset + nc;
+    if (!build_candidates(cus, n_cus, pus.data(), n, W, H, nrefs, cands, cu_cand, n_res, n_coef)) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_chain_create",
+             "CU outside the picture, bad size, or pu[r] is not its 2Nx2N PU for reference r");
+        return nullptr;
+    }
+    if (5 * (int64_t)cands.size() > INT32_MAX) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_chain_create", "too many candidates");
+        return nullptr;
     }
     auto *c = new xavs2gpu_chain();
     c->s = s;
     c->W = W; c->H = H; c->nrefs = nrefs; c->qp = qp; c->flags = flags; c->n_cus = n_cus;
+    c->n_cands = (int64_t)cands.size();
     c->stride = xavs2gpu_me_plane_stride(s);
     c->st = (cudaStream_t)xavs2gpu_me_stream(s);
     c->device = current_device();
@@ -208,12 +191,19 @@ extern "C" xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, con
     c->n_coef = n_coef;
     XG_CUDA(cudaMalloc((void **)&c->d_cus, sizeof(xavs2gpu_cu_t) * n_cus));
     XG_CUDA(cudaMemcpy(c->d_cus, cus, sizeof(xavs2gpu_cu_t) * n_cus, cudaMemcpyHostToDevice));
+    XG_CUDA(cudaMalloc((void **)&c->d_cands, sizeof(xavs2gpu_cand_t) * cands.size()));
+    XG_CUDA(cudaMemcpy(c->d_cands, cands.data(), sizeof(xavs2gpu_cand_t) * cands.size(), cudaMemcpyHostToDevice));
+    XG_CUDA(cudaMalloc((void **)&c->d_cu_cand, sizeof(int32_t) * cu_cand.size()));
+    XG_CUDA(cudaMemcpy(c->d_cu_cand, cu_cand.data(), sizeof(int32_t) * cu_cand.size(), cudaMemcpyHostToDevice));
+    XG_CUDA(cudaMalloc((void **)&c->d_cost, sizeof(int32_t) * c->n_cands));
+    XG_CUDA(cudaMalloc((void **)&c->d_dist, sizeof(int32_t) * 2 * c->n_cands));
     XG_CUDA(cudaMalloc((void **)&c->d_res, sizeof(int16_t) * n_res));
     XG_CUDA(cudaMalloc((void **)&c->d_rres, sizeof(int16_t) * n_res));
     XG_CUDA(cudaMalloc((void **)&c->d_coef, sizeof(int16_t) * n_coef));
-    XG_CUDA(cudaMalloc((void **)&c->d_nnz, sizeof(int32_t) * n_cus));
-    XG_CUDA(cudaMalloc((void **)&c->d_choice, sizeof(CuChoice) * n_cus));
-    XG_CUDA(cudaMalloc((void **)&c->d_blocks, sizeof(xavs2gpu_tq_block_t) * n_cus));
+    XG_CUDA(cudaMemset(c->d_coef, 0, sizeof(int16_t) * n_coef));
+    XG_CUDA(cudaMalloc((void **)&c->d_nnz, sizeof(int32_t) * 5 * c->n_cands));
+    XG_CUDA(cudaMalloc((void **)&c->d_choice, sizeof(xavs2gpu_cu_choice_t) * n_cus));
+    XG_CUDA(cudaMalloc((void **)&c->d_blocks, sizeof(xavs2gpu_tq_block_t) * 5 * c->n_cands));
     XG_CUDA(cudaMalloc((void **)&c->d_src, (size_t)W * H * (1 + nrefs)));
     XG_CUDA(cudaMemset(c->d_src, 0, (size_t)W * H * (1 + nrefs)));
     XG_CUDA(cudaMalloc((void **)&c->d_recon, (size_t)W * H));
@@ -222,6 +212,26 @@ extern "C" xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, con
         for (int k = 0; k < 16; k++) planes[16 * r + k] = xavs2gpu_me_plane_device(s, r, k);
     XG_CUDA(cudaMalloc((void **)&c->d_planes, sizeof(uint8_t *) * planes.size()));
     XG_CUDA(cudaMemcpy(c->d_planes, planes.data(), sizeof(uint8_t *) * planes.size(), cudaMemcpyHostToDevice));
+    PicView v{};
+    v.cur = xavs2gpu_me_plane_device(s, -1, 0);
+    v.planes = c->d_planes;
+    v.res = xavs2gpu_me_results_device(s);
+    v.cus = c->d_cus;
+    v.cands = c->d_cands;
+    v.cu_cand = c->d_cu_cand;
+    v.recon = c->d_recon;
+    v.hash = nullptr;
+    v.res_off = v.coef_off = v.cu_start = v.cand_start = 0;
+    v.n_coef = n_coef;
+    v.n_cus = n_cus;
+    v.n_cands = (int)c->n_cands;
+    v.stride = c->stride;
+    v.width = W;
+    v.height = H;
+    v.nrefs = nrefs;
+    v.n_pus = n;
+    XG_CUDA(cudaMalloc((void **)&c->d_view, sizeof(PicView)));
+    XG_CUDA(cudaMemcpy(c->d_view, &v, sizeof(PicView), cudaMemcpyHostToDevice));
     return c;
 }
 
@@ -233,7 +243,8 @@ extern "C" void xavs2gpu_chain_destroy(xavs2gpu_chain_t *c)
     drop_graph(c);
     cudaFree(c->d_cus); cudaFree(c->d_res); cudaFree(c->d_rres); cudaFree(c->d_coef); cudaFree(c->d_nnz);
     cudaFree(c->d_choice); cudaFree(c->d_blocks); cudaFree(c->d_src); cudaFree(c->d_recon);
-    cudaFree((void *)c->d_planes);
+    cudaFree((void *)c->d_planes); cudaFree(c->d_cands); cudaFree(c->d_cu_cand); cudaFree(c->d_cost);
+    cudaFree(c->d_dist); cudaFree(c->d_view);
     delete c;
 }
 
@@ -309,6 +320,10 @@ extern "C" int xavs2gpu_chain_get_outputs(xavs2gpu_chain_t *c, xavs2gpu_chain_ou
     o->choice = c->d_choice;
     o->n_residual = c->n_res;
     o->n_coef = c->n_coef;
+    o->cands = c->d_cands;
+    o->cand_cost = c->d_cost;
+    o->dist = c->d_dist;
+    o->n_cands = c->n_cands;
     return XAVS2GPU_OK;
 }
 

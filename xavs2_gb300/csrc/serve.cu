@@ -6,18 +6,20 @@
 //   reference 0, xavs2gpu_me_rotate_refs), sub-pel planes of the new
 //   reference, current picture;
 //   then for the whole batch: the motion search of every picture's leaf-CU
-//   PUs (xavs2gpu_me_batch_run), the motion-compensated residual of every
-//   CU from its best reference, one TU chain over all CUs (tq.cu), the
+//   PUs (xavs2gpu_me_batch_run), every inter candidate of every CU through
+//   the TU chain as the full-picture chain runs it (cand.cuh: predictions,
+//   residuals, one TU and the split TUs, SSDs), each CU's chosen
 //   reconstruction, and a per-picture checksum of levels, reconstruction and
 //   MVs.
 // Each stream's references and sub-pel planes stay resident in its own
-// motion-search session.  Streams are admitted against a device-memory
-// budget, pictures against the pixel capacity of the batch buffers; two
+// motion-search session.  Streams are admitted against the device's free
+// memory and an optional budget, pictures against the pixel capacity of the
+// batch buffers; two
 // batch buffer sets on two CUDA streams let the next batch be prepared and
 // enqueued while the current one runs.  A picture of a stream is only
 // batched once the stream's previous picture has completed, so every
 // result is independent of what else shares its batch.
-#include "xavs2gpu_common.cuh"
+#include "cand.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -39,102 +41,13 @@ namespace xg {
 
 int tq_batch_launch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
                     int16_t *recon, int32_t *nnz, int warps, cudaStream_t stream);
+bool build_candidates(const xavs2gpu_cu_t *cus, int n_cus, const xavs2gpu_pu_t *pus, int n_pus, int W, int H,
+                      int nrefs, std::vector<xavs2gpu_cand_t> &cands, std::vector<int32_t> &cu_cand, int64_t &n_res,
+                      int64_t &n_coef);
 
 namespace srv {
 
-// One picture of a batch as the kernels see it.
-struct JobView {
-    const uint8_t *cur;                 // current picture (session plane, stride `stride`)
-    const uint8_t *const *planes;       // reference planes, 16 r + k
-    const xavs2gpu_me_result_t *res;    // the session's search results
-    const xavs2gpu_cu_t *cus;           // the stream's leaf CUs (stream-local offsets)
-    uint8_t *recon;                     // reconstructed picture (stride `width`)
-    unsigned long long *hash;
-    int64_t res_off, coef_off;          // the picture's base in the batch residual / level buffers
-    int64_t cu_start;                   // first batch-wide CU index of the picture
-    int64_t n_coef;                     // levels of the picture
-    int n_cus, stride, width, height, nrefs, n_pus;
-};
-
-__device__ __forceinline__ int find_job(const JobView *v, int njobs, int64_t i)
-{
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (v[mid].cu_start <= i) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Warp per CU: best reference (smallest 2Nx2N cost, lowest index on ties),
-// prediction from its sub-pel plane, residual and TU descriptor.
-__global__ void __launch_bounds__(128) mc_residual_kernel(const JobView *__restrict__ views, int njobs, int64_t n,
-                                                          int qp, int16_t *__restrict__ residual,
-                                                          xavs2gpu_tq_block_t *__restrict__ blocks,
-                                                          xavs2gpu_cu_choice_t *__restrict__ choice)
-{
-    const int lane = threadIdx.x & 31;
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const JobView &v = views[find_job(views, njobs, i)];
-    const xavs2gpu_cu_t c = v.cus[i - v.cu_start];
-    int best = 0, bcost = 0, mvx = 0, mvy = 0;
-    for (int r = 0; r < v.nrefs; r++) {
-        const xavs2gpu_me_result_t q = v.res[c.pu[r]];
-        if (r == 0 || q.bcost < bcost) {
-            best = r;
-            bcost = q.bcost;
-            mvx = q.bmv_x;
-            mvy = q.bmv_y;
-        }
-    }
-    const int S = c.size, lg = 31 - __clz(S);
-    const uint8_t *pred = v.planes[best * 16 + ((mvy & 3) << 2) + (mvx & 3)] +
-                          (ptrdiff_t)(c.y + (mvy >> 2)) * v.stride + c.x + (mvx >> 2);
-    const uint8_t *src = v.cur + (ptrdiff_t)c.y * v.stride + c.x;
-    int16_t *dst = residual + v.res_off + c.offset;
-    for (int e = lane; e < S * S; e += 32) {
-        const int yy = e >> lg, xx = e & (S - 1);
-        dst[e] = (int16_t)((int)src[(ptrdiff_t)yy * v.stride + xx] - (int)pred[(ptrdiff_t)yy * v.stride + xx]);
-    }
-    if (lane == 0) {
-        xavs2gpu_tq_block_t b;
-        b.offset = v.res_off + c.offset;
-        b.coef_offset = v.coef_off + c.coef_offset;
-        b.part = S == 8 ? 1 : S == 16 ? 2 : S == 32 ? 3 : 4;
-        b.qp = qp;
-        b.flags = 0;
-        b.pad_ = 0;
-        blocks[i] = b;
-        xavs2gpu_cu_choice_t ch;
-        ch.ref = best;
-        ch.mv_x = (int16_t)mvx;
-        ch.mv_y = (int16_t)mvy;
-        choice[i] = ch;
-    }
-}
-
-__global__ void __launch_bounds__(128) reconstruct_kernel(const JobView *__restrict__ views, int njobs, int64_t n,
-                                                          const xavs2gpu_cu_choice_t *__restrict__ choice,
-                                                          const int16_t *__restrict__ rres)
-{
-    const int lane = threadIdx.x & 31;
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const JobView &v = views[find_job(views, njobs, i)];
-    const xavs2gpu_cu_t c = v.cus[i - v.cu_start];
-    const xavs2gpu_cu_choice_t ch = choice[i];
-    const int S = c.size, lg = 31 - __clz(S);
-    const uint8_t *pred = v.planes[ch.ref * 16 + ((ch.mv_y & 3) << 2) + (ch.mv_x & 3)] +
-                          (ptrdiff_t)(c.y + (ch.mv_y >> 2)) * v.stride + c.x + (ch.mv_x >> 2);
-    const int16_t *r = rres + v.res_off + c.offset;
-    uint8_t *o = v.recon + (ptrdiff_t)c.y * v.width + c.x;
-    for (int e = lane; e < S * S; e += 32) {
-        const int yy = e >> lg, xx = e & (S - 1);
-        o[(ptrdiff_t)yy * v.width + xx] = clip_pel_d((int)pred[(ptrdiff_t)yy * v.stride + xx] + r[e]);
-    }
-}
+using JobView = PicView;   // one picture of a batch as the kernels see it
 
 // Checksum of a picture's outputs: sum over the 32-bit words w_i of
 // [reconstruction (width*height bytes) | levels (int16 pairs) | search
@@ -174,7 +87,9 @@ struct Stream {
     int id = 0, W = 0, H = 0, nrefs = 2;
     xavs2gpu_me_session_t *sess = nullptr;
     xavs2gpu_cu_t *d_cus = nullptr;
-    int n_cus = 0, n_pus = 0;
+    xavs2gpu_cand_t *d_cands = nullptr;
+    int32_t *d_cu_cand = nullptr;
+    int n_cus = 0, n_pus = 0, n_cands = 0;
     int64_t n_res = 0, n_coef = 0;
     uint8_t *d_in = nullptr, *d_prev = nullptr;   // upload buffer, previous picture (next reference)
     uint8_t *h_ring = nullptr;                    // pinned picture slots
@@ -195,7 +110,7 @@ struct BatchSet {
     cudaEvent_t start = nullptr, done = nullptr;
     int16_t *d_res = nullptr, *d_rres = nullptr, *d_coef = nullptr;
     uint8_t *d_recon = nullptr;
-    int32_t *d_nnz = nullptr;
+    int32_t *d_nnz = nullptr, *d_cost = nullptr, *d_dist = nullptr;
     xavs2gpu_tq_block_t *d_blocks = nullptr;
     xavs2gpu_cu_choice_t *d_choice = nullptr;
     JobView *d_views = nullptr;
@@ -217,7 +132,8 @@ struct xavs2gpu_server {
     xavs2gpu_server_config_t cfg{};
     int device = 0;
     int64_t hbm_used = 0;
-    int64_t max_cus = 0;
+    int64_t hbm_pending = 0;                  // admitted streams whose memory is not allocated yet
+    int64_t max_cus = 0, max_cands = 0;
     std::vector<Stream *> streams;
     BatchSet sets[XG_SERVE_SETS];
     int next_set = 0;
@@ -243,7 +159,7 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
     std::vector<xavs2gpu_me_session_t *> sess;
     b.searched.clear();
     XG_CUDA(cudaEventRecord(b.start, b.st));
-    int64_t res_off = 0, coef_off = 0, cu_start = 0, rec_off = 0;
+    int64_t res_off = 0, coef_off = 0, cu_start = 0, cand_start = 0, rec_off = 0;
     int nv = 0;
     for (size_t k = 0; k < b.jobs.size(); k++) {
         Job &j = b.jobs[k];
@@ -264,12 +180,16 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
             v.planes = xavs2gpu_me_plane_table_device(S.sess);
             v.res = xavs2gpu_me_results_device(S.sess);
             v.cus = S.d_cus;
+            v.cands = S.d_cands;
+            v.cu_cand = S.d_cu_cand;
             v.recon = b.d_recon + rec_off;
             v.hash = b.d_hash + (nv - 1);
             v.res_off = res_off;
             v.coef_off = coef_off;
             v.cu_start = cu_start;
+            v.cand_start = cand_start;
             v.n_cus = S.n_cus;
+            v.n_cands = S.n_cands;
             v.n_coef = S.n_coef;
             v.stride = xavs2gpu_me_plane_stride(S.sess);
             v.width = S.W;
@@ -279,6 +199,7 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
             res_off += S.n_res;
             coef_off += S.n_coef;
             cu_start += S.n_cus;
+            cand_start += S.n_cands;
             rec_off += (int64_t)pic;
         }
         std::swap(S.d_in, S.d_prev);
@@ -288,11 +209,13 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
         xavs2gpu_me_batch_run(b.me, sess.data(), (int)sess.size(), &s->cfg.me, b.st);
         XG_CUDA(cudaMemcpyAsync(b.d_views, b.h_views, sizeof(JobView) * nv, cudaMemcpyHostToDevice, b.st));
         XG_CUDA(cudaMemsetAsync(b.d_hash, 0, sizeof(unsigned long long) * nv, b.st));
-        const int64_t n = cu_start;
-        const unsigned blocks = (unsigned)((n * 32 + 127) / 128);
-        mc_residual_kernel<<<blocks, 128, 0, b.st>>>(b.d_views, nv, n, s->cfg.qp, b.d_res, b.d_blocks, b.d_choice);
-        tq_batch_launch(b.d_blocks, (int)n, b.d_res, b.d_coef, b.d_rres, b.d_nnz, 4, b.st);
-        reconstruct_kernel<<<blocks, 128, 0, b.st>>>(b.d_views, nv, n, b.d_choice, b.d_rres);
+        const int64_t nc = cand_start, ncu = cu_start;
+        const unsigned cblocks = (unsigned)((nc * 32 + 127) / 128);
+        cand_residual_kernel<<<cblocks, 128, 0, b.st>>>(b.d_views, nv, nc, s->cfg.qp, b.d_res, b.d_blocks, b.d_cost);
+        tq_batch_launch(b.d_blocks, (int)(5 * nc), b.d_res, b.d_coef, b.d_rres, b.d_nnz, 4, b.st);
+        cand_eval_kernel<<<cblocks, 128, 0, b.st>>>(b.d_views, nv, nc, b.d_rres, b.d_dist);
+        cand_choose_kernel<<<(unsigned)((ncu * 32 + 127) / 128), 128, 0, b.st>>>(b.d_views, nv, ncu, b.d_cost,
+                                                                                 b.d_dist, b.d_rres, b.d_choice);
         int64_t max_words = 0;
         for (int k = 0; k < nv; k++) {
             const JobView &v = b.h_views[k];
@@ -301,7 +224,7 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
         // about 8 words of the largest picture per thread
         const unsigned hx = (unsigned)std::min<int64_t>(std::max<int64_t>((max_words + 2047) / 2048, 1), 4096);
         hash_kernel<<<dim3(hx, nv), 256, 0, b.st>>>(b.d_views, b.d_coef);
-        count_launch(3);
+        count_launch(4);
         XG_CUDA(cudaMemcpyAsync(b.h_hash, b.d_hash, sizeof(unsigned long long) * nv, cudaMemcpyDeviceToHost, b.st));
     }
     XG_CUDA(cudaEventRecord(b.done, b.st));
@@ -402,6 +325,7 @@ void free_set(BatchSet &b)
 {
     cudaFree(b.d_res); cudaFree(b.d_rres); cudaFree(b.d_coef); cudaFree(b.d_recon); cudaFree(b.d_nnz);
     cudaFree(b.d_blocks); cudaFree(b.d_choice); cudaFree(b.d_views); cudaFree(b.d_hash);
+    cudaFree(b.d_cost); cudaFree(b.d_dist);
     cudaFreeHost(b.h_hash); cudaFreeHost(b.h_views);
     if (b.me) xavs2gpu_me_batch_destroy(b.me);
     if (b.done) cudaEventDestroy(b.done);
@@ -423,23 +347,30 @@ extern "C" xavs2gpu_server_t *xavs2gpu_server_create(const xavs2gpu_server_confi
     s->device = current_device();
     const int64_t px = cfg->max_batch_pixels;
     s->max_cus = frame_cap_cus(px);
+    s->max_cands = 7 * s->max_cus;
+    // candidate residual / level regions: 2 S^2 per mode, at most 7 modes per
+    // CU, so at most 14 elements per luma pixel of a batch
+    const int64_t nres = 14 * px;
     for (auto &b : s->sets) {
         XG_CUDA(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
         XG_CUDA(cudaEventCreate(&b.start));
         XG_CUDA(cudaEventCreate(&b.done));
-        XG_CUDA(cudaMalloc((void **)&b.d_res, sizeof(int16_t) * px));
-        XG_CUDA(cudaMalloc((void **)&b.d_rres, sizeof(int16_t) * px));
-        XG_CUDA(cudaMalloc((void **)&b.d_coef, sizeof(int16_t) * px));
+        XG_CUDA(cudaMalloc((void **)&b.d_res, sizeof(int16_t) * nres));
+        XG_CUDA(cudaMalloc((void **)&b.d_rres, sizeof(int16_t) * nres));
+        XG_CUDA(cudaMalloc((void **)&b.d_coef, sizeof(int16_t) * nres));
+        XG_CUDA(cudaMemset(b.d_coef, 0, sizeof(int16_t) * nres));
         XG_CUDA(cudaMalloc((void **)&b.d_recon, px));
-        XG_CUDA(cudaMalloc((void **)&b.d_nnz, sizeof(int32_t) * s->max_cus));
-        XG_CUDA(cudaMalloc((void **)&b.d_blocks, sizeof(xavs2gpu_tq_block_t) * s->max_cus));
+        XG_CUDA(cudaMalloc((void **)&b.d_nnz, sizeof(int32_t) * 5 * s->max_cands));
+        XG_CUDA(cudaMalloc((void **)&b.d_blocks, sizeof(xavs2gpu_tq_block_t) * 5 * s->max_cands));
+        XG_CUDA(cudaMalloc((void **)&b.d_cost, sizeof(int32_t) * s->max_cands));
+        XG_CUDA(cudaMalloc((void **)&b.d_dist, sizeof(int32_t) * 2 * s->max_cands));
         XG_CUDA(cudaMalloc((void **)&b.d_choice, sizeof(xavs2gpu_cu_choice_t) * s->max_cus));
         XG_CUDA(cudaMalloc((void **)&b.d_views, sizeof(JobView) * 256));
         XG_CUDA(cudaMalloc((void **)&b.d_hash, sizeof(unsigned long long) * 256));
         XG_CUDA(cudaMallocHost((void **)&b.h_hash, sizeof(unsigned long long) * 256));
         XG_CUDA(cudaMallocHost((void **)&b.h_views, sizeof(JobView) * 256));
         b.me = xavs2gpu_me_batch_create();
-        s->hbm_used += px * 7 + s->max_cus * 44;
+        s->hbm_used += px + 3 * 2 * nres + s->max_cands * (5 * (32 + 4) + 12) + s->max_cus * 8;
     }
     if (cfg->hbm_budget_bytes > 0 && s->hbm_used > cfg->hbm_budget_bytes) {
         for (auto &b : s->sets) free_set(b);
@@ -470,6 +401,7 @@ extern "C" void xavs2gpu_server_destroy(xavs2gpu_server_t *s)
         xavs2gpu_me_set_stream(S->sess, nullptr);
         xavs2gpu_me_destroy(S->sess);
         cudaFree(S->d_cus); cudaFree(S->d_in); cudaFree(S->d_prev); cudaFreeHost(S->h_ring);
+        cudaFree(S->d_cands); cudaFree(S->d_cu_cand);
         delete S;
     }
     for (auto &b : s->sets) free_set(b);
@@ -487,16 +419,41 @@ extern "C" int xavs2gpu_server_open_stream(xavs2gpu_server_t *s, int width, int 
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_server_open_stream", "picture larger than a batch, or width not a multiple of 4");
         return -XAVS2GPU_ERR_ARG;
     }
-    // resident device memory of the stream: 33 padded planes, PU arrays, CUs, two pictures
+    // the stream's candidates (validates the CU list against its PUs); the
+    // leaf CUs tile the picture, so the batch buffers sized per luma pixel hold them
+    std::vector<xavs2gpu_cand_t> cands;
+    std::vector<int32_t> cu_cand;
+    int64_t n_res = 0, n_coef = 0;
+    if (!build_candidates(cus, n_cus, pus, n_pus, width, height, 2, cands, cu_cand, n_res, n_coef) ||
+        (int64_t)n_cus > (int64_t)width * height / 64 || n_res > 14 * (int64_t)width * height) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_server_open_stream", "CU list does not tile the picture over its 2Nx2N PUs");
+        return -XAVS2GPU_ERR_ARG;
+    }
+    // resident device memory of the stream: 33 padded planes, PU arrays, CUs,
+    // candidates, two pictures
     const int64_t plane = (int64_t)((width + 160 + 63) / 64 * 64) * (height + 160);
-    const int64_t need = 33 * plane + (int64_t)n_pus * (18 + 20 + 8 + 12 + 16) + (int64_t)n_cus * 40 +
-                         2 * (int64_t)width * height + (int64_t)n_cus * 849 * 4 / 16;
+    const int64_t need = 33 * plane + (int64_t)n_pus * (18 + 20 + 8 + 12 + 16) + (int64_t)n_cus * 44 +
+                         (int64_t)cands.size() * 24 + 2 * (int64_t)width * height + (int64_t)n_cus * 849 * 4 / 16;
     std::unique_lock<std::mutex> lk(s->mu);
     if (s->cfg.hbm_budget_bytes > 0 && s->hbm_used + need > s->cfg.hbm_budget_bytes) {
         fail(XAVS2GPU_ERR_CAPACITY, "xavs2gpu_server_open_stream", "device-memory budget exhausted");
         return -XAVS2GPU_ERR_CAPACITY;
     }
+    // admission by the device's free memory now, less the reserve and what
+    // streams admitted before us still have to allocate
+    {
+        size_t free_b = 0, total_b = 0;
+        XG_CUDA(cudaSetDevice(s->device));
+        XG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const int64_t reserve = s->cfg.hbm_reserve_bytes > 0 ? s->cfg.hbm_reserve_bytes
+                                                            : std::max<int64_t>((int64_t)total_b / 32, (int64_t)1 << 30);
+        if (need + s->hbm_pending > (int64_t)free_b - reserve) {
+            fail(XAVS2GPU_ERR_CAPACITY, "xavs2gpu_server_open_stream", "not enough free device memory");
+            return -XAVS2GPU_ERR_CAPACITY;
+        }
+    }
     s->hbm_used += need;
+    s->hbm_pending += need;
     lk.unlock();
     auto *S = new Stream();
     S->W = width;
@@ -510,24 +467,25 @@ extern "C" int xavs2gpu_server_open_stream(xavs2gpu_server_t *s, int width, int 
         delete S;
         lk.lock();
         s->hbm_used -= need;
+        s->hbm_pending -= need;
         return -XAVS2GPU_ERR_ARG;
-    }
-    int64_t n_res = 0, n_coef = 0;
-    for (int i = 0; i < n_cus; i++) {
-        const int sz = cus[i].size;
-        n_res = std::max<int64_t>(n_res, cus[i].offset + (int64_t)sz * sz);
-        n_coef = std::max<int64_t>(n_coef, cus[i].coef_offset + (sz == 64 ? 1024 : (int64_t)sz * sz));
     }
     S->n_res = n_res;
     S->n_coef = n_coef;
+    S->n_cands = (int)cands.size();
     S->bytes = need;
     S->ring = ring;
     XG_CUDA(cudaMalloc((void **)&S->d_cus, sizeof(xavs2gpu_cu_t) * n_cus));
     XG_CUDA(cudaMemcpy(S->d_cus, cus, sizeof(xavs2gpu_cu_t) * n_cus, cudaMemcpyHostToDevice));
+    XG_CUDA(cudaMalloc((void **)&S->d_cands, sizeof(xavs2gpu_cand_t) * cands.size()));
+    XG_CUDA(cudaMemcpy(S->d_cands, cands.data(), sizeof(xavs2gpu_cand_t) * cands.size(), cudaMemcpyHostToDevice));
+    XG_CUDA(cudaMalloc((void **)&S->d_cu_cand, sizeof(int32_t) * cu_cand.size()));
+    XG_CUDA(cudaMemcpy(S->d_cu_cand, cu_cand.data(), sizeof(int32_t) * cu_cand.size(), cudaMemcpyHostToDevice));
     XG_CUDA(cudaMalloc((void **)&S->d_in, (size_t)width * height));
     XG_CUDA(cudaMalloc((void **)&S->d_prev, (size_t)width * height));
     XG_CUDA(cudaMallocHost((void **)&S->h_ring, (size_t)width * height * ring));
     lk.lock();
+    s->hbm_pending -= need;
     S->id = (int)s->streams.size();
     s->streams.push_back(S);
     return S->id;
