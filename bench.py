@@ -594,23 +594,26 @@ def run_tq(args):
                               "GBs": algo_bytes / (kernel_ms / 1e3) / 1e9, "parts": args.tq_parts, "blocks": n}))
         return
 
-    # end to end with host buffers: pinned residual in, levels + recon + nnz out
+    # end to end through the host-buffer entry (xavs2gpu_tq_batch_host):
+    # page-locked descriptors and residual in, levels + recon + nnz out, the
+    # copies overlapped with the chain in chunks
     h_res = d_res.cpu().pin_memory()
     h_blocks = torch.from_numpy(blocks.view(np.uint8).copy()).pin_memory()
     h_coef = torch.empty(ncoef, dtype=torch.int16).pin_memory()
     h_rec = torch.empty(nres, dtype=torch.int16).pin_memory()
     h_nnz = torch.empty(n, dtype=torch.int32).pin_memory()
+    tq_host = xg.fn("xavs2gpu_tq_batch_host")
+
+    def step_host():
+        rc = tq_host(h_blocks.data_ptr(), n, h_res.data_ptr(), h_coef.data_ptr(), h_rec.data_ptr(),
+                     h_nnz.data_ptr(), args.tq_chunks)
+        assert rc == 0
+
+    step_host()      # device buffers of the host entry allocated outside the timed region
     barrier()
     t0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            d_blocks.copy_(h_blocks, non_blocking=True)
-            d_res.copy_(h_res, non_blocking=True)
-            step(stream)
-            h_coef.copy_(d_coef, non_blocking=True)
-            h_rec.copy_(d_rec, non_blocking=True)
-            h_nnz.copy_(d_nnz, non_blocking=True)
-        stream.synchronize()
+    for i in range(args.steps):
+        step_host()
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_s = reduce_max(e2e_s, dev)
@@ -642,7 +645,9 @@ def run_tq(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16", "data": "synthetic", "config": cfg,
         "e2e": {"value": e2e, "unit": "blocks/s", "h2d_bytes_per_step": int(2 * nres + 32 * n),
-                "d2h_bytes_per_step": int(2 * ncoef + 2 * nres + 4 * n)},
+                "d2h_bytes_per_step": int(2 * ncoef + 2 * nres + 4 * n),
+                "call": "xavs2gpu_tq_batch_host, page-locked buffers, %d chunks" % args.tq_chunks,
+                "host_link_gbs": (4 * nres + 2 * ncoef + 36 * n) * args.steps / e2e_s / 1e9},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "tq_batch", "achieved": achieved,
                      "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
@@ -1425,6 +1430,7 @@ def serve_trace(xg, srv, streams, pools, duration, warm, rate, seed):
     submitted = [0]
     deadline = [0.0]
     fails = 0
+    accepted = {sid: [] for sid in range(len(streams))}   # pool index of each accepted picture, in order
     th = threading.Thread(target=collect)
     th.start()
     t0 = time.perf_counter()
@@ -1436,6 +1442,7 @@ def serve_trace(xg, srv, streams, pools, duration, warm, rate, seed):
         pool = pools[res]
         if srv.submit(sid, pool[k % len(pool)], tag=int(t * 1e9)) == 0:
             submitted[0] += 1
+            accepted[sid].append(k % len(pool))
         else:
             fails += 1
     deadline[0] = time.time() + 30.0
@@ -1443,7 +1450,7 @@ def serve_trace(xg, srv, streams, pools, duration, warm, rate, seed):
     th.join()
     arr = np.array(results, dtype=xg.SERVER_RESULT_DTYPE)
     keep = (arr["ref_only"] == 0) & (arr["tag"] >= int(warm * 1e9))
-    return arr[keep], fails, len(events), t0_ns
+    return arr[keep], fails, len(events), accepted
 
 
 def serve_summary(arr, window):
@@ -1453,6 +1460,59 @@ def serve_summary(arr, window):
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "frames": int(len(lat)), "frames_per_s": float(len(lat) / window),
             "mean_batch_frames": float(arr["batch_frames"].mean())}
+
+
+def serve_parity(xg, arr, streams, layouts, res_idx, pools, accepted, prm, n_pictures=3, n_cus=12):
+    """Served pictures against the full-picture chain and the oracle: for up
+    to n_pictures served pictures (the largest resolutions first), the chain
+    on the same current picture and references (picture k of a stream is the
+    k-th picture the server accepted from it) gives the same checksum, and
+    the chain's outputs match the oracle on n_cus seeded CUs."""
+    import oracle
+    lib = xg.load()
+    cand = arr[arr["frame"] >= 2]
+    order = sorted(range(len(cand)), key=lambda i: (-int(res_idx[int(cand["stream"][i])]), i))
+    seen, picked = set(), []
+    for i in order:
+        r = int(res_idx[int(cand["stream"][i])])
+        if r not in seen:
+            seen.add(r)
+            picked.append(cand[i])
+        if len(picked) == n_pictures:
+            break
+    checked, mism, first, n_pu, n_cd = 0, 0, None, 0, 0
+    for rec in picked:
+        sid, f = int(rec["stream"]), int(rec["frame"])
+        pool = pools[streams[sid][0]]
+        cur, r0, r1 = (pool[accepted[sid][k]] for k in (f, f - 1, f - 2))
+        h, w = cur.shape
+        pus, cus = layouts[sid]
+        sess = xg.MeSession(w, h, 2, len(pus))
+        sess.set_pus(pus)
+        chain = xg.Chain(sess, cus, QP)
+        for idx, img in enumerate([cur, r0, r1]):
+            assert lib.xavs2gpu_copy_h2d(ctypes.c_void_p(chain.source(idx)), xg.ptr(img), img.nbytes) == 0
+        chain.run(prm)
+        out = chain.download()
+        want = xg.output_hash(out["recon"], out["coef"], sess.results())
+        checked += 1
+        if int(rec["hash"]) != want:
+            mism += 1
+            first = first or "hash of stream %d picture %d" % (sid, f)
+        rng = np.random.default_rng(sid)
+        cu_idx = np.sort(rng.choice(len(cus), min(n_cus, len(cus)), replace=False))
+        a, b, bad = oracle.chain_sample_check(oracle.lib(), out, cur, [r0, r1], pus, cus, sess.results(),
+                                              (prm.search_range, prm.lambda_factor, 1, 2, 0, 0), QP, cu_idx,
+                                              os.cpu_count() or 1)
+        n_pu += a
+        n_cd += b
+        if bad:
+            mism += len(bad)
+            first = first or bad[0]
+        chain.close()
+        sess.close()
+    return {"pictures": checked, "checked_pu_searches": n_pu, "checked_candidates": n_cd, "mismatches": mism,
+            "first": first, "against": "full-picture chain (checksum) and oracle (sampled CUs)"}
 
 
 def run_serve(args):
@@ -1492,12 +1552,13 @@ def run_serve(args):
     launches0 = lib.xavs2gpu_kernel_launches()
     srv, streams = make_server(args.serve_batch)
     clk.start()
-    arr, fails, n_events, _ = serve_trace(xg, srv, streams, pools, args.serve_seconds, args.serve_warm, rate, 5)
+    arr, fails, n_events, accepted = serve_trace(xg, srv, streams, pools, args.serve_seconds, args.serve_warm, rate, 5)
     clocks = clk.stop()
     stats = srv.stats()
     srv.close()
     launches = lib.xavs2gpu_kernel_launches() - launches0
     batched = serve_summary(arr, window)
+    parity = serve_parity(xg, arr, streams, layouts, res_idx, pools, accepted, prm)
     # the same trace, each picture alone (one picture per batch)
     srv1, streams1 = make_server(1)
     arr1, fails1, _, _ = serve_trace(xg, srv1, streams1, pools, args.serve_seconds, args.serve_warm, rate, 5)
@@ -1519,16 +1580,20 @@ def run_serve(args):
                    "search_range": args.serve_range, "qp": QP, "refs": 2,
                    "batch_cap": {"pictures": args.serve_batch, "luma_mpx": args.serve_batch_mpx},
                    "picture_job": "reference update + sub-pel planes, FS +-%d + quarter-pel SATD over the leaf-CU "
-                                  "PUs of a seeded split map, MC residual, TU chain, reconstruction" % args.serve_range},
+                                  "PUs of a seeded split map, every inter candidate through the TU chain (one TU and "
+                                  "the TU split), choice, reconstruction" % args.serve_range},
         "batched": batched, "unbatched_same_trace": alone,
         "submit_failures": {"batched": fails, "unbatched": fails1}, "offered_pictures": n_events,
         "server": stats,
         "e2e": {"value": batched.get("frames_per_s"), "unit": "pictures/s",
                 "h2d_bytes_per_step": int(mean_px), "d2h_bytes_per_step": 8},
         "gpu_launches": int(launches),
+        "parity": parity,
         "clocks": clocks,
     }
     print(json.dumps(line))
+    if parity.get("mismatches"):
+        sys.exit("bench: served pictures differ: %s" % parity["first"])
 
 
 def chain_parity(xg, chain, sess, order, pus, cus, prm_tuple, n_cus, seed):
@@ -1700,10 +1765,11 @@ def main():
     ap.add_argument("--chain-height", type=int, default=2160)
     ap.add_argument("--tq-blocks", type=int, default=1000000)
     ap.add_argument("--tq-parts", default="0,1,2,3,4", help="TU shapes (LumaPU indices) of the tq workload")
+    ap.add_argument("--tq-chunks", type=int, default=16, help="tq e2e: chunks the host entry overlaps")
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     ap.add_argument("--serve-warm", type=float, default=2.0)
-    ap.add_argument("--serve-range", type=int, default=16)
+    ap.add_argument("--serve-range", type=int, default=64)
     ap.add_argument("--serve-batch", type=int, default=64)
     # luma pixels per batch (MiB): about one and a half 2160p pictures keeps a
     # burst of arrivals from forming one long batch (p99 11.7 ms against 16-19

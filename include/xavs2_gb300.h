@@ -478,6 +478,17 @@ typedef struct xavs2gpu_tq_block {
 } xavs2gpu_tq_block_t;
 XAVS2GPU_API int xavs2gpu_tq_batch(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
                                    int16_t *recon, int32_t *nnz, void *stream);
+/* The same chain on host buffers (descriptors, residual, levels, recon,
+ * nnz in host memory, same layout); returns when the outputs are on the
+ * host.  The batch is cut into `chunks` runs of consecutive descriptors
+ * (1..256): while one run is transformed, the next one's inputs are copied
+ * in and the previous one's outputs copied out.  The overlap needs
+ * page-locked buffers (cudaHostAlloc / cudaHostRegister); with pageable ones
+ * the batch runs as one chunk.  Elements of the level and recon arrays that
+ * no valid descriptor owns may be overwritten.  Device buffers are kept per
+ * host thread and grow to the largest batch. */
+XAVS2GPU_API int xavs2gpu_tq_batch_host(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual,
+                                        int16_t *coef, int16_t *recon, int32_t *nnz, int chunks);
 
 /* ---- batched motion search -----------------------------------------------
  * Full search + sub-pel refinement of many PUs against device-resident

@@ -312,3 +312,48 @@ def test_tq_batch_edges(gpu, olib):
         assert np.array_equal(coef[co:co + nc], cf[:nc]), (i, p)
         assert np.array_equal(rec[o:o + w * h], blk), (i, p)
     assert nnz[-2] == -1 and nnz[-1] == -1
+
+
+@pytest.mark.parametrize("pinned,chunks", [(True, 7), (False, 4), (True, 1)])
+def test_tq_batch_host(gpu, pinned, chunks):
+    """The host-buffer TU chain (chunked copies overlapped with the chain)
+    gives exactly the device entry's outputs, for page-locked and pageable
+    host buffers, with descriptors out of offset order and invalid ones."""
+    import torch
+    import xavs2_gb300 as xg
+    import xavs2_gb300.synth as synth
+    n = 5000
+    blocks, nres, ncoef, zero = synth.tq_blocks(n, seed=12)
+    res = synth.tq_residual(blocks, zero, nres, seed=13).numpy()
+    rng = np.random.default_rng(14)
+    perm = rng.permutation(n)
+    blocks = np.ascontiguousarray(blocks[perm])      # offsets no longer monotone
+    blocks["part"][::97] = 30                          # invalid descriptors: nnz = -1, nothing written
+    d = {k: torch.from_numpy(v).cuda() for k, v in (("b", blocks.view(np.uint8).copy()), ("r", res))}
+    d_coef = torch.zeros(ncoef, dtype=torch.int16, device="cuda")
+    d_rec = torch.zeros(nres, dtype=torch.int16, device="cuda")
+    d_nnz = torch.zeros(n, dtype=torch.int32, device="cuda")
+    assert xg.fn("xavs2gpu_tq_batch")(d["b"].data_ptr(), n, d["r"].data_ptr(), d_coef.data_ptr(), d_rec.data_ptr(),
+                                      d_nnz.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+
+    def host(a):
+        t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy())
+        return t.pin_memory() if pinned else t
+    hb, hr = host(blocks), host(res)
+    hc, hrec, hn = host(np.zeros(ncoef, np.int16)), host(np.zeros(nres, np.int16)), host(np.zeros(n, np.int32))
+    # regions owned by valid descriptors (others are unspecified after the host call)
+    valid = blocks["part"] < 25
+    w, h = np.asarray(xg.PU_W)[blocks["part"][valid]], np.asarray(xg.PU_H)[blocks["part"][valid]]
+    sz = (w * h).astype(np.int64)
+    nc = np.where((w == 64) | (h == 64), sz // 4, sz)
+    own_r = np.concatenate([np.arange(o, o + k) for o, k in zip(blocks["offset"][valid], sz)])
+    own_c = np.concatenate([np.arange(o, o + k) for o, k in zip(blocks["coef_offset"][valid], nc)])
+    want_c, want_r = d_coef.cpu().numpy()[own_c], d_rec.cpu().numpy()[own_r]
+    for _ in range(2):
+        assert xg.fn("xavs2gpu_tq_batch_host")(hb.data_ptr(), n, hr.data_ptr(), hc.data_ptr(), hrec.data_ptr(),
+                                               hn.data_ptr(), chunks) == 0
+        assert np.array_equal(hn.numpy().view(np.int32), d_nnz.cpu().numpy())
+        assert np.array_equal(hc.numpy().view(np.int16)[own_c], want_c)
+        assert np.array_equal(hrec.numpy().view(np.int16)[own_r], want_r)
+    assert (hn.numpy().view(np.int32)[::97] == -1).all()

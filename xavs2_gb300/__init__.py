@@ -89,6 +89,7 @@ _SIGS = {
     "xavs2gpu_add_sign": (_I, [_P, _P, _I]),
     "xavs2gpu_cost_batch": (_I, [_I, _P, _I, _P, _P, _P, _P]),
     "xavs2gpu_interpolate_frame": (_I, [_P, _I, _I, _I, _I, _P, _I, _P]),
+    "xavs2gpu_tq_batch_host": (_I, [_P, _I, _P, _P, _P, _P, _I]),
     "xavs2gpu_expand_border": (_I, [_P, _I, _I, _I, _I, _P]),
     "xavs2gpu_tq_batch": (_I, [_P, _I, _P, _P, _P, _P, _P]),
     "xavs2gpu_pu_set_limits": (None, [_P, _I, _I, _I, _I]),

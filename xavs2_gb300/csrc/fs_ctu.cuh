@@ -140,6 +140,19 @@ __device__ __forceinline__ uint32_t sad4_acc(uint32_t a, uint32_t b, uint32_t c)
     return d;
 }
 
+// bytes o..o+3 of the 8-byte little-endian pair (lo, hi), o = 1..3
+#ifndef XG_CTU_PRMT
+#define XG_CTU_PRMT 1
+#endif
+__device__ __forceinline__ uint32_t align_bytes(uint32_t lo, uint32_t hi, int o)
+{
+#if XG_CTU_PRMT
+    return __byte_perm(lo, hi, o == 1 ? 0x4321 : o == 2 ? 0x5432 : 0x6543);
+#else
+    return __funnelshift_r(lo, hi, 8 * o);
+#endif
+}
+
 __device__ __forceinline__ uint32_t addmin(uint32_t a, uint32_t b, uint32_t c)
 {
     return __viaddmin_u32(a, b, c);   // min(a + b, c)
@@ -507,7 +520,9 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
                 for (int o = 0; o < 4; o++) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        const uint32_t a = o ? __funnelshift_r(w5[c], w5[c + 1], 8 * o) : w5[c];
+                        // the 4 bytes at byte offset o: a byte permute with a
+                        // constant selector (4321, 5432, 6543)
+                        const uint32_t a = o ? align_bytes(w5[c], w5[c + 1], o) : w5[c];
                         s[o][r >> 2][c] = sad4_acc(cw[r][c], a, s[o][r >> 2][c]);
                     }
                 }

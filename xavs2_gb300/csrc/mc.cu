@@ -204,32 +204,39 @@ __device__ __forceinline__ uint4 load_pairs(const uint32_t *row, const int (&lc)
     return make_uint4(row[lc[0]], row[lc[1]], row[lc[2]], row[lc[3]]);
 }
 
-// One CTA writes a 128 x 16 tile of every requested sub-pel plane over the
-// whole padded area [-pad, W+pad) x [-pad, H+pad).  The sample at (x, y) is
-// the filter output at (cx, cy) = (clamp(x, -4, W+3), clamp(y, -4, H+3)) (the
+// One CTA writes a 128 x 16 tile of every requested plane over the whole
+// padded area [-pad, W+pad) x [-pad, H+pad).  The sample at (x, y) is the
+// filter output at (cx, cy) = (clamp(x, -4, W+3), clamp(y, -4, H+3)) (the
 // reference filters [-4, W+4) x [-4, H+4) and replicates that region
 // outwards), so a tile needs the filter at the clamped columns cx0 + [0, 128)
-// and rows cy0 + [0, nL), nL <= 16 distinct clamped rows.
+// and rows cy0 + [0, nL), nL <= 16 distinct clamped rows.  Source reads are
+// clamped into the picture, so the source needs no border.
 //   1: the source window, 23 rows x 135 bytes, into shared memory (word loads
 //      away from the picture edge, clamped byte loads near it);
 //   2: the raw horizontal 8-tap sums of the three sub-pel phases (two byte
 //      dot products each) and the source bytes themselves, stored as row
-//      pairs (h[s], h[s+1]) of int16 for s = 0..21: thread = (4 columns,
-//      3 rows of pairs);
-//   3: thread = (horizontal phase fx, 4 columns, 8 rows): every vertical
-//      phase of a row is four 16-bit pair dot products on the pairs, the
-//      rounding (+32 >> 6 on bytes, +2048 >> 12 on raw sums) is one shift,
-//      and four samples are clipped and packed by two saturating packs; the
-//      row is stored to every output row that clamps to it (the top and
-//      bottom margins repeat rows -4 and H+3) as 32-bit stores, a warp
-//      writing 128 contiguous bytes of a plane row.
+//      pairs (h[s], h[s+1]) of int16 for s = 0..21: a warp per 2 pairs;
+//   3: thread = (horizontal phase fx, 4 columns, 4 rows): every vertical
+//      phase of a row is four 16-bit pair dot products on the pairs (one for
+//      the full-pel phase), the rounding (+32 >> 6 on bytes, +2048 >> 12 on
+//      raw sums) is one shift, and four samples are clipped and packed by two
+//      saturating packs; the row is stored to every output row that clamps
+//      to it (the top and bottom margins repeat rows -4 and H+3) as 32-bit
+//      stores, a warp writing 128 contiguous bytes of a plane row.
+// 512 threads per CTA: the 1,326 tiles of a 1080p plane set then make
+// 4.4 waves of 2 CTAs per SM rather than 2.2 waves of 4 smaller CTAs (the
+// partly filled last wave is the smaller share of the run).
+// mode: 1 planes 2, 8, 10 (half-pel), 2 all 15 sub-pel planes; | 4: also
+// plane 0 (the full-pel picture with its replicated border).
+constexpr int kPlaneThreads = 512;
 #ifndef XG_PLANES_MINB
-#define XG_PLANES_MINB 4
+#define XG_PLANES_MINB 2
 #endif
 
 template <bool VEC>
-__global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const uint8_t *__restrict__ src, int stride, int W, int H,
-                                                           int pad, PlaneSet planes, int mode, int src_words)
+__global__ void __launch_bounds__(kPlaneThreads, XG_PLANES_MINB)
+    frame_planes_kernel(const uint8_t *__restrict__ src, int src_stride, int stride, int W, int H, int pad,
+                        PlaneSet planes, int mode, int src_words)
 {
     __shared__ __align__(16) uint8_t s_src[PS_R][PS_C];
     __shared__ __align__(16) uint32_t s_pair[4][PP_R][PT_W];
@@ -239,45 +246,49 @@ __global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const
     const int tid = threadIdx.x;
     // ---- 1: source window: s_src[r][m] = src(cy0 - 3 + r, cx0 - 3 + m) for
     // m < 136 (words 0..33; the filters read bytes 0..134).  Word loads (src
-    // and stride 4-byte aligned) only where every byte they touch, up to
+    // and its stride 4-byte aligned) only where every byte they touch, up to
     // column cx0 + 136, lies inside the picture.
     constexpr int kWords = (PT_W + 8) / 4;
     const bool inner = src_words && cx0 - 6 >= 0 && cx0 + PT_W + 12 <= W && cy0 - 3 >= 0 && cy0 + PT_H + 4 <= H;
     if (inner) {
         const int xa = cx0 - 3, sh = 8 * (xa & 3);
-        for (int i = tid; i < PS_R * kWords; i += 256) {
+        for (int i = tid; i < PS_R * kWords; i += kPlaneThreads) {
             const int r = i / kWords, q = i - r * kWords;
             const uint32_t *p =
-                reinterpret_cast<const uint32_t *>(src + (ptrdiff_t)(cy0 - 3 + r) * stride + ((xa + 4 * q) & ~3));
+                reinterpret_cast<const uint32_t *>(src + (ptrdiff_t)(cy0 - 3 + r) * src_stride + ((xa + 4 * q) & ~3));
             const uint32_t lo = __ldg(p), hi = sh ? __ldg(p + 1) : 0u;
             *reinterpret_cast<uint32_t *>(&s_src[r][4 * q]) = __funnelshift_r(lo, hi, sh);
         }
     } else {
-        for (int i = tid; i < PS_R * PS_C; i += 256) {
+        for (int i = tid; i < PS_R * PS_C; i += kPlaneThreads) {
             const int r = i / PS_C, m = i - r * PS_C;
             const int sy = clampi(cy0 - 3 + r, 0, H - 1), sx = clampi(cx0 - 3 + m, 0, W - 1);
-            s_src[r][m] = src[(ptrdiff_t)sy * stride + sx];
+            s_src[r][m] = src[(ptrdiff_t)sy * src_stride + sx];
         }
     }
     __syncthreads();
-    // ---- 2: horizontal phases as row pairs
-    {
+    // ---- 2: horizontal phases as row pairs: warp `seg` < 11 makes pairs
+    // 2 seg and 2 seg + 1 from rows 2 seg .. 2 seg + 2
+    if ((tid >> 5) < PP_R / 2) {
         const int g = tid & 31, seg = tid >> 5;
-        const int r0 = 3 * seg, r1 = min(r0 + 3, PS_R - 1);
+        const int r0 = 2 * seg;
         uint32_t prev[4][4] = {};
-        for (int r = r0; r <= r1; r++) {
+#pragma unroll
+        for (int dr = 0; dr < 3; dr++) {
+            const int r = r0 + dr;
             const uint32_t *w = reinterpret_cast<const uint32_t *>(&s_src[r][0]);
             const uint32_t w0 = w[g], w1 = w[g + 1], w2 = w[g + 2];
             uint32_t cur[4][4];
-            const uint32_t ctr = __funnelshift_r(w0, w1, 24);   // the centre bytes (tap 3) of the 4 columns
+            const uint32_t ctr = __byte_perm(w0, w1, 0x6543);   // the centre bytes (tap 3) of the 4 columns
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const uint32_t lo = __funnelshift_r(w0, w1, 8 * j), hi = __funnelshift_r(w1, w2, 8 * j);
+                const uint32_t sel = j == 0 ? 0x3210 : j == 1 ? 0x4321 : j == 2 ? 0x5432 : 0x6543;
+                const uint32_t lo = __byte_perm(w0, w1, sel), hi = __byte_perm(w1, w2, sel);
 #pragma unroll
                 for (int f = 1; f < 4; f++) cur[f][j] = (uint32_t)dp4a_us(hi, tap_word(f, 1), dp4a_us(lo, tap_word(f, 0), 0));
                 cur[0][j] = (ctr >> (8 * j)) & 0xFFu;
             }
-            if (r > r0) {
+            if (dr > 0) {
                 const int s = r - 1;
 #pragma unroll
                 for (int f = 0; f < 4; f++) {
@@ -296,18 +307,18 @@ __global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const
         }
     }
     __syncthreads();
-    // ---- 3: vertical phases, 4 columns x 8 rows per thread
-    const int g = tid & 31, fx = (tid >> 5) & 3, half = tid >> 7;
-    const int l0 = 8 * half;
+    // ---- 3: vertical phases, 4 columns x 4 rows per thread
+    const int g = tid & 31, fx = (tid >> 5) & 3, qtr = tid >> 7;
+    const int l0 = 4 * qtr;
     const int xg = x0 + 4 * g, end_col = W + pad;
     if (l0 >= nL || xg >= end_col) return;
-    // planes this thread writes: fy = 0..3 of column phase fx (plane 0 is the
-    // full-pel picture itself; mode 1 keeps planes 2, 8, 10)
+    // planes this thread writes: fy = 0..3 of column phase fx (plane 0, the
+    // full-pel picture, only with mode bit 2; mode 1 keeps planes 2, 8, 10)
     int want = 0;
 #pragma unroll
     for (int fy = 0; fy < 4; fy++) {
         const int k = 4 * fy + fx;
-        if (k != 0 && (mode == 2 || k == 2 || k == 8 || k == 10)) want |= 1 << fy;
+        if (k == 0 ? (mode & 4) != 0 : ((mode & 3) == 2 || k == 2 || k == 8 || k == 10)) want |= 1 << fy;
     }
     if (!want) return;
     int lc[4];
@@ -325,9 +336,9 @@ __global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const
     for (int fy = 0; fy < 4; fy++)   // static parameter indices (a dynamic one copies the table to the stack)
         base[fy] = (fx == 0 ? planes.p[4 * fy] : fx == 1 ? planes.p[4 * fy + 1] : fx == 2 ? planes.p[4 * fy + 2]
                                                                                  : planes.p[4 * fy + 3]) + xg;
-    uint4 E[7], O[7];   // E[i] = pairs of row l0 + 2i, O[i] = of row l0 + 1 + 2i
+    uint4 E[5], O[5];   // E[i] = pairs of row l0 + 2i, O[i] = of row l0 + 1 + 2i
 #pragma unroll
-    for (int t = 0; t < 8; t++) {
+    for (int t = 0; t < 4; t++) {
         const int l = l0 + t;
         if (l >= nL) continue;
         if (t == 0) {
@@ -336,10 +347,10 @@ __global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const
         } else if (t == 1) {
 #pragma unroll
             for (int i = 0; i < 4; i++) O[i] = load_pairs(rows + (l0 + 1 + 2 * i) * PT_W, lc, vec);
-        } else if ((t & 1) == 0) {
-            E[t / 2 + 3] = load_pairs(rows + (l0 + t + 6) * PT_W, lc, vec);
+        } else if (t == 2) {
+            E[4] = load_pairs(rows + (l0 + 8) * PT_W, lc, vec);
         } else {
-            O[t / 2 + 3] = load_pairs(rows + (l0 + t + 6) * PT_W, lc, vec);
+            O[4] = load_pairs(rows + (l0 + 9) * PT_W, lc, vec);
         }
         uint4 A, B, C, D;
         if (t & 1) {
@@ -348,8 +359,17 @@ __global__ void __launch_bounds__(256, XG_PLANES_MINB) frame_planes_kernel(const
             A = E[t / 2]; B = E[t / 2 + 1]; C = E[t / 2 + 2]; D = E[t / 2 + 3];
         }
         uint32_t out[4];
+        // fy = 0 is the horizontal phase alone: 64 h[l + 3] = the upper half
+        // of pair (h[l + 2], h[l + 3]) times 64 (for fx = 0 the picture itself)
+        if (want & 1) {
+            constexpr uint32_t t64 = 0x40000000u;
+            out[0] = pack_sat_u8(dp2a_hi(B.x, t64, init) >> rsh, dp2a_hi(B.y, t64, init) >> rsh,
+                                 dp2a_hi(B.z, t64, init) >> rsh, dp2a_hi(B.w, t64, init) >> rsh);
+        } else {
+            out[0] = 0;
+        }
 #pragma unroll
-        for (int fy = 0; fy < 4; fy++) {
+        for (int fy = 1; fy < 4; fy++) {
             const uint32_t t03 = tap_word(fy, 0), t47 = tap_word(fy, 1);
             const int vx = vsum(A.x, B.x, C.x, D.x, t03, t47, init) >> rsh;
             const int vy = vsum(A.y, B.y, C.y, D.y, t03, t47, init) >> rsh;
@@ -570,6 +590,42 @@ extern "C" void xavs2gpu_intpl_chroma_block_ext(uint8_t *dst, int i_dst, uint8_t
 }
 
 // ---- whole-frame planes (device pointers) ---------------------------------------
+namespace xg {
+
+// Launches the planes kernel; `mask` has bit k for every plane written.
+static int planes_launch(const uint8_t *src, int src_stride, int stride, int width, int height, int pad,
+                         const PlaneSet &ps, int mask, int mode, cudaStream_t st)
+{
+    bool vec = stride % 4 == 0;
+    for (int k = 0; k < 16; k++)
+        if ((mask >> k) & 1) vec &= ((uintptr_t)ps.p[k] - (uintptr_t)pad) % 4 == 0;
+    const int src_words = src_stride % 4 == 0 && (uintptr_t)src % 4 == 0;
+    dim3 grid((width + 2 * pad + PT_W - 1) / PT_W, (height + 2 * pad + PT_H - 1) / PT_H);
+    if (vec)
+        frame_planes_kernel<true><<<grid, kPlaneThreads, 0, st>>>(src, src_stride, stride, width, height, pad, ps,
+                                                                   mode, src_words);
+    else
+        frame_planes_kernel<false><<<grid, kPlaneThreads, 0, st>>>(src, src_stride, stride, width, height, pad, ps,
+                                                                    mode, src_words);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
+}
+
+// A reference picture straight from a W x H source (any stride, no border)
+// into its 16 planes: the full-pel plane with its replicated border and the
+// 15 sub-pel planes, one launch (replaces the copy, border expansion and
+// planes of the reference's frame setup).
+int reference_planes_from(const uint8_t *src, int src_stride, int width, int height, int pad, uint8_t *const planes[16],
+                          int stride, cudaStream_t st)
+{
+    PlaneSet ps;
+    for (int k = 0; k < 16; k++) ps.p[k] = planes[k];
+    return planes_launch(src, src_stride, stride, width, height, pad, ps, 0xFFFF, 2 | 4, st);
+}
+
+}  // namespace xg
+
 extern "C" int xavs2gpu_interpolate_frame(const uint8_t *src, int stride, int width, int height, int pad,
                                           uint8_t *const planes[16], int mode, void *stream)
 {
@@ -591,18 +647,7 @@ extern "C" int xavs2gpu_interpolate_frame(const uint8_t *src, int stride, int wi
         }
     }
     cudaStream_t st = (cudaStream_t)stream;
-    bool vec = stride % 4 == 0;
-    for (int k = 1; k < 16; k++)
-        if ((mask >> k) & 1) vec &= ((uintptr_t)planes[k] - (uintptr_t)pad) % 4 == 0;
-    const int src_words = stride % 4 == 0 && (uintptr_t)src % 4 == 0;
-    dim3 grid((width + 2 * pad + PT_W - 1) / PT_W, (height + 2 * pad + PT_H - 1) / PT_H);
-    if (vec)
-        frame_planes_kernel<true><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode, src_words);
-    else
-        frame_planes_kernel<false><<<grid, 256, 0, st>>>(src, stride, width, height, pad, ps, mode, src_words);
-    count_launch();
-    XG_CUDA(cudaGetLastError());
-    return XAVS2GPU_OK;
+    return planes_launch(src, stride, stride, width, height, pad, ps, mask, mode, st);
 }
 
 extern "C" int xavs2gpu_expand_border(uint8_t *pix, int stride, int width, int height, int pad, void *stream)

@@ -1094,11 +1094,18 @@ static int finish_picture(MeSessionImpl &m, int slot)
     return XAVS2GPU_OK;
 }
 
-// copies a W x H picture (device memory, `stride`) into the slot's plane,
-// then finishes it as above
+// a W x H picture in device memory (`stride`) into the slot: the current
+// picture is copied into its plane and its border replicated; a reference's
+// 16 planes (full-pel with border, 15 sub-pel) come from one kernel reading
+// the source directly
 static int load_picture(MeSessionImpl &m, int slot, const uint8_t *dsrc, intptr_t stride)
 {
     const int idx = slot < 0 ? 0 : 1 + 16 * m.slot_buf[slot];
+    if (slot >= 0 && stride <= INT32_MAX) {
+        uint8_t *planes[16];
+        for (int k = 0; k < 16; k++) planes[k] = m.plane(idx + k);
+        return reference_planes_from(dsrc, (int)stride, m.W, m.H, kPad, planes, m.stride, m.st);
+    }
     XG_CUDA(cudaMemcpy2DAsync(m.plane(idx), m.stride, dsrc, stride, m.W, m.H, cudaMemcpyDeviceToDevice, m.st));
     return finish_picture(m, slot);
 }

@@ -23,6 +23,9 @@
 // transform.cu; transform.c:586-951).
 #include "transform_tables.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace xg {
 namespace tqw {
 
@@ -628,4 +631,132 @@ extern "C" int xavs2gpu_tq_batch(const xavs2gpu_tq_block_t *blocks, int n, const
                                  int16_t *recon, int32_t *nnz, void *stream)
 {
     return tq_batch_launch(blocks, n, residual, coef, recon, nnz, 4, (cudaStream_t)stream);
+}
+
+// ---- host-buffer form: copies and the chain overlapped by chunks ------------------
+namespace {
+
+struct HostTqCtx {
+    int device = -1;
+    cudaStream_t st[3] = {nullptr, nullptr, nullptr};   // copy in, chain, copy out
+    std::vector<cudaEvent_t> ev_in, ev_done;
+    xavs2gpu_tq_block_t *d_blocks = nullptr;
+    int16_t *d_res = nullptr, *d_coef = nullptr, *d_rec = nullptr;
+    int32_t *d_nnz = nullptr;
+    size_t cap_blocks = 0, cap_nnz = 0, cap_res = 0, cap_rec = 0, cap_coef = 0;
+    ~HostTqCtx()
+    {
+        if (device < 0) return;
+        cudaSetDevice(device);
+        for (auto s : st)
+            if (s) cudaStreamDestroy(s);
+        for (auto e : ev_in) cudaEventDestroy(e);
+        for (auto e : ev_done) cudaEventDestroy(e);
+        cudaFree(d_blocks); cudaFree(d_res); cudaFree(d_coef); cudaFree(d_rec); cudaFree(d_nnz);
+    }
+};
+thread_local HostTqCtx t_host_tq;
+
+template <typename T>
+int grow(T *&p, size_t &cap, size_t need)
+{
+    if (need <= cap) return XAVS2GPU_OK;
+    if (p) XG_CUDA(cudaFree(p));
+    p = nullptr;
+    XG_CUDA(cudaMalloc((void **)&p, sizeof(T) * need));
+    cap = need;
+    return XAVS2GPU_OK;
+}
+
+bool is_pinned(const void *p)
+{
+    cudaPointerAttributes a;
+    return p && cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+
+extern "C" int xavs2gpu_tq_batch_host(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual,
+                                      int16_t *coef, int16_t *recon, int32_t *nnz, int chunks)
+{
+    if (n < 0 || (n > 0 && (!blocks || !residual || !coef || !recon || !nnz)) || chunks < 1 || chunks > 256) {
+        fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch_host", "bad arguments");
+        return XAVS2GPU_ERR_ARG;
+    }
+    if (n == 0) return XAVS2GPU_OK;
+    HostTqCtx &c = t_host_tq;
+    const int dev = current_device();
+    XG_CUDA(cudaSetDevice(dev));
+    if (c.device != dev) {
+        if (c.device >= 0) {
+            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch_host", "one device per host thread");
+            return XAVS2GPU_ERR_ARG;
+        }
+        c.device = dev;
+        for (auto &s : c.st) XG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    }
+    // chunk extents over the residual / recon and level arrays (a chunk is a
+    // run of consecutive descriptors; invalid descriptors touch nothing)
+    chunks = std::min(chunks, n);
+    std::vector<int64_t> r0(chunks, INT64_MAX), r1(chunks, 0), c0(chunks, INT64_MAX), c1(chunks, 0);
+    int64_t res_len = 0, coef_len = 0;
+    for (int i = 0; i < n; i++) {
+        const xavs2gpu_tq_block_t &b = blocks[i];
+        if (b.part < 0 || b.part >= kNumParts || b.offset < 0 || b.coef_offset < 0) continue;
+        const int w = h_pu_w[b.part], h = h_pu_h[b.part];
+        const int64_t sz = (int64_t)w * h, nc = (w == 64 || h == 64) ? sz / 4 : sz;
+        const int k = (int)((int64_t)i * chunks / n);
+        r0[k] = std::min(r0[k], b.offset);
+        r1[k] = std::max(r1[k], b.offset + sz);
+        c0[k] = std::min(c0[k], b.coef_offset);
+        c1[k] = std::max(c1[k], b.coef_offset + nc);
+        res_len = std::max(res_len, b.offset + sz);
+        coef_len = std::max(coef_len, b.coef_offset + nc);
+    }
+    int rc;
+    const size_t nres = (size_t)std::max<int64_t>(res_len, 1), ncoef = (size_t)std::max<int64_t>(coef_len, 1);
+    if ((rc = grow(c.d_blocks, c.cap_blocks, (size_t)n)) != XAVS2GPU_OK ||
+        (rc = grow(c.d_nnz, c.cap_nnz, (size_t)n)) != XAVS2GPU_OK ||
+        (rc = grow(c.d_res, c.cap_res, nres)) != XAVS2GPU_OK || (rc = grow(c.d_rec, c.cap_rec, nres)) != XAVS2GPU_OK ||
+        (rc = grow(c.d_coef, c.cap_coef, ncoef)) != XAVS2GPU_OK)
+        return rc;
+    while ((int)c.ev_in.size() < chunks) {
+        cudaEvent_t a, b;
+        XG_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+        XG_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        c.ev_in.push_back(a);
+        c.ev_done.push_back(b);
+    }
+    const bool pinned = is_pinned(blocks) && is_pinned(residual) && is_pinned(coef) && is_pinned(recon) &&
+                        is_pinned(nnz);
+    if (!pinned) chunks = 1;   // pageable memory: the copies cannot overlap anyway
+    for (int k = 0; k < chunks; k++) {
+        const int b0 = pinned ? (int)(((int64_t)k * n + chunks - 1) / chunks) : 0;
+        const int b1 = pinned ? (int)(((int64_t)(k + 1) * n + chunks - 1) / chunks) : n;
+        if (b1 <= b0) continue;
+        XG_CUDA(cudaMemcpyAsync(c.d_blocks + b0, blocks + b0, sizeof(xavs2gpu_tq_block_t) * (b1 - b0),
+                                cudaMemcpyHostToDevice, c.st[0]));
+        const int64_t a = pinned ? r0[k] : 0, z = pinned ? r1[k] : res_len;
+        if (z > a)
+            XG_CUDA(cudaMemcpyAsync(c.d_res + a, residual + a, sizeof(int16_t) * (z - a), cudaMemcpyHostToDevice,
+                                    c.st[0]));
+        XG_CUDA(cudaEventRecord(c.ev_in[k], c.st[0]));
+        XG_CUDA(cudaStreamWaitEvent(c.st[1], c.ev_in[k], 0));
+        if ((rc = tq_batch_launch(c.d_blocks + b0, b1 - b0, c.d_res, c.d_coef, c.d_rec, c.d_nnz + b0, 4, c.st[1])) !=
+            XAVS2GPU_OK)
+            return rc;
+        XG_CUDA(cudaEventRecord(c.ev_done[k], c.st[1]));
+        XG_CUDA(cudaStreamWaitEvent(c.st[2], c.ev_done[k], 0));
+        const int64_t ca = pinned ? c0[k] : 0, cz = pinned ? c1[k] : coef_len;
+        if (z > a)
+            XG_CUDA(cudaMemcpyAsync(recon + a, c.d_rec + a, sizeof(int16_t) * (z - a), cudaMemcpyDeviceToHost,
+                                    c.st[2]));
+        if (cz > ca)
+            XG_CUDA(cudaMemcpyAsync(coef + ca, c.d_coef + ca, sizeof(int16_t) * (cz - ca), cudaMemcpyDeviceToHost,
+                                    c.st[2]));
+        XG_CUDA(cudaMemcpyAsync(nnz + b0, c.d_nnz + b0, sizeof(int32_t) * (b1 - b0), cudaMemcpyDeviceToHost, c.st[2]));
+    }
+    XG_CUDA(cudaStreamSynchronize(c.st[2]));
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
 }

@@ -49,6 +49,11 @@ CallCtx &call_ctx(size_t need_bytes);
 int current_device();
 // Number of SMs of the current device (queried once per device).
 int sm_count();
+// A reference picture (W x H, any stride, no border needed) into its 16
+// planes: the full-pel plane with `pad` replicated border and the 15
+// quarter-pel planes, one kernel (mc.cu).
+int reference_planes_from(const uint8_t *src, int src_stride, int width, int height, int pad, uint8_t *const planes[16],
+                          int stride, cudaStream_t st);
 
 // Byte offset rounded up to 256 for staging sub-buffers.
 static inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
