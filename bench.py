@@ -245,6 +245,49 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def per_pu_line(pus, phases, n_gen, peaks, peak_src):
+    """The per-PU search's share and rate: PU-area absolute differences
+    (w*h per displacement, (2R)^2 displacements) of the PUs whose predictor
+    does not round to (0,0) -- the PUs outside the CTU plan -- per second of
+    the per-PU kernel, against the same integer roof as the CTU search."""
+    import xavs2_gb300 as xg
+    off = ((pus["mvp_x"].astype(np.int64) + 2) >> 2 != 0) | ((pus["mvp_y"].astype(np.int64) + 2) >> 2 != 0)
+    area = (np.asarray(xg.PU_W)[pus["part"][off]] * np.asarray(xg.PU_H)[pus["part"][off]]).astype(np.int64).sum()
+    ms = float(phases[2])
+    px = float(area) * (2 * RANGE) ** 2
+    peak = sm_count() * 64 * 4 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    ach = px / (ms / 1e3) / 1e12 if ms > 0 and n_gen else 0.0
+    return {"pus": int(n_gen), "kernel_ms": ms, "share_of_step": ms / float(sum(phases)) if sum(phases) else 0.0,
+            "achieved": ach, "peak": peak, "unit": "Tpx-absdiff/s (PU area)", "frac": ach / peak,
+            "peak_source": peak_src}
+
+
+def temporal_mvps(xg, pus, refs, W, H, prm):
+    """Predictors from the previous picture's motion, the way an encoder's
+    temporal candidate supplies one: the previous picture (refs[0]) is
+    searched against the one before it (refs[1]) with zero predictors, and
+    every PU of the current picture takes the vector its co-located PU
+    found there, scaled by the temporal distance of its reference (x1 for
+    reference 0, x2 for reference 1) and kept inside its search limits."""
+    per_ref = len(pus) // NREFS
+    prev = xg.MeSession(W, H, NREFS, len(pus))
+    prev.set_picture(-1, refs[0])
+    for r in range(NREFS):
+        prev.set_picture(r, refs[1])
+    prev.set_pus(pus)
+    prev.run(prm)
+    res = prev.results()[:per_ref]
+    prev.close()
+    out = pus.copy()
+    for r in range(NREFS):
+        sl = slice(r * per_ref, (r + 1) * per_ref)
+        mx = res["bmv_x"].astype(np.int64) * (r + 1)
+        my = res["bmv_y"].astype(np.int64) * (r + 1)
+        out["mvp_x"][sl] = np.clip(mx, 4 * out["min_x"][sl], 4 * out["max_x"][sl])
+        out["mvp_y"][sl] = np.clip(my, 4 * out["min_y"][sl], 4 * out["max_y"][sl])
+    return out
+
+
 def run_ours(args):
     import torch
     import xavs2_gb300 as xg
@@ -274,6 +317,8 @@ def run_ours(args):
     else:
         pus = xg.frame_pus(WIDTH, HEIGHT, NREFS)
         prm = xg.MeParams(RANGE, lambda_factor(QP), 1, 2, 0, 0)
+        if args.mvp == "temporal":
+            pus = temporal_mvps(xg, pus, refs, WIDTH, HEIGHT, prm)
         evals = count_evals(pus, RANGE)
     sess = xg.MeSession(WIDTH, HEIGHT, NREFS, len(pus))
     sess.set_pus(pus)
@@ -426,7 +471,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "me_1080p_2ref_fs64_qpel_satd", "width": WIDTH, "height": HEIGHT, "refs": NREFS,
+        "config": {"workload": "me_1080p_2ref_fs64_qpel_satd" + ("_temporal_mvp" if args.mvp == "temporal" else ""),
+                   "mvp": "zero" if args.mvp == "zero" else "previous picture's co-located vectors, distance-scaled",
+                   "width": WIDTH, "height": HEIGHT, "refs": NREFS,
                    "search_range": RANGE, "qp": QP, "pus_per_picture": int(len(pus)),
                    "evals_per_step": evals, "l2": "flushed between steps (512 MiB write)",
                    "autotuned": {"refine_split_px": tuning[0], "refine_block": tuning[1], "cu_groups": tuning[2],
@@ -446,6 +493,7 @@ def run_ours(args):
         "interpolation_roofline": {"bound": "hbm", "achieved": interp_gbs, "peak": peaks.get("hbm_gbs"),
                                    "unit": "GB/s", "frac": interp_gbs / peaks.get("hbm_gbs", 6800.0)},
         "plan": {"ctu_pus": n_ctu, "per_pu_pus": n_gen, "ctu_jobs": n_jobs},
+        "per_pu_search": per_pu_line(pus, phases, n_gen, peaks, peak_src),
         "per_call": {"value": per_call, "unit": UNIT, "what": "xavs2gpu_pixel_sad_16x16 with host buffers"},
         "cpu_baseline": {"value": cpu_e / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": "random %.2f%% (%d) of the picture's PU searches, oracle C port, OpenMP"
@@ -1766,6 +1814,9 @@ def main():
     ap.add_argument("--tq-blocks", type=int, default=1000000)
     ap.add_argument("--tq-parts", default="0,1,2,3,4", help="TU shapes (LumaPU indices) of the tq workload")
     ap.add_argument("--tq-chunks", type=int, default=16, help="tq e2e: chunks the host entry overlaps")
+    ap.add_argument("--mvp", choices=["zero", "temporal"], default="zero",
+                    help="me: zero predictors (the shared-window CTU search) or the previous picture's vectors "
+                         "(each PU its own centre: the per-PU search)")
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     ap.add_argument("--serve-warm", type=float, default=2.0)

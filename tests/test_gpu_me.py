@@ -95,7 +95,9 @@ def test_generic_pus(gpu, olib):
     allp = np.concatenate([pus, layout])
     for prm in (xg.MeParams(12, oracle.lambda_factor(32), 1, 2, 0, 0),
                 xg.MeParams(6, oracle.lambda_factor(40), 0, 1, 0, 0),
-                xg.MeParams(10, oracle.lambda_factor(27), 1, 2, 1, 1)):
+                xg.MeParams(10, oracle.lambda_factor(27), 1, 2, 1, 1),
+                xg.MeParams(7, oracle.lambda_factor(32), 1, 2, 0, 0),
+                xg.MeParams(13, oracle.lambda_factor(35), 0, 2, 0, 0)):
         got, stats = _run(cur, [ref0], allp, prm)
         assert stats[1] >= n
         exp = _oracle(olib, cur, [ref0], allp, prm)
@@ -241,3 +243,34 @@ def test_headline_1080p_sample(gpu, olib):
     sel = np.ascontiguousarray(pus[idx])
     exp = _oracle(olib, cur, refs, sel, prm, threads=os.cpu_count() or 1)
     _assert_same(np.ascontiguousarray(got[idx]), exp, sel)
+
+
+def test_generic_pus_large_range(gpu, olib):
+    """The per-PU search at R = 64 (and the maximum R = 128 on a few PUs):
+    every shape with predictors far from (0,0), PUs at the picture corners
+    whose windows leave the padded plane, both references."""
+    import xavs2_gb300 as xg
+    rng = np.random.default_rng(640)
+    w, h = 256, 192
+    cur, ref0 = _frames(rng, w, h, shift=(5, -7))
+    _, ref1 = _frames(rng, w, h, shift=(-9, 3))
+    n = 60
+    pus = np.zeros(n, xg.PU_DTYPE)
+    pus["part"] = np.arange(n) % 25
+    pw = np.array(xg.PU_W)[pus["part"]]
+    ph = np.array(xg.PU_H)[pus["part"]]
+    corner = np.arange(n) % 3
+    pus["x"] = np.where(corner == 0, 0, np.where(corner == 1, w - pw, (rng.random(n) * (w - pw + 1)).astype(int)))
+    pus["y"] = np.where(corner == 0, h - ph, np.where(corner == 1, 0, (rng.random(n) * (h - ph + 1)).astype(int)))
+    pus["ref"] = np.arange(n) % 2
+    mvx = rng.integers(-120, 121, n)
+    pus["mvp_x"] = np.where(np.abs(mvx) < 3, 9, mvx)     # never rounds to (0, 0): the per-PU path
+    pus["mvp_y"] = rng.integers(-120, 121, n)
+    pus = xg.set_limits(pus, w, h)
+    for prm in (xg.MeParams(64, oracle.lambda_factor(32), 1, 2, 0, 0),
+                xg.MeParams(128, oracle.lambda_factor(30), 0, 2, 0, 0)):
+        sel = pus if prm.search_range == 64 else pus[::6].copy()
+        got, stats = _run(cur, [ref0, ref1], sel, prm)
+        assert stats[1] == len(sel)
+        exp = _oracle(olib, cur, [ref0, ref1], sel, prm, threads=os.cpu_count() or 1)
+        _assert_same(got, exp, sel)

@@ -133,12 +133,6 @@ struct SlotTable {
 };
 
 // ---- device helpers ------------------------------------------------------------------
-__device__ __forceinline__ uint32_t sad4_acc(uint32_t a, uint32_t b, uint32_t c)
-{
-    uint32_t d;
-    asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
 
 // bytes o..o+3 of the 8-byte little-endian pair (lo, hi), o = 1..3
 #ifndef XG_CTU_PRMT

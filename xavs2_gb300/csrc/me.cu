@@ -153,60 +153,130 @@ __global__ void reset_keys_kernel(const SessView *__restrict__ views, int nviews
 }
 
 // ---- 2b. per-PU full search (one CTA per PU) --------------------------------------
-// Visit order of window position (i, j) is 2 + (j+R)*2R + (i+R).
-__global__ void __launch_bounds__(256) fs_generic_kernel(const uint32_t *__restrict__ list, int n,
-                                                         const SessView *__restrict__ views, int R, int lambda)
+// For PUs outside the CTU plan (their own search centre and predictor).  The
+// CTA stages the PU's block and its (2R + w - 1) x (2R + h - 1) reference
+// window in shared memory; a thread takes groups of 4 horizontally adjacent
+// displacements: per block row and 4-pixel word it reads the block word (the
+// same for the whole warp) and one new window word, aligns the window at the
+// 4 byte offsets with byte permutes and accumulates 4 SADs with vabsdiff4.
+// MV bits per column / row of the window come from shared tables.  Visit
+// order of window position (i, j) is 2 + (j+R)*2R + (i+R); the first
+// strictly smaller (cost, order) key wins, merged with atomicMin.
+constexpr int kPuThreads = 256;
+
+// dynamic shared memory the per-PU search needs for range R
+__host__ __device__ __forceinline__ int fs_pu_smem(int R)
 {
-    __shared__ uint8_t s_cur[64 * 64];
-    __shared__ unsigned long long s_red[8];
+    const int pitch = ((2 * R + 64 + 8 + 15) / 16) * 16;          // window bytes per row (max block 64)
+    return 64 * 64 + 2 * (2 * R) * 4 + (2 * R + 64) * pitch + 8 * 8;
+}
+
+__global__ void __launch_bounds__(kPuThreads) fs_generic_kernel(const uint32_t *__restrict__ list, int n,
+                                                                const SessView *__restrict__ views, int R, int lambda)
+{
+    extern __shared__ __align__(16) uint8_t smem_pu[];
+    uint32_t *s_cur = reinterpret_cast<uint32_t *>(smem_pu);                 // [h][w/4] words
+    int *s_bx = reinterpret_cast<int *>(smem_pu + 64 * 64);                  // [2R] MV bits per column
+    int *s_by = s_bx + 2 * R;                                                // [2R] per row
+    uint8_t *s_win = reinterpret_cast<uint8_t *>(s_by + 2 * R);              // [2R + h - 1][pitch]
+    const int pitch = ((2 * R + 64 + 8 + 15) / 16) * 16;
+    unsigned long long *s_red = reinterpret_cast<unsigned long long *>(s_win + (2 * R + 64) * pitch);
+    const int tid = threadIdx.x;
     for (int li = blockIdx.x; li < n; li += gridDim.x) {
         const uint32_t e = list[li];
         const SessView &v = views[e >> kSessShift];
         const int i = (int)(e & kIdxMask);
-        const xavs2gpu_pu_t *__restrict__ pus = v.pus;
-        const PuState *__restrict__ state = v.state;
-        const uint8_t *__restrict__ cur = v.cur;
-        const uint8_t *const *refs = v.ref0;
+        const xavs2gpu_pu_t p = v.pus[i];
+        const PuState st = v.state[i];
+        if (!st.valid) continue;       // uniform over the CTA
         const Geometry g = v.g;
-        unsigned long long *__restrict__ keys = v.keys;
-        const xavs2gpu_pu_t p = pus[i];
-        const PuState st = state[i];
-        if (!st.valid) continue;
-        const int w = c_pu_w[p.part], h = c_pu_h[p.part];
-        const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
+        const int w = c_pu_w[p.part], h = c_pu_h[p.part], wq = w >> 2;
+        const int wx0 = p.x + st.cx - R, wy0 = p.y + st.cy - R;   // window origin (displacement -R, -R)
+        // bytes read per row: the last group of 4 displacements starts at most
+        // at 2R - 2 (odd R) and its words reach 6 bytes past the block width
+        const int wcols = 2 * R + w + 6, wrows = 2 * R + h - 1;
+        const uint8_t *ref = v.ref0[p.ref];
+        __syncthreads();   // the previous PU's readers are done
+        // block words
+        const uint8_t *o = v.cur + (ptrdiff_t)p.y * g.stride + p.x;
+        for (int k = tid; k < h * wq; k += kPuThreads) {
+            const int y = k / wq, c = k - y * wq;
+            const uint8_t *q = o + (ptrdiff_t)y * g.stride + 4 * c;
+            s_cur[k] = (uint32_t)q[0] | (uint32_t)q[1] << 8 | (uint32_t)q[2] << 16 | (uint32_t)q[3] << 24;
+        }
+        // MV bits of the window's columns and rows (me.c:614-641)
+        for (int k = tid; k < 2 * R; k += kPuThreads) {
+            s_bx[k] = mvbits_hd(4 * (st.cx + k - R) - p.mvp_x);
+            s_by[k] = mvbits_hd(4 * (st.cy + k - R) - p.mvp_y);
+        }
+        // window bytes, clamped into the padded plane (clamped bytes only
+        // feed displacements outside the limits)
+        for (int k = tid; k < wrows * wcols; k += kPuThreads) {
+            const int r = k / wcols, c = k - r * wcols;
+            const int y = min(max(wy0 + r, -kPad), g.H + kPad - 1), x = min(max(wx0 + c, -kPad), g.W + kPad - 1);
+            s_win[r * pitch + c] = ref[(ptrdiff_t)y * g.stride + x];
+        }
         __syncthreads();
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) s_cur[k] = o[(k / w) * g.stride + k % w];
-        __syncthreads();
-        const uint8_t *ref = refs[p.ref] + (ptrdiff_t)p.y * g.stride + p.x;
         unsigned long long best = kNoKey;
-        const int npos = 4 * R * R;
-        for (int q = threadIdx.x; q < npos; q += blockDim.x) {
-            const int j = q / (2 * R) - R, ii = q % (2 * R) - R;
-            const int mx = st.cx + ii, my = st.cy + j;
-            if (!in_box(p, mx, my)) continue;
-            const uint8_t *r = ref + (ptrdiff_t)my * g.stride + mx;
-            int s = 0;
+        const int groups = (2 * R + 3) >> 2;       // 4-displacement groups per window row
+        for (int q = tid; q < 2 * R * groups; q += kPuThreads) {
+            const int jr = q / groups, gx = q - jr * groups;   // displacement row j = jr - R, columns 4 gx ..
+            uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
             for (int y = 0; y < h; y++) {
-                const uint8_t *rr = r + (ptrdiff_t)y * g.stride;
-                const uint8_t *cc = s_cur + y * w;
-                for (int x = 0; x < w; x++) s += iabs_d((int)cc[x] - (int)rr[x]);
+                const uint32_t *wr = reinterpret_cast<const uint32_t *>(s_win + (jr + y) * pitch) + gx;
+                const uint32_t *cr = s_cur + y * wq;
+                uint32_t lo = wr[0];
+                for (int c = 0; c < wq; c++) {
+                    const uint32_t hi = wr[c + 1], cw = cr[c];
+                    a0 = sad4_acc(cw, lo, a0);
+                    a1 = sad4_acc(cw, __byte_perm(lo, hi, 0x4321), a1);
+                    a2 = sad4_acc(cw, __byte_perm(lo, hi, 0x5432), a2);
+                    a3 = sad4_acc(cw, __byte_perm(lo, hi, 0x6543), a3);
+                    lo = hi;
+                }
             }
-            int cost = s + mv_cost_hd(lambda, mx * 4, my * 4, p.mvp_x, p.mvp_y);
-            unsigned long long k = ((unsigned long long)(unsigned)cost << 32) | (unsigned)(2 + q);
-            if (k < best) best = k;
+            const int my = st.cy + jr - R, by = s_by[jr];
+            const uint32_t sads[4] = {a0, a1, a2, a3};
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int ir = 4 * gx + t, mx = st.cx + ir - R;
+                if (ir >= 2 * R || !in_box(p, mx, my)) continue;
+                const int cost = (int)sads[t] + (int)(((int64_t)lambda * (s_bx[ir] + by)) >> 16);
+                const unsigned long long k = ((unsigned long long)(unsigned)cost << 32) | (unsigned)(2 + jr * 2 * R + ir);
+                best = k < best ? k : best;
+            }
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
-            unsigned long long other = __shfl_xor_sync(0xffffffffu, best, off);
+            const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, off);
             best = other < best ? other : best;
         }
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = best;
+        if ((tid & 31) == 0) s_red[tid >> 5] = best;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int k = 1; k < (int)(blockDim.x >> 5); k++) best = s_red[k] < best ? s_red[k] : best;
-            atomicMin(&keys[i], best);
+        if (tid == 0) {
+            for (int k = 1; k < kPuThreads / 32; k++) best = s_red[k] < best ? s_red[k] : best;
+            if (best != kNoKey) atomicMin(&v.keys[i], best);
         }
     }
+}
+
+// Launch of the per-PU search with the dynamic shared memory of range R (the
+// attribute is raised once per device and size).
+static int fs_generic_launch(const uint32_t *list, int n, const SessView *views, int R, int lambda, cudaStream_t st)
+{
+    static int attr_bytes[64] = {0};
+    const int dev = current_device();
+    const int bytes = fs_pu_smem(R);
+    if (dev < 0 || dev >= 64) return XAVS2GPU_ERR_ARG;
+    if (attr_bytes[dev] < bytes) {
+        XG_CUDA(cudaFuncSetAttribute(fs_generic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        attr_bytes[dev] = bytes;
+    }
+    const int cap = sm_count() * 8;
+    fs_generic_kernel<<<n < cap ? n : cap, kPuThreads, bytes, st>>>(list, n, views, R, lambda);
+    count_launch();
+    XG_CUDA(cudaGetLastError());
+    return XAVS2GPU_OK;
 }
 
 // ---- 3. sub-pel refinement ------------------------------------------------------------
@@ -1333,10 +1403,8 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     ctu_jobs_run(m.plan.d_jobs, m.plan.n_jobs, m.plan.n_border, m.d_view, *prm, m.st);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
     if (m.n_generic) {
-        const int cap = sm_count() * 8;
-        int grid = m.n_generic < cap ? m.n_generic : cap;
-        fs_generic_kernel<<<grid, 256, 0, m.st>>>(gen, m.n_generic, m.d_view, R, lam);
-        count_launch();
+        const int rc = fs_generic_launch(gen, m.n_generic, m.d_view, R, lam, m.st);
+        if (rc != XAVS2GPU_OK) return rc;
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
     // the CU-grouped refinement follows the reference's per-PU order, which
@@ -1739,8 +1807,8 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     }
     ctu_jobs_run(bb.d_jobs, (int)nj, nborder, bb.d_views, *prm, st);
     if (ng) {
-        fs_generic_kernel<<<(unsigned)(ng < (size_t)sm_count() * 8 ? ng : (size_t)sm_count() * 8), 256, 0, st>>>(d_gen, (int)ng, bb.d_views, R, lam);
-        count_launch();
+        const int rc = fs_generic_launch(d_gen, (int)ng, bb.d_views, R, lam, st);
+        if (rc != XAVS2GPU_OK) return rc;
     }
     if (ngr) launch_groups(bb.d_groups, (int)ngr, d_members, bb.d_views, R, *prm, st);
     if (ns) {
@@ -1896,11 +1964,11 @@ extern "C" int xavs2gpu_me_search_noalloc(const uint8_t *cur, int stride, int wi
     const int R = prm->search_range, lam = prm->lambda_factor;
     noalloc_prepare_kernel<<<(n + 255) / 256, 256, 0, st>>>(pus, n, s, t, num_refs, width, height, cur, stride, out);
     me_init_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, cur, s->ref0, g, lam, s->state, s->keys);
-    const int grid = n < sm_count() * 8 ? n : sm_count() * 8;
-    fs_generic_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint32_t *>(s->list), n, &s->view, R, lam);
+    const int rc = fs_generic_launch(reinterpret_cast<const uint32_t *>(s->list), n, &s->view, R, lam, st);
+    if (rc != XAVS2GPU_OK) return rc;
     refine_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(s->pus, n, s->state, s->keys, cur, s->planes, g, R, *prm,
                                                         out);
-    count_launch(4);
+    count_launch(3);
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
 }

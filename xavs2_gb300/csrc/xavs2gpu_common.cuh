@@ -64,6 +64,13 @@ void unpack_rows(void *dst, intptr_t dst_stride_bytes, const uint8_t *src, int r
 
 // ---- device helpers ---------------------------------------------------------
 __device__ __forceinline__ int iabs_d(int v) { return v < 0 ? -v : v; }
+// c + sum over the four bytes of |a - b|
+__device__ __forceinline__ uint32_t sad4_acc(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t d;
+    asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
 __device__ __forceinline__ int clip3_d(int lo, int hi, int v) { return min(max(v, lo), hi); }
 __device__ __forceinline__ uint8_t clip_pel_d(int v) { return (uint8_t)min(max(v, 0), 255); }
 
