@@ -636,10 +636,13 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
     std::vector<CtuJob> jobs;
     std::vector<int32_t> slots;
     generic.clear();
+    // the CTU kernel walks a search row in steps of 4 displacements, so it
+    // takes ranges whose 2R is a multiple of 4 (odd R: every PU per-PU)
+    const bool range_ok = (2 * R) % 4 == 0;
     for (int i = 0; i < (int)pus.size(); i++) {
         const xavs2gpu_pu_t &u = pus[i];
         const int w = h_pu_w[u.part], h = h_pu_h[u.part];
-        bool ok = ((u.mvp_x + 2) >> 2) == 0 && ((u.mvp_y + 2) >> 2) == 0 && !(u.x & 3) && !(u.y & 3);
+        bool ok = range_ok && ((u.mvp_x + 2) >> 2) == 0 && ((u.mvp_y + 2) >> 2) == 0 && !(u.x & 3) && !(u.y & 3);
         // (0,0) must be inside the limits for it to be the centre
         ok = ok && u.min_x <= 0 && u.max_x >= 0 && u.min_y <= 0 && u.max_y >= 0;
         ok = ok && same_range_in_window(u.min_x, u.max_x, -kLimitMargin - u.x, W + kLimitMargin - u.x - w, R) &&
