@@ -336,57 +336,50 @@ __global__ void __launch_bounds__(kPlaneThreads, XG_PLANES_MINB)
     for (int fy = 0; fy < 4; fy++)   // static parameter indices (a dynamic one copies the table to the stack)
         base[fy] = (fx == 0 ? planes.p[4 * fy] : fx == 1 ? planes.p[4 * fy + 1] : fx == 2 ? planes.p[4 * fy + 2]
                                                                                  : planes.p[4 * fy + 3]) + xg;
-    uint4 E[5], O[5];   // E[i] = pairs of row l0 + 2i, O[i] = of row l0 + 1 + 2i
+    // rows in the order l0, l0 + 2, l0 + 1, l0 + 3: row l uses the pairs of
+    // rows l, l + 2, l + 4, l + 6, so two rows of one parity share three of
+    // their four pair words and only five are live at a time
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-        const int l = l0 + t;
-        if (l >= nL) continue;
-        if (t == 0) {
+    for (int par = 0; par < 2; par++) {
+        uint4 P[5];   // P[i] = pairs of row l0 + par + 2 i
 #pragma unroll
-            for (int i = 0; i < 4; i++) E[i] = load_pairs(rows + (l0 + 2 * i) * PT_W, lc, vec);
-        } else if (t == 1) {
+        for (int i = 0; i < 4; i++) P[i] = load_pairs(rows + (l0 + par + 2 * i) * PT_W, lc, vec);
 #pragma unroll
-            for (int i = 0; i < 4; i++) O[i] = load_pairs(rows + (l0 + 1 + 2 * i) * PT_W, lc, vec);
-        } else if (t == 2) {
-            E[4] = load_pairs(rows + (l0 + 8) * PT_W, lc, vec);
-        } else {
-            O[4] = load_pairs(rows + (l0 + 9) * PT_W, lc, vec);
-        }
-        uint4 A, B, C, D;
-        if (t & 1) {
-            A = O[t / 2]; B = O[t / 2 + 1]; C = O[t / 2 + 2]; D = O[t / 2 + 3];
-        } else {
-            A = E[t / 2]; B = E[t / 2 + 1]; C = E[t / 2 + 2]; D = E[t / 2 + 3];
-        }
-        uint32_t out[4];
-        // fy = 0 is the horizontal phase alone: 64 h[l + 3] = the upper half
-        // of pair (h[l + 2], h[l + 3]) times 64 (for fx = 0 the picture itself)
-        if (want & 1) {
-            constexpr uint32_t t64 = 0x40000000u;
-            out[0] = pack_sat_u8(dp2a_hi(B.x, t64, init) >> rsh, dp2a_hi(B.y, t64, init) >> rsh,
-                                 dp2a_hi(B.z, t64, init) >> rsh, dp2a_hi(B.w, t64, init) >> rsh);
-        } else {
-            out[0] = 0;
-        }
+        for (int u = 0; u < 2; u++) {
+            const int t = par + 2 * u, l = l0 + t;
+            if (l >= nL) continue;
+            if (u == 1) P[4] = load_pairs(rows + (l0 + par + 8) * PT_W, lc, vec);
+            const uint4 A = P[u], B = P[u + 1], C = P[u + 2], D = P[u + 3];
+            uint32_t out[4];
+            // fy = 0 is the horizontal phase alone: 64 h[l + 3] = the upper half
+            // of pair (h[l + 2], h[l + 3]) times 64 (for fx = 0 the picture itself)
+            if (want & 1) {
+                constexpr uint32_t t64 = 0x40000000u;
+                out[0] = pack_sat_u8(dp2a_hi(B.x, t64, init) >> rsh, dp2a_hi(B.y, t64, init) >> rsh,
+                                     dp2a_hi(B.z, t64, init) >> rsh, dp2a_hi(B.w, t64, init) >> rsh);
+            } else {
+                out[0] = 0;
+            }
 #pragma unroll
-        for (int fy = 1; fy < 4; fy++) {
-            const uint32_t t03 = tap_word(fy, 0), t47 = tap_word(fy, 1);
-            const int vx = vsum(A.x, B.x, C.x, D.x, t03, t47, init) >> rsh;
-            const int vy = vsum(A.y, B.y, C.y, D.y, t03, t47, init) >> rsh;
-            const int vz = vsum(A.z, B.z, C.z, D.z, t03, t47, init) >> rsh;
-            const int vw = vsum(A.w, B.w, C.w, D.w, t03, t47, init) >> rsh;
-            out[fy] = pack_sat_u8(vx, vy, vz, vw);
-        }
-        // output rows clamping to this row: one inside the picture's band,
-        // the whole margin run at rows -4 and H + 3
-        const int cyl = cy0 + l;
-        const int ya = max(cyl == -4 ? y0 : cyl, y0);
-        const int yb = min(min(cyl == H + 3 ? y0 + PT_H - 1 : cyl, y0 + PT_H - 1), H + pad - 1);
-        for (int y = ya; y <= yb; y++) {
-            const ptrdiff_t ro = (ptrdiff_t)y * stride;
+            for (int fy = 1; fy < 4; fy++) {
+                const uint32_t t03 = tap_word(fy, 0), t47 = tap_word(fy, 1);
+                const int vx = vsum(A.x, B.x, C.x, D.x, t03, t47, init) >> rsh;
+                const int vy = vsum(A.y, B.y, C.y, D.y, t03, t47, init) >> rsh;
+                const int vz = vsum(A.z, B.z, C.z, D.z, t03, t47, init) >> rsh;
+                const int vw = vsum(A.w, B.w, C.w, D.w, t03, t47, init) >> rsh;
+                out[fy] = pack_sat_u8(vx, vy, vz, vw);
+            }
+            // output rows clamping to this row: one inside the picture's band,
+            // the whole margin run at rows -4 and H + 3
+            const int cyl = cy0 + l;
+            const int ya = max(cyl == -4 ? y0 : cyl, y0);
+            const int yb = min(min(cyl == H + 3 ? y0 + PT_H - 1 : cyl, y0 + PT_H - 1), H + pad - 1);
+            for (int y = ya; y <= yb; y++) {
+                const ptrdiff_t ro = (ptrdiff_t)y * stride;
 #pragma unroll
-            for (int fy = 0; fy < 4; fy++)
-                if ((want >> fy) & 1) store_group<VEC>(base[fy] + ro, out[fy], xg, end_col);
+                for (int fy = 0; fy < 4; fy++)
+                    if ((want >> fy) & 1) store_group<VEC>(base[fy] + ro, out[fy], xg, end_col);
+            }
         }
     }
 }
