@@ -484,7 +484,9 @@ XAVS2GPU_API int xavs2gpu_tq_batch(const xavs2gpu_tq_block_t *blocks, int n, con
  * (1..256): while one run is transformed, the next one's inputs are copied
  * in and the previous one's outputs copied out.  The overlap needs
  * page-locked buffers (cudaHostAlloc / cudaHostRegister); with pageable ones
- * the batch runs as one chunk.  Elements of the level and recon arrays that
+ * the batch runs as one chunk.  chunks = 0 (page-locked arrays only): the
+ * chain reads and writes the host arrays in place over the host link, no
+ * copies (on a coherent CPU-GPU link this is the faster form).  Elements of the level and recon arrays that
  * no valid descriptor owns may be overwritten.  Device buffers are kept per
  * host thread and grow to the largest batch. */
 XAVS2GPU_API int xavs2gpu_tq_batch_host(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual,

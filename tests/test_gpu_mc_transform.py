@@ -314,7 +314,7 @@ def test_tq_batch_edges(gpu, olib):
     assert nnz[-2] == -1 and nnz[-1] == -1
 
 
-@pytest.mark.parametrize("pinned,chunks", [(True, 7), (False, 4), (True, 1)])
+@pytest.mark.parametrize("pinned,chunks", [(True, 7), (False, 4), (True, 1), (True, 0)])
 def test_tq_batch_host(gpu, pinned, chunks):
     """The host-buffer TU chain (chunked copies overlapped with the chain)
     gives exactly the device entry's outputs, for page-locked and pageable

@@ -676,9 +676,39 @@ bool is_pinned(const void *p)
 
 }  // namespace
 
+// Device address of page-locked host memory (nullptr if `p` is not).
+static void *mapped(const void *p)
+{
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) return nullptr;
+    return a.devicePointer;
+}
+
 extern "C" int xavs2gpu_tq_batch_host(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual,
                                       int16_t *coef, int16_t *recon, int32_t *nnz, int chunks)
 {
+    if (chunks == 0 && n > 0) {
+        // the chain reads and writes the page-locked host arrays in place
+        // over the host link (no copies, no device buffers)
+        void *b = mapped(blocks), *r = mapped(residual), *c = mapped(coef), *q = mapped(recon), *z = mapped(nnz);
+        if (!b || !r || !c || !q || !z) {
+            fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch_host", "chunks = 0 needs page-locked arrays");
+            return XAVS2GPU_ERR_ARG;
+        }
+        HostTqCtx &hc = t_host_tq;
+        const int dev = current_device();
+        XG_CUDA(cudaSetDevice(dev));
+        if (hc.device < 0) {
+            hc.device = dev;
+            for (auto &st : hc.st) XG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        }
+        int rc = tq_batch_launch(static_cast<const xavs2gpu_tq_block_t *>(b), n, static_cast<const int16_t *>(r),
+                                 static_cast<int16_t *>(c), static_cast<int16_t *>(q), static_cast<int32_t *>(z), 4,
+                                 hc.st[1]);
+        if (rc != XAVS2GPU_OK) return rc;
+        XG_CUDA(cudaStreamSynchronize(hc.st[1]));
+        return XAVS2GPU_OK;
+    }
     if (n < 0 || (n > 0 && (!blocks || !residual || !coef || !recon || !nnz)) || chunks < 1 || chunks > 256) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch_host", "bad arguments");
         return XAVS2GPU_ERR_ARG;
