@@ -329,6 +329,10 @@ __global__ void __launch_bounds__(kPlaneThreads, XG_PLANES_MINB)
         vec &= lc[c] == lc[0] + c;
     }
     vec &= (lc[0] & 3) == 0;
+    // a tile inside [-4, W+3] x [-4, H+3] whose columns map one to one: every
+    // computed row goes to exactly one output row, every group of 4 columns
+    // is a whole aligned word
+    const bool direct = VEC && vec && y0 >= -4 && y0 + PT_H - 1 <= H + 3 && xg + 3 <= W + 3;
     const uint32_t *rows = &s_pair[fx][0][0];
     const int init = fx ? 2048 : 32, rsh = fx ? 12 : 6;
     uint8_t *base[4];
@@ -368,6 +372,13 @@ __global__ void __launch_bounds__(kPlaneThreads, XG_PLANES_MINB)
                 const int vz = vsum(A.z, B.z, C.z, D.z, t03, t47, init) >> rsh;
                 const int vw = vsum(A.w, B.w, C.w, D.w, t03, t47, init) >> rsh;
                 out[fy] = pack_sat_u8(vx, vy, vz, vw);
+            }
+            if (direct) {
+                const ptrdiff_t ro = (ptrdiff_t)(y0 + l) * stride;
+#pragma unroll
+                for (int fy = 0; fy < 4; fy++)
+                    if ((want >> fy) & 1) *reinterpret_cast<uint32_t *>(base[fy] + ro) = out[fy];
+                continue;
             }
             // output rows clamping to this row: one inside the picture's band,
             // the whole margin run at rows -4 and H + 3
