@@ -77,16 +77,13 @@ __device__ __forceinline__ int mode_pu_index(int mode, int k) { return mode == 0
 // contiguous, in TU order)
 __device__ __forceinline__ int split_offset(int split_type, int S, int xx, int yy)
 {
-    if (split_type == 2) {                           // horizontal strips S x S/4
-        const int q = S >> 2;
-        return (yy / q) * (S * q) + (yy % q) * S + xx;
-    }
-    if (split_type == 3) {                           // vertical strips S/4 x S
-        const int q = S >> 2;
-        return (xx / q) * (S * q) + yy * q + (xx % q);
-    }
-    const int h = S >> 1;                            // quarters
-    return ((yy >= h) * 2 + (xx >= h)) * (h * h) + (yy % h) * h + (xx % h);
+    const int lq = 29 - __clz(S);                    // log2(S / 4)
+    if (split_type == 2)                             // horizontal strips S x S/4
+        return ((yy >> lq) << (2 * lq + 2)) + ((yy & ((1 << lq) - 1)) << (lq + 2)) + xx;
+    if (split_type == 3)                             // vertical strips S/4 x S
+        return ((xx >> lq) << (2 * lq + 2)) + (yy << lq) + (xx & ((1 << lq) - 1));
+    const int lh = lq + 1, h = S >> 1;               // quarters
+    return (((yy >> lh) * 2 + (xx >> lh)) << (2 * lh)) + ((yy & (h - 1)) << lh) + (xx & (h - 1));
 }
 
 __device__ __forceinline__ int luma_part(int w, int h)
@@ -122,6 +119,46 @@ __device__ __forceinline__ const uint8_t *pred_ptr(const PicView &v, int cx, int
            (p.mvx >> 2);
 }
 
+// Four-pixel groups.  CU sizes and TU sides are powers of two, PU and TU
+// boundaries inside a CU fall on multiples of 4 columns (the 8x8 CUs have no
+// AMP modes and split into 4x4 quarters), so the 4 pixels of a group share
+// their PU and their TU row: one 32-bit source word, one unaligned
+// prediction word and one 8-byte residual word per group.
+
+// 4 bytes at any address (two aligned words and a byte permute)
+__device__ __forceinline__ uint32_t load4u(const uint8_t *p)
+{
+    const uintptr_t a = (uintptr_t)p;
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    return __byte_perm(w[0], w[1], 0x3210u + 0x1111u * (uint32_t)(a & 3));
+}
+
+// bytes 0,1 / 2,3 of a word as two zero-extended halfwords
+__device__ __forceinline__ uint32_t lo_pairs(uint32_t b) { return __byte_perm(b, 0, 0x7170); }
+__device__ __forceinline__ uint32_t hi_pairs(uint32_t b) { return __byte_perm(b, 0, 0x7372); }
+
+// src - pred of 4 pixels as 4 int16 (pixel_sub_ps)
+__device__ __forceinline__ uint2 sub4_s16(uint32_t s4, uint32_t p4)
+{
+    return make_uint2(__vsub2(lo_pairs(s4), lo_pairs(p4)), __vsub2(hi_pairs(s4), hi_pairs(p4)));
+}
+
+// clip(pred + residual) of 4 pixels as bytes: pred + residual saturates at
+// the int16 limits, which the clip to [0, 255] then removes exactly
+__device__ __forceinline__ uint32_t recon4(uint32_t p4, uint2 r)
+{
+    const uint32_t lo = __vmins2(__vmaxs2(__vaddss2(lo_pairs(p4), r.x), 0u), 0x00ff00ffu);
+    const uint32_t hi = __vmins2(__vmaxs2(__vaddss2(hi_pairs(p4), r.y), 0u), 0x00ff00ffu);
+    return __byte_perm(lo, hi, 0x6420);
+}
+
+// acc + sum of squared differences of 4 byte pairs
+__device__ __forceinline__ unsigned ssd4(uint32_t a, uint32_t b, unsigned acc)
+{
+    const unsigned d = __vabsdiffu4(a, b);
+    return __dp4a(d, d, acc);
+}
+
 // Warp per candidate: prediction, residual in both TU layouts, the five TU
 // descriptors, and the sum of the mode's search costs.
 static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
@@ -141,12 +178,13 @@ static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView
     const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
     const uint8_t *src = v.cur + (ptrdiff_t)cy * v.stride + cx;
     int16_t *whole = residual + v.res_off + cd.res_offset, *split = whole + S * S;
-    for (int e = lane; e < S * S; e += 32) {
+    for (int e = 4 * lane; e < S * S; e += 128) {
         const int yy = e >> lg, xx = e & (S - 1);
+        const ptrdiff_t o = (ptrdiff_t)yy * v.stride + xx;
         const uint8_t *pr = mode_pu_of(mode, S, xx, yy) ? pr1 : pr0;
-        const int16_t r = (int16_t)((int)src[(ptrdiff_t)yy * v.stride + xx] - (int)pr[(ptrdiff_t)yy * v.stride + xx]);
-        whole[e] = r;
-        split[split_offset(cd.split_type, S, xx, yy)] = r;
+        const uint2 r = sub4_s16(*reinterpret_cast<const uint32_t *>(src + o), load4u(pr + o));
+        *reinterpret_cast<uint2 *>(whole + e) = r;
+        *reinterpret_cast<uint2 *>(split + split_offset(cd.split_type, S, xx, yy)) = r;
     }
     if (lane < 5) {
         xavs2gpu_tq_block_t b;
@@ -188,14 +226,14 @@ static __global__ void __launch_bounds__(128) cand_eval_kernel(const PicView *__
     const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
     const uint8_t *src = v.cur + (ptrdiff_t)cy * v.stride + cx;
     const int16_t *whole = rres + v.res_off + cd.res_offset, *split = whole + S * S;
-    int d0 = 0, d1 = 0;
-    for (int e = lane; e < S * S; e += 32) {
+    unsigned d0 = 0, d1 = 0;
+    for (int e = 4 * lane; e < S * S; e += 128) {
         const int yy = e >> lg, xx = e & (S - 1);
-        const int pv = (mode_pu_of(mode, S, xx, yy) ? pr1 : pr0)[(ptrdiff_t)yy * v.stride + xx];
-        const int sv = src[(ptrdiff_t)yy * v.stride + xx];
-        const int a = sv - clip_pel_d(pv + whole[e]), b = sv - clip_pel_d(pv + split[split_offset(cd.split_type, S, xx, yy)]);
-        d0 += a * a;
-        d1 += b * b;
+        const ptrdiff_t o = (ptrdiff_t)yy * v.stride + xx;
+        const uint32_t p4 = load4u((mode_pu_of(mode, S, xx, yy) ? pr1 : pr0) + o);
+        const uint32_t s4 = *reinterpret_cast<const uint32_t *>(src + o);
+        d0 = ssd4(s4, recon4(p4, *reinterpret_cast<const uint2 *>(whole + e)), d0);
+        d1 = ssd4(s4, recon4(p4, *reinterpret_cast<const uint2 *>(split + split_offset(cd.split_type, S, xx, yy))), d1);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -203,8 +241,8 @@ static __global__ void __launch_bounds__(128) cand_eval_kernel(const PicView *__
         d1 += __shfl_xor_sync(0xffffffffu, d1, o);
     }
     if (lane == 0) {
-        dist[2 * i] = d0;
-        dist[2 * i + 1] = d1;
+        dist[2 * i] = (int32_t)d0;
+        dist[2 * i + 1] = (int32_t)d1;
     }
 }
 
@@ -234,10 +272,17 @@ static __global__ void __launch_bounds__(128) cand_choose_kernel(const PicView *
     const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
     const int16_t *r = rres + v.res_off + cd.res_offset + (split ? S * S : 0);
     uint8_t *o = v.recon + (ptrdiff_t)cy * v.width + cx;
-    for (int e = lane; e < S * S; e += 32) {
+    const bool aligned = (v.width & 3) == 0;     // word stores into the reconstruction
+    for (int e = 4 * lane; e < S * S; e += 128) {
         const int yy = e >> lg, xx = e & (S - 1);
-        const int pv = (mode_pu_of(mode, S, xx, yy) ? pr1 : pr0)[(ptrdiff_t)yy * v.stride + xx];
-        o[(ptrdiff_t)yy * v.width + xx] = clip_pel_d(pv + r[split ? split_offset(cd.split_type, S, xx, yy) : e]);
+        const uint32_t p4 = load4u((mode_pu_of(mode, S, xx, yy) ? pr1 : pr0) + (ptrdiff_t)yy * v.stride + xx);
+        const uint32_t q = recon4(p4, *reinterpret_cast<const uint2 *>(r + (split ? split_offset(cd.split_type, S, xx, yy) : e)));
+        uint8_t *d = o + (ptrdiff_t)yy * v.width + xx;
+        if (aligned) {
+            *reinterpret_cast<uint32_t *>(d) = q;
+        } else {
+            d[0] = (uint8_t)q; d[1] = (uint8_t)(q >> 8); d[2] = (uint8_t)(q >> 16); d[3] = (uint8_t)(q >> 24);
+        }
     }
     if (lane == 0) {
         xavs2gpu_cu_choice_t ch;

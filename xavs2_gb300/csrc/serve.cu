@@ -77,7 +77,14 @@ __global__ void hash_kernel(const JobView *__restrict__ views, const int16_t *__
     for (uint64_t i = t0; i < nres; i += step) h += mixw(rw[i], nrec + ncw + i);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(v.hash, h);
+    // one atomic per CTA (thousands of CTAs add into one word per picture)
+    __shared__ unsigned long long part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = h;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) h += part[w];
+        atomicAdd(v.hash, h);
+    }
 }
 
 using Clock = std::chrono::steady_clock;
