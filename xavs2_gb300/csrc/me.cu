@@ -155,72 +155,96 @@ __global__ void reset_keys_kernel(const SessView *__restrict__ views, int nviews
 // ---- 2b. per-PU full search (one CTA per PU) --------------------------------------
 // For PUs outside the CTU plan (their own search centre and predictor).  The
 // CTA stages the PU's block and its (2R + w - 1) x (2R + h - 1) reference
-// window in shared memory; a thread takes groups of 4 horizontally adjacent
-// displacements: per block row and 4-pixel word it reads the block word (the
-// same for the whole warp) and one new window word, aligns the window at the
-// 4 byte offsets with byte permutes and accumulates 4 SADs with vabsdiff4.
-// MV bits per column / row of the window come from shared tables.  Visit
-// order of window position (i, j) is 2 + (j+R)*2R + (i+R); the first
-// strictly smaller (cost, order) key wins, merged with atomicMin.
+// window in shared memory (a warp per window row, aligned word loads and a
+// funnel shift when the window lies inside the padded plane); a thread takes
+// groups of 4 horizontally adjacent displacements: per block row and 4-pixel
+// word it reads the block word (the same for the whole warp) and one new
+// window word, aligns the window at the 4 byte offsets with byte permutes and
+// accumulates 4 SADs with vabsdiff4.  Only the rows and column groups inside
+// the PU's limits are visited.  lambda x MV bits per column / row of the
+// window come from shared tables (me.c:614-641): the cost of (i, j) is
+// SAD + (lx[i] + ly[j]) >> 16.  Visit order of window position (i, j) is
+// 2 + (j+R)*2R + (i+R); a thread visits its positions in increasing order,
+// so a strictly smaller 32-bit cost keeps the first minimum, and the CTA's
+// (cost, order) keys are reduced and merged with atomicMin.
 constexpr int kPuThreads = 256;
 
 // dynamic shared memory the per-PU search needs for range R
 __host__ __device__ __forceinline__ int fs_pu_smem(int R)
 {
     const int pitch = ((2 * R + 64 + 8 + 15) / 16) * 16;          // window bytes per row (max block 64)
-    return 64 * 64 + 2 * (2 * R) * 4 + (2 * R + 64) * pitch + 8 * 8;
+    return 64 * 64 + 2 * (2 * R) * 8 + (2 * R + 64) * pitch + 8 * 8;
 }
 
-__global__ void __launch_bounds__(kPuThreads) fs_generic_kernel(const uint32_t *__restrict__ list, int n,
-                                                                const SessView *__restrict__ views, int R, int lambda)
+// lambda x bits with lambda < 2^24 and bits < 128 fits 31 bits; larger
+// lambdas take 64-bit table entries
+template <bool WIDE> struct LamT { using T = int; };
+template <> struct LamT<true> { using T = long long; };
+
+template <bool WIDE>
+__device__ __forceinline__ void fs_pu_search(const xavs2gpu_pu_t &p, const PuState &st, const SessView &v, int R,
+                                             int lambda, uint8_t *smem_pu, unsigned long long *__restrict__ keys,
+                                             int i)
 {
-    extern __shared__ __align__(16) uint8_t smem_pu[];
+    using L = typename LamT<WIDE>::T;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint32_t *s_cur = reinterpret_cast<uint32_t *>(smem_pu);                 // [h][w/4] words
-    int *s_bx = reinterpret_cast<int *>(smem_pu + 64 * 64);                  // [2R] MV bits per column
-    int *s_by = s_bx + 2 * R;                                                // [2R] per row
-    uint8_t *s_win = reinterpret_cast<uint8_t *>(s_by + 2 * R);              // [2R + h - 1][pitch]
+    L *s_lx = reinterpret_cast<L *>(smem_pu + 64 * 64);                      // [2R] lambda x MV bits per column
+    L *s_ly = s_lx + 2 * R;                                                  // [2R] per row
+    uint8_t *s_win = smem_pu + 64 * 64 + 2 * (2 * R) * 8;                    // [2R + h - 1][pitch]
     const int pitch = ((2 * R + 64 + 8 + 15) / 16) * 16;
     unsigned long long *s_red = reinterpret_cast<unsigned long long *>(s_win + (2 * R + 64) * pitch);
-    const int tid = threadIdx.x;
-    for (int li = blockIdx.x; li < n; li += gridDim.x) {
-        const uint32_t e = list[li];
-        const SessView &v = views[e >> kSessShift];
-        const int i = (int)(e & kIdxMask);
-        const xavs2gpu_pu_t p = v.pus[i];
-        const PuState st = v.state[i];
-        if (!st.valid) continue;       // uniform over the CTA
-        const Geometry g = v.g;
-        const int w = c_pu_w[p.part], h = c_pu_h[p.part], wq = w >> 2;
-        const int wx0 = p.x + st.cx - R, wy0 = p.y + st.cy - R;   // window origin (displacement -R, -R)
-        // bytes read per row: the last group of 4 displacements starts at most
-        // at 2R - 2 (odd R) and its words reach 6 bytes past the block width
-        const int wcols = 2 * R + w + 6, wrows = 2 * R + h - 1;
-        const uint8_t *ref = v.ref0[p.ref];
-        __syncthreads();   // the previous PU's readers are done
-        // block words
-        const uint8_t *o = v.cur + (ptrdiff_t)p.y * g.stride + p.x;
-        for (int k = tid; k < h * wq; k += kPuThreads) {
-            const int y = k / wq, c = k - y * wq;
-            const uint8_t *q = o + (ptrdiff_t)y * g.stride + 4 * c;
-            s_cur[k] = (uint32_t)q[0] | (uint32_t)q[1] << 8 | (uint32_t)q[2] << 16 | (uint32_t)q[3] << 24;
+    const Geometry g = v.g;
+    const int w = c_pu_w[p.part], h = c_pu_h[p.part], wq = w >> 2;
+    const int wx0 = p.x + st.cx - R, wy0 = p.y + st.cy - R;   // window origin (displacement -R, -R)
+    // bytes read per row: the last group of 4 displacements starts at most
+    // at 2R - 2 (odd R) and its words reach 6 bytes past the block width
+    const int wcols = 2 * R + w + 6, wrows = 2 * R + h - 1, nwords = (wcols + 3) >> 2;
+    const uint8_t *ref = v.ref0[p.ref];
+    // block words
+    const uint8_t *o = v.cur + (ptrdiff_t)p.y * g.stride + p.x;
+    const bool oal = (((uintptr_t)o | (uintptr_t)g.stride) & 3) == 0;
+    for (int k = tid; k < h * wq; k += kPuThreads) {
+        const int y = k / wq, c = k - y * wq;
+        const uint8_t *q = o + (ptrdiff_t)y * g.stride + 4 * c;
+        s_cur[k] = oal ? *reinterpret_cast<const uint32_t *>(q)
+                       : (uint32_t)q[0] | (uint32_t)q[1] << 8 | (uint32_t)q[2] << 16 | (uint32_t)q[3] << 24;
+    }
+    // lambda x MV bits of the window's columns and rows (me.c:614-641)
+    for (int k = tid; k < 2 * R; k += kPuThreads) {
+        s_lx[k] = (L)lambda * mvbits_hd(4 * (st.cx + k - R) - p.mvp_x);
+        s_ly[k] = (L)lambda * mvbits_hd(4 * (st.cy + k - R) - p.mvp_y);
+    }
+    // window bytes: inside the padded plane a warp copies a row as aligned
+    // words (the 4 bytes past the row's last word included); elsewhere bytes
+    // clamped into the padded plane (clamped bytes only feed displacements
+    // outside the limits)
+    if (wx0 >= -kPad && wx0 + 4 * nwords + 4 <= g.W + kPad && wy0 >= -kPad && wy0 + wrows <= g.H + kPad) {
+        for (int r = warp; r < wrows; r += kPuThreads / 32) {
+            const uintptr_t a = (uintptr_t)(ref + (ptrdiff_t)(wy0 + r) * g.stride + wx0);
+            const uint32_t *aw = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+            const int sh = 8 * (int)(a & 3);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(s_win + r * pitch);
+            for (int c = lane; c < nwords; c += 32) dst[c] = __funnelshift_r(__ldg(aw + c), __ldg(aw + c + 1), sh);
         }
-        // MV bits of the window's columns and rows (me.c:614-641)
-        for (int k = tid; k < 2 * R; k += kPuThreads) {
-            s_bx[k] = mvbits_hd(4 * (st.cx + k - R) - p.mvp_x);
-            s_by[k] = mvbits_hd(4 * (st.cy + k - R) - p.mvp_y);
+    } else {
+        for (int r = warp; r < wrows; r += kPuThreads / 32) {
+            const int y = min(max(wy0 + r, -kPad), g.H + kPad - 1);
+            const uint8_t *row = ref + (ptrdiff_t)y * g.stride;
+            for (int c = lane; c < wcols; c += 32)
+                s_win[r * pitch + c] = row[min(max(wx0 + c, -kPad), g.W + kPad - 1)];
         }
-        // window bytes, clamped into the padded plane (clamped bytes only
-        // feed displacements outside the limits)
-        for (int k = tid; k < wrows * wcols; k += kPuThreads) {
-            const int r = k / wcols, c = k - r * wcols;
-            const int y = min(max(wy0 + r, -kPad), g.H + kPad - 1), x = min(max(wx0 + c, -kPad), g.W + kPad - 1);
-            s_win[r * pitch + c] = ref[(ptrdiff_t)y * g.stride + x];
-        }
-        __syncthreads();
-        unsigned long long best = kNoKey;
-        const int groups = (2 * R + 3) >> 2;       // 4-displacement groups per window row
-        for (int q = tid; q < 2 * R * groups; q += kPuThreads) {
-            const int jr = q / groups, gx = q - jr * groups;   // displacement row j = jr - R, columns 4 gx ..
+    }
+    __syncthreads();
+    // window positions inside the limits
+    const int ilo = max(0, p.min_x - (st.cx - R)), ihi = min(2 * R - 1, p.max_x - (st.cx - R));
+    const int jlo = max(0, p.min_y - (st.cy - R)), jhi = min(2 * R - 1, p.max_y - (st.cy - R));
+    uint32_t bestc = 0xffffffffu, besto = 0;
+    if (ilo <= ihi && jlo <= jhi) {
+        const int g0 = ilo >> 2, ng = (ihi >> 2) - g0 + 1, total = (jhi - jlo + 1) * ng;
+        const int dj = kPuThreads / ng, dg = kPuThreads - dj * ng;
+        int jr = jlo + tid / ng, gx = g0 + tid % ng;
+        for (int q = tid; q < total; q += kPuThreads) {
             uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
             for (int y = 0; y < h; y++) {
                 const uint32_t *wr = reinterpret_cast<const uint32_t *>(s_win + (jr + y) * pitch) + gx;
@@ -235,28 +259,52 @@ __global__ void __launch_bounds__(kPuThreads) fs_generic_kernel(const uint32_t *
                     lo = hi;
                 }
             }
-            const int my = st.cy + jr - R, by = s_by[jr];
+            const L ly = s_ly[jr];
             const uint32_t sads[4] = {a0, a1, a2, a3};
 #pragma unroll
             for (int t = 0; t < 4; t++) {
-                const int ir = 4 * gx + t, mx = st.cx + ir - R;
-                if (ir >= 2 * R || !in_box(p, mx, my)) continue;
-                const int cost = (int)sads[t] + (int)(((int64_t)lambda * (s_bx[ir] + by)) >> 16);
-                const unsigned long long k = ((unsigned long long)(unsigned)cost << 32) | (unsigned)(2 + jr * 2 * R + ir);
-                best = k < best ? k : best;
+                const int ir = 4 * gx + t;
+                const uint32_t cost = sads[t] + (uint32_t)((s_lx[min(ir, 2 * R - 1)] + ly) >> 16);
+                if (ir >= ilo && ir <= ihi && cost < bestc) {
+                    bestc = cost;
+                    besto = (uint32_t)(jr * 2 * R + ir);
+                }
+            }
+            gx += dg;
+            jr += dj;
+            if (gx >= g0 + ng) {
+                gx -= ng;
+                jr++;
             }
         }
+    }
+    unsigned long long best = bestc == 0xffffffffu ? kNoKey : ((unsigned long long)bestc << 32) | (2u + besto);
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, off);
-            best = other < best ? other : best;
-        }
-        if ((tid & 31) == 0) s_red[tid >> 5] = best;
-        __syncthreads();
-        if (tid == 0) {
-            for (int k = 1; k < kPuThreads / 32; k++) best = s_red[k] < best ? s_red[k] : best;
-            if (best != kNoKey) atomicMin(&v.keys[i], best);
-        }
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, off);
+        best = other < best ? other : best;
+    }
+    if (lane == 0) s_red[warp] = best;
+    __syncthreads();
+    if (tid == 0) {
+        for (int k = 1; k < kPuThreads / 32; k++) best = s_red[k] < best ? s_red[k] : best;
+        if (best != kNoKey) atomicMin(&keys[i], best);
+    }
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kPuThreads) fs_generic_kernel(const uint32_t *__restrict__ list, int n,
+                                                                const SessView *__restrict__ views, int R, int lambda)
+{
+    extern __shared__ __align__(16) uint8_t smem_pu[];
+    for (int li = blockIdx.x; li < n; li += gridDim.x) {
+        const uint32_t e = list[li];
+        const SessView &v = views[e >> kSessShift];
+        const int i = (int)(e & kIdxMask);
+        const PuState st = v.state[i];
+        if (!st.valid) continue;       // uniform over the CTA
+        __syncthreads();               // the previous PU's readers are done
+        fs_pu_search<WIDE>(v.pus[i], st, v, R, lambda, smem_pu, v.keys, i);
     }
 }
 
@@ -269,11 +317,15 @@ static int fs_generic_launch(const uint32_t *list, int n, const SessView *views,
     const int bytes = fs_pu_smem(R);
     if (dev < 0 || dev >= 64) return XAVS2GPU_ERR_ARG;
     if (attr_bytes[dev] < bytes) {
-        XG_CUDA(cudaFuncSetAttribute(fs_generic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        XG_CUDA(cudaFuncSetAttribute(fs_generic_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        XG_CUDA(cudaFuncSetAttribute(fs_generic_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         attr_bytes[dev] = bytes;
     }
-    const int cap = sm_count() * 8;
-    fs_generic_kernel<<<n < cap ? n : cap, kPuThreads, bytes, st>>>(list, n, views, R, lambda);
+    const int cap = sm_count() * 8, grid = n < cap ? n : cap;
+    if (lambda < (1 << 24))
+        fs_generic_kernel<false><<<grid, kPuThreads, bytes, st>>>(list, n, views, R, lambda);
+    else
+        fs_generic_kernel<true><<<grid, kPuThreads, bytes, st>>>(list, n, views, R, lambda);
     count_launch();
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
