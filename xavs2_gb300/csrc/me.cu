@@ -160,20 +160,25 @@ __global__ void reset_keys_kernel(const SessView *__restrict__ views, int nviews
 // groups of 4 horizontally adjacent displacements: per block row and 4-pixel
 // word it reads the block word (the same for the whole warp) and one new
 // window word, aligns the window at the 4 byte offsets with byte permutes and
-// accumulates 4 SADs with vabsdiff4.  Only the rows and column groups inside
-// the PU's limits are visited.  lambda x MV bits per column / row of the
-// window come from shared tables (me.c:614-641): the cost of (i, j) is
-// SAD + (lx[i] + ly[j]) >> 16.  Visit order of window position (i, j) is
-// 2 + (j+R)*2R + (i+R); a thread visits its positions in increasing order,
-// so a strictly smaller 32-bit cost keeps the first minimum, and the CTA's
+// accumulates 4 SADs with vabsdiff4.  A thread owns one column group and
+// kPuRows consecutive displacement rows at a time: each window word it loads
+// and aligns serves the block rows of all kPuRows displacement rows, so the
+// loads and permutes are shared by kPuRows x 4 displacements.  Only the rows
+// and column groups inside the PU's limits are visited.  lambda x MV bits per
+// column / row of the window come from shared tables (me.c:614-641): the
+// cost of (i, j) is SAD + (lx[i] + ly[j]) >> 16.  Visit order of window
+// position (i, j) is 2 + (j+R)*2R + (i+R); a thread's column group is fixed
+// and its row blocks ascend, so it visits its positions in increasing order
+// and a strictly smaller 32-bit cost keeps the first minimum; the CTA's
 // (cost, order) keys are reduced and merged with atomicMin.
 constexpr int kPuThreads = 256;
+constexpr int kPuRows = 4;        // displacement rows per thread and pass
 
 // dynamic shared memory the per-PU search needs for range R
 __host__ __device__ __forceinline__ int fs_pu_smem(int R)
 {
     const int pitch = ((2 * R + 64 + 8 + 15) / 16) * 16;          // window bytes per row (max block 64)
-    return 64 * 64 + 2 * (2 * R) * 8 + (2 * R + 64) * pitch + 8 * 8;
+    return 64 * 64 + 2 * (2 * R) * 8 + (2 * R + 64 + kPuRows) * pitch + 8 * 8;
 }
 
 // lambda x bits with lambda < 2^24 and bits < 128 fits 31 bits; larger
@@ -193,13 +198,15 @@ __device__ __forceinline__ void fs_pu_search(const xavs2gpu_pu_t &p, const PuSta
     L *s_ly = s_lx + 2 * R;                                                  // [2R] per row
     uint8_t *s_win = smem_pu + 64 * 64 + 2 * (2 * R) * 8;                    // [2R + h - 1][pitch]
     const int pitch = ((2 * R + 64 + 8 + 15) / 16) * 16;
-    unsigned long long *s_red = reinterpret_cast<unsigned long long *>(s_win + (2 * R + 64) * pitch);
+    unsigned long long *s_red = reinterpret_cast<unsigned long long *>(s_win + (2 * R + 64 + kPuRows) * pitch);
     const Geometry g = v.g;
     const int w = c_pu_w[p.part], h = c_pu_h[p.part], wq = w >> 2;
     const int wx0 = p.x + st.cx - R, wy0 = p.y + st.cy - R;   // window origin (displacement -R, -R)
     // bytes read per row: the last group of 4 displacements starts at most
     // at 2R - 2 (odd R) and its words reach 6 bytes past the block width
-    const int wcols = 2 * R + w + 6, wrows = 2 * R + h - 1, nwords = (wcols + 3) >> 2;
+    // rows: the last row block of kPuRows may reach kPuRows - 1 rows past the
+    // window (their sums are dropped)
+    const int wcols = 2 * R + w + 6, wrows = 2 * R + h - 1 + kPuRows - 1, nwords = (wcols + 3) >> 2;
     const uint8_t *ref = v.ref0[p.ref];
     // block words
     const uint8_t *o = v.cur + (ptrdiff_t)p.y * g.stride + p.x;
@@ -219,9 +226,10 @@ __device__ __forceinline__ void fs_pu_search(const xavs2gpu_pu_t &p, const PuSta
     // words (the 4 bytes past the row's last word included); elsewhere bytes
     // clamped into the padded plane (clamped bytes only feed displacements
     // outside the limits)
-    if (wx0 >= -kPad && wx0 + 4 * nwords + 4 <= g.W + kPad && wy0 >= -kPad && wy0 + wrows <= g.H + kPad) {
+    if (wx0 >= -kPad && wx0 + 4 * nwords + 4 <= g.W + kPad && wy0 >= -kPad) {
         for (int r = warp; r < wrows; r += kPuThreads / 32) {
-            const uintptr_t a = (uintptr_t)(ref + (ptrdiff_t)(wy0 + r) * g.stride + wx0);
+            const int y = min(wy0 + r, g.H + kPad - 1);
+            const uintptr_t a = (uintptr_t)(ref + (ptrdiff_t)y * g.stride + wx0);
             const uint32_t *aw = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
             const int sh = 8 * (int)(a & 3);
             uint32_t *dst = reinterpret_cast<uint32_t *>(s_win + r * pitch);
@@ -240,41 +248,57 @@ __device__ __forceinline__ void fs_pu_search(const xavs2gpu_pu_t &p, const PuSta
     const int ilo = max(0, p.min_x - (st.cx - R)), ihi = min(2 * R - 1, p.max_x - (st.cx - R));
     const int jlo = max(0, p.min_y - (st.cy - R)), jhi = min(2 * R - 1, p.max_y - (st.cy - R));
     uint32_t bestc = 0xffffffffu, besto = 0;
-    if (ilo <= ihi && jlo <= jhi) {
-        const int g0 = ilo >> 2, ng = (ihi >> 2) - g0 + 1, total = (jhi - jlo + 1) * ng;
-        const int dj = kPuThreads / ng, dg = kPuThreads - dj * ng;
-        int jr = jlo + tid / ng, gx = g0 + tid % ng;
-        for (int q = tid; q < total; q += kPuThreads) {
-            uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-            for (int y = 0; y < h; y++) {
-                const uint32_t *wr = reinterpret_cast<const uint32_t *>(s_win + (jr + y) * pitch) + gx;
-                const uint32_t *cr = s_cur + y * wq;
+    const int g0 = ilo >> 2, ng = (ihi >> 2) - g0 + 1;
+    const int tpg = ng > 0 ? kPuThreads / ng : 0;           // threads per column group
+    if (ilo <= ihi && jlo <= jhi && tid < tpg * ng) {
+        const int gx = g0 + tid % ng, trow = tid / ng;
+        L lx[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) lx[t] = s_lx[min(4 * gx + t, 2 * R - 1)];
+        for (int jr0 = jlo + kPuRows * trow; jr0 <= jhi; jr0 += kPuRows * tpg) {
+            uint32_t acc[kPuRows][4];
+#pragma unroll
+            for (int i = 0; i < kPuRows; i++)
+#pragma unroll
+                for (int t = 0; t < 4; t++) acc[i][t] = 0;
+            for (int r = 0; r < h + kPuRows - 1; r++) {
+                // window row jr0 + r meets block row y = r - i of displacement row jr0 + i
+                bool live[kPuRows];
+#pragma unroll
+                for (int i = 0; i < kPuRows; i++) live[i] = r - i >= 0 && r - i < h;
+                const uint32_t *wr = reinterpret_cast<const uint32_t *>(s_win + (jr0 + r) * pitch) + gx;
+                const uint32_t *cr = s_cur + r * wq;
                 uint32_t lo = wr[0];
                 for (int c = 0; c < wq; c++) {
-                    const uint32_t hi = wr[c + 1], cw = cr[c];
-                    a0 = sad4_acc(cw, lo, a0);
-                    a1 = sad4_acc(cw, __byte_perm(lo, hi, 0x4321), a1);
-                    a2 = sad4_acc(cw, __byte_perm(lo, hi, 0x5432), a2);
-                    a3 = sad4_acc(cw, __byte_perm(lo, hi, 0x6543), a3);
+                    const uint32_t hi = wr[c + 1];
+                    const uint32_t b1 = __byte_perm(lo, hi, 0x4321), b2 = __byte_perm(lo, hi, 0x5432),
+                                   b3 = __byte_perm(lo, hi, 0x6543);
+#pragma unroll
+                    for (int i = 0; i < kPuRows; i++) {
+                        if (!live[i]) continue;
+                        const uint32_t cw = cr[c - i * wq];
+                        acc[i][0] = sad4_acc(cw, lo, acc[i][0]);
+                        acc[i][1] = sad4_acc(cw, b1, acc[i][1]);
+                        acc[i][2] = sad4_acc(cw, b2, acc[i][2]);
+                        acc[i][3] = sad4_acc(cw, b3, acc[i][3]);
+                    }
                     lo = hi;
                 }
             }
-            const L ly = s_ly[jr];
-            const uint32_t sads[4] = {a0, a1, a2, a3};
 #pragma unroll
-            for (int t = 0; t < 4; t++) {
-                const int ir = 4 * gx + t;
-                const uint32_t cost = sads[t] + (uint32_t)((s_lx[min(ir, 2 * R - 1)] + ly) >> 16);
-                if (ir >= ilo && ir <= ihi && cost < bestc) {
-                    bestc = cost;
-                    besto = (uint32_t)(jr * 2 * R + ir);
+            for (int i = 0; i < kPuRows; i++) {
+                const int jr = jr0 + i;
+                if (jr > jhi) break;
+                const L ly = s_ly[jr];
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const int ir = 4 * gx + t;
+                    const uint32_t cost = acc[i][t] + (uint32_t)((lx[t] + ly) >> 16);
+                    if (ir >= ilo && ir <= ihi && cost < bestc) {
+                        bestc = cost;
+                        besto = (uint32_t)(jr * 2 * R + ir);
+                    }
                 }
-            }
-            gx += dg;
-            jr += dj;
-            if (gx >= g0 + ng) {
-                gx -= ng;
-                jr++;
             }
         }
     }
