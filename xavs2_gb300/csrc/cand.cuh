@@ -22,6 +22,8 @@
 
 #include "xavs2gpu_common.cuh"
 
+#include <vector>
+
 namespace xg {
 
 // The picture a group of candidates belongs to.  The chain has one; a
@@ -33,11 +35,14 @@ struct PicView {
     const xavs2gpu_cu_t *cus;           // leaf CUs
     const xavs2gpu_cand_t *cands;       // candidate table (picture-local offsets)
     const int32_t *cu_cand;             // per CU: first candidate; [n_cus] = number of candidates
+    const int32_t *cand_units;          // work units over candidates: candidate << 2 | chunk
+    const int32_t *cu_units;            // work units over CUs: CU << 2 | chunk
     uint8_t *recon;                     // reconstructed picture (stride `width`)
     unsigned long long *hash;           // serving checksum
     int64_t res_off, coef_off;          // base of the picture in the batch residual / level buffers
     int64_t cu_start;                   // first batch-wide CU index of the picture
     int64_t cand_start;                 // first batch-wide candidate index of the picture
+    int64_t cand_unit_start, cu_unit_start;   // first batch-wide work units of the picture
     int64_t n_coef;                     // levels of the picture
     int n_cus, n_cands, stride, width, height, nrefs, n_pus;
 };
@@ -159,18 +164,42 @@ __device__ __forceinline__ unsigned ssd4(uint32_t a, uint32_t b, unsigned acc)
     return __dp4a(d, d, acc);
 }
 
-// Warp per candidate: prediction, residual in both TU layouts, the five TU
-// descriptors, and the sum of the mode's search costs.
+// Work units: a warp takes at most kUnitPx pixels of a candidate (residual,
+// SSD) or of a CU (reconstruction); the 64x64 CUs split into 4 units, so no
+// warp runs four times longer than the rest of the launch.
+constexpr int kUnitPx = 1024;
+static inline void build_units(const xavs2gpu_cu_t *cus, int n_cus, const xavs2gpu_cand_t *cands, int n_cands,
+                               std::vector<int32_t> &units, int &n_cand_units, int &n_cu_units)
+{
+    units.clear();
+    for (int i = 0; i < n_cands; i++) {
+        const int S = cus[cands[i].cu].size, nu = S * S > kUnitPx ? S * S / kUnitPx : 1;
+        for (int k = 0; k < nu; k++) units.push_back(i << 2 | k);
+    }
+    n_cand_units = (int)units.size();
+    for (int c = 0; c < n_cus; c++) {
+        const int S = cus[c].size, nu = S * S > kUnitPx ? S * S / kUnitPx : 1;
+        for (int k = 0; k < nu; k++) units.push_back(c << 2 | k);
+    }
+    n_cu_units = (int)units.size() - n_cand_units;
+}
+
+// Warp per candidate unit: prediction and residual in both TU layouts; the
+// first unit of a candidate also writes its five TU descriptors, the sum of
+// the mode's search costs and zeroes its two SSDs.
 static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
                                                             int qp, int16_t *__restrict__ residual,
                                                             xavs2gpu_tq_block_t *__restrict__ blocks,
-                                                            int32_t *__restrict__ cand_cost)
+                                                            int32_t *__restrict__ cand_cost, int32_t *__restrict__ dist)
 {
     const int lane = threadIdx.x & 31;
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const PicView &v = views[find_view<&PicView::cand_start>(views, nviews, i)];
-    const xavs2gpu_cand_t cd = v.cands[i - v.cand_start];
+    const int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (u >= n) return;
+    const PicView &v = views[find_view<&PicView::cand_unit_start>(views, nviews, u)];
+    const int32_t ue = v.cand_units[u - v.cand_unit_start];
+    const int chunk = ue & 3;
+    const int64_t i = v.cand_start + (ue >> 2);
+    const xavs2gpu_cand_t cd = v.cands[ue >> 2];
     const xavs2gpu_cu_t *cp = v.cus + cd.cu;
     const int cx = cp->x, cy = cp->y, S = cp->size, lg = 31 - __clz(S), mode = cd.mode;
     const PuPick p0 = best_ref(v, cp, mode_pu_index(mode, 0));
@@ -178,7 +207,8 @@ static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView
     const uint8_t *pr0 = pred_ptr(v, cx, cy, p0), *pr1 = pred_ptr(v, cx, cy, p1);
     const uint8_t *src = v.cur + (ptrdiff_t)cy * v.stride + cx;
     int16_t *whole = residual + v.res_off + cd.res_offset, *split = whole + S * S;
-    for (int e = 4 * lane; e < S * S; e += 128) {
+    const int e1 = min(S * S, (chunk + 1) * kUnitPx);
+    for (int e = chunk * kUnitPx + 4 * lane; e < e1; e += 128) {
         const int yy = e >> lg, xx = e & (S - 1);
         const ptrdiff_t o = (ptrdiff_t)yy * v.stride + xx;
         const uint8_t *pr = mode_pu_of(mode, S, xx, yy) ? pr1 : pr0;
@@ -186,6 +216,7 @@ static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView
         *reinterpret_cast<uint2 *>(whole + e) = r;
         *reinterpret_cast<uint2 *>(split + split_offset(cd.split_type, S, xx, yy)) = r;
     }
+    if (chunk) return;
     if (lane < 5) {
         xavs2gpu_tq_block_t b;
         b.qp = qp;
@@ -207,18 +238,23 @@ static __global__ void __launch_bounds__(128) cand_residual_kernel(const PicView
         blocks[5 * i + lane] = b;
     }
     if (lane == 0) cand_cost[i] = p0.cost + (mode ? p1.cost : 0);
+    if (lane < 2) dist[2 * i + lane] = 0;
 }
 
-// Warp per candidate: SSD of clip(pred + reconstructed residual) against the
-// current picture for both TU variants (dist[2 i] one TU, dist[2 i + 1] split).
+// Warp per candidate unit: SSD of clip(pred + reconstructed residual) against
+// the current picture for both TU variants, added into dist[2 i] (one TU) and
+// dist[2 i + 1] (split).
 static __global__ void __launch_bounds__(128) cand_eval_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
                                                         const int16_t *__restrict__ rres, int32_t *__restrict__ dist)
 {
     const int lane = threadIdx.x & 31;
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const PicView &v = views[find_view<&PicView::cand_start>(views, nviews, i)];
-    const xavs2gpu_cand_t cd = v.cands[i - v.cand_start];
+    const int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (u >= n) return;
+    const PicView &v = views[find_view<&PicView::cand_unit_start>(views, nviews, u)];
+    const int32_t ue = v.cand_units[u - v.cand_unit_start];
+    const int chunk = ue & 3;
+    const int64_t i = v.cand_start + (ue >> 2);
+    const xavs2gpu_cand_t cd = v.cands[ue >> 2];
     const xavs2gpu_cu_t *cp = v.cus + cd.cu;
     const int cx = cp->x, cy = cp->y, S = cp->size, lg = 31 - __clz(S), mode = cd.mode;
     const PuPick p0 = best_ref(v, cp, mode_pu_index(mode, 0));
@@ -227,7 +263,8 @@ static __global__ void __launch_bounds__(128) cand_eval_kernel(const PicView *__
     const uint8_t *src = v.cur + (ptrdiff_t)cy * v.stride + cx;
     const int16_t *whole = rres + v.res_off + cd.res_offset, *split = whole + S * S;
     unsigned d0 = 0, d1 = 0;
-    for (int e = 4 * lane; e < S * S; e += 128) {
+    const int e1 = min(S * S, (chunk + 1) * kUnitPx);
+    for (int e = chunk * kUnitPx + 4 * lane; e < e1; e += 128) {
         const int yy = e >> lg, xx = e & (S - 1);
         const ptrdiff_t o = (ptrdiff_t)yy * v.stride + xx;
         const uint32_t p4 = load4u((mode_pu_of(mode, S, xx, yy) ? pr1 : pr0) + o);
@@ -241,13 +278,14 @@ static __global__ void __launch_bounds__(128) cand_eval_kernel(const PicView *__
         d1 += __shfl_xor_sync(0xffffffffu, d1, o);
     }
     if (lane == 0) {
-        dist[2 * i] = (int32_t)d0;
-        dist[2 * i + 1] = (int32_t)d1;
+        atomicAdd(&dist[2 * i], (int32_t)d0);
+        atomicAdd(&dist[2 * i + 1], (int32_t)d1);
     }
 }
 
-// Warp per CU: the mode with the smallest search cost, then the TU variant
-// with the smaller SSD; its reconstruction into the picture.
+// Warp per CU unit: the mode with the smallest search cost, then the TU
+// variant with the smaller SSD; its reconstruction into the picture (the
+// unit's pixels); the first unit records the choice.
 static __global__ void __launch_bounds__(128) cand_choose_kernel(const PicView *__restrict__ views, int nviews, int64_t n,
                                                           const int32_t *__restrict__ cand_cost,
                                                           const int32_t *__restrict__ dist,
@@ -255,10 +293,12 @@ static __global__ void __launch_bounds__(128) cand_choose_kernel(const PicView *
                                                           xavs2gpu_cu_choice_t *__restrict__ choice)
 {
     const int lane = threadIdx.x & 31;
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const PicView &v = views[find_view<&PicView::cu_start>(views, nviews, i)];
-    const int ci = (int)(i - v.cu_start);
+    const int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (u >= n) return;
+    const PicView &v = views[find_view<&PicView::cu_unit_start>(views, nviews, u)];
+    const int32_t ue = v.cu_units[u - v.cu_unit_start];
+    const int chunk = ue & 3, ci = ue >> 2;
+    const int64_t i = v.cu_start + ci;
     const int64_t first = v.cand_start + v.cu_cand[ci], last = v.cand_start + v.cu_cand[ci + 1];
     int64_t best = first;
     for (int64_t k = first + 1; k < last; k++)
@@ -273,7 +313,8 @@ static __global__ void __launch_bounds__(128) cand_choose_kernel(const PicView *
     const int16_t *r = rres + v.res_off + cd.res_offset + (split ? S * S : 0);
     uint8_t *o = v.recon + (ptrdiff_t)cy * v.width + cx;
     const bool aligned = (v.width & 3) == 0;     // word stores into the reconstruction
-    for (int e = 4 * lane; e < S * S; e += 128) {
+    const int e1 = min(S * S, (chunk + 1) * kUnitPx);
+    for (int e = chunk * kUnitPx + 4 * lane; e < e1; e += 128) {
         const int yy = e >> lg, xx = e & (S - 1);
         const uint32_t p4 = load4u((mode_pu_of(mode, S, xx, yy) ? pr1 : pr0) + (ptrdiff_t)yy * v.stride + xx);
         const uint32_t q = recon4(p4, *reinterpret_cast<const uint2 *>(r + (split ? split_offset(cd.split_type, S, xx, yy) : e)));
@@ -284,7 +325,7 @@ static __global__ void __launch_bounds__(128) cand_choose_kernel(const PicView *
             d[0] = (uint8_t)q; d[1] = (uint8_t)(q >> 8); d[2] = (uint8_t)(q >> 16); d[3] = (uint8_t)(q >> 24);
         }
     }
-    if (lane == 0) {
+    if (lane == 0 && chunk == 0) {
         xavs2gpu_cu_choice_t ch;
         ch.cand = (int32_t)(best - v.cand_start);
         ch.mode = (int16_t)mode;

@@ -94,6 +94,8 @@ struct xavs2gpu_chain {
     xavs2gpu_cu_t *d_cus = nullptr;
     xavs2gpu_cand_t *d_cands = nullptr;
     int32_t *d_cu_cand = nullptr, *d_cost = nullptr, *d_dist = nullptr;
+    int32_t *d_units = nullptr;                  // candidate units, then CU units
+    int n_cand_units = 0, n_cu_units = 0;
     int16_t *d_res = nullptr, *d_rres = nullptr, *d_coef = nullptr;
     int32_t *d_nnz = nullptr;
     xavs2gpu_cu_choice_t *d_choice = nullptr;
@@ -119,17 +121,17 @@ int chain_enqueue(xavs2gpu_chain_t *c, const xavs2gpu_me_params_t *prm)
         if ((rc = xavs2gpu_me_set_picture_device(c->s, r, c->src(1 + r), c->W)) != XAVS2GPU_OK) return rc;
     if ((rc = xavs2gpu_me_set_picture_device(c->s, -1, c->src(0), c->W)) != XAVS2GPU_OK) return rc;
     if ((rc = xavs2gpu_me_run(c->s, prm)) != XAVS2GPU_OK) return rc;
-    const unsigned cand_blocks = (unsigned)((c->n_cands * 32 + 127) / 128);
-    cand_residual_kernel<<<cand_blocks, 128, 0, c->st>>>(c->d_view, 1, c->n_cands, c->qp, c->d_res, c->d_blocks,
-                                                         c->d_cost);
+    const unsigned cand_blocks = (unsigned)(((int64_t)c->n_cand_units * 32 + 127) / 128);
+    cand_residual_kernel<<<cand_blocks, 128, 0, c->st>>>(c->d_view, 1, c->n_cand_units, c->qp, c->d_res, c->d_blocks,
+                                                         c->d_cost, c->d_dist);
     count_launch();
     if ((rc = tq_batch_launch(c->d_blocks, (int)(5 * c->n_cands), c->d_res, c->d_coef, c->d_rres, c->d_nnz,
                               c->tq_warps, c->st)) != XAVS2GPU_OK)
         return rc;
-    cand_eval_kernel<<<cand_blocks, 128, 0, c->st>>>(c->d_view, 1, c->n_cands, c->d_rres, c->d_dist);
+    cand_eval_kernel<<<cand_blocks, 128, 0, c->st>>>(c->d_view, 1, c->n_cand_units, c->d_rres, c->d_dist);
     count_launch();
-    cand_choose_kernel<<<(c->n_cus * 32 + 127) / 128, 128, 0, c->st>>>(c->d_view, 1, c->n_cus, c->d_cost, c->d_dist,
-                                                                       c->d_rres, c->d_choice);
+    cand_choose_kernel<<<(unsigned)(((int64_t)c->n_cu_units * 32 + 127) / 128), 128, 0, c->st>>>(
+        c->d_view, 1, c->n_cu_units, c->d_cost, c->d_dist, c->d_rres, c->d_choice);
     count_launch();
     if (c->flags & 1) {
         const size_t pic = (size_t)c->W * c->H;
@@ -195,6 +197,10 @@ extern "C" xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, con
     XG_CUDA(cudaMemcpy(c->d_cands, cands.data(), sizeof(xavs2gpu_cand_t) * cands.size(), cudaMemcpyHostToDevice));
     XG_CUDA(cudaMalloc((void **)&c->d_cu_cand, sizeof(int32_t) * cu_cand.size()));
     XG_CUDA(cudaMemcpy(c->d_cu_cand, cu_cand.data(), sizeof(int32_t) * cu_cand.size(), cudaMemcpyHostToDevice));
+    std::vector<int32_t> units;
+    build_units(cus, n_cus, cands.data(), (int)cands.size(), units, c->n_cand_units, c->n_cu_units);
+    XG_CUDA(cudaMalloc((void **)&c->d_units, sizeof(int32_t) * units.size()));
+    XG_CUDA(cudaMemcpy(c->d_units, units.data(), sizeof(int32_t) * units.size(), cudaMemcpyHostToDevice));
     XG_CUDA(cudaMalloc((void **)&c->d_cost, sizeof(int32_t) * c->n_cands));
     XG_CUDA(cudaMalloc((void **)&c->d_dist, sizeof(int32_t) * 2 * c->n_cands));
     XG_CUDA(cudaMalloc((void **)&c->d_res, sizeof(int16_t) * n_res));
@@ -219,6 +225,9 @@ extern "C" xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, con
     v.cus = c->d_cus;
     v.cands = c->d_cands;
     v.cu_cand = c->d_cu_cand;
+    v.cand_units = c->d_units;
+    v.cu_units = c->d_units + c->n_cand_units;
+    v.cand_unit_start = v.cu_unit_start = 0;
     v.recon = c->d_recon;
     v.hash = nullptr;
     v.res_off = v.coef_off = v.cu_start = v.cand_start = 0;
@@ -244,7 +253,7 @@ extern "C" void xavs2gpu_chain_destroy(xavs2gpu_chain_t *c)
     cudaFree(c->d_cus); cudaFree(c->d_res); cudaFree(c->d_rres); cudaFree(c->d_coef); cudaFree(c->d_nnz);
     cudaFree(c->d_choice); cudaFree(c->d_blocks); cudaFree(c->d_src); cudaFree(c->d_recon);
     cudaFree((void *)c->d_planes); cudaFree(c->d_cands); cudaFree(c->d_cu_cand); cudaFree(c->d_cost);
-    cudaFree(c->d_dist); cudaFree(c->d_view);
+    cudaFree(c->d_dist); cudaFree(c->d_view); cudaFree(c->d_units);
     delete c;
 }
 

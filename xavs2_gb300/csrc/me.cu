@@ -172,7 +172,10 @@ __global__ void reset_keys_kernel(const SessView *__restrict__ views, int nviews
 // and a strictly smaller 32-bit cost keeps the first minimum; the CTA's
 // (cost, order) keys are reduced and merged with atomicMin.
 constexpr int kPuThreads = 256;
-constexpr int kPuRows = 4;        // displacement rows per thread and pass
+#ifndef XG_PU_ROWS
+#define XG_PU_ROWS 4
+#endif
+constexpr int kPuRows = XG_PU_ROWS;   // displacement rows per thread and pass
 
 // dynamic shared memory the per-PU search needs for range R
 __host__ __device__ __forceinline__ int fs_pu_smem(int R)

@@ -96,7 +96,8 @@ struct Stream {
     xavs2gpu_cu_t *d_cus = nullptr;
     xavs2gpu_cand_t *d_cands = nullptr;
     int32_t *d_cu_cand = nullptr;
-    int n_cus = 0, n_pus = 0, n_cands = 0;
+    int32_t *d_units = nullptr;                   // candidate units, then CU units
+    int n_cus = 0, n_pus = 0, n_cands = 0, n_cand_units = 0, n_cu_units = 0;
     int64_t n_res = 0, n_coef = 0;
     uint8_t *d_in = nullptr, *d_prev = nullptr;   // upload buffer, previous picture (next reference)
     uint8_t *h_ring = nullptr;                    // pinned picture slots
@@ -166,7 +167,8 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
     std::vector<xavs2gpu_me_session_t *> sess;
     b.searched.clear();
     XG_CUDA(cudaEventRecord(b.start, b.st));
-    int64_t res_off = 0, coef_off = 0, cu_start = 0, cand_start = 0, rec_off = 0;
+    int64_t res_off = 0, coef_off = 0, cu_start = 0, cand_start = 0, rec_off = 0, cand_unit_start = 0,
+            cu_unit_start = 0;
     int nv = 0;
     for (size_t k = 0; k < b.jobs.size(); k++) {
         Job &j = b.jobs[k];
@@ -189,6 +191,10 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
             v.cus = S.d_cus;
             v.cands = S.d_cands;
             v.cu_cand = S.d_cu_cand;
+            v.cand_units = S.d_units;
+            v.cu_units = S.d_units + S.n_cand_units;
+            v.cand_unit_start = cand_unit_start;
+            v.cu_unit_start = cu_unit_start;
             v.recon = b.d_recon + rec_off;
             v.hash = b.d_hash + (nv - 1);
             v.res_off = res_off;
@@ -207,6 +213,8 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
             coef_off += S.n_coef;
             cu_start += S.n_cus;
             cand_start += S.n_cands;
+            cand_unit_start += S.n_cand_units;
+            cu_unit_start += S.n_cu_units;
             rec_off += (int64_t)pic;
         }
         std::swap(S.d_in, S.d_prev);
@@ -216,11 +224,12 @@ void enqueue_batch(xavs2gpu_server_t *s, BatchSet &b)
         xavs2gpu_me_batch_run(b.me, sess.data(), (int)sess.size(), &s->cfg.me, b.st);
         XG_CUDA(cudaMemcpyAsync(b.d_views, b.h_views, sizeof(JobView) * nv, cudaMemcpyHostToDevice, b.st));
         XG_CUDA(cudaMemsetAsync(b.d_hash, 0, sizeof(unsigned long long) * nv, b.st));
-        const int64_t nc = cand_start, ncu = cu_start;
-        const unsigned cblocks = (unsigned)((nc * 32 + 127) / 128);
-        cand_residual_kernel<<<cblocks, 128, 0, b.st>>>(b.d_views, nv, nc, s->cfg.qp, b.d_res, b.d_blocks, b.d_cost);
+        const int64_t nc = cand_start, ncu = cu_unit_start, ncand_u = cand_unit_start;
+        const unsigned cblocks = (unsigned)((ncand_u * 32 + 127) / 128);
+        cand_residual_kernel<<<cblocks, 128, 0, b.st>>>(b.d_views, nv, ncand_u, s->cfg.qp, b.d_res, b.d_blocks, b.d_cost,
+                                                        b.d_dist);
         tq_batch_launch(b.d_blocks, (int)(5 * nc), b.d_res, b.d_coef, b.d_rres, b.d_nnz, 4, b.st);
-        cand_eval_kernel<<<cblocks, 128, 0, b.st>>>(b.d_views, nv, nc, b.d_rres, b.d_dist);
+        cand_eval_kernel<<<cblocks, 128, 0, b.st>>>(b.d_views, nv, ncand_u, b.d_rres, b.d_dist);
         cand_choose_kernel<<<(unsigned)((ncu * 32 + 127) / 128), 128, 0, b.st>>>(b.d_views, nv, ncu, b.d_cost,
                                                                                  b.d_dist, b.d_rres, b.d_choice);
         int64_t max_words = 0;
@@ -408,7 +417,7 @@ extern "C" void xavs2gpu_server_destroy(xavs2gpu_server_t *s)
         xavs2gpu_me_set_stream(S->sess, nullptr);
         xavs2gpu_me_destroy(S->sess);
         cudaFree(S->d_cus); cudaFree(S->d_in); cudaFree(S->d_prev); cudaFreeHost(S->h_ring);
-        cudaFree(S->d_cands); cudaFree(S->d_cu_cand);
+        cudaFree(S->d_cands); cudaFree(S->d_cu_cand); cudaFree(S->d_units);
         delete S;
     }
     for (auto &b : s->sets) free_set(b);
@@ -440,7 +449,8 @@ extern "C" int xavs2gpu_server_open_stream(xavs2gpu_server_t *s, int width, int 
     // candidates, two pictures
     const int64_t plane = (int64_t)((width + 160 + 63) / 64 * 64) * (height + 160);
     const int64_t need = 33 * plane + (int64_t)n_pus * (18 + 20 + 8 + 12 + 16) + (int64_t)n_cus * 44 +
-                         (int64_t)cands.size() * 24 + 2 * (int64_t)width * height + (int64_t)n_cus * 849 * 4 / 16;
+                         (int64_t)cands.size() * 24 + 2 * (int64_t)width * height + (int64_t)n_cus * 849 * 4 / 16 +
+                         (int64_t)cands.size() * 16 + (int64_t)n_cus * 16;
     std::unique_lock<std::mutex> lk(s->mu);
     if (s->cfg.hbm_budget_bytes > 0 && s->hbm_used + need > s->cfg.hbm_budget_bytes) {
         fail(XAVS2GPU_ERR_CAPACITY, "xavs2gpu_server_open_stream", "device-memory budget exhausted");
@@ -488,6 +498,10 @@ extern "C" int xavs2gpu_server_open_stream(xavs2gpu_server_t *s, int width, int 
     XG_CUDA(cudaMemcpy(S->d_cands, cands.data(), sizeof(xavs2gpu_cand_t) * cands.size(), cudaMemcpyHostToDevice));
     XG_CUDA(cudaMalloc((void **)&S->d_cu_cand, sizeof(int32_t) * cu_cand.size()));
     XG_CUDA(cudaMemcpy(S->d_cu_cand, cu_cand.data(), sizeof(int32_t) * cu_cand.size(), cudaMemcpyHostToDevice));
+    std::vector<int32_t> units;
+    build_units(cus, n_cus, cands.data(), (int)cands.size(), units, S->n_cand_units, S->n_cu_units);
+    XG_CUDA(cudaMalloc((void **)&S->d_units, sizeof(int32_t) * units.size()));
+    XG_CUDA(cudaMemcpy(S->d_units, units.data(), sizeof(int32_t) * units.size(), cudaMemcpyHostToDevice));
     XG_CUDA(cudaMalloc((void **)&S->d_in, (size_t)width * height));
     XG_CUDA(cudaMalloc((void **)&S->d_prev, (size_t)width * height));
     XG_CUDA(cudaMallocHost((void **)&S->h_ring, (size_t)width * height * ring));
