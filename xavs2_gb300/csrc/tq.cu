@@ -270,10 +270,20 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
         constexpr int PX = 66, HP = 34, PL = TW + 2;
         if (act) {
             if (al_in) {
-                for (int e = lane; e < IW * IH / 8; e += 32) {
-                    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src) + e);
-                    uint32_t *d = reinterpret_cast<uint32_t *>(tA + ((e * 8) / IW) * PX + (e * 8) % IW);
-                    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+                // the lane's 16-byte loads in batches of 8 (a batch is one
+                // memory round trip), then the word stores into the padded rows
+                constexpr int NV = IW * IH / 8 / 32, NB = NV < 8 ? NV : 8;
+#pragma unroll 1
+                for (int k0 = 0; k0 < NV; k0 += NB) {
+                    uint4 v[NB];
+#pragma unroll
+                    for (int k = 0; k < NB; k++) v[k] = __ldg(reinterpret_cast<const uint4 *>(src) + lane + 32 * (k0 + k));
+#pragma unroll
+                    for (int k = 0; k < NB; k++) {
+                        const int e = lane + 32 * (k0 + k);
+                        uint32_t *d = reinterpret_cast<uint32_t *>(tA + ((e * 8) / IW) * PX + (e * 8) % IW);
+                        d[0] = v[k].x; d[1] = v[k].y; d[2] = v[k].z; d[3] = v[k].w;
+                    }
                 }
             } else {
                 for (int e = lane; e < IW * IH; e += 32) tA[(e / IW) * PX + e % IW] = src[e];
