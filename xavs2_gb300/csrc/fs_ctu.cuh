@@ -351,7 +351,71 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
 #define XG_CTU_MINB 3
 #endif
 
+// Ranges from which the search takes two displacement rows per window pass
+// (see ctu_search): the pair form needs about 240 registers (2 CTAs per SM
+// instead of 3) and measured 8 % faster at R = 64 (3.39 against 3.68 ms per
+// 1080p picture), 9 % slower at R = 16 (0.269 against 0.247 ms), where the
+// per-CTA setup of the 32-row chunk weighs more.
+#ifndef XG_CTU_PAIR_MIN_R
+#define XG_CTU_PAIR_MIN_R 32
+#endif
+
+// Folds the 4 displacements j0 .. j0 + 3 of one search row (SADs s[o]) into
+// the lane's keys.
 template <bool BORDER, int LV>
+__device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2][4], const uint32_t *mrow, int j0,
+                                          int R, bool brow0, bool brow1, bool row_safe, const CtuJob &job,
+                                          const Geometry &g, uint32_t (&ks)[25], uint32_t (&rowl)[3])
+{
+#if XG_CTU_SAFE_SPLIT
+    // in a border job, displacements whose every block stays inside the
+    // limits take the interior fold (same keys: nothing to poison)
+    const bool safe = !BORDER || (row_safe && job.x0 + j0 - R >= -kLimitMargin &&
+                                  job.x0 + 64 + j0 + 3 - R <= g.W + kLimitMargin);
+    if (BORDER && !safe) {
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+            const int dxr = j0 + o;
+            const uint32_t mks = mrow[dxr];
+            const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
+            fold_displacement<true, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+        }
+    } else {
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+            const int dxr = j0 + o;
+            const uint32_t mks = mrow[dxr];
+            const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;
+            fold_displacement<false, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+        }
+    }
+#else
+    (void)row_safe;
+    (void)job;
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+        const int dxr = j0 + o;
+        const uint32_t mks = mrow[dxr];
+        const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
+        fold_displacement<BORDER, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+    }
+#endif
+}
+
+// a search row's large-PU minima into the 64-bit (cost, order) keys
+__device__ __forceinline__ void merge_rowl(const uint32_t (&rowl)[3], int dy, int R, int nd,
+                                           unsigned long long (&kl)[3])
+{
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint32_t cost = rowl[k] >> 8, dxr = rowl[k] & 0xffu;
+        if (cost >= kCapLarge) continue;
+        const unsigned long long key = ((unsigned long long)cost << 32) | (unsigned)(2 + (dy + R) * nd + (int)dxr);
+        kl[k] = key < kl[k] ? key : kl[k];
+    }
+}
+
+template <bool BORDER, int LV, bool PAIR>
 __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const SessView *__restrict__ views, int R,
                                            int lambda, int ww, uint8_t *smem)
 {
@@ -479,6 +543,59 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
 #pragma unroll
     for (int k = 0; k < 25; k++) ks[k] = 0xffffffffu;
 
+    if constexpr (PAIR) {
+    // two displacement rows per pass: window rows wrow0 .. wrow0 + 8 are
+    // loaded and aligned once; row r serves block row r of the first
+    // displacement row and block row r - 1 of the second
+    for (int rr = 0; rr < kDyWarp; rr += 2) {
+        const int row = warp * kDyWarp + rr;
+        const int dy = dy0 + row;
+        if (dy >= R) break;     // 2R and kDyWarp are even: a pair is all in or all out
+        const int wrow0 = 16 * ry + 8 * half + row;
+        const uint32_t *mrowA = mvk + row * nd, *mrowB = mrowA + nd;
+        uint32_t rowlA[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, rowlB[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+        bool bA0 = true, bA1 = true, bB0 = true, bB1 = true;
+        if (BORDER) {
+            const int yb = L.by0 + dy;
+            bA0 = yb >= -kLimitMargin && yb + 4 <= g.H + kLimitMargin;
+            bA1 = yb + 4 >= -kLimitMargin && yb + 8 <= g.H + kLimitMargin;
+            bB0 = yb + 1 >= -kLimitMargin && yb + 5 <= g.H + kLimitMargin;
+            bB1 = yb + 5 >= -kLimitMargin && yb + 9 <= g.H + kLimitMargin;
+        }
+        const bool safeA = job.y0 + dy >= -kLimitMargin && job.y0 + 64 + dy <= g.H + kLimitMargin;
+        const bool safeB = job.y0 + dy + 1 >= -kLimitMargin && job.y0 + 65 + dy <= g.H + kLimitMargin;
+        for (int j0 = 0; j0 < nd; j0 += 4) {
+            uint32_t sA[4][2][4], sB[4][2][4];
+#pragma unroll
+            for (int o = 0; o < 4; o++)
+#pragma unroll
+                for (int br = 0; br < 2; br++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) sA[o][br][c] = sB[o][br][c] = 0;
+#pragma unroll
+            for (int r = 0; r < 9; r++) {
+                const int wr = wrow0 + r;
+                const uint32_t *wp = reinterpret_cast<const uint32_t *>(win + wr * ww + 4 * swz(wr) + 16 * rx + j0);
+                uint32_t w5[5];
+#pragma unroll
+                for (int k = 0; k < 5; k++) w5[k] = wp[k];
+#pragma unroll
+                for (int o = 0; o < 4; o++) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const uint32_t a = o ? align_bytes(w5[c], w5[c + 1], o) : w5[c];
+                        if (r < 8) sA[o][r >> 2][c] = sad4_acc(cw[r][c], a, sA[o][r >> 2][c]);
+                        if (r >= 1) sB[o][(r - 1) >> 2][c] = sad4_acc(cw[r - 1][c], a, sB[o][(r - 1) >> 2][c]);
+                    }
+                }
+            }
+            fold_four<BORDER, LV>(L, sA, mrowA, j0, R, bA0, bA1, safeA, job, g, ks, rowlA);
+            fold_four<BORDER, LV>(L, sB, mrowB, j0, R, bB0, bB1, safeB, job, g, ks, rowlB);
+        }
+        merge_rowl(rowlA, dy, R, nd, kl);
+        merge_rowl(rowlB, dy + 1, R, nd, kl);
+    }
+    } else {
     for (int rr = 0; rr < kDyWarp; rr++) {
         const int row = warp * kDyWarp + rr;
         const int dy = dy0 + row;
@@ -494,7 +611,6 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
         }
         // every block of the CTU inside the vertical limits at this dy
         const bool row_safe = job.y0 + dy >= -kLimitMargin && job.y0 + 64 + dy <= g.H + kLimitMargin;
-        (void)row_safe;
         for (int j0 = 0; j0 < nd; j0 += 4) {
             uint32_t s[4][2][4];
 #pragma unroll
@@ -521,47 +637,10 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
                     }
                 }
             }
-#if XG_CTU_SAFE_SPLIT
-            // in a border job, displacements whose every block stays inside
-            // the limits take the interior fold (same keys: nothing to poison)
-            const bool safe = !BORDER || (row_safe && job.x0 + j0 - R >= -kLimitMargin &&
-                                          job.x0 + 64 + j0 + 3 - R <= g.W + kLimitMargin);
-            if (BORDER && !safe) {
-#pragma unroll
-                for (int o = 0; o < 4; o++) {
-                    const int dxr = j0 + o;
-                    const uint32_t mks = mrow[dxr];
-                    const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
-                    fold_displacement<true, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
-                }
-            } else {
-#pragma unroll
-                for (int o = 0; o < 4; o++) {
-                    const int dxr = j0 + o;
-                    const uint32_t mks = mrow[dxr];
-                    const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;
-                    fold_displacement<false, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
-                }
-            }
-#else
-#pragma unroll
-            for (int o = 0; o < 4; o++) {
-                const int dxr = j0 + o;
-                const uint32_t mks = mrow[dxr];
-                const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
-                fold_displacement<BORDER, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
-            }
-#endif
+            fold_four<BORDER, LV>(L, s, mrow, j0, R, brow0, brow1, row_safe, job, g, ks, rowl);
         }
-        // fold this row's large-PU minima into 64-bit (cost, order) keys
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const uint32_t cost = rowl[k] >> 8, dxr = rowl[k] & 0xffu;
-            if (cost >= kCapLarge) continue;
-            const unsigned long long key =
-                ((unsigned long long)cost << 32) | (unsigned)(2 + (dy + R) * nd + (int)dxr);
-            kl[k] = key < kl[k] ? key : kl[k];
-        }
+        merge_rowl(rowl, dy, R, nd, kl);
+    }
     }
     // merge into the global keys
     const int dyw = dy0 + warp * kDyWarp;
@@ -590,21 +669,21 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
 #define XG_CTU_LEVELS 1
 #endif
 
-template <bool BORDER>
-__global__ void __launch_bounds__(kCtuThreads, XG_CTU_MINB) fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks,
-                                                            const SessView *__restrict__ views, int R, int lambda,
-                                                            int ww)
+template <bool BORDER, bool PAIR>
+__global__ void __launch_bounds__(kCtuThreads, PAIR ? 2 : XG_CTU_MINB)
+    fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks, const SessView *__restrict__ views, int R, int lambda,
+                  int ww)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int job_idx = blockIdx.x / nchunks, chunk = blockIdx.x % nchunks;
     const CtuJob job = jobs[job_idx];
     if (BORDER != (job.border != 0)) return;
 #if XG_CTU_LEVELS
-    if (job.levels & 1) ctu_search<BORDER, 15>(job, chunk, views, R, lambda, ww, smem);
-    else if (job.levels & 2) ctu_search<BORDER, 14>(job, chunk, views, R, lambda, ww, smem);
-    else ctu_search<BORDER, 12>(job, chunk, views, R, lambda, ww, smem);
+    if (job.levels & 1) ctu_search<BORDER, 15, PAIR>(job, chunk, views, R, lambda, ww, smem);
+    else if (job.levels & 2) ctu_search<BORDER, 14, PAIR>(job, chunk, views, R, lambda, ww, smem);
+    else ctu_search<BORDER, 12, PAIR>(job, chunk, views, R, lambda, ww, smem);
 #else
-    ctu_search<BORDER, 15>(job, chunk, views, R, lambda, ww, smem);
+    ctu_search<BORDER, 15, PAIR>(job, chunk, views, R, lambda, ww, smem);
 #endif
 }
 
@@ -713,18 +792,23 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     if (dev >= 0 && dev < 64 && !attr_done[dev]) {
         int ww_max;
         const int maxb = (int)ctu_smem_bytes(128, ww_max);
-        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
-        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
         attr_done[dev] = true;
     }
     const int nchunks = (2 * R + kDyChunk - 1) / kDyChunk;
     const int grid = n_jobs * nchunks;
+    const bool pair = R >= XG_CTU_PAIR_MIN_R;
     if (n_border < n_jobs) {
-        fs_ctu_kernel<false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        if (pair) fs_ctu_kernel<false, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        else fs_ctu_kernel<false, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
         count_launch();
     }
     if (n_border > 0) {
-        fs_ctu_kernel<true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        if (pair) fs_ctu_kernel<true, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        else fs_ctu_kernel<true, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
         count_launch();
     }
 }
