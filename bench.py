@@ -672,6 +672,22 @@ def run_tq(args):
         host_forms[chunks] = reduce_max(time.perf_counter() - t0, dev)
     best_chunks = min(host_forms, key=host_forms.get)
     e2e_s = host_forms[best_chunks]
+    # what the host link itself moves: one page-locked copy of the residual
+    # array each way, and both directions at once on two streams
+    link = {}
+    tmp = torch.empty_like(d_res)
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    nbytes = d_res.numel() * 2
+    for name, pairs in (("h2d", [(tmp, h_res, s_in)]), ("d2h", [(h_rec, d_res, s_out)]),
+                        ("both", [(tmp, h_res, s_in), (h_rec, d_res, s_out)])):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for dst, src, st in pairs:
+            with torch.cuda.stream(st):
+                dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        link[name] = nbytes * len(pairs) / (time.perf_counter() - t0) / 1e9
+    del tmp
     e2e = n * world * args.steps / e2e_s
     if rank != 0:
         return
@@ -704,6 +720,7 @@ def run_tq(args):
                 "call": "xavs2gpu_tq_batch_host, page-locked buffers, %s" %
                         ("in place over the host link (chunks = 0)" if best_chunks == 0 else "%d chunks" % best_chunks),
                 "host_link_gbs": (4 * nres + 2 * ncoef + 36 * n) * args.steps / e2e_s / 1e9,
+                "host_link_copy_gbs": link,
                 "forms_s_per_step": {("in_place" if k == 0 else "chunks_%d" % k): v / args.steps
                                      for k, v in host_forms.items()}},
         "gpu_launches": int(launches),
