@@ -21,7 +21,7 @@ def _planes(olib, refs):
     return flats, tab, stride
 
 
-@pytest.mark.parametrize("w,h,nrefs", [(256, 192, 2), (136, 72, 1), (320, 128, 3)])
+@pytest.mark.parametrize("w,h,nrefs", [(256, 192, 2), (136, 72, 1), (320, 128, 3), (416, 240, 2)])
 def test_skip_costs(gpu, olib, w, h, nrefs):
     import torch
     import xavs2_gb300 as xg
@@ -36,6 +36,17 @@ def test_skip_costs(gpu, olib, w, h, nrefs):
     cands[7]["x"] = w - 4
     cands[11]["ref"][0] = (-1, -1)
     cands[13]["ref"][0, 0] = nrefs
+    # the last candidate predicts from the last reference at quarter-pel (3, 3)
+    # with its block ending exactly at the bottom-right plane margin (the
+    # word-wise plane readers then touch the end of the planes' allocation;
+    # at 416x240 a plane's bytes are a multiple of 256)
+    last = cands[-1]
+    S = 1 << int(last["size_log2"])
+    last["n_pu"] = 1
+    last["ref"][:] = -1
+    last["ref"][0, 0] = nrefs - 1
+    last["mv"][0, 0] = (4 * (w + 80 - S - int(last["x"])) + 3, 4 * (h + 80 - S - int(last["y"])) + 3)
+    cands[-1] = last
     lam = 17.375
     flats, tab, stride = _planes(olib, refs)
     e_dist = np.zeros(len(cands), np.int32)
@@ -44,6 +55,7 @@ def test_skip_costs(gpu, olib, w, h, nrefs):
     olib.xo_skip_costs(oracle.ptr(cur), w, tab, stride, w, h, nrefs, oracle.ptr(cands), len(cands), lam, n_cu,
                        oracle.ptr(e_dist), oracle.ptr(e_cost), oracle.ptr(e_best))
     assert (e_dist == -1).sum() > 3 and (e_dist > 0).sum() > len(cands) // 2
+    assert e_dist[-1] > 0
     sess = xg.MeSession(w, h, nrefs, 1)
     sess.set_picture(-1, cur)
     for i, r in enumerate(refs):

@@ -309,11 +309,13 @@ __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (
     const uint32_t P = RS + __shfl_xor_sync(0xffffffffu, RS, LR.pr4);      // row | column pairs
     const uint32_t TOT = P + __shfl_xor_sync(0xffffffffu, P, LR.pr5);
     const int v64 = LR.c64[0] * (int)TOT + LR.c64[1] * (int)P + LR.c64[2] * (int)RS;
+    // without poisoned blocks a 64x64 cost stays below kCapLarge (1,044,480 <
+    // 2,000,000) and a lane without a key has all-zero coefficients
     if (LV & 4) {
-        rowl[0] = min(rowl[0], (min((uint32_t)va, kCapLarge) << 8) + mkl);
-        rowl[1] = min(rowl[1], (min((uint32_t)vb, kCapLarge) << 8) + mkl);
+        rowl[0] = addmin((BORDER ? min((uint32_t)va, kCapLarge) : (uint32_t)va) << 8, mkl, rowl[0]);
+        rowl[1] = addmin((BORDER ? min((uint32_t)vb, kCapLarge) : (uint32_t)vb) << 8, mkl, rowl[1]);
     }
-    if (LV & 8) rowl[2] = min(rowl[2], (min((uint32_t)v64, kCapLarge) << 8) + mkl);
+    if (LV & 8) rowl[2] = addmin((BORDER ? min((uint32_t)v64, kCapLarge) : (uint32_t)v64) << 8, mkl, rowl[2]);
 }
 
 // 4x4 SADs of the lane's half-region against window rows wrow0.. at byte
@@ -363,7 +365,7 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
 // Folds the 4 displacements j0 .. j0 + 3 of one search row (SADs s[o]) into
 // the lane's keys.
 template <bool BORDER, int LV>
-__device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2][4], const uint32_t *mrow, int j0,
+__device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2][4], const uint32_t *mrow, int nd, int j0,
                                           int R, bool brow0, bool brow1, bool row_safe, const CtuJob &job,
                                           const Geometry &g, uint32_t (&ks)[25], uint32_t (&rowl)[3])
 {
@@ -376,16 +378,14 @@ __device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2]
 #pragma unroll
         for (int o = 0; o < 4; o++) {
             const int dxr = j0 + o;
-            const uint32_t mks = mrow[dxr];
-            const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
+            const uint32_t mks = mrow[dxr], mkl = mrow[nd * kDyChunk + dxr];
             fold_displacement<true, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
         }
     } else {
 #pragma unroll
         for (int o = 0; o < 4; o++) {
             const int dxr = j0 + o;
-            const uint32_t mks = mrow[dxr];
-            const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;
+            const uint32_t mks = mrow[dxr], mkl = mrow[nd * kDyChunk + dxr];
             fold_displacement<false, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
         }
     }
@@ -395,8 +395,7 @@ __device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2]
 #pragma unroll
     for (int o = 0; o < 4; o++) {
         const int dxr = j0 + o;
-        const uint32_t mks = mrow[dxr];
-        const uint32_t mkl = ((mks >> 3) & 0xffffff00u) | (uint32_t)dxr;   // (mvc << 8) | dxr
+        const uint32_t mks = mrow[dxr], mkl = mrow[nd * kDyChunk + dxr];
         fold_displacement<BORDER, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
     }
 #endif
@@ -428,8 +427,9 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
     const int dy0 = -R + chunk * kDyChunk;
     const int wrows = 64 + kDyChunk - 1;
     const int nd = 2 * R;
-    uint32_t *mvk = reinterpret_cast<uint32_t *>(smem);                 // [kDyChunk][nd]
-    uint8_t *win = smem + sizeof(uint32_t) * kDyChunk * nd;              // [wrows][ww]
+    // MV-cost keys: small-PU form [kDyChunk][nd], then the large-PU form
+    uint32_t *mvk = reinterpret_cast<uint32_t *>(smem);                 // [2][kDyChunk][nd]
+    uint8_t *win = smem + 2 * sizeof(uint32_t) * kDyChunk * nd;          // [wrows][ww]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // MV cost keys of this chunk's displacements (uniform over the CTU)
@@ -438,6 +438,7 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
         const int dy = dy0 + row, dx = dxr - R;
         const uint32_t mvc = (uint32_t)mv_cost_hd(lambda, dx * 4, dy * 4, job.mvp_x, job.mvp_y);
         mvk[e] = (mvc << 11) | ((uint32_t)(row & (kDyWarp - 1)) << 8) | (uint32_t)dxr;
+        mvk[kDyChunk * nd + e] = (mvc << 8) | (uint32_t)dxr;
     }
     // reference window: rows y0+dy0 .., columns x0-R .., clamped into the plane
     const uint8_t *ref = refs[job.ref];
@@ -589,8 +590,8 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
                     }
                 }
             }
-            fold_four<BORDER, LV>(L, sA, mrowA, j0, R, bA0, bA1, safeA, job, g, ks, rowlA);
-            fold_four<BORDER, LV>(L, sB, mrowB, j0, R, bB0, bB1, safeB, job, g, ks, rowlB);
+            fold_four<BORDER, LV>(L, sA, mrowA, nd, j0, R, bA0, bA1, safeA, job, g, ks, rowlA);
+            fold_four<BORDER, LV>(L, sB, mrowB, nd, j0, R, bB0, bB1, safeB, job, g, ks, rowlB);
         }
         merge_rowl(rowlA, dy, R, nd, kl);
         merge_rowl(rowlB, dy + 1, R, nd, kl);
@@ -637,7 +638,7 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
                     }
                 }
             }
-            fold_four<BORDER, LV>(L, s, mrow, j0, R, brow0, brow1, row_safe, job, g, ks, rowl);
+            fold_four<BORDER, LV>(L, s, mrow, nd, j0, R, brow0, brow1, row_safe, job, g, ks, rowl);
         }
         merge_rowl(rowl, dy, R, nd, kl);
     }
@@ -774,7 +775,7 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
 static inline size_t ctu_smem_bytes(int R, int &ww)
 {
     ww = (int)align_up((size_t)64 + 2 * R + 8 + 4 * kSwzMax + 4, 128);
-    return sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
+    return 2 * sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
 }
 
 // One launch of each variant over `n_jobs` jobs (sessions per job.sess).
