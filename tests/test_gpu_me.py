@@ -74,6 +74,21 @@ def test_ctu_layout_all_pus(gpu, olib, R, w, h):
     _assert_same(got, exp, pus)
 
 
+@pytest.mark.parametrize("lam,on_ctu", [(1 << 25, True), (1 << 27, False)])
+def test_large_lambda(gpu, olib, lam, on_ctu):
+    """Large MV costs: lambda 2^25 keeps the CTU search (its 32-bit keys hold
+    costs with MV costs up to 2^14), lambda 2^27 plans every PU for the
+    per-PU search; both equal the oracle."""
+    import xavs2_gb300 as xg
+    rng = np.random.default_rng(lam & 0xffff)
+    cur, ref0 = _frames(rng, 136, 72)
+    pus = xg.frame_pus(136, 72, 1)
+    prm = xg.MeParams(8, lam, 1, 2, 0, 0)
+    got, stats = _run(cur, [ref0], pus, prm)
+    assert (stats[0] == len(pus)) if on_ctu else (stats[0] == 0), stats
+    _assert_same(got, _oracle(olib, cur, [ref0], pus, prm), pus)
+
+
 def test_generic_pus(gpu, olib):
     """PUs at arbitrary positions with arbitrary predictors take the per-PU
     kernel; both paths in one run."""

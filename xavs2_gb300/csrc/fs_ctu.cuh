@@ -210,8 +210,12 @@ struct LaneRole {
 // lane's eight 4x4 SADs; `mks` = (mvc << 11) | (row << 8) | dx+R for the
 // small keys, `mkl` = (mvc << 8) | dx+R for the large ones.
 // LV (a compile-time set of CU sizes, as CtuJob::levels) drops the key
-// updates of the CU sizes a job has no PU of.
-template <bool BORDER, int LV>
+// updates of the CU sizes a job has no PU of.  BORDER poisons the blocks
+// outside the limits; BJ marks a border job, whose large keys are
+// (cost << 8) | dx+R (poisoned sums need the room).  An interior job keeps its
+// large keys in the small-key form (cost << 11 | row << 8 | dx+R: a 64x64
+// cost plus its MV cost stays below 2^21), with no shifts.
+template <bool BORDER, int LV, bool BJ = BORDER>
 __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (&raw)[2][4], uint32_t mks,
                                                   uint32_t mkl, int dx, bool brow0, bool brow1, const Geometry &g,
                                                   uint32_t (&ks)[25], uint32_t (&rowl)[3])
@@ -290,10 +294,14 @@ __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (
         Fr = fh + fh_o;
         Tr = half ? fh_o : fh;
         Lr = lh + lh_o;
-    } else {
+    } else if (BJ) {
         Fr = F >> 11;
         Tr = (half ? Fh_o : Fh) >> 11;
         Lr = L >> 11;
+    } else {
+        Fr = F;
+        Tr = half ? Fh_o : Fh;
+        Lr = L;
     }
     // 32x32 CUs
     const uint32_t a1 = half ? Lr : Tr;
@@ -311,6 +319,14 @@ __device__ __forceinline__ void fold_displacement(const LaneRole &LR, uint32_t (
     const int v64 = LR.c64[0] * (int)TOT + LR.c64[1] * (int)P + LR.c64[2] * (int)RS;
     // without poisoned blocks a 64x64 cost stays below kCapLarge (1,044,480 <
     // 2,000,000) and a lane without a key has all-zero coefficients
+    if (!BJ) {
+        if (LV & 4) {
+            rowl[0] = addmin((uint32_t)va, mks, rowl[0]);
+            rowl[1] = addmin((uint32_t)vb, mks, rowl[1]);
+        }
+        if (LV & 8) rowl[2] = addmin((uint32_t)v64, mks, rowl[2]);
+        return;
+    }
     if (LV & 4) {
         rowl[0] = addmin((BORDER ? min((uint32_t)va, kCapLarge) : (uint32_t)va) << 8, mkl, rowl[0]);
         rowl[1] = addmin((BORDER ? min((uint32_t)vb, kCapLarge) : (uint32_t)vb) << 8, mkl, rowl[1]);
@@ -379,14 +395,14 @@ __device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2]
         for (int o = 0; o < 4; o++) {
             const int dxr = j0 + o;
             const uint32_t mks = mrow[dxr], mkl = mrow[nd * kDyChunk + dxr];
-            fold_displacement<true, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+            fold_displacement<true, LV, true>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
         }
     } else {
 #pragma unroll
         for (int o = 0; o < 4; o++) {
             const int dxr = j0 + o;
             const uint32_t mks = mrow[dxr], mkl = mrow[nd * kDyChunk + dxr];
-            fold_displacement<false, LV>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
+            fold_displacement<false, LV, BORDER>(L, s[o], mks, mkl, dxr - R, brow0, brow1, g, ks, rowl);
         }
     }
 #else
@@ -401,13 +417,15 @@ __device__ __forceinline__ void fold_four(const LaneRole &L, uint32_t (&s)[4][2]
 #endif
 }
 
-// a search row's large-PU minima into the 64-bit (cost, order) keys
+// a search row's large-PU minima into the 64-bit (cost, order) keys (cost
+// above the low 8 bits in a border job, above the low 11 in an interior job)
+template <bool BJ>
 __device__ __forceinline__ void merge_rowl(const uint32_t (&rowl)[3], int dy, int R, int nd,
                                            unsigned long long (&kl)[3])
 {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const uint32_t cost = rowl[k] >> 8, dxr = rowl[k] & 0xffu;
+        const uint32_t cost = rowl[k] >> (BJ ? 8 : 11), dxr = rowl[k] & 0xffu;
         if (cost >= kCapLarge) continue;
         const unsigned long long key = ((unsigned long long)cost << 32) | (unsigned)(2 + (dy + R) * nd + (int)dxr);
         kl[k] = key < kl[k] ? key : kl[k];
@@ -532,7 +550,7 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const uint32_t cost = rowl0[k] >> 8;
+            const uint32_t cost = rowl0[k] >> (BORDER ? 8 : 11);
             if (lm[k] < 0 || cost >= kCapLarge) continue;
             const int pu = smap[k < 2 ? 784 + cu32 * 13 + lm[k] : 836 + lm[k]];
             if (pu >= 0) atomicMin(&keys[pu], (unsigned long long)cost << 32);
@@ -593,8 +611,8 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
             fold_four<BORDER, LV>(L, sA, mrowA, nd, j0, R, bA0, bA1, safeA, job, g, ks, rowlA);
             fold_four<BORDER, LV>(L, sB, mrowB, nd, j0, R, bB0, bB1, safeB, job, g, ks, rowlB);
         }
-        merge_rowl(rowlA, dy, R, nd, kl);
-        merge_rowl(rowlB, dy + 1, R, nd, kl);
+        merge_rowl<BORDER>(rowlA, dy, R, nd, kl);
+        merge_rowl<BORDER>(rowlB, dy + 1, R, nd, kl);
     }
     } else {
     for (int rr = 0; rr < kDyWarp; rr++) {
@@ -640,7 +658,7 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
             }
             fold_four<BORDER, LV>(L, s, mrow, nd, j0, R, brow0, brow1, row_safe, job, g, ks, rowl);
         }
-        merge_rowl(rowl, dy, R, nd, kl);
+        merge_rowl<BORDER>(rowl, dy, R, nd, kl);
     }
     }
     // merge into the global keys
@@ -707,7 +725,7 @@ static inline bool same_range_in_window(int lo, int hi, int rule_lo, int rule_hi
 }
 
 static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, int W, int H, int nrefs, int R,
-                           std::vector<int> &generic, cudaStream_t st)
+                           bool allow, std::vector<int> &generic, cudaStream_t st)
 {
     static const SlotTable table;
     const int cw = (W + 63) / 64, ch = (H + 63) / 64;
@@ -718,7 +736,7 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
     generic.clear();
     // the CTU kernel walks a search row in steps of 4 displacements, so it
     // takes ranges whose 2R is a multiple of 4 (odd R: every PU per-PU)
-    const bool range_ok = (2 * R) % 4 == 0;
+    const bool range_ok = allow && (2 * R) % 4 == 0;
     for (int i = 0; i < (int)pus.size(); i++) {
         const xavs2gpu_pu_t &u = pus[i];
         const int w = h_pu_w[u.part], h = h_pu_h[u.part];

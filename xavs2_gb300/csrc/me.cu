@@ -1087,6 +1087,7 @@ struct MeSessionImpl {
     int n_generic = 0;
     CtuPlan plan;
     int plan_R = -1;               // search range the plan was built for (-1: stale)
+    bool plan_ctu = true;          // whether the plan could use the CTU search
     int n_ctu_pus = 0;
     std::vector<xavs2gpu_pu_t> h_pus;
     int *d_small = nullptr, *d_large = nullptr;   // refinement lists: thread / warp per search
@@ -1403,11 +1404,17 @@ static void build_groups(MeSessionImpl &m, const std::vector<int> &small, const 
 }
 
 // (Re)builds the split into CTU jobs and per-PU searches for window size R.
-static void ensure_plan(MeSessionImpl &m, int R)
+// The CTU search keeps (cost << 11 | order) keys in 32 bits, which holds the
+// MV costs of every lambda below 2^26 (the reference's QP range needs below
+// 2^23); larger lambdas plan every PU for the per-PU search.
+constexpr int kCtuMaxLambda = 1 << 26;
+
+static void ensure_plan(MeSessionImpl &m, int R, int lambda)
 {
-    if (m.plan_R == R) return;
+    const bool ctu = lambda < kCtuMaxLambda;
+    if (m.plan_R == R && m.plan_ctu == ctu) return;
     std::vector<int> generic;
-    ctu_plan_build(m.plan, m.h_pus, m.W, m.H, m.nrefs, R, generic, m.st);
+    ctu_plan_build(m.plan, m.h_pus, m.W, m.H, m.nrefs, R, ctu, generic, m.st);
     m.n_generic = (int)generic.size();
     m.n_ctu_pus = m.n - m.n_generic;
     m.h_generic.assign(generic.begin(), generic.end());
@@ -1457,6 +1464,7 @@ static void ensure_plan(MeSessionImpl &m, int R)
     refresh_view(m);
     XG_CUDA(cudaStreamSynchronize(m.st));
     m.plan_R = R;
+    m.plan_ctu = ctu;
 }
 
 extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_params_t *prm)
@@ -1470,7 +1478,7 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     if (m.n == 0) return XAVS2GPU_OK;
     XG_CUDA(cudaSetDevice(m.device));
     const int R = prm->search_range, lam = prm->lambda_factor;
-    ensure_plan(m, R);
+    ensure_plan(m, R, lam);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[0], m.st));
     XG_CUDA(cudaMemsetAsync(m.d_keys, 0xff, sizeof(unsigned long long) * m.n, m.st));
     const uint32_t *gen = reinterpret_cast<const uint32_t *>(m.d_generic);
@@ -1569,7 +1577,7 @@ extern "C" int xavs2gpu_me_autotune(xavs2gpu_me_session_t *s, const xavs2gpu_me_
             cand.refine_block = cfg & 1 ? 128 : 64;
             cand.cu_groups = cfg >> 1;
             if ((rc = xavs2gpu_me_set_tuning(s, &cand)) != XAVS2GPU_OK) break;
-            ensure_plan(m, prm->search_range);
+            ensure_plan(m, prm->search_range, prm->lambda_factor);
             if ((rc = xavs2gpu_me_run(s, prm)) != XAVS2GPU_OK) break;   // warm-up
             XG_CUDA(cudaEventRecord(e0, m.st));
             for (int i = 0; i < reps; i++)
@@ -1590,7 +1598,7 @@ extern "C" int xavs2gpu_me_autotune(xavs2gpu_me_session_t *s, const xavs2gpu_me_
     cudaEventDestroy(e1);
     if (rc != XAVS2GPU_OK) return rc;
     rc = xavs2gpu_me_set_tuning(s, &best);
-    if (rc == XAVS2GPU_OK) ensure_plan(m, prm->search_range);
+    if (rc == XAVS2GPU_OK) ensure_plan(m, prm->search_range, prm->lambda_factor);
     if (best_ms) *best_ms = best_t;
     return rc;
 }
@@ -1602,7 +1610,7 @@ extern "C" int xavs2gpu_me_prepare(xavs2gpu_me_session_t *s, const xavs2gpu_me_p
         return XAVS2GPU_ERR_ARG;
     }
     XG_CUDA(cudaSetDevice(s->impl.device));
-    ensure_plan(s->impl, prm->search_range);
+    ensure_plan(s->impl, prm->search_range, prm->lambda_factor);
     return XAVS2GPU_OK;
 }
 
@@ -1805,7 +1813,7 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
             fail(XAVS2GPU_ERR_ARG, "xavs2gpu_me_batch_run", "sessions on different devices");
             return XAVS2GPU_ERR_ARG;
         }
-        ensure_plan(m, R);
+        ensure_plan(m, R, prm->lambda_factor);
         const bool g = grouped && m.cu_groups;
         nj += m.plan.h_jobs.size();
         nborder += m.plan.n_border;
