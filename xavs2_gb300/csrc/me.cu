@@ -470,6 +470,115 @@ __global__ void __launch_bounds__(128) refine_kernel(const xavs2gpu_pu_t *__rest
 // step are fixed by the centre, so their costs are accumulated unit by unit
 // (the current block's unit is loaded once and compared with every
 // position), then the first strictly smaller cost wins in spiral order.
+// The refinement's unit costs (SATD with one rounding per 4x4 or 8x4 unit,
+// pixel.c:321, 347, or SAD) on packed 16-bit pairs: a pair holds column k of
+// the unit's left 4x4 block and column k of its right one (zero for a 4x4
+// unit), so each vadd2 / vsub2 takes one butterfly of both blocks.  The
+// differences (|d| <= 255) grow to at most 16 x 255 = 4080 through the two
+// 4-point passes, well inside 16 bits, so every value equals the 32-bit
+// form's; the absolute values are summed by dp2a.  Build option
+// XG_REFINE_PACKED=0 keeps the 32-bit form.
+#ifndef XG_REFINE_PACKED
+#define XG_REFINE_PACKED 1
+#endif
+
+// 8 bytes of a row at any alignment as two words (aligned loads; the words
+// after the row are read too: every plane has an 80-pixel margin and the
+// planes' allocation 256 bytes of slack, so they are in bounds)
+__device__ __forceinline__ void load8u(const uint8_t *p, uint32_t &lo, uint32_t &hi)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    const uint32_t sh = (uint32_t)(a & 3) * 8;
+    const uint32_t w0 = w[0], w1 = w[1], w2 = w[2];
+    lo = __funnelshift_r(w0, w1, sh);
+    hi = __funnelshift_r(w1, w2, sh);
+}
+
+// (byte k, byte 4 + k) of the 8-byte row (lo, hi) as zero-extended halves
+__device__ __forceinline__ void row_pairs(uint32_t lo, uint32_t hi, uint32_t (&q)[4])
+{
+    const uint32_t t = __byte_perm(lo, hi, 0x5140), u = __byte_perm(lo, hi, 0x7362);   // b0 b4 b1 b5 | b2 b6 b3 b7
+    q[0] = __byte_perm(t, 0, 0x7170);
+    q[1] = __byte_perm(t, 0, 0x7372);
+    q[2] = __byte_perm(u, 0, 0x7170);
+    q[3] = __byte_perm(u, 0, 0x7372);
+}
+
+// The current block's unit: raw row words (SAD) and column pairs (SATD).
+struct UnitCur {
+    uint32_t w[4][2];
+    uint32_t q[4][4];
+};
+
+template <bool U4>
+__device__ __forceinline__ void load_unit(const uint8_t *o, int stride, UnitCur &c)
+{
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        uint32_t lo, hi;
+        load8u(o + y * stride, lo, hi);
+        c.w[y][0] = lo;
+        c.w[y][1] = U4 ? 0u : hi;
+        row_pairs(lo, c.w[y][1], c.q[y]);
+    }
+}
+
+// |x| summed over the two halves of v, plus acc
+__device__ __forceinline__ int abs_pair_acc(uint32_t v, int acc)
+{
+    return __dp2a_lo((int)__vabsss2(v), 0x0101, acc);
+}
+
+template <bool U4>
+__device__ __forceinline__ int unit_cost_pre(bool had, const UnitCur &c, const uint8_t *r, int stride)
+{
+    if (!had) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            uint32_t lo, hi;
+            load8u(r + y * stride, lo, hi);
+            s = sad4_acc(c.w[y][0], lo, s);
+            if (!U4) s = sad4_acc(c.w[y][1], hi, s);
+        }
+        return (int)s;
+    }
+    uint32_t d[4][4];
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        uint32_t lo, hi, q[4];
+        load8u(r + y * stride, lo, hi);
+        row_pairs(lo, U4 ? 0u : hi, q);
+        // differences, then the 4-point transform of the row in both blocks
+        const uint32_t d0 = __vsub2(c.q[y][0], q[0]), d1 = __vsub2(c.q[y][1], q[1]);
+        const uint32_t d2 = __vsub2(c.q[y][2], q[2]), d3 = __vsub2(c.q[y][3], q[3]);
+        const uint32_t s0 = __vadd2(d0, d1), e0 = __vsub2(d0, d1), s1 = __vadd2(d2, d3), e1 = __vsub2(d2, d3);
+        d[y][0] = __vadd2(s0, s1);
+        d[y][1] = __vadd2(e0, e1);
+        d[y][2] = __vsub2(s0, s1);
+        d[y][3] = __vsub2(e0, e1);
+    }
+    int s = 0;
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+        const uint32_t s0 = __vadd2(d[0][x], d[1][x]), e0 = __vsub2(d[0][x], d[1][x]);
+        const uint32_t s1 = __vadd2(d[2][x], d[3][x]), e1 = __vsub2(d[2][x], d[3][x]);
+        s = abs_pair_acc(__vadd2(s0, s1), s);
+        s = abs_pair_acc(__vadd2(e0, e1), s);
+        s = abs_pair_acc(__vsub2(s0, s1), s);
+        s = abs_pair_acc(__vsub2(e0, e1), s);
+    }
+    return s >> 1;
+}
+
+#if XG_REFINE_PACKED
+using UnitC = UnitCur;
+#else
+using UnitC = int[4][8];
+#endif
+
+#if !XG_REFINE_PACKED
 // Bytes p[0..n) (n = 4 or 8) of an arbitrarily aligned row as ints, from
 // aligned 32-bit loads (the word after the row is read too; every plane has
 // an 80-pixel margin, so it is in bounds).
@@ -538,6 +647,8 @@ __device__ __forceinline__ void load_unit(const uint8_t *o, int stride, int (&c)
     }
 }
 
+#endif
+
 // Accumulates the costs of up to 9 positions over all units of the PU.
 template <bool U4>
 __device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, const uint8_t *o,
@@ -550,7 +661,7 @@ __device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, c
     for (int k = 0; k < 9; k++) acc[k] = 0;
     for (int u = 0; u < nu; u++) {
         const int uy = u / nux, ux = u - uy * nux;
-        int c[4][8];
+        UnitC c;
         load_unit<U4>(o + (ptrdiff_t)uy * 4 * stride + ux * UW, stride, c);
 #pragma unroll
         for (int k = 0; k < 9; k++) {
@@ -681,7 +792,7 @@ __device__ int qpel_cost_warp_vec(const xavs2gpu_pu_t &p, int w, int h, bool had
     for (int u = lane; u < nu; u += 32) {
         const int uy = u / nux, ux = u - uy * nux;
         const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * uw;
-        int c[4][8];
+        UnitC c;
         if (u4) {
             load_unit<true>(o + off, stride, c);
             s += unit_cost_pre<true>(had, c, r + off, stride);
@@ -840,7 +951,7 @@ __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had
         for (int u = lane; u < nu; u += 32) {
             const int uy = div_small(u, mcols), ux = u - uy * cols;
             if (!unit_covered(S, grp, ux * UW, uy * 4, U4)) continue;
-            int c[4][8];
+            UnitC c;
             const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * UW;
             load_unit<U4>(o + off, stride, c);
             // one copy of the unit's cost code (the kernel stays small in
@@ -860,7 +971,7 @@ __device__ __forceinline__ void group_table(GroupSmem &S, unsigned grp, bool had
             const int u = div_small(e, mp), k = e - u * P;
             const int uy = div_small(u, mcols), ux = u - uy * cols;
             if (!unit_covered(S, grp, ux * UW, uy * 4, U4)) continue;
-            int c[4][8];
+            UnitC c;
             const ptrdiff_t off = (ptrdiff_t)uy * 4 * stride + ux * UW;
             load_unit<U4>(o + off, stride, c);
             const int mx = ccx + offx[k], my = ccy + offy[k];
