@@ -673,7 +673,7 @@ XAVS2GPU_API int xavs2gpu_me_rotate_refs(xavs2gpu_me_session_t *s);
  * A CU whose partition PUs are not in the PU list (see below) has the 2Nx2N
  * candidate only. */
 typedef struct xavs2gpu_cu {
-    int16_t x, y;              /* luma position of the CU                          */
+    int16_t x, y;              /* luma position of the CU (multiples of 8)         */
     int16_t size;              /* 8, 16, 32 or 64                                  */
     int16_t pad_;
     int32_t pu[4];             /* index of the CU's 2Nx2N PU in the session's PU

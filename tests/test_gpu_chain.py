@@ -183,3 +183,31 @@ def test_chain_feedback_loop(gpu):
     assert np.array_equal(src2, refs[0])
     chain.close()
     sess.close()
+
+
+def test_chain_rejects_bad_cus(gpu):
+    """CU lists the chain cannot serve fail at creation with an error: a CU
+    off the 8x8 grid, a size other than 8..64, a CU past the picture, a
+    2Nx2N PU index of another position."""
+    import xavs2_gb300 as xg
+    cus_list = xg.split_map_cus(W, H, seed=9)
+    pus, cus = xg.cu_pus(cus_list, W, H, NREFS)
+    sess = xg.MeSession(W, H, NREFS, len(pus))
+    sess.set_pus(pus)
+    lib = xg.load()
+    lib.xavs2gpu_set_abort_on_error(0)      # report failures instead of aborting
+    try:
+        for field, value in (("x", 4), ("size", 12), ("y", H)):
+            bad = cus.copy()
+            bad[field][3] = value
+            with pytest.raises(RuntimeError):
+                xg.Chain(sess, bad, QP)
+        bad = cus.copy()
+        bad["pu"][3, 0] = bad["pu"][4, 0]
+        with pytest.raises(RuntimeError):
+            xg.Chain(sess, bad, QP)
+    finally:
+        lib.xavs2gpu_clear_error()
+        lib.xavs2gpu_set_abort_on_error(1)
+    xg.Chain(sess, cus, QP).close()     # the valid list still builds
+    sess.close()

@@ -43,7 +43,10 @@ bool build_candidates(const xavs2gpu_cu_t *cus, int n_cus, const xavs2gpu_pu_t *
     for (int i = 0; i < n_cus; i++) {
         const xavs2gpu_cu_t &c = cus[i];
         const int S = c.size;
-        if (!(S == 8 || S == 16 || S == 32 || S == 64) || c.x < 0 || c.y < 0 || c.x + S > W || c.y + S > H)
+        // CUs sit on the 8x8 grid (the candidate kernels read 4-pixel groups
+        // as words)
+        if (!(S == 8 || S == 16 || S == 32 || S == 64) || c.x < 0 || c.y < 0 || c.x + S > W || c.y + S > H ||
+            ((c.x | c.y) & 7))
             return false;
         const int nk = S == 8 ? 5 : 13;
         bool all = true;
@@ -175,7 +178,7 @@ extern "C" xavs2gpu_chain_t *xavs2gpu_chain_create(xavs2gpu_me_session_t *s, con
     int64_t n_res = 0, n_coef = 0;
     if (!build_candidates(cus, n_cus, pus.data(), n, W, H, nrefs, cands, cu_cand, n_res, n_coef)) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_chain_create",
-             "CU outside the picture, bad size, or pu[r] is not its 2Nx2N PU for reference r");
+             "CU outside the picture or off the 8x8 grid, bad size, or pu[r] is not its 2Nx2N PU for reference r");
         return nullptr;
     }
     if (5 * (int64_t)cands.size() > INT32_MAX) {

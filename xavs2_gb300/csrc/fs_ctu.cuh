@@ -20,8 +20,10 @@
 // (8 per warp) over the whole horizontal range; its reference window lives in
 // shared memory.  Each warp keeps, per PU, the minimum of a 32-bit key
 // (cost << 11 | row-in-warp << 8 | dx+R) for PUs up to 16x16 and per-row keys
-// (cost << 8 | dx+R) for the larger ones, and merges them into the global
-// 64-bit (cost, visit order) keys with atomicMin.
+// for the larger ones (the same form in interior jobs, cost << 8 | dx+R in
+// border jobs, whose poisoned sums need the room), and merges them into the
+// global 64-bit (cost, visit order) keys with atomicMin.  For ranges of 32
+// and up a warp takes two search rows per pass over the window.
 //
 // Search limits: a PU is valid at a displacement iff the referenced block
 // lies within [-58, W+58) x [-58, H+58) -- the limits pred_inter_search_single
