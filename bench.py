@@ -435,13 +435,21 @@ def run_ours(args):
     a = rng.integers(0, 256, (64, 64), dtype=np.uint8)
     b = rng.integers(0, 256, (64, 64), dtype=np.uint8)
     f = xg.pixel_fn("sad", 2)
-    for _ in range(50):
-        f(xg.ptr(a), 64, xg.ptr(b), 64)
-    n_calls = 2000
-    t0 = time.perf_counter()
-    for _ in range(n_calls):
-        f(xg.ptr(a), 64, xg.ptr(b), 64)
-    per_call = n_calls / (time.perf_counter() - t0)
+    expect_sad = int(np.abs(a[:16, :16].astype(np.int32) - b[:16, :16].astype(np.int32)).sum())
+    per_call_modes = {}
+    for mode in (0, 1):            # staged copies; blocks read in place where the device allows it
+        lib.xavs2gpu_set_percall_mode(mode)
+        for _ in range(50):
+            f(xg.ptr(a), 64, xg.ptr(b), 64)
+        if f(xg.ptr(a), 64, xg.ptr(b), 64) != expect_sad:
+            sys.exit("bench: per-call SAD differs from the host sum (mode %d)" % mode)
+        n_calls = 2000
+        t0 = time.perf_counter()
+        for _ in range(n_calls):
+            f(xg.ptr(a), 64, xg.ptr(b), 64)
+        per_call_modes[mode] = n_calls / (time.perf_counter() - t0)
+    per_call_in_place = lib.xavs2gpu_percall_in_place()
+    per_call = per_call_modes[1]
 
     if rank != 0:
         return
@@ -494,7 +502,9 @@ def run_ours(args):
                                    "unit": "GB/s", "frac": interp_gbs / peaks.get("hbm_gbs", 6800.0)},
         "plan": {"ctu_pus": n_ctu, "per_pu_pus": n_gen, "ctu_jobs": n_jobs},
         "per_pu_search": per_pu_line(pus, phases, n_gen, peaks, peak_src),
-        "per_call": {"value": per_call, "unit": UNIT, "what": "xavs2gpu_pixel_sad_16x16 with host buffers"},
+        "per_call": {"value": per_call, "unit": UNIT, "what": "xavs2gpu_pixel_sad_16x16 with host buffers",
+                     "staged_value": per_call_modes[0],
+                     "in_place": bool(per_call_in_place)},
         "cpu_baseline": {"value": cpu_e / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": "random %.2f%% (%d) of the picture's PU searches, oracle C port, OpenMP"
                                    % (100 * args.cpu_fraction, cpu_n)},

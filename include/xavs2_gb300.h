@@ -65,6 +65,16 @@ XAVS2GPU_API const char *xavs2gpu_get_error(void);
 XAVS2GPU_API void xavs2gpu_clear_error(void);
 /* 1 (default): print and abort on any failure.  0: record and return. */
 XAVS2GPU_API void xavs2gpu_set_abort_on_error(int enable);
+/* Per-call block costs (the SAD / SATD / SA8D / SSD and sad_x3 / sad_x4
+ * table entries).  1 (default): where the device reads pageable host memory
+ * coherently (cudaDevAttrPageableMemoryAccess, e.g. a Grace host over
+ * NVLink-C2C) the kernel reads the caller's blocks in place -- one launch
+ * and one synchronisation per call; elsewhere, and with 0, the blocks are
+ * packed into a pinned buffer and copied to the device and back. */
+XAVS2GPU_API void xavs2gpu_set_percall_mode(int in_place);
+/* 1 when this thread's per-call block costs run in place (mode 1 and a
+ * device that reads pageable host memory coherently). */
+XAVS2GPU_API int xavs2gpu_percall_in_place(void);
 /* Number of kernels this library has launched in the process. */
 XAVS2GPU_API uint64_t xavs2gpu_kernel_launches(void);
 XAVS2GPU_API const char *xavs2gpu_version(void);

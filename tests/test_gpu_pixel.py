@@ -26,8 +26,17 @@ def _pairs(rng):
     return out
 
 
+@pytest.fixture(params=[1, 0], ids=["in_place", "staged"])
+def percall_mode(request, gpu):
+    """Per-call block costs read in place (where the device reads pageable
+    host memory) and through the staged copies."""
+    gpu.xavs2gpu_set_percall_mode(request.param)
+    yield request.param
+    gpu.xavs2gpu_set_percall_mode(1)
+
+
 @pytest.mark.parametrize("kind", ["sad", "satd", "sa8d", "ssd"])
-def test_costs(gpu, olib, kind):
+def test_costs(gpu, olib, kind, percall_mode):
     import xavs2_gb300 as xg
     rng = np.random.default_rng(3)
     ofn = getattr(olib, "xo_" + kind)
@@ -38,7 +47,7 @@ def test_costs(gpu, olib, kind):
             assert got == exp, (kind, part, got, exp)
 
 
-def test_sad_x3_x4(gpu, olib):
+def test_sad_x3_x4(gpu, olib, percall_mode):
     import xavs2_gb300 as xg
     rng = np.random.default_rng(4)
     fenc = rng.integers(0, 256, (64, 64), dtype=np.uint8)

@@ -53,6 +53,8 @@ _SIGS = {
     "xavs2gpu_get_error": (ctypes.c_char_p, []),
     "xavs2gpu_clear_error": (None, []),
     "xavs2gpu_set_abort_on_error": (None, [_I]),
+    "xavs2gpu_set_percall_mode": (None, [_I]),
+    "xavs2gpu_percall_in_place": (_I, []),
     "xavs2gpu_kernel_launches": (ctypes.c_uint64, []),
     "xavs2gpu_version": (ctypes.c_char_p, []),
     "xavs2gpu_copy_d2h": (_I, [_P, _P, ctypes.c_size_t]),

@@ -171,10 +171,41 @@ __global__ void mad_kernel(const uint8_t *src, int n_side, int32_t *out)
 
 // ---- per-call staging helpers ---------------------------------------------
 // Layout of one call in the staging buffers: [jobs][inputs...][outputs].
+//
+// In place: when the device reads pageable host memory coherently
+// (cudaDevAttrPageableMemoryAccess: a Grace host's page tables over
+// NVLink-C2C), the block costs read the caller's blocks where they lie, the
+// job descriptors and the results sit in the pinned staging buffer, and a
+// call is one launch and one synchronisation, with no copies.
+// xavs2gpu_set_percall_mode(0) keeps the staged path.
+static bool percall_in_place(int dev)
+{
+    static int cache[64] = {0};   // 0 unknown, 1 no, 2 yes
+    if (!percall_mode() || dev < 0 || dev >= 64) return false;
+    if (!cache[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) v = 0;
+        cache[dev] = v ? 2 : 1;
+    }
+    return cache[dev] == 2;
+}
+
+}  // namespace xg
+extern "C" int xavs2gpu_percall_in_place(void) { return xg::percall_in_place(xg::current_device()) ? 1 : 0; }
+namespace xg {
 
 static int32_t percall_cost(int kind, int part, const uint8_t *p1, intptr_t s1, const uint8_t *p2, intptr_t s2)
 {
     const int w = h_pu_w[part], h = h_pu_h[part];
+    if (percall_in_place(current_device())) {
+        CallCtx &c = call_ctx(512);
+        CostJob *job = reinterpret_cast<CostJob *>(c.h_stage);
+        int32_t *out = reinterpret_cast<int32_t *>(c.h_stage + 256);
+        *job = CostJob{p1, p2, (int32_t)s1, (int32_t)s2, part, 0};
+        launch_cost(kind, job, 1, out, c.stream);
+        XG_CUDA(cudaStreamSynchronize(c.stream));
+        return *out;
+    }
     const size_t o_job = 0, o_a = 256, o_b = o_a + align_up((size_t)w * h), o_out = o_b + align_up((size_t)w * h);
     CallCtx &c = call_ctx(o_out + 256);
     pack_rows(c.h_stage + o_a, p1, s1, w, h);
@@ -193,6 +224,16 @@ static int32_t percall_cost(int kind, int part, const uint8_t *p1, intptr_t s1, 
 static void percall_sad_xn(int part, int nref, const uint8_t *fenc, const uint8_t *const *refs, intptr_t i_ref, int *scores)
 {
     const int w = h_pu_w[part], h = h_pu_h[part];
+    if (percall_in_place(current_device())) {
+        CallCtx &c = call_ctx(512);
+        CostJob *jobs = reinterpret_cast<CostJob *>(c.h_stage);
+        int32_t *out = reinterpret_cast<int32_t *>(c.h_stage + 256);
+        for (int r = 0; r < nref; r++) jobs[r] = CostJob{fenc, refs[r], 64, (int32_t)i_ref, part, 0};
+        launch_cost(0, jobs, nref, out, c.stream);
+        XG_CUDA(cudaStreamSynchronize(c.stream));
+        memcpy(scores, out, 4 * nref);
+        return;
+    }
     const size_t blk = align_up((size_t)w * h);
     const size_t o_job = 0, o_in = 256, o_out = o_in + blk * (1 + nref);
     CallCtx &c = call_ctx(o_out + 256);

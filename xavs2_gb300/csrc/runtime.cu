@@ -13,11 +13,14 @@ namespace xg {
 static std::atomic<int> g_status{XAVS2GPU_OK};
 static std::atomic<int> g_abort{1};
 static std::atomic<uint64_t> g_launches{0};
+static std::atomic<int> g_percall_mode{1};
 static std::mutex g_msg_mu;
 static char g_msg[512] = "";
 static thread_local int t_device = 0;
 
 void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+int percall_mode() { return g_percall_mode.load(std::memory_order_relaxed); }
 
 void fail(int status, const char *where, const char *msg)
 {
@@ -136,6 +139,8 @@ void xavs2gpu_clear_error(void)
 }
 
 void xavs2gpu_set_abort_on_error(int enable) { xg::g_abort.store(enable ? 1 : 0); }
+
+void xavs2gpu_set_percall_mode(int in_place) { xg::g_percall_mode.store(in_place ? 1 : 0); }
 
 uint64_t xavs2gpu_kernel_launches(void) { return xg::g_launches.load(); }
 

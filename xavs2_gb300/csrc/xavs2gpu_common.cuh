@@ -46,6 +46,8 @@ struct CallCtx {
     size_t cap = 0;
 };
 CallCtx &call_ctx(size_t need_bytes);
+// 1: per-call block costs read host blocks in place where the device allows
+int percall_mode();
 int current_device();
 // Number of SMs of the current device (queried once per device).
 int sm_count();
