@@ -246,7 +246,7 @@ struct Ctx {
 
 // One group of up to G TUs of shape PART; `idx` = the block index of this
 // lane's sub-warp (-1: no TU).
-template <int PART>
+template <int PART, int RA = kRegionA>
 __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t *smem)
 {
     using S = Shape<PART>;
@@ -259,7 +259,9 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
     xavs2gpu_tq_block_t b{};
     if (act) b = cx.blocks[idx];
     const bool sec = PART == 0 && (b.flags & 2);
-    int16_t *tA = reinterpret_cast<int16_t *>(smem) + sub * (kRegionA / 2 / S::G);
+    static_assert(S::WAV ? RA == kRegionA : RA / 2 / S::G >= 2 * TW * (TH + 2) + TW * TH,
+                  "region A holds the transposes and the staging of every TU of the group");
+    int16_t *tA = reinterpret_cast<int16_t *>(smem) + sub * (RA / 2 / S::G);
     int16_t *tB = reinterpret_cast<int16_t *>(smem + kRegionA);
     const int16_t *src = cx.residual + b.offset;
     const bool al_in = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
@@ -527,78 +529,121 @@ __global__ void tq_scatter_kernel(const xavs2gpu_tq_block_t *__restrict__ blocks
     sorted[start + base + __popc(same & ((1u << lane) - 1))] = i;
 }
 
-// 3. the chain, persistent: warp-strided over the groups of all classes
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) tq_chain_kernel(Ctx cx, const int *__restrict__ counts,
-                                                               const int *__restrict__ sorted)
+// 3. the chain, persistent: warp-strided over the groups of the classes
+//    [C0, C1), RA bytes of region A per warp (region B too when the range
+//    holds the wavelet classes 0..2)
+template <int WARPS, int C0, int C1, int RA, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) tq_chain_kernel(Ctx cx, const int *__restrict__ counts,
+                                                                     const int *__restrict__ sorted)
 {
+    constexpr int kWarpBytes = C0 == 0 ? RA + kRegionB : RA;
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    uint8_t *smem = smem_raw + (threadIdx.x >> 5) * kWarpSmem;
+    uint8_t *smem = smem_raw + (threadIdx.x >> 5) * kWarpBytes;
     const int lane = threadIdx.x & 31;
     int cnt[kNumClasses], gstart[kNumClasses + 1], istart[kNumClasses];
-    gstart[0] = 0;
     int acc = 0;
 #pragma unroll
     for (int c = 0; c < kNumClasses; c++) {
         cnt[c] = counts[c];
         istart[c] = acc;
         acc += cnt[c];
-        gstart[c + 1] = gstart[c] + (cnt[c] + class_g(c) - 1) / class_g(c);
     }
-    const int total = gstart[kNumClasses];
+    gstart[C0] = 0;
+#pragma unroll
+    for (int c = C0; c < C1; c++) gstart[c + 1] = gstart[c] + (cnt[c] + class_g(c) - 1) / class_g(c);
+    const int total = gstart[C1];
     const int nw = gridDim.x * WARPS;
     for (int item = blockIdx.x * WARPS + (threadIdx.x >> 5); item < total; item += nw) {
-        int c = 0, gs = 0, is = istart[0], cn = cnt[0], G = class_g(0);
+        int c = C0, gs = 0, is = istart[C0], cn = cnt[C0], G = class_g(C0);
 #pragma unroll
-        for (int k = 1; k < kNumClasses; k++)
+        for (int k = C0 + 1; k < C1; k++)
             if (item >= gstart[k]) {
                 c = k; gs = gstart[k]; is = istart[k]; cn = cnt[k]; G = class_g(k);
             }
         const int pos = (item - gs) * G + lane / (32 / G);
         const int idx = pos < cn ? sorted[is + pos] : -1;
-        switch (c_class_part[c]) {
-        case 4: tu_group<4>(cx, idx, lane, smem); break;
-        case 23: tu_group<23>(cx, idx, lane, smem); break;
-        case 24: tu_group<24>(cx, idx, lane, smem); break;
-        case 3: tu_group<3>(cx, idx, lane, smem); break;
-        case 19: tu_group<19>(cx, idx, lane, smem); break;
-        case 20: tu_group<20>(cx, idx, lane, smem); break;
-        case 2: tu_group<2>(cx, idx, lane, smem); break;
-        case 15: tu_group<15>(cx, idx, lane, smem); break;
-        case 16: tu_group<16>(cx, idx, lane, smem); break;
-        case 1: tu_group<1>(cx, idx, lane, smem); break;
-        default: tu_group<0>(cx, idx, lane, smem); break;
+        if constexpr (C0 == 0) {
+            if (c < 3) {
+                switch (c_class_part[c]) {
+                case 4: tu_group<4>(cx, idx, lane, smem); break;
+                case 23: tu_group<23>(cx, idx, lane, smem); break;
+                default: tu_group<24>(cx, idx, lane, smem); break;
+                }
+                continue;
+            }
+        }
+        if constexpr (C1 > 3) {
+            switch (c_class_part[c]) {
+            case 3: tu_group<3, RA>(cx, idx, lane, smem); break;
+            case 19: tu_group<19, RA>(cx, idx, lane, smem); break;
+            case 20: tu_group<20, RA>(cx, idx, lane, smem); break;
+            case 2: tu_group<2, RA>(cx, idx, lane, smem); break;
+            case 15: tu_group<15, RA>(cx, idx, lane, smem); break;
+            case 16: tu_group<16, RA>(cx, idx, lane, smem); break;
+            case 1: tu_group<1, RA>(cx, idx, lane, smem); break;
+            default: tu_group<0, RA>(cx, idx, lane, smem); break;
+            }
         }
     }
 }
 
 }  // namespace tqw
 
+// Region A of the non-wavelet classes: the 32x32 TU's two transposes and its
+// staging (2 x 32 x 34 + 32 x 32 int16).
+constexpr int kRegionSmall = 6400;
+
+// Build option: 1 runs the wavelet classes and the others as two launches,
+// the latter with 6.4 KB of shared memory per warp and a register budget for
+// more CTAs per SM; 0 one launch over all classes.
+#ifndef XG_TQ_SPLIT
+#define XG_TQ_SPLIT 1
+#endif
+#ifndef XG_TQ_SMALL_MINB
+#define XG_TQ_SMALL_MINB 6
+#endif
+
+// One persistent launch of the chain over the classes [C0, C1): the shared-
+// memory attribute and the occupancy are taken once per device and kernel
+// instance (the statics belong to the instantiation).
+template <int WARPS, int C0, int C1, int RA, int MINB>
+static void tq_run(const tqw::Ctx &cx, const int *counts, const int *sorted, long long ctas_needed, int dev,
+                   cudaStream_t st)
+{
+    constexpr int smem = WARPS * (C0 == 0 ? RA + tqw::kRegionB : RA);
+    static bool attr_set[64] = {false};
+    static int ctas_per_sm[64] = {0};
+    if (!attr_set[dev]) {
+        XG_CUDA(cudaFuncSetAttribute(tqw::tq_chain_kernel<WARPS, C0, C1, RA, MINB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas_per_sm[dev], tqw::tq_chain_kernel<WARPS, C0, C1, RA, MINB>,
+                                                              WARPS * 32, smem));
+        if (ctas_per_sm[dev] < 1) ctas_per_sm[dev] = 1;
+        attr_set[dev] = true;
+    }
+    long long grid = (long long)sm_count() * ctas_per_sm[dev];
+    if (grid > ctas_needed) grid = ctas_needed;
+    tqw::tq_chain_kernel<WARPS, C0, C1, RA, MINB><<<(int)grid, WARPS * 32, smem, st>>>(cx, counts, sorted);
+}
+
 template <int WARPS>
 static int tq_launch_w(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *residual, int16_t *coef,
                        int16_t *recon, int32_t *nnz, cudaStream_t stream)
 {
-    constexpr int smem = WARPS * tqw::kWarpSmem;
-    static bool attr_set[64] = {false};
-    static int ctas_per_sm[64] = {0}, sms[64] = {0};
+    static bool pool_set[64] = {false};
     const int dev = current_device();
     if (dev < 0 || dev >= 64) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_tq_batch", "device index out of range");
         return XAVS2GPU_ERR_ARG;
     }
-    if (!attr_set[dev]) {
-        XG_CUDA(cudaFuncSetAttribute(tqw::tq_chain_kernel<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas_per_sm[dev], tqw::tq_chain_kernel<WARPS>,
-                                                              WARPS * 32, smem));
-        XG_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev));
-        if (ctas_per_sm[dev] < 1) ctas_per_sm[dev] = 1;
+    if (!pool_set[dev]) {
         // keep freed stream-ordered scratch in the pool between batches
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
             uint64_t keep = UINT64_MAX;
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
-        attr_set[dev] = true;
+        pool_set[dev] = true;
     }
     // scratch: class counts and cursors (32 ints each), then the ordered list
     int *scratch = nullptr;
@@ -609,12 +654,18 @@ static int tq_launch_w(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *
     const int nb = (n + 255) / 256;
     tqw::tq_count_kernel<<<nb, 256, 0, stream>>>(blocks, n, counts, nnz);
     tqw::tq_scatter_kernel<<<nb, 256, 0, stream>>>(blocks, n, counts, cursor, sorted);
-    long long grid = (long long)sms[dev] * ctas_per_sm[dev];
-    const long long ctas_needed = ((long long)n + WARPS - 1) / WARPS;
-    if (grid > ctas_needed) grid = ctas_needed;
     tqw::Ctx cx{blocks, residual, coef, recon, nnz};
-    tqw::tq_chain_kernel<WARPS><<<(int)grid, WARPS * 32, smem, stream>>>(cx, counts, sorted);
+    const long long ctas_needed = ((long long)n + WARPS - 1) / WARPS;
+#if XG_TQ_SPLIT
+    tq_run<WARPS, 0, 3, tqw::kRegionA, 1>(cx, counts, sorted, ctas_needed, dev, stream);
+    tq_run<WARPS, 3, tqw::kNumClasses, kRegionSmall, XG_TQ_SMALL_MINB * 4 / WARPS>(cx, counts, sorted, ctas_needed, dev,
+                                                                                   stream);
+    count_launch(4);
+#else
+    // 16 warps per SM (128 registers)
+    tq_run<WARPS, 0, tqw::kNumClasses, tqw::kRegionA, 16 / WARPS>(cx, counts, sorted, ctas_needed, dev, stream);
     count_launch(3);
+#endif
     XG_CUDA(cudaFreeAsync(scratch, stream));
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
