@@ -231,10 +231,11 @@ __device__ __forceinline__ int class_of(int part)
 __host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v / 2); }
 
 // Per-warp shared memory: region A holds the wavelet input (64 rows, pitch
-// 66 int16) or the transposes and the output staging of the warp's G TUs;
-// region B the wavelet's horizontal low band (64 rows, pitch 34 int16) and
-// later the inverse transform's output for the upsampling.
-constexpr int kRegionA = 64 * 66 * 2, kRegionB = 64 * 34 * 2;
+// 66 int16; the horizontal lifting leaves each row's low band in its first
+// half) or the transposes and the output staging of the warp's G TUs;
+// region B the wavelet's LL band (up to 32 rows, pitch 34 int16) and later
+// the inverse transform's output for the upsampling.
+constexpr int kRegionA = 64 * 66 * 2, kRegionB = 32 * 34 * 2;
 constexpr int kWarpSmem = kRegionA + kRegionB;
 
 struct Ctx {
@@ -269,7 +270,7 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
     // ---- forward rows -> T1[k][j] (pitch P1) in region A
     uint32_t xp[TW / 2];
     if constexpr (S::WAV) {
-        constexpr int PX = 66, HP = 34, PL = TW + 2;
+        constexpr int PX = 66, PL = TW + 2;
         if (act) {
             if (al_in) {
                 // the lane's 16-byte loads in batches of 8 (a batch is one
@@ -294,23 +295,25 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
         __syncwarp();
         // horizontal lifting, one row per lane: odd[m] = p[2m+1] - (p[2m] +
         // p[2m+2]) >> 1, H[m] = p[2m] + (odd[m-1] + odd[m] + 2) >> 2, int16
-        // after each step, mirrored ends (p[IW] = p[IW-2], odd[-1] = odd[0])
+        // after each step, mirrored ends (p[IW] = p[IW-2], odd[-1] = odd[0]);
+        // H[m] goes to sample m of the same row (the samples still to be
+        // read, 2m+1 on, lie beyond it)
         if (act) {
             for (int r = lane; r < IH; r += 32) {
-                const int16_t *p = tA + r * PX;
+                int16_t *p = tA + r * PX;
                 int prev_odd = 0, pe = p[0];
                 for (int m = 0; m < IW / 2; m++) {
                     const int po = p[2 * m + 1], pn = m + 1 < IW / 2 ? p[2 * m + 2] : p[IW - 2];
                     const int odd = (int16_t)(po - ((pe + pn) >> 1));
                     if (m == 0) prev_odd = odd;
-                    tB[r * HP + m] = (int16_t)(pe + ((prev_odd + odd + 2) >> 2));
+                    p[m] = (int16_t)(pe + ((prev_odd + odd + 2) >> 2));
                     prev_odd = odd;
                     pe = pn;
                 }
             }
         }
         __syncwarp();
-        // vertical lifting, one LL row per lane (j < TH), into region A:
+        // vertical lifting, one LL row per lane (j < TH), into region B:
         // odd'[m] = q[2m+1] - (q[2m] + q[2m+2]) >> 1,
         // LL[m] = 2 q[2m] + (odd'[m-1] + odd'[m] + 1) >> 1
         if (act && lane < TH) {
@@ -318,15 +321,15 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
             const int rm2 = j == 0 ? 2 : 2 * j - 2, rm1 = j == 0 ? 1 : 2 * j - 1;
             const int rp1 = 2 * j + 1, rp2 = j == TH - 1 ? 2 * j : 2 * j + 2;
             for (int i = 0; i < TW; i++) {
-                const int qa = tB[rm2 * HP + i], qb = tB[rm1 * HP + i], qc = tB[2 * j * HP + i];
-                const int qd = tB[rp1 * HP + i], qe = tB[rp2 * HP + i];
+                const int qa = tA[rm2 * PX + i], qb = tA[rm1 * PX + i], qc = tA[2 * j * PX + i];
+                const int qd = tA[rp1 * PX + i], qe = tA[rp2 * PX + i];
                 const int oa = (int16_t)(qb - ((qa + qc) >> 1));
                 const int ob = (int16_t)(qd - ((qc + qe) >> 1));
-                tA[j * PL + i] = (int16_t)((qc << 1) + ((oa + ob + 1) >> 1));
+                tB[j * PL + i] = (int16_t)((qc << 1) + ((oa + ob + 1) >> 1));
             }
         }
         __syncwarp();
-        if (act && lane < TH) load_pairs<TW>(tA + lane * PL, xp);
+        if (act && lane < TH) load_pairs<TW>(tB + lane * PL, xp);
         __syncwarp();
     } else {
         if (act && l < TH) load_pairs_global<TW>(src + l * TW, al_in, xp);
@@ -602,6 +605,12 @@ constexpr int kRegionSmall = 6400;
 #ifndef XG_TQ_SMALL_MINB
 #define XG_TQ_SMALL_MINB 6
 #endif
+// resident CTAs of 4 warps per SM the register budgets are sized for: the
+// wavelet classes at 5 (96 registers; 10.4 KB of shared memory per warp),
+// the rest at 6 (85 registers; 6.25 KB)
+#ifndef XG_TQ_BIG_MINB
+#define XG_TQ_BIG_MINB 5
+#endif
 
 // One persistent launch of the chain over the classes [C0, C1): the shared-
 // memory attribute and the occupancy are taken once per device and kernel
@@ -657,7 +666,7 @@ static int tq_launch_w(const xavs2gpu_tq_block_t *blocks, int n, const int16_t *
     tqw::Ctx cx{blocks, residual, coef, recon, nnz};
     const long long ctas_needed = ((long long)n + WARPS - 1) / WARPS;
 #if XG_TQ_SPLIT
-    tq_run<WARPS, 0, 3, tqw::kRegionA, 1>(cx, counts, sorted, ctas_needed, dev, stream);
+    tq_run<WARPS, 0, 3, tqw::kRegionA, XG_TQ_BIG_MINB * 4 / WARPS>(cx, counts, sorted, ctas_needed, dev, stream);
     tq_run<WARPS, 3, tqw::kNumClasses, kRegionSmall, XG_TQ_SMALL_MINB * 4 / WARPS>(cx, counts, sorted, ctas_needed, dev,
                                                                                    stream);
     count_launch(4);
