@@ -682,6 +682,10 @@ __device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, c
 #define XG_REFINE_MINB 4
 #endif
 
+// HAD: SATD (1) or SAD (0) unit costs, fixed per launch so that each
+// instance holds the code of one (the kernel waits on its instruction cache
+// otherwise)
+template <bool HAD>
 __global__ void __launch_bounds__(128, XG_REFINE_MINB) refine_thread_kernel(const uint32_t *__restrict__ list, int n,
                                                             const SessView *__restrict__ views, int R,
                                                             xavs2gpu_me_params_t prm)
@@ -723,7 +727,7 @@ __global__ void __launch_bounds__(128, XG_REFINE_MINB) refine_thread_kernel(cons
     int bx = bmx * 4, by = bmy * 4, best = icost;
     if (prm.fractional_me) {
         const int w = c_pu_w[p.part], h = c_pu_h[p.part];
-        const bool had = prm.use_hadamard != 0;
+        const bool had = HAD;
         const bool u4 = had ? satd_unit4(w, h) : (w == 4 || w == 12);
         const int nux = w / (u4 ? 4 : 8), nu = nux * (h >> 2);
         const uint8_t *o = cur + (ptrdiff_t)p.y * g.stride + p.x;
@@ -1612,8 +1616,13 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     const int *lst_s = grouped ? m.d_small_g : m.d_small, *lst_l = grouped ? m.d_large_g : m.d_large;
     if (grouped) launch_groups(m.d_groups, m.n_groups, m.d_members, m.d_view, R, *prm, m.st);
     if (ns) {
-        refine_thread_kernel<<<(ns + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
-            reinterpret_cast<const uint32_t *>(lst_s), ns, m.d_view, R, *prm);
+        const unsigned g = (ns + m.tune_block - 1) / m.tune_block;
+        if (prm->use_hadamard)
+            refine_thread_kernel<true><<<g, m.tune_block, 0, m.st>>>(reinterpret_cast<const uint32_t *>(lst_s), ns,
+                                                                     m.d_view, R, *prm);
+        else
+            refine_thread_kernel<false><<<g, m.tune_block, 0, m.st>>>(reinterpret_cast<const uint32_t *>(lst_s), ns,
+                                                                      m.d_view, R, *prm);
         count_launch();
     }
     if (nl) {
@@ -2010,8 +2019,11 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
     }
     if (ngr) launch_groups(bb.d_groups, (int)ngr, d_members, bb.d_views, R, *prm, st);
     if (ns) {
-        refine_thread_kernel<<<(unsigned)((ns + block - 1) / block), block, 0, st>>>(d_small, (int)ns, bb.d_views, R,
-                                                                                  *prm);
+        const unsigned g = (unsigned)((ns + block - 1) / block);
+        if (prm->use_hadamard)
+            refine_thread_kernel<true><<<g, block, 0, st>>>(d_small, (int)ns, bb.d_views, R, *prm);
+        else
+            refine_thread_kernel<false><<<g, block, 0, st>>>(d_small, (int)ns, bb.d_views, R, *prm);
         count_launch();
     }
     if (nl) {
