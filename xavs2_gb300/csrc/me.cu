@@ -649,27 +649,93 @@ __device__ __forceinline__ void load_unit(const uint8_t *o, int stride, int (&c)
 
 #endif
 
+#if XG_REFINE_PACKED
+// The unit loads and costs with the unit width a run-time flag (one copy of
+// the code for 4x4 and 8x4 units: the per-thread refinement is bound by its
+// instruction cache).
+__device__ __forceinline__ void load_unit_rt(const uint8_t *o, int stride, UnitCur &c, bool u4)
+{
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        uint32_t lo, hi;
+        load8u(o + y * stride, lo, hi);
+        c.w[y][0] = lo;
+        c.w[y][1] = u4 ? 0u : hi;
+        row_pairs(lo, c.w[y][1], c.q[y]);
+    }
+}
+
+__device__ __forceinline__ int unit_cost_pre_rt(bool had, bool u4, const UnitCur &c, const uint8_t *r, int stride)
+{
+    if (!had) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            uint32_t lo, hi;
+            load8u(r + y * stride, lo, hi);
+            s = sad4_acc(c.w[y][0], lo, s);
+            s = sad4_acc(c.w[y][1], u4 ? 0u : hi, s);
+        }
+        return (int)s;
+    }
+    uint32_t d[4][4];
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        uint32_t lo, hi, q[4];
+        load8u(r + y * stride, lo, hi);
+        row_pairs(lo, u4 ? 0u : hi, q);
+        const uint32_t d0 = __vsub2(c.q[y][0], q[0]), d1 = __vsub2(c.q[y][1], q[1]);
+        const uint32_t d2 = __vsub2(c.q[y][2], q[2]), d3 = __vsub2(c.q[y][3], q[3]);
+        const uint32_t s0 = __vadd2(d0, d1), e0 = __vsub2(d0, d1), s1 = __vadd2(d2, d3), e1 = __vsub2(d2, d3);
+        d[y][0] = __vadd2(s0, s1);
+        d[y][1] = __vadd2(e0, e1);
+        d[y][2] = __vsub2(s0, s1);
+        d[y][3] = __vsub2(e0, e1);
+    }
+    int s = 0;
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+        const uint32_t s0 = __vadd2(d[0][x], d[1][x]), e0 = __vsub2(d[0][x], d[1][x]);
+        const uint32_t s1 = __vadd2(d[2][x], d[3][x]), e1 = __vsub2(d[2][x], d[3][x]);
+        s = abs_pair_acc(__vadd2(s0, s1), s);
+        s = abs_pair_acc(__vadd2(e0, e1), s);
+        s = abs_pair_acc(__vsub2(s0, s1), s);
+        s = abs_pair_acc(__vsub2(e0, e1), s);
+    }
+    return s >> 1;
+}
+#endif
+
 // Accumulates the costs of up to 9 positions over all units of the PU.
-template <bool U4>
-__device__ __forceinline__ void refine_stage_thread(bool had, int nux, int nu, const uint8_t *o,
+__device__ __forceinline__ void refine_stage_thread(bool had, bool u4, int nux, int nu, const uint8_t *o,
                                                     const uint8_t *const *planes, int stride, int px, int py,
                                                     const int (&mxs)[9], const int (&mys)[9], int npos,
                                                     int (&acc)[9])
 {
-    constexpr int UW = U4 ? 4 : 8;
+    const int uw = u4 ? 4 : 8;
 #pragma unroll
     for (int k = 0; k < 9; k++) acc[k] = 0;
     for (int u = 0; u < nu; u++) {
         const int uy = u / nux, ux = u - uy * nux;
         UnitC c;
-        load_unit<U4>(o + (ptrdiff_t)uy * 4 * stride + ux * UW, stride, c);
+        const uint8_t *ou = o + (ptrdiff_t)uy * 4 * stride + ux * uw;
+#if XG_REFINE_PACKED
+        load_unit_rt(ou, stride, c, u4);
+#else
+        if (u4) load_unit<true>(ou, stride, c);
+        else load_unit<false>(ou, stride, c);
+#endif
 #pragma unroll
         for (int k = 0; k < 9; k++) {
             if (k < npos) {
                 const int mx = mxs[k], my = mys[k];
                 const uint8_t *r = planes[((my & 3) << 2) + (mx & 3)] +
-                                   (ptrdiff_t)(py + uy * 4 + (my >> 2)) * stride + px + ux * UW + (mx >> 2);
-                acc[k] += unit_cost_pre<U4>(had, c, r, stride);
+                                   (ptrdiff_t)(py + uy * 4 + (my >> 2)) * stride + px + ux * uw + (mx >> 2);
+#if XG_REFINE_PACKED
+                acc[k] += unit_cost_pre_rt(had, u4, c, r, stride);
+#else
+                acc[k] += u4 ? unit_cost_pre<true>(had, c, r, stride) : unit_cost_pre<false>(had, c, r, stride);
+#endif
             }
         }
     }
@@ -765,8 +831,7 @@ __global__ void __launch_bounds__(128, XG_REFINE_MINB) refine_thread_kernel(cons
                 npos++;
             }
             int acc[9];
-            if (u4) refine_stage_thread<true>(had, nux, nu, o, planes, g.stride, p.x, p.y, mxs, mys, npos, acc);
-            else refine_stage_thread<false>(had, nux, nu, o, planes, g.stride, p.x, p.y, mxs, mys, npos, acc);
+            refine_stage_thread(had, u4, nux, nu, o, planes, g.stride, p.x, p.y, mxs, mys, npos, acc);
             const int k0 = (stage == 0 && had) ? 1 : 0;
             if (k0) best = acc[0] + mv_cost_hd(lam, cx, cy, pmx, pmy);
 #pragma unroll
