@@ -570,6 +570,10 @@ XAVS2GPU_API int xavs2gpu_me_plane_stride(xavs2gpu_me_session_t *s);
  * host memory with row stride `stride`; waits. */
 XAVS2GPU_API int xavs2gpu_me_get_plane(xavs2gpu_me_session_t *s, int slot, int k, uint8_t *out, intptr_t stride);
 XAVS2GPU_API int xavs2gpu_me_plane_pad(xavs2gpu_me_session_t *s);
+/* 1 when the session's CTU search copies its reference windows with the
+ * tensor memory accelerator (a tensor map over the session's planes was
+ * encoded), 0 when it uses 16-byte loads.  Results are the same either way. */
+XAVS2GPU_API int xavs2gpu_me_window_tma(xavs2gpu_me_session_t *s);
 XAVS2GPU_API void *xavs2gpu_me_stream(xavs2gpu_me_session_t *s);
 /* Geometry and PU list of a session (host copies). */
 XAVS2GPU_API void xavs2gpu_me_session_info(const xavs2gpu_me_session_t *s, int *width, int *height, int *num_refs,

@@ -42,6 +42,7 @@ def _run(cur, refs, pus, prm):
     for i, r in enumerate(refs):
         s.set_picture(i, r)
     s.set_pus(pus)
+    assert s.window_tma(), "no tensor map for the window copies"
     s.run(prm)
     out = s.results()
     stats = s.plan_stats()

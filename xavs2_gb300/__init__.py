@@ -107,6 +107,7 @@ _SIGS = {
     "xavs2gpu_me_plane_device": (_P, [_P, _I, _I]),
     "xavs2gpu_me_plane_stride": (_I, [_P]),
     "xavs2gpu_me_plane_pad": (_I, [_P]),
+    "xavs2gpu_me_window_tma": (_I, [_P]),
     "xavs2gpu_me_stream": (_P, [_P]),
     "xavs2gpu_me_plan_stats": (None, [_P, _P, _P, _P]),
     "xavs2gpu_me_get_plane": (_I, [_P, _I, _I, _P, _S]),
@@ -298,6 +299,10 @@ class MeSession:
 
     def stream(self):
         return self.lib.xavs2gpu_me_stream(self.h)
+
+    def window_tma(self):
+        """Whether the CTU search copies its windows with the TMA."""
+        return bool(self.lib.xavs2gpu_me_window_tma(self.h))
 
     def set_profiling(self, on=True):
         self.lib.xavs2gpu_me_set_profiling(self.h, 1 if on else 0)

@@ -365,6 +365,59 @@ __device__ __forceinline__ void sad_at(const uint8_t *win, int ww, int wrow0, in
 #define XG_CTU_VEC_FILL 1
 #endif
 
+// Window fill by the tensor memory accelerator: where the session has a
+// tensor map over its plane pool (3-D: column, row, plane; box 64 columns x
+// 95 rows) and the window qualifies for the 16-byte fill, one thread issues
+// the window as 64-column boxes into a dense staging area before the CTA
+// computes its MV-cost keys, so the copy overlaps that work.  The search's
+// row layout shifts rows by 1-3 words (the bank spread above), which no
+// 16-byte-aligned TMA destination can hold, so a shared-to-shared pass then
+// places the rows.
+#ifndef XG_CTU_TMA
+#define XG_CTU_TMA 1
+#endif
+constexpr int kTmaBoxCols = 64;
+constexpr int kTmaBoxRows = 64 + kDyChunk - 1;
+constexpr int kTmaPieceBytes = (kTmaBoxCols * kTmaBoxRows + 127) / 128 * 128;   // 6144
+constexpr int kWaitLimit = 1 << 20;   // mbarrier polls before a CTA gives up its window
+
+__host__ __device__ constexpr int tma_pieces(int R) { return (64 + 2 * R + 8 + kTmaBoxCols - 1) / kTmaBoxCols; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < kWaitLimit; i++) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Thread 0 only: the window rows [y, y + 95) of plane z, columns x .. x + 64*np
+// (x a multiple of 16), as np boxes into stage (128-byte aligned), counted
+// on the barrier at bar.
+__device__ __forceinline__ void tma_window_issue(const void *tmap, uint32_t stage, uint32_t bar, int x, int y, int z,
+                                                 int np)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"((uint32_t)(np * kTmaBoxCols * kTmaBoxRows))
+                 : "memory");
+    for (int p = 0; p < np; p++)
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                     " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(stage + (uint32_t)(p * kTmaPieceBytes)),
+                     "l"(tmap), "r"(x + p * kTmaBoxCols), "r"(y), "r"(z), "r"(bar)
+                     : "memory");
+}
+
 // resident CTAs per SM the register budget is sized for (3: up to 168
 // registers; measured faster than 4 CTAs of 128 registers and than 2)
 #ifndef XG_CTU_MINB
@@ -451,6 +504,32 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
     uint32_t *mvk = reinterpret_cast<uint32_t *>(smem);                 // [2][kDyChunk][nd]
     uint8_t *win = smem + 2 * sizeof(uint32_t) * kDyChunk * nd;          // [wrows][ww]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // reference window: rows y0+dy0 .., columns x0-R .., clamped into the plane
+    const uint8_t *ref = refs[job.ref];
+    const int wx0 = job.x0 - R, wy0 = job.y0 + dy0;
+    const int rowlen = ww - 4 * kSwzMax - 4;   // bytes of a row that are filled (a multiple of 16)
+    const bool vec_ok = wx0 >= -kPad && wx0 + rowlen <= g.W + kPad && wy0 >= -kPad && wy0 + wrows <= g.H + kPad &&
+                        (g.stride & 15) == 0 &&
+                        ((uintptr_t)(ref + (ptrdiff_t)wy0 * g.stride + wx0) & 15) == 0;
+#if XG_CTU_TMA
+    // staging area after the window (128-byte aligned when the dynamic shared
+    // memory base is), the barrier after it
+    uint8_t *stage = win + (size_t)wrows * ww;
+    const int np = tma_pieces(R);
+    const uint32_t stage_s = smem_u32(stage), bar_s = stage_s + (uint32_t)(np * kTmaPieceBytes);
+    int tx = 0, ty = 0, tz = 0;
+    bool use_tma = false;
+    if (view.tmap != nullptr && vec_ok && (stage_s & 127) == 0) {
+        const ptrdiff_t off = (ref + (ptrdiff_t)wy0 * g.stride + wx0) - view.pool;
+        tz = (int)(off / (ptrdiff_t)view.plane_bytes);
+        const ptrdiff_t rem = off - (ptrdiff_t)tz * view.plane_bytes;
+        ty = (int)(rem / g.stride);
+        tx = (int)(rem - (ptrdiff_t)ty * g.stride);
+        use_tma = off >= 0 && (tx & 15) == 0;
+    }
+    if (use_tma && tid == 0) tma_window_issue(view.tmap, stage_s, bar_s, tx, ty, tz, np);
+    __syncthreads();   // the barrier's initialisation, before any thread polls it
+#endif
 
     // MV cost keys of this chunk's displacements (uniform over the CTU)
     for (int e = tid; e < kDyChunk * nd; e += kCtuThreads) {
@@ -460,13 +539,33 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
         mvk[e] = (mvc << 11) | ((uint32_t)(row & (kDyWarp - 1)) << 8) | (uint32_t)dxr;
         mvk[kDyChunk * nd + e] = (mvc << 8) | (uint32_t)dxr;
     }
-    // reference window: rows y0+dy0 .., columns x0-R .., clamped into the plane
-    const uint8_t *ref = refs[job.ref];
-    const int wx0 = job.x0 - R, wy0 = job.y0 + dy0;
-    const int rowlen = ww - 4 * kSwzMax - 4;   // bytes of a row that are filled (a multiple of 16)
+#if XG_CTU_TMA
+    if (use_tma) {
+        const bool ok = mbar_wait_bounded(bar_s, 0);
+        if (__syncthreads_or(!ok)) {
+            // the copy did not land: record it, give the copies in flight
+            // one more bounded wait, and leave this chunk unsearched
+            if (tid == 0 && view.wait_flag) atomicOr(view.wait_flag, 1u);
+            mbar_wait_bounded(bar_s, 0);
+            return;
+        }
+        // staged rows [95][64] per box -> the swizzled window rows; only the
+        // bytes the row layout holds (a multiple of 16, at least 64 + 2R + 8)
+        const int cols = min(np * kTmaBoxCols, rowlen) >> 4;
+        for (int e = tid; e < wrows * cols; e += kCtuThreads) {
+            const int r = e / cols, c = (e - r * cols) << 4;
+            const uint4 v = *reinterpret_cast<const uint4 *>(stage + (c >> 6) * kTmaPieceBytes + r * kTmaBoxCols +
+                                                             (c & (kTmaBoxCols - 1)));
+            uint32_t *d = reinterpret_cast<uint32_t *>(win + r * ww + 4 * swz(r) + c);
+            d[0] = v.x;
+            d[1] = v.y;
+            d[2] = v.z;
+            d[3] = v.w;
+        }
+    } else
+#endif
 #if XG_CTU_VEC_FILL
-    if (wx0 >= -kPad && wx0 + rowlen <= g.W + kPad && wy0 >= -kPad && wy0 + wrows <= g.H + kPad &&
-        (g.stride & 15) == 0 && ((uintptr_t)(ref + (ptrdiff_t)wy0 * g.stride + wx0) & 15) == 0) {
+    if (vec_ok) {
         // the window lies inside the padded plane and its rows start on
         // 16-byte boundaries: 16-byte loads, word stores into the swizzled rows
         const int q = rowlen >> 4;
@@ -795,7 +894,12 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
 static inline size_t ctu_smem_bytes(int R, int &ww)
 {
     ww = (int)align_up((size_t)64 + 2 * R + 8 + 4 * kSwzMax + 4, 128);
-    return 2 * sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
+    const size_t keys_win = 2 * sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
+#if XG_CTU_TMA
+    return keys_win + (size_t)tma_pieces(R) * kTmaPieceBytes + 16;   // staging boxes and their barrier
+#else
+    return keys_win;
+#endif
 }
 
 // One launch of each variant over `n_jobs` jobs (sessions per job.sess).

@@ -18,6 +18,8 @@
 // and refine_kernel.
 #include "xavs2gpu_common.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -54,6 +56,12 @@ struct SessView {
     const int32_t *slots;           // CTU slot map
     Geometry g;
     int n;                          // PUs
+    // plane pool (every plane of the session, plane_bytes apart) and a
+    // tensor map over it (3-D: column, row, plane), or null
+    const void *tmap;
+    const uint8_t *pool;
+    size_t plane_bytes;
+    unsigned *wait_flag;            // set by a kernel that gave up a bounded wait
 };
 constexpr int kSessShift = 24;
 constexpr uint32_t kIdxMask = (1u << kSessShift) - 1;
@@ -1251,6 +1259,7 @@ struct MeSessionImpl {
     int device = 0;
     cudaStream_t st = nullptr;
     uint8_t *d_planes = nullptr;          // plane 0: current picture; 1 + r*16 + k: reference r, sub-pel k
+    void *d_tmap = nullptr;               // tensor map over d_planes (window copies), or null
     uint8_t **d_plane_ptrs = nullptr;     // [1 + nrefs*16] pointers at pixel (0,0)
     const uint8_t **d_ref0 = nullptr;     // [nrefs] full-pel plane of each reference
     uint8_t *h_stage = nullptr;           // pinned staging for pictures
@@ -1299,6 +1308,78 @@ struct MeSessionImpl {
     uint8_t *ref_plane(int slot, int k) { return plane(1 + 16 * slot_buf[slot] + k); }
 };
 
+// A mapped pinned word that kernels set when they give up a bounded wait
+// (the window copy of the CTU search); the host reads it after a
+// synchronisation.  Null when mapped memory is unavailable.
+static unsigned *wait_flag_word()
+{
+    static unsigned *word = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *h = nullptr;
+        if (cudaHostAlloc(&h, sizeof(unsigned), cudaHostAllocMapped | cudaHostAllocPortable) == cudaSuccess) {
+            *static_cast<volatile unsigned *>(h) = 0;
+            word = static_cast<unsigned *>(h);
+        } else {
+            cudaGetLastError();
+        }
+    });
+    return word;
+}
+
+// Reports (once) a bounded wait a kernel gave up since the last check.
+static int check_wait_flag(const char *where)
+{
+    unsigned *w = wait_flag_word();
+    if (w && *static_cast<volatile unsigned *>(w)) {
+        *static_cast<volatile unsigned *>(w) = 0;
+        fail(XAVS2GPU_ERR_CUDA, where, "a search window copy did not complete within its wait limit");
+        return XAVS2GPU_ERR_CUDA;
+    }
+    return XAVS2GPU_OK;
+}
+
+// Tensor map over a session's plane pool for the CTU search's window copies:
+// 3-D u8 (column < stride, row < rows, plane < nplanes), rows stride bytes
+// and planes plane_bytes apart, box kTmaBoxCols x kTmaBoxRows x 1, zero fill
+// outside.  Returns a device copy (64-byte aligned), or null when the driver
+// entry point or the encoding is unavailable (the search then fills its
+// window with 16-byte loads).
+static void *plane_pool_tmap(const uint8_t *pool, int stride, int rows, size_t plane_bytes, int nplanes)
+{
+#if XG_CTU_TMA
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    });
+    if (!encode || ((uintptr_t)pool & 255) || (stride & 15) || (plane_bytes & 15)) return nullptr;
+    CUtensorMap tm;
+    const cuuint64_t dims[3] = {(cuuint64_t)stride, (cuuint64_t)rows, (cuuint64_t)nplanes};
+    const cuuint64_t strides[2] = {(cuuint64_t)stride, (cuuint64_t)plane_bytes};
+    const cuuint32_t box[3] = {(cuuint32_t)kTmaBoxCols, (cuuint32_t)kTmaBoxRows, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    if (encode(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<uint8_t *>(pool), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return nullptr;
+    void *d = nullptr;
+    XG_CUDA(cudaMalloc(&d, sizeof(CUtensorMap)));
+    XG_CUDA(cudaMemcpy(d, &tm, sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+    return d;
+#else
+    (void)pool; (void)stride; (void)rows; (void)plane_bytes; (void)nplanes;
+    return nullptr;
+#endif
+}
+
 static void refresh_view(MeSessionImpl &m)
 {
     SessView v;
@@ -1312,6 +1393,10 @@ static void refresh_view(MeSessionImpl &m)
     v.slots = m.plan.d_slots;
     v.g = Geometry{m.W, m.H, m.stride};
     v.n = m.n;
+    v.tmap = m.d_tmap;
+    v.pool = m.d_planes;
+    v.plane_bytes = m.plane_bytes;
+    v.wait_flag = wait_flag_word();
     m.h_view = v;
     XG_CUDA(cudaMemcpyAsync(m.d_view, &m.h_view, sizeof(SessView), cudaMemcpyHostToDevice, m.st));
 }
@@ -1365,6 +1450,7 @@ extern "C" xavs2gpu_me_session_t *xavs2gpu_me_create(int width, int height, int 
     for (int k = 0; k < nplanes; k++) ptrs[k] = m.plane(k);
     XG_CUDA(cudaMalloc((void **)&m.d_plane_ptrs, sizeof(uint8_t *) * nplanes));
     XG_CUDA(cudaMemcpy(m.d_plane_ptrs, ptrs.data(), sizeof(uint8_t *) * nplanes, cudaMemcpyHostToDevice));
+    m.d_tmap = plane_pool_tmap(m.d_planes, m.stride, m.rows, m.plane_bytes, nplanes);
     std::vector<const uint8_t *> r0(num_refs);
     for (int r = 0; r < num_refs; r++) r0[r] = m.plane(1 + 16 * r);
     XG_CUDA(cudaMalloc((void **)&m.d_ref0, sizeof(uint8_t *) * num_refs));
@@ -1399,6 +1485,7 @@ extern "C" void xavs2gpu_me_destroy(xavs2gpu_me_session_t *s)
     cudaFree(m.d_view);
     ctu_plan_free(m.plan);
     cudaFree(m.d_planes); cudaFree(m.d_plane_ptrs); cudaFree(m.d_ref0);
+    if (m.d_tmap) cudaFree(m.d_tmap);
     cudaFreeHost(m.h_stage); cudaFree(m.d_upload);
     cudaFree(m.d_pus); cudaFree(m.d_res); cudaFreeHost(m.h_res); cudaFree(m.d_keys);
     cudaFree(m.d_state); cudaFree(m.d_generic); 
@@ -1829,14 +1916,14 @@ extern "C" int xavs2gpu_me_get_results(xavs2gpu_me_session_t *s, xavs2gpu_me_res
         XG_CUDA(cudaMemcpyAsync(out, m.d_res, sizeof(xavs2gpu_me_result_t) * m.n, cudaMemcpyDeviceToHost, m.st));
         XG_CUDA(cudaStreamSynchronize(m.st));
     }
-    return XAVS2GPU_OK;
+    return check_wait_flag("xavs2gpu_me_get_results");
 }
 
 extern "C" int xavs2gpu_me_sync(xavs2gpu_me_session_t *s)
 {
     if (!s) return XAVS2GPU_ERR_ARG;
     XG_CUDA(cudaStreamSynchronize(s->impl.st));
-    return XAVS2GPU_OK;
+    return check_wait_flag("xavs2gpu_me_sync");
 }
 
 extern "C" const xavs2gpu_me_result_t *xavs2gpu_me_results_device(xavs2gpu_me_session_t *s)
@@ -1867,6 +1954,7 @@ extern "C" int xavs2gpu_me_get_plane(xavs2gpu_me_session_t *s, int slot, int k, 
     return XAVS2GPU_OK;
 }
 extern "C" int xavs2gpu_me_plane_pad(xavs2gpu_me_session_t *) { return kPad; }
+extern "C" int xavs2gpu_me_window_tma(xavs2gpu_me_session_t *s) { return s && s->impl.d_tmap ? 1 : 0; }
 extern "C" void *xavs2gpu_me_stream(xavs2gpu_me_session_t *s) { return s ? (void *)s->impl.st : nullptr; }
 
 extern "C" void xavs2gpu_me_plan_stats(xavs2gpu_me_session_t *s, int *n_ctu_pus, int *n_generic_pus, int *n_ctu_jobs)
@@ -2154,6 +2242,10 @@ __global__ void noalloc_prepare_kernel(const xavs2gpu_pu_t *__restrict__ in, int
         v.slots = nullptr;
         v.g = Geometry{W, H, stride};
         v.n = n;
+        v.tmap = nullptr;
+        v.pool = nullptr;
+        v.plane_bytes = 0;
+        v.wait_flag = nullptr;
         s->view = v;
     }
     if (i >= n) return;
