@@ -192,6 +192,17 @@ __device__ __forceinline__ void inv_split(const uint32_t (&cp)[N / 2], Out out)
     }
 }
 
+// The wavelet's forward lifting on 32-bit words (two samples each), a chunk
+// of each row loaded before the in-place stores, instead of one 16-bit
+// sample per step.
+#ifndef XG_TQ_LIFT_WORDS
+#define XG_TQ_LIFT_WORDS 1
+#endif
+// The inverse upsampling reads the low band 4 rows ahead of its stores.
+#ifndef XG_TQ_UPS_CHUNK
+#define XG_TQ_UPS_CHUNK 1
+#endif
+
 // ---- shapes ------------------------------------------------------------------
 template <int PART> struct Shape;
 #define XG_TQ_SHAPE(P, IW_, IH_, TW_, TH_, S1_, S2_)                                                               \
@@ -299,6 +310,38 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
         // H[m] goes to sample m of the same row (the samples still to be
         // read, 2m+1 on, lie beyond it)
         if (act) {
+#if XG_TQ_LIFT_WORDS
+            // the row as words (samples 2m, 2m+1), 8 words per chunk loaded
+            // before any store; H[c..c+8) stored as 4 words behind the reads
+            constexpr int NW = IW / 2;
+            static_assert(NW % 8 == 0 && PX % 2 == 0, "word-wise lifting: rows of 16k samples, even pitch");
+            for (int r = lane; r < IH; r += 32) {
+                uint32_t *pw = reinterpret_cast<uint32_t *>(tA + r * PX);
+                int prev_odd = 0, pe = (int)(int16_t)(pw[0] & 0xFFFFu);
+#pragma unroll 1
+                for (int c = 0; c < NW; c += 8) {
+                    uint32_t w[9];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) w[k] = pw[c + k];
+                    w[8] = c + 8 < NW ? pw[c + 8] : w[7];   // last row: p[IW] mirrors to p[IW-2]
+                    uint32_t hw[4];
+                    int hl = 0;
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        const int po = (int)w[k] >> 16, pn = (int)(int16_t)(w[k + 1] & 0xFFFFu);
+                        const int odd = (int16_t)(po - ((pe + pn) >> 1));
+                        if (c + k == 0) prev_odd = odd;
+                        const int h = (int16_t)(pe + ((prev_odd + odd + 2) >> 2));
+                        prev_odd = odd;
+                        pe = pn;
+                        if (k & 1) hw[k >> 1] = pack16(hl, h);
+                        else hl = h;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; k++) pw[c / 2 + k] = hw[k];
+                }
+            }
+#else
             for (int r = lane; r < IH; r += 32) {
                 int16_t *p = tA + r * PX;
                 int prev_odd = 0, pe = p[0];
@@ -311,6 +354,7 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
                     pe = pn;
                 }
             }
+#endif
         }
         __syncwarp();
         // vertical lifting, one LL row per lane (j < TH), into region B:
@@ -320,6 +364,35 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
             const int j = lane;
             const int rm2 = j == 0 ? 2 : 2 * j - 2, rm1 = j == 0 ? 1 : 2 * j - 1;
             const int rp1 = 2 * j + 1, rp2 = j == TH - 1 ? 2 * j : 2 * j + 2;
+#if XG_TQ_LIFT_WORDS
+            // two columns per word, 4 words of each of the 5 rows per chunk
+            static_assert(TW % 8 == 0 && PL % 2 == 0, "word-wise vertical lifting");
+            const uint32_t *qa = reinterpret_cast<const uint32_t *>(tA + rm2 * PX);
+            const uint32_t *qb = reinterpret_cast<const uint32_t *>(tA + rm1 * PX);
+            const uint32_t *qc = reinterpret_cast<const uint32_t *>(tA + 2 * j * PX);
+            const uint32_t *qd = reinterpret_cast<const uint32_t *>(tA + rp1 * PX);
+            const uint32_t *qe = reinterpret_cast<const uint32_t *>(tA + rp2 * PX);
+            uint32_t *ow = reinterpret_cast<uint32_t *>(tB + j * PL);
+            auto ll = [](int a, int b, int c, int d, int e) {
+                const int oa = (int16_t)(b - ((a + c) >> 1));
+                const int ob = (int16_t)(d - ((c + e) >> 1));
+                return (int16_t)((c << 1) + ((oa + ob + 1) >> 1));
+            };
+            auto lo = [](uint32_t v) { return (int)(int16_t)(v & 0xFFFFu); };
+            auto hi = [](uint32_t v) { return (int)v >> 16; };
+#pragma unroll 1
+            for (int i0 = 0; i0 < TW / 2; i0 += 4) {
+                uint32_t a[4], b[4], c[4], d[4], e[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    a[k] = qa[i0 + k]; b[k] = qb[i0 + k]; c[k] = qc[i0 + k]; d[k] = qd[i0 + k]; e[k] = qe[i0 + k];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    ow[i0 + k] = pack16(ll(lo(a[k]), lo(b[k]), lo(c[k]), lo(d[k]), lo(e[k])),
+                                        ll(hi(a[k]), hi(b[k]), hi(c[k]), hi(d[k]), hi(e[k])));
+            }
+#else
             for (int i = 0; i < TW; i++) {
                 const int qa = tA[rm2 * PX + i], qb = tA[rm1 * PX + i], qc = tA[2 * j * PX + i];
                 const int qd = tA[rp1 * PX + i], qe = tA[rp2 * PX + i];
@@ -327,6 +400,7 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
                 const int ob = (int16_t)(qd - ((qc + qe) >> 1));
                 tB[j * PL + i] = (int16_t)((qc << 1) + ((oa + ob + 1) >> 1));
             }
+#endif
         }
         __syncwarp();
         if (act && lane < TH) load_pairs<TW>(tB + lane * PL, xp);
@@ -467,6 +541,37 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
             const int i = lane, in1 = i + 1 < TW ? i + 1 : i;
             uint32_t *dw = reinterpret_cast<uint32_t *>(dst);
             int h0 = stage[i] >> 1, h1 = stage[in1] >> 1;
+#if XG_TQ_UPS_CHUNK
+            // low-band rows in chunks of 4: their reads before the stores
+            static_assert(TH % 4 == 0, "upsampling by chunks of 4 rows");
+#pragma unroll 1
+            for (int y0 = 0; y0 < TH; y0 += 4) {
+                int n0[4], n1[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int yn = y0 + k + 1 < TH ? y0 + k + 1 : TH - 1;
+                    n0[k] = stage[yn * PS + i] >> 1;
+                    n1[k] = stage[yn * PS + in1] >> 1;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int v0 = (h0 + n0[k]) >> 1, v1 = (h1 + n1[k]) >> 1;
+                    const uint32_t we = pack16(h0, (h0 + h1) >> 1), wo = pack16(v0, (v0 + v1) >> 1);
+                    const int e = 2 * (y0 + k) * TW + i;
+                    if (al_out) {
+                        dw[e] = we;
+                        dw[e + TW] = wo;
+                    } else {
+                        dst[2 * e] = (int16_t)(we & 0xFFFF);
+                        dst[2 * e + 1] = (int16_t)(we >> 16);
+                        dst[2 * (e + TW)] = (int16_t)(wo & 0xFFFF);
+                        dst[2 * (e + TW) + 1] = (int16_t)(wo >> 16);
+                    }
+                    h0 = n0[k];
+                    h1 = n1[k];
+                }
+            }
+#else
             for (int y = 0; y < TH; y++) {
                 const int yn = y + 1 < TH ? y + 1 : y;
                 const int n0 = stage[yn * PS + i] >> 1, n1 = stage[yn * PS + in1] >> 1;
@@ -485,6 +590,7 @@ __device__ __noinline__ void tu_group(const Ctx &cx, int idx, int lane, uint8_t 
                 h0 = n0;
                 h1 = n1;
             }
+#endif
         }
     }
     __syncwarp();
