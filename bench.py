@@ -1632,7 +1632,8 @@ def run_serve(args):
         layouts.append(xg.cu_pus(xg.split_map_cus(w, h, 1000 + sid), w, h, 2))
 
     def make_server(max_frames):
-        cfg = xg.ServerConfig(args.serve_hbm_gb << 30, args.serve_batch_mpx << 20, max_frames, QP, prm)
+        cfg = xg.ServerConfig(args.serve_hbm_gb << 30, args.serve_batch_mpx << 20, max_frames, QP, prm,
+                              hbm_reserve_bytes=0, batch_pixels_target=args.serve_batch_target_mpx << 20)
         srv = xg.Server(cfg)
         streams = []
         for sid in range(nstreams):
@@ -1674,7 +1675,8 @@ def run_serve(args):
                    "resolutions": {"%dx%d" % SERVE_RES[r]: int((res_idx == r).sum()) for r in range(4)},
                    "arrivals": "Poisson 30 fps per stream", "seconds": args.serve_seconds, "warm_s": args.serve_warm,
                    "search_range": args.serve_range, "qp": QP, "refs": 2,
-                   "batch_cap": {"pictures": args.serve_batch, "luma_mpx": args.serve_batch_mpx},
+                   "batch_cap": {"pictures": args.serve_batch, "luma_mpx": args.serve_batch_mpx,
+                                 "target_luma_mpx": args.serve_batch_target_mpx},
                    "picture_job": "reference update + sub-pel planes, FS +-%d + quarter-pel SATD over the leaf-CU "
                                   "PUs of a seeded split map, every inter candidate through the TU chain (one TU and "
                                   "the TU split), choice, reconstruction" % args.serve_range},
@@ -1870,10 +1872,14 @@ def main():
     ap.add_argument("--serve-warm", type=float, default=2.0)
     ap.add_argument("--serve-range", type=int, default=64)
     ap.add_argument("--serve-batch", type=int, default=64)
-    # luma pixels per batch (MiB): about one and a half 2160p pictures keeps a
-    # burst of arrivals from forming one long batch (p99 11.7 ms against 16-19
-    # ms with 48 MiB batches at 64 streams)
-    ap.add_argument("--serve-batch-mpx", type=int, default=12)
+    # luma pixels per batch (MiB): batches of 12 Mi keep a burst of arrivals
+    # from forming one long batch while the backlog is short; with more than
+    # two such batches waiting they grow to 24 Mi, which carries 64 streams of
+    # 1080p in full (12 Mi alone: 1,860 of 1,942 pictures/s)
+    ap.add_argument("--serve-batch-mpx", type=int, default=24,
+                    help="luma Mi-pixels a batch may take (sizes the batch buffers)")
+    ap.add_argument("--serve-batch-target-mpx", type=int, default=12,
+                    help="luma Mi-pixels a batch takes while the backlog is short (0: the full size)")
     ap.add_argument("--serve-res", choices=["mix", "360p", "720p", "1080p", "2160p"], default="mix",
                     help="stream resolutions: the 360p..2160p mix, or every stream at one size")
     ap.add_argument("--serve-pool", type=int, default=4)

@@ -792,6 +792,8 @@ typedef struct xavs2gpu_server_config {
     int32_t qp;                  /* quantiser of every TU */
     xavs2gpu_me_params_t me;     /* search parameters */
     int64_t hbm_reserve_bytes;   /* device memory admission leaves free (0: 1/32 of the device, at least 1 GiB) */
+    int64_t batch_pixels_target; /* luma pixels a batch takes while the backlog is short (0: max_batch_pixels);
+                                    while more than twice this waits, batches grow up to max_batch_pixels */
 } xavs2gpu_server_config_t;
 
 typedef struct xavs2gpu_server_result {

@@ -31,9 +31,9 @@ def _streams(xg):
     return out
 
 
-def _serve(xg, streams, max_frames):
+def _serve(xg, streams, max_frames, target=0):
     prm = xg.MeParams(R, oracle.lambda_factor(QP), 1, 2, 0, 0)
-    cfg = xg.ServerConfig(0, 1 << 20, max_frames, QP, prm)
+    cfg = xg.ServerConfig(0, 1 << 20, max_frames, QP, prm, hbm_reserve_bytes=0, batch_pixels_target=target)
     srv = xg.Server(cfg)
     ids = [srv.open_stream(w, h, pus, cus, ring=NFRAMES) for (w, h, _, pus, cus) in streams]
     assert all(i >= 0 for i in ids)
@@ -80,6 +80,20 @@ def test_server_alone_equals_mixed_and_chain(gpu):
         assert int(mixed[(sid, 2)]["hash"]) == want, sid
         chain.close()
         sess.close()
+
+
+def test_server_batch_target(gpu):
+    """A batch target below every picture but the smallest: batches grow to
+    the full size only while the backlog exceeds twice the target, a batch's
+    first picture always fits, every picture is served, and the outputs equal
+    the pictures run alone."""
+    import xavs2_gb300 as xg
+    streams = _streams(xg)
+    alone = _serve(xg, streams, 1)
+    small = _serve(xg, streams, 8, target=128 * 64)
+    assert set(small) == set(alone)
+    for key, a in alone.items():
+        assert int(a["hash"]) == int(small[key]["hash"]), key
 
 
 def test_server_admission_budget(gpu):

@@ -362,7 +362,7 @@ class MeBatch:
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_pixels", ctypes.c_int64),
                 ("max_batch_frames", ctypes.c_int32), ("qp", ctypes.c_int32), ("me", MeParams),
-                ("hbm_reserve_bytes", ctypes.c_int64)]
+                ("hbm_reserve_bytes", ctypes.c_int64), ("batch_pixels_target", ctypes.c_int64)]
 
 
 SERVER_RESULT_DTYPE = np.dtype([("stream", "<i4"), ("frame", "<i4"), ("tag", "<i8"), ("t_submit_ns", "<i8"),

@@ -33,6 +33,10 @@
 
 // batch buffer sets (each with its own CUDA stream): while one batch runs,
 // the next ones are formed and enqueued
+// backlog (in batch targets) beyond which batches take the full size
+#ifndef XG_SERVE_BACKLOG
+#define XG_SERVE_BACKLOG 2
+#endif
 #ifndef XG_SERVE_SETS
 #define XG_SERVE_SETS 2
 #endif
@@ -261,10 +265,28 @@ void scheduler(xavs2gpu_server_t *s)
         if (free_set) {
             int64_t pix = 0;
             std::vector<char> used(s->streams.size(), 0);
+            // the batch size: the target while the backlog (one picture per
+            // idle stream) is short, the buffers' full size while more than
+            // two target-sized batches wait
+            const int64_t tgt = s->cfg.batch_pixels_target;
+            int64_t cap = s->cfg.max_batch_pixels;
+            if (tgt > 0 && tgt < cap) {
+                int64_t backlog = 0;
+                for (const Job &j : s->pending) {
+                    Stream &S = *s->streams[j.stream];
+                    if (S.in_flight || used[j.stream]) continue;
+                    used[j.stream] = 1;
+                    backlog += (int64_t)S.W * S.H;
+                }
+                std::fill(used.begin(), used.end(), 0);
+                if (backlog <= XG_SERVE_BACKLOG * tgt) cap = tgt;
+            }
             for (auto it = s->pending.begin(); it != s->pending.end() && (int)take.size() < s->cfg.max_batch_frames;) {
                 Stream &S = *s->streams[it->stream];
                 const int64_t p = (int64_t)S.W * S.H;
-                if (S.in_flight || used[it->stream] || pix + p > s->cfg.max_batch_pixels) {
+                // a batch's first picture may take the full size (a picture
+                // larger than the target never waits for a backlog)
+                if (S.in_flight || used[it->stream] || pix + p > (take.empty() ? s->cfg.max_batch_pixels : cap)) {
                     ++it;
                     continue;
                 }
@@ -354,6 +376,7 @@ void free_set(BatchSet &b)
 extern "C" xavs2gpu_server_t *xavs2gpu_server_create(const xavs2gpu_server_config_t *cfg)
 {
     if (!cfg || cfg->max_batch_frames < 1 || cfg->max_batch_frames > 256 || cfg->max_batch_pixels < 64 * 64 ||
+        cfg->batch_pixels_target < 0 ||
         cfg->qp < 0 || cfg->qp > 79 || cfg->me.search_range < 1 || cfg->me.search_range > 128) {
         fail(XAVS2GPU_ERR_ARG, "xavs2gpu_server_create", "bad configuration");
         return nullptr;
