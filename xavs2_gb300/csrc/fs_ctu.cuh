@@ -423,6 +423,10 @@ __device__ __forceinline__ void tma_window_issue(const void *tmap, uint32_t stag
 #ifndef XG_CTU_MINB
 #define XG_CTU_MINB 3
 #endif
+// the same for the two-row form (2: up to 255 registers)
+#ifndef XG_CTU_PAIR_MINB
+#define XG_CTU_PAIR_MINB 2
+#endif
 
 // Ranges from which the search takes two displacement rows per window pass
 // (see ctu_search): the pair form needs about 240 registers (2 CTAs per SM
@@ -790,7 +794,7 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
 #endif
 
 template <bool BORDER, bool PAIR>
-__global__ void __launch_bounds__(kCtuThreads, PAIR ? 2 : XG_CTU_MINB)
+__global__ void __launch_bounds__(kCtuThreads, PAIR ? XG_CTU_PAIR_MINB : XG_CTU_MINB)
     fs_ctu_kernel(const CtuJob *__restrict__ jobs, int nchunks, const SessView *__restrict__ views, int R, int lambda,
                   int ww)
 {
