@@ -29,6 +29,11 @@
 namespace xg {
 namespace tqw {
 
+// The forward transforms' even/odd fold on packed 16-bit pairs.
+#ifndef XG_TQ_PACKED_FOLD
+#define XG_TQ_PACKED_FOLD 1
+#endif
+
 // ---- byte-packed basis rows --------------------------------------------------
 // Forward table of an N-point transform: row k holds T_N[k][0..N) as N/4
 // words (byte j of word w = T_N[k][4w + j]).  Inverse table: row n holds
@@ -142,6 +147,22 @@ template <int N>
 __device__ __forceinline__ void fold_line(const uint32_t (&xp)[N / 2], uint32_t (&ep)[N / 4], uint32_t (&op)[N / 4],
                                           bool &bad)
 {
+#if XG_TQ_PACKED_FOLD
+    // on the packed pairs: (x[2m], x[2m+1]) +- (x[N-1-2m], x[N-2-2m]), the
+    // second the half-swapped pair N/2-1-m; a 16-bit sum is exact iff the
+    // wrapping and the saturating forms agree (the wrapped value of an
+    // overflowing sum of two int16 is never the saturation bound)
+    uint32_t ov = 0;
+#pragma unroll
+    for (int m = 0; m < N / 4; m++) {
+        const uint32_t a = xp[m], b = __byte_perm(xp[N / 2 - 1 - m], 0, 0x1032);
+        const uint32_t e = __vadd2(a, b), o = __vsub2(a, b);
+        ov |= (e ^ __vaddss2(a, b)) | (o ^ __vsubss2(a, b));
+        ep[m] = e;
+        op[m] = o;
+    }
+    bad |= ov != 0;
+#else
     int x[N];
 #pragma unroll
     for (int i = 0; i < N / 2; i++) {
@@ -157,6 +178,7 @@ __device__ __forceinline__ void fold_line(const uint32_t (&xp)[N / 2], uint32_t 
         ep[m] = pack16(e0, e1);
         op[m] = pack16(o0, o1);
     }
+#endif
 }
 
 template <int N, typename Out>
@@ -247,7 +269,6 @@ __host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c
 // region B the wavelet's LL band (up to 32 rows, pitch 34 int16) and later
 // the inverse transform's output for the upsampling.
 constexpr int kRegionA = 64 * 66 * 2, kRegionB = 32 * 34 * 2;
-constexpr int kWarpSmem = kRegionA + kRegionB;
 
 struct Ctx {
     const xavs2gpu_tq_block_t *blocks;
