@@ -288,6 +288,58 @@ def temporal_mvps(xg, pus, refs, W, H, prm):
     return out
 
 
+# The other measured configurations, run once each in a child process after
+# the config-1 measurement of a default single-GPU run, so that one default
+# run also carries configs 2-4: the batched TU chain, the 4K full-picture
+# chain, and the 64-stream server with the configuration's FS +-64 job and
+# with the serving-size FS +-16 search (4 s of arrivals each).  A child that
+# fails or runs past its limit is recorded as such; the config-1 line stands.
+OTHER_CONFIGS = {
+    "config2_tq": ["--workload", "tq", "--steps", "5", "--warmup", "3"],
+    "config3_chain": ["--workload", "chain", "--steps", "5", "--warmup", "3"],
+    "config4_serve_fs64": ["--workload", "serve", "--serve-seconds", "4", "--serve-warm", "1"],
+    "config4_serve_fs16": ["--workload", "serve", "--serve-range", "16", "--serve-seconds", "4", "--serve-warm", "1"],
+}
+
+
+def condense(d):
+    keep = {k: d[k] for k in ("metric", "value", "unit", "ms_per_step", "higher_is_better", "parity",
+                              "sample_bit_exact", "offered_pictures", "submit_failures") if k in d}
+    if isinstance(d.get("e2e"), dict):
+        keep["e2e"] = {k: d["e2e"][k] for k in ("value", "unit") if k in d["e2e"]}
+    if isinstance(d.get("roofline"), dict):
+        keep["roofline"] = {k: d["roofline"][k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac")
+                            if k in d["roofline"]}
+    if isinstance(d.get("batched"), dict):
+        keep["served"] = {k: d["batched"][k] for k in ("p50_ms", "p99_ms", "frames_per_s", "mean_batch_frames")
+                          if k in d["batched"]}
+    if isinstance(d.get("cpu_baseline"), dict):
+        keep["cpu_baseline"] = {k: d["cpu_baseline"][k] for k in ("value", "unit", "cores", "kind")
+                                if k in d["cpu_baseline"]}
+    if isinstance(d.get("clocks"), dict):
+        keep["clocks"] = {k: d["clocks"][k] for k in ("sm_mhz", "reasons") if k in d["clocks"]}
+    return keep
+
+
+def other_configs(limit_s=300):
+    out = {}
+    for name, extra in OTHER_CONFIGS.items():
+        t0 = time.time()
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__)] + extra, capture_output=True, text=True,
+                               timeout=limit_s)
+            lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": "exit status %d" % r.returncode, "tail": (r.stderr or r.stdout)[-400:]}
+            else:
+                out[name] = condense(json.loads(lines[-1]))
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": "no line within %d s" % limit_s}
+        out[name]["wall_s"] = round(time.time() - t0, 1)
+        out[name]["command"] = "python bench.py " + " ".join(extra)
+    return out
+
+
 def run_ours(args):
     import torch
     import xavs2_gb300 as xg
@@ -511,8 +563,12 @@ def run_ours(args):
         "parity": parity,
         "clocks": clocks,
     }
-    print(json.dumps(line))
     sess.close()
+    if (args.configs and world == 1 and not args.quick and args.mvp == "zero"
+            and (WIDTH, HEIGHT) == (1920, 1080)):
+        torch.cuda.empty_cache()
+        line["other_configs"] = other_configs()
+    print(json.dumps(line))
     if parity["mismatches"] or not same:
         sys.exit("bench: motion-search results differ from the oracle on %d of %d sampled PU searches"
                  " (e2e equal to device run: %s)" % (parity["mismatches"], parity["checked"], same))
@@ -1852,6 +1908,8 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--quick", action="store_true", help="device timing only (for profiler runs)")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="default run: skip the one-off runs of configs 2-4 added to the line")
     ap.add_argument("--me-leaf", action="store_true",
                     help="with --quick: the serving-shaped search (leaf-CU partitions, FS +-16) instead of every PU")
     ap.add_argument("--workload", choices=["me", "tq", "chain", "serve", "intra", "loopfilter", "lookahead", "skip"],
