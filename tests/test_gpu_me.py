@@ -57,17 +57,19 @@ def _assert_same(got, exp, pus):
                                                  int(pus[i]["ref"]), got[i], exp[i]) for i in diff[:5]]
 
 
-@pytest.mark.parametrize("R,w,h", [(16, 256, 192), (8, 136, 72), (64, 320, 256)])
+@pytest.mark.parametrize("R,w,h", [(16, 256, 192), (8, 136, 72), (64, 320, 256), (96, 256, 192)])
 def test_ctu_layout_all_pus(gpu, olib, R, w, h):
     """Every PU of the CTU quadtree layout (all 25 shapes), two references,
-    MVP (0,0): the shared-window CTU kernel, edge CTUs included."""
+    MVP (0,0): the shared-window CTU kernel, edge CTUs included.  R = 96 is a
+    range where the launch leaves out the TMA staging area (it would cost a
+    CTA per SM) and the windows are filled with 16-byte loads."""
     import xavs2_gb300 as xg
     rng = np.random.default_rng(R + w)
     cur, ref0 = _frames(rng, w, h)
     _, ref1 = _frames(rng, w, h, shift=(-3, 4))
     pus = xg.frame_pus(w, h, 2)
-    if R == 64:
-        pus = pus[rng.random(len(pus)) < 0.25]     # keep the CPU oracle quick
+    if R >= 64:
+        pus = pus[rng.random(len(pus)) < (0.25 if R == 64 else 0.15)]     # keep the CPU oracle quick
     prm = xg.MeParams(R, oracle.lambda_factor(32), 1, 2, 0, 0)
     got, stats = _run(cur, [ref0, ref1], pus, prm)
     assert stats[0] == len(pus) and stats[1] == 0, stats

@@ -523,7 +523,12 @@ __device__ __forceinline__ void ctu_search(const CtuJob &job, int chunk, const S
     const uint32_t stage_s = smem_u32(stage), bar_s = stage_s + (uint32_t)(np * kTmaPieceBytes);
     int tx = 0, ty = 0, tz = 0;
     bool use_tma = false;
-    if (view.tmap != nullptr && vec_ok && (stage_s & 127) == 0) {
+    // the launch gave the CTA the staging area (it does not where that would
+    // cost a CTA per SM)
+    uint32_t dyn_smem;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_smem));
+    const bool staged = (uint32_t)(stage - smem) + (uint32_t)(np * kTmaPieceBytes) + 16u <= dyn_smem;
+    if (view.tmap != nullptr && staged && vec_ok && (stage_s & 127) == 0) {
         const ptrdiff_t off = (ref + (ptrdiff_t)wy0 * g.stride + wx0) - view.pool;
         tz = (int)(off / (ptrdiff_t)view.plane_bytes);
         const ptrdiff_t rem = off - (ptrdiff_t)tz * view.plane_bytes;
@@ -895,14 +900,40 @@ static void ctu_plan_build(CtuPlan &p, const std::vector<xavs2gpu_pu_t> &pus, in
 
 // ww: row pitch of the window (bytes), a multiple of 128 that holds the
 // 64 + 2R + 8 bytes a row needs after its swizzle shift.
-static inline size_t ctu_smem_bytes(int R, int &ww)
+static inline size_t ctu_smem_bytes(int R, int &ww, bool staging)
 {
     ww = (int)align_up((size_t)64 + 2 * R + 8 + 4 * kSwzMax + 4, 128);
     const size_t keys_win = 2 * sizeof(uint32_t) * kDyChunk * 2 * R + (size_t)(64 + kDyChunk - 1) * ww;
+    // the TMA staging boxes and their barrier
+    return staging ? keys_win + (size_t)tma_pieces(R) * kTmaPieceBytes + 16 : keys_win;
+}
+
+// Dynamic shared memory of a launch of variant (border, pair) at range R:
+// with the TMA staging area where it costs no CTA per SM (it would from
+// R = 96 on in the two-row form), else without (the CTAs then fill their
+// windows with 16-byte loads).  Cached per device, variant and range.
+template <bool BORDER, bool PAIR>
+static size_t ctu_launch_smem(int dev, int R, int &ww)
+{
+    static int choice[64][129];   // 0 unknown, 1 without, 2 with
+    const size_t base = ctu_smem_bytes(R, ww, false);
 #if XG_CTU_TMA
-    return keys_win + (size_t)tma_pieces(R) * kTmaPieceBytes + 16;   // staging boxes and their barrier
+    if (dev < 0 || dev >= 64 || R < 1 || R > 128) return base;
+    int &c = choice[dev][R];
+    if (c == 0) {
+        int wwt, nb = 0, nt = 0;
+        const size_t with = ctu_smem_bytes(R, wwt, true);
+        const bool ok = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fs_ctu_kernel<BORDER, PAIR>, kCtuThreads,
+                                                                      base) == cudaSuccess &&
+                        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nt, fs_ctu_kernel<BORDER, PAIR>, kCtuThreads,
+                                                                      with) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+        c = ok && nt >= nb ? 2 : 1;
+    }
+    return c == 2 ? ctu_smem_bytes(R, ww, true) : base;
 #else
-    return keys_win;
+    (void)dev;
+    return base;
 #endif
 }
 
@@ -915,12 +946,11 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     if (n_jobs == 0) return;
     const int R = prm.search_range;
     int ww;
-    const size_t smem = ctu_smem_bytes(R, ww);
     static bool attr_done[64] = {false};
     const int dev = current_device();
     if (dev >= 0 && dev < 64 && !attr_done[dev]) {
         int ww_max;
-        const int maxb = (int)ctu_smem_bytes(128, ww_max);
+        const int maxb = (int)ctu_smem_bytes(128, ww_max, XG_CTU_TMA != 0);
         XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
         XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
         XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
@@ -930,14 +960,25 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     const int nchunks = (2 * R + kDyChunk - 1) / kDyChunk;
     const int grid = n_jobs * nchunks;
     const bool pair = R >= XG_CTU_PAIR_MIN_R;
+    const int lam = prm.lambda_factor;
     if (n_border < n_jobs) {
-        if (pair) fs_ctu_kernel<false, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
-        else fs_ctu_kernel<false, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        if (pair) {
+            const size_t smem = ctu_launch_smem<false, true>(dev, R, ww);
+            fs_ctu_kernel<false, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, lam, ww);
+        } else {
+            const size_t smem = ctu_launch_smem<false, false>(dev, R, ww);
+            fs_ctu_kernel<false, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, lam, ww);
+        }
         count_launch();
     }
     if (n_border > 0) {
-        if (pair) fs_ctu_kernel<true, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
-        else fs_ctu_kernel<true, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, prm.lambda_factor, ww);
+        if (pair) {
+            const size_t smem = ctu_launch_smem<true, true>(dev, R, ww);
+            fs_ctu_kernel<true, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, lam, ww);
+        } else {
+            const size_t smem = ctu_launch_smem<true, false>(dev, R, ww);
+            fs_ctu_kernel<true, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, lam, ww);
+        }
         count_launch();
     }
 }
