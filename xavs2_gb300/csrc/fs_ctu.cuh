@@ -937,6 +937,38 @@ static size_t ctu_launch_smem(int dev, int R, int &ww)
 #endif
 }
 
+// Run the border variant on a side stream forked from the caller's, so its
+// CTAs fill the SMs the interior launch's last wave leaves idle (and the
+// reverse); joined back before the call returns.
+#ifndef XG_CTU_FORK
+#define XG_CTU_FORK 1
+#endif
+
+// A side stream and its fork / join events, per host thread and device
+// (a thread's launches are sequenced, so they may share them; the fork and
+// the join happen within one call, so stream capture sees a complete
+// fork-join).
+struct CtuSide {
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+static CtuSide *ctu_side(int dev)
+{
+    thread_local CtuSide side[64];
+    if (dev < 0 || dev >= 64) return nullptr;
+    CtuSide &s = side[dev];
+    if (!s.st) {
+        if (cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            s = CtuSide();
+            return nullptr;
+        }
+    }
+    return &s;
+}
+
 // One launch of each variant over `n_jobs` jobs (sessions per job.sess).
 // n_border of the jobs need the border variant; a variant with no job of
 // its kind is not launched.
@@ -961,6 +993,14 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     const int grid = n_jobs * nchunks;
     const bool pair = R >= XG_CTU_PAIR_MIN_R;
     const int lam = prm.lambda_factor;
+    // the border launch on the side stream when both variants run
+    CtuSide *side = XG_CTU_FORK && n_border > 0 && n_border < n_jobs ? ctu_side(dev) : nullptr;
+    cudaStream_t bst = st;
+    if (side) {
+        XG_CUDA(cudaEventRecord(side->fork, st));
+        XG_CUDA(cudaStreamWaitEvent(side->st, side->fork, 0));
+        bst = side->st;
+    }
     if (n_border < n_jobs) {
         if (pair) {
             const size_t smem = ctu_launch_smem<false, true>(dev, R, ww);
@@ -974,12 +1014,16 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     if (n_border > 0) {
         if (pair) {
             const size_t smem = ctu_launch_smem<true, true>(dev, R, ww);
-            fs_ctu_kernel<true, true><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, lam, ww);
+            fs_ctu_kernel<true, true><<<grid, kCtuThreads, smem, bst>>>(d_jobs, nchunks, d_views, R, lam, ww);
         } else {
             const size_t smem = ctu_launch_smem<true, false>(dev, R, ww);
-            fs_ctu_kernel<true, false><<<grid, kCtuThreads, smem, st>>>(d_jobs, nchunks, d_views, R, lam, ww);
+            fs_ctu_kernel<true, false><<<grid, kCtuThreads, smem, bst>>>(d_jobs, nchunks, d_views, R, lam, ww);
         }
         count_launch();
+    }
+    if (side) {
+        XG_CUDA(cudaEventRecord(side->join, side->st));
+        XG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
     }
 }
 
