@@ -1233,6 +1233,24 @@ static void launch_groups(const RefineGroup *groups, int n, const uint32_t *memb
 
 namespace xg {
 
+// The refinement's per-warp list on the CTU search's side stream when the
+// per-thread list runs too: the lists are disjoint, and each launch's last
+// wave then overlaps the other's work.  fork returns the stream to launch on.
+static cudaStream_t refine_fork(cudaStream_t st, bool both, CtuSide *&side)
+{
+    side = XG_CTU_FORK && both ? ctu_side(current_device()) : nullptr;
+    if (!side) return st;
+    XG_CUDA(cudaEventRecord(side->fork, st));
+    XG_CUDA(cudaStreamWaitEvent(side->st, side->fork, 0));
+    return side->st;
+}
+static void refine_join(cudaStream_t st, CtuSide *side)
+{
+    if (!side) return;
+    XG_CUDA(cudaEventRecord(side->join, side->st));
+    XG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+}
+
 // ---- session ---------------------------------------------------------------------
 // CU-grouped refinement on (1) or per-PU kernels only (0); the results are
 // the same either way
@@ -1767,6 +1785,8 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
     const int ns = grouped ? m.n_small_g : m.n_small, nl = grouped ? m.n_large_g : m.n_large;
     const int *lst_s = grouped ? m.d_small_g : m.d_small, *lst_l = grouped ? m.d_large_g : m.d_large;
     if (grouped) launch_groups(m.d_groups, m.n_groups, m.d_members, m.d_view, R, *prm, m.st);
+    CtuSide *side = nullptr;
+    const cudaStream_t wst = refine_fork(m.st, ns && nl, side);
     if (ns) {
         const unsigned g = (ns + m.tune_block - 1) / m.tune_block;
         if (prm->use_hadamard)
@@ -1778,10 +1798,11 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
         count_launch();
     }
     if (nl) {
-        refine_warp_list_kernel<<<(nl * 32 + m.tune_block - 1) / m.tune_block, m.tune_block, 0, m.st>>>(
+        refine_warp_list_kernel<<<(nl * 32 + m.tune_block - 1) / m.tune_block, m.tune_block, 0, wst>>>(
             reinterpret_cast<const uint32_t *>(lst_l), nl, m.d_view, R, *prm);
         count_launch();
     }
+    refine_join(m.st, side);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[4], m.st));
     XG_CUDA(cudaGetLastError());
     return XAVS2GPU_OK;
@@ -2171,6 +2192,8 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         if (rc != XAVS2GPU_OK) return rc;
     }
     if (ngr) launch_groups(bb.d_groups, (int)ngr, d_members, bb.d_views, R, *prm, st);
+    CtuSide *side = nullptr;
+    const cudaStream_t wst = refine_fork(st, ns && nl, side);
     if (ns) {
         const unsigned g = (unsigned)((ns + block - 1) / block);
         if (prm->use_hadamard)
@@ -2180,10 +2203,11 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         count_launch();
     }
     if (nl) {
-        refine_warp_list_kernel<<<(unsigned)((nl * 32 + block - 1) / block), block, 0, st>>>(d_large, (int)nl,
-                                                                                          bb.d_views, R, *prm);
+        refine_warp_list_kernel<<<(unsigned)((nl * 32 + block - 1) / block), block, 0, wst>>>(d_large, (int)nl,
+                                                                                           bb.d_views, R, *prm);
         count_launch();
     }
+    refine_join(st, side);
     XG_CUDA(cudaEventRecord(bb.done, st));
     bb.used = true;
     XG_CUDA(cudaGetLastError());
