@@ -908,6 +908,21 @@ static inline size_t ctu_smem_bytes(int R, int &ww, bool staging)
     return staging ? keys_win + (size_t)tma_pieces(R) * kTmaPieceBytes + 16 : keys_win;
 }
 
+// The kernels' dynamic shared-memory limit (the largest range's need), once
+// per device; launches and occupancy queries come after it.
+static void ctu_attrs(int dev)
+{
+    static bool done[64] = {false};
+    if (dev < 0 || dev >= 64 || done[dev]) return;
+    int ww_max;
+    const int maxb = (int)ctu_smem_bytes(128, ww_max, XG_CTU_TMA != 0);
+    XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+    XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+    XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+    XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
+    done[dev] = true;
+}
+
 // Dynamic shared memory of a launch of variant (border, pair) at range R:
 // with the TMA staging area where it costs no CTA per SM (it would from
 // R = 96 on in the two-row form), else without (the CTAs then fill their
@@ -921,6 +936,7 @@ static size_t ctu_launch_smem(int dev, int R, int &ww)
     if (dev < 0 || dev >= 64 || R < 1 || R > 128) return base;
     int &c = choice[dev][R];
     if (c == 0) {
+        ctu_attrs(dev);
         int wwt, nb = 0, nt = 0;
         const size_t with = ctu_smem_bytes(R, wwt, true);
         const bool ok = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fs_ctu_kernel<BORDER, PAIR>, kCtuThreads,
@@ -928,7 +944,7 @@ static size_t ctu_launch_smem(int dev, int R, int &ww)
                         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nt, fs_ctu_kernel<BORDER, PAIR>, kCtuThreads,
                                                                       with) == cudaSuccess;
         if (!ok) cudaGetLastError();
-        c = ok && nt >= nb ? 2 : 1;
+        c = ok && nb > 0 && nt >= nb ? 2 : 1;
     }
     return c == 2 ? ctu_smem_bytes(R, ww, true) : base;
 #else
@@ -951,6 +967,12 @@ static size_t ctu_launch_smem(int dev, int R, int &ww)
 struct CtuSide {
     cudaStream_t st = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    ~CtuSide()   // at thread exit (a pool's threads do not keep theirs)
+    {
+        if (join) cudaEventDestroy(join);
+        if (fork) cudaEventDestroy(fork);
+        if (st) cudaStreamDestroy(st);
+    }
 };
 static CtuSide *ctu_side(int dev)
 {
@@ -962,12 +984,16 @@ static CtuSide *ctu_side(int dev)
             cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
-            s = CtuSide();
-            return nullptr;
+            return nullptr;   // the launches then stay on the caller's stream
         }
     }
     return &s;
 }
+
+// Creates what a search at range R launches with on this thread -- the side
+// stream and the shared-memory choices -- ahead of a stream capture.
+template <bool BORDER, bool PAIR> static size_t ctu_launch_smem(int dev, int R, int &ww);
+static void ctu_prime(int R);
 
 // One launch of each variant over `n_jobs` jobs (sessions per job.sess).
 // n_border of the jobs need the border variant; a variant with no job of
@@ -978,17 +1004,8 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     if (n_jobs == 0) return;
     const int R = prm.search_range;
     int ww;
-    static bool attr_done[64] = {false};
     const int dev = current_device();
-    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-        int ww_max;
-        const int maxb = (int)ctu_smem_bytes(128, ww_max, XG_CTU_TMA != 0);
-        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
-        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
-        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
-        XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
-        attr_done[dev] = true;
-    }
+    ctu_attrs(dev);
     const int nchunks = (2 * R + kDyChunk - 1) / kDyChunk;
     const int grid = n_jobs * nchunks;
     const bool pair = R >= XG_CTU_PAIR_MIN_R;
@@ -1024,6 +1041,22 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     if (side) {
         XG_CUDA(cudaEventRecord(side->join, side->st));
         XG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+    }
+}
+
+// (see the declaration above)
+static void ctu_prime(int R)
+{
+    const int dev = current_device();
+    int ww;
+    if (XG_CTU_FORK) ctu_side(dev);
+    if (R < 1 || R > 128) return;
+    if (R >= XG_CTU_PAIR_MIN_R) {
+        ctu_launch_smem<false, true>(dev, R, ww);
+        ctu_launch_smem<true, true>(dev, R, ww);
+    } else {
+        ctu_launch_smem<false, false>(dev, R, ww);
+        ctu_launch_smem<true, false>(dev, R, ww);
     }
 }
 

@@ -1904,6 +1904,7 @@ extern "C" int xavs2gpu_me_prepare(xavs2gpu_me_session_t *s, const xavs2gpu_me_p
     }
     XG_CUDA(cudaSetDevice(s->impl.device));
     ensure_plan(s->impl, prm->search_range, prm->lambda_factor);
+    ctu_prime(prm->search_range);   // nothing created inside a capture that follows
     return XAVS2GPU_OK;
 }
 
