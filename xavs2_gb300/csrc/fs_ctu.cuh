@@ -912,15 +912,15 @@ static inline size_t ctu_smem_bytes(int R, int &ww, bool staging)
 // per device; launches and occupancy queries come after it.
 static void ctu_attrs(int dev)
 {
-    static bool done[64] = {false};
-    if (dev < 0 || dev >= 64 || done[dev]) return;
+    static std::atomic<bool> done[64];
+    if (dev < 0 || dev >= 64 || done[dev].load(std::memory_order_acquire)) return;
     int ww_max;
     const int maxb = (int)ctu_smem_bytes(128, ww_max, XG_CTU_TMA != 0);
     XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
     XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
     XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
     XG_CUDA(cudaFuncSetAttribute(fs_ctu_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb));
-    done[dev] = true;
+    done[dev].store(true, std::memory_order_release);
 }
 
 // Dynamic shared memory of a launch of variant (border, pair) at range R:
@@ -930,11 +930,12 @@ static void ctu_attrs(int dev)
 template <bool BORDER, bool PAIR>
 static size_t ctu_launch_smem(int dev, int R, int &ww)
 {
-    static int choice[64][129];   // 0 unknown, 1 without, 2 with
+    static std::atomic<int> choice[64][129];   // 0 unknown, 1 without, 2 with (threads agree)
     const size_t base = ctu_smem_bytes(R, ww, false);
 #if XG_CTU_TMA
     if (dev < 0 || dev >= 64 || R < 1 || R > 128) return base;
-    int &c = choice[dev][R];
+    std::atomic<int> &slot = choice[dev][R];
+    int c = slot.load(std::memory_order_relaxed);
     if (c == 0) {
         ctu_attrs(dev);
         int wwt, nb = 0, nt = 0;
@@ -945,6 +946,7 @@ static size_t ctu_launch_smem(int dev, int R, int &ww)
                                                                       with) == cudaSuccess;
         if (!ok) cudaGetLastError();
         c = ok && nb > 0 && nt >= nb ? 2 : 1;
+        slot.store(c, std::memory_order_relaxed);
     }
     return c == 2 ? ctu_smem_bytes(R, ww, true) : base;
 #else
@@ -992,8 +994,20 @@ static CtuSide *ctu_side(int dev)
 
 // Creates what a search at range R launches with on this thread -- the side
 // stream and the shared-memory choices -- ahead of a stream capture.
-template <bool BORDER, bool PAIR> static size_t ctu_launch_smem(int dev, int R, int &ww);
-static void ctu_prime(int R);
+static void ctu_prime(int R)
+{
+    const int dev = current_device();
+    int ww;
+    if (XG_CTU_FORK) ctu_side(dev);
+    if (R < 1 || R > 128) return;
+    if (R >= XG_CTU_PAIR_MIN_R) {
+        ctu_launch_smem<false, true>(dev, R, ww);
+        ctu_launch_smem<true, true>(dev, R, ww);
+    } else {
+        ctu_launch_smem<false, false>(dev, R, ww);
+        ctu_launch_smem<true, false>(dev, R, ww);
+    }
+}
 
 // One launch of each variant over `n_jobs` jobs (sessions per job.sess).
 // n_border of the jobs need the border variant; a variant with no job of
@@ -1041,22 +1055,6 @@ static void ctu_jobs_run(const CtuJob *d_jobs, int n_jobs, int n_border, const S
     if (side) {
         XG_CUDA(cudaEventRecord(side->join, side->st));
         XG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
-    }
-}
-
-// (see the declaration above)
-static void ctu_prime(int R)
-{
-    const int dev = current_device();
-    int ww;
-    if (XG_CTU_FORK) ctu_side(dev);
-    if (R < 1 || R > 128) return;
-    if (R >= XG_CTU_PAIR_MIN_R) {
-        ctu_launch_smem<false, true>(dev, R, ww);
-        ctu_launch_smem<true, true>(dev, R, ww);
-    } else {
-        ctu_launch_smem<false, false>(dev, R, ww);
-        ctu_launch_smem<true, false>(dev, R, ww);
     }
 }
 
