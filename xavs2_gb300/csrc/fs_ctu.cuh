@@ -976,11 +976,11 @@ struct CtuSide {
         if (st) cudaStreamDestroy(st);
     }
 };
-static CtuSide *ctu_side(int dev)
+static CtuSide *ctu_side(int dev, int k = 0)   // k: 0 the search's own, 1 the per-PU search's
 {
-    thread_local CtuSide side[64];
-    if (dev < 0 || dev >= 64) return nullptr;
-    CtuSide &s = side[dev];
+    thread_local CtuSide side[2][64];
+    if (dev < 0 || dev >= 64 || k < 0 || k > 1) return nullptr;
+    CtuSide &s = side[k][dev];
     if (!s.st) {
         if (cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -998,7 +998,10 @@ static void ctu_prime(int R)
 {
     const int dev = current_device();
     int ww;
-    if (XG_CTU_FORK) ctu_side(dev);
+    if (XG_CTU_FORK) {
+        ctu_side(dev, 0);
+        ctu_side(dev, 1);
+    }
     if (R < 1 || R > 128) return;
     if (R >= XG_CTU_PAIR_MIN_R) {
         ctu_launch_smem<false, true>(dev, R, ww);

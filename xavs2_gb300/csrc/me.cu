@@ -1252,6 +1252,17 @@ static void refine_join(cudaStream_t st, CtuSide *side)
     XG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
 }
 
+// The per-PU search beside the CTU search (their PUs are disjoint) on a
+// second side stream, when both have work and phases are not being timed.
+static cudaStream_t search_fork(cudaStream_t st, bool both, CtuSide *&side)
+{
+    side = XG_CTU_FORK && both ? ctu_side(current_device(), 1) : nullptr;
+    if (!side) return st;
+    XG_CUDA(cudaEventRecord(side->fork, st));
+    XG_CUDA(cudaStreamWaitEvent(side->st, side->fork, 0));
+    return side->st;
+}
+
 // ---- session ---------------------------------------------------------------------
 // CU-grouped refinement on (1) or per-PU kernels only (0); the results are
 // the same either way
@@ -1773,12 +1784,22 @@ extern "C" int xavs2gpu_me_run(xavs2gpu_me_session_t *s, const xavs2gpu_me_param
         count_launch();
     }
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[1], m.st));
+    CtuSide *gside = nullptr;
+    const cudaStream_t gst = search_fork(m.st, !m.profiling && m.n_generic && m.plan.n_jobs, gside);
+    if (gside && m.n_generic) {
+        const int rc = fs_generic_launch(gen, m.n_generic, m.d_view, R, lam, gst);
+        if (rc != XAVS2GPU_OK) {
+            refine_join(m.st, gside);
+            return rc;
+        }
+    }
     ctu_jobs_run(m.plan.d_jobs, m.plan.n_jobs, m.plan.n_border, m.d_view, *prm, m.st);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[2], m.st));
-    if (m.n_generic) {
+    if (!gside && m.n_generic) {
         const int rc = fs_generic_launch(gen, m.n_generic, m.d_view, R, lam, m.st);
         if (rc != XAVS2GPU_OK) return rc;
     }
+    refine_join(m.st, gside);
     if (m.profiling) XG_CUDA(cudaEventRecord(m.ev[3], m.st));
     // the CU-grouped refinement follows the reference's per-PU order, which
     // with PMVR depends on each PU's predictor; PMVR keeps the per-PU kernels
@@ -2188,11 +2209,21 @@ extern "C" int xavs2gpu_me_batch_run(xavs2gpu_me_batch_t *b, xavs2gpu_me_session
         me_init_list_kernel<<<(unsigned)((ng * 32 + 127) / 128), 128, 0, st>>>(d_gen, (int)ng, bb.d_views, lam);
         count_launch();
     }
+    CtuSide *gside = nullptr;
+    const cudaStream_t gst = search_fork(st, ng && nj, gside);
+    if (gside) {
+        const int rc = fs_generic_launch(d_gen, (int)ng, bb.d_views, R, lam, gst);
+        if (rc != XAVS2GPU_OK) {
+            refine_join(st, gside);
+            return rc;
+        }
+    }
     ctu_jobs_run(bb.d_jobs, (int)nj, nborder, bb.d_views, *prm, st);
-    if (ng) {
+    if (!gside && ng) {
         const int rc = fs_generic_launch(d_gen, (int)ng, bb.d_views, R, lam, st);
         if (rc != XAVS2GPU_OK) return rc;
     }
+    refine_join(st, gside);
     if (ngr) launch_groups(bb.d_groups, (int)ngr, d_members, bb.d_views, R, *prm, st);
     CtuSide *side = nullptr;
     const cudaStream_t wst = refine_fork(st, ns && nl, side);
